@@ -1,0 +1,272 @@
+"""Benchmark of the BP hot path: belief-propagation message updates per second.
+
+Workload (default): a batch of 16 independent 32x32 open PEPS, d=2, chi=8,
+i.i.d. N(0,1) site tensors (seeded), all-edges-at-once (Jacobi) sweeps.  One
+step = one sweep over the whole batch = 16 * 3968 directed-edge message
+updates.  The FP64 tensors of the batch take 1.07 GB and the FP32 copies
+537 MB, both larger than L2, so no L2 flush is needed between steps.
+
+Output: one JSON line (rank 0).  ``--impl reference`` times the CPU
+restatement of the reference's per-edge update (FP64, all host threads) on a
+bounded sample of the same workload."""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "itensornetworks.jl_gb300"))
+
+L, CHI, D, BATCH = 32, 8, 2, 16
+MSGS_PER_NET = 4 * L * (L - 1)
+
+
+def flops_per_sweep(L=L, chi=CHI, d=D):
+    """Algorithmic work of one sweep: per directed edge 2*d*prod(chi)*sum(chi)
+    over the legs of its source vertex."""
+    tot = 0
+    for j in range(L):
+        for i in range(L):
+            k = (i > 0) + (i < L - 1) + (j > 0) + (j < L - 1)
+            tot += k * 2 * d * chi ** k * (k * chi)
+    return tot
+
+
+def bytes_per_sweep(elt, L=L, chi=CHI, d=D):
+    """Compulsory traffic of one Jacobi sweep: every site tensor read once,
+    every message read once and written once."""
+    tens = 0
+    for j in range(L):
+        for i in range(L):
+            k = (i > 0) + (i < L - 1) + (j > 0) + (j < L - 1)
+            tens += d * chi ** k
+    msgs = MSGS_PER_NET * chi * chi
+    return tens * elt + msgs * elt * 2
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_batch(seed0=0):
+    import gbtn
+    nets = [gbtn.random_network(gbtn.square_lattice(L, L, chi=CHI, d=D), seed0 + k) for k in range(BATCH)]
+    return gbtn.disjoint_union(nets)
+
+
+def cpu_reference_rate(seconds=10.0, nthreads=0):
+    """Messages/s of the C restatement (FP64, OpenMP over directed edges) on
+    one 32x32 chi=8 network, Jacobi sweeps, until ``seconds`` elapsed."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import bp_oracle as O
+    import build_oracle
+    g = O.square_lattice(L, L, chi=CHI, d=D)
+    A = O.flatten_tensors(O.random_network(g, 0))
+    m0 = O.flatten_messages(g, O.identity_messages(g))
+    build_oracle.run(g, A, m0, "parallel", None, 1, nthreads=nthreads)  # warm-up
+    sweeps, t0 = 0, time.perf_counter()
+    while True:
+        build_oracle.run(g, A, m0, "parallel", None, 1, nthreads=nthreads)
+        sweeps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    cores = nthreads or os.cpu_count()
+    return sweeps * MSGS_PER_NET / el, cores, f"{sweeps} Jacobi sweeps of one 32x32 chi=8 PEPS ({el:.1f} s)"
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    rates = []
+    for _ in range(args.warmup):
+        cpu_reference_rate(seconds=0.5)
+    for _ in range(args.steps):
+        r, cores, sample = cpu_reference_rate(seconds=2.0)
+        rates.append(r)
+    val = float(np.mean(rates))
+    line = {"impl": "reference", "metric": "bp_msg_updates_per_s", "value": val, "unit": "msg-updates/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * BATCH * MSGS_PER_NET / val, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "bp_sweep_16x_peps32x32_d2_chi8", "batch": BATCH, "L": L, "chi": CHI, "d": D,
+                       "schedule": "parallel", "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": val, "unit": "msg-updates/s", "cores": cores, "kind": "port",
+                             "sample": "per step: " + sample},
+            "e2e": {"value": val, "unit": "msg-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import ctypes as C
+
+    import torch
+
+    import gbtn
+    from gbtn import _lib
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    ctx = gbtn.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    tn = make_batch(seed0=1000 * rank)
+    bpc = gbtn.BeliefPropagationCache(tn, ctx=ctx)
+    lib = ctx.lib
+
+    def sweeps(n, precision):
+        o = _lib.BPOpts()
+        o.schedule, o.precision, o.maxiter, o.normalize, o.tol = 1, _lib.PRECISION[precision], n, 1, -1.0
+        o.edge_sequence = C.cast(None, C.POINTER(C.c_int32))
+        _lib.check(ctx.handle, lib.gbtn_bp_run(bpc.handle, C.byref(o), None, None))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed(precision, steps, warmup):
+        sweeps(warmup, precision)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sweeps(steps, precision)
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms / steps
+
+    msgs_step = BATCH * MSGS_PER_NET
+    with ClockSampler(local) as clk:
+        ms_f32 = timed("f32", args.steps, args.warmup)
+    ms_f64 = timed("f64", max(2, args.steps // 2), 1)
+
+    # end to end through the public API: pinned host tensors -> device, one sweep,
+    # messages back to the host, every step
+    n_fac, n_msg = bpc.n_factor, bpc.n_message
+    host_fac = torch.from_numpy(tn.flat()).pin_memory()
+    host_msg = torch.empty(n_msg, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        _lib.check(ctx.handle, lib.gbtn_set_factors(bpc.handle, C.c_void_p(host_fac.data_ptr()), None, _lib.HOST))
+        bpc.init_messages("identity")
+        sweeps(1, "f32")
+        _lib.check(ctx.handle, lib.gbtn_get_messages(bpc.handle, C.c_void_p(host_msg.data_ptr()), _lib.HOST))
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+
+    value = world * msgs_step / (ms_f32 * 1e-3)
+    fl = flops_per_sweep() * BATCH
+    byt = bytes_per_sweep(4) * BATCH
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    achieved_gbs = byt / (ms_f32 * 1e-3) / 1e9
+    if rank == 0:
+        cpu_val, cores, sample = cpu_reference_rate(seconds=10.0)
+        line = {
+            "metric": "bp_msg_updates_per_s", "value": value, "unit": "msg-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_f32, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "bp_sweep_16x_peps32x32_d2_chi8", "batch": BATCH, "L": L, "chi": CHI, "d": D,
+                       "schedule": "parallel", "chosen_precision": "f32", "l2": "inputs larger than L2",
+                       "parallelism": f"replicas{world}"},
+            "fp64_path": {"value": world * msgs_step / (ms_f64 * 1e-3), "ms_per_step": ms_f64},
+            "chosen_over_fp64": ms_f64 / ms_f32,
+            "algorithmic_tflops": fl / (ms_f32 * 1e-3) / 1e12,
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved_gbs / hbm, "traffic": None,
+                         "note": "FP32 SIMT sweep kernel; algorithmic bytes per sweep / measured time, of measured peak"},
+            "cpu_baseline": {"value": cpu_val, "unit": "msg-updates/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": world * msgs_step / (e2e_ms * 1e-3), "unit": "msg-updates/s",
+                    "h2d_bytes_per_step": n_fac * 8, "d2h_bytes_per_step": n_msg * 8},
+            "gpu_launches": args.steps * 2 + 2,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    bpc.close()
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

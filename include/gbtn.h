@@ -1,0 +1,181 @@
+/*
+ * gbtn.h -- C ABI of the GB300 belief-propagation library (libgbtn.so).
+ *
+ * Drop-in boundary for the belief-propagation hot path of ITensorNetworks.jl.
+ * A Julia package extension (or the Python host package shipped beside this
+ * library) binds these entry points with ccall / ctypes.  Plain C types only:
+ * pointers, sizes and status codes; no exceptions cross the boundary and no
+ * call aborts the process.
+ *
+ * Data conventions (identical on host and device):
+ *   - vertices 0..nv-1; undirected edges 0..ne-1 with endpoints (edge_u[e],
+ *     edge_v[e]); directed edge 2e is edge_u -> edge_v, 2e+1 the reverse.
+ *   - the tensor of vertex v has shape (d_v, chi_{leg_edge[leg_ptr[v]]}, ...)
+ *     in column-major order (site index fastest), i.e. NDTensors Dense order
+ *     with the site index first and the links in the vertex's leg order.
+ *     All vertex tensors are concatenated in vertex order.
+ *   - the message of a directed edge u -> v is a chi x chi matrix M[b, a]
+ *     (b = bra/primed link, a = ket link), column-major, concatenated in
+ *     directed-edge order (2e, 2e+1, ...).
+ *   - every entry point that takes or returns numbers uses float64 on the
+ *     host side; reduced precisions exist only inside the library.
+ *
+ * Return value of every int function: GBTN_OK (0) or an error code; the
+ * message is available from gbtn_last_error(ctx).
+ */
+#ifndef GBTN_H
+#define GBTN_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBTN_ABI_VERSION 1
+
+enum gbtn_status {
+  GBTN_OK = 0,
+  GBTN_ERR_INVALID = 1,     /* bad argument (maps to the reference's error()) */
+  GBTN_ERR_CUDA = 2,        /* CUDA runtime error */
+  GBTN_ERR_UNSUPPORTED = 3, /* shape outside the compiled kernel limits */
+  GBTN_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+  GBTN_ERR_NUMERIC = 5,     /* non-finite value where one is not allowed */
+  GBTN_ERR_NOMEM = 6
+};
+
+enum gbtn_mem { GBTN_HOST = 0, GBTN_DEVICE = 1 };
+
+/* Message-update schedules.
+ *   SEQUENTIAL: directed edges in the order given by edge_sequence, each
+ *               update seeing every earlier one (update_iteration,
+ *               abstractbeliefpropagationcache.jl:272-287).
+ *   PARALLEL:   every message of a sweep computed from the previous sweep
+ *               (update_iteration over edge groups, :294-308).
+ *   COLORED:    vertices in colour classes; all out-messages of one class
+ *               computed from the current messages, class after class. */
+enum gbtn_schedule { GBTN_SCHED_SEQUENTIAL = 0, GBTN_SCHED_PARALLEL = 1, GBTN_SCHED_COLORED = 2 };
+
+/* Arithmetic of the message contractions.  MIXED runs BF16 tensor-core
+ * sweeps (FP32 accumulation), then FP32 sweeps, then FP64 sweeps, each phase
+ * started from the previous phase's fixed point. */
+enum gbtn_precision { GBTN_F64 = 0, GBTN_F32 = 1, GBTN_BF16 = 2, GBTN_MIXED = 3 };
+
+enum gbtn_message_init { GBTN_INIT_IDENTITY = 0, GBTN_INIT_ONES = 1 };
+
+typedef struct gbtn_ctx gbtn_ctx;
+typedef struct gbtn_plan gbtn_plan;
+
+/* Network structure of one or many independent networks (a disjoint union;
+ * vertex_network[v] names the network of v, NULL means one network). */
+typedef struct gbtn_graph_desc {
+  int32_t nv;
+  int32_t ne;
+  const int32_t* edge_u;         /* [ne] */
+  const int32_t* edge_v;         /* [ne] */
+  const int32_t* edge_dim;       /* [ne] bond dimension chi_e >= 1 */
+  const int32_t* site_dim;       /* [nv] physical dimension d_v >= 1 */
+  const int32_t* leg_ptr;        /* [nv+1] CSR offsets into leg_edge */
+  const int32_t* leg_edge;       /* [leg_ptr[nv]] edges of v in tensor leg order */
+  const int32_t* vertex_network; /* [nv] or NULL */
+  int32_t n_networks;            /* >= 1 (ignored when vertex_network is NULL) */
+  int32_t separate_bra;          /* 0: bra = conj(ket) (QuadraticFormNetwork);
+                                    1: bra tensors are set separately
+                                    (LinearFormNetwork / inner(phi, psi)) */
+} gbtn_graph_desc;
+
+typedef struct gbtn_bp_opts {
+  int32_t schedule;              /* gbtn_schedule */
+  int32_t precision;             /* gbtn_precision */
+  int32_t maxiter;               /* > 0 (the reference errors when absent) */
+  int32_t normalize;             /* 1: divide each new message by its norm */
+  double tol;                    /* < 0: no convergence test (tol = nothing) */
+  const int32_t* edge_sequence;  /* SEQUENTIAL: directed edges, per sweep */
+  int32_t edge_sequence_len;     /*   (one sequence shared by all networks is
+                                      not allowed; give the full sequence) */
+  /* MIXED only: per-phase limits; zeros select the defaults. */
+  double tol_bf16;               /* default 1e-6 */
+  double tol_f32;                /* default 1e-13 */
+  int32_t maxiter_bf16;          /* default maxiter */
+  int32_t maxiter_f32;           /* default maxiter */
+  int32_t refine_f64;            /* cap on the FP64 sweeps after FP32 (they stop
+                                    at tol), default maxiter */
+} gbtn_bp_opts;
+
+/* ---- context ----------------------------------------------------------- */
+/* Replaces: the host process of ITensorNetworks (no counterpart; one context
+ * per host thread, bound to one CUDA device). */
+int gbtn_ctx_create(int device, gbtn_ctx** out);
+int gbtn_ctx_destroy(gbtn_ctx* ctx);
+const char* gbtn_last_error(const gbtn_ctx* ctx);
+/* Stream used by every later launch of this context (NULL = the context's own). */
+int gbtn_ctx_set_stream(gbtn_ctx* ctx, void* cuda_stream);
+void* gbtn_ctx_get_stream(const gbtn_ctx* ctx);
+int gbtn_abi_version(void);
+
+/* ---- plan (BeliefPropagationCache storage) ------------------------------ */
+/* Replaces: BeliefPropagationCache(ptn; messages) and initialize_cache
+ * (src/caches/beliefpropagationcache.jl:20-35, src/initialize_cache.jl:14-28):
+ * validates the graph (no self loops, legs consistent with edges) and
+ * allocates device storage for tensors and messages. */
+int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* desc, gbtn_plan** out);
+int gbtn_plan_destroy(gbtn_plan* plan);
+/* Element counts of the concatenated tensor and message arrays. */
+int gbtn_plan_sizes(const gbtn_plan* plan, int64_t* n_factor, int64_t* n_message);
+
+/* Replaces: bpc[v] = tensor (update_factors, abstractbeliefpropagationcache.jl:158-171).
+ * bra may be NULL unless the plan has separate_bra. */
+int gbtn_set_factors(gbtn_plan* plan, const double* ket, const double* bra, int mem);
+int gbtn_get_factors(gbtn_plan* plan, double* ket, int mem);
+/* Replaces: set_messages! / messages (abstractbeliefpropagationcache.jl:173-191). */
+int gbtn_set_messages(gbtn_plan* plan, const double* msgs, int mem);
+int gbtn_get_messages(gbtn_plan* plan, double* msgs, int mem);
+/* Replaces: identity_messages (src/formnetworks/quadraticformnetwork.jl:96-124);
+ * GBTN_INIT_ONES gives all-ones messages of unit Frobenius norm. */
+int gbtn_init_messages(gbtn_plan* plan, int kind);
+
+/* ---- message passing ------------------------------------------------------ */
+/* Replaces: update(bpc; maxiter, tol, edge_sequence, message_update_alg)
+ * (abstractbeliefpropagationcache.jl:313-337, message update :225-239).
+ * iters[n_networks] and mean_diff[n_networks] (may be NULL) receive, per
+ * network, the sweeps run and sum(diff)/len(sequence) of the last sweep
+ * (NaN when tol < 0). */
+int gbtn_bp_run(gbtn_plan* plan, const gbtn_bp_opts* opts, int32_t* iters, double* mean_diff);
+/* Replaces: updated_message(bpc, edge) (abstractbeliefpropagationcache.jl:225-239,
+ * 254-261): the normalised new message of one directed edge, FP64, written to
+ * out (chi*chi) without changing the cache. */
+int gbtn_updated_message(gbtn_plan* plan, int32_t directed_edge, double* out);
+
+/* ---- environments, scalars, expectation values (FP64) ------------------- */
+/* Replaces: environment(bpc, [operator_vertex(v)]) contracted with the ket and
+ * bra of v (expect.jl:5-19): rho_v[s', s], d_v*d_v per vertex, concatenated. */
+int gbtn_vertex_rdms(gbtn_plan* plan, double* out);
+/* Replaces: expect(psi, op; alg="bp") over all vertices (expect.jl:21-41).
+ * ops: d*d matrix O[s', s] shared by all vertices (per_vertex = 0) or one per
+ * vertex concatenated (per_vertex = 1).  out[nv] = tr(rho O)/tr(rho). */
+int gbtn_expect1(gbtn_plan* plan, const double* ops, int per_vertex, double* out);
+/* Replaces: the two-site RDM of test/test_belief_propagation.jl:64-91 on the
+ * listed undirected edges: (du*dv)^2 per edge, row s'_u + du*s'_v, column
+ * s_u + du*s_v. */
+int gbtn_edge_rdms(gbtn_plan* plan, const int32_t* edges, int32_t n_edges, double* out);
+/* Two-site expectation values with one shared (du*dv)^2 operator. */
+int gbtn_expect2(gbtn_plan* plan, const int32_t* edges, int32_t n_edges, const double* op,
+                 double* out);
+/* Replaces: vertex_scalars / edge_scalars (abstractbeliefpropagationcache.jl:83-97,
+ * beliefpropagationcache.jl:107-119). */
+int gbtn_vertex_scalars(gbtn_plan* plan, double* out);
+int gbtn_edge_scalars(gbtn_plan* plan, double* out);
+/* Replaces: logscalar(bpc) (abstractbeliefpropagationcache.jl:397-408), FP64
+ * accumulation per network: re[n] + i*im[n]; -Inf real part when an edge
+ * scalar is zero. */
+int gbtn_logscalar(gbtn_plan* plan, double* re, double* im);
+/* Replaces: rescale_messages (beliefpropagationcache.jl:121-139). */
+int gbtn_rescale_messages(gbtn_plan* plan);
+/* Replaces: rescale_partitions on ket+bra vertices (abstractbeliefpropagationcache.jl:349-379,
+ * normalize.jl:77): every vertex scalar becomes 1. */
+int gbtn_rescale_partitions(gbtn_plan* plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBTN_H */

@@ -1,0 +1,910 @@
+// C-ABI layer of libgbtn: context and plan bookkeeping, argument validation,
+// and the launch sequences behind update / environment / expect / logscalar /
+// rescale.  No exception crosses the ABI: every entry point returns a status
+// and records a message for gbtn_last_error.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+
+#include "gbtn_internal.h"
+
+namespace gbtn {
+void upload_schedules(const DeviceSched& s);
+}
+
+using namespace gbtn;
+
+struct gbtn_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  DeviceSched sched{};
+};
+
+namespace {
+
+thread_local std::string g_err_noctx;
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  void alloc(size_t count) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = count;
+    if (count) GBTN_CUDA(cudaMalloc(&p, count * sizeof(T)));
+  }
+  void upload(const std::vector<T>& h, cudaStream_t s) {
+    alloc(h.size());
+    if (!h.empty()) GBTN_CUDA(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+};
+
+struct HostWork {
+  std::vector<int> vertices;
+  int ncap = 0, maxdeg = 0, team = 32;
+};
+
+}  // namespace
+
+struct gbtn_plan {
+  gbtn_ctx* ctx = nullptr;
+  int nv = 0, ne = 0, nnet = 1;
+  bool sep_bra = false;
+  long long n_fac = 0, n_msg = 0, n_rdm = 0;
+  int ncap = 0, maxdeg = 0;
+  std::vector<VDesc> vd;
+  std::vector<int> eu, ev, dchi, dsite, vnet;
+  std::vector<long long> msg_off, rdm_off;
+  std::vector<int> color;
+
+  DevBuf<VDesc> d_vd;
+  DevBuf<long long> d_msg_off, d_rdm_off;
+  DevBuf<int> d_dchi, d_dsite;
+  DevBuf<double> d_fac, d_bra;
+  DevBuf<float> d_fac32, d_bra32;
+  bool fac32_valid = false;
+  DevBuf<double> d_msg[2];
+  DevBuf<float> d_msg32[2];
+  int cur = 0;  // buffer holding the current messages
+  DevBuf<double> d_diffs, d_mean, d_rdm, d_edge_sc, d_re, d_im, d_scale, d_out;
+  DevBuf<int> d_conv, d_iters;
+  DevBuf<int> d_net_de_ptr, d_net_de, d_net_v_ptr, d_net_v, d_net_e_ptr, d_net_e;
+  // work lists: index 0 = all vertices, 1.. = colour classes; two size classes each
+  std::vector<std::pair<WorkList, WorkList>> lists;
+  std::vector<std::unique_ptr<DevBuf<int>>> list_store;
+  // sequential schedule storage
+  DevBuf<int2> d_seq;
+  DevBuf<int> d_seq_ptr;
+  DevBuf<int> d_jobs;
+  DevBuf<long long> d_half_off;
+  DevBuf<double> d_halves;
+};
+
+namespace {
+
+constexpr int kSmallN = 1024;  // vertices with n <= kSmallN run one per warp
+
+void set_err(const gbtn_ctx* ctx, const std::string& m) {
+  if (ctx)
+    const_cast<gbtn_ctx*>(ctx)->err = m;
+  else
+    g_err_noctx = m;
+}
+
+#define API_TRY try {
+#define API_CATCH(CTX)                                      \
+  }                                                         \
+  catch (const InvalidArg& e) {                             \
+    set_err(CTX, e.what());                                 \
+    return GBTN_ERR_INVALID;                                \
+  }                                                         \
+  catch (const Unsupported& e) {                            \
+    set_err(CTX, e.what());                                 \
+    return GBTN_ERR_UNSUPPORTED;                            \
+  }                                                         \
+  catch (const CudaError& e) {                              \
+    set_err(CTX, e.what());                                 \
+    return GBTN_ERR_CUDA;                                   \
+  }                                                         \
+  catch (const std::bad_alloc&) {                           \
+    set_err(CTX, "host allocation failed");                 \
+    return GBTN_ERR_NOMEM;                                  \
+  }                                                         \
+  catch (const std::exception& e) {                         \
+    set_err(CTX, e.what());                                 \
+    return GBTN_ERR_INVALID;                                \
+  }                                                         \
+  return GBTN_OK;
+
+void require(bool c, const std::string& m) {
+  if (!c) throw InvalidArg(m);
+}
+
+WorkList make_list(gbtn_plan* P, const std::vector<int>& verts, int team) {
+  WorkList w;
+  w.count = (int)verts.size();
+  w.team = team;
+  for (int v : verts) {
+    w.ncap = std::max(w.ncap, P->vd[v].n);
+    w.maxdeg = std::max(w.maxdeg, P->vd[v].k);
+  }
+  auto buf = std::make_unique<DevBuf<int>>();
+  buf->upload(verts, P->ctx->stream);
+  w.d_vertices = buf->p;
+  P->list_store.push_back(std::move(buf));
+  return w;
+}
+
+std::pair<WorkList, WorkList> split_list(gbtn_plan* P, const std::vector<int>& verts) {
+  std::vector<int> small, large;
+  for (int v : verts) (P->vd[v].n <= kSmallN ? small : large).push_back(v);
+  return {make_list(P, small, 32), make_list(P, large, 256)};
+}
+
+void copy_out(gbtn_plan* P, void* dst, const void* src, size_t bytes, int mem) {
+  GBTN_CUDA(cudaMemcpyAsync(dst, src, bytes, mem == GBTN_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                            P->ctx->stream));
+  if (mem == GBTN_HOST) GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));
+}
+
+void copy_in(gbtn_plan* P, void* dst, const void* src, size_t bytes, int mem) {
+  GBTN_CUDA(cudaMemcpyAsync(dst, src, bytes, mem == GBTN_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                            P->ctx->stream));
+  if (mem == GBTN_HOST) GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));
+}
+
+void ensure_f32(gbtn_plan* P) {
+  cudaStream_t s = P->ctx->stream;
+  if (!P->d_fac32.p) {
+    P->d_fac32.alloc(P->n_fac);
+    if (P->sep_bra) P->d_bra32.alloc(P->n_fac);
+    P->d_msg32[0].alloc(P->n_msg);
+    P->d_msg32[1].alloc(P->n_msg);
+  }
+  if (!P->fac32_valid) {
+    launch_convert_f64_to_f32(P->d_fac.p, P->d_fac32.p, P->n_fac, s);
+    if (P->sep_bra) launch_convert_f64_to_f32(P->d_bra.p, P->d_bra32.p, P->n_fac, s);
+    P->fac32_valid = true;
+  }
+}
+
+size_t smem_need(int n, int k, bool sep_bra, size_t elt, int team) {
+  const int nbuf = k <= 4 ? 3 : kNumBufs;
+  size_t b = (sizeof(VDesc) + 15) / 16 * 16;
+  b += elt * ((size_t)n * (nbuf + (sep_bra ? 1 : 0)) + kMaxDeg * 64 + (team / 32) * 64 + 64);
+  return (b + 15) / 16 * 16;
+}
+
+// Sweeps of the parallel or coloured schedule in precision T.
+template <typename T>
+void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normalize, DevBuf<T>* msg, const T* fac,
+                const T* bra, int& cur) {
+  cudaStream_t s = P->ctx->stream;
+  const bool want_diff = tol >= 0.0;
+  GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int) * P->nnet, s));
+  GBTN_CUDA(cudaMemsetAsync(P->d_iters.p, 0, sizeof(int) * P->nnet, s));
+  const int* conv = want_diff ? P->d_conv.p : nullptr;
+  for (int it = 0; it < maxiter; ++it) {
+    if (schedule == GBTN_SCHED_PARALLEL) {
+      const T* in = msg[cur].p;
+      T* out = msg[cur ^ 1].p;
+      launch_bp_vertices<T>(P->lists[0].first, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
+                            normalize, want_diff, s);
+      launch_bp_vertices<T>(P->lists[0].second, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
+                            normalize, want_diff, s);
+      cur ^= 1;
+    } else {
+      for (size_t c = 1; c < P->lists.size(); ++c) {
+        T* m = msg[cur].p;
+        launch_bp_vertices<T>(P->lists[c].first, P->d_vd.p, fac, bra, m, m, P->d_msg_off.p, P->d_diffs.p, conv,
+                              normalize, want_diff, s);
+        launch_bp_vertices<T>(P->lists[c].second, P->d_vd.p, fac, bra, m, m, P->d_msg_off.p, P->d_diffs.p, conv,
+                              normalize, want_diff, s);
+      }
+    }
+    if (want_diff)
+      launch_reduce_diffs(P->nnet, P->d_net_de_ptr.p, P->d_net_de.p, P->d_diffs.p, tol, P->d_conv.p, P->d_iters.p,
+                          P->d_mean.p, s);
+  }
+}
+
+void finish_iters(gbtn_plan* P, bool want_diff, int maxiter, int32_t* iters, double* mean_diff) {
+  cudaStream_t s = P->ctx->stream;
+  if (!iters && !mean_diff) return;
+  std::vector<int> it(P->nnet, maxiter);
+  std::vector<double> md(P->nnet, NAN);
+  if (want_diff) {
+    GBTN_CUDA(cudaMemcpyAsync(it.data(), P->d_iters.p, sizeof(int) * P->nnet, cudaMemcpyDeviceToHost, s));
+    GBTN_CUDA(cudaMemcpyAsync(md.data(), P->d_mean.p, sizeof(double) * P->nnet, cudaMemcpyDeviceToHost, s));
+  }
+  GBTN_CUDA(cudaStreamSynchronize(s));
+  if (iters) std::copy(it.begin(), it.end(), iters);
+  if (mean_diff) std::copy(md.begin(), md.end(), mean_diff);
+}
+
+void compute_rdms(gbtn_plan* P) {
+  cudaStream_t s = P->ctx->stream;
+  launch_vertex_rdms(P->lists[0].first, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p,
+                     P->d_msg_off.p, P->d_rdm_off.p, P->d_rdm.p, s);
+  launch_vertex_rdms(P->lists[0].second, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p,
+                     P->d_msg_off.p, P->d_rdm_off.p, P->d_rdm.p, s);
+}
+
+}  // namespace
+
+// Small kernels of the API layer.
+__global__ void expect1_kernel(int nv, const long long* rdm_off, const double* rdm, const int* dsite, const double* ops,
+                               const long long* op_off, double* out) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int d = dsite[v];
+  const double* r = rdm + rdm_off[v];
+  const double* o = ops + (op_off ? op_off[v] : 0);
+  double num = 0.0, den = 0.0;
+  for (int i = 0; i < d * d; ++i) num += r[i] * o[i];
+  for (int q = 0; q < d; ++q) den += r[q + d * q];
+  out[v] = num / den;
+}
+
+// rho[(s'u, s'v), (su, sv)] = sum_{b,a} Ru[s'u, su, b, a] Rv[s'v, sv, b, a]
+__global__ void edge_rdm_combine_kernel(int nedges, const int* du_, const int* dv_, const int* chi_,
+                                        const long long* hu_off, const long long* hv_off, const double* halves,
+                                        const long long* out_off, double* out) {
+  const int j = blockIdx.x;
+  if (j >= nedges) return;
+  const int du = du_[j], dv = dv_[j], c2 = chi_[j] * chi_[j];
+  const int D = du * dv;
+  for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) {
+    const int row = idx % D, col = idx / D;
+    const int spu = row % du, spv = row / du, su = col % du, sv = col / du;
+    const double* ru = halves + hu_off[j] + (long long)(spu + du * su) * c2;
+    const double* rv = halves + hv_off[j] + (long long)(spv + dv * sv) * c2;
+    double acc = 0.0;
+    for (int i = 0; i < c2; ++i) acc += ru[i] * rv[i];
+    out[out_off[j] + idx] = acc;
+  }
+}
+
+__global__ void expect2_kernel(int nedges, const long long* rdm_off, const int* D_, const double* rdm, const double* op,
+                               double* out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nedges) return;
+  const int D = D_[j];
+  const double* r = rdm + rdm_off[j];
+  double num = 0.0, den = 0.0;
+  for (int i = 0; i < D * D; ++i) num += r[i] * op[i];
+  for (int q = 0; q < D; ++q) den += r[q + D * q];
+  out[j] = num / den;
+}
+
+// Partition scale factors (rescale_partitions): ket *= vn/|ket|, bra *= s*vn/|bra|
+// with Z' = Z/(|ket||bra|), s = sign(Z'), vn = |Z'|^(-1/2).  With a shared
+// bra a negative Z' cannot be represented and yields NaN scales.
+__global__ void partition_scale_kernel(int nv, const VDesc* vd, const double* fac, const double* bra,
+                                       const long long* rdm_off, const double* rdm, double* scale) {
+  const int v = blockIdx.x;
+  const long long off = vd[v].a_off;
+  const int n = vd[v].n, d = vd[v].d;
+  double nk = 0.0, nb = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    nk += fac[off + i] * fac[off + i];
+    if (bra) nb += bra[off + i] * bra[off + i];
+  }
+  __shared__ double r1[32], r2[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    nk += __shfl_xor_sync(0xffffffffu, nk, o);
+    nb += __shfl_xor_sync(0xffffffffu, nb, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    r1[threadIdx.x >> 5] = nk;
+    r2[threadIdx.x >> 5] = nb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += r1[w];
+      b += r2[w];
+    }
+    const double normk = sqrt(a);
+    const double normb = bra ? sqrt(b) : normk;
+    double z = 0.0;
+    for (int q = 0; q < d; ++q) z += rdm[rdm_off[v] + q + d * q];
+    const double zp = z / (normk * normb);
+    const double sgn = zp > 0.0 ? 1.0 : (zp < 0.0 ? -1.0 : 0.0);
+    const double vn = 1.0 / sqrt(fabs(zp));
+    if (bra) {
+      scale[2 * v] = vn / normk;
+      scale[2 * v + 1] = sgn * vn / normb;
+    } else {
+      scale[2 * v] = sgn > 0.0 ? vn / normk : NAN;
+      scale[2 * v + 1] = 1.0;
+    }
+  }
+}
+
+extern "C" {
+
+int gbtn_abi_version(void) { return GBTN_ABI_VERSION; }
+
+const char* gbtn_last_error(const gbtn_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err_noctx.c_str(); }
+
+int gbtn_ctx_create(int device, gbtn_ctx** out) {
+  API_TRY
+  require(out != nullptr, "out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  GBTN_CUDA(cudaGetDeviceCount(&ndev));
+  require(device >= 0 && device < ndev, "device index out of range");
+  GBTN_CUDA(cudaSetDevice(device));
+  auto c = std::make_unique<gbtn_ctx>();
+  c->device = device;
+  GBTN_CUDA(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking));
+  c->stream = c->own;
+  c->sched = build_schedules();
+  upload_schedules(c->sched);
+  *out = c.release();
+  API_CATCH(nullptr)
+}
+
+int gbtn_ctx_destroy(gbtn_ctx* ctx) {
+  if (!ctx) return GBTN_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->own) {
+    cudaStreamSynchronize(ctx->own);
+    cudaStreamDestroy(ctx->own);
+  }
+  delete ctx;
+  return GBTN_OK;
+}
+
+int gbtn_ctx_set_stream(gbtn_ctx* ctx, void* stream) {
+  if (!ctx) return GBTN_ERR_INVALID;
+  ctx->stream = stream ? reinterpret_cast<cudaStream_t>(stream) : ctx->own;
+  return GBTN_OK;
+}
+
+void* gbtn_ctx_get_stream(const gbtn_ctx* ctx) { return ctx ? reinterpret_cast<void*>(ctx->stream) : nullptr; }
+
+int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
+  API_TRY
+  require(ctx && g && out, "NULL argument");
+  *out = nullptr;
+  GBTN_CUDA(cudaSetDevice(ctx->device));
+  require(g->nv >= 1 && g->ne >= 0, "graph needs nv >= 1 and ne >= 0");
+  require(g->ne == 0 || (g->edge_u && g->edge_v && g->edge_dim), "edge arrays are NULL");
+  require(g->site_dim && g->leg_ptr && (g->leg_edge || g->ne == 0), "vertex arrays are NULL");
+  auto P = std::make_unique<gbtn_plan>();
+  P->ctx = ctx;
+  P->nv = g->nv;
+  P->ne = g->ne;
+  P->sep_bra = g->separate_bra != 0;
+  P->nnet = g->vertex_network ? g->n_networks : 1;
+  require(P->nnet >= 1, "n_networks must be >= 1");
+  P->eu.assign(g->edge_u, g->edge_u + g->ne);
+  P->ev.assign(g->edge_v, g->edge_v + g->ne);
+  P->dsite.assign(g->site_dim, g->site_dim + g->nv);
+  P->vnet.assign(g->nv, 0);
+  if (g->vertex_network) P->vnet.assign(g->vertex_network, g->vertex_network + g->nv);
+  for (int v = 0; v < g->nv; ++v) {
+    require(P->vnet[v] >= 0 && P->vnet[v] < P->nnet, "vertex_network out of range");
+    require(P->dsite[v] >= 1 && P->dsite[v] <= kMaxSite, "site dimension must be in 1..8");
+  }
+  P->dchi.resize(2 * (size_t)g->ne);
+  for (int e = 0; e < g->ne; ++e) {
+    const int u = P->eu[e], v = P->ev[e], c = g->edge_dim[e];
+    require(u >= 0 && u < g->nv && v >= 0 && v < g->nv, "edge endpoint out of range");
+    require(u != v, "self loops are not allowed");
+    require(P->vnet[u] == P->vnet[v], "edge joins two different networks");
+    if (c < 1 || c > kMaxChi) throw Unsupported("bond dimension must be in 1..8");
+    P->dchi[2 * e] = P->dchi[2 * e + 1] = c;
+  }
+  // messages
+  P->msg_off.resize(2 * (size_t)g->ne);
+  long long off = 0;
+  for (int de = 0; de < 2 * g->ne; ++de) {
+    P->msg_off[de] = off;
+    off += (long long)P->dchi[de] * P->dchi[de];
+  }
+  P->n_msg = off;
+  // vertices
+  require(g->leg_ptr[0] == 0, "leg_ptr[0] must be 0");
+  std::vector<int> seen_count(g->ne, 0);
+  P->vd.resize(g->nv);
+  off = 0;
+  long long roff = 0;
+  P->rdm_off.resize(g->nv);
+  for (int v = 0; v < g->nv; ++v) {
+    VDesc d{};
+    const int b = g->leg_ptr[v], e_ = g->leg_ptr[v + 1];
+    require(e_ >= b, "leg_ptr must be non-decreasing");
+    d.k = e_ - b;
+    if (d.k > kMaxDeg) throw Unsupported("vertex degree above 8");
+    d.d = P->dsite[v];
+    d.net = P->vnet[v];
+    d.a_off = off;
+    long long n = d.d;
+    for (int p = 0; p < d.k; ++p) {
+      const int e = g->leg_edge[b + p];
+      require(e >= 0 && e < g->ne, "leg_edge out of range");
+      require(P->eu[e] == v || P->ev[e] == v, "leg_edge names an edge not incident to the vertex");
+      seen_count[e]++;
+      d.chi[p] = P->dchi[2 * e];
+      d.st[p] = (int)n;
+      n *= d.chi[p];
+      const bool fwd = P->eu[e] == v;
+      d.out_de[p] = fwd ? 2 * e : 2 * e + 1;
+      d.in_de[p] = fwd ? 2 * e + 1 : 2 * e;
+    }
+    if (n > (1 << 20)) throw Unsupported("vertex tensor above 2^20 elements");
+    d.n = (int)n;
+    P->vd[v] = d;
+    off += n;
+    P->rdm_off[v] = roff;
+    roff += (long long)d.d * d.d;
+    P->ncap = std::max(P->ncap, d.d == 0 ? 0 : (int)n);
+    P->maxdeg = std::max(P->maxdeg, d.k);
+    // the FP64 sweep needs its tensors in shared memory
+    const int team = n <= kSmallN ? 32 : 256;
+    const size_t need = smem_need((int)n, d.k, P->sep_bra, sizeof(double), team) * (team == 32 ? 4 : 1);
+    if (need > 227 * 1024) throw Unsupported("vertex tensor too large for the shared-memory kernels");
+  }
+  for (int e = 0; e < g->ne; ++e) require(seen_count[e] == 2, "every edge must appear once in the legs of each endpoint");
+  P->n_fac = off;
+  P->n_rdm = roff;
+
+  cudaStream_t s = ctx->stream;
+  P->d_vd.upload(P->vd, s);
+  P->d_msg_off.upload(P->msg_off, s);
+  P->d_rdm_off.upload(P->rdm_off, s);
+  P->d_dchi.upload(P->dchi, s);
+  P->d_dsite.upload(P->dsite, s);
+  P->d_fac.alloc(P->n_fac);
+  GBTN_CUDA(cudaMemsetAsync(P->d_fac.p, 0, sizeof(double) * std::max<long long>(P->n_fac, 1), s));
+  if (P->sep_bra) P->d_bra.alloc(P->n_fac);
+  P->d_msg[0].alloc(std::max<long long>(P->n_msg, 1));
+  P->d_msg[1].alloc(std::max<long long>(P->n_msg, 1));
+  P->d_diffs.alloc(std::max<long long>(2LL * P->ne, 1));
+  P->d_mean.alloc(P->nnet);
+  P->d_conv.alloc(P->nnet);
+  P->d_iters.alloc(P->nnet);
+  P->d_rdm.alloc(std::max<long long>(P->n_rdm, 1));
+  P->d_edge_sc.alloc(std::max(P->ne, 1));
+  P->d_re.alloc(P->nnet);
+  P->d_im.alloc(P->nnet);
+  P->d_scale.alloc(2 * (size_t)P->nv);
+
+  // per-network bookkeeping (parallel-sequence order of directed edges)
+  std::vector<std::vector<int>> nde(P->nnet), nvv(P->nnet), nee(P->nnet);
+  for (int e = 0; e < g->ne; ++e) nde[P->vnet[P->eu[e]]].push_back(2 * e);
+  for (int e = 0; e < g->ne; ++e) nde[P->vnet[P->eu[e]]].push_back(2 * e + 1);
+  for (int v = 0; v < g->nv; ++v) nvv[P->vnet[v]].push_back(v);
+  for (int e = 0; e < g->ne; ++e) nee[P->vnet[P->eu[e]]].push_back(e);
+  auto csr = [&](const std::vector<std::vector<int>>& L, DevBuf<int>& ptr, DevBuf<int>& idx) {
+    std::vector<int> p(1, 0), x;
+    for (auto& l : L) {
+      x.insert(x.end(), l.begin(), l.end());
+      p.push_back((int)x.size());
+    }
+    ptr.upload(p, s);
+    if (x.empty()) x.push_back(0);
+    idx.upload(x, s);
+  };
+  csr(nde, P->d_net_de_ptr, P->d_net_de);
+  csr(nvv, P->d_net_v_ptr, P->d_net_v);
+  csr(nee, P->d_net_e_ptr, P->d_net_e);
+
+  // work lists: all vertices, then greedy colour classes in vertex order
+  std::vector<int> all(g->nv);
+  std::iota(all.begin(), all.end(), 0);
+  P->lists.push_back(split_list(P.get(), all));
+  std::vector<std::vector<int>> nbrs(g->nv);
+  for (int e = 0; e < g->ne; ++e) {
+    nbrs[P->eu[e]].push_back(P->ev[e]);
+    nbrs[P->ev[e]].push_back(P->eu[e]);
+  }
+  P->color.assign(g->nv, -1);
+  int ncol = 0;
+  for (int v = 0; v < g->nv; ++v) {
+    std::vector<char> used(g->nv + 1, 0);
+    for (int w : nbrs[v])
+      if (P->color[w] >= 0) used[P->color[w]] = 1;
+    int c = 0;
+    while (used[c]) ++c;
+    P->color[v] = c;
+    ncol = std::max(ncol, c + 1);
+  }
+  for (int c = 0; c < ncol; ++c) {
+    std::vector<int> vs;
+    for (int v = 0; v < g->nv; ++v)
+      if (P->color[v] == c) vs.push_back(v);
+    P->lists.push_back(split_list(P.get(), vs));
+  }
+  launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[0].p, GBTN_INIT_IDENTITY, s);
+  GBTN_CUDA(cudaStreamSynchronize(s));
+  *out = P.release();
+  API_CATCH(ctx)
+}
+
+int gbtn_plan_destroy(gbtn_plan* plan) {
+  if (!plan) return GBTN_OK;
+  cudaStreamSynchronize(plan->ctx->stream);
+  delete plan;
+  return GBTN_OK;
+}
+
+int gbtn_plan_sizes(const gbtn_plan* P, int64_t* n_factor, int64_t* n_message) {
+  if (!P) return GBTN_ERR_INVALID;
+  if (n_factor) *n_factor = P->n_fac;
+  if (n_message) *n_message = P->n_msg;
+  return GBTN_OK;
+}
+
+int gbtn_set_factors(gbtn_plan* P, const double* ket, const double* bra, int mem) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && ket, "NULL argument");
+  require(!P->sep_bra || bra, "plan has separate_bra: bra tensors are required");
+  copy_in(P, P->d_fac.p, ket, sizeof(double) * P->n_fac, mem);
+  if (P->sep_bra) copy_in(P, P->d_bra.p, bra, sizeof(double) * P->n_fac, mem);
+  P->fac32_valid = false;
+  API_CATCH(C)
+}
+
+int gbtn_get_factors(gbtn_plan* P, double* ket, int mem) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && ket, "NULL argument");
+  copy_out(P, ket, P->d_fac.p, sizeof(double) * P->n_fac, mem);
+  API_CATCH(C)
+}
+
+int gbtn_set_messages(gbtn_plan* P, const double* m, int mem) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && m, "NULL argument");
+  copy_in(P, P->d_msg[P->cur].p, m, sizeof(double) * P->n_msg, mem);
+  API_CATCH(C)
+}
+
+int gbtn_get_messages(gbtn_plan* P, double* m, int mem) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && m, "NULL argument");
+  copy_out(P, m, P->d_msg[P->cur].p, sizeof(double) * P->n_msg, mem);
+  API_CATCH(C)
+}
+
+int gbtn_init_messages(gbtn_plan* P, int kind) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P, "NULL plan");
+  require(kind == GBTN_INIT_IDENTITY || kind == GBTN_INIT_ONES, "unknown message init");
+  launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, kind, P->ctx->stream);
+  API_CATCH(C)
+}
+
+int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mean_diff) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && o, "NULL argument");
+  require(o->maxiter >= 1, "You need to specify a number of iterations for BP!");
+  require(o->schedule >= 0 && o->schedule <= 2, "unknown schedule");
+  require(o->precision >= 0 && o->precision <= 3, "unknown precision");
+  cudaStream_t s = P->ctx->stream;
+  const bool want_diff = o->tol >= 0.0;
+  if (P->ne == 0) {
+    finish_iters(P, false, o->maxiter, iters, mean_diff);
+    return GBTN_OK;
+  }
+  if (o->precision == GBTN_BF16) throw Unsupported("BF16 sweeps need the tensor-core kernel (not in this build)");
+  if (o->schedule == GBTN_SCHED_SEQUENTIAL) {
+    require(o->edge_sequence && o->edge_sequence_len > 0, "SEQUENTIAL needs an edge sequence");
+    std::vector<std::vector<int2>> per(P->nnet);
+    for (int i = 0; i < o->edge_sequence_len; ++i) {
+      const int de = o->edge_sequence[i];
+      require(de >= 0 && de < 2 * P->ne, "edge_sequence entry out of range");
+      const int e = de / 2;
+      const int v = (de & 1) ? P->ev[e] : P->eu[e];
+      int leg = -1;
+      for (int p = 0; p < P->vd[v].k; ++p)
+        if (P->vd[v].out_de[p] == de) leg = p;
+      per[P->vnet[v]].push_back(make_int2(v, leg));
+    }
+    std::vector<int2> seq;
+    std::vector<int> ptr(1, 0);
+    for (auto& l : per) {
+      require(!l.empty() || P->nnet == 1, "edge_sequence misses a network");
+      seq.insert(seq.end(), l.begin(), l.end());
+      ptr.push_back((int)seq.size());
+    }
+    for (int n = 0; n < P->nnet; ++n) require(ptr[n + 1] > ptr[n], "edge_sequence misses a network");
+    P->d_seq.upload(seq, s);
+    P->d_seq_ptr.upload(ptr, s);
+    if (o->precision == GBTN_F64) {
+      launch_bp_sequential<double>(P->nnet, P->d_vd.p, P->d_seq.p, P->d_seq_ptr.p, P->d_fac.p,
+                                   P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p, P->d_msg_off.p, o->maxiter,
+                                   o->tol, o->normalize, P->d_iters.p, P->d_mean.p, P->ncap, P->maxdeg, s);
+    } else {
+      ensure_f32(P);
+      launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, s);
+      launch_bp_sequential<float>(P->nnet, P->d_vd.p, P->d_seq.p, P->d_seq_ptr.p, P->d_fac32.p,
+                                  P->sep_bra ? P->d_bra32.p : nullptr, P->d_msg32[0].p, P->d_msg_off.p, o->maxiter,
+                                  o->tol, o->normalize, P->d_iters.p, P->d_mean.p, P->ncap, P->maxdeg, s);
+      launch_convert_f32_to_f64(P->d_msg32[0].p, P->d_msg[P->cur].p, P->n_msg, s);
+    }
+    // the sequential kernel reports iterations itself
+    if (iters || mean_diff) {
+      std::vector<int> it(P->nnet);
+      std::vector<double> md(P->nnet);
+      GBTN_CUDA(cudaMemcpyAsync(it.data(), P->d_iters.p, sizeof(int) * P->nnet, cudaMemcpyDeviceToHost, s));
+      GBTN_CUDA(cudaMemcpyAsync(md.data(), P->d_mean.p, sizeof(double) * P->nnet, cudaMemcpyDeviceToHost, s));
+      GBTN_CUDA(cudaStreamSynchronize(s));
+      if (iters) std::copy(it.begin(), it.end(), iters);
+      if (mean_diff) std::copy(md.begin(), md.end(), mean_diff);
+    }
+    return GBTN_OK;
+  }
+  if (o->precision == GBTN_F64) {
+    run_sweeps<double>(P, o->schedule, o->maxiter, o->tol, o->normalize, P->d_msg, P->d_fac.p,
+                       P->sep_bra ? P->d_bra.p : nullptr, P->cur);
+    finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
+  } else if (o->precision == GBTN_F32) {
+    ensure_f32(P);
+    int c32 = 0;
+    launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, s);
+    run_sweeps<float>(P, o->schedule, o->maxiter, o->tol, o->normalize, P->d_msg32, P->d_fac32.p,
+                      P->sep_bra ? P->d_bra32.p : nullptr, c32);
+    launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
+    finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
+  } else {  // MIXED: FP32 phase then FP64 refinement
+    ensure_f32(P);
+    int c32 = 0;
+    const double tol32 = o->tol_f32 > 0 ? o->tol_f32 : 1e-13;
+    const int it32 = o->maxiter_f32 > 0 ? o->maxiter_f32 : o->maxiter;
+    launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, s);
+    run_sweeps<float>(P, o->schedule, it32, tol32, o->normalize, P->d_msg32, P->d_fac32.p,
+                      P->sep_bra ? P->d_bra32.p : nullptr, c32);
+    launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
+    // FP64 sweeps from the FP32 fixed point until tol (or refine_f64 / maxiter sweeps)
+    const int nref = o->refine_f64 > 0 ? std::min(o->refine_f64, o->maxiter) : o->maxiter;
+    run_sweeps<double>(P, o->schedule, nref, o->tol, o->normalize, P->d_msg, P->d_fac.p,
+                       P->sep_bra ? P->d_bra.p : nullptr, P->cur);
+    finish_iters(P, want_diff, nref, iters, mean_diff);
+  }
+  API_CATCH(C)
+}
+
+int gbtn_updated_message(gbtn_plan* P, int32_t de, double* out) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && out, "NULL argument");
+  require(de >= 0 && de < 2 * P->ne, "directed edge out of range");
+  const int e = de / 2;
+  const int v = (de & 1) ? P->ev[e] : P->eu[e];
+  int leg = -1;
+  for (int p = 0; p < P->vd[v].k; ++p)
+    if (P->vd[v].out_de[p] == de) leg = p;
+  const int c = P->dchi[de];
+  P->d_out.alloc(c * c);
+  launch_updated_message(P->d_vd.p, v, leg, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p,
+                         P->d_msg_off.p, P->d_out.p, P->ncap, P->ctx->stream);
+  copy_out(P, out, P->d_out.p, sizeof(double) * c * c, GBTN_HOST);
+  API_CATCH(C)
+}
+
+int gbtn_vertex_rdms(gbtn_plan* P, double* out) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && out, "NULL argument");
+  compute_rdms(P);
+  copy_out(P, out, P->d_rdm.p, sizeof(double) * P->n_rdm, GBTN_HOST);
+  API_CATCH(C)
+}
+
+int gbtn_expect1(gbtn_plan* P, const double* ops, int per_vertex, double* out) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && ops && out, "NULL argument");
+  cudaStream_t s = P->ctx->stream;
+  compute_rdms(P);
+  DevBuf<double> d_ops, d_res;
+  DevBuf<long long> d_opoff;
+  if (per_vertex) {
+    std::vector<double> h(ops, ops + P->n_rdm);
+    d_ops.upload(h, s);
+    d_opoff.upload(P->rdm_off, s);
+  } else {
+    for (int v = 0; v < P->nv; ++v)
+      require(P->dsite[v] == P->dsite[0], "a shared operator needs one site dimension; pass per-vertex operators");
+    std::vector<double> h(ops, ops + P->dsite[0] * P->dsite[0]);
+    d_ops.upload(h, s);
+  }
+  d_res.alloc(P->nv);
+  expect1_kernel<<<(P->nv + 127) / 128, 128, 0, s>>>(P->nv, P->d_rdm_off.p, P->d_rdm.p, P->d_dsite.p, d_ops.p,
+                                                      per_vertex ? d_opoff.p : nullptr, d_res.p);
+  GBTN_CUDA(cudaGetLastError());
+  copy_out(P, out, d_res.p, sizeof(double) * P->nv, GBTN_HOST);
+  API_CATCH(C)
+}
+
+static void edge_rdms_device(gbtn_plan* P, const int32_t* edges, int32_t n, DevBuf<double>& d_out,
+                             std::vector<long long>& out_off) {
+  cudaStream_t s = P->ctx->stream;
+  std::vector<int> jobs;
+  std::vector<long long> hoff;
+  std::vector<int> du, dv, ch;
+  std::vector<long long> hu, hv;
+  long long off = 0, ooff = 0;
+  out_off.clear();
+  for (int j = 0; j < n; ++j) {
+    const int e = edges[j];
+    require(e >= 0 && e < P->ne, "edge out of range");
+    const int u = P->eu[e], v = P->ev[e];
+    int pu = -1, pv = -1;
+    for (int p = 0; p < P->vd[u].k; ++p)
+      if (P->vd[u].out_de[p] == 2 * e) pu = p;
+    for (int p = 0; p < P->vd[v].k; ++p)
+      if (P->vd[v].out_de[p] == 2 * e + 1) pv = p;
+    const int c = P->dchi[2 * e];
+    jobs.push_back(u);
+    jobs.push_back(pu);
+    hoff.push_back(off);
+    hu.push_back(off);
+    off += (long long)P->dsite[u] * P->dsite[u] * c * c;
+    jobs.push_back(v);
+    jobs.push_back(pv);
+    hoff.push_back(off);
+    hv.push_back(off);
+    off += (long long)P->dsite[v] * P->dsite[v] * c * c;
+    du.push_back(P->dsite[u]);
+    dv.push_back(P->dsite[v]);
+    ch.push_back(c);
+    out_off.push_back(ooff);
+    const long long D = (long long)P->dsite[u] * P->dsite[v];
+    ooff += D * D;
+  }
+  P->d_jobs.upload(jobs, s);
+  P->d_half_off.upload(hoff, s);
+  P->d_halves.alloc(std::max<long long>(off, 1));
+  launch_edge_halves(P->d_jobs.p, 2 * n, P->ncap, P->maxdeg, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr,
+                     P->d_msg[P->cur].p, P->d_msg_off.p, P->d_halves.p, P->d_half_off.p, s);
+  DevBuf<int> d_du, d_dv, d_ch;
+  DevBuf<long long> d_hu, d_hv, d_oo;
+  d_du.upload(du, s);
+  d_dv.upload(dv, s);
+  d_ch.upload(ch, s);
+  d_hu.upload(hu, s);
+  d_hv.upload(hv, s);
+  d_oo.upload(out_off, s);
+  d_out.alloc(std::max<long long>(ooff, 1));
+  edge_rdm_combine_kernel<<<n, 128, 0, s>>>(n, d_du.p, d_dv.p, d_ch.p, d_hu.p, d_hv.p, P->d_halves.p, d_oo.p, d_out.p);
+  GBTN_CUDA(cudaGetLastError());
+  GBTN_CUDA(cudaStreamSynchronize(s));
+}
+
+int gbtn_edge_rdms(gbtn_plan* P, const int32_t* edges, int32_t n, double* out) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && edges && out && n >= 0, "bad argument");
+  if (n == 0) return GBTN_OK;
+  DevBuf<double> d_out;
+  std::vector<long long> oo;
+  edge_rdms_device(P, edges, n, d_out, oo);
+  long long tot = 0;
+  for (int j = 0; j < n; ++j) {
+    const int e = edges[j];
+    const long long D = (long long)P->dsite[P->eu[e]] * P->dsite[P->ev[e]];
+    tot += D * D;
+  }
+  copy_out(P, out, d_out.p, sizeof(double) * tot, GBTN_HOST);
+  API_CATCH(C)
+}
+
+int gbtn_expect2(gbtn_plan* P, const int32_t* edges, int32_t n, const double* op, double* out) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && edges && op && out && n >= 0, "bad argument");
+  if (n == 0) return GBTN_OK;
+  cudaStream_t s = P->ctx->stream;
+  std::vector<int> D(n);
+  for (int j = 0; j < n; ++j) {
+    const int e = edges[j];
+    require(e >= 0 && e < P->ne, "edge out of range");
+    D[j] = P->dsite[P->eu[e]] * P->dsite[P->ev[e]];
+    require(D[j] == D[0], "a shared two-site operator needs equal site dimensions");
+  }
+  DevBuf<double> d_rdm, d_op, d_res;
+  std::vector<long long> oo;
+  edge_rdms_device(P, edges, n, d_rdm, oo);
+  DevBuf<long long> d_oo;
+  DevBuf<int> d_D;
+  d_oo.upload(oo, s);
+  d_D.upload(D, s);
+  std::vector<double> hop(op, op + D[0] * D[0]);
+  d_op.upload(hop, s);
+  d_res.alloc(n);
+  expect2_kernel<<<(n + 127) / 128, 128, 0, s>>>(n, d_oo.p, d_D.p, d_rdm.p, d_op.p, d_res.p);
+  GBTN_CUDA(cudaGetLastError());
+  copy_out(P, out, d_res.p, sizeof(double) * n, GBTN_HOST);
+  API_CATCH(C)
+}
+
+int gbtn_vertex_scalars(gbtn_plan* P, double* out) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && out, "NULL argument");
+  compute_rdms(P);
+  std::vector<double> r(P->n_rdm);
+  copy_out(P, r.data(), P->d_rdm.p, sizeof(double) * P->n_rdm, GBTN_HOST);
+  // trace of each d x d block (a host-side read-out of the device RDMs)
+  for (int v = 0; v < P->nv; ++v) {
+    double z = 0.0;
+    for (int q = 0; q < P->dsite[v]; ++q) z += r[P->rdm_off[v] + q + P->dsite[v] * q];
+    out[v] = z;
+  }
+  API_CATCH(C)
+}
+
+int gbtn_edge_scalars(gbtn_plan* P, double* out) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && out, "NULL argument");
+  if (P->ne == 0) return GBTN_OK;
+  launch_edge_scalars(P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, P->d_edge_sc.p, P->ctx->stream);
+  copy_out(P, out, P->d_edge_sc.p, sizeof(double) * P->ne, GBTN_HOST);
+  API_CATCH(C)
+}
+
+int gbtn_logscalar(gbtn_plan* P, double* re, double* im) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && re, "NULL argument");
+  cudaStream_t s = P->ctx->stream;
+  compute_rdms(P);
+  if (P->ne) launch_edge_scalars(P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, P->d_edge_sc.p, s);
+  launch_logscalar(P->nnet, P->d_net_v_ptr.p, P->d_net_v.p, P->d_net_e_ptr.p, P->d_net_e.p, P->d_rdm_off.p,
+                   P->d_rdm.p, P->d_dsite.p, P->d_edge_sc.p, P->d_re.p, P->d_im.p, s);
+  copy_out(P, re, P->d_re.p, sizeof(double) * P->nnet, GBTN_HOST);
+  if (im) copy_out(P, im, P->d_im.p, sizeof(double) * P->nnet, GBTN_HOST);
+  API_CATCH(C)
+}
+
+int gbtn_rescale_messages(gbtn_plan* P) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P, "NULL plan");
+  if (P->ne) launch_rescale_messages(P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, P->ctx->stream);
+  GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));
+  API_CATCH(C)
+}
+
+int gbtn_rescale_partitions(gbtn_plan* P) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P, "NULL plan");
+  cudaStream_t s = P->ctx->stream;
+  compute_rdms(P);
+  partition_scale_kernel<<<P->nv, 256, 0, s>>>(P->nv, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr,
+                                              P->d_rdm_off.p, P->d_rdm.p, P->d_scale.p);
+  GBTN_CUDA(cudaGetLastError());
+  launch_scale_vertices(P->nv, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_scale.p, s);
+  P->fac32_valid = false;
+  GBTN_CUDA(cudaStreamSynchronize(s));
+  API_CATCH(C)
+}
+
+}  // extern "C"

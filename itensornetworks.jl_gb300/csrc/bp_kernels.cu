@@ -1,0 +1,819 @@
+// SIMT kernels of the belief-propagation hot path (FP64 and FP32 arithmetic).
+//
+// A vertex v of the quadratic-form network <psi|psi> holds the ket tensor
+// A_v[s, a_1..a_k] (column-major); the bra is conj(A_v) (or a separate bra
+// tensor).  Every kernel here is built from two shared-memory "fiber" steps:
+//
+//   ABSORB(src -> dst, leg p):  dst[.., b_p, ..] = sum_a M_p[b_p, a] src[.., a, ..]
+//     (the incoming message on leg p moves the ket index a_p to the bra index b_p)
+//   CLOSE(src, leg p):          out[b, a] = sum_{fibers} bra[.., b, ..] * src[.., a, ..]
+//     (all other legs of src already carry bra indices; the site index is shared)
+//
+// The outgoing message on leg p (updated_message,
+// src/caches/abstractbeliefpropagationcache.jl:225-239) is CLOSE(p) of the
+// tensor with every other incoming message absorbed; all k outgoing messages
+// of a vertex share absorbed prefixes through a host-built schedule
+// (12 instead of 16 contraction steps at degree 4).  CLOSE on the site leg
+// gives the one-site reduced density matrix (expect.jl:5-19).
+#include <cmath>
+#include <functional>
+#include <numeric>
+
+#include "gbtn_internal.h"
+
+namespace gbtn {
+
+__constant__ DeviceSched c_sched;
+
+// ---------------------------------------------------------------------------
+// Host: vertex schedules
+// ---------------------------------------------------------------------------
+
+DeviceSched build_schedules() {
+  DeviceSched s{};
+  for (int k = 0; k <= kMaxDeg; ++k) {
+    std::vector<SchedOp> ops;
+    int maxbuf = 0;
+    std::function<void(int, const std::vector<int>&, const std::vector<int>&)> gen =
+        [&](int src, const std::vector<int>& W, const std::vector<int>& freeb) {
+          if (W.size() == 1) {
+            ops.push_back({1, (int8_t)src, 0, (int8_t)W[0]});
+            return;
+          }
+          const size_t h = W.size() / 2;
+          std::vector<int> W1(W.begin(), W.begin() + h), W2(W.begin() + h, W.end());
+          for (int half = 0; half < 2; ++half) {
+            const std::vector<int>& keep = half == 0 ? W1 : W2;
+            const std::vector<int>& absorb = half == 0 ? W2 : W1;
+            int cur = src;
+            for (int leg : absorb) {
+              int dst = -1;
+              for (int b : freeb)
+                if (b != cur) {
+                  dst = b;
+                  break;
+                }
+              if (dst < 0) throw std::logic_error("schedule: out of buffers");
+              ops.push_back({0, (int8_t)cur, (int8_t)dst, (int8_t)leg});
+              maxbuf = std::max(maxbuf, dst);
+              cur = dst;
+            }
+            std::vector<int> fb2;
+            for (int b : freeb)
+              if (b != cur) fb2.push_back(b);
+            gen(cur, keep, fb2);
+          }
+        };
+    if (k >= 1) {
+      std::vector<int> W(k);
+      std::iota(W.begin(), W.end(), 0);
+      std::vector<int> freeb;
+      for (int b = 1; b < kNumBufs; ++b) freeb.push_back(b);
+      gen(0, W, freeb);
+    }
+    if ((int)ops.size() > kMaxOps) throw std::logic_error("schedule too long");
+    for (size_t i = 0; i < ops.size(); ++i) s.ops[k][i] = ops[i];
+    s.len[k] = (int)ops.size();
+    s.nbuf[k] = maxbuf + 1;
+  }
+  return s;
+}
+
+void upload_schedules(const DeviceSched& s) { GBTN_CUDA(cudaMemcpyToSymbol(c_sched, &s, sizeof(s))); }
+
+// ---------------------------------------------------------------------------
+// Device helpers
+// ---------------------------------------------------------------------------
+
+template <int TEAM>
+__device__ __forceinline__ void tsync() {
+  if constexpr (TEAM == 32)
+    __syncwarp();
+  else
+    __syncthreads();
+}
+
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+// Reduce-scatter of P2 values over a warp: afterwards lane L holds the
+// warp-wide sums of entries [L*P2/32, (L+1)*P2/32) in v[0 .. P2/32).
+template <typename T, int P2>
+__device__ __forceinline__ void warp_reduce_scatter(T (&v)[P2], int lane) {
+#pragma unroll
+  for (int step = 0; step < 5; ++step) {
+    constexpr int dummy = 0;
+    (void)dummy;
+    const int h = P2 >> (step + 1);
+    const int mask = 16 >> step;
+    const bool upper = (lane & mask) != 0;
+#pragma unroll
+    for (int i = 0; i < P2 / 2; ++i) {
+      if (i < h) {
+        T send = upper ? v[i] : v[i + h];
+        T keep = upper ? v[i + h] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, mask);
+      }
+    }
+  }
+}
+
+template <typename T, int CHI>
+__device__ __forceinline__ void absorb_fibers(const T* __restrict__ in, T* __restrict__ out, int n, int st,
+                                              const T* __restrict__ M, int tid, int nth) {
+  T m[CHI][CHI];
+#pragma unroll
+  for (int b = 0; b < CHI; ++b)
+#pragma unroll
+    for (int a = 0; a < CHI; ++a) m[b][a] = M[b + CHI * a];
+  const int nfib = n / CHI;
+  for (int f = tid; f < nfib; f += nth) {
+    const int lo = f % st;
+    const int base = lo + (f - lo) * CHI;
+    T x[CHI];
+#pragma unroll
+    for (int a = 0; a < CHI; ++a) x[a] = in[base + a * st];
+#pragma unroll
+    for (int b = 0; b < CHI; ++b) {
+      T y = T(0);
+#pragma unroll
+      for (int a = 0; a < CHI; ++a) y = fma(m[b][a], x[a], y);
+      out[base + b * st] = y;
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void absorb_any(int chi, const T* in, T* out, int n, int st, const T* M, int tid,
+                                           int nth) {
+  switch (chi) {
+    case 1: absorb_fibers<T, 1>(in, out, n, st, M, tid, nth); break;
+    case 2: absorb_fibers<T, 2>(in, out, n, st, M, tid, nth); break;
+    case 3: absorb_fibers<T, 3>(in, out, n, st, M, tid, nth); break;
+    case 4: absorb_fibers<T, 4>(in, out, n, st, M, tid, nth); break;
+    case 5: absorb_fibers<T, 5>(in, out, n, st, M, tid, nth); break;
+    case 6: absorb_fibers<T, 6>(in, out, n, st, M, tid, nth); break;
+    case 7: absorb_fibers<T, 7>(in, out, n, st, M, tid, nth); break;
+    case 8: absorb_fibers<T, 8>(in, out, n, st, M, tid, nth); break;
+    default: break;
+  }
+}
+
+constexpr int kRedStride = 64;  // per-warp slot of the close reduction (CHI <= 8)
+
+// CLOSE over fibers ff = fib_add + fib_mul*f of leg (st, CHI); result
+// res[b + CHI*a] = sum bra[base+shift+b*st] * t[base+a*st] (team-wide sum).
+template <typename T, int CHI, int TEAM>
+__device__ __forceinline__ void close_fibers(const T* __restrict__ t, const T* __restrict__ bra, int n, int st,
+                                             int fib_mul, int fib_add, int bra_shift, T* red, T* res,
+                                             int tid) {
+  constexpr int P = CHI * CHI;
+  constexpr int P2 = P <= 32 ? 32 : 64;
+  T acc[P2];
+#pragma unroll
+  for (int i = 0; i < P2; ++i) acc[i] = T(0);
+  const int nfib = n / (CHI * fib_mul);
+  for (int f = tid; f < nfib; f += TEAM) {
+    const int ff = fib_add + fib_mul * f;
+    const int lo = ff % st;
+    const int base = lo + (ff - lo) * CHI;
+    T x[CHI], y[CHI];
+#pragma unroll
+    for (int a = 0; a < CHI; ++a) {
+      x[a] = t[base + a * st];
+      y[a] = bra[base + bra_shift + a * st];
+    }
+#pragma unroll
+    for (int a = 0; a < CHI; ++a)
+#pragma unroll
+      for (int b = 0; b < CHI; ++b) acc[b + CHI * a] = fma(y[b], x[a], acc[b + CHI * a]);
+  }
+  const int lane = tid & 31, warp = tid >> 5;
+  warp_reduce_scatter<T, P2>(acc, lane);
+  constexpr int PER = P2 / 32;
+  if constexpr (TEAM == 32) {
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int o = lane * PER + j;
+      if (o < P) res[o] = acc[j];
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < PER; ++j) red[warp * kRedStride + lane * PER + j] = acc[j];
+    __syncthreads();
+    for (int o = tid; o < P; o += TEAM) {
+      T s = T(0);
+#pragma unroll
+      for (int w = 0; w < TEAM / 32; ++w) s += red[w * kRedStride + o];
+      res[o] = s;
+    }
+  }
+  tsync<TEAM>();
+}
+
+template <typename T, int TEAM>
+__device__ __forceinline__ void close_any(int chi, const T* t, const T* bra, int n, int st, int fib_mul,
+                                          int fib_add, int bra_shift, T* red, T* res, int tid) {
+  switch (chi) {
+    case 1: close_fibers<T, 1, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 2: close_fibers<T, 2, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 3: close_fibers<T, 3, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 4: close_fibers<T, 4, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 5: close_fibers<T, 5, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 6: close_fibers<T, 6, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 7: close_fibers<T, 7, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 8: close_fibers<T, 8, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    default: break;
+  }
+}
+
+// Normalise res (chi x chi) in FP64, write it to out, and (when diff != NULL)
+// return message_diff(new, old) (abstractbeliefpropagationcache.jl:32-36) on
+// lane 0.  Called by one full warp; old may alias out.
+template <typename T>
+__device__ __forceinline__ double finalize_message(const T* res, int chi, const T* old, T* out, int normalize,
+                                                   bool want_diff, int lane) {
+  const int P = chi * chi;
+  const double v0 = lane < P ? (double)res[lane] : 0.0;
+  const double v1 = lane + 32 < P ? (double)res[lane + 32] : 0.0;
+  const double nrm2 = warp_sum(v0 * v0 + v1 * v1);
+  const double sc = (normalize && nrm2 > 0.0) ? 1.0 / sqrt(nrm2) : 1.0;
+  const T n0 = (T)(v0 * sc), n1 = (T)(v1 * sc);
+  double o0 = 0.0, o1 = 0.0;
+  if (want_diff) {
+    if (lane < P) o0 = (double)old[lane];
+    if (lane + 32 < P) o1 = (double)old[lane + 32];
+  }
+  __syncwarp();
+  if (lane < P) out[lane] = n0;
+  if (lane + 32 < P) out[lane + 32] = n1;
+  double diff = 0.0;
+  if (want_diff) {
+    const double a0 = (double)n0, a1 = (double)n1;
+    const double dot = warp_sum(a0 * o0 + a1 * o1);
+    const double na = warp_sum(a0 * a0 + a1 * a1);
+    const double nb = warp_sum(o0 * o0 + o1 * o1);
+    diff = 1.0 - (dot * dot) / (na * nb);
+  }
+  return diff;
+}
+
+// Shared-memory carve-up of one team.
+template <typename T>
+struct TeamSmem {
+  VDesc* desc;
+  T* buf[kNumBufs];
+  T* bra;
+  T* msg;  // kMaxDeg x 64
+  T* red;  // (TEAM/32) x kRedStride
+  T* res;  // 64
+};
+
+__host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+template <typename T>
+__host__ __device__ inline size_t team_smem_bytes(int ncap, int nbuf, bool sep_bra, int team) {
+  size_t b = align_up(sizeof(VDesc), 16);
+  b += sizeof(T) * ((size_t)ncap * (nbuf + (sep_bra ? 1 : 0)) + kMaxDeg * 64 + (team / 32) * kRedStride + 64);
+  return align_up(b, 16);
+}
+
+template <typename T>
+__device__ __forceinline__ TeamSmem<T> carve(unsigned char* p, int ncap, int nbuf, bool sep_bra, int team) {
+  TeamSmem<T> s;
+  s.desc = reinterpret_cast<VDesc*>(p);
+  T* q = reinterpret_cast<T*>(p + align_up(sizeof(VDesc), 16));
+  for (int i = 0; i < kNumBufs; ++i) s.buf[i] = q + (size_t)ncap * (i < nbuf ? i : 0);
+  q += (size_t)ncap * nbuf;
+  if (sep_bra) {
+    s.bra = q;
+    q += ncap;
+  } else {
+    s.bra = s.buf[0];
+  }
+  s.msg = q;
+  q += kMaxDeg * 64;
+  s.red = q;
+  q += (team / 32) * kRedStride;
+  s.res = q;
+  return s;
+}
+
+template <int TEAM>
+__device__ __forceinline__ void load_desc(VDesc* dst, const VDesc* src, int tid) {
+  constexpr int W = sizeof(VDesc) / 4;
+  const int* s = reinterpret_cast<const int*>(src);
+  int* d = reinterpret_cast<int*>(dst);
+  for (int i = tid; i < W; i += TEAM) d[i] = s[i];
+}
+
+// Load the tensor (and bra) of a vertex and its incoming messages (all legs,
+// or all but skip_leg) into shared memory.
+template <typename T, int TEAM>
+__device__ __forceinline__ void load_vertex(const TeamSmem<T>& S, const T* fac, const T* bra_g, const T* msgs,
+                                            const long long* msg_off, int skip_leg, int tid) {
+  const VDesc& d = *S.desc;
+  const T* a = fac + d.a_off;
+  for (int i = tid; i < d.n; i += TEAM) S.buf[0][i] = a[i];
+  if (bra_g) {
+    const T* b = bra_g + d.a_off;
+    for (int i = tid; i < d.n; i += TEAM) S.bra[i] = b[i];
+  }
+  for (int p = 0; p < d.k; ++p) {
+    if (p == skip_leg) continue;
+    const int c2 = d.chi[p] * d.chi[p];
+    const T* m = msgs + msg_off[d.in_de[p]];
+    for (int i = tid; i < c2; i += TEAM) S.msg[p * 64 + i] = m[i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi / coloured sweep kernel: every listed vertex computes all of its
+// outgoing messages from msg_in into msg_out.
+// ---------------------------------------------------------------------------
+
+template <typename T, int TEAM>
+__global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
+    bp_vertex_kernel(const int* __restrict__ work, int nwork, const VDesc* __restrict__ vd,
+                     const T* __restrict__ fac, const T* __restrict__ bra_g, const T* msg_in, T* msg_out,
+                     const long long* __restrict__ msg_off, double* diffs, const int* converged,
+                     int normalize, int want_diff, int ncap, int nbuf) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int TPB = TEAM == 32 ? 4 : 1;
+  const int team = threadIdx.x / TEAM, tid = threadIdx.x % TEAM, lane = tid & 31;
+  const size_t tb = team_smem_bytes<T>(ncap, nbuf, bra_g != nullptr, TEAM);
+  TeamSmem<T> S = carve<T>(smem_raw + team * tb, ncap, nbuf, bra_g != nullptr, TEAM);
+  for (int w = blockIdx.x * TPB + team; w < nwork; w += gridDim.x * TPB) {
+    const int v = work[w];
+    load_desc<TEAM>(S.desc, vd + v, tid);
+    tsync<TEAM>();
+    const VDesc& d = *S.desc;
+    if (converged && converged[d.net]) {
+      if (msg_in != msg_out) {
+        for (int p = 0; p < d.k; ++p) {
+          const long long off = msg_off[d.out_de[p]];
+          const int c2 = d.chi[p] * d.chi[p];
+          for (int i = tid; i < c2; i += TEAM) msg_out[off + i] = msg_in[off + i];
+        }
+      }
+      tsync<TEAM>();
+      continue;
+    }
+    load_vertex<T, TEAM>(S, fac, bra_g, msg_in, msg_off, -1, tid);
+    tsync<TEAM>();
+    const int k = d.k;
+    const int len = c_sched.len[k];
+    for (int i = 0; i < len; ++i) {
+      const SchedOp op = c_sched.ops[k][i];
+      const int leg = op.leg;
+      const int chi = d.chi[leg], st = d.st[leg];
+      if (op.type == 0) {
+        absorb_any<T>(chi, S.buf[op.src], S.buf[op.dst], d.n, st, S.msg + leg * 64, tid, TEAM);
+        tsync<TEAM>();
+      } else {
+        close_any<T, TEAM>(chi, S.buf[op.src], S.bra, d.n, st, 1, 0, 0, S.red, S.res, tid);
+        if (tid < 32) {
+          const int de = d.out_de[leg];
+          const long long off = msg_off[de];
+          const double df = finalize_message<T>(S.res, chi, msg_in + off, msg_out + off, normalize,
+                                                want_diff != 0, lane);
+          if (want_diff && lane == 0) diffs[de] = df;
+        }
+        tsync<TEAM>();
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Sequential schedule: one block per network walks its edge sequence for all
+// sweeps, each update seeing every earlier one; convergence is tested on the
+// device after every sweep (abstractbeliefpropagationcache.jl:272-287,313-329).
+// ---------------------------------------------------------------------------
+
+// Compute the message leaving v on leg p from the loaded vertex: absorb every
+// other leg (ping-pong through buffers 1 and 2), then CLOSE on p.
+template <typename T, int TEAM>
+__device__ __forceinline__ int chain_absorb(const TeamSmem<T>& S, int skip_leg, int tid) {
+  const VDesc& d = *S.desc;
+  int cur = 0;
+  for (int j = 0; j < d.k; ++j) {
+    if (j == skip_leg) continue;
+    const int nxt = cur == 1 ? 2 : 1;
+    absorb_any<T>(d.chi[j], S.buf[cur], S.buf[nxt], d.n, d.st[j], S.msg + j * 64, tid, TEAM);
+    tsync<TEAM>();
+    cur = nxt;
+  }
+  return cur;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    bp_sequential_kernel(const VDesc* __restrict__ vd, const int2* __restrict__ seq, const int* __restrict__ seq_ptr,
+                         const T* __restrict__ fac, const T* __restrict__ bra_g, T* msgs,
+                         const long long* __restrict__ msg_off, int maxiter, double tol, int normalize,
+                         int* iters, double* mean_diff, int ncap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int TEAM = 256;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int net = blockIdx.x;
+  TeamSmem<T> S = carve<T>(smem_raw, ncap, 3, bra_g != nullptr, TEAM);
+  __shared__ int s_stop;
+  const int begin = seq_ptr[net], end = seq_ptr[net + 1];
+  const bool want_diff = tol >= 0.0;
+  for (int it = 1; it <= maxiter; ++it) {
+    double sum = 0.0;
+    for (int i = begin; i < end; ++i) {
+      const int2 e = seq[i];
+      load_desc<TEAM>(S.desc, vd + e.x, tid);
+      __syncthreads();
+      load_vertex<T, TEAM>(S, fac, bra_g, msgs, msg_off, e.y, tid);
+      __syncthreads();
+      const int cur = chain_absorb<T, TEAM>(S, e.y, tid);
+      const VDesc& d = *S.desc;
+      close_any<T, TEAM>(d.chi[e.y], S.buf[cur], S.bra, d.n, d.st[e.y], 1, 0, 0, S.red, S.res, tid);
+      if (tid < 32) {
+        const long long off = msg_off[d.out_de[e.y]];
+        const double df = finalize_message<T>(S.res, d.chi[e.y], msgs + off, msgs + off, normalize, want_diff, lane);
+        sum += df;  // meaningful on tid 0 only
+      }
+      __syncthreads();
+    }
+    if (tid == 0) {
+      const double mean = sum / (double)(end - begin);
+      iters[net] = it;
+      mean_diff[net] = want_diff ? mean : NAN;
+      s_stop = (want_diff && mean <= tol) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_stop) break;
+  }
+}
+
+// One message, FP64, written to out without touching the cache.
+__global__ void __launch_bounds__(256)
+    updated_message_kernel(const VDesc* __restrict__ vd, int v, int leg, const double* __restrict__ fac,
+                           const double* __restrict__ bra_g, const double* msgs, const long long* msg_off,
+                           double* out, int ncap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int TEAM = 256;
+  const int tid = threadIdx.x;
+  TeamSmem<double> S = carve<double>(smem_raw, ncap, 3, bra_g != nullptr, TEAM);
+  load_desc<TEAM>(S.desc, vd + v, tid);
+  __syncthreads();
+  load_vertex<double, TEAM>(S, fac, bra_g, msgs, msg_off, leg, tid);
+  __syncthreads();
+  const int cur = chain_absorb<double, TEAM>(S, leg, tid);
+  const VDesc& d = *S.desc;
+  close_any<double, TEAM>(d.chi[leg], S.buf[cur], S.bra, d.n, d.st[leg], 1, 0, 0, S.red, S.res, tid);
+  if (tid < 32) finalize_message<double>(S.res, d.chi[leg], out, out, 1, false, tid);
+}
+
+// ---------------------------------------------------------------------------
+// Environment kernels (FP64)
+// ---------------------------------------------------------------------------
+
+// rho_v[s', s] for every listed vertex: absorb all incoming messages, CLOSE on
+// the site index.
+template <int TEAM>
+__global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
+    vertex_rdm_kernel(const int* __restrict__ work, int nwork, const VDesc* __restrict__ vd,
+                      const double* __restrict__ fac, const double* __restrict__ bra_g, const double* msgs,
+                      const long long* __restrict__ msg_off, const long long* __restrict__ rdm_off, double* rdm,
+                      int ncap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int TPB = TEAM == 32 ? 4 : 1;
+  const int team = threadIdx.x / TEAM, tid = threadIdx.x % TEAM;
+  const size_t tb = team_smem_bytes<double>(ncap, 3, bra_g != nullptr, TEAM);
+  TeamSmem<double> S = carve<double>(smem_raw + team * tb, ncap, 3, bra_g != nullptr, TEAM);
+  for (int w = blockIdx.x * TPB + team; w < nwork; w += gridDim.x * TPB) {
+    const int v = work[w];
+    load_desc<TEAM>(S.desc, vd + v, tid);
+    tsync<TEAM>();
+    load_vertex<double, TEAM>(S, fac, bra_g, msgs, msg_off, -1, tid);
+    tsync<TEAM>();
+    const int cur = chain_absorb<double, TEAM>(S, -1, tid);
+    const VDesc& d = *S.desc;
+    close_any<double, TEAM>(d.d, S.buf[cur], S.bra, d.n, 1, 1, 0, 0, S.red, S.res, tid);
+    for (int i = tid; i < d.d * d.d; i += TEAM) rdm[rdm_off[v] + i] = S.res[i];
+    tsync<TEAM>();
+  }
+}
+
+// Half of a two-site RDM: for job (v, p), R[s', s, b, a] with every incoming
+// message of v except the one on leg p absorbed, stored at
+// half[(s' + d*s)*chi*chi + b + chi*a].
+__global__ void __launch_bounds__(256)
+    edge_half_kernel(const int2* __restrict__ jobs, int njobs, const VDesc* __restrict__ vd,
+                     const double* __restrict__ fac, const double* __restrict__ bra_g, const double* msgs,
+                     const long long* __restrict__ msg_off, double* halves, const long long* __restrict__ half_off,
+                     int ncap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int TEAM = 256;
+  const int tid = threadIdx.x;
+  TeamSmem<double> S = carve<double>(smem_raw, ncap, 3, bra_g != nullptr, TEAM);
+  for (int j = blockIdx.x; j < njobs; j += gridDim.x) {
+    const int2 jb = jobs[j];
+    load_desc<TEAM>(S.desc, vd + jb.x, tid);
+    __syncthreads();
+    load_vertex<double, TEAM>(S, fac, bra_g, msgs, msg_off, jb.y, tid);
+    __syncthreads();
+    const int cur = chain_absorb<double, TEAM>(S, jb.y, tid);
+    const VDesc& d = *S.desc;
+    const int chi = d.chi[jb.y];
+    for (int s = 0; s < d.d; ++s)
+      for (int sp = 0; sp < d.d; ++sp) {
+        close_any<double, TEAM>(chi, S.buf[cur], S.bra, d.n, d.st[jb.y], d.d, s, sp - s, S.red, S.res, tid);
+        for (int i = tid; i < chi * chi; i += TEAM) halves[half_off[j] + (long long)(sp + d.d * s) * chi * chi + i] = S.res[i];
+        __syncthreads();
+      }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Small elementwise / per-edge kernels
+// ---------------------------------------------------------------------------
+
+__global__ void reduce_diffs_kernel(const int* __restrict__ net_de_ptr, const int* __restrict__ net_de,
+                                    const double* __restrict__ diffs, double tol, int* converged, int* iters,
+                                    double* mean_diff) {
+  const int net = blockIdx.x;
+  if (converged[net]) return;
+  const int b = net_de_ptr[net], e = net_de_ptr[net + 1];
+  double s = 0.0;
+  for (int i = b + threadIdx.x; i < e; i += blockDim.x) s += diffs[net_de[i]];
+  __shared__ double red[32];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = threadIdx.x < (int)(blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    t = warp_sum(t);
+    if (threadIdx.x == 0) {
+      const double mean = t / (double)(e - b);
+      iters[net] += 1;
+      mean_diff[net] = tol >= 0.0 ? mean : NAN;
+      if (tol >= 0.0 && mean <= tol) converged[net] = 1;
+    }
+  }
+}
+
+__global__ void convert_kernel_f64_f32(const double* a, float* b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+__global__ void convert_kernel_f32_f64(const float* a, double* b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+__global__ void convert_kernel_f64_bf16(const double* a, __nv_bfloat16* b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = __double2bfloat16(a[i]);
+}
+
+__global__ void fill_messages_kernel(int ndir, const int* dchi, const long long* msg_off, double* msgs, int kind) {
+  const int de = blockIdx.x;
+  if (de >= ndir) return;
+  const int c = dchi[de];
+  for (int i = threadIdx.x; i < c * c; i += blockDim.x) {
+    const int b = i % c, a = i / c;
+    msgs[msg_off[de] + i] = kind == GBTN_INIT_ONES ? 1.0 / c : (a == b ? 1.0 : 0.0);
+  }
+}
+
+__global__ void scale_vertices_kernel(int nv, const VDesc* vd, double* fac, double* bra, const double* scale) {
+  const int v = blockIdx.x;
+  if (v >= nv) return;
+  const long long off = vd[v].a_off;
+  const int n = vd[v].n;
+  const double sk = scale[2 * v], sb = scale[2 * v + 1];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    fac[off + i] *= sk;
+    if (bra) bra[off + i] *= sb;
+  }
+}
+
+// rescale_messages (beliefpropagationcache.jl:121-139), one warp per edge.
+__global__ void rescale_messages_kernel(int ne, const int* dchi, const long long* msg_off, double* msgs) {
+  const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (e >= ne) return;
+  const int c2 = dchi[2 * e] * dchi[2 * e];
+  double* m1 = msgs + msg_off[2 * e];
+  double* m2 = msgs + msg_off[2 * e + 1];
+  double a0 = lane < c2 ? m1[lane] : 0.0, a1 = lane + 32 < c2 ? m1[lane + 32] : 0.0;
+  double b0 = lane < c2 ? m2[lane] : 0.0, b1 = lane + 32 < c2 ? m2[lane + 32] : 0.0;
+  const double na = sqrt(warp_sum(a0 * a0 + a1 * a1));
+  const double nb = sqrt(warp_sum(b0 * b0 + b1 * b1));
+  a0 /= na; a1 /= na; b0 /= nb; b1 /= nb;
+  double n = warp_sum(a0 * b0 + a1 * b1);
+  const double s = n > 0.0 ? 1.0 : (n < 0.0 ? -1.0 : 0.0);
+  a0 *= s; a1 *= s;
+  n *= s;
+  const double sf = 1.0 / sqrt(n);
+  if (lane < c2) { m1[lane] = sf * a0; m2[lane] = sf * b0; }
+  if (lane + 32 < c2) { m1[lane + 32] = sf * a1; m2[lane + 32] = sf * b1; }
+}
+
+__global__ void edge_scalars_kernel(int ne, const int* dchi, const long long* msg_off, const double* msgs, double* out) {
+  const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (e >= ne) return;
+  const int c2 = dchi[2 * e] * dchi[2 * e];
+  const double* m1 = msgs + msg_off[2 * e];
+  const double* m2 = msgs + msg_off[2 * e + 1];
+  double s = 0.0;
+  for (int i = lane; i < c2; i += 32) s += m1[i] * m2[i];
+  s = warp_sum(s);
+  if (lane == 0) out[e] = s;
+}
+
+// logscalar per network: sum_v log Z_v - sum_e log z_e in FP64, negative
+// terms promoted to complex (log|x| + i*pi), -Inf on a zero edge scalar.
+__global__ void logscalar_kernel(const int* net_v_ptr, const int* net_v, const int* net_e_ptr, const int* net_e,
+                                 const long long* rdm_off, const double* rdm, const int* dsite, const double* edge_sc,
+                                 double* re, double* im) {
+  const int net = blockIdx.x;
+  double lre = 0.0, neg = 0.0, eneg = 0.0, ere = 0.0, zero_e = 0.0;
+  for (int i = net_v_ptr[net] + threadIdx.x; i < net_v_ptr[net + 1]; i += blockDim.x) {
+    const int v = net_v[i];
+    const int d = dsite[v];
+    double z = 0.0;
+    for (int s = 0; s < d; ++s) z += rdm[rdm_off[v] + s + d * s];
+    lre += log(fabs(z));
+    neg += z < 0.0 ? 1.0 : 0.0;
+  }
+  for (int i = net_e_ptr[net] + threadIdx.x; i < net_e_ptr[net + 1]; i += blockDim.x) {
+    const double z = edge_sc[net_e[i]];
+    ere += log(fabs(z));
+    eneg += z < 0.0 ? 1.0 : 0.0;
+    zero_e += z == 0.0 ? 1.0 : 0.0;
+  }
+  __shared__ double red[5][32];
+  double vals[5] = {lre, neg, ere, eneg, zero_e};
+  for (int q = 0; q < 5; ++q) {
+    const double t = warp_sum(vals[q]);
+    if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < 5; ++q) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[q][w];
+      vals[q] = t;
+    }
+    const double pi = 3.14159265358979323846;
+    if (vals[4] > 0.0) {
+      re[net] = -INFINITY;
+      im[net] = 0.0;
+    } else {
+      re[net] = vals[0] - vals[2];
+      im[net] = pi * (vals[1] - vals[3]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+
+template <typename T>
+void launch_bp_vertices(const WorkList& wl, const VDesc* vd, const T* fac, const T* bra, const T* msg_in, T* msg_out,
+                        const long long* msg_off, double* diffs, const int* converged, int normalize, int want_diff,
+                        cudaStream_t s) {
+  if (wl.count == 0) return;
+  const int nbuf = wl.maxdeg <= 4 ? 3 : kNumBufs;
+  if (wl.team == 32) {
+    const size_t sm = 4 * team_smem_bytes<T>(wl.ncap, nbuf, bra != nullptr, 32);
+    auto kern = bp_vertex_kernel<T, 32>;
+    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const int blocks = (wl.count + 3) / 4;
+    kern<<<blocks, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
+                                 normalize, want_diff, wl.ncap, nbuf);
+  } else {
+    const size_t sm = team_smem_bytes<T>(wl.ncap, nbuf, bra != nullptr, 256);
+    auto kern = bp_vertex_kernel<T, 256>;
+    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    kern<<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
+                                   normalize, want_diff, wl.ncap, nbuf);
+  }
+  GBTN_CUDA(cudaGetLastError());
+}
+
+template void launch_bp_vertices<double>(const WorkList&, const VDesc*, const double*, const double*, const double*,
+                                         double*, const long long*, double*, const int*, int, int, cudaStream_t);
+template void launch_bp_vertices<float>(const WorkList&, const VDesc*, const float*, const float*, const float*, float*,
+                                        const long long*, double*, const int*, int, int, cudaStream_t);
+
+template <typename T>
+void launch_bp_sequential(int n_networks, const VDesc* vd, const int2* seq, const int* seq_ptr, const T* fac,
+                          const T* bra, T* msgs, const long long* msg_off, int maxiter, double tol, int normalize,
+                          int* iters, double* mean_diff, int ncap, int maxdeg, cudaStream_t s) {
+  (void)maxdeg;
+  const size_t sm = team_smem_bytes<T>(ncap, 3, bra != nullptr, 256);
+  auto kern = bp_sequential_kernel<T>;
+  GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  kern<<<n_networks, 256, sm, s>>>(vd, seq, seq_ptr, fac, bra, msgs, msg_off, maxiter, tol, normalize, iters, mean_diff,
+                                   ncap);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+template void launch_bp_sequential<double>(int, const VDesc*, const int2*, const int*, const double*, const double*,
+                                           double*, const long long*, int, double, int, int*, double*, int, int,
+                                           cudaStream_t);
+template void launch_bp_sequential<float>(int, const VDesc*, const int2*, const int*, const float*, const float*, float*,
+                                          const long long*, int, double, int, int*, double*, int, int, cudaStream_t);
+
+void launch_reduce_diffs(int n_networks, const int* net_de_ptr, const int* net_de, const double* diffs, double tol,
+                         int* converged, int* iters, double* mean_diff, cudaStream_t s) {
+  reduce_diffs_kernel<<<n_networks, 256, 0, s>>>(net_de_ptr, net_de, diffs, tol, converged, iters, mean_diff);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_updated_message(const VDesc* vd, int v, int leg, const double* fac, const double* bra, const double* msgs,
+                            const long long* msg_off, double* out, int ncap, cudaStream_t s) {
+  const size_t sm = team_smem_bytes<double>(ncap, 3, bra != nullptr, 256);
+  GBTN_CUDA(cudaFuncSetAttribute(updated_message_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  updated_message_kernel<<<1, 256, sm, s>>>(vd, v, leg, fac, bra, msgs, msg_off, out, ncap);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_vertex_rdms(const WorkList& wl, const VDesc* vd, const double* fac, const double* bra, const double* msgs,
+                        const long long* msg_off, const long long* rdm_off, double* rdm, cudaStream_t s) {
+  if (wl.count == 0) return;
+  if (wl.team == 32) {
+    const size_t sm = 4 * team_smem_bytes<double>(wl.ncap, 3, bra != nullptr, 32);
+    GBTN_CUDA(cudaFuncSetAttribute(vertex_rdm_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    vertex_rdm_kernel<32><<<(wl.count + 3) / 4, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msgs, msg_off,
+                                                              rdm_off, rdm, wl.ncap);
+  } else {
+    const size_t sm = team_smem_bytes<double>(wl.ncap, 3, bra != nullptr, 256);
+    GBTN_CUDA(cudaFuncSetAttribute(vertex_rdm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    vertex_rdm_kernel<256><<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msgs, msg_off, rdm_off,
+                                                      rdm, wl.ncap);
+  }
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_edge_halves(const int* jobs, int njobs, int ncap, int maxdeg, const VDesc* vd, const double* fac,
+                        const double* bra, const double* msgs, const long long* msg_off, double* halves,
+                        const long long* half_off, cudaStream_t s) {
+  (void)maxdeg;
+  if (njobs == 0) return;
+  const size_t sm = team_smem_bytes<double>(ncap, 3, bra != nullptr, 256);
+  GBTN_CUDA(cudaFuncSetAttribute(edge_half_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  edge_half_kernel<<<njobs, 256, sm, s>>>(reinterpret_cast<const int2*>(jobs), njobs, vd, fac, bra, msgs, msg_off,
+                                          halves, half_off, ncap);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+static int grid_for(long long n) {
+  long long b = (n + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  return (int)(b < 1 ? 1 : b);
+}
+
+void launch_convert_f64_to_f32(const double* a, float* b, long long n, cudaStream_t s) {
+  convert_kernel_f64_f32<<<grid_for(n), 256, 0, s>>>(a, b, n);
+  GBTN_CUDA(cudaGetLastError());
+}
+void launch_convert_f32_to_f64(const float* a, double* b, long long n, cudaStream_t s) {
+  convert_kernel_f32_f64<<<grid_for(n), 256, 0, s>>>(a, b, n);
+  GBTN_CUDA(cudaGetLastError());
+}
+void launch_convert_f64_to_bf16(const double* a, __nv_bfloat16* b, long long n, cudaStream_t s) {
+  convert_kernel_f64_bf16<<<grid_for(n), 256, 0, s>>>(a, b, n);
+  GBTN_CUDA(cudaGetLastError());
+}
+void launch_fill_messages(int ndir, const int* dchi, const long long* msg_off, double* msgs, int kind, cudaStream_t s) {
+  if (ndir == 0) return;
+  fill_messages_kernel<<<ndir, 64, 0, s>>>(ndir, dchi, msg_off, msgs, kind);
+  GBTN_CUDA(cudaGetLastError());
+}
+void launch_scale_vertices(int nv, const VDesc* vd, double* fac, double* bra, const double* scale, cudaStream_t s) {
+  if (nv == 0) return;
+  scale_vertices_kernel<<<nv, 256, 0, s>>>(nv, vd, fac, bra, scale);
+  GBTN_CUDA(cudaGetLastError());
+}
+void launch_rescale_messages(int ne, const int* dchi, const long long* msg_off, double* msgs, cudaStream_t s) {
+  if (ne == 0) return;
+  rescale_messages_kernel<<<(ne + 7) / 8, 256, 0, s>>>(ne, dchi, msg_off, msgs);
+  GBTN_CUDA(cudaGetLastError());
+}
+void launch_edge_scalars(int ne, const int* dchi, const long long* msg_off, const double* msgs, double* out,
+                         cudaStream_t s) {
+  if (ne == 0) return;
+  edge_scalars_kernel<<<(ne + 7) / 8, 256, 0, s>>>(ne, dchi, msg_off, msgs, out);
+  GBTN_CUDA(cudaGetLastError());
+}
+void launch_logscalar(int n_networks, const int* net_v_ptr, const int* net_v, const int* net_e_ptr, const int* net_e,
+                      const long long* rdm_off, const double* rdm, const int* dsite, const double* edge_sc, double* re,
+                      double* im, cudaStream_t s) {
+  logscalar_kernel<<<n_networks, 256, 0, s>>>(net_v_ptr, net_v, net_e_ptr, net_e, rdm_off, rdm, dsite, edge_sc, re, im);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+}  // namespace gbtn

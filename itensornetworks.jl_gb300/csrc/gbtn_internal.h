@@ -1,0 +1,123 @@
+// Internal declarations shared by the C-ABI layer and the kernels of libgbtn.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/gbtn.h"
+
+namespace gbtn {
+
+// Limits of the compiled kernels.
+constexpr int kMaxDeg = 8;        // links per vertex (site index excluded)
+constexpr int kMaxChi = 8;        // bond dimension per link
+constexpr int kMaxSite = 8;       // physical dimension
+constexpr int kMaxOps = 48;       // schedule length per degree
+constexpr int kNumBufs = 4;       // shared-memory tensor buffers (0 = site tensor)
+
+// Per-vertex descriptor, read by every message / environment kernel.
+struct __align__(16) VDesc {
+  long long a_off;          // element offset of the vertex tensor
+  int n;                    // d * prod(chi)
+  int d;                    // site dimension
+  int k;                    // number of links
+  int net;                  // network id
+  int chi[kMaxDeg];         // bond dim of leg p
+  int st[kMaxDeg];          // element stride of leg p (site stride is 1)
+  int in_de[kMaxDeg];       // directed edge entering v on leg p
+  int out_de[kMaxDeg];      // directed edge leaving v on leg p
+};
+
+// One step of a vertex schedule: ABSORB src->dst on leg, or CLOSE src on leg.
+struct SchedOp {
+  int8_t type;  // 0 absorb, 1 close
+  int8_t src;
+  int8_t dst;
+  int8_t leg;
+};
+
+struct DeviceSched {
+  SchedOp ops[kMaxDeg + 1][kMaxOps];
+  int len[kMaxDeg + 1];
+  int nbuf[kMaxDeg + 1];
+};
+
+// Build, for every degree, the shared-prefix schedule that produces all
+// outgoing messages of a vertex (host side).
+DeviceSched build_schedules();
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct InvalidArg : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct Unsupported : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+#define GBTN_CUDA(call)                                                             \
+  do {                                                                              \
+    cudaError_t err__ = (call);                                                     \
+    if (err__ != cudaSuccess)                                                       \
+      throw ::gbtn::CudaError(std::string(#call) + ": " + cudaGetErrorString(err__)); \
+  } while (0)
+
+// Launch parameters of a batch of vertices processed by one message kernel.
+struct WorkList {
+  int* d_vertices = nullptr;  // device list of vertex ids
+  int count = 0;
+  int ncap = 0;               // largest n in the list
+  int maxdeg = 0;
+  int team = 32;              // threads per vertex (32 or 256)
+};
+
+// Kernel launchers (bp_kernels.cu).  T = double or float.
+template <typename T>
+void launch_bp_vertices(const WorkList& wl, const VDesc* vd, const T* fac, const T* bra,
+                        const T* msg_in, T* msg_out, const long long* msg_off, double* diffs,
+                        const int* converged, int normalize, int want_diff, cudaStream_t s);
+
+template <typename T>
+void launch_bp_sequential(int n_networks, const VDesc* vd, const int2* seq, const int* seq_ptr,
+                          const T* fac, const T* bra, T* msgs, const long long* msg_off,
+                          int maxiter, double tol, int normalize, int* iters, double* mean_diff,
+                          int ncap, int maxdeg, cudaStream_t s);
+
+void launch_reduce_diffs(int n_networks, const int* net_de_ptr, const int* net_de, const double* diffs,
+                         double tol, int* converged, int* iters, double* mean_diff, cudaStream_t s);
+
+void launch_updated_message(const VDesc* vd, int v, int leg, const double* fac, const double* bra,
+                            const double* msgs, const long long* msg_off, double* out, int ncap,
+                            cudaStream_t s);
+
+void launch_vertex_rdms(const WorkList& wl, const VDesc* vd, const double* fac, const double* bra,
+                        const double* msgs, const long long* msg_off, const long long* rdm_off,
+                        double* rdm, cudaStream_t s);
+
+void launch_edge_halves(const int* jobs /*pairs (v, leg)*/, int njobs, int ncap, int maxdeg,
+                        const VDesc* vd, const double* fac, const double* bra, const double* msgs,
+                        const long long* msg_off, double* halves /* per job d*d*chi*chi */,
+                        const long long* half_off, cudaStream_t s);
+
+void launch_convert_f64_to_f32(const double* a, float* b, long long n, cudaStream_t s);
+void launch_convert_f32_to_f64(const float* a, double* b, long long n, cudaStream_t s);
+void launch_convert_f64_to_bf16(const double* a, __nv_bfloat16* b, long long n, cudaStream_t s);
+void launch_fill_messages(int ndir, const int* dchi, const long long* msg_off, double* msgs, int kind,
+                          cudaStream_t s);
+void launch_scale_vertices(int nv, const VDesc* vd, double* fac, double* bra, const double* scale,
+                           cudaStream_t s);
+void launch_rescale_messages(int ne, const int* dchi, const long long* msg_off, double* msgs,
+                             cudaStream_t s);
+void launch_edge_scalars(int ne, const int* dchi, const long long* msg_off, const double* msgs,
+                         double* out, cudaStream_t s);
+void launch_logscalar(int n_networks, const int* net_v_ptr, const int* net_v, const int* net_e_ptr,
+                      const int* net_e, const long long* rdm_off, const double* rdm, const int* dsite,
+                      const double* edge_sc, double* re, double* im, cudaStream_t s);
+
+}  // namespace gbtn

@@ -1,0 +1,18 @@
+"""GB300-native belief propagation for tensor networks (host package).
+
+Python mirror of ITensorNetworks.jl's BP interface over the C ABI of
+libgbtn.so (include/gbtn.h).  Every numerical step runs on the GPU."""
+from . import _lib
+from ._lib import Context, GBTNError, InvalidArgument, LibraryNotBuilt, Unsupported, default_context
+from .cache import (BeliefPropagationCache, environment, expect, initialize_cache, inner, loginner, logscalar,
+                    message_diff, norm, norm_sqr, normalize, rescale, scalar, update, updated_message)
+from .network import (TensorNetwork, default_edge_sequence, disjoint_union, parallel_edge_sequence,
+                      random_network, random_tensors, square_lattice)
+
+__all__ = [
+    "BeliefPropagationCache", "Context", "GBTNError", "InvalidArgument", "LibraryNotBuilt", "TensorNetwork",
+    "Unsupported", "default_context", "default_edge_sequence", "disjoint_union", "environment", "expect",
+    "initialize_cache", "inner", "loginner", "logscalar", "message_diff", "norm", "norm_sqr", "normalize",
+    "parallel_edge_sequence", "random_network", "random_tensors", "rescale", "scalar", "square_lattice", "update",
+    "updated_message",
+]

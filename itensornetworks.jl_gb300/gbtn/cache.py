@@ -1,0 +1,333 @@
+"""BeliefPropagationCache on the GPU and the reference-facing entry points.
+
+Mirrors the interface of ITensorNetworks.jl's BP cache and its users:
+
+* ``BeliefPropagationCache`` / ``initialize_cache`` -- src/caches/beliefpropagationcache.jl:13-35,
+  src/initialize_cache.jl:14-28 (identity messages on loopy graphs)
+* ``update(bpc; maxiter, tol, edge_sequence, ...)`` -- abstractbeliefpropagationcache.jl:313-337
+* ``updated_message`` / ``message_diff`` -- :225-239, :32-36
+* ``environment`` -- beliefpropagationcache.jl:100-105
+* ``vertex_scalars`` / ``edge_scalars`` / ``logscalar`` / ``scalar`` -- :83-97, :397-412
+* ``rescale_messages`` / ``rescale_partitions`` / ``rescale`` -- beliefpropagationcache.jl:121-139,
+  abstractbeliefpropagationcache.jl:349-395
+* ``expect`` -- src/expect.jl:21-109; ``inner``/``loginner``/``norm_sqr``/``norm`` -- src/inner.jl;
+  ``logscalar``/``scalar`` on networks -- src/contract.jl:41-62; ``normalize``/``rescale`` -- src/normalize.jl.
+
+All arithmetic runs in libgbtn on the GPU; this module only moves arrays and
+keeps the bookkeeping.  The cache is updated in place and returned, where the
+reference returns an updated copy."""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, dptr, iptr
+from .network import TensorNetwork, default_edge_sequence, parallel_edge_sequence
+
+
+class BeliefPropagationCache:
+    def __init__(self, tn: TensorNetwork, messages=None, bra=None, ctx=None):
+        if tn.tensors is None:
+            raise ValueError("the network has no tensors")
+        self.tn = tn
+        self.ctx = ctx or _lib.default_context()
+        self.lib = self.ctx.lib
+        self.separate_bra = bra is not None
+        desc, keep = tn.graph_desc(separate_bra=self.separate_bra)
+        h = C.c_void_p()
+        check(self.ctx.handle, self.lib.gbtn_plan_create(self.ctx.handle, C.byref(desc), C.byref(h)))
+        self.handle = h
+        nf, nm = C.c_int64(), C.c_int64()
+        check(self.ctx.handle, self.lib.gbtn_plan_sizes(h, C.byref(nf), C.byref(nm)))
+        self.n_factor, self.n_message = nf.value, nm.value
+        self.set_factors(tn.tensors, bra)
+        if messages is not None:
+            self.set_messages(messages)
+
+    # -- storage ---------------------------------------------------------------
+    def _c(self, code):
+        check(self.ctx.handle, code)
+
+    def set_factors(self, ket, bra=None):
+        k = self.tn.flat(ket)
+        if self.separate_bra:
+            b = self.tn.flat(bra)
+            self._c(self.lib.gbtn_set_factors(self.handle, k.ctypes.data, b.ctypes.data, _lib.HOST))
+        else:
+            self._c(self.lib.gbtn_set_factors(self.handle, k.ctypes.data, None, _lib.HOST))
+        self.tn.tensors = [np.asarray(t, dtype=np.float64) for t in ket]
+
+    def factors(self):
+        out = np.empty(self.n_factor)
+        self._c(self.lib.gbtn_get_factors(self.handle, out.ctypes.data, _lib.HOST))
+        return self.tn.unflat(out)
+
+    def messages(self):
+        out = np.empty(max(self.n_message, 1))
+        self._c(self.lib.gbtn_get_messages(self.handle, out.ctypes.data, _lib.HOST))
+        return self.tn.unflat_messages(out)
+
+    def message(self, de):
+        return self.messages()[de]
+
+    def set_messages(self, msgs):
+        flat = self.tn.flat_messages(msgs) if isinstance(msgs, (list, tuple)) else np.ascontiguousarray(msgs, dtype=np.float64)
+        self._c(self.lib.gbtn_set_messages(self.handle, flat.ctypes.data, _lib.HOST))
+
+    def init_messages(self, kind="identity"):
+        self._c(self.lib.gbtn_init_messages(self.handle, _lib.INIT[kind]))
+
+    # -- message passing -------------------------------------------------------
+    def default_maxiter(self):
+        """1 on trees, none on loopy graphs (abstractbeliefpropagationcache.jl:38-41)."""
+        return 1 if self.tn.is_tree() else None
+
+    def update(self, maxiter=None, tol=None, schedule="sequential", edge_sequence=None, precision="f64",
+               normalize=True, verbose=False, **mixed):
+        """Run BP sweeps; returns the cache.  ``schedule``: "sequential" (the
+        reference default, forest-cover order unless ``edge_sequence`` is
+        given), "parallel" (Jacobi) or "colored" (colour-class Gauss-Seidel)."""
+        if maxiter is None:
+            maxiter = self.default_maxiter()
+        if maxiter is None:
+            raise _lib.InvalidArgument(1, "You need to specify a number of iterations for BP!")
+        o = _lib.BPOpts()
+        o.schedule = _lib.SCHED[schedule]
+        o.precision = _lib.PRECISION[precision]
+        o.maxiter = int(maxiter)
+        o.normalize = 1 if normalize else 0
+        o.tol = -1.0 if tol is None else float(tol)
+        seq = None
+        if schedule == "sequential":
+            seq = np.ascontiguousarray(default_edge_sequence(self.tn) if edge_sequence is None else edge_sequence,
+                                       dtype=np.int32)
+            o.edge_sequence = iptr(seq)
+            o.edge_sequence_len = len(seq)
+        else:
+            o.edge_sequence = C.cast(None, C.POINTER(C.c_int32))
+            o.edge_sequence_len = 0
+        o.tol_bf16 = float(mixed.get("tol_bf16", 0.0))
+        o.tol_f32 = float(mixed.get("tol_f32", 0.0))
+        o.maxiter_bf16 = int(mixed.get("maxiter_bf16", 0))
+        o.maxiter_f32 = int(mixed.get("maxiter_f32", 0))
+        o.refine_f64 = int(mixed.get("refine_f64", 0))
+        it = np.zeros(self.tn.n_networks, dtype=np.int32)
+        md = np.zeros(self.tn.n_networks)
+        self._c(self.lib.gbtn_bp_run(self.handle, C.byref(o), iptr(it), dptr(md)))
+        self.iterations, self.mean_diff = it, md
+        if verbose:
+            for n in range(self.tn.n_networks):
+                if tol is not None and md[n] <= tol:
+                    print(f"BP converged to desired precision after {it[n]} iterations.")
+        return self
+
+    def updated_message(self, de):
+        c = self.tn.edge_dims[de // 2]
+        out = np.empty(c * c)
+        self._c(self.lib.gbtn_updated_message(self.handle, int(de), dptr(out)))
+        return out.reshape((c, c), order="F")
+
+    # -- environments and scalars ---------------------------------------------
+    def environment(self, verts):
+        """Incoming messages into the partitions of ``verts`` (directed edge id,
+        message) and the vertex tensors (beliefpropagationcache.jl:100-105)."""
+        vs = set(verts)
+        msgs = self.messages()
+        incoming = []
+        for v in verts:
+            for e in self.tn.legs[v]:
+                w = self.tn.other(v, e)
+                if w in vs:
+                    continue
+                de = self.tn.directed(e, w)
+                incoming.append((de, msgs[de]))
+        return incoming, [self.tn.tensors[v] for v in verts]
+
+    def vertex_rdms(self):
+        n = sum(d * d for d in self.tn.site_dims)
+        out = np.empty(n)
+        self._c(self.lib.gbtn_vertex_rdms(self.handle, dptr(out)))
+        res, off = [], 0
+        for d in self.tn.site_dims:
+            res.append(out[off:off + d * d].reshape((d, d), order="F"))
+            off += d * d
+        return res
+
+    def edge_rdms(self, edges=None):
+        edges = list(range(self.tn.ne)) if edges is None else list(edges)
+        if not edges:
+            return []
+        es = np.ascontiguousarray(edges, dtype=np.int32)
+        Ds = [self.tn.site_dims[self.tn.edges[e][0]] * self.tn.site_dims[self.tn.edges[e][1]] for e in edges]
+        out = np.empty(sum(D * D for D in Ds))
+        self._c(self.lib.gbtn_edge_rdms(self.handle, iptr(es), len(edges), dptr(out)))
+        res, off = [], 0
+        for D in Ds:
+            res.append(out[off:off + D * D].reshape((D, D), order="F"))
+            off += D * D
+        return res
+
+    def vertex_scalars(self):
+        out = np.empty(self.tn.nv)
+        self._c(self.lib.gbtn_vertex_scalars(self.handle, dptr(out)))
+        return out
+
+    def edge_scalars(self):
+        out = np.empty(max(self.tn.ne, 1))
+        self._c(self.lib.gbtn_edge_scalars(self.handle, dptr(out)))
+        return out[:self.tn.ne]
+
+    def logscalar(self):
+        """Per network log of the BP estimate (a Python complex when negative
+        terms appear, -inf when an edge scalar is zero)."""
+        re = np.empty(self.tn.n_networks)
+        im = np.empty(self.tn.n_networks)
+        self._c(self.lib.gbtn_logscalar(self.handle, dptr(re), dptr(im)))
+        vals = [complex(r, i) if i != 0.0 else float(r) for r, i in zip(re, im)]
+        return vals[0] if self.tn.n_networks == 1 else vals
+
+    def scalar(self):
+        ls = self.logscalar()
+        f = (lambda x: complex(np.exp(x)) if isinstance(x, complex) else math.exp(x))
+        return f(ls) if not isinstance(ls, list) else [f(x) for x in ls]
+
+    def expect(self, op, per_vertex=False):
+        out = np.empty(self.tn.nv)
+        if per_vertex:
+            ops = np.ascontiguousarray(np.concatenate([np.asarray(o, float).reshape(-1, order="F") for o in op]))
+        else:
+            ops = np.ascontiguousarray(np.asarray(op, float).reshape(-1, order="F"))
+        self._c(self.lib.gbtn_expect1(self.handle, dptr(ops), 1 if per_vertex else 0, dptr(out)))
+        return out
+
+    def expect2(self, op2, edges=None):
+        edges = list(range(self.tn.ne)) if edges is None else list(edges)
+        es = np.ascontiguousarray(edges, dtype=np.int32)
+        op = np.ascontiguousarray(np.asarray(op2, float).reshape(-1, order="F"))
+        out = np.empty(len(edges))
+        self._c(self.lib.gbtn_expect2(self.handle, iptr(es), len(edges), dptr(op), dptr(out)))
+        return out
+
+    # -- rescaling -------------------------------------------------------------
+    def rescale_messages(self):
+        self._c(self.lib.gbtn_rescale_messages(self.handle))
+        return self
+
+    def rescale_partitions(self):
+        self._c(self.lib.gbtn_rescale_partitions(self.handle))
+        self.tn.tensors = self.factors()
+        return self
+
+    def rescale(self):
+        return self.rescale_messages().rescale_partitions()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.gbtn_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# -----------------------------------------------------------------------------
+# Module-level functions with the reference's names
+# -----------------------------------------------------------------------------
+
+def initialize_cache(tn, messages=None, bra=None, ctx=None):
+    """``initialize_cache(Algorithm"bp", QuadraticFormNetwork(tn))``: identity
+    messages (trees included; one sweep overwrites them there)."""
+    return BeliefPropagationCache(tn, messages=messages, bra=bra, ctx=ctx)
+
+
+def update(bpc, **kwargs):
+    return bpc.update(**kwargs)
+
+
+def updated_message(bpc, de):
+    return bpc.updated_message(de)
+
+
+def message_diff(a, b):
+    """1 - |<a/|a|, b/|b|>|^2 (host-side helper on two message matrices)."""
+    a = np.asarray(a, float)
+    b = np.asarray(b, float)
+    return 1.0 - float(np.vdot(a / np.linalg.norm(a), b / np.linalg.norm(b))) ** 2
+
+
+def _cache_for(tn, cache, update_cache, cache_update_kwargs, bra=None):
+    if cache is None:
+        cache = initialize_cache(tn, bra=bra)
+        update_cache = True if update_cache is None else update_cache
+    elif update_cache is None:
+        update_cache = False
+    if update_cache:
+        cache.update(**(cache_update_kwargs or {}))
+    return cache
+
+
+def expect(psi, op, vertices=None, alg="bp", cache=None, update_cache=None, cache_update_kwargs=None):
+    """<psi|O_v|psi>/<psi|psi> on every vertex (expect.jl:58-109); ``op`` is a
+    d x d matrix O[s', s].  Returns a numpy array (or the subset ``vertices``)."""
+    if alg != "bp":
+        raise ValueError("only alg='bp' runs on the GPU")
+    cache = _cache_for(psi, cache, update_cache, cache_update_kwargs)
+    out = cache.expect(op)
+    return out if vertices is None else out[list(vertices)]
+
+
+def environment(bpc, verts):
+    return bpc.environment(verts)
+
+
+def logscalar(tn, alg="bp", cache=None, update_cache=None, cache_update_kwargs=None, bra=None):
+    """logscalar(alg, tn; cache!, ...) (contract.jl:41-58) on <bra|tn> (bra =
+    conj(tn) when not given)."""
+    if alg != "bp":
+        raise ValueError("only alg='bp' runs on the GPU")
+    return _cache_for(tn, cache, update_cache, cache_update_kwargs, bra).logscalar()
+
+
+def scalar(tn, alg="bp", **kw):
+    ls = logscalar(tn, alg=alg, **kw)
+    return complex(np.exp(ls)) if isinstance(ls, complex) else math.exp(ls)
+
+
+def loginner(phi, psi, alg="bp", **kw):
+    """log <phi|psi> by BP on the two-layer network (inner.jl:93-149)."""
+    return logscalar(psi, alg=alg, bra=phi.tensors, **kw)
+
+
+def inner(phi, psi, alg="bp", **kw):
+    """<phi|psi> by BP (inner.jl:151-160)."""
+    ls = loginner(phi, psi, alg=alg, **kw)
+    return complex(np.exp(ls)) if isinstance(ls, complex) else math.exp(ls)
+
+
+def norm_sqr(psi, alg="bp", **kw):
+    return scalar(psi, alg=alg, **kw)
+
+
+def norm(psi, alg="bp", **kw):
+    return math.sqrt(abs(float(np.real(norm_sqr(psi, alg=alg, **kw)))))
+
+
+def rescale(tn, alg="bp", cache=None, update_cache=None, cache_update_kwargs=None):
+    """rescale(alg, tn; cache!) (normalize.jl:23-31): every partition scalar 1."""
+    cache = _cache_for(tn, cache, update_cache, cache_update_kwargs)
+    cache.rescale()
+    out = tn.copy()
+    out.tensors = cache.factors()
+    return out
+
+
+def normalize(tn, alg="bp", cache=None, update_cache=None, cache_update_kwargs=None):
+    """normalize(alg="bp") (normalize.jl:63-80): rescale the messages, then the
+    ket/bra partitions, so the BP norm of the returned state is 1."""
+    return rescale(tn, alg=alg, cache=cache, update_cache=update_cache, cache_update_kwargs=cache_update_kwargs)

@@ -1,0 +1,92 @@
+"""Host-side logic of the gbtn package and the C-ABI library surface (CPU)."""
+import ctypes as C
+import subprocess
+
+import numpy as np
+import pytest
+
+import bp_oracle as O
+import gbtn
+from gbtn import _lib
+from gbtn.network import default_edge_sequence, disjoint_union, parallel_edge_sequence, square_lattice
+
+
+@pytest.mark.parametrize("L", [(1, 1), (2, 2), (4, 4), (5, 3), (16, 16)])
+def test_lattice_bookkeeping_matches_oracle(L):
+    tn = square_lattice(*L, chi=3)
+    g = O.square_lattice(*L, chi=3)
+    assert tn.edges == g.edges
+    assert tn.legs == g.legs
+    assert [tn.shape(v) for v in range(tn.nv)] == [g.shape(v) for v in range(g.nv)]
+
+
+@pytest.mark.parametrize("L", [(2, 2), (4, 4), (7, 5), (32, 32)])
+def test_edge_sequences_bit_exact(L):
+    tn = square_lattice(*L)
+    g = O.square_lattice(*L)
+    seq = default_edge_sequence(tn)
+    assert seq == O.default_edge_sequence(g)
+    assert sorted(seq) == list(range(2 * tn.ne))  # every directed edge once per sweep
+    assert parallel_edge_sequence(tn) == O.parallel_edge_sequence(g)
+
+
+def test_tree_sequence_is_collect_then_distribute():
+    g = O.random_tree(12, seed=2)
+    tn = gbtn.TensorNetwork(g.nv, g.edges, g.site_dims, g.edge_dims)
+    seq = default_edge_sequence(tn)
+    assert seq == O.default_edge_sequence(g)
+    half = len(seq) // 2
+    assert seq[half:] == [de ^ 1 for de in reversed(seq[:half])]
+
+
+def test_disjoint_union_offsets():
+    a = gbtn.random_network(square_lattice(2, 2, chi=2), 1)
+    b = gbtn.random_network(square_lattice(3, 2, chi=3), 2)
+    u = disjoint_union([a, b])
+    assert u.nv == 10 and u.ne == a.ne + b.ne and u.n_networks == 2
+    assert u.vertex_network == [0] * 4 + [1] * 6
+    assert u.edges[a.ne] == (b.edges[0][0] + 4, b.edges[0][1] + 4)
+    assert u.legs[4] == [e + a.ne for e in b.legs[0]]
+    np.testing.assert_array_equal(u.flat(), np.concatenate([a.flat(), b.flat()]))
+
+
+def test_graph_desc_arrays():
+    tn = square_lattice(3, 2, chi=2)
+    d, keep = tn.graph_desc()
+    assert d.nv == 6 and d.ne == tn.ne and d.separate_bra == 0
+    lp = np.ctypeslib.as_array(d.leg_ptr, shape=(7,))
+    assert list(lp) == [0] + list(np.cumsum([len(l) for l in tn.legs]))
+
+
+def test_flat_roundtrip():
+    tn = gbtn.random_network(square_lattice(3, 3, edge_dims=[2, 3, 1, 2, 3, 2, 1, 2, 3, 2, 2, 3]), 5)
+    np.testing.assert_array_equal(tn.flat(tn.unflat(tn.flat())), tn.flat())
+    msgs = O.identity_messages(O.square_lattice(3, 3, edge_dims=tn.edge_dims))
+    np.testing.assert_array_equal(tn.flat_messages(tn.unflat_messages(tn.flat_messages(msgs))), tn.flat_messages(msgs))
+
+
+def test_struct_layouts():
+    # GraphDesc: 2 ints, 6 pointers, 1 pointer, 2 ints (x86-64 / aarch64 LP64)
+    assert C.sizeof(_lib.GraphDesc) == 8 + 7 * 8 + 8
+    assert C.sizeof(_lib.BPOpts) == 16 + 8 + 8 + 8 + 8 + 8 + 16
+
+
+def test_library_builds_and_exports_every_declared_symbol(lib_built):
+    declared = _lib.declared_symbols()
+    assert "gbtn_bp_run" in declared and len(declared) >= 20
+    out = subprocess.run(["nm", "-D", "--defined-only", str(lib_built)], capture_output=True, text=True, check=True)
+    exported = {ln.split()[-1] for ln in out.stdout.splitlines() if " T " in ln}
+    missing = [s for s in declared if s not in exported]
+    assert not missing, missing
+    lib = _lib.load()
+    assert lib.gbtn_abi_version() == 1
+    assert set(_lib.SIGNATURES) == set(declared)
+
+
+def test_missing_maxiter_on_loopy_graph_raises_before_gpu():
+    class Fake(gbtn.BeliefPropagationCache):
+        def __init__(self, tn):
+            self.tn = tn
+    bpc = Fake(gbtn.random_network(square_lattice(3, 3), 1))
+    with pytest.raises(gbtn.InvalidArgument, match="number of iterations"):
+        bpc.update()
