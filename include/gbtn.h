@@ -175,6 +175,27 @@ int gbtn_rescale_messages(gbtn_plan* plan);
  * normalize.jl:77): every vertex scalar becomes 1. */
 int gbtn_rescale_partitions(gbtn_plan* plan);
 
+/* ---- allocation-free sweep ------------------------------------------------ */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they need a message update (a framework capturing its stream
+ * into a CUDA graph, or an application that gives the library a fixed memory
+ * budget): one FP64 parallel (Jacobi) sweep, msg_in -> msg_out, with the mean
+ * message diff over all directed edges written to *mean_diff.  Every pointer,
+ * including the arrays inside *dev_graph (the struct itself stays on the
+ * host), is DEVICE memory owned by the caller; the library allocates
+ * nothing and keeps its scratch in a fixed ~1.2 MiB device array.  The first
+ * call on a device sets that array up (make it before any stream capture);
+ * calls that overlap on the GPU share the array and race.  Asynchronous on
+ * `stream` (NULL = the legacy default stream).
+ * Returns GBTN_ERR_UNSUPPORTED when nv > GBTN_STATIC_MAX_VERTICES or
+ * 2*ne > GBTN_STATIC_MAX_DIRECTED_EDGES; a vertex beyond the kernel limits
+ * (degree > 8, chi > 8, d > 8, d*prod(chi) > 8192) is skipped on the device and
+ * makes *mean_diff NaN. */
+#define GBTN_STATIC_MAX_VERTICES 16384
+#define GBTN_STATIC_MAX_DIRECTED_EDGES 65536
+int gbtn_bp_sweep_static(int device, const gbtn_graph_desc* dev_graph, const double* factors,
+                         const double* msg_in, double* msg_out, double* mean_diff, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

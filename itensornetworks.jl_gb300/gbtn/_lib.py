@@ -113,6 +113,7 @@ SIGNATURES = {
     "gbtn_logscalar": (_I, [_P, _D, _D]),
     "gbtn_rescale_messages": (_I, [_P]),
     "gbtn_rescale_partitions": (_I, [_P]),
+    "gbtn_bp_sweep_static": (_I, [_I, C.POINTER(GraphDesc), _P, _P, _P, _P, _P]),
 }
 
 
