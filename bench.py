@@ -141,7 +141,7 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * BATCH * MSGS_PER_NET / val, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "bp_sweep_16x_peps32x32_d2_chi8", "batch": BATCH, "L": L, "chi": CHI, "d": D,
+            "config": {"workload": f"bp_sweep_{BATCH}x_peps32x32_d2_chi8", "batch": BATCH, "L": L, "chi": CHI, "d": D,
                        "schedule": "parallel", "l2": "inputs larger than L2"},
             "cpu_baseline": {"value": val, "unit": "msg-updates/s", "cores": cores, "kind": "port",
                              "sample": "per step: " + sample},
@@ -234,7 +234,7 @@ def run_ours(args):
             "metric": "bp_msg_updates_per_s", "value": value, "unit": "msg-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_f32, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "bp_sweep_16x_peps32x32_d2_chi8", "batch": BATCH, "L": L, "chi": CHI, "d": D,
+            "config": {"workload": f"bp_sweep_{BATCH}x_peps32x32_d2_chi8", "batch": BATCH, "L": L, "chi": CHI, "d": D,
                        "schedule": "parallel", "chosen_precision": "f32", "l2": "inputs larger than L2",
                        "parallelism": f"replicas{world}"},
             "fp64_path": {"value": world * msgs_step / (ms_f64 * 1e-3), "ms_per_step": ms_f64},
@@ -261,7 +261,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=BATCH, help="networks per step (default 16; smaller for profiling)")
     args = ap.parse_args()
+    globals()["BATCH"] = args.batch
     if args.impl == "reference":
         run_reference(args)
     else:
