@@ -85,6 +85,14 @@ struct gbtn_plan {
   // work lists: index 0 = all vertices, 1.. = colour classes; two size classes each
   std::vector<std::pair<WorkList, WorkList>> lists;
   std::vector<std::unique_ptr<DevBuf<int>>> list_store;
+  // tensor-core split of every list: eligible vertices (degree 4, d = 2,
+  // chi = 8, bra = ket) and the rest, which run the SIMT kernel
+  std::vector<WorkList> tc_lists;
+  std::vector<std::pair<WorkList, WorkList>> rest_lists;
+  std::vector<int> tc_slot_vertex;
+  DevBuf<int> d_vslot, d_tc_slot_vertex, d_err;
+  DevBuf<__nv_bfloat16> d_zimg;
+  bool zimg_valid = false;
   // sequential schedule storage
   DevBuf<int2> d_seq;
   DevBuf<int> d_seq_ptr;
@@ -114,6 +122,10 @@ void set_err(const gbtn_ctx* ctx, const std::string& m) {
   catch (const Unsupported& e) {                            \
     set_err(CTX, e.what());                                 \
     return GBTN_ERR_UNSUPPORTED;                            \
+  }                                                         \
+  catch (const Timeout& e) {                                \
+    set_err(CTX, e.what());                                 \
+    return GBTN_ERR_TIMEOUT;                                \
   }                                                         \
   catch (const CudaError& e) {                              \
     set_err(CTX, e.what());                                 \
@@ -221,9 +233,62 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
   }
 }
 
+// Raise the device-side error word (set by a bounded wait that gave up).
+void check_device_error(gbtn_plan* P) {
+  int e = 0;
+  GBTN_CUDA(cudaMemcpyAsync(&e, P->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, P->ctx->stream));
+  GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));
+  if (e != 0) {
+    GBTN_CUDA(cudaMemsetAsync(P->d_err.p, 0, sizeof(int), P->ctx->stream));
+    throw Timeout("tensor-core sweep: a bounded device wait gave up (TMA copy or MMA did not complete)");
+  }
+}
+
+void ensure_zimg(gbtn_plan* P) {
+  const int n = (int)P->tc_slot_vertex.size();
+  if (n == 0) return;
+  if (!P->d_zimg.p) P->d_zimg.alloc((size_t)n * 8192);
+  if (!P->zimg_valid) {
+    launch_build_zimg(P->d_tc_slot_vertex.p, n, P->d_vd.p, P->d_fac.p, P->d_zimg.p, P->ctx->stream);
+    P->zimg_valid = true;
+  }
+}
+
+// BF16 sweeps (parallel or coloured): tensor-core kernel on the eligible
+// vertices, FP32 SIMT kernel on the rest, FP32 messages.
+void run_sweeps_bf16(gbtn_plan* P, int schedule, int maxiter, double tol, int normalize, int& c32) {
+  cudaStream_t s = P->ctx->stream;
+  const bool want_diff = tol >= 0.0;
+  GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int) * P->nnet, s));
+  GBTN_CUDA(cudaMemsetAsync(P->d_iters.p, 0, sizeof(int) * P->nnet, s));
+  const int* conv = want_diff ? P->d_conv.p : nullptr;
+  const float* fac = P->d_fac32.p;
+  auto one = [&](size_t li, const float* in, float* out) {
+    const WorkList& tl = P->tc_lists[li];
+    launch_tc_vertices(tl.d_vertices, tl.count, P->d_vslot.p, P->d_vd.p, P->d_zimg.p, in, out, P->d_msg_off.p,
+                       P->d_diffs.p, conv, normalize, want_diff, P->d_err.p, s);
+    launch_bp_vertices<float>(P->rest_lists[li].first, P->d_vd.p, fac, nullptr, in, out, P->d_msg_off.p,
+                              P->d_diffs.p, conv, normalize, want_diff, s);
+    launch_bp_vertices<float>(P->rest_lists[li].second, P->d_vd.p, fac, nullptr, in, out, P->d_msg_off.p,
+                              P->d_diffs.p, conv, normalize, want_diff, s);
+  };
+  for (int it = 0; it < maxiter; ++it) {
+    if (schedule == GBTN_SCHED_PARALLEL) {
+      one(0, P->d_msg32[c32].p, P->d_msg32[c32 ^ 1].p);
+      c32 ^= 1;
+    } else {
+      for (size_t c = 1; c < P->tc_lists.size(); ++c) one(c, P->d_msg32[c32].p, P->d_msg32[c32].p);
+    }
+    if (want_diff)
+      launch_reduce_diffs(P->nnet, P->d_net_de_ptr.p, P->d_net_de.p, P->d_diffs.p, tol, P->d_conv.p, P->d_iters.p,
+                          P->d_mean.p, s);
+  }
+}
+
 void finish_iters(gbtn_plan* P, bool want_diff, int maxiter, int32_t* iters, double* mean_diff) {
   cudaStream_t s = P->ctx->stream;
   if (!iters && !mean_diff) return;
+  check_device_error(P);
   std::vector<int> it(P->nnet, maxiter);
   std::vector<double> md(P->nnet, NAN);
   if (want_diff) {
@@ -533,6 +598,31 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
       if (P->color[v] == c) vs.push_back(v);
     P->lists.push_back(split_list(P.get(), vs));
   }
+  // tensor-core vertices: one swizzled BF16 image slot each
+  std::vector<int> vslot(g->nv, -1);
+  if (!P->sep_bra)
+    for (int v = 0; v < g->nv; ++v)
+      if (tc_eligible(P->vd[v])) {
+        vslot[v] = (int)P->tc_slot_vertex.size();
+        P->tc_slot_vertex.push_back(v);
+      }
+  P->d_vslot.upload(vslot, s);
+  {
+    std::vector<int> sv = P->tc_slot_vertex;
+    if (sv.empty()) sv.push_back(0);
+    P->d_tc_slot_vertex.upload(sv, s);
+  }
+  P->d_err.alloc(1);
+  GBTN_CUDA(cudaMemsetAsync(P->d_err.p, 0, sizeof(int), s));
+  for (int li = 0; li <= ncol; ++li) {
+    std::vector<int> tcv, rest;
+    for (int v = 0; v < g->nv; ++v) {
+      if (li > 0 && P->color[v] != li - 1) continue;
+      (vslot[v] >= 0 ? tcv : rest).push_back(v);
+    }
+    P->tc_lists.push_back(make_list(P.get(), tcv, 128));
+    P->rest_lists.push_back(split_list(P.get(), rest));
+  }
   launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[0].p, GBTN_INIT_IDENTITY, s);
   GBTN_CUDA(cudaStreamSynchronize(s));
   *out = P.release();
@@ -561,6 +651,7 @@ int gbtn_set_factors(gbtn_plan* P, const double* ket, const double* bra, int mem
   copy_in(P, P->d_fac.p, ket, sizeof(double) * P->n_fac, mem);
   if (P->sep_bra) copy_in(P, P->d_bra.p, bra, sizeof(double) * P->n_fac, mem);
   P->fac32_valid = false;
+  P->zimg_valid = false;
   API_CATCH(C)
 }
 
@@ -610,7 +701,8 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     finish_iters(P, false, o->maxiter, iters, mean_diff);
     return GBTN_OK;
   }
-  if (o->precision == GBTN_BF16) throw Unsupported("BF16 sweeps need the tensor-core kernel (not in this build)");
+  if (o->precision == GBTN_BF16 && o->schedule == GBTN_SCHED_SEQUENTIAL)
+    throw Unsupported("BF16 sweeps run the parallel or coloured schedule");
   if (o->schedule == GBTN_SCHED_SEQUENTIAL) {
     require(o->edge_sequence && o->edge_sequence_len > 0, "SEQUENTIAL needs an edge sequence");
     std::vector<std::vector<int2>> per(P->nnet);
@@ -670,12 +762,26 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
                       P->sep_bra ? P->d_bra32.p : nullptr, c32);
     launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
     finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
-  } else {  // MIXED: FP32 phase then FP64 refinement
+  } else if (o->precision == GBTN_BF16) {
+    ensure_f32(P);
+    ensure_zimg(P);
+    int c32 = 0;
+    launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, s);
+    run_sweeps_bf16(P, o->schedule, o->maxiter, o->tol, o->normalize, c32);
+    launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
+    finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
+  } else {  // MIXED: BF16 tensor-core phase, FP32 phase, then FP64 refinement
     ensure_f32(P);
     int c32 = 0;
     const double tol32 = o->tol_f32 > 0 ? o->tol_f32 : 1e-13;
     const int it32 = o->maxiter_f32 > 0 ? o->maxiter_f32 : o->maxiter;
     launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, s);
+    if (o->schedule != GBTN_SCHED_SEQUENTIAL && !P->tc_slot_vertex.empty()) {
+      ensure_zimg(P);
+      const double tol16 = o->tol_bf16 > 0 ? o->tol_bf16 : 1e-6;
+      const int it16 = o->maxiter_bf16 > 0 ? o->maxiter_bf16 : o->maxiter;
+      run_sweeps_bf16(P, o->schedule, it16, tol16, o->normalize, c32);
+    }
     run_sweeps<float>(P, o->schedule, it32, tol32, o->normalize, P->d_msg32, P->d_fac32.p,
                       P->sep_bra ? P->d_bra32.p : nullptr, c32);
     launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
@@ -903,6 +1009,7 @@ int gbtn_rescale_partitions(gbtn_plan* P) {
   GBTN_CUDA(cudaGetLastError());
   launch_scale_vertices(P->nv, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_scale.p, s);
   P->fac32_valid = false;
+  P->zimg_valid = false;
   GBTN_CUDA(cudaStreamSynchronize(s));
   API_CATCH(C)
 }

@@ -60,6 +60,9 @@ struct InvalidArg : std::runtime_error {
 struct Unsupported : std::runtime_error {
   using std::runtime_error::runtime_error;
 };
+struct Timeout : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
 
 #define GBTN_CUDA(call)                                                             \
   do {                                                                              \
@@ -119,5 +122,13 @@ void launch_edge_scalars(int ne, const int* dchi, const long long* msg_off, cons
 void launch_logscalar(int n_networks, const int* net_v_ptr, const int* net_v, const int* net_e_ptr,
                       const int* net_e, const long long* rdm_off, const double* rdm, const int* dsite,
                       const double* edge_sc, double* re, double* im, cudaStream_t s);
+
+// BF16 tensor-core path (bp_tc.cu): degree-4 vertices, d = 2, chi = 8.
+bool tc_eligible(const VDesc& d);
+void launch_build_zimg(const int* slot_vertex, int nslot, const VDesc* vd, const double* fac, __nv_bfloat16* zimg,
+                       cudaStream_t s);
+void launch_tc_vertices(const int* work, int nwork, const int* vslot, const VDesc* vd, const __nv_bfloat16* zimg,
+                        const float* msg_in, float* msg_out, const long long* msg_off, double* diffs,
+                        const int* converged, int normalize, int want_diff, int* err, cudaStream_t s);
 
 }  // namespace gbtn
