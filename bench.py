@@ -3,8 +3,13 @@
 Workload (default): a batch of 16 independent 32x32 open PEPS, d=2, chi=8,
 i.i.d. N(0,1) site tensors (seeded), all-edges-at-once (Jacobi) sweeps.  One
 step = one sweep over the whole batch = 16 * 3968 directed-edge message
-updates.  The FP64 tensors of the batch take 1.07 GB and the FP32 copies
-537 MB, both larger than L2, so no L2 flush is needed between steps.
+updates.  The chosen path runs the contractions in BF16 on the tensor cores
+(FP32 accumulation, FP64 normalisation); the plain FP64 and the FP32 paths
+are measured beside it, and the mixed pipeline (BF16 -> FP32 -> FP64
+refinement) is timed to convergence against the plain FP64 path with its
+<Sz> error.  The BF16 tensor images of the batch take 236 MB, the FP32 copies
+486 MB and the FP64 tensors 972 MB -- all larger than L2 (129 MB), so no L2
+flush is needed between steps.
 
 Output: one JSON line (rank 0).  ``--impl reference`` times the CPU
 restatement of the reference's per-edge update (FP64, all host threads) on a
@@ -149,6 +154,11 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def tc_vertices_per_net(L=L):
+    """Vertices of the tensor-core class (interior, degree 4) per L x L lattice."""
+    return max(L - 2, 0) ** 2
+
+
 def run_ours(args):
     import ctypes as C
 
@@ -170,39 +180,83 @@ def run_ours(args):
     bpc = gbtn.BeliefPropagationCache(tn, ctx=ctx)
     lib = ctx.lib
 
-    def sweeps(n, precision):
+    def run(n, precision, tol=None, **mixed):
         o = _lib.BPOpts()
-        o.schedule, o.precision, o.maxiter, o.normalize, o.tol = 1, _lib.PRECISION[precision], n, 1, -1.0
+        o.schedule, o.precision, o.maxiter, o.normalize = 1, _lib.PRECISION[precision], n, 1
+        o.tol = -1.0 if tol is None else tol
         o.edge_sequence = C.cast(None, C.POINTER(C.c_int32))
-        _lib.check(ctx.handle, lib.gbtn_bp_run(bpc.handle, C.byref(o), None, None))
+        o.tol_bf16 = mixed.get("tol_bf16", 0.0)
+        o.tol_f32 = mixed.get("tol_f32", 0.0)
+        o.refine_f64 = mixed.get("refine_f64", 0)
+        if tol is None:
+            _lib.check(ctx.handle, lib.gbtn_bp_run(bpc.handle, C.byref(o), None, None))
+            return None
+        it = np.zeros(tn.n_networks, dtype=np.int32)
+        md = np.zeros(tn.n_networks)
+        _lib.check(ctx.handle, lib.gbtn_bp_run(bpc.handle, C.byref(o), _lib.iptr(it), _lib.dptr(md)))
+        return it
 
     def barrier():
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
 
+    def max_over_ranks(x):
+        if world > 1:
+            t = torch.tensor([x], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            x = float(t.item())
+        return x
+
     def timed(precision, steps, warmup):
-        sweeps(warmup, precision)
+        """ms per sweep: W untimed sweeps, then K sweeps between CUDA events."""
+        run(warmup, precision)
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        sweeps(steps, precision)
+        run(steps, precision)
         e1.record(stream)
         barrier()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms / steps
+        return max_over_ranks(e0.elapsed_time(e1) / steps)
 
     msgs_step = BATCH * MSGS_PER_NET
+    # 1. chosen path: BF16 tensor-core sweeps (clocks sampled during the timed region)
     with ClockSampler(local) as clk:
-        ms_f32 = timed("f32", args.steps, args.warmup)
+        ms_bf16 = timed("bf16", args.steps, args.warmup)
+    ms_f32 = timed("f32", args.steps, args.warmup)
     ms_f64 = timed("f64", max(2, args.steps // 2), 1)
 
-    # end to end through the public API: pinned host tensors -> device, one sweep,
-    # messages back to the host, every step
+    # 2. the dominant kernel's own duration, CUDA events around every launch
+    ctx.set_profiling(True)
+    run(args.steps, "bf16")
+    barrier()
+    tc_ms, tc_n = ctx.kernel_time(_lib.KCLASS_TENSOR_CORE)
+    simt_ms, simt_n = ctx.kernel_time(_lib.KCLASS_SIMT_F32)
+    ctx.set_profiling(False)
+
+    # 3. time to solution: plain FP64 vs the mixed pipeline, same start, same tol
+    sz_op = np.array([[0.5, 0.0], [0.0, -0.5]])
+
+    def solve(precision, **kw):
+        bpc.init_messages("identity")
+        barrier()
+        t0 = time.perf_counter()
+        it = run(args.solve_maxiter, precision, tol=args.solve_tol, **kw)
+        barrier()
+        return (time.perf_counter() - t0) * 1e3, it
+
+    fp64_ms, fp64_it = solve("f64")
+    sz64 = bpc.expect(sz_op)
+    mix_ms, mix_it = solve("mixed", refine_f64=2)
+    szmix = bpc.expect(sz_op)
+    per_net = []
+    for k in range(BATCH):
+        a = sz64[k * L * L:(k + 1) * L * L]
+        b = szmix[k * L * L:(k + 1) * L * L]
+        per_net.append(float(np.max(np.abs(b - a)) / np.max(np.abs(a))))
+
+    # 4. end to end through the public API: pinned host tensors -> device, one
+    #    BF16 sweep (tensor images rebuilt from the new tensors), all messages back
     n_fac, n_msg = bpc.n_factor, bpc.n_message
     host_fac = torch.from_numpy(tn.flat()).pin_memory()
     host_msg = torch.empty(n_msg, dtype=torch.float64).pin_memory()
@@ -210,7 +264,7 @@ def run_ours(args):
     def e2e_step():
         _lib.check(ctx.handle, lib.gbtn_set_factors(bpc.handle, C.c_void_p(host_fac.data_ptr()), None, _lib.HOST))
         bpc.init_messages("identity")
-        sweeps(1, "f32")
+        run(1, "bf16")
         _lib.check(ctx.handle, lib.gbtn_get_messages(bpc.handle, C.c_void_p(host_msg.data_ptr()), _lib.HOST))
 
     for _ in range(args.warmup):
@@ -220,34 +274,50 @@ def run_ours(args):
     for _ in range(args.steps):
         e2e_step()
     barrier()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
 
-    value = world * msgs_step / (ms_f32 * 1e-3)
-    fl = flops_per_sweep() * BATCH
-    byt = bytes_per_sweep(4) * BATCH
+    value = world * msgs_step / (ms_bf16 * 1e-3)
+    n_tc = BATCH * tc_vertices_per_net()
+    alg_flops_vertex = 4 * (2 * D * CHI ** 4 * 4 * CHI)  # k * F at k = 4
+    mma_flops_vertex = 2 * (2 * 128 * 64 * 64) + 2 * (2 * 128 * 128 * 64)
+    tc_launch_ms = tc_ms / max(tc_n, 1)
+    achieved = n_tc * alg_flops_vertex / (tc_launch_ms * 1e-3) / 1e12
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-    hbm = peaks.get("hbm_gbs", 6800.0)
-    achieved_gbs = byt / (ms_f32 * 1e-3) / 1e9
+    peak = peaks.get("bf16_tflops")
+    peak_src = "measured burst" if peak else "fallback"
+    peak = peak or 1900.0
+    traffic = None
+    tfile = ROOT / "profiles" / "tc_vertex_kernel_traffic.json"
+    if tfile.exists():
+        tj = json.loads(tfile.read_text())
+        traffic = tj["dram_bytes_per_vertex"] * n_tc
     if rank == 0:
         cpu_val, cores, sample = cpu_reference_rate(seconds=10.0)
         line = {
             "metric": "bp_msg_updates_per_s", "value": value, "unit": "msg-updates/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_f32, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_bf16, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
             "config": {"workload": f"bp_sweep_{BATCH}x_peps32x32_d2_chi8", "batch": BATCH, "L": L, "chi": CHI, "d": D,
-                       "schedule": "parallel", "chosen_precision": "f32", "l2": "inputs larger than L2",
-                       "parallelism": f"replicas{world}"},
-            "fp64_path": {"value": world * msgs_step / (ms_f64 * 1e-3), "ms_per_step": ms_f64},
-            "chosen_over_fp64": ms_f64 / ms_f32,
-            "algorithmic_tflops": fl / (ms_f32 * 1e-3) / 1e12,
-            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved_gbs / hbm, "traffic": None,
-                         "note": "FP32 SIMT sweep kernel; algorithmic bytes per sweep / measured time, of measured peak"},
+                       "schedule": "parallel (Jacobi)",
+                       "chosen_path": "bf16 tcgen05 contractions, fp32 accumulation, fp64 normalisation",
+                       "l2": "inputs larger than L2 (bf16 images 236 MB)", "parallelism": f"replicas{world}"},
+            "paths_ms_per_sweep": {"bf16_tensor_core": ms_bf16, "f32_simt": ms_f32, "f64_simt": ms_f64},
+            "chosen_over_fp64_per_sweep": ms_f64 / ms_bf16,
+            "time_to_solution": {
+                "tol": args.solve_tol, "fp64_ms": fp64_ms, "fp64_sweeps": int(np.max(fp64_it)),
+                "mixed_ms": mix_ms, "mixed_final_fp64_sweeps": int(np.max(mix_it)),
+                "speedup": fp64_ms / mix_ms, "mixed_max_rel_err_sz": max(per_net)},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "tc_vertex_kernel", "launch_ms": tc_launch_ms, "launches": tc_n,
+                         "units_per_launch": n_tc, "alg_flops_per_unit": alg_flops_vertex,
+                         "mma_tflops": n_tc * mma_flops_vertex / (tc_launch_ms * 1e-3) / 1e12,
+                         "note": f"algorithmic FP flops of the degree-4 vertices / event-timed kernel duration, of {peak_src} bf16 peak"},
             "cpu_baseline": {"value": cpu_val, "unit": "msg-updates/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": world * msgs_step / (e2e_ms * 1e-3), "unit": "msg-updates/s",
                     "h2d_bytes_per_step": n_fac * 8, "d2h_bytes_per_step": n_msg * 8},
-            "gpu_launches": args.steps * 2 + 2,
+            "gpu_launches": int(tc_n + simt_n + 2),
             "clocks": clk.summary(),
         }
         print(json.dumps(line))
@@ -262,6 +332,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH, help="networks per step (default 16; smaller for profiling)")
+    ap.add_argument("--solve-tol", type=float, default=1e-14, help="tol of the time-to-solution runs")
+    ap.add_argument("--solve-maxiter", type=int, default=300)
     args = ap.parse_args()
     globals()["BATCH"] = args.batch
     if args.impl == "reference":

@@ -93,7 +93,9 @@ typedef struct gbtn_bp_opts {
   const int32_t* edge_sequence;  /* SEQUENTIAL: directed edges, per sweep */
   int32_t edge_sequence_len;     /*   (one sequence shared by all networks is
                                       not allowed; give the full sequence) */
-  /* MIXED only: per-phase limits; zeros select the defaults. */
+  /* MIXED only: per-phase limits; zeros select the defaults.  The BF16 and
+     FP32 phases also stop at their noise floor: when a network's mean diff
+     has not dropped below 0.9x its best value for 5 sweeps. */
   double tol_bf16;               /* default 1e-6 */
   double tol_f32;                /* default 1e-13 */
   int32_t maxiter_bf16;          /* default maxiter */
@@ -112,6 +114,13 @@ const char* gbtn_last_error(const gbtn_ctx* ctx);
 int gbtn_ctx_set_stream(gbtn_ctx* ctx, void* cuda_stream);
 void* gbtn_ctx_get_stream(const gbtn_ctx* ctx);
 int gbtn_abi_version(void);
+/* Instrumentation (no counterpart in the reference): with profiling on, every
+ * message-kernel launch of the context is bracketed by CUDA events on the
+ * context's stream.  gbtn_ctx_kernel_time returns, and forgets, the summed
+ * device time and the launch count of one kernel class. */
+enum gbtn_kernel_class { GBTN_KCLASS_TENSOR_CORE = 0, GBTN_KCLASS_SIMT_F32 = 1, GBTN_KCLASS_SIMT_F64 = 2 };
+int gbtn_ctx_set_profiling(gbtn_ctx* ctx, int on);
+int gbtn_ctx_kernel_time(gbtn_ctx* ctx, int kernel_class, double* total_ms, int64_t* launches);
 
 /* ---- plan (BeliefPropagationCache storage) ------------------------------ */
 /* Replaces: BeliefPropagationCache(ptn; messages) and initialize_cache

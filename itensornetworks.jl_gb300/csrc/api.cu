@@ -24,6 +24,13 @@ struct gbtn_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   DeviceSched sched{};
+  // optional per-kernel-class event timing (gbtn_ctx_set_profiling)
+  int profiling = 0;
+  struct Rec {
+    int cls;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> recs;
 };
 
 namespace {
@@ -80,7 +87,8 @@ struct gbtn_plan {
   DevBuf<float> d_msg32[2];
   int cur = 0;  // buffer holding the current messages
   DevBuf<double> d_diffs, d_mean, d_rdm, d_edge_sc, d_re, d_im, d_scale, d_out;
-  DevBuf<int> d_conv, d_iters;
+  DevBuf<int> d_conv, d_iters, d_since;
+  DevBuf<double> d_best;
   DevBuf<int> d_net_de_ptr, d_net_de, d_net_v_ptr, d_net_v, d_net_e_ptr, d_net_e;
   // work lists: index 0 = all vertices, 1.. = colour classes; two size classes each
   std::vector<std::pair<WorkList, WorkList>> lists;
@@ -104,6 +112,26 @@ struct gbtn_plan {
 namespace {
 
 constexpr int kSmallN = 1024;  // vertices with n <= kSmallN run one per warp
+constexpr int kStallSweeps = 5;  // reduced-precision phases stop at their noise floor
+
+// Brackets one kernel launch with CUDA events when the context profiles.
+struct KTimer {
+  gbtn_ctx* c;
+  int cls;
+  cudaEvent_t a = nullptr;
+  KTimer(gbtn_ctx* ctx, int k, bool active = true) : c(ctx), cls(k) {
+    if (c->profiling && active) {
+      GBTN_CUDA(cudaEventCreate(&a));
+      GBTN_CUDA(cudaEventRecord(a, c->stream));
+    }
+  }
+  ~KTimer() {
+    if (!a) return;
+    cudaEvent_t b = nullptr;
+    if (cudaEventCreate(&b) == cudaSuccess && cudaEventRecord(b, c->stream) == cudaSuccess)
+      c->recs.push_back({cls, a, b});
+  }
+};
 
 void set_err(const gbtn_ctx* ctx, const std::string& m) {
   if (ctx)
@@ -203,7 +231,7 @@ size_t smem_need(int n, int k, bool sep_bra, size_t elt, int team) {
 // Sweeps of the parallel or coloured schedule in precision T.
 template <typename T>
 void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normalize, DevBuf<T>* msg, const T* fac,
-                const T* bra, int& cur) {
+                const T* bra, int& cur, int stall = 0) {
   cudaStream_t s = P->ctx->stream;
   const bool want_diff = tol >= 0.0;
   GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int) * P->nnet, s));
@@ -213,10 +241,16 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
     if (schedule == GBTN_SCHED_PARALLEL) {
       const T* in = msg[cur].p;
       T* out = msg[cur ^ 1].p;
-      launch_bp_vertices<T>(P->lists[0].first, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
-                            normalize, want_diff, s);
-      launch_bp_vertices<T>(P->lists[0].second, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
-                            normalize, want_diff, s);
+      {
+        KTimer kt(P->ctx, sizeof(T) == 4 ? GBTN_KCLASS_SIMT_F32 : GBTN_KCLASS_SIMT_F64, P->lists[0].first.count > 0);
+        launch_bp_vertices<T>(P->lists[0].first, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
+                              normalize, want_diff, s);
+      }
+      {
+        KTimer kt(P->ctx, sizeof(T) == 4 ? GBTN_KCLASS_SIMT_F32 : GBTN_KCLASS_SIMT_F64, P->lists[0].second.count > 0);
+        launch_bp_vertices<T>(P->lists[0].second, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
+                              normalize, want_diff, s);
+      }
       cur ^= 1;
     } else {
       for (size_t c = 1; c < P->lists.size(); ++c) {
@@ -229,7 +263,7 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
     }
     if (want_diff)
       launch_reduce_diffs(P->nnet, P->d_net_de_ptr.p, P->d_net_de.p, P->d_diffs.p, tol, P->d_conv.p, P->d_iters.p,
-                          P->d_mean.p, s);
+                          P->d_mean.p, s, stall, P->d_best.p, P->d_since.p);
   }
 }
 
@@ -256,7 +290,7 @@ void ensure_zimg(gbtn_plan* P) {
 
 // BF16 sweeps (parallel or coloured): tensor-core kernel on the eligible
 // vertices, FP32 SIMT kernel on the rest, FP32 messages.
-void run_sweeps_bf16(gbtn_plan* P, int schedule, int maxiter, double tol, int normalize, int& c32) {
+void run_sweeps_bf16(gbtn_plan* P, int schedule, int maxiter, double tol, int normalize, int& c32, int stall = 0) {
   cudaStream_t s = P->ctx->stream;
   const bool want_diff = tol >= 0.0;
   GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int) * P->nnet, s));
@@ -265,12 +299,21 @@ void run_sweeps_bf16(gbtn_plan* P, int schedule, int maxiter, double tol, int no
   const float* fac = P->d_fac32.p;
   auto one = [&](size_t li, const float* in, float* out) {
     const WorkList& tl = P->tc_lists[li];
-    launch_tc_vertices(tl.d_vertices, tl.count, P->d_vslot.p, P->d_vd.p, P->d_zimg.p, in, out, P->d_msg_off.p,
-                       P->d_diffs.p, conv, normalize, want_diff, P->d_err.p, s);
-    launch_bp_vertices<float>(P->rest_lists[li].first, P->d_vd.p, fac, nullptr, in, out, P->d_msg_off.p,
-                              P->d_diffs.p, conv, normalize, want_diff, s);
-    launch_bp_vertices<float>(P->rest_lists[li].second, P->d_vd.p, fac, nullptr, in, out, P->d_msg_off.p,
-                              P->d_diffs.p, conv, normalize, want_diff, s);
+    {
+      KTimer kt(P->ctx, GBTN_KCLASS_TENSOR_CORE, tl.count > 0);
+      launch_tc_vertices(tl.d_vertices, tl.count, P->d_vslot.p, P->d_vd.p, P->d_zimg.p, in, out, P->d_msg_off.p,
+                         P->d_diffs.p, conv, normalize, want_diff, P->d_err.p, s);
+    }
+    {
+      KTimer kt(P->ctx, GBTN_KCLASS_SIMT_F32, P->rest_lists[li].first.count > 0);
+      launch_bp_vertices<float>(P->rest_lists[li].first, P->d_vd.p, fac, nullptr, in, out, P->d_msg_off.p,
+                                P->d_diffs.p, conv, normalize, want_diff, s);
+    }
+    {
+      KTimer kt(P->ctx, GBTN_KCLASS_SIMT_F32, P->rest_lists[li].second.count > 0);
+      launch_bp_vertices<float>(P->rest_lists[li].second, P->d_vd.p, fac, nullptr, in, out, P->d_msg_off.p,
+                                P->d_diffs.p, conv, normalize, want_diff, s);
+    }
   };
   for (int it = 0; it < maxiter; ++it) {
     if (schedule == GBTN_SCHED_PARALLEL) {
@@ -281,7 +324,7 @@ void run_sweeps_bf16(gbtn_plan* P, int schedule, int maxiter, double tol, int no
     }
     if (want_diff)
       launch_reduce_diffs(P->nnet, P->d_net_de_ptr.p, P->d_net_de.p, P->d_diffs.p, tol, P->d_conv.p, P->d_iters.p,
-                          P->d_mean.p, s);
+                          P->d_mean.p, s, stall, P->d_best.p, P->d_since.p);
   }
 }
 
@@ -444,6 +487,37 @@ int gbtn_ctx_set_stream(gbtn_ctx* ctx, void* stream) {
 
 void* gbtn_ctx_get_stream(const gbtn_ctx* ctx) { return ctx ? reinterpret_cast<void*>(ctx->stream) : nullptr; }
 
+int gbtn_ctx_set_profiling(gbtn_ctx* ctx, int on) {
+  if (!ctx) return GBTN_ERR_INVALID;
+  ctx->profiling = on ? 1 : 0;
+  return GBTN_OK;
+}
+
+int gbtn_ctx_kernel_time(gbtn_ctx* ctx, int kernel_class, double* total_ms, int64_t* launches) {
+  API_TRY
+  require(ctx && total_ms && launches, "NULL argument");
+  double ms = 0.0;
+  int64_t n = 0;
+  std::vector<gbtn_ctx::Rec> keep;
+  for (auto& r : ctx->recs) {
+    if (r.cls != kernel_class) {
+      keep.push_back(r);
+      continue;
+    }
+    GBTN_CUDA(cudaEventSynchronize(r.b));
+    float t = 0.f;
+    GBTN_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+    ms += t;
+    ++n;
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  ctx->recs.swap(keep);
+  *total_ms = ms;
+  *launches = n;
+  API_CATCH(ctx)
+}
+
 int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   API_TRY
   require(ctx && g && out, "NULL argument");
@@ -546,6 +620,8 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   P->d_mean.alloc(P->nnet);
   P->d_conv.alloc(P->nnet);
   P->d_iters.alloc(P->nnet);
+  P->d_since.alloc(P->nnet);
+  P->d_best.alloc(P->nnet);
   P->d_rdm.alloc(std::max<long long>(P->n_rdm, 1));
   P->d_edge_sc.alloc(std::max(P->ne, 1));
   P->d_re.alloc(P->nnet);
@@ -780,10 +856,10 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
       ensure_zimg(P);
       const double tol16 = o->tol_bf16 > 0 ? o->tol_bf16 : 1e-6;
       const int it16 = o->maxiter_bf16 > 0 ? o->maxiter_bf16 : o->maxiter;
-      run_sweeps_bf16(P, o->schedule, it16, tol16, o->normalize, c32);
+      run_sweeps_bf16(P, o->schedule, it16, tol16, o->normalize, c32, kStallSweeps);
     }
     run_sweeps<float>(P, o->schedule, it32, tol32, o->normalize, P->d_msg32, P->d_fac32.p,
-                      P->sep_bra ? P->d_bra32.p : nullptr, c32);
+                      P->sep_bra ? P->d_bra32.p : nullptr, c32, kStallSweeps);
     launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
     // FP64 sweeps from the FP32 fixed point until tol (or refine_f64 / maxiter sweeps)
     const int nref = o->refine_f64 > 0 ? std::min(o->refine_f64, o->maxiter) : o->maxiter;

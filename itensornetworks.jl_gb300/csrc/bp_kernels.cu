@@ -537,9 +537,13 @@ __global__ void __launch_bounds__(256)
 // Small elementwise / per-edge kernels
 // ---------------------------------------------------------------------------
 
+// Per network: mean message diff of the sweep, iteration count, convergence
+// flag (mean <= tol).  With stall > 0 a network also stops when its mean diff
+// has not dropped below 0.9x its best value for `stall` sweeps -- the noise
+// floor of a reduced-precision phase.
 __global__ void reduce_diffs_kernel(const int* __restrict__ net_de_ptr, const int* __restrict__ net_de,
                                     const double* __restrict__ diffs, double tol, int* converged, int* iters,
-                                    double* mean_diff) {
+                                    double* mean_diff, int stall, double* best, int* since) {
   const int net = blockIdx.x;
   if (converged[net]) return;
   const int b = net_de_ptr[net], e = net_de_ptr[net + 1];
@@ -557,6 +561,14 @@ __global__ void reduce_diffs_kernel(const int* __restrict__ net_de_ptr, const in
       iters[net] += 1;
       mean_diff[net] = tol >= 0.0 ? mean : NAN;
       if (tol >= 0.0 && mean <= tol) converged[net] = 1;
+      if (stall > 0) {
+        if (iters[net] == 1 || mean < 0.9 * best[net]) {
+          best[net] = mean;
+          since[net] = 0;
+        } else if (++since[net] >= stall) {
+          converged[net] = 1;
+        }
+      }
     }
   }
 }
@@ -728,8 +740,10 @@ template void launch_bp_sequential<float>(int, const VDesc*, const int2*, const 
                                           const long long*, int, double, int, int*, double*, int, int, cudaStream_t);
 
 void launch_reduce_diffs(int n_networks, const int* net_de_ptr, const int* net_de, const double* diffs, double tol,
-                         int* converged, int* iters, double* mean_diff, cudaStream_t s) {
-  reduce_diffs_kernel<<<n_networks, 256, 0, s>>>(net_de_ptr, net_de, diffs, tol, converged, iters, mean_diff);
+                         int* converged, int* iters, double* mean_diff, cudaStream_t s, int stall, double* best,
+                         int* since) {
+  reduce_diffs_kernel<<<n_networks, 256, 0, s>>>(net_de_ptr, net_de, diffs, tol, converged, iters, mean_diff, stall,
+                                                 best, since);
   GBTN_CUDA(cudaGetLastError());
 }
 

@@ -23,6 +23,7 @@ ERRORS = {
     6: "GBTN_ERR_NOMEM",
 }
 HOST, DEVICE = 0, 1
+KCLASS_TENSOR_CORE, KCLASS_SIMT_F32, KCLASS_SIMT_F64 = 0, 1, 2
 SCHED = {"sequential": 0, "parallel": 1, "colored": 2}
 PRECISION = {"f64": 0, "f32": 1, "bf16": 2, "mixed": 3}
 INIT = {"identity": 0, "ones": 1}
@@ -94,6 +95,8 @@ SIGNATURES = {
     "gbtn_ctx_destroy": (_I, [_P]),
     "gbtn_ctx_set_stream": (_I, [_P, _P]),
     "gbtn_ctx_get_stream": (_P, [_P]),
+    "gbtn_ctx_set_profiling": (_I, [_P, _I]),
+    "gbtn_ctx_kernel_time": (_I, [_P, _I, _D, C.POINTER(C.c_int64)]),
     "gbtn_plan_create": (_I, [_P, C.POINTER(GraphDesc), C.POINTER(_P)]),
     "gbtn_plan_destroy": (_I, [_P]),
     "gbtn_plan_sizes": (_I, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
@@ -178,6 +181,16 @@ class Context:
 
     def set_stream(self, stream_ptr: int | None):
         check(self.handle, self.lib.gbtn_ctx_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
+
+    def set_profiling(self, on: bool):
+        check(self.handle, self.lib.gbtn_ctx_set_profiling(self.handle, 1 if on else 0))
+
+    def kernel_time(self, kernel_class: int):
+        """(total ms, launches) of one kernel class since the last read."""
+        ms = C.c_double()
+        n = C.c_int64()
+        check(self.handle, self.lib.gbtn_ctx_kernel_time(self.handle, kernel_class, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
 
     @property
     def stream(self) -> int:
