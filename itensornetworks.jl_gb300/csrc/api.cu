@@ -99,6 +99,7 @@ struct gbtn_plan {
   std::vector<std::pair<WorkList, WorkList>> rest_lists;
   std::vector<int> tc_slot_vertex;
   DevBuf<int> d_vslot, d_tc_slot_vertex, d_err;
+  DevBuf<TcRec> d_tcrec;
   DevBuf<__nv_bfloat16> d_zimg;
   bool zimg_valid = false;
   // sequential schedule storage
@@ -301,8 +302,8 @@ void run_sweeps_bf16(gbtn_plan* P, int schedule, int maxiter, double tol, int no
     const WorkList& tl = P->tc_lists[li];
     {
       KTimer kt(P->ctx, GBTN_KCLASS_TENSOR_CORE, tl.count > 0);
-      launch_tc_vertices(tl.d_vertices, tl.count, P->d_vslot.p, P->d_vd.p, P->d_zimg.p, in, out, P->d_msg_off.p,
-                         P->d_diffs.p, conv, normalize, want_diff, P->d_err.p, s);
+      launch_tc_vertices(tl.d_vertices, tl.count, P->d_vslot.p, P->d_tcrec.p, P->d_zimg.p, in, out, P->d_diffs.p,
+                         conv, normalize, want_diff, P->d_err.p, s);
     }
     {
       KTimer kt(P->ctx, GBTN_KCLASS_SIMT_F32, P->rest_lists[li].first.count > 0);
@@ -676,13 +677,28 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   }
   // tensor-core vertices: one swizzled BF16 image slot each
   std::vector<int> vslot(g->nv, -1);
-  if (!P->sep_bra)
+  if (!P->sep_bra && P->n_msg < (1LL << 31))
     for (int v = 0; v < g->nv; ++v)
       if (tc_eligible(P->vd[v])) {
         vslot[v] = (int)P->tc_slot_vertex.size();
         P->tc_slot_vertex.push_back(v);
       }
   P->d_vslot.upload(vslot, s);
+  {
+    std::vector<TcRec> recs(std::max<size_t>(P->tc_slot_vertex.size(), 1));
+    for (size_t i = 0; i < P->tc_slot_vertex.size(); ++i) {
+      const VDesc& d = P->vd[P->tc_slot_vertex[i]];
+      TcRec r{};
+      for (int p = 0; p < 4; ++p) {
+        r.in_off[p] = (int)P->msg_off[d.in_de[p]];
+        r.out_off[p] = (int)P->msg_off[d.out_de[p]];
+        r.out_de[p] = d.out_de[p];
+      }
+      r.net = d.net;
+      recs[i] = r;
+    }
+    P->d_tcrec.upload(recs, s);
+  }
   {
     std::vector<int> sv = P->tc_slot_vertex;
     if (sv.empty()) sv.push_back(0);

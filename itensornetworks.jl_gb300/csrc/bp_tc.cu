@@ -18,14 +18,18 @@
 // G34[(a3,a4),(b3,b4)] and G12[(a1,a2),(b1,b2)] (ket x bra), from which
 //   out3[b3,a3] = sum G34[(a3,a4),(b3,b4)] M4[b4,a4],  out4 likewise with M3,
 //   out1[b1,a1] = sum G12[(a1,a2),(b1,b2)] M2[b2,a2],  out2 likewise with M1
-// are 64 x 64 x 64 FP32 contractions on the CUDA cores.  Outputs are
-// normalised in FP64 and written as FP32 messages (updated_message,
-// src/caches/abstractbeliefpropagationcache.jl:225-239).
+// are 64 x 64 x 64 FP32 contractions on the CUDA cores.  Each output is
+// normalised with an FP64 sum of squares and written as an FP32 message
+// (updated_message, src/caches/abstractbeliefpropagationcache.jl:225-239).
 //
-// Per vertex: one 16 KB TMA bulk copy of the pre-swizzled BF16 image of Z
-// (double-buffered, prefetched one vertex ahead), 16 tcgen05.mma instructions
-// with FP32 accumulation in TMEM (256 columns), 8 tcgen05.ld per thread.
-// 128 threads per CTA, 2 CTAs per SM, persistent over the vertex list.
+// Per vertex: one 16 KB TMA bulk copy of the pre-swizzled BF16 image of Z,
+// 16 tcgen05.mma instructions accumulating in FP32 in TMEM (128 columns,
+// reused by the three MMA phases), 128 threads.  Four CTAs share an SM
+// (52 KB of shared memory each: the Kronecker products, then T12, then the
+// environment G reuse one region), so one CTA's MMAs overlap the others'
+// epilogues; each CTA also overlaps GEMM2' with the G34 epilogue, copies the
+// next vertex's Z while finishing the current one, and loads the next
+// vertex's messages into registers ahead of time.
 #include <cuda_bf16.h>
 
 #include "gbtn_internal.h"
@@ -35,22 +39,28 @@ namespace gbtn {
 namespace {
 
 constexpr int kTcThreads = 128;
+constexpr int kTcBlocksPerSm = 4;
 constexpr uint32_t kZElems = 8192;
 constexpr uint32_t kZBytes = kZElems * 2;
 constexpr uint64_t kWaitNs = 1000000000ull;  // 1 s bound on every wait
 
 // shared-memory carve-up (bytes from a 1024-aligned base)
-constexpr int kOffZ0 = 0, kOffZ1 = 16384, kOffT12 = 32768, kOffT34 = 49152, kOffK12 = 65536, kOffK34 = 73728;
-constexpr int kGStride = 65;  // padded FP32 row of the 64 x 64 environment
-constexpr int kOffG = 81920;
-constexpr int kOffMsg = kOffG + 64 * kGStride * 4;  // 4 x 64 FP32 incoming messages
-constexpr int kOffRes = kOffMsg + 4 * 64 * 4;       // 4 x 64 FP32 outgoing messages
-constexpr int kOffBar = kOffRes + 4 * 64 * 4;       // mma bar, 2 TMA bars
-constexpr int kOffTmem = kOffBar + 3 * 8;
+constexpr int kOffZ = 0;           // 16 KB: Z image (TMA destination)
+constexpr int kOffKT = 16384;      // K12 | K34 (2 x 8 KB), then T12 (16 KB), then G (16.25 KB)
+constexpr int kGStride = 65;       // padded FP32 row of the 64 x 64 environment
+constexpr int kKTBytes = 17408;    // >= 64 * 65 * 4, multiple of 1024
+constexpr int kOffT34 = kOffKT + kKTBytes;
+constexpr int kOffMsg = kOffT34 + 16384;  // 4 x 64 FP32 incoming messages
+constexpr int kOffRes = kOffMsg + 1024;   // 4 x 64 FP32 outgoing messages
+constexpr int kOffBar = kOffRes + 1024;   // mma bar, TMA bar
+constexpr int kOffTmem = kOffBar + 16;
 constexpr int kOffFlag = kOffTmem + 4;
 constexpr int kSmemUsed = kOffFlag + 4;
 constexpr int kSmemBytes = kSmemUsed + 1024;  // room to align the base
-constexpr uint32_t kTmemCols = 256;
+constexpr uint32_t kTmemCols = 128;
+
+static_assert(kOffT34 % 1024 == 0, "swizzled tiles need 1024-byte alignment");
+static_assert(64 * kGStride * 4 <= kKTBytes, "environment does not fit its region");
 
 constexpr uint32_t kIdescG1 = tc::idesc_bf16(128, 64, 0, 0);
 constexpr uint32_t kIdescG1mn = tc::idesc_bf16(128, 64, 1, 0);
@@ -63,32 +73,54 @@ __device__ __forceinline__ double tc_warp_sum(double x) {
   return x;
 }
 
-// Write 64 FP32 values as one 128-byte BF16 row of a 128B-swizzled tile.
-__device__ __forceinline__ void store_row_swizzled(__nv_bfloat16* tile, int row, const float (&v)[64]) {
-  uint4* base = reinterpret_cast<uint4*>(tile + row * 64);
+// 32 lanes x 32 bits, 32 consecutive columns per thread.
+__device__ __forceinline__ void tmem_ld_x32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    __nv_bfloat162 p0 = __floats2bfloat162_rn(v[8 * j + 0], v[8 * j + 1]);
-    __nv_bfloat162 p1 = __floats2bfloat162_rn(v[8 * j + 2], v[8 * j + 3]);
-    __nv_bfloat162 p2 = __floats2bfloat162_rn(v[8 * j + 4], v[8 * j + 5]);
-    __nv_bfloat162 p3 = __floats2bfloat162_rn(v[8 * j + 6], v[8 * j + 7]);
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 p = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&p);
+}
+
+// 32 FP32 values -> 16-byte chunks [c0, c0+4) of one 128-byte BF16 row of a
+// 128B-swizzled tile (chunk j lands at j ^ (row % 8)).
+__device__ __forceinline__ void store_half_row(unsigned char* tile, int row, int c0, const float (&v)[32]) {
+  uint4* base = reinterpret_cast<uint4*>(tile + row * 128);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
     uint4 q;
-    q.x = *reinterpret_cast<uint32_t*>(&p0);
-    q.y = *reinterpret_cast<uint32_t*>(&p1);
-    q.z = *reinterpret_cast<uint32_t*>(&p2);
-    q.w = *reinterpret_cast<uint32_t*>(&p3);
-    base[j ^ (row & 7)] = q;
+    q.x = pack_bf16(v[8 * j + 0], v[8 * j + 1]);
+    q.y = pack_bf16(v[8 * j + 2], v[8 * j + 3]);
+    q.z = pack_bf16(v[8 * j + 4], v[8 * j + 5]);
+    q.w = pack_bf16(v[8 * j + 6], v[8 * j + 7]);
+    base[(c0 + j) ^ (row & 7)] = q;
   }
 }
 
-// FP64 normalisation, FP32 store and message diff of one 8 x 8 message by one warp.
+// Normalise one 8 x 8 message held by a warp (two values per lane) with an
+// FP64 sum of squares, store it as FP32, and (want_diff) return
+// message_diff(new, old) (abstractbeliefpropagationcache.jl:32-36).
 __device__ __forceinline__ double tc_finalize(const float* res, const float* old, float* out, int normalize,
                                               bool want_diff, int lane) {
-  const double v0 = res[lane], v1 = res[lane + 32];
-  const double nrm2 = tc_warp_sum(v0 * v0 + v1 * v1);
-  const double sc = (normalize && nrm2 > 0.0) ? 1.0 / sqrt(nrm2) : 1.0;
-  const float n0 = (float)(v0 * sc), n1 = (float)(v1 * sc);
-  double o0 = 0.0, o1 = 0.0;
+  const float x0 = res[lane], x1 = res[lane + 32];
+  const double ss = tc_warp_sum((double)x0 * (double)x0 + (double)x1 * (double)x1);
+  const float sc = (normalize && ss > 0.0) ? (float)rsqrt(ss) : 1.f;
+  const float n0 = x0 * sc, n1 = x1 * sc;
+  float o0 = 0.f, o1 = 0.f;
   if (want_diff) {
     o0 = old[lane];
     o1 = old[lane + 32];
@@ -98,10 +130,10 @@ __device__ __forceinline__ double tc_finalize(const float* res, const float* old
   out[lane + 32] = n1;
   double diff = 0.0;
   if (want_diff) {
-    const double a0 = n0, a1 = n1;
-    const double dot = tc_warp_sum(a0 * o0 + a1 * o1);
+    const double a0 = n0, a1 = n1, b0 = o0, b1 = o1;
+    const double dot = tc_warp_sum(a0 * b0 + a1 * b1);
     const double na = tc_warp_sum(a0 * a0 + a1 * a1);
-    const double nb = tc_warp_sum(o0 * o0 + o1 * o1);
+    const double nb = tc_warp_sum(b0 * b0 + b1 * b1);
     diff = 1.0 - (dot * dot) / (na * nb);
   }
   return diff;
@@ -109,28 +141,76 @@ __device__ __forceinline__ double tc_finalize(const float* res, const float* old
 
 }  // namespace
 
+namespace {
+
+// D2 / D2' diagonal block of this thread's row (s = row / 64) summed over s
+// into G[c][.] (c = row % 64): rows with s = 0 store, rows with s = 1 add.
+__device__ __forceinline__ void diag_to_env(uint32_t taddr, float* G, int t) {
+  const int s = t >> 6, c = t & 63;
+  float d0[32], d1[32];
+  tmem_ld_x32(taddr + 64 * s, d0);
+  tmem_ld_x32(taddr + 64 * s + 32, d1);
+  float* g = G + c * kGStride;
+  if (s == 0) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      g[j] = d0[j];
+      g[32 + j] = d1[j];
+    }
+  }
+  __syncthreads();
+  if (s == 1) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      g[j] += d0[j];
+      g[32 + j] += d1[j];
+    }
+  }
+  __syncthreads();
+}
+
+// Outgoing messages of one leg pair from its environment G[(ax,ay),(bx,by)]:
+// threads 0-63 contract the second leg with Mx (result on the first leg),
+// threads 64-127 contract the first leg with My (result on the second leg).
+__device__ __forceinline__ void env_to_out(const float* G, const float* Mx, const float* My, float* res_first,
+                                           float* res_second, int t) {
+  const int u = t & 63, bx = u & 7, ax = u >> 3;
+  float acc = 0.f;
+  if (t < 64) {
+#pragma unroll
+    for (int ay = 0; ay < 8; ++ay)
+#pragma unroll
+      for (int by = 0; by < 8; ++by) acc = fmaf(G[(ax + 8 * ay) * kGStride + bx + 8 * by], Mx[by + 8 * ay], acc);
+    res_first[u] = acc;
+  } else {
+#pragma unroll
+    for (int ay = 0; ay < 8; ++ay)
+#pragma unroll
+      for (int by = 0; by < 8; ++by) acc = fmaf(G[(ay + 8 * ax) * kGStride + by + 8 * bx], My[by + 8 * ay], acc);
+    res_second[u] = acc;
+  }
+}
+
+}  // namespace
+
 // One CTA walks work[blockIdx.x], work[blockIdx.x + gridDim.x], ...; vertex v
-// reads its Z image at zimg + vslot[v] * 8192.  err (device) receives
-// GBTN_ERR_TIMEOUT when a bounded wait gives up; the CTA then drains its own
-// copies in flight, frees its TMEM and returns.
-__global__ void __launch_bounds__(kTcThreads, 2)
+// uses image slot vslot[v] (Z at zimg + slot * 8192, offsets in recs[slot]).
+// err (device) receives GBTN_ERR_TIMEOUT when a bounded wait gives up; the CTA
+// then drains its own copies and MMAs in flight, frees its TMEM and returns.
+__global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     tc_vertex_kernel(const int* __restrict__ work, int nwork, const int* __restrict__ vslot,
-                     const VDesc* __restrict__ vd, const __nv_bfloat16* __restrict__ zimg, const float* msg_in,
-                     float* msg_out, const long long* __restrict__ msg_off, double* diffs, const int* converged,
-                     int normalize, int want_diff, int* err) {
+                     const TcRec* __restrict__ recs, const __nv_bfloat16* __restrict__ zimg, const float* msg_in,
+                     float* msg_out, double* diffs, const int* converged, int normalize, int want_diff, int* err) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  __nv_bfloat16* Zbuf[2] = {reinterpret_cast<__nv_bfloat16*>(sm + kOffZ0),
-                            reinterpret_cast<__nv_bfloat16*>(sm + kOffZ1)};
-  __nv_bfloat16* T12 = reinterpret_cast<__nv_bfloat16*>(sm + kOffT12);
-  __nv_bfloat16* T34 = reinterpret_cast<__nv_bfloat16*>(sm + kOffT34);
-  __nv_bfloat16* K12 = reinterpret_cast<__nv_bfloat16*>(sm + kOffK12);
-  __nv_bfloat16* K34 = reinterpret_cast<__nv_bfloat16*>(sm + kOffK34);
-  float* G = reinterpret_cast<float*>(sm + kOffG);
+  unsigned char* Z = sm + kOffZ;
+  unsigned char* KT = sm + kOffKT;  // K12 | K34, later T12, later G
+  unsigned char* T34 = sm + kOffT34;
+  float* G = reinterpret_cast<float*>(KT);
   float* MSG = reinterpret_cast<float*>(sm + kOffMsg);
   float* RES = reinterpret_cast<float*>(sm + kOffRes);
   uint64_t* mma_bar = reinterpret_cast<uint64_t*>(sm + kOffBar);
-  uint64_t* tma_bar = mma_bar + 1;  // [2]
+  uint64_t* tma_bar = mma_bar + 1;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kOffTmem);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(sm + kOffFlag);
 
@@ -141,8 +221,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   }
   if (t == 0) {
     tc::mbar_init(mma_bar, 1);
-    tc::mbar_init(&tma_bar[0], 1);
-    tc::mbar_init(&tma_bar[1], 1);
+    tc::mbar_init(tma_bar, 1);
     tc::fence_mbar_init();
     *abort_flag = 0;
   }
@@ -150,178 +229,201 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's TMEM lanes
 
   // thread-0 bookkeeping of the asynchronous work in flight
-  uint32_t mma_phase = 0, tma_phase0 = 0, tma_phase1 = 0;
-  int tma_pending0 = 0, tma_pending1 = 0, mma_pending = 0;
-
-  auto issue_z = [&](int w, int b) {
-    uint64_t* bar = &tma_bar[b];
-    tc::mbar_expect_tx(bar, kZBytes);
-    tc::tma_load_1d(Zbuf[b], zimg + (size_t)vslot[work[w]] * kZElems, kZBytes, bar);
-    if (b == 0) tma_pending0 = 1; else tma_pending1 = 1;
+  uint32_t mma_phase = 0, tma_phase = 0;
+  int tma_pending = 0, mma_pending = 0;
+  auto issue_z = [&](int slot) {
+    tc::mbar_expect_tx(tma_bar, kZBytes);
+    tc::tma_load_1d(Z, zimg + (size_t)slot * kZElems, kZBytes, tma_bar);
+    tma_pending = 1;
   };
-  // thread 0: wait for buffer b's copy; returns false on timeout
-  auto wait_z = [&](int b) -> bool {
-    const bool ok = tc::mbar_wait(&tma_bar[b], b == 0 ? tma_phase0 : tma_phase1, kWaitNs);
+  auto wait_z = [&]() -> bool {
+    const bool ok = tc::mbar_wait(tma_bar, tma_phase, kWaitNs);
     if (ok) {
-      if (b == 0) { tma_phase0 ^= 1; tma_pending0 = 0; } else { tma_phase1 ^= 1; tma_pending1 = 0; }
+      tma_phase ^= 1;
+      tma_pending = 0;
     }
     return ok;
   };
   auto wait_mma = [&]() -> bool {
     const bool ok = tc::mbar_wait(mma_bar, mma_phase, kWaitNs);
-    if (ok) { mma_phase ^= 1; mma_pending = 0; }
+    if (ok) {
+      mma_phase ^= 1;
+      mma_pending = 0;
+    }
     return ok;
   };
+  auto commit = [&]() {
+    tc::mma_commit(mma_bar);
+    mma_pending = 1;
+  };
 
+  const int q0 = t, q1 = t + 128;  // this thread's entries of the 4 x 64 message block
+  const int e = t & 63;
   int w = blockIdx.x;
-  if (t == 0 && w < nwork) issue_z(w, 0);
-  for (int i = 0; w < nwork; ++i, w += gridDim.x) {
-    const int buf = i & 1;
-    const int v = work[w];
+  float cm0 = 0.f, cm1 = 0.f;  // current vertex's incoming-message entries q0, q1
+  int cnet = 0;
+  if (w < nwork) {
+    const int sl = vslot[work[w]];
+    if (t == 0) issue_z(sl);
+    cnet = recs[sl].net;
+    cm0 = msg_in[recs[sl].in_off[q0 >> 6] + e];
+    cm1 = msg_in[recs[sl].in_off[q1 >> 6] + e];
+  }
+  for (; w < nwork; w += gridDim.x) {
+    const int sl = vslot[work[w]];
+    const int out_off_w = recs[sl].out_off[warp];
+    const int out_de_w = recs[sl].out_de[warp];
+    // next vertex: record now, messages later in this iteration
     const int wn = w + gridDim.x;
-    if (t == 0 && wn < nwork) issue_z(wn, buf ^ 1);  // buffer buf^1 is idle: its MMAs completed last iteration
-    const VDesc& dv = vd[v];
-    const bool skip = converged && converged[dv.net];
-    for (int q = t; q < 256; q += kTcThreads) {
-      const int p = q >> 6, e = q & 63;
-      const long long off = msg_off[skip ? dv.out_de[p] : dv.in_de[p]];
-      if (skip)
-        msg_out[off + e] = msg_in[off + e];
-      else
-        MSG[q] = msg_in[off + e];
+    int nsl = -1, nin0 = 0, nin1 = 0, nnet = 0;
+    if (wn < nwork) {
+      nsl = vslot[work[wn]];
+      nin0 = recs[nsl].in_off[q0 >> 6];
+      nin1 = recs[nsl].in_off[q1 >> 6];
+      nnet = recs[nsl].net;
     }
+    float nm0 = 0.f, nm1 = 0.f;
+
+    if (converged && converged[cnet]) {  // network done: carry its messages forward
+      const int o0 = recs[sl].out_off[q0 >> 6], o1 = recs[sl].out_off[q1 >> 6];
+      msg_out[o0 + e] = msg_in[o0 + e];
+      msg_out[o1 + e] = msg_in[o1 + e];
+      if (t == 0) {
+        const bool ok = wait_z();
+        *abort_flag = ok ? 0 : 1;
+        if (ok && nsl >= 0) issue_z(nsl);
+      }
+      __syncthreads();
+      if (*abort_flag) break;
+      if (nsl >= 0) {
+        cm0 = msg_in[nin0 + e];
+        cm1 = msg_in[nin1 + e];
+        cnet = nnet;
+      }
+      continue;
+    }
+
+    MSG[q0] = cm0;
+    MSG[q1] = cm1;
     __syncthreads();
-    if (!skip) {
-      // Kronecker products K12 = M1 (x) M2 (threads 0-63) and K34 = M3 (x) M4 (64-127):
-      // row n = b_a + 8 b_b, column k = a_a + 8 a_b, value M_a[b_a, a_a] M_b[b_b, a_b].
-      const int n = t & 63;
+    {
+      // Kronecker products: threads 0-63 build K12 = M1 (x) M2, 64-127 K34 = M3 (x) M4;
+      // row n = b_a + 8 b_b, column k = a_a + 8 a_b (16-byte chunk a_b), value M_a[b_a,a_a] M_b[b_b,a_b]
+      const int n = t & 63, ba = n & 7, bb = n >> 3;
       const float* Ma = MSG + (t < 64 ? 0 : 128);
       const float* Mb = Ma + 64;
-      const int ba = n & 7, bb = n >> 3;
-      float row[64];
+      float ma[8];
+#pragma unroll
+      for (int aa = 0; aa < 8; ++aa) ma[aa] = Ma[ba + 8 * aa];
+      uint4* row = reinterpret_cast<uint4*>(KT + (t < 64 ? 0 : 8192) + n * 128);
 #pragma unroll
       for (int ab = 0; ab < 8; ++ab) {
         const float mb = Mb[bb + 8 * ab];
-#pragma unroll
-        for (int aa = 0; aa < 8; ++aa) row[aa + 8 * ab] = Ma[ba + 8 * aa] * mb;
+        uint4 qv;
+        qv.x = pack_bf16(ma[0] * mb, ma[1] * mb);
+        qv.y = pack_bf16(ma[2] * mb, ma[3] * mb);
+        qv.z = pack_bf16(ma[4] * mb, ma[5] * mb);
+        qv.w = pack_bf16(ma[6] * mb, ma[7] * mb);
+        row[ab ^ (n & 7)] = qv;
       }
-      store_row_swizzled(t < 64 ? K12 : K34, n, row);
       tc::fence_proxy_async_smem();
     }
-    if (t == 0) *abort_flag = wait_z(buf) ? 0 : 1;
+    if (t == 0) *abort_flag = wait_z() ? 0 : 1;
     __syncthreads();
     if (*abort_flag) break;
-    if (skip) continue;
 
-    // ---- GEMM1 / GEMM1' ----
-    const uint32_t zaddr = tc::smem_u32(Zbuf[buf]);
+    const uint32_t zaddr = tc::smem_u32(Z), ktaddr = tc::smem_u32(KT), t34addr = tc::smem_u32(T34);
+    // ---- GEMM1 -> columns [0,64), GEMM1' -> [64,128) ----
     if (t == 0) {
       tc::tc_fence_after();
-      const uint32_t k12 = tc::smem_u32(K12), k34 = tc::smem_u32(K34);
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk)
-        tc::mma_bf16(tmem + 0, tc::smem_desc(zaddr + 32 * kk, 16, 1024), tc::smem_desc(k12 + 32 * kk, 16, 1024),
+        tc::mma_bf16(tmem + 0, tc::smem_desc(zaddr + 32 * kk, 16, 1024), tc::smem_desc(ktaddr + 32 * kk, 16, 1024),
                      kIdescG1, kk > 0);
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk)
         tc::mma_bf16(tmem + 64, tc::smem_desc(zaddr + 2048 * kk, 8192, 1024),
-                     tc::smem_desc(k34 + 32 * kk, 16, 1024), kIdescG1mn, kk > 0);
-      tc::mma_commit(mma_bar);
-      mma_pending = 1;
+                     tc::smem_desc(ktaddr + 8192 + 32 * kk, 16, 1024), kIdescG1mn, kk > 0);
+      commit();
       *abort_flag = wait_mma() ? 0 : 1;
     }
     __syncthreads();
     if (*abort_flag) break;
     tc::tc_fence_after();
     {
-      float d[64];
-      tc::tmem_ld_x64(tmem + lane_base + 0, d);
-      store_row_swizzled(T12, t, d);
-      tc::tmem_ld_x64(tmem + lane_base + 64, d);
-      store_row_swizzled(T34, t, d);
+      float d[32];
+      tmem_ld_x32(trow + 0, d);
+      store_half_row(KT, t, 0, d);  // T12 overwrites the Kronecker products (their MMAs are done)
+      tmem_ld_x32(trow + 32, d);
+      store_half_row(KT, t, 4, d);
+      tmem_ld_x32(trow + 64, d);
+      store_half_row(T34, t, 0, d);
+      tmem_ld_x32(trow + 96, d);
+      store_half_row(T34, t, 4, d);
     }
     tc::fence_proxy_async_smem();
     tc::tc_fence_before();
     __syncthreads();
-
-    // ---- GEMM2 / GEMM2' ----
+    // ---- GEMM2 -> columns [0,128) ----
     if (t == 0) {
       tc::tc_fence_after();
-      const uint32_t t12 = tc::smem_u32(T12), t34 = tc::smem_u32(T34);
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk)
-        tc::mma_bf16(tmem + 0, tc::smem_desc(t12 + 32 * kk, 16, 1024), tc::smem_desc(zaddr + 32 * kk, 16, 1024),
+        tc::mma_bf16(tmem + 0, tc::smem_desc(ktaddr + 32 * kk, 16, 1024), tc::smem_desc(zaddr + 32 * kk, 16, 1024),
                      kIdescG2, kk > 0);
-#pragma unroll
-      for (int kk = 0; kk < 4; ++kk)
-        tc::mma_bf16(tmem + 128, tc::smem_desc(t34 + 32 * kk, 16, 1024),
-                     tc::smem_desc(zaddr + 2048 * kk, 8192, 1024), kIdescG2mn, kk > 0);
-      tc::mma_commit(mma_bar);
-      mma_pending = 1;
+      commit();
       *abort_flag = wait_mma() ? 0 : 1;
+    }
+    // the next vertex's incoming messages, ahead of use
+    if (nsl >= 0) {
+      nm0 = msg_in[nin0 + e];
+      nm1 = msg_in[nin1 + e];
     }
     __syncthreads();
     if (*abort_flag) break;
     tc::tc_fence_after();
-
-    // ---- two-leg environments and the four outgoing messages ----
-    const int s = warp >> 1, c = t & 63;
-    const float* M1 = MSG;
-    const float* M2 = MSG + 64;
-    const float* M3 = MSG + 128;
-    const float* M4 = MSG + 192;
-    for (int half = 0; half < 2; ++half) {
-      float d[64];
-      tc::tmem_ld_x64(tmem + lane_base + 128 * half + 64 * s, d);
-      if (s == 0) {
-#pragma unroll
-        for (int j = 0; j < 64; ++j) G[c * kGStride + j] = d[j];
-      }
-      __syncthreads();
-      if (s == 1) {
-#pragma unroll
-        for (int j = 0; j < 64; ++j) G[c * kGStride + j] += d[j];
-      }
-      __syncthreads();
-      // half 0: G = G34 -> out3 (t < 64, uses M4) and out4 (t >= 64, uses M3)
-      // half 1: G = G12 -> out1 (t < 64, uses M2) and out2 (t >= 64, uses M1)
-      const int u = t & 63, bx = u & 7, ax = u >> 3;
-      float acc = 0.f;
-      if (t < 64) {
-        const float* Mo = half == 0 ? M4 : M2;  // other leg of the pair, contracted
-#pragma unroll
-        for (int ay = 0; ay < 8; ++ay)
-#pragma unroll
-          for (int by = 0; by < 8; ++by) acc = fmaf(G[(ax + 8 * ay) * kGStride + bx + 8 * by], Mo[by + 8 * ay], acc);
-        RES[(half == 0 ? 2 : 0) * 64 + u] = acc;
-      } else {
-        const float* Mo = half == 0 ? M3 : M1;
-#pragma unroll
-        for (int ay = 0; ay < 8; ++ay)
-#pragma unroll
-          for (int by = 0; by < 8; ++by) acc = fmaf(G[(ay + 8 * ax) * kGStride + by + 8 * bx], Mo[by + 8 * ay], acc);
-        RES[(half == 0 ? 3 : 1) * 64 + u] = acc;
-      }
-      __syncthreads();
-    }
+    diag_to_env(trow, G, t);  // G34 (overwrites T12: GEMM2 is done)
     tc::tc_fence_before();
-    // warp p finalises the message leaving on leg p
-    {
-      const int de = dv.out_de[warp];
-      const long long off = msg_off[de];
-      const double df = tc_finalize(RES + 64 * warp, msg_in + off, msg_out + off, normalize, want_diff != 0, lane);
-      if (want_diff && lane == 0) diffs[de] = df;
+    __syncthreads();
+    // ---- GEMM2' -> columns [0,128), overlapped with the G34 epilogue ----
+    if (t == 0) {
+      tc::tc_fence_after();
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+        tc::mma_bf16(tmem + 0, tc::smem_desc(t34addr + 32 * kk, 16, 1024),
+                     tc::smem_desc(zaddr + 2048 * kk, 8192, 1024), kIdescG2mn, kk > 0);
+      commit();
     }
+    env_to_out(G, MSG + 192, MSG + 128, RES + 128, RES + 192, t);  // out3 (with M4), out4 (with M3)
+    if (t == 0) {
+      const bool ok = wait_mma();
+      *abort_flag = ok ? 0 : 1;
+      if (ok && nsl >= 0) issue_z(nsl);  // Z is free: fetch the next vertex's image
+    }
+    __syncthreads();
+    if (*abort_flag) break;
+    tc::tc_fence_after();
+    diag_to_env(trow, G, t);  // G12
+    env_to_out(G, MSG + 64, MSG, RES, RES + 64, t);  // out1 (with M2), out2 (with M1)
+    tc::tc_fence_before();
+    __syncthreads();
+    {
+      const double df = tc_finalize(RES + 64 * warp, msg_in + out_off_w, msg_out + out_off_w, normalize,
+                                    want_diff != 0, lane);
+      if (want_diff && lane == 0) diffs[out_de_w] = df;
+    }
+    cm0 = nm0;
+    cm1 = nm1;
+    cnet = nnet;
   }
 
-  // drain: after a timeout, wait (bounded) for this CTA's own copies and MMAs
+  // drain: after a timeout, wait (bounded) for this CTA's own copy and MMAs
   if (t == 0 && *abort_flag) {
     atomicExch(err, (int)GBTN_ERR_TIMEOUT);
-    if (tma_pending0) wait_z(0);
-    if (tma_pending1) wait_z(1);
+    if (tma_pending) wait_z();
     if (mma_pending) wait_mma();
   }
   tc::tc_fence_before();
@@ -329,6 +431,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   tc::tc_fence_after();
   if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
+
+namespace {
 
 // Swizzled BF16 image of Z for every slot: element A[s, c1, c2] (idx = s + 2 c1
 // + 128 c2) goes to row r = 64 s + c2, 16-byte chunk (c1 / 8) ^ (r % 8).
@@ -345,9 +449,7 @@ __global__ void build_zimg_kernel(const int* __restrict__ slot_vertex, int nslot
   }
 }
 
-}  // namespace gbtn
-
-namespace gbtn {
+}  // namespace
 
 bool tc_eligible(const VDesc& d) {
   if (d.k != 4 || d.d != 2) return false;
@@ -363,9 +465,9 @@ void launch_build_zimg(const int* slot_vertex, int nslot, const VDesc* vd, const
   GBTN_CUDA(cudaGetLastError());
 }
 
-void launch_tc_vertices(const int* work, int nwork, const int* vslot, const VDesc* vd, const __nv_bfloat16* zimg,
-                        const float* msg_in, float* msg_out, const long long* msg_off, double* diffs,
-                        const int* converged, int normalize, int want_diff, int* err, cudaStream_t s) {
+void launch_tc_vertices(const int* work, int nwork, const int* vslot, const TcRec* recs, const __nv_bfloat16* zimg,
+                        const float* msg_in, float* msg_out, double* diffs, const int* converged, int normalize,
+                        int want_diff, int* err, cudaStream_t s) {
   if (nwork == 0) return;
   static int nsm = 0;
   if (nsm == 0) {
@@ -374,9 +476,10 @@ void launch_tc_vertices(const int* work, int nwork, const int* vslot, const VDes
     GBTN_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   }
   GBTN_CUDA(cudaFuncSetAttribute(tc_vertex_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-  const int grid = nwork < 2 * nsm ? nwork : 2 * nsm;
-  tc_vertex_kernel<<<grid, kTcThreads, kSmemBytes, s>>>(work, nwork, vslot, vd, zimg, msg_in, msg_out, msg_off,
-                                                         diffs, converged, normalize, want_diff, err);
+  const int slots = kTcBlocksPerSm * nsm;
+  const int grid = nwork < slots ? nwork : slots;
+  tc_vertex_kernel<<<grid, kTcThreads, kSmemBytes, s>>>(work, nwork, vslot, recs, zimg, msg_in, msg_out, diffs,
+                                                         converged, normalize, want_diff, err);
   GBTN_CUDA(cudaGetLastError());
 }
 

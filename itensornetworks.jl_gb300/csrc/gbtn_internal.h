@@ -125,11 +125,20 @@ void launch_logscalar(int n_networks, const int* net_v_ptr, const int* net_v, co
                       const double* edge_sc, double* re, double* im, cudaStream_t s);
 
 // BF16 tensor-core path (bp_tc.cu): degree-4 vertices, d = 2, chi = 8.
+// Per-slot record: element offsets of the incoming / outgoing messages on the
+// four legs, the outgoing directed-edge ids and the network id.
+struct __align__(16) TcRec {
+  int in_off[4];
+  int out_off[4];
+  int out_de[4];
+  int net;
+  int pad[3];
+};
 bool tc_eligible(const VDesc& d);
 void launch_build_zimg(const int* slot_vertex, int nslot, const VDesc* vd, const double* fac, __nv_bfloat16* zimg,
                        cudaStream_t s);
-void launch_tc_vertices(const int* work, int nwork, const int* vslot, const VDesc* vd, const __nv_bfloat16* zimg,
-                        const float* msg_in, float* msg_out, const long long* msg_off, double* diffs,
-                        const int* converged, int normalize, int want_diff, int* err, cudaStream_t s);
+void launch_tc_vertices(const int* work, int nwork, const int* vslot, const TcRec* recs, const __nv_bfloat16* zimg,
+                        const float* msg_in, float* msg_out, double* diffs, const int* converged, int normalize,
+                        int want_diff, int* err, cudaStream_t s);
 
 }  // namespace gbtn
