@@ -279,7 +279,7 @@ def run_ours(args):
     value = world * msgs_step / (ms_bf16 * 1e-3)
     n_tc = BATCH * tc_vertices_per_net()
     alg_flops_vertex = 4 * (2 * D * CHI ** 4 * 4 * CHI)  # k * F at k = 4
-    mma_flops_vertex = 2 * (2 * 128 * 64 * 64) + 2 * (2 * 128 * 128 * 64)
+    mma_flops_vertex = 2 * (2 * 128 * 64 * 64) + 2 * (2 * 64 * 64 * 128)  # GEMM1, GEMM1', GEMM2, GEMM2'
     tc_launch_ms = tc_ms / max(tc_n, 1)
     achieved = n_tc * alg_flops_vertex / (tc_launch_ms * 1e-3) / 1e12
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
@@ -310,6 +310,7 @@ def run_ours(args):
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "tc_vertex_kernel", "launch_ms": tc_launch_ms, "launches": tc_n,
+                         "other_kernels_ms_per_sweep": {"simt_f32_boundary": simt_ms / max(args.steps, 1)},
                          "units_per_launch": n_tc, "alg_flops_per_unit": alg_flops_vertex,
                          "mma_tflops": n_tc * mma_flops_vertex / (tc_launch_ms * 1e-3) / 1e12,
                          "note": f"algorithmic FP flops of the degree-4 vertices / event-timed kernel duration, of {peak_src} bf16 peak"},

@@ -7,29 +7,30 @@
 // (A[s, l1..l4] = Z_s[c2][c1]).  Stacked, Z is a 128 x 64 BF16 matrix kept in
 // shared memory in the 128-byte-swizzled layout, which the tensor core reads
 // both as a K-major operand (rows (s,c2), K = c1) and, through the symmetry of
-// the swizzle atom, as an MN-major operand (M = (s,c1), K = c2).  With the
+// the swizzle atom, as an MN-major operand (M or N = c1, K = (s,c2)).  With the
 // Kronecker products K12 = M1 (x) M2 and K34 = M3 (x) M4 of the incoming
 // messages (bra x ket):
-//   GEMM1   T12[(s,c2), (b1,b2)] = sum_c1 Z[(s,c2), c1] K12[(b1,b2), c1]       M=128 N=64  K=64
-//   GEMM1'  T34[(s,c1), (b3,b4)] = sum_c2 Z_s[c2][c1]  K34[(b3,b4), c2]        M=128 N=64  K=64
-//   GEMM2   D2[(s,c2), (s',c2')] = sum_c1' T12[(s,c2), c1'] Z_s'[c2'][c1']     M=128 N=128 K=64
-//   GEMM2'  D2'[(s,c1),(s',c1')] = sum_c2' T34[(s,c1), c2'] Z_s'[c2'][c1']     M=128 N=128 K=64
-// The s = s' diagonal blocks summed over s give the two-leg environments
-// G34[(a3,a4),(b3,b4)] and G12[(a1,a2),(b1,b2)] (ket x bra), from which
-//   out3[b3,a3] = sum G34[(a3,a4),(b3,b4)] M4[b4,a4],  out4 likewise with M3,
-//   out1[b1,a1] = sum G12[(a1,a2),(b1,b2)] M2[b2,a2],  out2 likewise with M1
-// are 64 x 64 x 64 FP32 contractions on the CUDA cores.  Each output is
-// normalised with an FP64 sum of squares and written as an FP32 message
+//   GEMM1   T12[(s,c2), (b1,b2)] = sum_c1 Z[(s,c2), c1] K12[(b1,b2), c1]          M=128 N=64 K=64
+//   GEMM1'  T34[(s,c1), (b3,b4)] = sum_c2 Z_s[c2][c1] K34[(b3,b4), c2]            M=128 N=64 K=64
+//   GEMM2   G34[c2, c2']  = sum_{s,c1'} T12[(s,c2), c1'] Z_s[c2'][c1']             M=64  N=64 K=128
+//   GEMM2'  G12[c1, c1']  = sum_{s,c2'} T34[(s,c1), c2'] Z_s[c2'][c1']             M=64  N=64 K=128
+// G34[(a3,a4),(b3,b4)] and G12[(a1,a2),(b1,b2)] are the two-leg environments
+// (ket x bra); the outgoing messages
+//   out3[b3,a3] = sum G34[(a3,a4),(b3,b4)] M4[b4,a4],  out4[b4,a4] = sum G34 M3[b3,a3],
+//   out1[b1,a1] = sum G12[(a1,a2),(b1,b2)] M2[b2,a2],  out2[b2,a2] = sum G12 M1[b1,a1]
+// are FP32 contractions done from registers (warp shuffles plus one
+// cross-warp sum).  Each message is normalised and written as FP32
 // (updated_message, src/caches/abstractbeliefpropagationcache.jl:225-239).
+// BP is invariant under message scaling, so this reduced-precision phase
+// normalises in FP32; the FP64 refinement sweeps that follow normalise in FP64.
 //
 // Per vertex: one 16 KB TMA bulk copy of the pre-swizzled BF16 image of Z,
-// 16 tcgen05.mma instructions accumulating in FP32 in TMEM (128 columns,
-// reused by the three MMA phases), 128 threads.  Four CTAs share an SM
-// (52 KB of shared memory each: the Kronecker products, then T12, then the
-// environment G reuse one region), so one CTA's MMAs overlap the others'
-// epilogues; each CTA also overlaps GEMM2' with the G34 epilogue, copies the
-// next vertex's Z while finishing the current one, and loads the next
-// vertex's messages into registers ahead of time.
+// 24 tcgen05.mma instructions (4.2 MFLOP) accumulating in FP32 in TMEM (128
+// columns: D1 | D1', then G34 | G12), two MMA round trips, seven CTA barriers,
+// 128 threads.  Four CTAs share an SM (53 KB of shared memory each; the
+// Kronecker products and then T12 share one region), the next vertex's Z is
+// copied while the current one finishes and its messages are loaded into
+// registers ahead of use.
 #include <cuda_bf16.h>
 
 #include "gbtn_internal.h"
@@ -46,11 +47,10 @@ constexpr uint64_t kWaitNs = 1000000000ull;  // 1 s bound on every wait
 
 // shared-memory carve-up (bytes from a 1024-aligned base)
 constexpr int kOffZ = 0;           // 16 KB: Z image (TMA destination)
-constexpr int kOffKT = 16384;      // K12 | K34 (2 x 8 KB), then T12 (16 KB), then G (16.25 KB)
-constexpr int kGStride = 65;       // padded FP32 row of the 64 x 64 environment
-constexpr int kKTBytes = 17408;    // >= 64 * 65 * 4, multiple of 1024
-constexpr int kOffT34 = kOffKT + kKTBytes;
-constexpr int kOffMsg = kOffT34 + 16384;  // 4 x 64 FP32 incoming messages
+constexpr int kOffKT = 16384;      // K12 | K34 (2 x 8 KB), then T12 as two 8 KB tiles (s = 0, 1)
+constexpr int kOffT34 = 32768;     // T34 as two 8 KB tiles (s = 0, 1)
+constexpr int kOffPart = 49152;    // cross-warp partial sums: 2 pairs x 4 warps x 64 FP32
+constexpr int kOffMsg = kOffPart + 2048;  // 4 x 64 FP32 incoming messages
 constexpr int kOffRes = kOffMsg + 1024;   // 4 x 64 FP32 outgoing messages
 constexpr int kOffBar = kOffRes + 1024;   // mma bar, TMA bar
 constexpr int kOffTmem = kOffBar + 16;
@@ -59,13 +59,10 @@ constexpr int kSmemUsed = kOffFlag + 4;
 constexpr int kSmemBytes = kSmemUsed + 1024;  // room to align the base
 constexpr uint32_t kTmemCols = 128;
 
-static_assert(kOffT34 % 1024 == 0, "swizzled tiles need 1024-byte alignment");
-static_assert(64 * kGStride * 4 <= kKTBytes, "environment does not fit its region");
-
 constexpr uint32_t kIdescG1 = tc::idesc_bf16(128, 64, 0, 0);
 constexpr uint32_t kIdescG1mn = tc::idesc_bf16(128, 64, 1, 0);
-constexpr uint32_t kIdescG2 = tc::idesc_bf16(128, 128, 0, 0);
-constexpr uint32_t kIdescG2mn = tc::idesc_bf16(128, 128, 0, 1);
+constexpr uint32_t kIdescG2 = tc::idesc_bf16(64, 64, 0, 0);
+constexpr uint32_t kIdescG2mn = tc::idesc_bf16(64, 64, 0, 1);
 
 __device__ __forceinline__ double tc_warp_sum(double x) {
 #pragma unroll
@@ -111,14 +108,16 @@ __device__ __forceinline__ void store_half_row(unsigned char* tile, int row, int
   }
 }
 
-// Normalise one 8 x 8 message held by a warp (two values per lane) with an
-// FP64 sum of squares, store it as FP32, and (want_diff) return
-// message_diff(new, old) (abstractbeliefpropagationcache.jl:32-36).
+// Normalise one 8 x 8 message held by a warp (two values per lane), store it
+// as FP32, and (want_diff) return message_diff(new, old)
+// (abstractbeliefpropagationcache.jl:32-36), accumulated in FP64.
 __device__ __forceinline__ double tc_finalize(const float* res, const float* old, float* out, int normalize,
                                               bool want_diff, int lane) {
   const float x0 = res[lane], x1 = res[lane + 32];
-  const double ss = tc_warp_sum((double)x0 * (double)x0 + (double)x1 * (double)x1);
-  const float sc = (normalize && ss > 0.0) ? (float)rsqrt(ss) : 1.f;
+  float ss = fmaf(x0, x0, x1 * x1);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  const float sc = (normalize && ss > 0.f) ? rsqrtf(ss) : 1.f;
   const float n0 = x0 * sc, n1 = x1 * sc;
   float o0 = 0.f, o1 = 0.f;
   if (want_diff) {
@@ -143,51 +142,49 @@ __device__ __forceinline__ double tc_finalize(const float* res, const float* old
 
 namespace {
 
-// D2 / D2' diagonal block of this thread's row (s = row / 64) summed over s
-// into G[c][.] (c = row % 64): rows with s = 0 store, rows with s = 1 add.
-__device__ __forceinline__ void diag_to_env(uint32_t taddr, float* G, int t) {
-  const int s = t >> 6, c = t & 63;
-  float d0[32], d1[32];
-  tmem_ld_x32(taddr + 64 * s, d0);
-  tmem_ld_x32(taddr + 64 * s + 32, d1);
-  float* g = G + c * kGStride;
-  if (s == 0) {
+// Outgoing messages of one leg pair (x, y) from its environment
+// G[(ax,ay),(bx,by)] (ket row ax + 8 ay, bra column bx + 8 by; M = 64 layout:
+// warp w holds rows 16 w .. 16 w + 15 in lanes 0-15 of its TMEM quadrant):
+//   out_y[by, ay] = sum_{ax,bx} G Mx[bx, ax]  -> res_y (complete within the warp)
+//   out_x[bx, ax] = sum_{ay,by} G My[by, ay]  -> per-warp partials part[warp][ax][bx]
+__device__ __forceinline__ void pair_epilogue(uint32_t taddr, const float* Mx, const float* My, float* res_y,
+                                              float* part, int warp, int lane) {
+  const int ax = lane & 7, ay = 2 * warp + ((lane >> 3) & 1);
+  float q[8], p[8];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      g[j] = d0[j];
-      g[32 + j] = d1[j];
+  for (int i = 0; i < 8; ++i) q[i] = p[i] = 0.f;
+  float mx[8], my[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    mx[i] = Mx[i + 8 * ax];  // Mx[bx = i, ax]
+    my[i] = My[i + 8 * ay];  // My[by = i, ay]
+  }
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    float g[32];
+    tmem_ld_x32(taddr + 32 * h, g);
+#pragma unroll
+    for (int jj = 0; jj < 32; ++jj) {
+      const int bx = jj & 7, by = 4 * h + (jj >> 3);
+      q[by] = fmaf(g[jj], mx[bx], q[by]);
+      p[bx] = fmaf(g[jj], my[by], p[bx]);
     }
   }
-  __syncthreads();
-  if (s == 1) {
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      g[j] += d0[j];
-      g[32 + j] += d1[j];
-    }
+  for (int o = 1; o < 8; o <<= 1)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) q[i] += __shfl_xor_sync(0xffffffffu, q[i], o);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) p[i] += __shfl_xor_sync(0xffffffffu, p[i], 8);
+  if (lane < 16) {
+    float sel = q[0];
+#pragma unroll
+    for (int i = 1; i < 8; ++i) sel = (ax == i) ? q[i] : sel;
+    res_y[ax + 8 * ay] = sel;  // by = ax here: lane's bra index on leg y
   }
-  __syncthreads();
-}
-
-// Outgoing messages of one leg pair from its environment G[(ax,ay),(bx,by)]:
-// threads 0-63 contract the second leg with Mx (result on the first leg),
-// threads 64-127 contract the first leg with My (result on the second leg).
-__device__ __forceinline__ void env_to_out(const float* G, const float* Mx, const float* My, float* res_first,
-                                           float* res_second, int t) {
-  const int u = t & 63, bx = u & 7, ax = u >> 3;
-  float acc = 0.f;
-  if (t < 64) {
+  if (lane < 8) {
 #pragma unroll
-    for (int ay = 0; ay < 8; ++ay)
-#pragma unroll
-      for (int by = 0; by < 8; ++by) acc = fmaf(G[(ax + 8 * ay) * kGStride + bx + 8 * by], Mx[by + 8 * ay], acc);
-    res_first[u] = acc;
-  } else {
-#pragma unroll
-    for (int ay = 0; ay < 8; ++ay)
-#pragma unroll
-      for (int by = 0; by < 8; ++by) acc = fmaf(G[(ay + 8 * ax) * kGStride + by + 8 * bx], My[by + 8 * ay], acc);
-    res_second[u] = acc;
+    for (int i = 0; i < 8; ++i) part[warp * 64 + ax * 8 + i] = p[i];
   }
 }
 
@@ -196,7 +193,7 @@ __device__ __forceinline__ void env_to_out(const float* G, const float* Mx, cons
 // One CTA walks work[blockIdx.x], work[blockIdx.x + gridDim.x], ...; vertex v
 // uses image slot vslot[v] (Z at zimg + slot * 8192, offsets in recs[slot]).
 // err (device) receives GBTN_ERR_TIMEOUT when a bounded wait gives up; the CTA
-// then drains its own copies and MMAs in flight, frees its TMEM and returns.
+// then drains its own copy and MMAs in flight, frees its TMEM and returns.
 __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     tc_vertex_kernel(const int* __restrict__ work, int nwork, const int* __restrict__ vslot,
                      const TcRec* __restrict__ recs, const __nv_bfloat16* __restrict__ zimg, const float* msg_in,
@@ -204,9 +201,9 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* Z = sm + kOffZ;
-  unsigned char* KT = sm + kOffKT;  // K12 | K34, later T12, later G
+  unsigned char* KT = sm + kOffKT;  // K12 | K34, later the two T12 tiles
   unsigned char* T34 = sm + kOffT34;
-  float* G = reinterpret_cast<float*>(KT);
+  float* PART = reinterpret_cast<float*>(sm + kOffPart);
   float* MSG = reinterpret_cast<float*>(sm + kOffMsg);
   float* RES = reinterpret_cast<float*>(sm + kOffRes);
   uint64_t* mma_bar = reinterpret_cast<uint64_t*>(sm + kOffBar);
@@ -254,10 +251,6 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
       mma_pending = 0;
     }
     return ok;
-  };
-  auto commit = [&]() {
-    tc::mma_commit(mma_bar);
-    mma_pending = 1;
   };
 
   const int q0 = t, q1 = t + 128;  // this thread's entries of the 4 x 64 message block
@@ -336,7 +329,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     if (*abort_flag) break;
 
     const uint32_t zaddr = tc::smem_u32(Z), ktaddr = tc::smem_u32(KT), t34addr = tc::smem_u32(T34);
-    // ---- GEMM1 -> columns [0,64), GEMM1' -> [64,128) ----
+    // ---- GEMM1 -> columns [0,64), GEMM1' -> [64,128) (M = 128) ----
     if (t == 0) {
       tc::tc_fence_after();
 #pragma unroll
@@ -347,57 +340,52 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
       for (int kk = 0; kk < 4; ++kk)
         tc::mma_bf16(tmem + 64, tc::smem_desc(zaddr + 2048 * kk, 8192, 1024),
                      tc::smem_desc(ktaddr + 8192 + 32 * kk, 16, 1024), kIdescG1mn, kk > 0);
-      commit();
+      tc::mma_commit(mma_bar);
+      mma_pending = 1;
       *abort_flag = wait_mma() ? 0 : 1;
     }
     __syncthreads();
     if (*abort_flag) break;
     tc::tc_fence_after();
     {
+      // row t = (s, c) of D1 / D1' -> row c of tile s of T12 / T34 (K = (s, c') = 128)
+      const int s = t >> 6, c = t & 63;
       float d[32];
       tmem_ld_x32(trow + 0, d);
-      store_half_row(KT, t, 0, d);  // T12 overwrites the Kronecker products (their MMAs are done)
+      store_half_row(KT + 8192 * s, c, 0, d);  // T12 overwrites the Kronecker products (their MMAs are done)
       tmem_ld_x32(trow + 32, d);
-      store_half_row(KT, t, 4, d);
+      store_half_row(KT + 8192 * s, c, 4, d);
       tmem_ld_x32(trow + 64, d);
-      store_half_row(T34, t, 0, d);
+      store_half_row(T34 + 8192 * s, c, 0, d);
       tmem_ld_x32(trow + 96, d);
-      store_half_row(T34, t, 4, d);
+      store_half_row(T34 + 8192 * s, c, 4, d);
     }
     tc::fence_proxy_async_smem();
     tc::tc_fence_before();
     __syncthreads();
-    // ---- GEMM2 -> columns [0,128) ----
+    // ---- GEMM2 -> G34 in columns [0,64), GEMM2' -> G12 in [64,128) (M = 64, K = 128) ----
     if (t == 0) {
       tc::tc_fence_after();
 #pragma unroll
-      for (int kk = 0; kk < 4; ++kk)
-        tc::mma_bf16(tmem + 0, tc::smem_desc(ktaddr + 32 * kk, 16, 1024), tc::smem_desc(zaddr + 32 * kk, 16, 1024),
+      for (int kk = 0; kk < 8; ++kk) {
+        const uint32_t so = 8192 * (kk >> 2), ko = 32 * (kk & 3);
+        tc::mma_bf16(tmem + 0, tc::smem_desc(ktaddr + so + ko, 16, 1024), tc::smem_desc(zaddr + so + ko, 16, 1024),
                      kIdescG2, kk > 0);
-      commit();
-      *abort_flag = wait_mma() ? 0 : 1;
+      }
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) {
+        const uint32_t so = 8192 * (kk >> 2), ko = 32 * (kk & 3);
+        tc::mma_bf16(tmem + 64, tc::smem_desc(t34addr + so + ko, 16, 1024),
+                     tc::smem_desc(zaddr + 2048 * kk, 8192, 1024), kIdescG2mn, kk > 0);
+      }
+      tc::mma_commit(mma_bar);
+      mma_pending = 1;
     }
     // the next vertex's incoming messages, ahead of use
     if (nsl >= 0) {
       nm0 = msg_in[nin0 + e];
       nm1 = msg_in[nin1 + e];
     }
-    __syncthreads();
-    if (*abort_flag) break;
-    tc::tc_fence_after();
-    diag_to_env(trow, G, t);  // G34 (overwrites T12: GEMM2 is done)
-    tc::tc_fence_before();
-    __syncthreads();
-    // ---- GEMM2' -> columns [0,128), overlapped with the G34 epilogue ----
-    if (t == 0) {
-      tc::tc_fence_after();
-#pragma unroll
-      for (int kk = 0; kk < 4; ++kk)
-        tc::mma_bf16(tmem + 0, tc::smem_desc(t34addr + 32 * kk, 16, 1024),
-                     tc::smem_desc(zaddr + 2048 * kk, 8192, 1024), kIdescG2mn, kk > 0);
-      commit();
-    }
-    env_to_out(G, MSG + 192, MSG + 128, RES + 128, RES + 192, t);  // out3 (with M4), out4 (with M3)
     if (t == 0) {
       const bool ok = wait_mma();
       *abort_flag = ok ? 0 : 1;
@@ -406,9 +394,16 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     __syncthreads();
     if (*abort_flag) break;
     tc::tc_fence_after();
-    diag_to_env(trow, G, t);  // G12
-    env_to_out(G, MSG + 64, MSG, RES, RES + 64, t);  // out1 (with M2), out2 (with M1)
+    // legs (3,4): out4 complete per warp, out3 as partials; legs (1,2): out2, out1 partials
+    pair_epilogue(trow + 0, MSG + 128, MSG + 192, RES + 192, PART, warp, lane);
+    pair_epilogue(trow + 64, MSG, MSG + 64, RES + 64, PART + 256, warp, lane);
     tc::tc_fence_before();
+    __syncthreads();
+    {
+      const float* pp = PART + (t < 64 ? 0 : 256);
+      const int u = t & 63;
+      RES[(t < 64 ? 128 : 0) + u] = pp[u] + pp[64 + u] + pp[128 + u] + pp[192 + u];  // out3 | out1
+    }
     __syncthreads();
     {
       const double df = tc_finalize(RES + 64 * warp, msg_in + out_off_w, msg_out + out_off_w, normalize,
