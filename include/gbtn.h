@@ -184,6 +184,35 @@ int gbtn_rescale_messages(gbtn_plan* plan);
  * normalize.jl:77): every vertex scalar becomes 1. */
 int gbtn_rescale_partitions(gbtn_plan* plan);
 
+/* ---- energies and gradients (FP64) ------------------------------------------ */
+/* Two-site energy sum_e sum_t coef[t] <O_t (x) O_t>_e with BP reduced density
+ * matrices (the pattern of test/test_belief_propagation.jl:64-91 applied to
+ * every edge); ops holds n_terms d x d matrices O[s', s] (all vertices share d).
+ * energy[n_networks] receives each network's sum.  No counterpart to the
+ * gradient exists in the reference (it has no automatic differentiation). */
+enum gbtn_grad_mode { GBTN_GRAD_IMPLICIT = 0, GBTN_GRAD_UNROLLED = 1 };
+typedef struct gbtn_grad_opts {
+  int32_t mode;        /* IMPLICIT: through the converged messages already in the
+                          plan (adjoint BP solve); UNROLLED: through `unroll`
+                          parallel sweeps from identity messages, which also
+                          leave their messages in the plan */
+  int32_t maxiter;     /* IMPLICIT: adjoint iterations (default 500) */
+  double tol;          /* IMPLICIT: stop at |l_new - l| <= tol |l_new| (default 1e-12) */
+  int32_t unroll;      /* UNROLLED: number of sweeps */
+  int32_t checkpoint;  /* UNROLLED: keep every k-th sweep (0 = ceil(sqrt(unroll))) */
+} gbtn_grad_opts;
+int gbtn_energy2(gbtn_plan* plan, int32_t n_terms, const double* coef, const double* ops, double* energy);
+/* Energy and its gradient with respect to every site tensor (n_factor values,
+ * same layout as gbtn_set_factors).  iters / resid (may be NULL): adjoint
+ * iterations and final relative residual (IMPLICIT), or sweeps (UNROLLED). */
+int gbtn_energy2_grad(gbtn_plan* plan, int32_t n_terms, const double* coef, const double* ops,
+                      const gbtn_grad_opts* opts, double* energy, double* grad, int32_t* iters, double* resid);
+/* Vector-Jacobian product through the BP fixed point: given dL/dm for the
+ * converged messages (n_message values), the gradient dL/dA (n_factor values)
+ * by implicit differentiation (opts->mode must be IMPLICIT). */
+int gbtn_bp_vjp(gbtn_plan* plan, const double* msg_cot, const gbtn_grad_opts* opts, double* grad, int32_t* iters,
+                double* resid);
+
 /* ---- allocation-free sweep ------------------------------------------------ */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory when they need a message update (a framework capturing its stream

@@ -1,0 +1,324 @@
+// Hand-written adjoints of the BP hot path (FP64).
+//
+// The reference has no automatic differentiation; these kernels are the
+// reverse-mode rules of the forward kernels:
+//
+//  * vertex VJP.  For one vertex with ket tensor K (A_v, or O.A_v with a site
+//    operator O applied), bra A_v, incoming messages m_q and cotangents C_w of
+//    its unnormalised outgoing messages F_w = CLOSE_w(K absorbed with m_q, q != w):
+//      L = sum_w <C_w, F_w> = sum_w sum K[s,a] A[s,b] prod_q M^(w)_q[b_q, a_q],
+//      M^(w)_q = m_q (q != w), C_w (q = w);
+//      dL/dm_p  = sum_{w != p} CLOSE_p(K absorbed with M^(w)_q, q != p)
+//      dL/dK    = sum_w A absorbed with every (M^(w)_q)^T,
+//      dL/dA    = O^T dL/dK + sum_w K absorbed with every M^(w)_q.
+//  * normalisation VJP: n = f/|f|  =>  f_bar = (n_bar - <n, n_bar> n) / |f|
+//    (updated_message's division by the norm,
+//    src/caches/abstractbeliefpropagationcache.jl:234-237).
+//  * two-site energy terms: with F^O the message computed with O applied to the
+//    ket, tr(rho_e (O (x) O)) = <F^O_{u->v}, F^O_{v->u}> (Frobenius), so
+//    E = sum_e sum_t c_t <F^{O_t}_{u->v}, F^{O_t}_{v->u}> / <F^I_{u->v}, F^I_{v->u}>
+//    and its cotangents on F^{O_t} are products of the opposite messages.
+// The host side (api.cu) chains them into the implicit adjoint at the BP fixed
+// point (iterating lambda <- dE/dm + (dF/dm)^T lambda) and into backpropagation
+// through unrolled, checkpointed Jacobi sweeps.
+#include "bp_device.cuh"
+
+namespace gbtn {
+namespace {
+
+// out[v] = O . A_v on the site index (O[s', s], d x d, column-major).
+__global__ void site_op_kernel(int nv, const VDesc* __restrict__ vd, const double* __restrict__ fac,
+                               const double* __restrict__ op, double* __restrict__ out) {
+  const int v = blockIdx.x;
+  if (v >= nv) return;
+  const VDesc d = vd[v];
+  const double* a = fac + d.a_off;
+  double* o = out + d.a_off;
+  for (int i = threadIdx.x; i < d.n; i += blockDim.x) {
+    const int s = i % d.d, r = i - s;
+    double acc = 0.0;
+    for (int t = 0; t < d.d; ++t) acc += op[s + d.d * t] * a[r + t];
+    o[i] = acc;
+  }
+}
+
+// Normalisation VJP per directed edge (one warp each).
+__global__ void norm_vjp_kernel(int ndir, const int* __restrict__ dchi, const long long* __restrict__ msg_off,
+                                const double* __restrict__ f, const double* __restrict__ nbar,
+                                double* __restrict__ fbar) {
+  const int de = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (de >= ndir) return;
+  const int c2 = dchi[de] * dchi[de];
+  const long long off = msg_off[de];
+  const double f0 = lane < c2 ? f[off + lane] : 0.0, f1 = lane + 32 < c2 ? f[off + lane + 32] : 0.0;
+  const double g0 = lane < c2 ? nbar[off + lane] : 0.0, g1 = lane + 32 < c2 ? nbar[off + lane + 32] : 0.0;
+  const double nrm = sqrt(warp_sum(f0 * f0 + f1 * f1));
+  double r0 = 0.0, r1 = 0.0;
+  if (nrm > 0.0) {
+    const double inv = 1.0 / nrm;
+    const double dot = warp_sum(f0 * g0 + f1 * g1) * inv;  // <n, n_bar>
+    r0 = (g0 - dot * f0 * inv) * inv;
+    r1 = (g1 - dot * f1 * inv) * inv;
+  }
+  if (lane < c2) fbar[off + lane] = r0;
+  if (lane + 32 < c2) fbar[off + lane + 32] = r1;
+}
+
+// One CTA per vertex (256 threads); see the file comment.  mbar / abar may be
+// NULL to skip that part.  Results are accumulated (+=): mbar by incoming
+// directed edge (each one belongs to exactly one vertex), abar by tensor entry.
+constexpr int kVjpTeam = 256;
+
+__global__ void __launch_bounds__(kVjpTeam)
+    vertex_vjp_kernel(const int* __restrict__ work, int nwork, const VDesc* __restrict__ vd,
+                      const double* __restrict__ ket, const double* __restrict__ bra, const double* __restrict__ msgs,
+                      const double* __restrict__ cot, const long long* __restrict__ msg_off, const double* __restrict__ op,
+                      double* mbar, double* abar, int ncap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int TEAM = kVjpTeam;
+  const int tid = threadIdx.x;
+  VDesc* D = reinterpret_cast<VDesc*>(smem_raw);
+  double* base = reinterpret_cast<double*>(smem_raw + align_up(sizeof(VDesc), 16));
+  double* K = base;
+  double* B = K + ncap;
+  double* W[2] = {B + ncap, B + 2 * (size_t)ncap};
+  double* GK = B + 3 * (size_t)ncap;
+  double* GB = B + 4 * (size_t)ncap;
+  double* MS = B + 5 * (size_t)ncap;  // incoming messages, kMaxDeg x 64
+  double* CT = MS + kMaxDeg * 64;     // cotangents of outgoing messages, kMaxDeg x 64
+  double* MT = CT + kMaxDeg * 64;     // one transposed message
+  double* MB = MT + 64;               // accumulated incoming-message cotangents, kMaxDeg x 64
+  double* red = MB + kMaxDeg * 64;    // (TEAM/32) x kRedStride
+  double* res = red + (TEAM / 32) * kRedStride;
+  for (int w_ = blockIdx.x; w_ < nwork; w_ += gridDim.x) {
+    const int v = work[w_];
+    load_desc<TEAM>(D, vd + v, tid);
+    __syncthreads();
+    const VDesc& d = *D;
+    const int n = d.n, k = d.k;
+    for (int i = tid; i < n; i += TEAM) {
+      K[i] = ket[d.a_off + i];
+      B[i] = bra[d.a_off + i];
+      GK[i] = 0.0;
+      GB[i] = 0.0;
+    }
+    for (int p = 0; p < k; ++p) {
+      const int c2 = d.chi[p] * d.chi[p];
+      for (int i = tid; i < c2; i += TEAM) {
+        MS[p * 64 + i] = msgs[msg_off[d.in_de[p]] + i];
+        CT[p * 64 + i] = cot[msg_off[d.out_de[p]] + i];
+        MB[p * 64 + i] = 0.0;
+      }
+    }
+    __syncthreads();
+    if (mbar) {
+      for (int w = 0; w < k; ++w)
+        for (int p = 0; p < k; ++p) {
+          if (p == w) continue;
+          const double* cur = K;
+          int nx = 0;
+          for (int q = 0; q < k; ++q) {
+            if (q == p) continue;
+            absorb_any<double>(d.chi[q], cur, W[nx], n, d.st[q], q == w ? CT + w * 64 : MS + q * 64, tid, TEAM);
+            __syncthreads();
+            cur = W[nx];
+            nx ^= 1;
+          }
+          close_any<double, TEAM>(d.chi[p], cur, B, n, d.st[p], 1, 0, 0, red, res, tid);
+          for (int i = tid; i < d.chi[p] * d.chi[p]; i += TEAM) MB[p * 64 + i] += res[i];
+          __syncthreads();
+        }
+      for (int p = 0; p < k; ++p) {
+        const int c2 = d.chi[p] * d.chi[p];
+        const long long off = msg_off[d.in_de[p]];
+        for (int i = tid; i < c2; i += TEAM) mbar[off + i] += MB[p * 64 + i];
+      }
+    }
+    if (abar) {
+      for (int w = 0; w < k; ++w) {
+        // dL/dK: the bra absorbed with every transposed message
+        const double* cur = B;
+        int nx = 0;
+        for (int q = 0; q < k; ++q) {
+          const int c = d.chi[q];
+          const double* M = q == w ? CT + w * 64 : MS + q * 64;
+          for (int i = tid; i < c * c; i += TEAM) MT[(i / c) + c * (i % c)] = M[i];
+          __syncthreads();
+          absorb_any<double>(c, cur, W[nx], n, d.st[q], MT, tid, TEAM);
+          __syncthreads();
+          cur = W[nx];
+          nx ^= 1;
+        }
+        for (int i = tid; i < n; i += TEAM) GK[i] += cur[i];
+        __syncthreads();
+        // dL/dA (bra side): the ket absorbed with every message
+        cur = K;
+        for (int q = 0; q < k; ++q) {
+          absorb_any<double>(d.chi[q], cur, W[nx], n, d.st[q], q == w ? CT + w * 64 : MS + q * 64, tid, TEAM);
+          __syncthreads();
+          cur = W[nx];
+          nx ^= 1;
+        }
+        for (int i = tid; i < n; i += TEAM) GB[i] += cur[i];
+        __syncthreads();
+      }
+      // abar += O^T . GK + GB
+      for (int i = tid; i < n; i += TEAM) {
+        const int s = i % d.d, r = i - s;
+        double acc = GB[i];
+        for (int t = 0; t < d.d; ++t) acc += (op ? op[t + d.d * s] : (t == s ? 1.0 : 0.0)) * GK[r + t];
+        abar[d.a_off + i] += acc;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Per edge: t[e] = <F[2e], F[2e+1]> (one warp per edge).
+__global__ void edge_dot_kernel(int ne, const int* __restrict__ dchi, const long long* __restrict__ msg_off,
+                                const double* __restrict__ F, double* __restrict__ out) {
+  const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (e >= ne) return;
+  const int c2 = dchi[2 * e] * dchi[2 * e];
+  double s = 0.0;
+  for (int i = lane; i < c2; i += 32) s += F[msg_off[2 * e] + i] * F[msg_off[2 * e + 1] + i];
+  s = warp_sum(s);
+  if (lane == 0) out[e] = s;
+}
+
+// Cotangents of the energy on the term messages: for directed edge de of edge e,
+// C[de] = scale[e] * F[de ^ 1] (scale = c_t / t_I for an operator term,
+// -E_e / t_I for the identity term).
+__global__ void energy_cot_kernel(int ndir, const int* __restrict__ dchi, const long long* __restrict__ msg_off,
+                                  const double* __restrict__ F, const double* __restrict__ scale,
+                                  double* __restrict__ C) {
+  const int de = blockIdx.x;
+  if (de >= ndir) return;
+  const int c2 = dchi[de] * dchi[de];
+  const double sc = scale[de >> 1];
+  for (int i = threadIdx.x; i < c2; i += blockDim.x) C[msg_off[de] + i] = sc * F[msg_off[de ^ 1] + i];
+}
+
+}  // namespace
+
+namespace {
+
+// Per edge: E_e = sum_t c_t t[t][e] / t[I][e] and the cotangent scales
+// scale[t][e] = c_t / t[I][e], scale[I][e] = -E_e / t[I][e] (term 0 = identity).
+__global__ void energy_terms_kernel(int ne, int nterms, const double* __restrict__ coef, const double* __restrict__ t,
+                                    double* __restrict__ Ee, double* __restrict__ scale) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const double tI = t[e];
+  double E = 0.0;
+  for (int k = 1; k <= nterms; ++k) {
+    E += coef[k - 1] * t[(size_t)k * ne + e] / tI;
+    scale[(size_t)k * ne + e] = coef[k - 1] / tI;
+  }
+  Ee[e] = E;
+  scale[e] = -E / tI;
+}
+
+// Per network: sum of its edges' energies.
+__global__ void net_sum_kernel(const int* __restrict__ net_e_ptr, const int* __restrict__ net_e,
+                               const double* __restrict__ Ee, double* __restrict__ out) {
+  const int net = blockIdx.x;
+  double s = 0.0;
+  for (int i = net_e_ptr[net] + threadIdx.x; i < net_e_ptr[net + 1]; i += blockDim.x) s += Ee[net_e[i]];
+  __shared__ double red[32];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    out[net] = t;
+  }
+}
+
+// y = a + b (elementwise) and the squared norms of y and y - old.
+__global__ void axpy_resid_kernel(long long n, const double* __restrict__ a, const double* __restrict__ b,
+                                  const double* __restrict__ old, double* __restrict__ y, double* __restrict__ acc) {
+  double s_new = 0.0, s_diff = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = a[i] + b[i];
+    const double dlt = v - old[i];
+    y[i] = v;
+    s_new += v * v;
+    s_diff += dlt * dlt;
+  }
+  s_new = warp_sum(s_new);
+  s_diff = warp_sum(s_diff);
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&acc[0], s_new);
+    atomicAdd(&acc[1], s_diff);
+  }
+}
+
+}  // namespace
+
+size_t vertex_vjp_smem(int ncap) {
+  return align_up(sizeof(VDesc), 16) +
+         sizeof(double) * (6 * (size_t)ncap + 3 * kMaxDeg * 64 + 64 + (kVjpTeam / 32) * kRedStride + 64);
+}
+
+void launch_site_op(int nv, const VDesc* vd, const double* fac, const double* op, double* out, cudaStream_t s) {
+  site_op_kernel<<<nv, 256, 0, s>>>(nv, vd, fac, op, out);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_norm_vjp(int ndir, const int* dchi, const long long* msg_off, const double* f, const double* nbar,
+                     double* fbar, cudaStream_t s) {
+  if (ndir == 0) return;
+  norm_vjp_kernel<<<(ndir + 7) / 8, 256, 0, s>>>(ndir, dchi, msg_off, f, nbar, fbar);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_vertex_vjp(const int* work, int nwork, const VDesc* vd, const double* ket, const double* bra,
+                       const double* msgs, const double* cot, const long long* msg_off, const double* op, double* mbar,
+                       double* abar, int ncap, cudaStream_t s) {
+  if (nwork == 0) return;
+  const size_t sm = vertex_vjp_smem(ncap);
+  GBTN_CUDA(cudaFuncSetAttribute(vertex_vjp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  vertex_vjp_kernel<<<nwork, kVjpTeam, sm, s>>>(work, nwork, vd, ket, bra, msgs, cot, msg_off, op, mbar, abar, ncap);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_edge_dot(int ne, const int* dchi, const long long* msg_off, const double* F, double* out, cudaStream_t s) {
+  if (ne == 0) return;
+  edge_dot_kernel<<<(ne + 7) / 8, 256, 0, s>>>(ne, dchi, msg_off, F, out);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_energy_cot(int ndir, const int* dchi, const long long* msg_off, const double* F, const double* scale,
+                       double* C, cudaStream_t s) {
+  if (ndir == 0) return;
+  energy_cot_kernel<<<ndir, 64, 0, s>>>(ndir, dchi, msg_off, F, scale, C);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_energy_terms(int ne, int nterms, const double* coef, const double* t, double* Ee, double* scale,
+                         cudaStream_t s) {
+  if (ne == 0) return;
+  energy_terms_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, nterms, coef, t, Ee, scale);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_net_sum(int nnet, const int* net_e_ptr, const int* net_e, const double* Ee, double* out, cudaStream_t s) {
+  net_sum_kernel<<<nnet, 256, 0, s>>>(net_e_ptr, net_e, Ee, out);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_axpy_resid(long long n, const double* a, const double* b, const double* old, double* y, double* acc,
+                       cudaStream_t s) {
+  GBTN_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), s));
+  long long blocks = (n + 255) / 256;
+  if (blocks > 1216) blocks = 1216;
+  if (blocks < 1) blocks = 1;
+  axpy_resid_kernel<<<(int)blocks, 256, 0, s>>>(n, a, b, old, y, acc);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+}  // namespace gbtn

@@ -1107,3 +1107,249 @@ int gbtn_rescale_partitions(gbtn_plan* P) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Energies and gradients: chains of the adjoint kernels (adjoint.cu)
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Energy2 {
+  gbtn_plan* P;
+  int nterms = 0, d = 0;
+  DevBuf<double> ops, coef, ket, t, Ee, scale, netE;
+  std::vector<std::unique_ptr<DevBuf<double>>> F;  // F[0] identity term, F[k] term k
+  DevBuf<int> allv;
+};
+
+// Unnormalised (or normalised) messages of every directed edge computed with
+// ket tensor `ket` and bra = the plan's tensors (bra pointer NULL when ket is
+// the plan's own tensors).
+void raw_forward(gbtn_plan* P, const double* ket, const double* bra, const double* msgs, double* out, int normalize) {
+  cudaStream_t s = P->ctx->stream;
+  launch_bp_vertices<double>(P->lists[0].first, P->d_vd.p, ket, bra, msgs, out, P->d_msg_off.p, P->d_diffs.p, nullptr,
+                             normalize, 0, s);
+  launch_bp_vertices<double>(P->lists[0].second, P->d_vd.p, ket, bra, msgs, out, P->d_msg_off.p, P->d_diffs.p,
+                             nullptr, normalize, 0, s);
+}
+
+const double* term_ket(Energy2& E, int k) {
+  if (k == 0) return E.P->d_fac.p;
+  launch_site_op(E.P->nv, E.P->d_vd.p, E.P->d_fac.p, E.ops.p + (size_t)(k - 1) * E.d * E.d, E.ket.p,
+                 E.P->ctx->stream);
+  return E.ket.p;
+}
+
+void energy_setup(Energy2& E, gbtn_plan* P, int nterms, const double* coef, const double* ops) {
+  require(!P->sep_bra, "energies and gradients need bra = conj(ket) (a quadratic-form network)");
+  require(nterms >= 1 && coef && ops, "need at least one operator term");
+  cudaStream_t s = P->ctx->stream;
+  E.P = P;
+  E.nterms = nterms;
+  E.d = P->dsite[0];
+  for (int v = 0; v < P->nv; ++v) require(P->dsite[v] == E.d, "all vertices must share the site dimension of the operators");
+  const size_t need = vertex_vjp_smem(P->ncap);
+  if (need > 227 * 1024) throw Unsupported("vertex tensor too large for the adjoint kernels");
+  std::vector<double> h(ops, ops + (size_t)nterms * E.d * E.d), c(coef, coef + nterms);
+  E.ops.upload(h, s);
+  E.coef.upload(c, s);
+  E.ket.alloc(P->n_fac);
+  E.t.alloc((size_t)(nterms + 1) * std::max(P->ne, 1));
+  E.scale.alloc((size_t)(nterms + 1) * std::max(P->ne, 1));
+  E.Ee.alloc(std::max(P->ne, 1));
+  E.netE.alloc(P->nnet);
+  for (int k = 0; k <= nterms; ++k) {
+    E.F.push_back(std::make_unique<DevBuf<double>>());
+    E.F.back()->alloc(std::max<long long>(P->n_msg, 1));
+  }
+  std::vector<int> all(P->nv);
+  std::iota(all.begin(), all.end(), 0);
+  E.allv.upload(all, s);
+}
+
+// Forward energy at messages `msgs`: term messages, edge dots, per-edge energies
+// and cotangent scales, per-network sums.
+void energy_forward(Energy2& E, const double* msgs) {
+  gbtn_plan* P = E.P;
+  cudaStream_t s = P->ctx->stream;
+  for (int k = 0; k <= E.nterms; ++k) {
+    const double* ket = term_ket(E, k);
+    raw_forward(P, ket, k == 0 ? nullptr : P->d_fac.p, msgs, E.F[k]->p, 0);
+    launch_edge_dot(P->ne, P->d_dchi.p, P->d_msg_off.p, E.F[k]->p, E.t.p + (size_t)k * P->ne, s);
+  }
+  launch_energy_terms(P->ne, E.nterms, E.coef.p, E.t.p, E.Ee.p, E.scale.p, s);
+  launch_net_sum(P->nnet, P->d_net_e_ptr.p, P->d_net_e.p, E.Ee.p, E.netE.p, s);
+}
+
+// Direct part of the energy gradient at messages `msgs`: g += dE/dm, grad += dE/dA.
+void energy_direct_vjp(Energy2& E, const double* msgs, double* cot, double* g, double* grad) {
+  gbtn_plan* P = E.P;
+  cudaStream_t s = P->ctx->stream;
+  for (int k = 0; k <= E.nterms; ++k) {
+    launch_energy_cot(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, E.F[k]->p, E.scale.p + (size_t)k * P->ne, cot, s);
+    const double* ket = term_ket(E, k);
+    launch_vertex_vjp(E.allv.p, P->nv, P->d_vd.p, ket, P->d_fac.p, msgs, cot, P->d_msg_off.p,
+                      k == 0 ? nullptr : E.ops.p + (size_t)(k - 1) * E.d * E.d, g, grad, P->ncap, s);
+  }
+}
+
+// lambda = g + (dF/dm)^T lambda at the fixed point `msgs`, then grad += (dF/dA)^T lambda.
+void implicit_adjoint(gbtn_plan* P, const int* allv, const double* msgs, const double* g, double* grad, int maxiter,
+                      double tol, int32_t* iters, double* resid) {
+  cudaStream_t s = P->ctx->stream;
+  const long long nm = std::max<long long>(P->n_msg, 1);
+  DevBuf<double> fraw, fbar, lam, lam2, mbar, acc;
+  fraw.alloc(nm);
+  fbar.alloc(nm);
+  lam.alloc(nm);
+  lam2.alloc(nm);
+  mbar.alloc(nm);
+  acc.alloc(2);
+  raw_forward(P, P->d_fac.p, nullptr, msgs, fraw.p, 0);
+  GBTN_CUDA(cudaMemcpyAsync(lam.p, g, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
+  int it = 0;
+  double rel = 0.0;
+  for (it = 1; it <= maxiter; ++it) {
+    launch_norm_vjp(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, fraw.p, lam.p, fbar.p, s);
+    GBTN_CUDA(cudaMemsetAsync(mbar.p, 0, sizeof(double) * nm, s));
+    launch_vertex_vjp(allv, P->nv, P->d_vd.p, P->d_fac.p, P->d_fac.p, msgs, fbar.p, P->d_msg_off.p, nullptr, mbar.p,
+                      nullptr, P->ncap, s);
+    launch_axpy_resid(nm, g, mbar.p, lam.p, lam2.p, acc.p, s);
+    double h[2];
+    GBTN_CUDA(cudaMemcpyAsync(h, acc.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+    GBTN_CUDA(cudaStreamSynchronize(s));
+    std::swap(lam.p, lam2.p);
+    rel = h[0] > 0.0 ? std::sqrt(h[1] / h[0]) : 0.0;
+    if (!std::isfinite(rel)) throw CudaError("adjoint BP solve produced non-finite values");
+    if (rel <= tol) break;
+  }
+  if (it > maxiter) it = maxiter;
+  launch_norm_vjp(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, fraw.p, lam.p, fbar.p, s);
+  launch_vertex_vjp(allv, P->nv, P->d_vd.p, P->d_fac.p, P->d_fac.p, msgs, fbar.p, P->d_msg_off.p, nullptr, nullptr,
+                    grad, P->ncap, s);
+  if (iters) *iters = it;
+  if (resid) *resid = rel;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbtn_energy2(gbtn_plan* P, int32_t nterms, const double* coef, const double* ops, double* energy) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && energy, "NULL argument");
+  Energy2 E;
+  energy_setup(E, P, nterms, coef, ops);
+  energy_forward(E, P->d_msg[P->cur].p);
+  copy_out(P, energy, E.netE.p, sizeof(double) * P->nnet, GBTN_HOST);
+  API_CATCH(C)
+}
+
+int gbtn_energy2_grad(gbtn_plan* P, int32_t nterms, const double* coef, const double* ops, const gbtn_grad_opts* o,
+                      double* energy, double* grad, int32_t* iters, double* resid) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && o && grad, "NULL argument");
+  require(o->mode == GBTN_GRAD_IMPLICIT || o->mode == GBTN_GRAD_UNROLLED, "unknown gradient mode");
+  cudaStream_t s = P->ctx->stream;
+  Energy2 E;
+  energy_setup(E, P, nterms, coef, ops);
+  const long long nm = std::max<long long>(P->n_msg, 1);
+  DevBuf<double> g, cot, dgrad;
+  g.alloc(nm);
+  cot.alloc(nm);
+  dgrad.alloc(std::max<long long>(P->n_fac, 1));
+  GBTN_CUDA(cudaMemsetAsync(g.p, 0, sizeof(double) * nm, s));
+  GBTN_CUDA(cudaMemsetAsync(dgrad.p, 0, sizeof(double) * std::max<long long>(P->n_fac, 1), s));
+  if (o->mode == GBTN_GRAD_IMPLICIT) {
+    const double* m = P->d_msg[P->cur].p;
+    energy_forward(E, m);
+    energy_direct_vjp(E, m, cot.p, g.p, dgrad.p);
+    implicit_adjoint(P, E.allv.p, m, g.p, dgrad.p, o->maxiter > 0 ? o->maxiter : 500, o->tol > 0 ? o->tol : 1e-12,
+                     iters, resid);
+  } else {
+    const int T = o->unroll;
+    require(T >= 1, "UNROLLED needs unroll >= 1");
+    const int c = o->checkpoint > 0 ? o->checkpoint : (int)std::ceil(std::sqrt((double)T));
+    const int nck = T / c + 1;
+    std::vector<std::unique_ptr<DevBuf<double>>> ck, seg;
+    for (int j = 0; j < nck; ++j) {
+      ck.push_back(std::make_unique<DevBuf<double>>());
+      ck.back()->alloc(nm);
+    }
+    for (int j = 0; j < c; ++j) {
+      seg.push_back(std::make_unique<DevBuf<double>>());
+      seg.back()->alloc(nm);
+    }
+    DevBuf<double> cur, nxt, fraw, fbar, lam, mbar;
+    cur.alloc(nm);
+    nxt.alloc(nm);
+    fraw.alloc(nm);
+    fbar.alloc(nm);
+    lam.alloc(nm);
+    mbar.alloc(nm);
+    // forward: identity messages, T normalised Jacobi sweeps, every c-th kept
+    launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, cur.p, GBTN_INIT_IDENTITY, s);
+    GBTN_CUDA(cudaMemcpyAsync(ck[0]->p, cur.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
+    for (int t = 1; t <= T; ++t) {
+      raw_forward(P, P->d_fac.p, nullptr, cur.p, nxt.p, 1);
+      std::swap(cur.p, nxt.p);
+      if (t % c == 0 && t / c < nck)
+        GBTN_CUDA(cudaMemcpyAsync(ck[t / c]->p, cur.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
+    }
+    // the final messages stay in the plan
+    GBTN_CUDA(cudaMemcpyAsync(P->d_msg[P->cur].p, cur.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
+    energy_forward(E, cur.p);
+    energy_direct_vjp(E, cur.p, cot.p, g.p, dgrad.p);
+    GBTN_CUDA(cudaMemcpyAsync(lam.p, g.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
+    // backward, one checkpoint segment at a time
+    for (int j = (T - 1) / c; j >= 0; --j) {
+      const int t0 = j * c, t1 = std::min(T, (j + 1) * c);
+      GBTN_CUDA(cudaMemcpyAsync(seg[0]->p, ck[j]->p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
+      for (int i = 1; i < t1 - t0; ++i) raw_forward(P, P->d_fac.p, nullptr, seg[i - 1]->p, seg[i]->p, 1);
+      for (int t = t1; t > t0; --t) {
+        const double* mprev = seg[t - 1 - t0]->p;
+        raw_forward(P, P->d_fac.p, nullptr, mprev, fraw.p, 0);
+        launch_norm_vjp(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, fraw.p, lam.p, fbar.p, s);
+        GBTN_CUDA(cudaMemsetAsync(mbar.p, 0, sizeof(double) * nm, s));
+        launch_vertex_vjp(E.allv.p, P->nv, P->d_vd.p, P->d_fac.p, P->d_fac.p, mprev, fbar.p, P->d_msg_off.p, nullptr,
+                          mbar.p, dgrad.p, P->ncap, s);
+        std::swap(lam.p, mbar.p);
+      }
+    }
+    if (iters) *iters = T;
+    if (resid) *resid = 0.0;
+  }
+  if (energy) copy_out(P, energy, E.netE.p, sizeof(double) * P->nnet, GBTN_HOST);
+  copy_out(P, grad, dgrad.p, sizeof(double) * P->n_fac, GBTN_HOST);
+  API_CATCH(C)
+}
+
+int gbtn_bp_vjp(gbtn_plan* P, const double* msg_cot, const gbtn_grad_opts* o, double* grad, int32_t* iters,
+                double* resid) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && msg_cot && o && grad, "NULL argument");
+  require(o->mode == GBTN_GRAD_IMPLICIT, "gbtn_bp_vjp differentiates through the fixed point (IMPLICIT)");
+  require(!P->sep_bra, "gradients need bra = conj(ket) (a quadratic-form network)");
+  if (vertex_vjp_smem(P->ncap) > 227 * 1024) throw Unsupported("vertex tensor too large for the adjoint kernels");
+  cudaStream_t s = P->ctx->stream;
+  const long long nm = std::max<long long>(P->n_msg, 1);
+  DevBuf<double> g, dgrad;
+  DevBuf<int> allv;
+  std::vector<double> hg(msg_cot, msg_cot + P->n_msg);
+  if (hg.empty()) hg.push_back(0.0);
+  g.upload(hg, s);
+  dgrad.alloc(std::max<long long>(P->n_fac, 1));
+  GBTN_CUDA(cudaMemsetAsync(dgrad.p, 0, sizeof(double) * std::max<long long>(P->n_fac, 1), s));
+  std::vector<int> all(P->nv);
+  std::iota(all.begin(), all.end(), 0);
+  allv.upload(all, s);
+  implicit_adjoint(P, allv.p, P->d_msg[P->cur].p, g.p, dgrad.p, o->maxiter > 0 ? o->maxiter : 500,
+                   o->tol > 0 ? o->tol : 1e-12, iters, resid);
+  copy_out(P, grad, dgrad.p, sizeof(double) * P->n_fac, GBTN_HOST);
+  (void)nm;
+  API_CATCH(C)
+}
+
+}  // extern "C"

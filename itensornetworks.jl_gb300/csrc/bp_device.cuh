@@ -1,0 +1,260 @@
+// Shared-memory fiber primitives of the SIMT belief-propagation kernels
+// (ABSORB a message into one leg of a vertex tensor, CLOSE a tensor against the
+// bra on one leg), team synchronisation, warp reductions and the per-team
+// shared-memory carve-up.  Included by bp_kernels.cu and adjoint.cu.
+#pragma once
+
+#include "gbtn_internal.h"
+
+namespace gbtn {
+
+// ---------------------------------------------------------------------------
+// Device helpers
+// ---------------------------------------------------------------------------
+
+template <int TEAM>
+__device__ __forceinline__ void tsync() {
+  if constexpr (TEAM == 32)
+    __syncwarp();
+  else
+    __syncthreads();
+}
+
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+// Reduce-scatter of P2 values over a warp: afterwards lane L holds the
+// warp-wide sums of entries [L*P2/32, (L+1)*P2/32) in v[0 .. P2/32).
+template <typename T, int P2>
+__device__ __forceinline__ void warp_reduce_scatter(T (&v)[P2], int lane) {
+#pragma unroll
+  for (int step = 0; step < 5; ++step) {
+    constexpr int dummy = 0;
+    (void)dummy;
+    const int h = P2 >> (step + 1);
+    const int mask = 16 >> step;
+    const bool upper = (lane & mask) != 0;
+#pragma unroll
+    for (int i = 0; i < P2 / 2; ++i) {
+      if (i < h) {
+        T send = upper ? v[i] : v[i + h];
+        T keep = upper ? v[i + h] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, mask);
+      }
+    }
+  }
+}
+
+template <typename T, int CHI>
+__device__ __forceinline__ void absorb_fibers(const T* __restrict__ in, T* __restrict__ out, int n, int st,
+                                              const T* __restrict__ M, int tid, int nth) {
+  T m[CHI][CHI];
+#pragma unroll
+  for (int b = 0; b < CHI; ++b)
+#pragma unroll
+    for (int a = 0; a < CHI; ++a) m[b][a] = M[b + CHI * a];
+  const int nfib = n / CHI;
+  for (int f = tid; f < nfib; f += nth) {
+    const int lo = f % st;
+    const int base = lo + (f - lo) * CHI;
+    T x[CHI];
+#pragma unroll
+    for (int a = 0; a < CHI; ++a) x[a] = in[base + a * st];
+#pragma unroll
+    for (int b = 0; b < CHI; ++b) {
+      T y = T(0);
+#pragma unroll
+      for (int a = 0; a < CHI; ++a) y = fma(m[b][a], x[a], y);
+      out[base + b * st] = y;
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void absorb_any(int chi, const T* in, T* out, int n, int st, const T* M, int tid,
+                                           int nth) {
+  switch (chi) {
+    case 1: absorb_fibers<T, 1>(in, out, n, st, M, tid, nth); break;
+    case 2: absorb_fibers<T, 2>(in, out, n, st, M, tid, nth); break;
+    case 3: absorb_fibers<T, 3>(in, out, n, st, M, tid, nth); break;
+    case 4: absorb_fibers<T, 4>(in, out, n, st, M, tid, nth); break;
+    case 5: absorb_fibers<T, 5>(in, out, n, st, M, tid, nth); break;
+    case 6: absorb_fibers<T, 6>(in, out, n, st, M, tid, nth); break;
+    case 7: absorb_fibers<T, 7>(in, out, n, st, M, tid, nth); break;
+    case 8: absorb_fibers<T, 8>(in, out, n, st, M, tid, nth); break;
+    default: break;
+  }
+}
+
+constexpr int kRedStride = 64;  // per-warp slot of the close reduction (CHI <= 8)
+
+// CLOSE over fibers ff = fib_add + fib_mul*f of leg (st, CHI); result
+// res[b + CHI*a] = sum bra[base+shift+b*st] * t[base+a*st] (team-wide sum).
+template <typename T, int CHI, int TEAM>
+__device__ __forceinline__ void close_fibers(const T* __restrict__ t, const T* __restrict__ bra, int n, int st,
+                                             int fib_mul, int fib_add, int bra_shift, T* red, T* res,
+                                             int tid) {
+  constexpr int P = CHI * CHI;
+  constexpr int P2 = P <= 32 ? 32 : 64;
+  T acc[P2];
+#pragma unroll
+  for (int i = 0; i < P2; ++i) acc[i] = T(0);
+  const int nfib = n / (CHI * fib_mul);
+  for (int f = tid; f < nfib; f += TEAM) {
+    const int ff = fib_add + fib_mul * f;
+    const int lo = ff % st;
+    const int base = lo + (ff - lo) * CHI;
+    T x[CHI], y[CHI];
+#pragma unroll
+    for (int a = 0; a < CHI; ++a) {
+      x[a] = t[base + a * st];
+      y[a] = bra[base + bra_shift + a * st];
+    }
+#pragma unroll
+    for (int a = 0; a < CHI; ++a)
+#pragma unroll
+      for (int b = 0; b < CHI; ++b) acc[b + CHI * a] = fma(y[b], x[a], acc[b + CHI * a]);
+  }
+  const int lane = tid & 31, warp = tid >> 5;
+  warp_reduce_scatter<T, P2>(acc, lane);
+  constexpr int PER = P2 / 32;
+  if constexpr (TEAM == 32) {
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int o = lane * PER + j;
+      if (o < P) res[o] = acc[j];
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < PER; ++j) red[warp * kRedStride + lane * PER + j] = acc[j];
+    __syncthreads();
+    for (int o = tid; o < P; o += TEAM) {
+      T s = T(0);
+#pragma unroll
+      for (int w = 0; w < TEAM / 32; ++w) s += red[w * kRedStride + o];
+      res[o] = s;
+    }
+  }
+  tsync<TEAM>();
+}
+
+template <typename T, int TEAM>
+__device__ __forceinline__ void close_any(int chi, const T* t, const T* bra, int n, int st, int fib_mul,
+                                          int fib_add, int bra_shift, T* red, T* res, int tid) {
+  switch (chi) {
+    case 1: close_fibers<T, 1, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 2: close_fibers<T, 2, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 3: close_fibers<T, 3, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 4: close_fibers<T, 4, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 5: close_fibers<T, 5, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 6: close_fibers<T, 6, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 7: close_fibers<T, 7, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 8: close_fibers<T, 8, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    default: break;
+  }
+}
+
+// Normalise res (chi x chi) in FP64, write it to out, and (when diff != NULL)
+// return message_diff(new, old) (abstractbeliefpropagationcache.jl:32-36) on
+// lane 0.  Called by one full warp; old may alias out.
+template <typename T>
+__device__ __forceinline__ double finalize_message(const T* res, int chi, const T* old, T* out, int normalize,
+                                                   bool want_diff, int lane) {
+  const int P = chi * chi;
+  const double v0 = lane < P ? (double)res[lane] : 0.0;
+  const double v1 = lane + 32 < P ? (double)res[lane + 32] : 0.0;
+  const double nrm2 = warp_sum(v0 * v0 + v1 * v1);
+  const double sc = (normalize && nrm2 > 0.0) ? 1.0 / sqrt(nrm2) : 1.0;
+  const T n0 = (T)(v0 * sc), n1 = (T)(v1 * sc);
+  double o0 = 0.0, o1 = 0.0;
+  if (want_diff) {
+    if (lane < P) o0 = (double)old[lane];
+    if (lane + 32 < P) o1 = (double)old[lane + 32];
+  }
+  __syncwarp();
+  if (lane < P) out[lane] = n0;
+  if (lane + 32 < P) out[lane + 32] = n1;
+  double diff = 0.0;
+  if (want_diff) {
+    const double a0 = (double)n0, a1 = (double)n1;
+    const double dot = warp_sum(a0 * o0 + a1 * o1);
+    const double na = warp_sum(a0 * a0 + a1 * a1);
+    const double nb = warp_sum(o0 * o0 + o1 * o1);
+    diff = 1.0 - (dot * dot) / (na * nb);
+  }
+  return diff;
+}
+
+// Shared-memory carve-up of one team.
+template <typename T>
+struct TeamSmem {
+  VDesc* desc;
+  T* buf[kNumBufs];
+  T* bra;
+  T* msg;  // kMaxDeg x 64
+  T* red;  // (TEAM/32) x kRedStride
+  T* res;  // 64
+};
+
+__host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+template <typename T>
+__host__ __device__ inline size_t team_smem_bytes(int ncap, int nbuf, bool sep_bra, int team) {
+  size_t b = align_up(sizeof(VDesc), 16);
+  b += sizeof(T) * ((size_t)ncap * (nbuf + (sep_bra ? 1 : 0)) + kMaxDeg * 64 + (team / 32) * kRedStride + 64);
+  return align_up(b, 16);
+}
+
+template <typename T>
+__device__ __forceinline__ TeamSmem<T> carve(unsigned char* p, int ncap, int nbuf, bool sep_bra, int team) {
+  TeamSmem<T> s;
+  s.desc = reinterpret_cast<VDesc*>(p);
+  T* q = reinterpret_cast<T*>(p + align_up(sizeof(VDesc), 16));
+  for (int i = 0; i < kNumBufs; ++i) s.buf[i] = q + (size_t)ncap * (i < nbuf ? i : 0);
+  q += (size_t)ncap * nbuf;
+  if (sep_bra) {
+    s.bra = q;
+    q += ncap;
+  } else {
+    s.bra = s.buf[0];
+  }
+  s.msg = q;
+  q += kMaxDeg * 64;
+  s.red = q;
+  q += (team / 32) * kRedStride;
+  s.res = q;
+  return s;
+}
+
+template <int TEAM>
+__device__ __forceinline__ void load_desc(VDesc* dst, const VDesc* src, int tid) {
+  constexpr int W = sizeof(VDesc) / 4;
+  const int* s = reinterpret_cast<const int*>(src);
+  int* d = reinterpret_cast<int*>(dst);
+  for (int i = tid; i < W; i += TEAM) d[i] = s[i];
+}
+
+// Load the tensor (and bra) of a vertex and its incoming messages (all legs,
+// or all but skip_leg) into shared memory.
+template <typename T, int TEAM>
+__device__ __forceinline__ void load_vertex(const TeamSmem<T>& S, const T* fac, const T* bra_g, const T* msgs,
+                                            const long long* msg_off, int skip_leg, int tid) {
+  const VDesc& d = *S.desc;
+  const T* a = fac + d.a_off;
+  for (int i = tid; i < d.n; i += TEAM) S.buf[0][i] = a[i];
+  if (bra_g) {
+    const T* b = bra_g + d.a_off;
+    for (int i = tid; i < d.n; i += TEAM) S.bra[i] = b[i];
+  }
+  for (int p = 0; p < d.k; ++p) {
+    if (p == skip_leg) continue;
+    const int c2 = d.chi[p] * d.chi[p];
+    const T* m = msgs + msg_off[d.in_de[p]];
+    for (int i = tid; i < c2; i += TEAM) S.msg[p * 64 + i] = m[i];
+  }
+}
+
+}  // namespace gbtn

@@ -141,4 +141,21 @@ void launch_tc_vertices(const int* work, int nwork, const int* vslot, const TcRe
                         const float* msg_in, float* msg_out, double* diffs, const int* converged, int normalize,
                         int want_diff, int* err, cudaStream_t s);
 
+// Adjoint kernels (adjoint.cu), FP64.
+size_t vertex_vjp_smem(int ncap);
+void launch_site_op(int nv, const VDesc* vd, const double* fac, const double* op, double* out, cudaStream_t s);
+void launch_norm_vjp(int ndir, const int* dchi, const long long* msg_off, const double* f, const double* nbar,
+                     double* fbar, cudaStream_t s);
+void launch_vertex_vjp(const int* work, int nwork, const VDesc* vd, const double* ket, const double* bra,
+                       const double* msgs, const double* cot, const long long* msg_off, const double* op, double* mbar,
+                       double* abar, int ncap, cudaStream_t s);
+void launch_edge_dot(int ne, const int* dchi, const long long* msg_off, const double* F, double* out, cudaStream_t s);
+void launch_energy_cot(int ndir, const int* dchi, const long long* msg_off, const double* F, const double* scale,
+                       double* C, cudaStream_t s);
+void launch_energy_terms(int ne, int nterms, const double* coef, const double* t, double* Ee, double* scale,
+                         cudaStream_t s);
+void launch_net_sum(int nnet, const int* net_e_ptr, const int* net_e, const double* Ee, double* out, cudaStream_t s);
+void launch_axpy_resid(long long n, const double* a, const double* b, const double* old, double* y, double* acc,
+                       cudaStream_t s);
+
 }  // namespace gbtn

@@ -83,6 +83,16 @@ class BPOpts(C.Structure):
     ]
 
 
+class GradOpts(C.Structure):
+    _fields_ = [
+        ("mode", C.c_int32),
+        ("maxiter", C.c_int32),
+        ("tol", C.c_double),
+        ("unroll", C.c_int32),
+        ("checkpoint", C.c_int32),
+    ]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _D = C.POINTER(C.c_double)
@@ -116,6 +126,9 @@ SIGNATURES = {
     "gbtn_logscalar": (_I, [_P, _D, _D]),
     "gbtn_rescale_messages": (_I, [_P]),
     "gbtn_rescale_partitions": (_I, [_P]),
+    "gbtn_energy2": (_I, [_P, C.c_int32, _D, _D, _D]),
+    "gbtn_energy2_grad": (_I, [_P, C.c_int32, _D, _D, C.POINTER(GradOpts), _D, _D, _I32, _D]),
+    "gbtn_bp_vjp": (_I, [_P, _D, C.POINTER(GradOpts), _D, _I32, _D]),
     "gbtn_bp_sweep_static": (_I, [_I, C.POINTER(GraphDesc), _P, _P, _P, _P, _P]),
 }
 

@@ -211,6 +211,47 @@ class BeliefPropagationCache:
         self._c(self.lib.gbtn_expect2(self.handle, iptr(es), len(edges), dptr(op), dptr(out)))
         return out
 
+    # -- energies and gradients -----------------------------------------------
+    @staticmethod
+    def _terms(terms):
+        coef = np.ascontiguousarray([float(c) for c, _ in terms])
+        ops = np.ascontiguousarray(np.concatenate([np.asarray(o, float).reshape(-1, order="F") for _, o in terms]))
+        return coef, ops
+
+    def energy2(self, terms):
+        """sum_e sum_t c_t <O_t (x) O_t>_e over every edge (terms = [(c_t, O_t)])."""
+        coef, ops = self._terms(terms)
+        out = np.empty(self.tn.n_networks)
+        self._c(self.lib.gbtn_energy2(self.handle, len(terms), dptr(coef), dptr(ops), dptr(out)))
+        return out[0] if self.tn.n_networks == 1 else out
+
+    def energy2_grad(self, terms, mode="implicit", maxiter=500, tol=1e-12, unroll=30, checkpoint=0):
+        """(energy, [dE/dA_v]) through the converged messages ("implicit") or
+        through `unroll` Jacobi sweeps from identity messages ("unrolled")."""
+        coef, ops = self._terms(terms)
+        o = _lib.GradOpts()
+        o.mode = 0 if mode == "implicit" else 1
+        o.maxiter, o.tol, o.unroll, o.checkpoint = int(maxiter), float(tol), int(unroll), int(checkpoint)
+        e = np.empty(self.tn.n_networks)
+        g = np.empty(self.n_factor)
+        it = np.zeros(1, dtype=np.int32)
+        res = np.zeros(1)
+        self._c(self.lib.gbtn_energy2_grad(self.handle, len(terms), dptr(coef), dptr(ops), C.byref(o), dptr(e),
+                                           dptr(g), iptr(it), dptr(res)))
+        self.adjoint_iterations, self.adjoint_residual = int(it[0]), float(res[0])
+        return (e[0] if self.tn.n_networks == 1 else e), self.tn.unflat(g)
+
+    def vjp(self, msg_cot, maxiter=500, tol=1e-12):
+        """dL/dA from dL/dm at the fixed point (implicit differentiation)."""
+        mc = self.tn.flat_messages(msg_cot) if isinstance(msg_cot, (list, tuple)) else np.ascontiguousarray(msg_cot, float)
+        o = _lib.GradOpts()
+        o.mode, o.maxiter, o.tol = 0, int(maxiter), float(tol)
+        g = np.empty(self.n_factor)
+        it = np.zeros(1, dtype=np.int32)
+        res = np.zeros(1)
+        self._c(self.lib.gbtn_bp_vjp(self.handle, dptr(mc), C.byref(o), dptr(g), iptr(it), dptr(res)))
+        return self.tn.unflat(g)
+
     # -- rescaling -------------------------------------------------------------
     def rescale_messages(self):
         self._c(self.lib.gbtn_rescale_messages(self.handle))
