@@ -154,6 +154,48 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def gradient_timing(gbtn, ctx, barrier, rank, Lg=12, chig=6, reps=3):
+    """Seconds per gradient of the BP Heisenberg energy on an Lg x Lg PEPS."""
+    from gbtn.operators import HEISENBERG
+    tn = gbtn.random_network(gbtn.square_lattice(Lg, Lg, chi=chig), 77, unit_norm=True)
+    bpc = gbtn.BeliefPropagationCache(tn, ctx=ctx)
+
+    def implicit():
+        bpc.init_messages("identity")
+        bpc.update(maxiter=300, tol=1e-13, schedule="parallel", precision="mixed", refine_f64=3)
+        return bpc.energy2_grad(HEISENBERG, mode="implicit", tol=1e-10)
+
+    def unrolled():
+        return bpc.energy2_grad(HEISENBERG, mode="unrolled", unroll=30)
+
+    out = {"workload": f"heisenberg_{Lg}x{Lg}_chi{chig}_unit_norm", "unit": "s/grad"}
+    for name, fn in (("implicit", implicit), ("unrolled30", unrolled)):
+        fn()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            E, G = fn()
+        barrier()
+        out[name + "_s"] = (time.perf_counter() - t0) / reps
+        out[name + "_energy"] = float(E)
+    out["adjoint_iterations"] = bpc.adjoint_iterations
+    bpc.close()
+    if rank == 0:
+        # CPU baseline: reverse-mode autograd (FP64, all host threads) through
+        # 30 parallel sweeps of the oracle's restatement, one gradient
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import bp_autograd
+        import bp_oracle as O
+        import torch
+        g = O.square_lattice(Lg, Lg, chi=chig)
+        A = O.random_network(g, 77, unit_norm=True)
+        t0 = time.perf_counter()
+        bp_autograd.energy_and_grad(g, A, 30)
+        out["cpu_autograd_unrolled30_s"] = time.perf_counter() - t0
+        out["cpu_threads"] = torch.get_num_threads()
+    return out
+
+
 def tc_vertices_per_net(L=L):
     """Vertices of the tensor-core class (interior, degree 4) per L x L lattice."""
     return max(L - 2, 0) ** 2
@@ -276,6 +318,11 @@ def run_ours(args):
     barrier()
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
 
+    # 5. gradient of the BP energy (Heisenberg, 12x12, d=2, chi=6, unit-norm tensors):
+    #    mixed-precision BP to convergence + FP64 implicit adjoint, and the
+    #    checkpointed 30-sweep unrolled variant; seconds per full dE/dA
+    grad = gradient_timing(gbtn, ctx, barrier, rank)
+
     value = world * msgs_step / (ms_bf16 * 1e-3)
     n_tc = BATCH * tc_vertices_per_net()
     alg_flops_vertex = 4 * (2 * D * CHI ** 4 * 4 * CHI)  # k * F at k = 4
@@ -314,6 +361,7 @@ def run_ours(args):
                          "units_per_launch": n_tc, "alg_flops_per_unit": alg_flops_vertex,
                          "mma_tflops": n_tc * mma_flops_vertex / (tc_launch_ms * 1e-3) / 1e12,
                          "note": f"algorithmic FP flops of the degree-4 vertices / event-timed kernel duration, of {peak_src} bf16 peak"},
+            "gradient": grad,
             "cpu_baseline": {"value": cpu_val, "unit": "msg-updates/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": world * msgs_step / (e2e_ms * 1e-3), "unit": "msg-updates/s",

@@ -184,6 +184,31 @@ int gbtn_rescale_messages(gbtn_plan* plan);
  * normalize.jl:77): every vertex scalar becomes 1. */
 int gbtn_rescale_partitions(gbtn_plan* plan);
 
+/* ---- simple update / apply (FP64) ------------------------------------------- */
+/* Replaces: the network state updated by apply(o, psi; envs, maxdim, cutoff,
+ * normalize) (src/apply.jl:97-160, simple_update_bp :33-95) and tebd
+ * (src/tebd.jl:2-31).  Site tensors keep their current bond dimensions, which
+ * grow up to chi_max; the graph descriptor's edge_dim gives the initial ones. */
+typedef struct gbtn_su gbtn_su;
+int gbtn_su_create(gbtn_ctx* ctx, const gbtn_graph_desc* desc, int32_t chi_max, gbtn_su** out);
+int gbtn_su_destroy(gbtn_su* su);
+/* Current bond dimension of every edge. */
+int gbtn_su_edge_dims(gbtn_su* su, int32_t* dims);
+/* Tensors with the current bond dimensions, concatenated in vertex order (host). */
+int gbtn_su_set_factors(gbtn_su* su, const double* ket);
+int gbtn_su_get_factors(gbtn_su* su, double* ket, int64_t capacity);
+/* Apply two-site gates in the given order (consecutive vertex-disjoint gates
+ * run concurrently).  Gate j acts on edge edges[j] = (u, v) as a (du*dv)^2
+ * matrix, row s'_u + du*s'_v, column s_u + du*s_v; per_gate = 0 shares one
+ * gate.  envs: NULL (tebd) or 2*ne messages of chi_max^2 values each, the
+ * current chi x chi message M[b, a] of every directed edge in its leading
+ * chi*chi entries.  maxdim <= chi_max, cutoff < 0 disables the cutoff.
+ * truncerr[n_gates] and svals[n_gates * maxdim] (kept singular values, zero
+ * padded) may be NULL. */
+int gbtn_su_apply(gbtn_su* su, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
+                  const double* envs, int32_t maxdim, double cutoff, int32_t normalize, double* truncerr,
+                  double* svals);
+
 /* ---- energies and gradients (FP64) ------------------------------------------ */
 /* Two-site energy sum_e sum_t coef[t] <O_t (x) O_t>_e with BP reduced density
  * matrices (the pattern of test/test_belief_propagation.jl:64-91 applied to

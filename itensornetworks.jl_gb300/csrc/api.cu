@@ -445,6 +445,11 @@ __global__ void partition_scale_kernel(int nv, const VDesc* vd, const double* fa
   }
 }
 
+namespace gbtn {
+cudaStream_t ctx_stream(gbtn_ctx* c) { return c->stream; }
+void set_ctx_error(gbtn_ctx* c, const char* msg) { set_err(c, msg); }
+}  // namespace gbtn
+
 extern "C" {
 
 int gbtn_abi_version(void) { return GBTN_ABI_VERSION; }

@@ -1,0 +1,812 @@
+// Simple update on the GPU (FP64): apply(o, psi; envs, maxdim, cutoff) for
+// two-site gates (simple_update_bp, src/apply.jl:33-95; apply, :97-146), and
+// the gate batches of tebd (src/tebd.jl:2-31).
+//
+// One CTA (256 threads) per gate; the gates of one launch touch disjoint
+// vertices, so they commute with each other and run concurrently.  Per gate:
+//   1. sqrt / inverse-sqrt of every environment message on the other legs of
+//      both sites (Hermitian eigen-decomposition, eigenvalues below 10 eps of
+//      the total magnitude dropped -- map_eigvals, apply.jl:9-25);
+//   2. each site absorbs its sqrt environments and is QR-factorised as
+//      (other legs) x (site, bond) with Householder reflectors: psi = Q R;
+//   3. theta = R_u R_v over the bond, the gate applied on the two site indices;
+//   4. one-sided Jacobi SVD of theta (columns rotated in round-robin pairs,
+//      one warp per pair), singular values sorted in descending order;
+//   5. truncation by the rule of ITensors' svd: at most maxdim values, then drop
+//      from the tail while the discarded sum of squares stays within
+//      cutoff * sum of squares (at least one value kept); truncation error =
+//      discarded fraction;
+//   6. psi_u = Q_u U sqrt(S), psi_v = Q_v (sqrt(S) V^T)^T, inverse-sqrt
+//      environments absorbed back, optional normalisation.
+// Site tensors live in fixed-capacity slots (chi_max per leg) holding the
+// current shape column-major (site index first); bond dimensions are a device
+// array updated by the gate that changes them.
+#include <math.h>
+
+#include <algorithm>
+#include <memory>
+#include <numeric>
+#include <vector>
+
+#include "bp_device.cuh"
+
+namespace gbtn {
+namespace {
+
+constexpr int kSuThreads = 256;
+constexpr int kSuWarps = kSuThreads / 32;
+constexpr int kSuMaxN = 8192;     // elements of one site tensor
+constexpr int kSuMaxTheta = 64;   // rows / columns of theta
+constexpr int kSvdMaxSweeps = 40;
+
+__device__ __forceinline__ double block_sum(double x, double* red) {
+  x = warp_sum(x);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = x;
+  __syncthreads();
+  double t = 0.0;
+#pragma unroll
+  for (int i = 0; i < kSuWarps; ++i) t += red[i];
+  __syncthreads();
+  return t;
+}
+
+// One-sided Jacobi SVD of A (m x n, column-major, lda = m, m <= 64, n <= 64).
+// On return: columns of A hold U (unit columns, zero where sigma = 0), V (n x n,
+// ldv = n) the right singular vectors, sig[n] the singular values, all sorted
+// in descending order of sig.  work: >= m*n + n*n doubles, ord: n ints.
+__device__ void cta_svd(double* A, int m, int n, double* V, double* sig, double* work, int* ord, int* flag) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < n * n; i += kSuThreads) V[i] = (i % n == i / n) ? 1.0 : 0.0;
+  const int N = n + (n & 1);  // players of the round-robin (one dummy when n is odd)
+  __syncthreads();
+  for (int sweep = 0; sweep < kSvdMaxSweeps; ++sweep) {
+    if (tid == 0) *flag = 0;
+    __syncthreads();
+    for (int r = 0; r < N - 1; ++r) {
+      for (int pi = warp; pi < N / 2; pi += kSuWarps) {
+        int p, q;
+        if (pi == 0) {
+          p = N - 1;
+          q = r;
+        } else {
+          p = (r + pi) % (N - 1);
+          q = (r - pi + N - 1) % (N - 1);
+        }
+        if (p >= n || q >= n) continue;
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
+        }
+        double* a = A + (size_t)p * m;
+        double* b = A + (size_t)q * m;
+        double al = 0.0, be = 0.0, ga = 0.0;
+        for (int i = lane; i < m; i += 32) {
+          al += a[i] * a[i];
+          be += b[i] * b[i];
+          ga += a[i] * b[i];
+        }
+        al = warp_sum(al);
+        be = warp_sum(be);
+        ga = warp_sum(ga);
+        if (ga == 0.0 || fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
+        if (lane == 0) *flag = 1;
+        const double zeta = (be - al) / (2.0 * ga);
+        const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+        for (int i = lane; i < m; i += 32) {
+          const double x = a[i], y = b[i];
+          a[i] = c * x - s * y;
+          b[i] = s * x + c * y;
+        }
+        double* va = V + (size_t)p * n;
+        double* vb = V + (size_t)q * n;
+        for (int i = lane; i < n; i += 32) {
+          const double x = va[i], y = vb[i];
+          va[i] = c * x - s * y;
+          vb[i] = s * x + c * y;
+        }
+      }
+      __syncthreads();
+    }
+    if (*flag == 0) break;
+    __syncthreads();
+  }
+  // column norms, descending order, normalised U
+  for (int j = warp; j < n; j += kSuWarps) {
+    double s2 = 0.0;
+    for (int i = lane; i < m; i += 32) s2 += A[(size_t)j * m + i] * A[(size_t)j * m + i];
+    s2 = warp_sum(s2);
+    if (lane == 0) sig[j] = sqrt(s2);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int j = 0; j < n; ++j) ord[j] = j;
+    for (int i = 1; i < n; ++i) {  // insertion sort, descending, stable
+      const int x = ord[i];
+      int j = i - 1;
+      while (j >= 0 && sig[ord[j]] < sig[x]) {
+        ord[j + 1] = ord[j];
+        --j;
+      }
+      ord[j + 1] = x;
+    }
+  }
+  __syncthreads();
+  double* U2 = work;
+  double* V2 = work + (size_t)m * n;
+  for (int i = tid; i < m * n; i += kSuThreads) {
+    const int j = i / m, row = i % m, src = ord[j];
+    const double sg = sig[src];
+    U2[i] = sg > 0.0 ? A[(size_t)src * m + row] / sg : 0.0;
+  }
+  for (int i = tid; i < n * n; i += kSuThreads) V2[i] = V[(size_t)ord[i / n] * n + (i % n)];
+  __syncthreads();
+  for (int i = tid; i < m * n; i += kSuThreads) A[i] = U2[i];
+  for (int i = tid; i < n * n; i += kSuThreads) V[i] = V2[i];
+  if (tid == 0) {
+    double* ss = work;  // reuse: sorted values
+    for (int j = 0; j < n; ++j) ss[j] = sig[ord[j]];
+    for (int j = 0; j < n; ++j) sig[j] = ss[j];
+  }
+  __syncthreads();
+}
+
+// Householder QR of M (m x n column-major, lda = m): R (r x n, ldr = r) and
+// Q (m x r, ldq = m), r = min(m, n).  M is overwritten; beta: >= n doubles.
+__device__ void cta_qr(double* M, int m, int n, double* R, double* Q, double* beta, double* red) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int r = m < n ? m : n;
+  for (int j = 0; j < r; ++j) {
+    double* x = M + (size_t)j * m;
+    double s2 = 0.0;
+    for (int i = j + tid; i < m; i += kSuThreads) s2 += x[i] * x[i];
+    s2 = block_sum(s2, red);
+    const double x0 = x[j];
+    const double nrm = sqrt(s2);
+    const double alpha = x0 >= 0.0 ? -nrm : nrm;
+    const double v0 = x0 - alpha;
+    const double vn2 = s2 - x0 * x0 + v0 * v0;
+    const double bj = (vn2 > 0.0 && nrm > 0.0) ? 2.0 / vn2 : 0.0;
+    __syncthreads();
+    if (tid == 0) {
+      x[j] = v0;  // the reflector v occupies x[j..m)
+      beta[j] = bj;
+      R[j + (size_t)r * j] = bj > 0.0 ? alpha : x0;
+    }
+    __syncthreads();
+    if (bj > 0.0) {
+      for (int c = j + 1 + warp; c < n; c += kSuWarps) {
+        double* y = M + (size_t)c * m;
+        double w = 0.0;
+        for (int i = j + lane; i < m; i += 32) w += x[i] * y[i];
+        w = warp_sum(w) * bj;
+        for (int i = j + lane; i < m; i += 32) y[i] -= w * x[i];
+      }
+    }
+    __syncthreads();
+  }
+  // R: upper triangle (diagonal set above), rest from M
+  for (int i = tid; i < r * n; i += kSuThreads) {
+    const int row = i % r, col = i / r;
+    if (col > row) R[i] = M[(size_t)col * m + row];
+    else if (col < row) R[i] = 0.0;
+  }
+  // Q = H_0 ... H_{r-1} [I; 0]
+  for (int i = tid; i < m * r; i += kSuThreads) Q[i] = (i % m == i / m) ? 1.0 : 0.0;
+  __syncthreads();
+  for (int j = r - 1; j >= 0; --j) {
+    const double bj = beta[j];
+    if (bj == 0.0) continue;
+    const double* x = M + (size_t)j * m;
+    for (int c = warp; c < r; c += kSuWarps) {
+      double* y = Q + (size_t)c * m;
+      double w = 0.0;
+      for (int i = j + lane; i < m; i += 32) w += x[i] * y[i];
+      w = warp_sum(w) * bj;
+      for (int i = j + lane; i < m; i += 32) y[i] -= w * x[i];
+    }
+    __syncthreads();
+  }
+}
+
+// sqrt(env) and inverse sqrt(env) of a symmetric chi x chi message through its
+// eigen-decomposition (the singular vectors of a positive semi-definite
+// matrix), dropping the smallest eigenvalues while their summed magnitude is
+// within 10 eps of the total.  S, Si: chi x chi column-major.
+__device__ void cta_env_sqrt(const double* env, int chi, double* S, double* Si, double* A, double* V, double* sig,
+                             double* work, int* ord, int* flag) {
+  const int tid = threadIdx.x;
+  for (int i = tid; i < chi * chi; i += kSuThreads) {
+    const int b = i % chi, a = i / chi;
+    A[i] = 0.5 * (env[b + chi * a] + env[a + chi * b]);
+  }
+  __syncthreads();
+  cta_svd(A, chi, chi, V, sig, work, ord, flag);
+  __shared__ int s_keep;
+  if (tid == 0) {
+    double tot = 0.0;
+    for (int j = 0; j < chi; ++j) tot += sig[j];
+    if (tot == 0.0) tot = 1.0;
+    int k = chi;
+    double disc = 0.0;
+    while (k > 1 && disc + sig[k - 1] <= 10.0 * 2.220446049250313e-16 * tot) {
+      disc += sig[k - 1];
+      --k;
+    }
+    s_keep = k;
+  }
+  __syncthreads();
+  const int k = s_keep;
+  for (int i = tid; i < chi * chi; i += kSuThreads) {
+    const int b = i % chi, a = i / chi;
+    double s = 0.0, si = 0.0;
+    for (int j = 0; j < k; ++j) {
+      const double vv = V[b + chi * j] * V[a + chi * j];
+      const double r = sqrt(sig[j]);
+      s += vv * r;
+      si += vv / r;
+    }
+    S[i] = s;
+    Si[i] = si;
+  }
+  __syncthreads();
+}
+
+}  // namespace
+}  // namespace gbtn
+
+namespace gbtn {
+namespace {
+
+struct SuJob {
+  int e, u, v, pu, pv;
+};
+
+struct SuArgs {
+  const SuJob* jobs;
+  int njobs;
+  const int* leg_ptr;
+  const int* leg_edge;
+  const int* edge_u;
+  const int* site_dim;
+  int* edim;                 // current bond dimensions (updated)
+  const long long* cap_off;  // slot of every vertex
+  double* tens;              // capacity storage
+  const double* envs;        // NULL or 2*ne messages of chi_max^2 each (compact chi x chi)
+  const double* gates;
+  long long gate_stride;     // 0: one gate for all jobs
+  int maxdim;
+  double cutoff;
+  int normalize;
+  int chimax;
+  double* qscratch;          // 2 * kSuMaxN doubles per job
+  double* truncerr;          // [njobs] or NULL
+  double* svals;             // [njobs * maxdim] or NULL
+  int* status;               // set to 1 when a shape exceeds the kernel limits
+};
+
+struct SideShape {
+  int d, k, n, p;   // site dim, links, elements, leg of the bond
+  int chi[kMaxDeg];
+  int m;            // product of the other legs' dims
+};
+
+__device__ void side_shape(const SuArgs& a, int x, int p, SideShape& sh) {
+  sh.d = a.site_dim[x];
+  sh.k = a.leg_ptr[x + 1] - a.leg_ptr[x];
+  sh.p = p;
+  int n = sh.d, m = 1;
+  for (int q = 0; q < sh.k; ++q) {
+    sh.chi[q] = a.edim[a.leg_edge[a.leg_ptr[x] + q]];
+    n *= sh.chi[q];
+    if (q != p) m *= sh.chi[q];
+  }
+  sh.n = n;
+  sh.m = m;
+}
+
+// element idx of a tensor with dims (d, chi[0..k)) -> (row over the other legs, site s, bond index)
+__device__ __forceinline__ void split_index(const SideShape& sh, const int* chi, int idx, int& row, int& s, int& b) {
+  s = idx % sh.d;
+  int rest = idx / sh.d, rs = 1;
+  row = 0;
+  b = 0;
+  for (int q = 0; q < sh.k; ++q) {
+    const int l = rest % chi[q];
+    rest /= chi[q];
+    if (q == sh.p) {
+      b = l;
+    } else {
+      row += l * rs;
+      rs *= chi[q];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
+  extern __shared__ __align__(16) double smem[];
+  double* T = smem;                       // kSuMaxN
+  double* W = T + kSuMaxN;                // kSuMaxN
+  double* TH = W + kSuMaxN;               // 64 x 64
+  double* V = TH + kSuMaxTheta * kSuMaxTheta;  // 64 x 64
+  double* RU = V + kSuMaxTheta * kSuMaxTheta;  // 32 x 32
+  double* RV = RU + 1024;                 // 32 x 32
+  double* SI = RV + 1024;                 // 2 sides x kMaxDeg x 64 inverse-sqrt environments
+  double* S = SI + 2 * kMaxDeg * 64;      // 64
+  double* sig = S + 64;                   // 64
+  double* beta = sig + 64;                // 64
+  double* red = beta + 64;                // 32
+  int* ord = reinterpret_cast<int*>(red + 32);  // 64
+  __shared__ int s_flag, s_k, s_ok;
+  __shared__ double s_scale;
+  const int tid = threadIdx.x;
+  const int j = blockIdx.x;
+  if (j >= a.njobs) return;
+  const SuJob job = a.jobs[j];
+  SideShape sh[2];
+  side_shape(a, job.u, job.pu, sh[0]);
+  side_shape(a, job.v, job.pv, sh[1]);
+  const int ce = sh[0].chi[job.pu];
+  if (tid == 0) {
+    int ok = sh[0].n <= kSuMaxN && sh[1].n <= kSuMaxN;
+    for (int x = 0; x < 2; ++x) ok = ok && sh[x].d * ce <= 32 && sh[x].k <= kMaxDeg;
+    const int ru = min(sh[0].m, sh[0].d * ce), rv = min(sh[1].m, sh[1].d * ce);
+    ok = ok && ru * sh[0].d <= kSuMaxTheta && rv * sh[1].d <= kSuMaxTheta;
+    s_ok = ok;
+    if (!ok) atomicExch(a.status, 1);
+  }
+  __syncthreads();
+  if (!s_ok) return;
+  double* R[2] = {RU, RV};
+  int r[2];
+  const int xs[2] = {job.u, job.v};
+  for (int side = 0; side < 2; ++side) {
+    const SideShape& h = sh[side];
+    const int x = xs[side];
+    const double* src = a.tens + a.cap_off[x];
+    for (int i = tid; i < h.n; i += kSuThreads) T[i] = src[i];
+    __syncthreads();
+    double* cur = T;
+    double* nxt = W;
+    int st = h.d;
+    for (int q = 0; q < h.k; ++q) {
+      if (q != h.p && a.envs) {
+        const int f = a.leg_edge[a.leg_ptr[x] + q];
+        const int de_in = a.edge_u[f] == x ? 2 * f + 1 : 2 * f;
+        const double* env = a.envs + (size_t)de_in * a.chimax * a.chimax;
+        cta_env_sqrt(env, h.chi[q], S, SI + (side * kMaxDeg + q) * 64, TH, V, sig, nxt, ord, &s_flag);
+        absorb_any<double>(h.chi[q], cur, nxt, h.n, st, S, tid, kSuThreads);
+        __syncthreads();
+        double* t = cur;
+        cur = nxt;
+        nxt = t;
+      }
+      st *= h.chi[q];
+    }
+    // matricise: M[row, s + d * bond] (rows = other legs), into the free buffer
+    const int ncol = h.d * ce;
+    for (int i = tid; i < h.n; i += kSuThreads) {
+      int row, s, b;
+      split_index(h, h.chi, i, row, s, b);
+      nxt[row + (size_t)h.m * (s + h.d * b)] = cur[i];
+    }
+    __syncthreads();
+    r[side] = min(h.m, ncol);
+    cta_qr(nxt, h.m, ncol, R[side], cur, beta, red);  // Q into cur
+    double* qs = a.qscratch + ((size_t)j * 2 + side) * kSuMaxN;
+    for (int i = tid; i < h.m * r[side]; i += kSuThreads) qs[i] = cur[i];
+    __syncthreads();
+  }
+  // theta[(ru, su), (sv, rv)] = sum_e Ru[ru, su + du e] Rv[rv, sv + dv e], then the gate
+  const int du = sh[0].d, dv = sh[1].d, ru = r[0], rv = r[1];
+  const int mt = ru * du, nt = dv * rv;
+  for (int i = tid; i < mt * nt; i += kSuThreads) {
+    const int row = i % mt, col = i / mt;
+    const int iu = row % ru, su = row / ru, sv = col % dv, iv = col / dv;
+    double acc = 0.0;
+    for (int e = 0; e < ce; ++e) acc += RU[iu + ru * (su + du * e)] * RV[iv + rv * (sv + dv * e)];
+    W[i] = acc;
+  }
+  __syncthreads();
+  const double* G = a.gates + (size_t)a.gate_stride * j;
+  const int D = du * dv;
+  for (int i = tid; i < mt * nt; i += kSuThreads) {
+    const int row = i % mt, col = i / mt;
+    const int iu = row % ru, spu = row / ru, spv = col % dv, iv = col / dv;
+    double acc = 0.0;
+    for (int sv = 0; sv < dv; ++sv)
+      for (int su = 0; su < du; ++su)
+        acc += G[(spu + du * spv) + D * (su + du * sv)] * W[(iu + ru * su) + mt * (sv + dv * iv)];
+    TH[i] = acc;
+  }
+  __syncthreads();
+  cta_svd(TH, mt, nt, V, sig, W, ord, &s_flag);
+  if (tid == 0) {
+    // ITensors truncation of p = sigma^2 (descending): maxdim, then relative cutoff
+    const int nsv = min(mt, nt);
+    int n = nsv;
+    double te = 0.0, scale = 0.0;
+    for (int i = 0; i < nsv; ++i) scale += sig[i] * sig[i];
+    if (a.maxdim > 0)
+      while (n > a.maxdim) {
+        te += sig[n - 1] * sig[n - 1];
+        --n;
+      }
+    if (scale == 0.0) scale = 1.0;
+    if (a.cutoff >= 0.0)
+      while (n > 1 && te + sig[n - 1] * sig[n - 1] <= a.cutoff * scale) {
+        te += sig[n - 1] * sig[n - 1];
+        --n;
+      }
+    if (n < 1) n = 1;
+    s_k = n;
+    if (a.truncerr) a.truncerr[j] = te / scale;
+    if (a.svals)
+      for (int i = 0; i < a.maxdim; ++i) a.svals[(size_t)j * a.maxdim + i] = i < n ? sig[i] : 0.0;
+  }
+  __syncthreads();
+  const int kk = s_k;
+  // reassemble both sites with the new bond dimension kk
+  for (int side = 0; side < 2; ++side) {
+    SideShape h = sh[side];
+    const int x = xs[side];
+    int chi2[kMaxDeg];
+    for (int q = 0; q < h.k; ++q) chi2[q] = h.chi[q];
+    chi2[h.p] = kk;
+    int n2 = h.d;
+    for (int q = 0; q < h.k; ++q) n2 *= chi2[q];
+    const double* qs = a.qscratch + ((size_t)j * 2 + side) * kSuMaxN;
+    for (int i = tid; i < h.m * r[side]; i += kSuThreads) T[i] = qs[i];
+    __syncthreads();
+    for (int i = tid; i < n2; i += kSuThreads) {
+      int row, s, b;
+      split_index(h, chi2, i, row, s, b);
+      const double sq = sqrt(sig[b]);
+      double acc = 0.0;
+      if (side == 0) {
+        for (int t = 0; t < ru; ++t) acc += T[row + (size_t)h.m * t] * TH[(t + ru * s) + (size_t)mt * b];
+      } else {
+        for (int t = 0; t < rv; ++t) acc += T[row + (size_t)h.m * t] * V[(s + dv * t) + (size_t)nt * b];
+      }
+      W[i] = acc * sq;
+    }
+    __syncthreads();
+    double* cur = W;
+    double* nxt = T;
+    int st = h.d;
+    for (int q = 0; q < h.k; ++q) {
+      if (q != h.p && a.envs) {
+        const int c = chi2[q];
+        const double* si = SI + (side * kMaxDeg + q) * 64;
+        for (int i = tid; i < c * c; i += kSuThreads) S[(i / c) + c * (i % c)] = si[i];  // transpose
+        __syncthreads();
+        absorb_any<double>(c, cur, nxt, n2, st, S, tid, kSuThreads);
+        __syncthreads();
+        double* t = cur;
+        cur = nxt;
+        nxt = t;
+      }
+      st *= chi2[q];
+    }
+    if (a.normalize) {
+      double s2 = 0.0;
+      for (int i = tid; i < n2; i += kSuThreads) s2 += cur[i] * cur[i];
+      s2 = block_sum(s2, red);
+      if (tid == 0) s_scale = s2 > 0.0 ? 1.0 / sqrt(s2) : 1.0;
+      __syncthreads();
+    } else if (tid == 0) {
+      s_scale = 1.0;
+    }
+    __syncthreads();
+    double* dst = a.tens + a.cap_off[x];
+    for (int i = tid; i < n2; i += kSuThreads) dst[i] = cur[i] * s_scale;
+    __syncthreads();
+  }
+  if (tid == 0) a.edim[job.e] = kk;
+}
+
+}  // namespace
+}  // namespace gbtn
+
+namespace gbtn {
+
+constexpr int kSuMaxNHost = kSuMaxN;
+
+size_t su_smem_bytes() {
+  return sizeof(double) * (2 * (size_t)kSuMaxN + 2 * (size_t)kSuMaxTheta * kSuMaxTheta + 2 * 1024 +
+                           2 * kMaxDeg * 64 + 64 * 3 + 32) +
+         sizeof(int) * 64;
+}
+
+void su_prepare(size_t smem) {
+  GBTN_CUDA(cudaFuncSetAttribute(su_gate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+}
+
+void su_launch(const SuArgs& a, size_t smem, cudaStream_t s) {
+  if (a.njobs == 0) return;
+  su_gate_kernel<<<a.njobs, kSuThreads, smem, s>>>(a);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+}  // namespace gbtn
+
+// ---------------------------------------------------------------------------
+// Host side: the simple-update state and its C ABI
+// ---------------------------------------------------------------------------
+
+struct gbtn_su {
+  gbtn_ctx* ctx = nullptr;
+  cudaStream_t stream = nullptr;
+  int nv = 0, ne = 0, chimax = 0;
+  std::vector<int> eu, ev, leg_ptr, leg_edge, dsite, edim;
+  std::vector<long long> cap_off;
+  long long cap_total = 0;
+  int *d_leg_ptr = nullptr, *d_leg_edge = nullptr, *d_edge_u = nullptr, *d_dsite = nullptr, *d_edim = nullptr;
+  int* d_status = nullptr;
+  long long* d_cap_off = nullptr;
+  double* d_tens = nullptr;
+  ~gbtn_su() {
+    for (void* p : {(void*)d_leg_ptr, (void*)d_leg_edge, (void*)d_edge_u, (void*)d_dsite, (void*)d_edim,
+                    (void*)d_status, (void*)d_cap_off, (void*)d_tens})
+      if (p) cudaFree(p);
+  }
+};
+
+namespace gbtn {
+cudaStream_t ctx_stream(gbtn_ctx* c);
+void set_ctx_error(gbtn_ctx* c, const char* msg);
+}  // namespace gbtn
+
+namespace {
+
+template <typename T>
+T* dev_upload(const std::vector<T>& h, cudaStream_t s) {
+  T* p = nullptr;
+  GBTN_CUDA(cudaMalloc(&p, std::max<size_t>(h.size(), 1) * sizeof(T)));
+  if (!h.empty()) GBTN_CUDA(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return p;
+}
+
+long long su_size(const gbtn_su* S, int v) {
+  long long n = S->dsite[v];
+  for (int q = S->leg_ptr[v]; q < S->leg_ptr[v + 1]; ++q) n *= S->edim[S->leg_edge[q]];
+  return n;
+}
+
+void su_pull_dims(gbtn_su* S) {
+  GBTN_CUDA(cudaMemcpyAsync(S->edim.data(), S->d_edim, sizeof(int) * S->ne, cudaMemcpyDeviceToHost, S->stream));
+  GBTN_CUDA(cudaStreamSynchronize(S->stream));
+}
+
+int su_fail(gbtn_su* S, int code, const char* msg) {
+  if (S && S->ctx) gbtn::set_ctx_error(S->ctx, msg);
+  return code;
+}
+
+}  // namespace
+
+using gbtn::SuArgs;
+using gbtn::SuJob;
+
+extern "C" {
+
+int gbtn_su_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, int32_t chi_max, gbtn_su** out) {
+  if (!ctx || !g || !out) return GBTN_ERR_INVALID;
+  *out = nullptr;
+  try {
+    auto S = std::make_unique<gbtn_su>();
+    S->ctx = ctx;
+    S->stream = gbtn::ctx_stream(ctx);
+    S->nv = g->nv;
+    S->ne = g->ne;
+    S->chimax = chi_max;
+    if (g->nv < 1 || g->ne < 0 || chi_max < 1 || chi_max > gbtn::kMaxChi)
+      return su_fail(S.get(), GBTN_ERR_INVALID, "simple update: need nv >= 1 and 1 <= chi_max <= 8");
+    S->eu.assign(g->edge_u, g->edge_u + g->ne);
+    S->ev.assign(g->edge_v, g->edge_v + g->ne);
+    S->edim.assign(g->edge_dim, g->edge_dim + g->ne);
+    S->dsite.assign(g->site_dim, g->site_dim + g->nv);
+    S->leg_ptr.assign(g->leg_ptr, g->leg_ptr + g->nv + 1);
+    S->leg_edge.assign(g->leg_edge, g->leg_edge + S->leg_ptr[g->nv]);
+    for (int e = 0; e < g->ne; ++e)
+      if (S->edim[e] < 1 || S->edim[e] > chi_max || S->eu[e] == S->ev[e] || S->eu[e] < 0 || S->ev[e] < 0 ||
+          S->eu[e] >= g->nv || S->ev[e] >= g->nv)
+        return su_fail(S.get(), GBTN_ERR_INVALID, "simple update: bad edge or bond dimension above chi_max");
+    S->cap_off.resize(g->nv);
+    long long off = 0;
+    for (int v = 0; v < g->nv; ++v) {
+      const int k = S->leg_ptr[v + 1] - S->leg_ptr[v];
+      if (k > gbtn::kMaxDeg || S->dsite[v] < 1 || S->dsite[v] > gbtn::kMaxSite)
+        return su_fail(S.get(), GBTN_ERR_UNSUPPORTED, "simple update: degree above 8 or site dimension above 8");
+      long long cap = S->dsite[v];
+      for (int q = 0; q < k; ++q) cap *= chi_max;
+      S->cap_off[v] = off;
+      off += (cap + 31) / 32 * 32;
+    }
+    S->cap_total = off;
+    S->d_leg_ptr = dev_upload(S->leg_ptr, S->stream);
+    S->d_leg_edge = dev_upload(S->leg_edge, S->stream);
+    S->d_edge_u = dev_upload(S->eu, S->stream);
+    S->d_dsite = dev_upload(S->dsite, S->stream);
+    S->d_edim = dev_upload(S->edim, S->stream);
+    S->d_cap_off = dev_upload(S->cap_off, S->stream);
+    std::vector<int> zero(1, 0);
+    S->d_status = dev_upload(zero, S->stream);
+    GBTN_CUDA(cudaMalloc(&S->d_tens, sizeof(double) * std::max<long long>(S->cap_total, 1)));
+    GBTN_CUDA(cudaMemsetAsync(S->d_tens, 0, sizeof(double) * std::max<long long>(S->cap_total, 1), S->stream));
+    GBTN_CUDA(cudaStreamSynchronize(S->stream));
+    *out = S.release();
+    return GBTN_OK;
+  } catch (const std::exception& e) {
+    gbtn::set_ctx_error(ctx, e.what());
+    return GBTN_ERR_CUDA;
+  }
+}
+
+int gbtn_su_destroy(gbtn_su* S) {
+  if (!S) return GBTN_OK;
+  cudaStreamSynchronize(S->stream);
+  delete S;
+  return GBTN_OK;
+}
+
+int gbtn_su_edge_dims(gbtn_su* S, int32_t* dims) {
+  if (!S || !dims) return GBTN_ERR_INVALID;
+  try {
+    su_pull_dims(S);
+  } catch (const std::exception& e) {
+    return su_fail(S, GBTN_ERR_CUDA, e.what());
+  }
+  std::copy(S->edim.begin(), S->edim.end(), dims);
+  return GBTN_OK;
+}
+
+// Tensors with the current bond dimensions, concatenated in vertex order.
+int gbtn_su_set_factors(gbtn_su* S, const double* ket) {
+  if (!S || !ket) return GBTN_ERR_INVALID;
+  try {
+    su_pull_dims(S);
+    long long off = 0;
+    for (int v = 0; v < S->nv; ++v) {
+      const long long n = su_size(S, v);
+      GBTN_CUDA(cudaMemcpyAsync(S->d_tens + S->cap_off[v], ket + off, sizeof(double) * n, cudaMemcpyHostToDevice,
+                                S->stream));
+      off += n;
+    }
+    GBTN_CUDA(cudaStreamSynchronize(S->stream));
+  } catch (const std::exception& e) {
+    return su_fail(S, GBTN_ERR_CUDA, e.what());
+  }
+  return GBTN_OK;
+}
+
+int gbtn_su_get_factors(gbtn_su* S, double* ket, int64_t capacity) {
+  if (!S || !ket) return GBTN_ERR_INVALID;
+  try {
+    su_pull_dims(S);
+    long long tot = 0;
+    for (int v = 0; v < S->nv; ++v) tot += su_size(S, v);
+    if (tot > capacity) return su_fail(S, GBTN_ERR_INVALID, "simple update: output buffer too small");
+    long long off = 0;
+    for (int v = 0; v < S->nv; ++v) {
+      const long long n = su_size(S, v);
+      GBTN_CUDA(cudaMemcpyAsync(ket + off, S->d_tens + S->cap_off[v], sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                S->stream));
+      off += n;
+    }
+    GBTN_CUDA(cudaStreamSynchronize(S->stream));
+  } catch (const std::exception& e) {
+    return su_fail(S, GBTN_ERR_CUDA, e.what());
+  }
+  return GBTN_OK;
+}
+
+int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
+                  const double* envs, int32_t maxdim, double cutoff, int32_t normalize, double* truncerr,
+                  double* svals) {
+  if (!S || n_gates < 0 || (n_gates > 0 && (!edges || !gates))) return GBTN_ERR_INVALID;
+  if (n_gates == 0) return GBTN_OK;
+  try {
+    cudaStream_t s = S->stream;
+    int D = 0;
+    std::vector<SuJob> jobs(n_gates);
+    for (int j = 0; j < n_gates; ++j) {
+      const int e = edges[j];
+      if (e < 0 || e >= S->ne) return su_fail(S, GBTN_ERR_INVALID, "simple update: edge out of range");
+      SuJob jb{e, S->eu[e], S->ev[e], -1, -1};
+      for (int q = S->leg_ptr[jb.u]; q < S->leg_ptr[jb.u + 1]; ++q)
+        if (S->leg_edge[q] == e) jb.pu = q - S->leg_ptr[jb.u];
+      for (int q = S->leg_ptr[jb.v]; q < S->leg_ptr[jb.v + 1]; ++q)
+        if (S->leg_edge[q] == e) jb.pv = q - S->leg_ptr[jb.v];
+      jobs[j] = jb;
+      const int dd = S->dsite[jb.u] * S->dsite[jb.v];
+      if (j == 0) D = dd;
+      if (per_gate && dd != D) return su_fail(S, GBTN_ERR_INVALID, "simple update: per-gate operators need equal sizes");
+    }
+    const long long gsz = (long long)D * D;
+    double* d_gates = nullptr;
+    GBTN_CUDA(cudaMalloc(&d_gates, sizeof(double) * gsz * (per_gate ? n_gates : 1)));
+    std::unique_ptr<double, decltype(&cudaFree)> g_guard(d_gates, cudaFree);
+    GBTN_CUDA(cudaMemcpyAsync(d_gates, gates, sizeof(double) * gsz * (per_gate ? n_gates : 1),
+                              cudaMemcpyHostToDevice, s));
+    double* d_envs = nullptr;
+    if (envs) {
+      const long long ne2 = 2LL * S->ne * S->chimax * S->chimax;
+      GBTN_CUDA(cudaMalloc(&d_envs, sizeof(double) * std::max<long long>(ne2, 1)));
+      GBTN_CUDA(cudaMemcpyAsync(d_envs, envs, sizeof(double) * ne2, cudaMemcpyHostToDevice, s));
+    }
+    std::unique_ptr<double, decltype(&cudaFree)> e_guard(d_envs, cudaFree);
+    const int md = maxdim > 0 ? std::min(maxdim, S->chimax) : S->chimax;
+    double *d_te = nullptr, *d_sv = nullptr, *d_q = nullptr;
+    SuJob* d_jobs = nullptr;
+    GBTN_CUDA(cudaMalloc(&d_te, sizeof(double) * n_gates));
+    GBTN_CUDA(cudaMalloc(&d_sv, sizeof(double) * (size_t)n_gates * md));
+    GBTN_CUDA(cudaMalloc(&d_jobs, sizeof(SuJob) * n_gates));
+    std::unique_ptr<double, decltype(&cudaFree)> te_guard(d_te, cudaFree), sv_guard(d_sv, cudaFree);
+    std::unique_ptr<SuJob, decltype(&cudaFree)> j_guard(d_jobs, cudaFree);
+    GBTN_CUDA(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SuJob) * n_gates, cudaMemcpyHostToDevice, s));
+    // batches of consecutive, vertex-disjoint gates (they commute): sequential semantics
+    std::vector<std::pair<int, int>> batches;
+    std::vector<int> mark(S->nv, -1);
+    int start = 0, maxb = 0;
+    for (int j = 0; j < n_gates; ++j) {
+      if (mark[jobs[j].u] == (int)batches.size() || mark[jobs[j].v] == (int)batches.size()) {
+        batches.push_back({start, j});
+        maxb = std::max(maxb, j - start);
+        start = j;
+      }
+      mark[jobs[j].u] = mark[jobs[j].v] = (int)batches.size();
+    }
+    batches.push_back({start, n_gates});
+    maxb = std::max(maxb, n_gates - start);
+    GBTN_CUDA(cudaMalloc(&d_q, sizeof(double) * (size_t)maxb * 2 * gbtn::kSuMaxNHost));
+    std::unique_ptr<double, decltype(&cudaFree)> q_guard(d_q, cudaFree);
+    const size_t smem = gbtn::su_smem_bytes();
+    gbtn::su_prepare(smem);
+    GBTN_CUDA(cudaMemsetAsync(S->d_status, 0, sizeof(int), s));
+    for (auto& b : batches) {
+      SuArgs a{};
+      a.jobs = d_jobs + b.first;
+      a.njobs = b.second - b.first;
+      a.leg_ptr = S->d_leg_ptr;
+      a.leg_edge = S->d_leg_edge;
+      a.edge_u = S->d_edge_u;
+      a.site_dim = S->d_dsite;
+      a.edim = S->d_edim;
+      a.cap_off = S->d_cap_off;
+      a.tens = S->d_tens;
+      a.envs = d_envs;
+      a.gates = d_gates + (per_gate ? gsz * b.first : 0);
+      a.gate_stride = per_gate ? gsz : 0;
+      a.maxdim = md;
+      a.cutoff = cutoff;
+      a.normalize = normalize;
+      a.chimax = S->chimax;
+      a.qscratch = d_q;
+      a.truncerr = d_te + b.first;
+      a.svals = d_sv + (size_t)b.first * md;
+      a.status = S->d_status;
+      gbtn::su_launch(a, smem, s);
+    }
+    int status = 0;
+    GBTN_CUDA(cudaMemcpyAsync(&status, S->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    std::vector<double> te(n_gates), sv((size_t)n_gates * md);
+    GBTN_CUDA(cudaMemcpyAsync(te.data(), d_te, sizeof(double) * n_gates, cudaMemcpyDeviceToHost, s));
+    GBTN_CUDA(cudaMemcpyAsync(sv.data(), d_sv, sizeof(double) * sv.size(), cudaMemcpyDeviceToHost, s));
+    GBTN_CUDA(cudaStreamSynchronize(s));
+    if (status) return su_fail(S, GBTN_ERR_UNSUPPORTED, "simple update: a gate exceeds the kernel limits (site tensor > 8192 elements or theta > 64 x 64)");
+    if (truncerr) std::copy(te.begin(), te.end(), truncerr);
+    if (svals)
+      for (int j = 0; j < n_gates; ++j)
+        for (int i = 0; i < maxdim; ++i) svals[(size_t)j * maxdim + i] = i < md ? sv[(size_t)j * md + i] : 0.0;
+    su_pull_dims(S);
+  } catch (const std::exception& e) {
+    return su_fail(S, GBTN_ERR_CUDA, e.what());
+  }
+  return GBTN_OK;
+}
+
+}  // extern "C"

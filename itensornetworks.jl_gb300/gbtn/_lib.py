@@ -126,6 +126,12 @@ SIGNATURES = {
     "gbtn_logscalar": (_I, [_P, _D, _D]),
     "gbtn_rescale_messages": (_I, [_P]),
     "gbtn_rescale_partitions": (_I, [_P]),
+    "gbtn_su_create": (_I, [_P, C.POINTER(GraphDesc), C.c_int32, C.POINTER(_P)]),
+    "gbtn_su_destroy": (_I, [_P]),
+    "gbtn_su_edge_dims": (_I, [_P, _I32]),
+    "gbtn_su_set_factors": (_I, [_P, _D]),
+    "gbtn_su_get_factors": (_I, [_P, _D, C.c_int64]),
+    "gbtn_su_apply": (_I, [_P, C.c_int32, _I32, _D, C.c_int32, _D, C.c_int32, C.c_double, C.c_int32, _D, _D]),
     "gbtn_energy2": (_I, [_P, C.c_int32, _D, _D, _D]),
     "gbtn_energy2_grad": (_I, [_P, C.c_int32, _D, _D, C.POINTER(GradOpts), _D, _D, _I32, _D]),
     "gbtn_bp_vjp": (_I, [_P, _D, C.POINTER(GradOpts), _D, _I32, _D]),

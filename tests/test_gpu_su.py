@@ -1,0 +1,133 @@
+"""Simple update (apply / tebd) on the GPU against the oracle's restatement of
+simple_update_bp (src/apply.jl:33-95).
+
+The factors of an SVD / QR are gauge dependent, so the comparisons use
+gauge-invariant quantities: kept singular values and truncation errors
+(1e-10 relative / 1e-12 absolute), bond dimensions (exact) and the contracted
+state vector, normalised and up to a global sign (1e-9)."""
+import numpy as np
+import pytest
+
+import bp_oracle as O
+import gbtn
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(lib_built):
+    yield
+
+
+def state(g, A):
+    ops, lid = [], {e: 20 + e for e in range(g.ne)}
+    for v in range(g.nv):
+        ops += [A[v], [v] + [lid[e] for e in g.legs[v]]]
+    psi = np.einsum(*ops, list(range(g.nv)), optimize=True)
+    return psi / np.linalg.norm(psi)
+
+
+def same_up_to_sign(a, b, tol):
+    return min(np.max(np.abs(a - b)), np.max(np.abs(a + b))) < tol
+
+
+def random_gate(seed, dt=0.3):
+    rng = np.random.default_rng(seed)
+    H = rng.standard_normal((4, 4))
+    H = H + H.T
+    w, U = np.linalg.eigh(H)
+    return (U * np.exp(-dt * w)) @ U.T
+
+
+def oracle_gate(g, A, gate, e, envs=None, maxdim=None, cutoff=None, normalize=True):
+    u, v = g.edges[e]
+    pu, pv = g.legs[u].index(e), g.legs[v].index(e)
+    eu, ev = {}, {}
+    if envs is not None:
+        eu = {1 + p: envs[g.directed(f, g.other(u, f))] for p, f in enumerate(g.legs[u]) if f != e}
+        ev = {1 + p: envs[g.directed(f, g.other(v, f))] for p, f in enumerate(g.legs[v]) if f != e}
+    Au, Av, S, te = O.simple_update(gate, A[u], A[v], pu, pv, eu, ev, maxdim=maxdim, cutoff=cutoff)
+    if normalize:
+        Au, Av = Au / np.linalg.norm(Au), Av / np.linalg.norm(Av)
+    B = list(A)
+    B[u], B[v] = Au, Av
+    g2 = O.Graph(g.nv, g.edges, g.site_dims, list(g.edge_dims), [list(l) for l in g.legs])
+    g2.edge_dims[e] = Au.shape[pu + 1]
+    return g2, B, S, te
+
+
+def gpu_net(g, A):
+    return gbtn.TensorNetwork(g.nv, g.edges, g.site_dims, g.edge_dims, [a.copy() for a in A])
+
+
+@pytest.mark.parametrize("e", [0, 3, 7])
+def test_single_gate_matches_oracle(e):
+    g = O.square_lattice(3, 3, chi=2)
+    A = O.random_network(g, 21)
+    gate = random_gate(e)
+    g2, B, S, te = oracle_gate(g, A, gate, e, maxdim=2, cutoff=1e-12)
+    st = gbtn.SimpleUpdateState(gpu_net(g, A), chi_max=4)
+    te_g, sv = st.apply(gate, [e], maxdim=2, cutoff=1e-12, normalize=True)
+    assert st.edge_dims()[e] == g2.edge_dims[e]
+    np.testing.assert_allclose(sv[0][:len(S)], S, rtol=1e-10)
+    assert te_g[0] == pytest.approx(te, rel=1e-9, abs=1e-14)
+    out = st.network()
+    assert same_up_to_sign(state(g2, out.tensors), state(g2, B), 1e-9)
+
+
+def test_single_gate_with_bp_environment():
+    g = O.square_lattice(3, 3, chi=3)
+    A = O.random_network(g, 5)
+    bpc = gbtn.BeliefPropagationCache(gpu_net(g, A)).update(maxiter=100, tol=1e-15, schedule="parallel")
+    envs = bpc.messages()
+    e = 5
+    gate = random_gate(3)
+    g2, B, S, te = oracle_gate(g, A, gate, e, envs=envs, maxdim=3, cutoff=1e-10)
+    st = gbtn.SimpleUpdateState(gpu_net(g, A), chi_max=6)
+    te_g, sv = st.apply(gate, [e], envs=envs, maxdim=3, cutoff=1e-10, normalize=True)
+    np.testing.assert_allclose(sv[0][:len(S)], S, rtol=1e-9)
+    assert te_g[0] == pytest.approx(te, rel=1e-8, abs=1e-14)
+    assert same_up_to_sign(state(g2, st.network().tensors), state(g2, B), 1e-8)
+
+
+def test_tfim_tebd_matches_oracle():
+    Lx, Ly, g_field, dt, steps, maxdim = 3, 3, 3.0, 0.05, 4, 4
+    g = O.square_lattice(Lx, Ly, chi=1)
+    plus = np.array([1.0, 1.0]) / np.sqrt(2)
+    A = [plus.reshape((2,) + (1,) * len(g.legs[v])) for v in range(g.nv)]
+    z = [len(l) for l in g.legs]
+    order = [e for cls in gbtn.checkerboard_edges(Lx, Ly) for e in cls]
+    gate_of = lambda e: gbtn.tfim_gate(dt, g_field, z[g.edges[e][0]], z[g.edges[e][1]])
+    st = gbtn.SimpleUpdateState(gpu_net(g, A), chi_max=maxdim)
+    gg, B = g, list(A)
+    for _ in range(steps):
+        te_g, _ = st.apply([gate_of(e) for e in order], order, maxdim=maxdim, cutoff=1e-10, normalize=True)
+        tes = []
+        for e in order:
+            gg, B, S, te = oracle_gate(gg, B, gate_of(e), e, maxdim=maxdim, cutoff=1e-10)
+            tes.append(te)
+        np.testing.assert_allclose(te_g, tes, rtol=1e-6, atol=1e-13)
+    assert st.edge_dims() == gg.edge_dims
+    assert same_up_to_sign(state(gg, st.network().tensors), state(gg, B), 1e-9)
+
+
+def test_tfim_20x20_chi8_runs_and_lowers_energy():
+    # the shape of the TFIM benchmark (20x20, chi_max 8, cutoff 1e-10), 10 steps
+    L, g_field, dt = 20, 3.0, 0.01
+    tn = gbtn.square_lattice(L, L, chi=1)
+    plus = np.array([1.0, 1.0]) / np.sqrt(2)
+    tn.tensors = [plus.reshape((2,) + (1,) * len(tn.legs[v])) for v in range(tn.nv)]
+    z = [len(l) for l in tn.legs]
+    classes = gbtn.checkerboard_edges(L, L)
+    st, te = gbtn.tebd(tn, lambda e: gbtn.tfim_gate(dt, g_field, z[tn.edges[e][0]], z[tn.edges[e][1]]), classes,
+                       nsteps=10, maxdim=8, cutoff=1e-10, normalize=True, chi_max=8)
+    dims = st.edge_dims()
+    assert max(dims) <= 8 and min(dims) >= 1
+    net = st.network()
+    bpc = gbtn.BeliefPropagationCache(net).update(maxiter=100, tol=1e-12, schedule="parallel")
+    x = bpc.expect(O.PX)
+    zz = bpc.expect2(np.kron(O.PZ, O.PZ))
+    e_site = (-zz.sum() - g_field * x.sum()) / tn.nv
+    # the |+> product state has energy -g = -3 per site; imaginary time lowers it
+    assert e_site < -3.0
+    assert np.all(np.abs(x) <= 1 + 1e-12)
