@@ -196,6 +196,64 @@ def gradient_timing(gbtn, ctx, barrier, rank, Lg=12, chig=6, reps=3):
     return out
 
 
+def simple_update_timing(gbtn, ctx, barrier, rank, Ls=20, steps=200, g_field=3.0, dt=0.01, chi_max=8):
+    """TFIM imaginary-time evolution by simple update: H = -sum ZZ - g sum X on an
+    Ls x Ls open lattice from |+>, gates exp(-dt h_e) in checkerboard order,
+    chi_max 8, cutoff 1e-10, FP64.  Reports gate updates per second and the
+    BP-gauged <X> and energy per site of the final state."""
+    tn = gbtn.square_lattice(Ls, Ls, chi=1)
+    plus = np.array([1.0, 1.0]) / np.sqrt(2)
+    tn.tensors = [plus.reshape((2,) + (1,) * len(tn.legs[v])) for v in range(tn.nv)]
+    z = [len(l) for l in tn.legs]
+    classes = gbtn.checkerboard_edges(Ls, Ls)
+    order = [e for c in classes for e in c]
+    gates = [gbtn.tfim_gate(dt, g_field, z[tn.edges[e][0]], z[tn.edges[e][1]]) for e in order]
+    st = gbtn.SimpleUpdateState(tn, chi_max, ctx=ctx)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        st.apply(gates, order, maxdim=chi_max, cutoff=1e-10, normalize=True)
+    barrier()
+    el = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    st.apply(gates, order, maxdim=chi_max, cutoff=1e-10, normalize=True)
+    barrier()
+    last_step_s = time.perf_counter() - t1
+    net = st.network()
+    bpc = gbtn.BeliefPropagationCache(net, ctx=ctx).update(maxiter=200, tol=1e-14, schedule="parallel")
+    px = np.array([[0.0, 1.0], [1.0, 0.0]])
+    pz = np.array([[1.0, 0.0], [0.0, -1.0]])
+    x = bpc.expect(px)
+    zz = bpc.expect2(np.kron(pz, pz))
+    out = {"workload": f"tfim_{Ls}x{Ls}_g{g_field}_dt{dt}_{steps}steps_chimax{chi_max}_cutoff1e-10",
+           "gate_updates_per_s": steps * len(order) / el, "total_s": el,
+           "gate_updates_per_s_at_chi8": len(order) / last_step_s,
+           "max_bond_dim": max(st.edge_dims()), "x_per_site": float(np.mean(x)),
+           "energy_per_site": float((-zz.sum() - g_field * x.sum()) / tn.nv)}
+    if rank == 0:
+        # CPU baseline: the oracle's FP64 simple update (NumPy/LAPACK) on the
+        # gates of one step from the final state
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import bp_oracle as O
+        g = O.Graph(net.nv, net.edges, net.site_dims, list(net.edge_dims), [list(l) for l in net.legs])
+        A = [t.copy() for t in net.tensors]
+        t0 = time.perf_counter()
+        n = 0
+        for e, gate in zip(order, gates):
+            u, v = g.edges[e]
+            pu, pv = g.legs[u].index(e), g.legs[v].index(e)
+            Au, Av, S, te = O.simple_update(gate, A[u], A[v], pu, pv, {}, {}, maxdim=chi_max, cutoff=1e-10)
+            A[u], A[v] = Au / np.linalg.norm(Au), Av / np.linalg.norm(Av)
+            g.edge_dims[e] = Au.shape[pu + 1]
+            n += 1
+            if time.perf_counter() - t0 > 10.0:
+                break
+        out["cpu_oracle_gate_updates_per_s_at_chi8"] = n / (time.perf_counter() - t0)
+    bpc.close()
+    st.close()
+    return out
+
+
 def tc_vertices_per_net(L=L):
     """Vertices of the tensor-core class (interior, degree 4) per L x L lattice."""
     return max(L - 2, 0) ** 2
@@ -322,6 +380,8 @@ def run_ours(args):
     #    mixed-precision BP to convergence + FP64 implicit adjoint, and the
     #    checkpointed 30-sweep unrolled variant; seconds per full dE/dA
     grad = gradient_timing(gbtn, ctx, barrier, rank)
+    # 6. simple update (TFIM, 20x20, 200 steps)
+    su = simple_update_timing(gbtn, ctx, barrier, rank)
 
     value = world * msgs_step / (ms_bf16 * 1e-3)
     n_tc = BATCH * tc_vertices_per_net()
@@ -362,6 +422,7 @@ def run_ours(args):
                          "mma_tflops": n_tc * mma_flops_vertex / (tc_launch_ms * 1e-3) / 1e12,
                          "note": f"algorithmic FP flops of the degree-4 vertices / event-timed kernel duration, of {peak_src} bf16 peak"},
             "gradient": grad,
+            "simple_update": su,
             "cpu_baseline": {"value": cpu_val, "unit": "msg-updates/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": world * msgs_step / (e2e_ms * 1e-3), "unit": "msg-updates/s",
