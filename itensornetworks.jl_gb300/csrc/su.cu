@@ -10,8 +10,9 @@
 //   2. each site absorbs its sqrt environments and is QR-factorised as
 //      (other legs) x (site, bond) with Householder reflectors: psi = Q R;
 //   3. theta = R_u R_v over the bond, the gate applied on the two site indices;
-//   4. one-sided Jacobi SVD of theta (columns rotated in round-robin pairs,
-//      one warp per pair), singular values sorted in descending order;
+//   4. SVD of theta: pivoted QR, then one-sided Jacobi on R^T (columns
+//      rotated in round-robin pairs, eight lanes per pair), singular values
+//      sorted in descending order;
 //   5. truncation by the rule of ITensors' svd: at most maxdim values, then drop
 //      from the tail while the discarded sum of squares stays within
 //      cutoff * sum of squares (at least one value kept); truncation error =
@@ -38,75 +39,219 @@ constexpr int kSuWarps = kSuThreads / 32;
 constexpr int kSuMaxN = 8192;     // elements of one site tensor
 constexpr int kSuMaxTheta = 64;   // rows / columns of theta
 constexpr int kSvdMaxSweeps = 40;
+// A Jacobi pair is left alone when its columns are orthogonal to this
+// relative precision (a few ulps above the rounding of a 64-long FP64 dot)
+// or when either column is below 1e-15 of ||A||_F (rotating rounding noise
+// cannot change the decomposition beyond eps ||A||).
+constexpr double kJacobiTol = 4e-15;
+constexpr double kJacobiTiny = 1e-30;
 
+// FP64 runs at a small fraction of the FP32 rate on this part, and a warp
+// instruction costs the FP64 pipe the same whether one lane or 32 are active,
+// so the helpers below keep the number of FP64 warp instructions low: scalar
+// work is done by one warp (or one lane) and broadcast through shared memory.
+
+// Sum over the CTA; every thread receives the total.  red: >= kSuWarps + 1.
 __device__ __forceinline__ double block_sum(double x, double* red) {
   x = warp_sum(x);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   __syncthreads();
   if (lane == 0) red[w] = x;
   __syncthreads();
-  double t = 0.0;
+  if (w == 0) {
+    double t = lane < kSuWarps ? red[lane] : 0.0;
 #pragma unroll
-  for (int i = 0; i < kSuWarps; ++i) t += red[i];
+    for (int o = kSuWarps / 2; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) red[kSuWarps] = t;
+  }
   __syncthreads();
-  return t;
+  return red[kSuWarps];
 }
 
-// One-sided Jacobi SVD of A (m x n, column-major, lda = m, m <= 64, n <= 64).
-// On return: columns of A hold U (unit columns, zero where sigma = 0), V (n x n,
-// ldv = n) the right singular vectors, sig[n] the singular values, all sorted
-// in descending order of sig.  work: >= m*n + n*n doubles, ord: n ints.
-__device__ void cta_svd(double* A, int m, int n, double* V, double* sig, double* work, int* ord, int* flag) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i = tid; i < n * n; i += kSuThreads) V[i] = (i % n == i / n) ? 1.0 : 0.0;
-  const int N = n + (n & 1);  // players of the round-robin (one dummy when n is odd)
+// Scratch of the SVD: work >= m*n + n*n doubles; cn, rdiag, bet, V-row
+// permutation perm and sort order ord >= n entries; flag and red as in
+// block_sum.
+struct SvdBufs {
+  double* work;
+  double* cn;
+  double* rdiag;
+  double* bet;
+  int* perm;
+  int* ord;
+  int* flag;
+  double* red;
+};
+
+// Sum of x over the 8 lanes of a group (all 32 lanes must take part).
+__device__ __forceinline__ double group8_sum(double x) {
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+// Householder QR with column pivoting of A (m x n, m >= n, lda = m), in place:
+// A P = Q R, column j of A P being column perm[j] of A.  On return the strict
+// upper triangle of A holds R, rdiag its diagonal, the columns below the
+// diagonal the reflectors (bet their coefficients).  The group that updates a
+// column also returns its squared norm below the next row, so the pivot
+// norms are exact rather than downdated.
+__device__ void cta_qrcp(double* A, int m, int n, SvdBufs& b) {
+  __shared__ double s_bj;
+  __shared__ int s_piv;
+  const int tid = threadIdx.x, grp = tid >> 3, gl = tid & 7, warp = tid >> 5;
+  for (int c0 = 0; c0 < n; c0 += 32) {
+    const int c = c0 + grp;
+    double s2 = 0.0;
+    if (c < n)
+      for (int i = gl; i < m; i += 8) s2 = fma(A[(size_t)c * m + i], A[(size_t)c * m + i], s2);
+    s2 = group8_sum(s2);
+    if (c < n && gl == 0) {
+      b.cn[c] = s2;
+      b.perm[c] = c;
+    }
+  }
   __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    if (tid == 0) {  // pivot: largest remaining norm (bit patterns of non-negative doubles order like values)
+      int piv = j;
+      long long best = __double_as_longlong(b.cn[j]);
+      for (int c = j + 1; c < n; ++c) {
+        const long long k = __double_as_longlong(b.cn[c]);
+        if (k > best) {
+          best = k;
+          piv = c;
+        }
+      }
+      s_piv = piv;
+      if (piv != j) {
+        const double t = b.cn[j];
+        b.cn[j] = b.cn[piv];
+        b.cn[piv] = t;
+        const int q = b.perm[j];
+        b.perm[j] = b.perm[piv];
+        b.perm[piv] = q;
+      }
+    }
+    __syncthreads();
+    const int piv = s_piv;
+    if (piv != j)
+      for (int i = tid; i < m; i += kSuThreads) {
+        const double t = A[(size_t)j * m + i];
+        A[(size_t)j * m + i] = A[(size_t)piv * m + i];
+        A[(size_t)piv * m + i] = t;
+      }
+    __syncthreads();
+    double* x = A + (size_t)j * m;
+    if (tid == 0) {
+      const double s2 = b.cn[j], x0 = x[j];
+      const double nrm = sqrt(s2);
+      const double alpha = x0 >= 0.0 ? -nrm : nrm;
+      const double v0 = x0 - alpha;
+      const double vn2 = s2 - x0 * x0 + v0 * v0;
+      const double bj = (vn2 > 0.0 && nrm > 0.0) ? 2.0 / vn2 : 0.0;
+      if (bj > 0.0) x[j] = v0;
+      b.bet[j] = bj;
+      b.rdiag[j] = bj > 0.0 ? alpha : x0;
+      s_bj = bj;
+    }
+    __syncthreads();
+    const double bj = s_bj;
+    for (int c0 = j + 1; c0 < n; c0 += 32) {
+      if (c0 + 4 * warp >= n) continue;  // warp-uniform
+      const int c = c0 + grp;
+      const bool act = c < n;
+      double* y = A + (size_t)(act ? c : j) * m;
+      double w = 0.0;
+      if (act && bj > 0.0)
+        for (int i = j + gl; i < m; i += 8) w = fma(x[i], y[i], w);
+      w = group8_sum(w) * bj;
+      double nx = 0.0;
+      if (act)
+        for (int i = j + gl; i < m; i += 8) {
+          double v = y[i];
+          if (bj > 0.0) {
+            v = fma(-w, x[i], v);
+            y[i] = v;
+          }
+          if (i > j) nx = fma(v, v, nx);
+        }
+      nx = group8_sum(nx);
+      if (act && gl == 0) b.cn[c] = nx;
+    }
+    __syncthreads();
+  }
+}
+
+// One-sided Jacobi (Hestenes) on the columns of X (m x n, ldx = m).  Columns
+// are paired by a round-robin tournament; each pair of a round is handled by
+// a group of 8 lanes (32 groups, so a whole round runs at once and one warp
+// instruction serves four pairs).  The rotation angle is computed in FP32
+// from the FP64 inner products, scaled by the larger norm: it only has to
+// shrink the pair's coupling, c^2 + s^2 = 1 is formed in FP64 for whatever
+// tangent is used (the transformation stays orthogonal), and the FP64
+// stopping test decides the accuracy.  Sweeps stop when a sweep rotates
+// nothing.  The rotations are not accumulated: the caller recovers the right
+// factor from the rotated columns.
+__device__ void cta_jacobi(double* X, int m, int n, int* flag, double* red) {
+  const int tid = threadIdx.x, grp = tid >> 3, gl = tid & 7;
+  double f = 0.0;
+  for (int i = tid; i < m * n; i += kSuThreads) f = fma(X[i], X[i], f);
+  f = block_sum(f, red);
+  const double tiny = f * kJacobiTiny, tol2 = kJacobiTol * kJacobiTol;
+  const int N = n + (n & 1);  // players of the round-robin (one dummy when n is odd)
+  const int npair = N / 2;
+  const bool warp_busy = (tid >> 5) * 4 < npair;  // warp-uniform
   for (int sweep = 0; sweep < kSvdMaxSweeps; ++sweep) {
     if (tid == 0) *flag = 0;
     __syncthreads();
     for (int r = 0; r < N - 1; ++r) {
-      for (int pi = warp; pi < N / 2; pi += kSuWarps) {
-        int p, q;
-        if (pi == 0) {
-          p = N - 1;
-          q = r;
-        } else {
-          p = (r + pi) % (N - 1);
-          q = (r - pi + N - 1) % (N - 1);
+      if (warp_busy) {
+        int p = 0, q = 0;
+        bool act = grp < npair;
+        if (act) {
+          if (grp == 0) {
+            p = N - 1;
+            q = r;
+          } else {
+            p = (r + grp) % (N - 1);
+            q = (r - grp + N - 1) % (N - 1);
+          }
+          if (p > q) {
+            const int t = p;
+            p = q;
+            q = t;
+          }
+          act = q < n;
         }
-        if (p >= n || q >= n) continue;
-        if (p > q) {
-          const int t = p;
-          p = q;
-          q = t;
-        }
-        double* a = A + (size_t)p * m;
-        double* b = A + (size_t)q * m;
+        double* a = X + (size_t)p * m;
+        double* b = X + (size_t)q * m;
         double al = 0.0, be = 0.0, ga = 0.0;
-        for (int i = lane; i < m; i += 32) {
-          al += a[i] * a[i];
-          be += b[i] * b[i];
-          ga += a[i] * b[i];
-        }
-        al = warp_sum(al);
-        be = warp_sum(be);
-        ga = warp_sum(ga);
-        if (ga == 0.0 || fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
-        if (lane == 0) *flag = 1;
-        const double zeta = (be - al) / (2.0 * ga);
-        const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
-        for (int i = lane; i < m; i += 32) {
-          const double x = a[i], y = b[i];
-          a[i] = c * x - s * y;
-          b[i] = s * x + c * y;
-        }
-        double* va = V + (size_t)p * n;
-        double* vb = V + (size_t)q * n;
-        for (int i = lane; i < n; i += 32) {
-          const double x = va[i], y = vb[i];
-          va[i] = c * x - s * y;
-          vb[i] = s * x + c * y;
+        if (act)
+          for (int i = gl; i < m; i += 8) {
+            const double x = a[i], y = b[i];
+            al = fma(x, x, al);
+            be = fma(y, y, be);
+            ga = fma(x, y, ga);
+          }
+        al = group8_sum(al);
+        be = group8_sum(be);
+        ga = group8_sum(ga);
+        const bool rot = act && al > tiny && be > tiny && ga * ga > tol2 * al * be;
+        if (__any_sync(0xffffffffu, rot)) {
+          // tan of the angle: 2 g sgn(d) / (|d| + sqrt(d^2 + 4 g^2)), d = (be - al) / mx, g = ga / mx
+          const float inv = 1.0f / (float)fmax(al, be);
+          const float d = (float)(be - al) * inv, g = (float)ga * inv;
+          const float t32 = rot ? (d >= 0.f ? 2.f : -2.f) * g / (fabsf(d) + sqrtf(fmaf(d, d, 4.f * g * g))) : 0.f;
+          const double t = t32;
+          const double c = rsqrt(fma(t, t, 1.0)), s = c * t;
+          if (rot) {
+            for (int i = gl; i < m; i += 8) {
+              const double x = a[i], y = b[i];
+              a[i] = fma(c, x, -s * y);
+              b[i] = fma(s, x, c * y);
+            }
+            if (gl == 0) *flag = 1;
+          }
         }
       }
       __syncthreads();
@@ -114,76 +259,137 @@ __device__ void cta_svd(double* A, int m, int n, double* V, double* sig, double*
     if (*flag == 0) break;
     __syncthreads();
   }
-  // column norms, descending order, normalised U
-  for (int j = warp; j < n; j += kSuWarps) {
-    double s2 = 0.0;
-    for (int i = lane; i < m; i += 32) s2 += A[(size_t)j * m + i] * A[(size_t)j * m + i];
-    s2 = warp_sum(s2);
-    if (lane == 0) sig[j] = sqrt(s2);
+}
+
+// SVD of A (m x n, m >= n, lda = m, n <= 64, m <= 64) by one-sided Jacobi
+// preconditioned with a pivoted QR (Drmac and Veselic, SIAM J. Matrix Anal.
+// Appl. 29 (2008)): A P = Q R and Jacobi on the columns of X = R^T give
+// X W = U_x S, so R = W S U_x^T and A = (A P U_x S^-1) S (P U_x)^T:
+// V = P U_x and U = A V S^-1.  The pivoting grades R, which cuts the number
+// of sweeps on the wide-range spectra of truncated states.  On return: the
+// columns of A hold U (zero where sigma = 0), V (n x n, ldv = n) the right
+// singular vectors, sig[n] the singular values, all in descending order of
+// sig.  U is accurate to eps ||A|| / sigma per column, which is the accuracy
+// of the reconstruction U S V^T that the callers use.
+__device__ void cta_svd(double* A, int m, int n, double* V, double* sig, SvdBufs& b) {
+  const int tid = threadIdx.x, grp = tid >> 3, gl = tid & 7;
+  double* A0 = b.work;                  // m x n copy of the input
+  double* X = b.work + (size_t)m * n;   // n x n
+  for (int i = tid; i < m * n; i += kSuThreads) A0[i] = A[i];
+  __syncthreads();
+  cta_qrcp(A, m, n, b);
+  for (int i = tid; i < n * n; i += kSuThreads) {  // X[c, r] = R[r, c]
+    const int c = i % n, r = i / n;
+    X[i] = r < c ? A[(size_t)c * m + r] : (r == c ? b.rdiag[r] : 0.0);
   }
   __syncthreads();
-  if (tid == 0) {
-    for (int j = 0; j < n; ++j) ord[j] = j;
-    for (int i = 1; i < n; ++i) {  // insertion sort, descending, stable
-      const int x = ord[i];
-      int j = i - 1;
-      while (j >= 0 && sig[ord[j]] < sig[x]) {
-        ord[j + 1] = ord[j];
-        --j;
+  cta_jacobi(X, n, n, b.flag, b.red);
+  // sigma = column norms of X, U_x = unit columns (a group per column)
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    const int j = j0 + grp;
+    double s2 = 0.0;
+    if (j < n)
+      for (int i = gl; i < n; i += 8) s2 = fma(X[(size_t)j * n + i], X[(size_t)j * n + i], s2);
+    s2 = group8_sum(s2);
+    const double sg = sqrt(s2);
+    const double iv = sg > 0.0 ? 1.0 / sg : 0.0;
+    if (j < n) {
+      for (int i = gl; i < n; i += 8) X[(size_t)j * n + i] *= iv;
+      if (gl == 0) {
+        sig[j] = sg;
+        b.cn[j] = iv;
       }
-      ord[j + 1] = x;
     }
   }
   __syncthreads();
-  double* U2 = work;
-  double* V2 = work + (size_t)m * n;
-  for (int i = tid; i < m * n; i += kSuThreads) {
-    const int j = i / m, row = i % m, src = ord[j];
-    const double sg = sig[src];
-    U2[i] = sg > 0.0 ? A[(size_t)src * m + row] / sg : 0.0;
+  // V = P U_x: row perm[j] of V is row j of U_x
+  for (int i = tid; i < n * n; i += kSuThreads) {
+    const int j = i % n, k = i / n;
+    V[(size_t)k * n + b.perm[j]] = X[i];
   }
-  for (int i = tid; i < n * n; i += kSuThreads) V2[i] = V[(size_t)ord[i / n] * n + (i % n)];
+  __syncthreads();
+  // U = A V S^-1
+  for (int i = tid; i < m * n; i += kSuThreads) {
+    const int r = i % m, k = i / m;
+    double acc = 0.0;
+    for (int c = 0; c < n; ++c) acc = fma(A0[(size_t)c * m + r], V[(size_t)k * n + c], acc);
+    A[i] = acc * b.cn[k];
+  }
+  __syncthreads();
+  // descending, stable order by rank counting; sigma >= 0, so the IEEE bit
+  // patterns order like the values and the comparisons stay off the FP64 pipe
+  if (tid < n) {
+    const long long kj = __double_as_longlong(sig[tid]);
+    int rank = 0;
+    for (int i = 0; i < n; ++i) {
+      const long long ki = __double_as_longlong(sig[i]);
+      rank += (ki > kj) || (ki == kj && i < tid);
+    }
+    b.ord[rank] = tid;
+  }
+  __syncthreads();
+  double* U2 = b.work;
+  double* V2 = b.work + (size_t)m * n;
+  for (int i = tid; i < m * n; i += kSuThreads) U2[i] = A[(size_t)b.ord[i / m] * m + (i % m)];
+  for (int i = tid; i < n * n; i += kSuThreads) V2[i] = V[(size_t)b.ord[i / n] * n + (i % n)];
   __syncthreads();
   for (int i = tid; i < m * n; i += kSuThreads) A[i] = U2[i];
   for (int i = tid; i < n * n; i += kSuThreads) V[i] = V2[i];
-  if (tid == 0) {
-    double* ss = work;  // reuse: sorted values
-    for (int j = 0; j < n; ++j) ss[j] = sig[ord[j]];
-    for (int j = 0; j < n; ++j) sig[j] = ss[j];
-  }
+  __syncthreads();
+  if (tid < n) b.work[tid] = sig[b.ord[tid]];
+  __syncthreads();
+  if (tid < n) sig[tid] = b.work[tid];
   __syncthreads();
 }
 
 // Householder QR of M (m x n column-major, lda = m): R (r x n, ldr = r) and
 // Q (m x r, ldq = m), r = min(m, n).  M is overwritten; beta: >= n doubles.
+// The warp that updates column j + 1 also returns that column's squared norm
+// below row j + 1, so each reflector costs two barriers; Q is accumulated
+// backwards, touching only the columns a reflector changes.
 __device__ void cta_qr(double* M, int m, int n, double* R, double* Q, double* beta, double* red) {
+  __shared__ double s_bj, s_next;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int r = m < n ? m : n;
+  double s2_first = 0.0;
+  for (int i = tid; i < m; i += kSuThreads) s2_first = fma(M[i], M[i], s2_first);
+  s2_first = block_sum(s2_first, red);
   for (int j = 0; j < r; ++j) {
     double* x = M + (size_t)j * m;
-    double s2 = 0.0;
-    for (int i = j + tid; i < m; i += kSuThreads) s2 += x[i] * x[i];
-    s2 = block_sum(s2, red);
-    const double x0 = x[j];
-    const double nrm = sqrt(s2);
-    const double alpha = x0 >= 0.0 ? -nrm : nrm;
-    const double v0 = x0 - alpha;
-    const double vn2 = s2 - x0 * x0 + v0 * v0;
-    const double bj = (vn2 > 0.0 && nrm > 0.0) ? 2.0 / vn2 : 0.0;
-    __syncthreads();
     if (tid == 0) {
-      x[j] = v0;  // the reflector v occupies x[j..m)
+      const double s2 = j == 0 ? s2_first : s_next;
+      const double x0 = x[j];
+      const double nrm = sqrt(s2);
+      const double alpha = x0 >= 0.0 ? -nrm : nrm;
+      const double v0 = x0 - alpha;
+      const double vn2 = s2 - x0 * x0 + v0 * v0;
+      const double bj = (vn2 > 0.0 && nrm > 0.0) ? 2.0 / vn2 : 0.0;
+      if (bj > 0.0) x[j] = v0;  // the reflector v occupies x[j..m)
       beta[j] = bj;
       R[j + (size_t)r * j] = bj > 0.0 ? alpha : x0;
+      s_bj = bj;
     }
     __syncthreads();
-    if (bj > 0.0) {
-      for (int c = j + 1 + warp; c < n; c += kSuWarps) {
-        double* y = M + (size_t)c * m;
-        double w = 0.0;
-        for (int i = j + lane; i < m; i += 32) w += x[i] * y[i];
+    const double bj = s_bj;
+    for (int c = j + 1 + warp; c < n; c += kSuWarps) {
+      double* y = M + (size_t)c * m;
+      double w = 0.0;
+      if (bj > 0.0) {
+        for (int i = j + lane; i < m; i += 32) w = fma(x[i], y[i], w);
         w = warp_sum(w) * bj;
-        for (int i = j + lane; i < m; i += 32) y[i] -= w * x[i];
+      }
+      double nx = 0.0;
+      for (int i = j + lane; i < m; i += 32) {
+        double v = y[i];
+        if (bj > 0.0) {
+          v = fma(-w, x[i], v);
+          y[i] = v;
+        }
+        if (c == j + 1 && i > j) nx = fma(v, v, nx);
+      }
+      if (c == j + 1) {
+        nx = warp_sum(nx);
+        if (lane == 0) s_next = nx;
       }
     }
     __syncthreads();
@@ -194,19 +400,19 @@ __device__ void cta_qr(double* M, int m, int n, double* R, double* Q, double* be
     if (col > row) R[i] = M[(size_t)col * m + row];
     else if (col < row) R[i] = 0.0;
   }
-  // Q = H_0 ... H_{r-1} [I; 0]
+  // Q = H_0 ... H_{r-1} [I; 0]; H_j leaves the columns c < j (still e_c) alone
   for (int i = tid; i < m * r; i += kSuThreads) Q[i] = (i % m == i / m) ? 1.0 : 0.0;
   __syncthreads();
   for (int j = r - 1; j >= 0; --j) {
     const double bj = beta[j];
     if (bj == 0.0) continue;
     const double* x = M + (size_t)j * m;
-    for (int c = warp; c < r; c += kSuWarps) {
+    for (int c = j + warp; c < r; c += kSuWarps) {
       double* y = Q + (size_t)c * m;
       double w = 0.0;
-      for (int i = j + lane; i < m; i += 32) w += x[i] * y[i];
+      for (int i = j + lane; i < m; i += 32) w = fma(x[i], y[i], w);
       w = warp_sum(w) * bj;
-      for (int i = j + lane; i < m; i += 32) y[i] -= w * x[i];
+      for (int i = j + lane; i < m; i += 32) y[i] = fma(-w, x[i], y[i]);
     }
     __syncthreads();
   }
@@ -217,14 +423,14 @@ __device__ void cta_qr(double* M, int m, int n, double* R, double* Q, double* be
 // matrix), dropping the smallest eigenvalues while their summed magnitude is
 // within 10 eps of the total.  S, Si: chi x chi column-major.
 __device__ void cta_env_sqrt(const double* env, int chi, double* S, double* Si, double* A, double* V, double* sig,
-                             double* work, int* ord, int* flag) {
+                             SvdBufs& sb) {
   const int tid = threadIdx.x;
   for (int i = tid; i < chi * chi; i += kSuThreads) {
     const int b = i % chi, a = i / chi;
     A[i] = 0.5 * (env[b + chi * a] + env[a + chi * b]);
   }
   __syncthreads();
-  cta_svd(A, chi, chi, V, sig, work, ord, flag);
+  cta_svd(A, chi, chi, V, sig, sb);
   __shared__ int s_keep;
   if (tid == 0) {
     double tot = 0.0;
@@ -240,14 +446,21 @@ __device__ void cta_env_sqrt(const double* env, int chi, double* S, double* Si, 
   }
   __syncthreads();
   const int k = s_keep;
+  double* rs = sb.work;       // sqrt of the kept eigenvalues
+  double* ri = sb.work + 64;  // and their inverses
+  if (tid < k) {
+    const double q = sqrt(sig[tid]);
+    rs[tid] = q;
+    ri[tid] = 1.0 / q;
+  }
+  __syncthreads();
   for (int i = tid; i < chi * chi; i += kSuThreads) {
     const int b = i % chi, a = i / chi;
     double s = 0.0, si = 0.0;
     for (int j = 0; j < k; ++j) {
       const double vv = V[b + chi * j] * V[a + chi * j];
-      const double r = sqrt(sig[j]);
-      s += vv * r;
-      si += vv / r;
+      s = fma(vv, rs[j], s);
+      si = fma(vv, ri[j], si);
     }
     S[i] = s;
     Si[i] = si;
@@ -339,12 +552,15 @@ __global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
   double* sig = S + 64;                   // 64
   double* beta = sig + 64;                // 64
   double* red = beta + 64;                // 32
-  int* ord = reinterpret_cast<int*>(red + 32);  // 64
+  double* aux = red + 32;                 // 3 x 64: pivot norms, R diagonal, reflector coefficients
+  int* ord = reinterpret_cast<int*>(aux + 192);  // 64
+  int* perm = ord + 64;                   // 64
   __shared__ int s_flag, s_k, s_ok;
   __shared__ double s_scale;
   const int tid = threadIdx.x;
   const int j = blockIdx.x;
   if (j >= a.njobs) return;
+  SvdBufs sb{W, aux, aux + 64, aux + 128, perm, ord, &s_flag, red};
   const SuJob job = a.jobs[j];
   SideShape sh[2];
   side_shape(a, job.u, job.pu, sh[0]);
@@ -377,7 +593,8 @@ __global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
         const int f = a.leg_edge[a.leg_ptr[x] + q];
         const int de_in = a.edge_u[f] == x ? 2 * f + 1 : 2 * f;
         const double* env = a.envs + (size_t)de_in * a.chimax * a.chimax;
-        cta_env_sqrt(env, h.chi[q], S, SI + (side * kMaxDeg + q) * 64, TH, V, sig, nxt, ord, &s_flag);
+        sb.work = nxt;
+        cta_env_sqrt(env, h.chi[q], S, SI + (side * kMaxDeg + q) * 64, TH, V, sig, sb);
         absorb_any<double>(h.chi[q], cur, nxt, h.n, st, S, tid, kSuThreads);
         __syncthreads();
         double* t = cur;
@@ -423,7 +640,19 @@ __global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
     TH[i] = acc;
   }
   __syncthreads();
-  cta_svd(TH, mt, nt, V, sig, W, ord, &s_flag);
+  // the SVD wants rows >= columns: a wide theta is decomposed transposed, and
+  // its factors swap roles (U of theta^T is V of theta)
+  const bool wide = mt < nt;
+  if (wide) {
+    for (int i = tid; i < mt * nt; i += kSuThreads) W[(i / mt) + nt * (i % mt)] = TH[i];
+    __syncthreads();
+    for (int i = tid; i < mt * nt; i += kSuThreads) TH[i] = W[i];
+    __syncthreads();
+  }
+  sb.work = W;
+  cta_svd(TH, wide ? nt : mt, wide ? mt : nt, V, sig, sb);
+  const double* UF = wide ? V : TH;  // left factor, mt x nsv (ld mt)
+  const double* VF = wide ? TH : V;  // right factor, nt x nsv (ld nt)
   if (tid == 0) {
     // ITensors truncation of p = sigma^2 (descending): maxdim, then relative cutoff
     const int nsv = min(mt, nt);
@@ -449,6 +678,8 @@ __global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
   }
   __syncthreads();
   const int kk = s_k;
+  if (tid < kk) sig[tid] = sqrt(sig[tid]);  // sqrt(S), split onto both sites
+  __syncthreads();
   // reassemble both sites with the new bond dimension kk
   for (int side = 0; side < 2; ++side) {
     SideShape h = sh[side];
@@ -464,12 +695,12 @@ __global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
     for (int i = tid; i < n2; i += kSuThreads) {
       int row, s, b;
       split_index(h, chi2, i, row, s, b);
-      const double sq = sqrt(sig[b]);
+      const double sq = sig[b];
       double acc = 0.0;
       if (side == 0) {
-        for (int t = 0; t < ru; ++t) acc += T[row + (size_t)h.m * t] * TH[(t + ru * s) + (size_t)mt * b];
+        for (int t = 0; t < ru; ++t) acc += T[row + (size_t)h.m * t] * UF[(t + ru * s) + (size_t)mt * b];
       } else {
-        for (int t = 0; t < rv; ++t) acc += T[row + (size_t)h.m * t] * V[(s + dv * t) + (size_t)nt * b];
+        for (int t = 0; t < rv; ++t) acc += T[row + (size_t)h.m * t] * VF[(s + dv * t) + (size_t)nt * b];
       }
       W[i] = acc * sq;
     }
@@ -517,8 +748,8 @@ constexpr int kSuMaxNHost = kSuMaxN;
 
 size_t su_smem_bytes() {
   return sizeof(double) * (2 * (size_t)kSuMaxN + 2 * (size_t)kSuMaxTheta * kSuMaxTheta + 2 * 1024 +
-                           2 * kMaxDeg * 64 + 64 * 3 + 32) +
-         sizeof(int) * 64;
+                           2 * kMaxDeg * 64 + 64 * 3 + 32 + 192) +
+         sizeof(int) * 128;
 }
 
 void su_prepare(size_t smem) {
