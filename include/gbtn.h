@@ -131,6 +131,20 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* desc, gbtn_plan** out
 int gbtn_plan_destroy(gbtn_plan* plan);
 /* Element counts of the concatenated tensor and message arrays. */
 int gbtn_plan_sizes(const gbtn_plan* plan, int64_t* n_factor, int64_t* n_message);
+/* Tensor-core routing of the BF16 phase (no counterpart in the reference,
+ * which contracts every vertex the same way; the "autotuner keyed on chi, d
+ * and degree").  Vertices with d = 2, at most four legs and chi <= 8 can run
+ * the tensor-core kernel zero-padded to degree 4, chi = 8; the rest run the
+ * FP32 SIMT kernel.  AUTO (default) times splits of the candidates, ordered
+ * by their algorithmic flops, on the plan's own vertices at the first BF16 /
+ * MIXED run after the policy is set; ALL routes every candidate, NATIVE only
+ * degree-4 chi = 8 vertices, OFF none.  gbtn_plan_tc_split writes 1 per
+ * tensor-core vertex into is_tc[nv] (tuning first if needed) and, when
+ * tuned_ms is not NULL, the measured time of the chosen split (0 if the
+ * policy is not AUTO). */
+enum gbtn_tc_policy { GBTN_TC_AUTO = 0, GBTN_TC_ALL = 1, GBTN_TC_NATIVE = 2, GBTN_TC_OFF = 3 };
+int gbtn_plan_set_tc_policy(gbtn_plan* plan, int32_t policy);
+int gbtn_plan_tc_split(gbtn_plan* plan, int32_t* is_tc, double* tuned_ms);
 
 /* Replaces: bpc[v] = tensor (update_factors, abstractbeliefpropagationcache.jl:158-171).
  * bra may be NULL unless the plan has separate_bra. */

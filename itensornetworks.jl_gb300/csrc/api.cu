@@ -93,11 +93,19 @@ struct gbtn_plan {
   // work lists: index 0 = all vertices, 1.. = colour classes; two size classes each
   std::vector<std::pair<WorkList, WorkList>> lists;
   std::vector<std::unique_ptr<DevBuf<int>>> list_store;
-  // tensor-core split of every list: eligible vertices (degree 4, d = 2,
-  // chi = 8, bra = ket) and the rest, which run the SIMT kernel
+  // tensor-core split of every list: vertices routed to the tensor-core
+  // kernel (padded to degree 4, chi = 8; bra = ket) and the rest, which run
+  // the FP32 SIMT kernel.  Candidates (tc_paddable) own an image slot; the
+  // policy (and, for GBTN_TC_AUTO, the autotuner) chooses which of them use it.
   std::vector<WorkList> tc_lists;
   std::vector<std::pair<WorkList, WorkList>> rest_lists;
+  std::vector<std::unique_ptr<DevBuf<int>>> tc_store;
   std::vector<int> tc_slot_vertex;
+  std::vector<char> tc_cand, tc_use;
+  int tc_policy = GBTN_TC_AUTO;
+  bool tc_tuned = false;
+  int ncol = 0;
+  double tc_tune_best_ms = 0.0;
   DevBuf<int> d_vslot, d_tc_slot_vertex, d_err;
   DevBuf<TcRec> d_tcrec;
   DevBuf<__nv_bfloat16> d_zimg;
@@ -174,7 +182,8 @@ void require(bool c, const std::string& m) {
   if (!c) throw InvalidArg(m);
 }
 
-WorkList make_list(gbtn_plan* P, const std::vector<int>& verts, int team) {
+WorkList make_list(gbtn_plan* P, const std::vector<int>& verts, int team,
+                   std::vector<std::unique_ptr<DevBuf<int>>>* store = nullptr) {
   WorkList w;
   w.count = (int)verts.size();
   w.team = team;
@@ -185,14 +194,15 @@ WorkList make_list(gbtn_plan* P, const std::vector<int>& verts, int team) {
   auto buf = std::make_unique<DevBuf<int>>();
   buf->upload(verts, P->ctx->stream);
   w.d_vertices = buf->p;
-  P->list_store.push_back(std::move(buf));
+  (store ? *store : P->list_store).push_back(std::move(buf));
   return w;
 }
 
-std::pair<WorkList, WorkList> split_list(gbtn_plan* P, const std::vector<int>& verts) {
+std::pair<WorkList, WorkList> split_list(gbtn_plan* P, const std::vector<int>& verts,
+                                         std::vector<std::unique_ptr<DevBuf<int>>>* store = nullptr) {
   std::vector<int> small, large;
   for (int v : verts) (P->vd[v].n <= kSmallN ? small : large).push_back(v);
-  return {make_list(P, small, 32), make_list(P, large, 256)};
+  return {make_list(P, small, 32, store), make_list(P, large, 256, store)};
 }
 
 void copy_out(gbtn_plan* P, void* dst, const void* src, size_t bytes, int mem) {
@@ -287,6 +297,136 @@ void ensure_zimg(gbtn_plan* P) {
     launch_build_zimg(P->d_tc_slot_vertex.p, n, P->d_vd.p, P->d_fac.p, P->d_zimg.p, P->ctx->stream);
     P->zimg_valid = true;
   }
+}
+
+// Algorithmic flops of all outgoing messages of a vertex: k messages of
+// 2 d prod(chi) sum(chi) each (updated_message, abstractbeliefpropagationcache.jl:225-239).
+double vertex_flops(const VDesc& d) {
+  double sc = 0.0;
+  for (int p = 0; p < d.k; ++p) sc += d.chi[p];
+  return d.k * 2.0 * d.n * sc;
+}
+
+// Image slots and records for every candidate vertex.
+void build_tc_slots(gbtn_plan* P) {
+  cudaStream_t s = P->ctx->stream;
+  std::vector<int> vslot(P->nv, -1);
+  P->tc_slot_vertex.clear();
+  for (int v = 0; v < P->nv; ++v)
+    if (P->tc_cand[v]) {
+      vslot[v] = (int)P->tc_slot_vertex.size();
+      P->tc_slot_vertex.push_back(v);
+    }
+  P->d_vslot.upload(vslot, s);
+  std::vector<TcRec> recs(std::max<size_t>(P->tc_slot_vertex.size(), 1));
+  for (size_t i = 0; i < P->tc_slot_vertex.size(); ++i) recs[i] = tc_record(P->vd[P->tc_slot_vertex[i]], P->msg_off);
+  P->d_tcrec.upload(recs, s);
+  std::vector<int> sv = P->tc_slot_vertex;
+  if (sv.empty()) sv.push_back(0);
+  P->d_tc_slot_vertex.upload(sv, s);
+  P->zimg_valid = false;
+}
+
+// Work lists (all vertices, then every colour class) for the split `use`.
+void build_tc_lists(gbtn_plan* P, const std::vector<char>& use) {
+  GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));  // no launch still reads the old lists
+  P->tc_use = use;
+  P->tc_lists.clear();
+  P->rest_lists.clear();
+  P->tc_store.clear();
+  for (int li = 0; li <= P->ncol; ++li) {
+    std::vector<int> tcv, rest;
+    for (int v = 0; v < P->nv; ++v) {
+      if (li > 0 && P->color[v] != li - 1) continue;
+      (use[v] ? tcv : rest).push_back(v);
+    }
+    P->tc_lists.push_back(make_list(P, tcv, 128, &P->tc_store));
+    P->rest_lists.push_back(split_list(P, rest, &P->tc_store));
+  }
+}
+
+template <class F>
+float time_ms(cudaStream_t s, F&& fn, int reps) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  GBTN_CUDA(cudaEventCreate(&a));
+  GBTN_CUDA(cudaEventCreate(&b));
+  fn();  // warm-up
+  GBTN_CUDA(cudaEventRecord(a, s));
+  for (int r = 0; r < reps; ++r) fn();
+  GBTN_CUDA(cudaEventRecord(b, s));
+  GBTN_CUDA(cudaEventSynchronize(b));
+  float ms = 0.f;
+  GBTN_CUDA(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / reps;
+}
+
+// Choose which candidates run on the tensor cores.  GBTN_TC_AUTO measures:
+// candidates sorted by algorithmic flops are split at a point q (the q
+// smallest on the FP32 SIMT kernel, the rest on the tensor-core kernel --
+// padding makes the tensor-core cost per vertex independent of its shape,
+// while the SIMT cost grows with it), both launches of every split are timed
+// on this plan's own vertices and messages, and the fastest split is kept
+// (split points 0, 1/4, .., 1, then +-1/8 around the best).  The FP32
+// messages of the current state must be in msg32[0].
+void tune_tc_split(gbtn_plan* P) {
+  if (P->tc_tuned) return;
+  const int nv = P->nv;
+  std::vector<char> use(nv, 0);
+  if (P->tc_policy == GBTN_TC_ALL) {
+    use = P->tc_cand;
+  } else if (P->tc_policy == GBTN_TC_NATIVE) {
+    for (int v = 0; v < nv; ++v) use[v] = P->tc_cand[v] && tc_native(P->vd[v]);
+  } else if (P->tc_policy == GBTN_TC_AUTO) {
+    std::vector<int> cv;
+    for (int v = 0; v < nv; ++v)
+      if (P->tc_cand[v]) cv.push_back(v);
+    if (!cv.empty()) {
+      std::stable_sort(cv.begin(), cv.end(),
+                       [&](int a, int b) { return vertex_flops(P->vd[a]) < vertex_flops(P->vd[b]); });
+      cudaStream_t s = P->ctx->stream;
+      ensure_zimg(P);
+      DevBuf<float> out;
+      out.alloc(P->n_msg);
+      const float* in = P->d_msg32[0].p;
+      const int N = (int)cv.size();
+      std::map<int, double> cost;  // split index -> measured ms
+      auto measure = [&](int k) {
+        if (cost.count(k)) return;
+        std::vector<std::unique_ptr<DevBuf<int>>> store;
+        const std::vector<int> lo(cv.begin(), cv.begin() + k), hi(cv.begin() + k, cv.end());
+        const std::pair<WorkList, WorkList> sl = split_list(P, lo, &store);
+        const WorkList th = make_list(P, hi, 128, &store);
+        double ms = 0.0;
+        if (!lo.empty())
+          ms += time_ms(s, [&] {
+            launch_bp_vertices<float>(sl.first, P->d_vd.p, P->d_fac32.p, nullptr, in, out.p, P->d_msg_off.p,
+                                      P->d_diffs.p, nullptr, 1, 1, s);
+            launch_bp_vertices<float>(sl.second, P->d_vd.p, P->d_fac32.p, nullptr, in, out.p, P->d_msg_off.p,
+                                      P->d_diffs.p, nullptr, 1, 1, s);
+          }, 3);
+        if (!hi.empty())
+          ms += time_ms(s, [&] {
+            launch_tc_vertices(th.d_vertices, th.count, P->d_vslot.p, P->d_tcrec.p, P->d_zimg.p, in, out.p,
+                               P->d_diffs.p, nullptr, 1, 1, P->d_err.p, s);
+          }, 3);
+        cost[k] = ms;
+      };
+      int best = 0;
+      for (int q = 0; q <= 4; ++q) measure((int)((long long)N * q / 4));
+      for (auto& kv : cost)
+        if (kv.second < cost[best]) best = kv.first;
+      for (int d : {-1, 1}) measure(std::min(N, std::max(0, best + d * N / 8)));
+      for (auto& kv : cost)
+        if (kv.second < cost[best]) best = kv.first;
+      P->tc_tune_best_ms = cost[best];
+      for (int i = best; i < N; ++i) use[cv[i]] = 1;
+      check_device_error(P);
+    }
+  }
+  build_tc_lists(P, use);
+  P->tc_tuned = true;
 }
 
 // BF16 sweeps (parallel or coloured): tensor-core kernel on the eligible
@@ -680,45 +820,19 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
       if (P->color[v] == c) vs.push_back(v);
     P->lists.push_back(split_list(P.get(), vs));
   }
-  // tensor-core vertices: one swizzled BF16 image slot each
-  std::vector<int> vslot(g->nv, -1);
+  // tensor-core candidates: one swizzled BF16 image slot each; until the
+  // first reduced-precision run tunes the split, only native vertices use it
+  P->ncol = ncol;
+  P->tc_cand.assign(g->nv, 0);
   if (!P->sep_bra && P->n_msg < (1LL << 31))
-    for (int v = 0; v < g->nv; ++v)
-      if (tc_eligible(P->vd[v])) {
-        vslot[v] = (int)P->tc_slot_vertex.size();
-        P->tc_slot_vertex.push_back(v);
-      }
-  P->d_vslot.upload(vslot, s);
-  {
-    std::vector<TcRec> recs(std::max<size_t>(P->tc_slot_vertex.size(), 1));
-    for (size_t i = 0; i < P->tc_slot_vertex.size(); ++i) {
-      const VDesc& d = P->vd[P->tc_slot_vertex[i]];
-      TcRec r{};
-      for (int p = 0; p < 4; ++p) {
-        r.in_off[p] = (int)P->msg_off[d.in_de[p]];
-        r.out_off[p] = (int)P->msg_off[d.out_de[p]];
-        r.out_de[p] = d.out_de[p];
-      }
-      r.net = d.net;
-      recs[i] = r;
-    }
-    P->d_tcrec.upload(recs, s);
-  }
-  {
-    std::vector<int> sv = P->tc_slot_vertex;
-    if (sv.empty()) sv.push_back(0);
-    P->d_tc_slot_vertex.upload(sv, s);
-  }
+    for (int v = 0; v < g->nv; ++v) P->tc_cand[v] = tc_paddable(P->vd[v]) ? 1 : 0;
+  build_tc_slots(P.get());
   P->d_err.alloc(1);
   GBTN_CUDA(cudaMemsetAsync(P->d_err.p, 0, sizeof(int), s));
-  for (int li = 0; li <= ncol; ++li) {
-    std::vector<int> tcv, rest;
-    for (int v = 0; v < g->nv; ++v) {
-      if (li > 0 && P->color[v] != li - 1) continue;
-      (vslot[v] >= 0 ? tcv : rest).push_back(v);
-    }
-    P->tc_lists.push_back(make_list(P.get(), tcv, 128));
-    P->rest_lists.push_back(split_list(P.get(), rest));
+  {
+    std::vector<char> use(g->nv, 0);
+    for (int v = 0; v < g->nv; ++v) use[v] = P->tc_cand[v] && tc_native(P->vd[v]);
+    build_tc_lists(P.get(), use);
   }
   launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[0].p, GBTN_INIT_IDENTITY, s);
   GBTN_CUDA(cudaStreamSynchronize(s));
@@ -861,9 +975,10 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
   } else if (o->precision == GBTN_BF16) {
     ensure_f32(P);
-    ensure_zimg(P);
     int c32 = 0;
     launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, s);
+    tune_tc_split(P);
+    ensure_zimg(P);
     run_sweeps_bf16(P, o->schedule, o->maxiter, o->tol, o->normalize, c32);
     launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
     finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
@@ -874,6 +989,7 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     const int it32 = o->maxiter_f32 > 0 ? o->maxiter_f32 : o->maxiter;
     launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, s);
     if (o->schedule != GBTN_SCHED_SEQUENTIAL && !P->tc_slot_vertex.empty()) {
+      tune_tc_split(P);
       ensure_zimg(P);
       const double tol16 = o->tol_bf16 > 0 ? o->tol_bf16 : 1e-6;
       const int it16 = o->maxiter_bf16 > 0 ? o->maxiter_bf16 : o->maxiter;
@@ -888,6 +1004,31 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
                        P->sep_bra ? P->d_bra.p : nullptr, P->cur);
     finish_iters(P, want_diff, nref, iters, mean_diff);
   }
+  API_CATCH(C)
+}
+
+int gbtn_plan_set_tc_policy(gbtn_plan* P, int32_t policy) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P, "NULL argument");
+  require(policy >= GBTN_TC_AUTO && policy <= GBTN_TC_OFF, "unknown tensor-core policy");
+  P->tc_policy = policy;
+  P->tc_tuned = false;
+  P->tc_tune_best_ms = 0.0;
+  API_CATCH(C)
+}
+
+int gbtn_plan_tc_split(gbtn_plan* P, int32_t* is_tc, double* tuned_ms) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && is_tc, "NULL argument");
+  if (!P->tc_tuned) {
+    ensure_f32(P);
+    launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, P->ctx->stream);
+    tune_tc_split(P);
+  }
+  for (int v = 0; v < P->nv; ++v) is_tc[v] = P->tc_use[v] ? 1 : 0;
+  if (tuned_ms) *tuned_ms = P->tc_tune_best_ms;
   API_CATCH(C)
 }
 

@@ -24,6 +24,13 @@
 // BP is invariant under message scaling, so this reduced-precision phase
 // normalises in FP32; the FP64 refinement sweeps that follow normalise in FP64.
 //
+// A vertex with fewer legs or smaller bond dimensions (d = 2, degree <= 4,
+// chi <= 8) runs the same kernel zero-padded: its image holds zeros beyond
+// each chi, a missing leg has dimension 1 and receives the 1 x 1 message 1,
+// compact chi x chi messages are gathered into the 8 x 8 layout and scattered
+// back.  Every product with a padding entry is an exact zero, so norms and
+// message_diff are those of the compact messages.
+//
 // Per vertex: one 16 KB TMA bulk copy of the pre-swizzled BF16 image of Z,
 // 24 tcgen05.mma instructions (4.2 MFLOP) accumulating in FP32 in TMEM (128
 // columns: D1 | D1', then G34 | G12), two MMA round trips, seven CTA barriers,
@@ -108,10 +115,21 @@ __device__ __forceinline__ void store_half_row(unsigned char* tile, int row, int
   }
 }
 
-// Normalise one 8 x 8 message held by a warp (two values per lane), store it
-// as FP32, and (want_diff) return message_diff(new, old)
-// (abstractbeliefpropagationcache.jl:32-36), accumulated in FP64.
-__device__ __forceinline__ double tc_finalize(const float* res, const float* old, float* out, int normalize,
+// Entry e (b = e % 8, a = e / 8) of the 8 x 8 padded image of a compact
+// chi x chi message; chi = 0 marks a padding leg, whose message is 1 at (0, 0).
+__device__ __forceinline__ float padded_msg(const float* m, int off, int chi, int e) {
+  const int b = e & 7, a = e >> 3;
+  if (chi == 0) return e == 0 ? 1.f : 0.f;
+  return (b < chi && a < chi) ? m[off + b + chi * a] : 0.f;
+}
+
+__device__ __forceinline__ int rec_chi(int chi4, int p) { return (chi4 >> (8 * p)) & 0xff; }
+
+// Normalise one 8 x 8 message held by a warp (two values per lane), store its
+// compact chi x chi part as FP32, and (want_diff) return
+// message_diff(new, old) (abstractbeliefpropagationcache.jl:32-36),
+// accumulated in FP64.  Entries outside chi x chi are exact zeros.
+__device__ __forceinline__ double tc_finalize(const float* res, const float* old, float* out, int chi, int normalize,
                                               bool want_diff, int lane) {
   const float x0 = res[lane], x1 = res[lane + 32];
   float ss = fmaf(x0, x0, x1 * x1);
@@ -119,25 +137,27 @@ __device__ __forceinline__ double tc_finalize(const float* res, const float* old
   for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
   const float sc = (normalize && ss > 0.f) ? rsqrtf(ss) : 1.f;
   const float n0 = x0 * sc, n1 = x1 * sc;
+  const int b = lane & 7, a0 = lane >> 3, a1 = a0 + 4;
+  const bool v0 = b < chi && a0 < chi, v1 = b < chi && a1 < chi;
+  const int i0 = b + chi * a0, i1 = b + chi * a1;
   float o0 = 0.f, o1 = 0.f;
   if (want_diff) {
-    o0 = old[lane];
-    o1 = old[lane + 32];
+    if (v0) o0 = old[i0];
+    if (v1) o1 = old[i1];
   }
   __syncwarp();
-  out[lane] = n0;
-  out[lane + 32] = n1;
+  if (v0) out[i0] = n0;
+  if (v1) out[i1] = n1;
   double diff = 0.0;
   if (want_diff) {
-    const double a0 = n0, a1 = n1, b0 = o0, b1 = o1;
-    const double dot = tc_warp_sum(a0 * b0 + a1 * b1);
-    const double na = tc_warp_sum(a0 * a0 + a1 * a1);
+    const double a0d = n0, a1d = n1, b0 = o0, b1 = o1;
+    const double dot = tc_warp_sum(a0d * b0 + a1d * b1);
+    const double na = tc_warp_sum(a0d * a0d + a1d * a1d);
     const double nb = tc_warp_sum(b0 * b0 + b1 * b1);
     diff = 1.0 - (dot * dot) / (na * nb);
   }
   return diff;
 }
-
 }  // namespace
 
 namespace {
@@ -262,28 +282,35 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     const int sl = vslot[work[w]];
     if (t == 0) issue_z(sl);
     cnet = recs[sl].net;
-    cm0 = msg_in[recs[sl].in_off[q0 >> 6] + e];
-    cm1 = msg_in[recs[sl].in_off[q1 >> 6] + e];
+    const int c4 = recs[sl].chi4;
+    cm0 = padded_msg(msg_in, recs[sl].in_off[q0 >> 6], rec_chi(c4, q0 >> 6), e);
+    cm1 = padded_msg(msg_in, recs[sl].in_off[q1 >> 6], rec_chi(c4, q1 >> 6), e);
   }
   for (; w < nwork; w += gridDim.x) {
     const int sl = vslot[work[w]];
     const int out_off_w = recs[sl].out_off[warp];
     const int out_de_w = recs[sl].out_de[warp];
+    const int cchi4 = recs[sl].chi4;
+    const int chi_w = rec_chi(cchi4, warp);
     // next vertex: record now, messages later in this iteration
     const int wn = w + gridDim.x;
-    int nsl = -1, nin0 = 0, nin1 = 0, nnet = 0;
+    int nsl = -1, nin0 = 0, nin1 = 0, nnet = 0, nchi0 = 8, nchi1 = 8;
     if (wn < nwork) {
       nsl = vslot[work[wn]];
       nin0 = recs[nsl].in_off[q0 >> 6];
       nin1 = recs[nsl].in_off[q1 >> 6];
       nnet = recs[nsl].net;
+      const int n4 = recs[nsl].chi4;
+      nchi0 = rec_chi(n4, q0 >> 6);
+      nchi1 = rec_chi(n4, q1 >> 6);
     }
     float nm0 = 0.f, nm1 = 0.f;
 
     if (converged && converged[cnet]) {  // network done: carry its messages forward
-      const int o0 = recs[sl].out_off[q0 >> 6], o1 = recs[sl].out_off[q1 >> 6];
-      msg_out[o0 + e] = msg_in[o0 + e];
-      msg_out[o1 + e] = msg_in[o1 + e];
+      const int p0 = q0 >> 6, p1 = q1 >> 6;
+      const int c0 = rec_chi(cchi4, p0), c1 = rec_chi(cchi4, p1);
+      if (e < c0 * c0) msg_out[recs[sl].out_off[p0] + e] = msg_in[recs[sl].out_off[p0] + e];
+      if (e < c1 * c1) msg_out[recs[sl].out_off[p1] + e] = msg_in[recs[sl].out_off[p1] + e];
       if (t == 0) {
         const bool ok = wait_z();
         *abort_flag = ok ? 0 : 1;
@@ -292,8 +319,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
       __syncthreads();
       if (*abort_flag) break;
       if (nsl >= 0) {
-        cm0 = msg_in[nin0 + e];
-        cm1 = msg_in[nin1 + e];
+        cm0 = padded_msg(msg_in, nin0, nchi0, e);
+        cm1 = padded_msg(msg_in, nin1, nchi1, e);
         cnet = nnet;
       }
       continue;
@@ -383,8 +410,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     }
     // the next vertex's incoming messages, ahead of use
     if (nsl >= 0) {
-      nm0 = msg_in[nin0 + e];
-      nm1 = msg_in[nin1 + e];
+      nm0 = padded_msg(msg_in, nin0, nchi0, e);
+      nm1 = padded_msg(msg_in, nin1, nchi1, e);
     }
     if (t == 0) {
       const bool ok = wait_mma();
@@ -405,8 +432,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
       RES[(t < 64 ? 128 : 0) + u] = pp[u] + pp[64 + u] + pp[128 + u] + pp[192 + u];  // out3 | out1
     }
     __syncthreads();
-    {
-      const double df = tc_finalize(RES + 64 * warp, msg_in + out_off_w, msg_out + out_off_w, normalize,
+    if (chi_w > 0) {  // warp-uniform: a padding leg has no outgoing message
+      const double df = tc_finalize(RES + 64 * warp, msg_in + out_off_w, msg_out + out_off_w, chi_w, normalize,
                                     want_diff != 0, lane);
       if (want_diff && lane == 0) diffs[out_de_w] = df;
     }
@@ -429,28 +456,69 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
 
 namespace {
 
-// Swizzled BF16 image of Z for every slot: element A[s, c1, c2] (idx = s + 2 c1
-// + 128 c2) goes to row r = 64 s + c2, 16-byte chunk (c1 / 8) ^ (r % 8).
+// Swizzled BF16 image of Z for every slot: image element (s, c1, c2) with
+// c1 = l1 + 8 l2, c2 = l3 + 8 l4 goes to row r = 64 s + c2, 16-byte chunk
+// (c1 / 8) ^ (r % 8); it holds A[s, l1..lk] when every l_p is inside the
+// vertex's bond dimension (l_p = 0 on a padding leg p >= k) and zero otherwise.
 __global__ void build_zimg_kernel(const int* __restrict__ slot_vertex, int nslot, const VDesc* __restrict__ vd,
                                   const double* __restrict__ fac, __nv_bfloat16* __restrict__ zimg) {
   const int slot = blockIdx.x;
   if (slot >= nslot) return;
-  const double* a = fac + vd[slot_vertex[slot]].a_off;
+  const VDesc d = vd[slot_vertex[slot]];
+  const double* a = fac + d.a_off;
   __nv_bfloat16* z = zimg + (size_t)slot * kZElems;
   for (int idx = threadIdx.x; idx < (int)kZElems; idx += blockDim.x) {
     const int s = idx & 1, c1 = (idx >> 1) & 63, c2 = idx >> 7;
+    const int l[4] = {c1 & 7, c1 >> 3, c2 & 7, c2 >> 3};
+    bool in = true;
+    long long src = s;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      if (p < d.k) {
+        in = in && l[p] < d.chi[p];
+        src += (long long)l[p] * d.st[p];
+      } else {
+        in = in && l[p] == 0;
+      }
+    }
     const int r = 64 * s + c2;
-    z[r * 64 + (((c1 >> 3) ^ (r & 7)) << 3) + (c1 & 7)] = __double2bfloat16(a[idx]);
+    z[r * 64 + (((c1 >> 3) ^ (r & 7)) << 3) + (c1 & 7)] = __double2bfloat16(in ? a[src] : 0.0);
   }
 }
 
 }  // namespace
 
-bool tc_eligible(const VDesc& d) {
+bool tc_native(const VDesc& d) {
   if (d.k != 4 || d.d != 2) return false;
   for (int p = 0; p < 4; ++p)
     if (d.chi[p] != 8) return false;
   return true;
+}
+
+bool tc_paddable(const VDesc& d) {
+  if (d.k < 1 || d.k > 4 || d.d != 2) return false;
+  for (int p = 0; p < d.k; ++p)
+    if (d.chi[p] < 1 || d.chi[p] > 8) return false;
+  return true;
+}
+
+TcRec tc_record(const VDesc& d, const std::vector<long long>& msg_off) {
+  TcRec r{};
+  r.chi4 = 0;
+  for (int p = 0; p < 4; ++p) {
+    if (p < d.k) {
+      r.in_off[p] = (int)msg_off[d.in_de[p]];
+      r.out_off[p] = (int)msg_off[d.out_de[p]];
+      r.out_de[p] = d.out_de[p];
+      r.chi4 |= d.chi[p] << (8 * p);
+    } else {
+      r.in_off[p] = 0;
+      r.out_off[p] = 0;
+      r.out_de[p] = -1;
+    }
+  }
+  r.net = d.net;
+  return r;
 }
 
 void launch_build_zimg(const int* slot_vertex, int nslot, const VDesc* vd, const double* fac, __nv_bfloat16* zimg,

@@ -24,6 +24,7 @@ ERRORS = {
 }
 HOST, DEVICE = 0, 1
 KCLASS_TENSOR_CORE, KCLASS_SIMT_F32, KCLASS_SIMT_F64 = 0, 1, 2
+TC_POLICIES = {"auto": 0, "all": 1, "native": 2, "off": 3}
 SCHED = {"sequential": 0, "parallel": 1, "colored": 2}
 PRECISION = {"f64": 0, "f32": 1, "bf16": 2, "mixed": 3}
 INIT = {"identity": 0, "ones": 1}
@@ -110,6 +111,8 @@ SIGNATURES = {
     "gbtn_plan_create": (_I, [_P, C.POINTER(GraphDesc), C.POINTER(_P)]),
     "gbtn_plan_destroy": (_I, [_P]),
     "gbtn_plan_sizes": (_I, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "gbtn_plan_set_tc_policy": (_I, [_P, C.c_int32]),
+    "gbtn_plan_tc_split": (_I, [_P, _I32, _D]),
     "gbtn_set_factors": (_I, [_P, _P, _P, _I]),
     "gbtn_get_factors": (_I, [_P, _P, _I]),
     "gbtn_set_messages": (_I, [_P, _P, _I]),

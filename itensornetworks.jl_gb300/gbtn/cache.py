@@ -124,6 +124,20 @@ class BeliefPropagationCache:
                     print(f"BP converged to desired precision after {it[n]} iterations.")
         return self
 
+    def set_tc_policy(self, policy):
+        """Tensor-core routing of the BF16 phase: "auto" (timed on this plan's
+        vertices), "all" (every d = 2, degree <= 4, chi <= 8 vertex, padded),
+        "native" (degree 4, chi = 8 only) or "off"."""
+        self._c(self.lib.gbtn_plan_set_tc_policy(self.handle, _lib.TC_POLICIES[policy]))
+        return self
+
+    def tc_split(self):
+        """(is_tc per vertex as a bool array, measured ms of the chosen split)."""
+        out = np.zeros(max(self.tn.nv, 1), dtype=np.int32)
+        ms = C.c_double(0.0)
+        self._c(self.lib.gbtn_plan_tc_split(self.handle, iptr(out), C.byref(ms)))
+        return out[:self.tn.nv].astype(bool), ms.value
+
     def updated_message(self, de):
         c = self.tn.edge_dims[de // 2]
         out = np.empty(c * c)

@@ -3,7 +3,9 @@
 Tolerances: one BF16 sweep from the same input messages agrees with the FP64
 sweep to 3e-2 absolute on unit-norm messages (BF16 keeps 8 significant bits;
 a layout or descriptor error shows up as O(0.1-1) differences); messages of
-vertices outside the tensor-core class run FP32 and agree to 1e-5.  The mixed
+vertices outside the tensor-core class run FP32 and agree to 1e-5.  Vertices
+padded to the kernel's shape (boundary legs, bond dimensions below 8, leaves)
+meet the same 3e-2 and keep their compact shapes.  The mixed
 pipeline (BF16 -> FP32 -> FP64) meets <= 1e-6 max relative error in <Sz>
 after two FP64 sweeps and 1e-10 after a full FP64 phase."""
 import numpy as np
@@ -41,11 +43,13 @@ def test_one_bf16_sweep_matches_fp64_sweep():
     tn, g, A = pair(6, 3)
     m3, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=3, schedule="parallel")
     m4, _, _ = O.bp_update(g, A, m3, maxiter=1, schedule="parallel")
-    bpc = gbtn.BeliefPropagationCache(tn)
+    bpc = gbtn.BeliefPropagationCache(tn).set_tc_policy("native")
     bpc.set_messages(m3)
     bpc.update(maxiter=1, schedule="parallel", precision="bf16")
     got = bpc.messages()
     tcset = tc_directed_edges(g)
+    is_tc, _ = bpc.tc_split()
+    assert {v for v in range(g.nv) if is_tc[v]} == {v for v in range(g.nv) if len(g.legs[v]) == 4}
     assert len(tcset) == 4 * 16
     err_tc = max(np.max(np.abs(got[de] - m4[de])) for de in tcset)
     err_rest = max(np.max(np.abs(got[de] - m4[de])) for de in range(2 * g.ne) if de not in tcset)
@@ -59,7 +63,7 @@ def test_bf16_colored_schedule_matches_fp64():
     tn, g, A = pair(5, 8)
     m2, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=2, schedule="parallel")
     m3, _, _ = O.bp_update(g, A, m2, maxiter=1, schedule="colored")
-    bpc = gbtn.BeliefPropagationCache(tn)
+    bpc = gbtn.BeliefPropagationCache(tn).set_tc_policy("all")
     bpc.set_messages(m2)
     bpc.update(maxiter=1, schedule="colored", precision="bf16")
     got = bpc.messages()
@@ -100,4 +104,102 @@ def test_bf16_batch_with_uneven_shapes_and_convergence():
                                     "parallel", None, 400, tol=None, nthreads=4)
         ref = O.expect1(g, A, O.unflatten_messages(g, mc), O.SZ)
         np.testing.assert_allclose(sz[off:off + g.nv], ref, atol=1e-6 * np.max(np.abs(ref)))
+        off += g.nv
+
+
+def uneven(L, seed, lo=2, hi=8, d=2):
+    rng = np.random.default_rng(1000 + seed)
+    g0 = O.square_lattice(L, L, chi=2, d=d)
+    dims = [int(x) for x in rng.integers(lo, hi + 1, size=g0.ne)]
+    g = O.square_lattice(L, L, d=d, edge_dims=dims)
+    A = O.random_network(g, seed)
+    tn = gbtn.TensorNetwork(g.nv, g.edges, g.site_dims, g.edge_dims, [a.copy() for a in A])
+    return tn, g, A
+
+
+def test_padded_boundary_sweep_matches_fp64():
+    tn, g, A = pair(6, 5)
+    m3, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=3, schedule="parallel")
+    m4, _, _ = O.bp_update(g, A, m3, maxiter=1, schedule="parallel")
+    bpc = gbtn.BeliefPropagationCache(tn).set_tc_policy("all")
+    bpc.set_messages(m3)
+    bpc.update(maxiter=1, schedule="parallel", precision="bf16")
+    is_tc, _ = bpc.tc_split()
+    assert is_tc.all()  # corners (2 legs) and edges (3 legs) padded
+    got = bpc.messages()
+    err = max(np.max(np.abs(got[de] - m4[de])) for de in range(2 * g.ne))
+    assert err < 3e-2, f"padded tensor-core messages differ by {err:.3e}"
+    for de in range(2 * g.ne):
+        assert np.linalg.norm(got[de]) == pytest.approx(1.0, rel=1e-5)
+
+
+def test_padded_uneven_bond_dims_sweep_and_mixed_fixed_point():
+    tn, g, A = uneven(6, 7)
+    assert len(set(g.edge_dims)) > 3
+    m3, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=3, schedule="parallel")
+    m4, _, _ = O.bp_update(g, A, m3, maxiter=1, schedule="parallel")
+    bpc = gbtn.BeliefPropagationCache(tn).set_tc_policy("all")
+    bpc.set_messages(m3)
+    bpc.update(maxiter=1, schedule="parallel", precision="bf16")
+    got = bpc.messages()
+    for de in range(2 * g.ne):
+        assert got[de].shape == m4[de].shape
+    err = max(np.max(np.abs(got[de] - m4[de])) for de in range(2 * g.ne))
+    assert err < 3e-2, f"padded uneven-chi messages differ by {err:.3e}"
+    ref = gbtn.BeliefPropagationCache(tn).update(maxiter=400, schedule="parallel", precision="f64")
+    sz_ref = ref.expect(O.SZ)
+    mix = gbtn.BeliefPropagationCache(tn).set_tc_policy("all").update(maxiter=400, schedule="parallel",
+                                                                       precision="mixed")
+    np.testing.assert_allclose(mix.expect(O.SZ), sz_ref, rtol=0, atol=1e-10 * np.max(np.abs(sz_ref)))
+
+
+def test_padded_leaves_on_a_tree():
+    # random tree of degree <= 4 (vertex i attaches to an earlier vertex with a free leg)
+    rng = np.random.default_rng(4)
+    deg, edges = [0] * 24, []
+    for i in range(1, 24):
+        u = int(rng.choice([w for w in range(i) if deg[w] < 4]))
+        edges.append((u, i))
+        deg[u] += 1
+        deg[i] += 1
+    dims = [int(x) for x in rng.integers(2, 9, size=len(edges))]
+    g = O.Graph(24, sorted(edges), [2] * 24, dims)
+    A = O.random_network(g, 9)
+    tn = gbtn.TensorNetwork(g.nv, g.edges, g.site_dims, g.edge_dims, [a.copy() for a in A])
+    degs = [len(l) for l in g.legs]
+    assert 1 in degs
+    bpc = gbtn.BeliefPropagationCache(tn).set_tc_policy("all")
+    bpc.update(maxiter=60, schedule="parallel", precision="bf16")
+    is_tc, _ = bpc.tc_split()
+    assert all(is_tc[v] == (degs[v] <= 4) for v in range(g.nv))
+    m, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=60, schedule="parallel")
+    got = bpc.messages()
+    err = max(np.max(np.abs(got[de] - m[de])) for de in range(2 * g.ne))
+    assert err < 3e-2
+    mix = gbtn.BeliefPropagationCache(tn).set_tc_policy("all").update(maxiter=60, schedule="parallel",
+                                                                       precision="mixed")
+    ref = O.expect1(g, A, m, O.SZ)
+    np.testing.assert_allclose(mix.expect(O.SZ), ref, rtol=0, atol=1e-10 * np.max(np.abs(ref)))
+
+
+def test_autotuned_split_on_uneven_batch():
+    nets, pairs = [], []
+    for k, L in enumerate([8, 12, 16]):
+        tn, g, A = uneven(L, 20 + k)
+        nets.append(tn)
+        pairs.append((g, A))
+    batch = gbtn.disjoint_union(nets)
+    bpc = gbtn.BeliefPropagationCache(batch)
+    is_tc, ms = bpc.tc_split()
+    assert ms > 0.0
+    cand = [batch.site_dims[v] == 2 and len(batch.legs[v]) <= 4 for v in range(batch.nv)]
+    assert all(cand[v] for v in range(batch.nv) if is_tc[v])
+    bpc.update(maxiter=300, schedule="parallel", precision="mixed")
+    sz = bpc.expect(O.SZ)
+    off = 0
+    for g, A in pairs:
+        mc, _, _ = build_oracle.run(g, O.flatten_tensors(A), O.flatten_messages(g, O.identity_messages(g)),
+                                    "parallel", None, 400, tol=None, nthreads=4)
+        ref = O.expect1(g, A, O.unflatten_messages(g, mc), O.SZ)
+        np.testing.assert_allclose(sz[off:off + g.nv], ref, rtol=0, atol=1e-10 * np.max(np.abs(ref)))
         off += g.nv
