@@ -59,6 +59,12 @@ struct DevBuf {
   }
 };
 
+// Tensor-core work list: one record per vertex, in list order.
+struct TcList {
+  TcRec* d_recs = nullptr;
+  int count = 0;
+};
+
 struct HostWork {
   std::vector<int> vertices;
   int ncap = 0, maxdeg = 0, team = 32;
@@ -97,17 +103,18 @@ struct gbtn_plan {
   // kernel (padded to degree 4, chi = 8; bra = ket) and the rest, which run
   // the FP32 SIMT kernel.  Candidates (tc_paddable) own an image slot; the
   // policy (and, for GBTN_TC_AUTO, the autotuner) chooses which of them use it.
-  std::vector<WorkList> tc_lists;
+  std::vector<TcList> tc_lists;
   std::vector<std::pair<WorkList, WorkList>> rest_lists;
   std::vector<std::unique_ptr<DevBuf<int>>> tc_store;
-  std::vector<int> tc_slot_vertex;
+  std::vector<std::unique_ptr<DevBuf<TcRec>>> tc_rec_store;
+  std::vector<int> tc_slot_vertex, tc_vslot;
+  std::vector<TcRec> tc_recs;  // by slot
   std::vector<char> tc_cand, tc_use;
   int tc_policy = GBTN_TC_AUTO;
   bool tc_tuned = false;
   int ncol = 0;
   double tc_tune_best_ms = 0.0;
-  DevBuf<int> d_vslot, d_tc_slot_vertex, d_err;
-  DevBuf<TcRec> d_tcrec;
+  DevBuf<int> d_tc_slot_vertex, d_err;
   DevBuf<__nv_bfloat16> d_zimg;
   bool zimg_valid = false;
   // sequential schedule storage
@@ -310,21 +317,34 @@ double vertex_flops(const VDesc& d) {
 // Image slots and records for every candidate vertex.
 void build_tc_slots(gbtn_plan* P) {
   cudaStream_t s = P->ctx->stream;
-  std::vector<int> vslot(P->nv, -1);
+  P->tc_vslot.assign(P->nv, -1);
   P->tc_slot_vertex.clear();
+  P->tc_recs.clear();
   for (int v = 0; v < P->nv; ++v)
     if (P->tc_cand[v]) {
-      vslot[v] = (int)P->tc_slot_vertex.size();
+      P->tc_vslot[v] = (int)P->tc_slot_vertex.size();
       P->tc_slot_vertex.push_back(v);
+      TcRec r = tc_record(P->vd[v], P->msg_off);
+      r.slot = P->tc_vslot[v];
+      P->tc_recs.push_back(r);
     }
-  P->d_vslot.upload(vslot, s);
-  std::vector<TcRec> recs(std::max<size_t>(P->tc_slot_vertex.size(), 1));
-  for (size_t i = 0; i < P->tc_slot_vertex.size(); ++i) recs[i] = tc_record(P->vd[P->tc_slot_vertex[i]], P->msg_off);
-  P->d_tcrec.upload(recs, s);
   std::vector<int> sv = P->tc_slot_vertex;
   if (sv.empty()) sv.push_back(0);
   P->d_tc_slot_vertex.upload(sv, s);
   P->zimg_valid = false;
+}
+
+TcList make_tc_list(gbtn_plan* P, const std::vector<int>& verts, std::vector<std::unique_ptr<DevBuf<TcRec>>>& store) {
+  std::vector<TcRec> recs;
+  recs.reserve(verts.size());
+  for (int v : verts) recs.push_back(P->tc_recs[P->tc_vslot[v]]);
+  auto buf = std::make_unique<DevBuf<TcRec>>();
+  buf->upload(recs, P->ctx->stream);
+  TcList l;
+  l.d_recs = buf->p;
+  l.count = (int)verts.size();
+  store.push_back(std::move(buf));
+  return l;
 }
 
 // Work lists (all vertices, then every colour class) for the split `use`.
@@ -334,13 +354,14 @@ void build_tc_lists(gbtn_plan* P, const std::vector<char>& use) {
   P->tc_lists.clear();
   P->rest_lists.clear();
   P->tc_store.clear();
+  P->tc_rec_store.clear();
   for (int li = 0; li <= P->ncol; ++li) {
     std::vector<int> tcv, rest;
     for (int v = 0; v < P->nv; ++v) {
       if (li > 0 && P->color[v] != li - 1) continue;
       (use[v] ? tcv : rest).push_back(v);
     }
-    P->tc_lists.push_back(make_list(P, tcv, 128, &P->tc_store));
+    P->tc_lists.push_back(make_tc_list(P, tcv, P->tc_rec_store));
     P->rest_lists.push_back(split_list(P, rest, &P->tc_store));
   }
 }
@@ -395,9 +416,10 @@ void tune_tc_split(gbtn_plan* P) {
       auto measure = [&](int k) {
         if (cost.count(k)) return;
         std::vector<std::unique_ptr<DevBuf<int>>> store;
+        std::vector<std::unique_ptr<DevBuf<TcRec>>> rstore;
         const std::vector<int> lo(cv.begin(), cv.begin() + k), hi(cv.begin() + k, cv.end());
         const std::pair<WorkList, WorkList> sl = split_list(P, lo, &store);
-        const WorkList th = make_list(P, hi, 128, &store);
+        const TcList th = make_tc_list(P, hi, rstore);
         double ms = 0.0;
         if (!lo.empty())
           ms += time_ms(s, [&] {
@@ -408,7 +430,7 @@ void tune_tc_split(gbtn_plan* P) {
           }, 3);
         if (!hi.empty())
           ms += time_ms(s, [&] {
-            launch_tc_vertices(th.d_vertices, th.count, P->d_vslot.p, P->d_tcrec.p, P->d_zimg.p, in, out.p,
+            launch_tc_vertices(th.d_recs, th.count, P->d_zimg.p, in, out.p,
                                P->d_diffs.p, nullptr, 1, 1, P->d_err.p, s);
           }, 3);
         cost[k] = ms;
@@ -439,10 +461,10 @@ void run_sweeps_bf16(gbtn_plan* P, int schedule, int maxiter, double tol, int no
   const int* conv = want_diff ? P->d_conv.p : nullptr;
   const float* fac = P->d_fac32.p;
   auto one = [&](size_t li, const float* in, float* out) {
-    const WorkList& tl = P->tc_lists[li];
+    const TcList& tl = P->tc_lists[li];
     {
       KTimer kt(P->ctx, GBTN_KCLASS_TENSOR_CORE, tl.count > 0);
-      launch_tc_vertices(tl.d_vertices, tl.count, P->d_vslot.p, P->d_tcrec.p, P->d_zimg.p, in, out, P->d_diffs.p,
+      launch_tc_vertices(tl.d_recs, tl.count, P->d_zimg.p, in, out, P->d_diffs.p,
                          conv, normalize, want_diff, P->d_err.p, s);
     }
     {

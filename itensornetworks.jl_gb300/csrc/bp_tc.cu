@@ -77,9 +77,9 @@ __device__ __forceinline__ double tc_warp_sum(double x) {
   return x;
 }
 
-// 32 lanes x 32 bits, 32 consecutive columns per thread.
-__device__ __forceinline__ void tmem_ld_x32(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[32];
+// 32 lanes x 32 bits, 32 consecutive columns per thread; the values are valid
+// after tmem_wait_ld (several loads may be in flight before one wait).
+__device__ __forceinline__ void tmem_ld_x32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
       "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -90,10 +90,9 @@ __device__ __forceinline__ void tmem_ld_x32(uint32_t taddr, float (&v)[32]) {
         "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr)
       : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   __nv_bfloat162 p = __floats2bfloat162_rn(a, b);
@@ -102,15 +101,15 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 
 // 32 FP32 values -> 16-byte chunks [c0, c0+4) of one 128-byte BF16 row of a
 // 128B-swizzled tile (chunk j lands at j ^ (row % 8)).
-__device__ __forceinline__ void store_half_row(unsigned char* tile, int row, int c0, const float (&v)[32]) {
+__device__ __forceinline__ void store_half_row(unsigned char* tile, int row, int c0, const uint32_t (&v)[32]) {
   uint4* base = reinterpret_cast<uint4*>(tile + row * 128);
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     uint4 q;
-    q.x = pack_bf16(v[8 * j + 0], v[8 * j + 1]);
-    q.y = pack_bf16(v[8 * j + 2], v[8 * j + 3]);
-    q.z = pack_bf16(v[8 * j + 4], v[8 * j + 5]);
-    q.w = pack_bf16(v[8 * j + 6], v[8 * j + 7]);
+    q.x = pack_bf16(__uint_as_float(v[8 * j + 0]), __uint_as_float(v[8 * j + 1]));
+    q.y = pack_bf16(__uint_as_float(v[8 * j + 2]), __uint_as_float(v[8 * j + 3]));
+    q.z = pack_bf16(__uint_as_float(v[8 * j + 4]), __uint_as_float(v[8 * j + 5]));
+    q.w = pack_bf16(__uint_as_float(v[8 * j + 6]), __uint_as_float(v[8 * j + 7]));
     base[(c0 + j) ^ (row & 7)] = q;
   }
 }
@@ -127,9 +126,10 @@ __device__ __forceinline__ int rec_chi(int chi4, int p) { return (chi4 >> (8 * p
 
 // Normalise one 8 x 8 message held by a warp (two values per lane), store its
 // compact chi x chi part as FP32, and (want_diff) return
-// message_diff(new, old) (abstractbeliefpropagationcache.jl:32-36),
-// accumulated in FP64.  Entries outside chi x chi are exact zeros.
-__device__ __forceinline__ double tc_finalize(const float* res, const float* old, float* out, int chi, int normalize,
+// message_diff(new, old) (abstractbeliefpropagationcache.jl:32-36) against
+// the previous message's entries o0, o1 (same positions, zero outside
+// chi x chi), accumulated in FP64.  Entries outside chi x chi are exact zeros.
+__device__ __forceinline__ double tc_finalize(const float* res, float o0, float o1, float* out, int chi, int normalize,
                                               bool want_diff, int lane) {
   const float x0 = res[lane], x1 = res[lane + 32];
   float ss = fmaf(x0, x0, x1 * x1);
@@ -140,12 +140,6 @@ __device__ __forceinline__ double tc_finalize(const float* res, const float* old
   const int b = lane & 7, a0 = lane >> 3, a1 = a0 + 4;
   const bool v0 = b < chi && a0 < chi, v1 = b < chi && a1 < chi;
   const int i0 = b + chi * a0, i1 = b + chi * a1;
-  float o0 = 0.f, o1 = 0.f;
-  if (want_diff) {
-    if (v0) o0 = old[i0];
-    if (v1) o1 = old[i1];
-  }
-  __syncwarp();
   if (v0) out[i0] = n0;
   if (v1) out[i1] = n1;
   double diff = 0.0;
@@ -179,29 +173,43 @@ __device__ __forceinline__ void pair_epilogue(uint32_t taddr, const float* Mx, c
     mx[i] = Mx[i + 8 * ax];  // Mx[bx = i, ax]
     my[i] = My[i + 8 * ay];  // My[by = i, ay]
   }
+  uint32_t g[2][32];
+  tmem_ld_x32(taddr, g[0]);
+  tmem_ld_x32(taddr + 32, g[1]);
+  tmem_wait_ld();
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    float g[32];
-    tmem_ld_x32(taddr + 32 * h, g);
+  for (int h = 0; h < 2; ++h)
 #pragma unroll
     for (int jj = 0; jj < 32; ++jj) {
       const int bx = jj & 7, by = 4 * h + (jj >> 3);
-      q[by] = fmaf(g[jj], mx[bx], q[by]);
-      p[bx] = fmaf(g[jj], my[by], p[bx]);
+      const float gv = __uint_as_float(g[h][jj]);
+      q[by] = fmaf(gv, mx[bx], q[by]);
+      p[bx] = fmaf(gv, my[by], p[bx]);
     }
+  // reduce-scatter of q over the 8 lanes of ax: lane ax ends with the sum of q[ax]
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const bool up = ax & 4;
+    const float send = up ? q[i] : q[i + 4];
+    const float keep = up ? q[i + 4] : q[i];
+    q[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
   }
 #pragma unroll
-  for (int o = 1; o < 8; o <<= 1)
-#pragma unroll
-    for (int i = 0; i < 8; ++i) q[i] += __shfl_xor_sync(0xffffffffu, q[i], o);
+  for (int i = 0; i < 2; ++i) {
+    const bool up = ax & 2;
+    const float send = up ? q[i] : q[i + 2];
+    const float keep = up ? q[i + 2] : q[i];
+    q[i] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+  }
+  {
+    const bool up = ax & 1;
+    const float send = up ? q[0] : q[1];
+    const float keep = up ? q[1] : q[0];
+    q[0] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+  }
 #pragma unroll
   for (int i = 0; i < 8; ++i) p[i] += __shfl_xor_sync(0xffffffffu, p[i], 8);
-  if (lane < 16) {
-    float sel = q[0];
-#pragma unroll
-    for (int i = 1; i < 8; ++i) sel = (ax == i) ? q[i] : sel;
-    res_y[ax + 8 * ay] = sel;  // by = ax here: lane's bra index on leg y
-  }
+  if (lane < 16) res_y[ax + 8 * ay] = q[0];  // by = ax here: lane's bra index on leg y
   if (lane < 8) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) part[warp * 64 + ax * 8 + i] = p[i];
@@ -210,13 +218,13 @@ __device__ __forceinline__ void pair_epilogue(uint32_t taddr, const float* Mx, c
 
 }  // namespace
 
-// One CTA walks work[blockIdx.x], work[blockIdx.x + gridDim.x], ...; vertex v
-// uses image slot vslot[v] (Z at zimg + slot * 8192, offsets in recs[slot]).
+// One CTA walks recs[blockIdx.x], recs[blockIdx.x + gridDim.x], ... (one
+// record per vertex of the work list, in list order; Z at zimg + slot * 8192).
 // err (device) receives GBTN_ERR_TIMEOUT when a bounded wait gives up; the CTA
 // then drains its own copy and MMAs in flight, frees its TMEM and returns.
 __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
-    tc_vertex_kernel(const int* __restrict__ work, int nwork, const int* __restrict__ vslot,
-                     const TcRec* __restrict__ recs, const __nv_bfloat16* __restrict__ zimg, const float* msg_in,
+    tc_vertex_kernel(const TcRec* __restrict__ recs, int nwork, const __nv_bfloat16* __restrict__ zimg,
+                     const float* msg_in,
                      float* msg_out, double* diffs, const int* converged, int normalize, int want_diff, int* err) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -279,28 +287,36 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
   float cm0 = 0.f, cm1 = 0.f;  // current vertex's incoming-message entries q0, q1
   int cnet = 0;
   if (w < nwork) {
-    const int sl = vslot[work[w]];
-    if (t == 0) issue_z(sl);
-    cnet = recs[sl].net;
-    const int c4 = recs[sl].chi4;
-    cm0 = padded_msg(msg_in, recs[sl].in_off[q0 >> 6], rec_chi(c4, q0 >> 6), e);
-    cm1 = padded_msg(msg_in, recs[sl].in_off[q1 >> 6], rec_chi(c4, q1 >> 6), e);
+    const TcRec* r = recs + w;
+    if (t == 0) issue_z(r->slot);
+    cnet = r->net;
+    const int c4 = r->chi4;
+    cm0 = padded_msg(msg_in, r->in_off[q0 >> 6], rec_chi(c4, q0 >> 6), e);
+    cm1 = padded_msg(msg_in, r->in_off[q1 >> 6], rec_chi(c4, q1 >> 6), e);
   }
   for (; w < nwork; w += gridDim.x) {
-    const int sl = vslot[work[w]];
-    const int out_off_w = recs[sl].out_off[warp];
-    const int out_de_w = recs[sl].out_de[warp];
-    const int cchi4 = recs[sl].chi4;
+    const TcRec* cr = recs + w;
+    const int out_off_w = cr->out_off[warp];
+    const int out_de_w = cr->out_de[warp];
+    const int cchi4 = cr->chi4;
     const int chi_w = rec_chi(cchi4, warp);
+    // the previous outgoing message of this warp's leg (message_diff), loaded now, used last
+    float old0 = 0.f, old1 = 0.f;
+    if (want_diff) {
+      const int b = lane & 7, a0 = lane >> 3;
+      if (b < chi_w && a0 < chi_w) old0 = msg_in[out_off_w + b + chi_w * a0];
+      if (b < chi_w && a0 + 4 < chi_w) old1 = msg_in[out_off_w + b + chi_w * (a0 + 4)];
+    }
     // next vertex: record now, messages later in this iteration
     const int wn = w + gridDim.x;
     int nsl = -1, nin0 = 0, nin1 = 0, nnet = 0, nchi0 = 8, nchi1 = 8;
     if (wn < nwork) {
-      nsl = vslot[work[wn]];
-      nin0 = recs[nsl].in_off[q0 >> 6];
-      nin1 = recs[nsl].in_off[q1 >> 6];
-      nnet = recs[nsl].net;
-      const int n4 = recs[nsl].chi4;
+      const TcRec* nr = recs + wn;
+      nsl = nr->slot;
+      nin0 = nr->in_off[q0 >> 6];
+      nin1 = nr->in_off[q1 >> 6];
+      nnet = nr->net;
+      const int n4 = nr->chi4;
       nchi0 = rec_chi(n4, q0 >> 6);
       nchi1 = rec_chi(n4, q1 >> 6);
     }
@@ -309,8 +325,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     if (converged && converged[cnet]) {  // network done: carry its messages forward
       const int p0 = q0 >> 6, p1 = q1 >> 6;
       const int c0 = rec_chi(cchi4, p0), c1 = rec_chi(cchi4, p1);
-      if (e < c0 * c0) msg_out[recs[sl].out_off[p0] + e] = msg_in[recs[sl].out_off[p0] + e];
-      if (e < c1 * c1) msg_out[recs[sl].out_off[p1] + e] = msg_in[recs[sl].out_off[p1] + e];
+      if (e < c0 * c0) msg_out[cr->out_off[p0] + e] = msg_in[cr->out_off[p0] + e];
+      if (e < c1 * c1) msg_out[cr->out_off[p1] + e] = msg_in[cr->out_off[p1] + e];
       if (t == 0) {
         const bool ok = wait_z();
         *abort_flag = ok ? 0 : 1;
@@ -377,15 +393,17 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     {
       // row t = (s, c) of D1 / D1' -> row c of tile s of T12 / T34 (K = (s, c') = 128)
       const int s = t >> 6, c = t & 63;
-      float d[32];
-      tmem_ld_x32(trow + 0, d);
-      store_half_row(KT + 8192 * s, c, 0, d);  // T12 overwrites the Kronecker products (their MMAs are done)
-      tmem_ld_x32(trow + 32, d);
-      store_half_row(KT + 8192 * s, c, 4, d);
-      tmem_ld_x32(trow + 64, d);
-      store_half_row(T34 + 8192 * s, c, 0, d);
-      tmem_ld_x32(trow + 96, d);
-      store_half_row(T34 + 8192 * s, c, 4, d);
+      uint32_t d[2][32];
+      tmem_ld_x32(trow + 0, d[0]);
+      tmem_ld_x32(trow + 32, d[1]);
+      tmem_wait_ld();
+      store_half_row(KT + 8192 * s, c, 0, d[0]);  // T12 overwrites the Kronecker products (their MMAs are done)
+      store_half_row(KT + 8192 * s, c, 4, d[1]);
+      tmem_ld_x32(trow + 64, d[0]);
+      tmem_ld_x32(trow + 96, d[1]);
+      tmem_wait_ld();
+      store_half_row(T34 + 8192 * s, c, 0, d[0]);
+      store_half_row(T34 + 8192 * s, c, 4, d[1]);
     }
     tc::fence_proxy_async_smem();
     tc::tc_fence_before();
@@ -433,7 +451,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     }
     __syncthreads();
     if (chi_w > 0) {  // warp-uniform: a padding leg has no outgoing message
-      const double df = tc_finalize(RES + 64 * warp, msg_in + out_off_w, msg_out + out_off_w, chi_w, normalize,
+      const double df = tc_finalize(RES + 64 * warp, old0, old1, msg_out + out_off_w, chi_w, normalize,
                                     want_diff != 0, lane);
       if (want_diff && lane == 0) diffs[out_de_w] = df;
     }
@@ -518,6 +536,7 @@ TcRec tc_record(const VDesc& d, const std::vector<long long>& msg_off) {
     }
   }
   r.net = d.net;
+  r.slot = -1;
   return r;
 }
 
@@ -528,7 +547,7 @@ void launch_build_zimg(const int* slot_vertex, int nslot, const VDesc* vd, const
   GBTN_CUDA(cudaGetLastError());
 }
 
-void launch_tc_vertices(const int* work, int nwork, const int* vslot, const TcRec* recs, const __nv_bfloat16* zimg,
+void launch_tc_vertices(const TcRec* recs, int nwork, const __nv_bfloat16* zimg,
                         const float* msg_in, float* msg_out, double* diffs, const int* converged, int normalize,
                         int want_diff, int* err, cudaStream_t s) {
   if (nwork == 0) return;
@@ -541,7 +560,7 @@ void launch_tc_vertices(const int* work, int nwork, const int* vslot, const TcRe
   GBTN_CUDA(cudaFuncSetAttribute(tc_vertex_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
   const int slots = kTcBlocksPerSm * nsm;
   const int grid = nwork < slots ? nwork : slots;
-  tc_vertex_kernel<<<grid, kTcThreads, kSmemBytes, s>>>(work, nwork, vslot, recs, zimg, msg_in, msg_out, diffs,
+  tc_vertex_kernel<<<grid, kTcThreads, kSmemBytes, s>>>(recs, nwork, zimg, msg_in, msg_out, diffs,
                                                          converged, normalize, want_diff, err);
   GBTN_CUDA(cudaGetLastError());
 }

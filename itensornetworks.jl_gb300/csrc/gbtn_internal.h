@@ -127,24 +127,26 @@ void launch_logscalar(int n_networks, const int* net_v_ptr, const int* net_v, co
 // BF16 tensor-core path (bp_tc.cu): the kernel works on degree-4 vertices with
 // d = 2 and chi = 8; a vertex with d = 2, at most four legs and chi <= 8 is
 // zero-padded to that shape (missing legs carry the fixed 1 x 1 message 1).
-// Per-slot record: element offsets of the incoming / outgoing messages on the
-// four legs (compact chi x chi storage), the outgoing directed-edge ids (-1 on
-// a padding leg), the network id and the four bond dimensions (one byte each,
-// 0 on a padding leg).
+// Per-vertex record (the kernel reads one per work item, in list order):
+// element offsets of the incoming / outgoing messages on the four legs
+// (compact chi x chi storage), the outgoing directed-edge ids (-1 on a padding
+// leg), the network id, the four bond dimensions (one byte each, 0 on a
+// padding leg) and the vertex's image slot.
 struct __align__(16) TcRec {
   int in_off[4];
   int out_off[4];
   int out_de[4];
   int net;
   int chi4;
-  int pad[2];
+  int slot;  // image slot
+  int pad;
 };
 bool tc_native(const VDesc& d);    // degree 4, d = 2, chi = 8 on every leg
 bool tc_paddable(const VDesc& d);  // d = 2, 1 <= degree <= 4, chi <= 8
 TcRec tc_record(const VDesc& d, const std::vector<long long>& msg_off);
 void launch_build_zimg(const int* slot_vertex, int nslot, const VDesc* vd, const double* fac, __nv_bfloat16* zimg,
                        cudaStream_t s);
-void launch_tc_vertices(const int* work, int nwork, const int* vslot, const TcRec* recs, const __nv_bfloat16* zimg,
+void launch_tc_vertices(const TcRec* recs, int nwork, const __nv_bfloat16* zimg,
                         const float* msg_in, float* msg_out, double* diffs, const int* converged, int normalize,
                         int want_diff, int* err, cudaStream_t s);
 
