@@ -94,6 +94,22 @@ __device__ __forceinline__ void tmem_ld_x32(uint32_t taddr, uint32_t (&r)[32]) {
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// 16 lanes x 32 bits in two halves: threads 0-15 read lanes 0-15 of the
+// warp's quadrant at columns [c, c + 32), threads 16-31 the same lanes at
+// columns [c + 32, c + 64) -- the rows of an M = 64 result, all 32 threads busy.
+__device__ __forceinline__ void tmem_ld_16x32bx2_x32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.16x32bx2.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32], 32;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   __nv_bfloat162 p = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<uint32_t*>(&p);
@@ -158,61 +174,80 @@ namespace {
 
 // Outgoing messages of one leg pair (x, y) from its environment
 // G[(ax,ay),(bx,by)] (ket row ax + 8 ay, bra column bx + 8 by; M = 64 layout:
-// warp w holds rows 16 w .. 16 w + 15 in lanes 0-15 of its TMEM quadrant):
+// warp w holds rows 16 w .. 16 w + 15 in lanes 0-15 of its TMEM quadrant).
+// Lane l works on row r = l % 16 (ax = r % 8, ay = 2 w + r / 8) and the column
+// half h = l / 16 (by = 4 h .. 4 h + 3):
 //   out_y[by, ay] = sum_{ax,bx} G Mx[bx, ax]  -> res_y (complete within the warp)
 //   out_x[bx, ax] = sum_{ay,by} G My[by, ay]  -> per-warp partials part[warp][ax][bx]
 __device__ __forceinline__ void pair_epilogue(uint32_t taddr, const float* Mx, const float* My, float* res_y,
                                               float* part, int warp, int lane) {
-  const int ax = lane & 7, ay = 2 * warp + ((lane >> 3) & 1);
-  float q[8], p[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) q[i] = p[i] = 0.f;
-  float mx[8], my[8];
+  const int r = lane & 15, h = lane >> 4;
+  const int ax = r & 7, ay = 2 * warp + (r >> 3);
+  float mx[8], my[4], q[4], p[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     mx[i] = Mx[i + 8 * ax];  // Mx[bx = i, ax]
-    my[i] = My[i + 8 * ay];  // My[by = i, ay]
+    p[i] = 0.f;
   }
-  uint32_t g[2][32];
-  tmem_ld_x32(taddr, g[0]);
-  tmem_ld_x32(taddr + 32, g[1]);
-  tmem_wait_ld();
-#pragma unroll
-  for (int h = 0; h < 2; ++h)
-#pragma unroll
-    for (int jj = 0; jj < 32; ++jj) {
-      const int bx = jj & 7, by = 4 * h + (jj >> 3);
-      const float gv = __uint_as_float(g[h][jj]);
-      q[by] = fmaf(gv, mx[bx], q[by]);
-      p[bx] = fmaf(gv, my[by], p[bx]);
-    }
-  // reduce-scatter of q over the 8 lanes of ax: lane ax ends with the sum of q[ax]
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    const bool up = ax & 4;
-    const float send = up ? q[i] : q[i + 4];
-    const float keep = up ? q[i + 4] : q[i];
-    q[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    my[i] = My[4 * h + i + 8 * ay];  // My[by = 4 h + i, ay]
+    q[i] = 0.f;
   }
+  uint32_t g[32];
+  tmem_ld_16x32bx2_x32(taddr, g);
+  tmem_wait_ld();
 #pragma unroll
-  for (int i = 0; i < 2; ++i) {
-    const bool up = ax & 2;
-    const float send = up ? q[i] : q[i + 2];
-    const float keep = up ? q[i + 2] : q[i];
-    q[i] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+  for (int jj = 0; jj < 32; ++jj) {
+    const int bx = jj & 7, i = jj >> 3;  // column 32 h + jj: by = 4 h + i
+    const float gv = __uint_as_float(g[jj]);
+    q[i] = fmaf(gv, mx[bx], q[i]);
+    p[bx] = fmaf(gv, my[i], p[bx]);
+  }
+  // q: sum over ax (lane bits 0-2), scattered: lanes ax, ax ^ 1 end with by = 4 h + 2 ax2 + ax1
+  {
+    const bool up = ax & 4;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const float send = up ? q[i] : q[i + 2];
+      const float keep = up ? q[i + 2] : q[i];
+      q[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
   }
   {
-    const bool up = ax & 1;
+    const bool up = ax & 2;
     const float send = up ? q[0] : q[1];
     const float keep = up ? q[1] : q[0];
-    q[0] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+    q[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
   }
+  q[0] += __shfl_xor_sync(0xffffffffu, q[0], 1);
+  if ((ax & 1) == 0) {
+    const int by = 4 * h + 2 * ((ax >> 2) & 1) + ((ax >> 1) & 1);
+    res_y[by + 8 * ay] = q[0];
+  }
+  // p: sum over the column half (lane bit 4) and the warp's two ay (lane bit 3), scattered
+  {
+    const bool up = lane & 16;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) p[i] += __shfl_xor_sync(0xffffffffu, p[i], 8);
-  if (lane < 16) res_y[ax + 8 * ay] = q[0];  // by = ax here: lane's bra index on leg y
-  if (lane < 8) {
+    for (int i = 0; i < 4; ++i) {
+      const float send = up ? p[i] : p[i + 4];
+      const float keep = up ? p[i + 4] : p[i];
+      p[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+  }
+  {
+    const bool up = lane & 8;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) part[warp * 64 + ax * 8 + i] = p[i];
+    for (int i = 0; i < 2; ++i) {
+      const float send = up ? p[i] : p[i + 2];
+      const float keep = up ? p[i + 2] : p[i];
+      p[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+  }
+  {
+    const int bx0 = 4 * ((lane >> 4) & 1) + 2 * ((lane >> 3) & 1);
+    part[warp * 64 + ax * 8 + bx0] = p[0];
+    part[warp * 64 + ax * 8 + bx0 + 1] = p[1];
   }
 }
 
