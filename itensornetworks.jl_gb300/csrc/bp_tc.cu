@@ -183,26 +183,31 @@ __device__ __forceinline__ void pair_epilogue(uint32_t taddr, const float* Mx, c
                                               float* part, int warp, int lane) {
   const int r = lane & 15, h = lane >> 4;
   const int ax = r & 7, ay = 2 * warp + (r >> 3);
-  float mx[8], my[4], q[4], p[8];
+  float2 mx2[4], p2[4], q2[4];  // pairs (bx, bx + 1); q2 holds the even / odd bx halves of q
+  float my[4], q[4], p[8];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    mx[i] = Mx[i + 8 * ax];  // Mx[bx = i, ax]
-    p[i] = 0.f;
+  for (int k = 0; k < 4; ++k) {
+    mx2[k] = *reinterpret_cast<const float2*>(Mx + 2 * k + 8 * ax);  // Mx[bx = 2k, 2k + 1; ax]
+    p2[k] = make_float2(0.f, 0.f);
+    q2[k] = make_float2(0.f, 0.f);
   }
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    my[i] = My[4 * h + i + 8 * ay];  // My[by = 4 h + i, ay]
-    q[i] = 0.f;
-  }
+  for (int i = 0; i < 4; ++i) my[i] = My[4 * h + i + 8 * ay];  // My[by = 4 h + i, ay]
   uint32_t g[32];
   tmem_ld_16x32bx2_x32(taddr, g);
   tmem_wait_ld();
 #pragma unroll
-  for (int jj = 0; jj < 32; ++jj) {
-    const int bx = jj & 7, i = jj >> 3;  // column 32 h + jj: by = 4 h + i
-    const float gv = __uint_as_float(g[jj]);
-    q[i] = fmaf(gv, mx[bx], q[i]);
-    p[bx] = fmaf(gv, my[i], p[bx]);
+  for (int jj = 0; jj < 32; jj += 2) {
+    const int k = (jj & 7) >> 1, i = jj >> 3;  // columns 32 h + jj, + 1: bx = 2k, 2k + 1; by = 4 h + i
+    const float2 gv = make_float2(__uint_as_float(g[jj]), __uint_as_float(g[jj + 1]));
+    q2[i] = __ffma2_rn(gv, mx2[k], q2[i]);
+    p2[k] = __ffma2_rn(gv, make_float2(my[i], my[i]), p2[k]);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    q[i] = q2[i].x + q2[i].y;
+    p[2 * i] = p2[i].x;
+    p[2 * i + 1] = p2[i].y;
   }
   // q: sum over ax (lane bits 0-2), scattered: lanes ax, ax ^ 1 end with by = 4 h + 2 ax2 + ax1
   {
@@ -386,19 +391,21 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
       const int n = t & 63, ba = n & 7, bb = n >> 3;
       const float* Ma = MSG + (t < 64 ? 0 : 128);
       const float* Mb = Ma + 64;
-      float ma[8];
+      float2 ma[4];
 #pragma unroll
-      for (int aa = 0; aa < 8; ++aa) ma[aa] = Ma[ba + 8 * aa];
+      for (int k = 0; k < 4; ++k) ma[k] = make_float2(Ma[ba + 16 * k], Ma[ba + 16 * k + 8]);
       uint4* row = reinterpret_cast<uint4*>(KT + (t < 64 ? 0 : 8192) + n * 128);
 #pragma unroll
       for (int ab = 0; ab < 8; ++ab) {
         const float mb = Mb[bb + 8 * ab];
-        uint4 qv;
-        qv.x = pack_bf16(ma[0] * mb, ma[1] * mb);
-        qv.y = pack_bf16(ma[2] * mb, ma[3] * mb);
-        qv.z = pack_bf16(ma[4] * mb, ma[5] * mb);
-        qv.w = pack_bf16(ma[6] * mb, ma[7] * mb);
-        row[ab ^ (n & 7)] = qv;
+        const float2 mb2 = make_float2(mb, mb);
+        uint32_t w[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float2 pr = __fmul2_rn(ma[k], mb2);
+          w[k] = pack_bf16(pr.x, pr.y);
+        }
+        row[ab ^ (n & 7)] = make_uint4(w[0], w[1], w[2], w[3]);
       }
       tc::fence_proxy_async_smem();
     }
