@@ -145,6 +145,12 @@ int gbtn_plan_sizes(const gbtn_plan* plan, int64_t* n_factor, int64_t* n_message
 enum gbtn_tc_policy { GBTN_TC_AUTO = 0, GBTN_TC_ALL = 1, GBTN_TC_NATIVE = 2, GBTN_TC_OFF = 3 };
 int gbtn_plan_set_tc_policy(gbtn_plan* plan, int32_t policy);
 int gbtn_plan_tc_split(gbtn_plan* plan, int32_t* is_tc, double* tuned_ms);
+/* CUDA graphs for the parallel / coloured sweeps (no counterpart in the
+ * reference): with on = 1, a run of three or more sweeps launches its first
+ * sweep directly and replays the rest from a CUDA graph of two sweeps, kept
+ * in the plan per launch configuration.  Off by default; event profiling
+ * (gbtn_ctx_set_profiling) bypasses the graphs. */
+int gbtn_plan_set_graphs(gbtn_plan* plan, int32_t on);
 
 /* Replaces: bpc[v] = tensor (update_factors, abstractbeliefpropagationcache.jl:158-171).
  * bra may be NULL unless the plan has separate_bra. */

@@ -117,6 +117,19 @@ struct gbtn_plan {
   DevBuf<int> d_tc_slot_vertex, d_err;
   DevBuf<__nv_bfloat16> d_zimg;
   bool zimg_valid = false;
+  // CUDA graphs of two sweeps (gbtn_plan_set_graphs), keyed by the launch
+  // parameters; list_version changes whenever the work lists are rebuilt
+  int graphs = 0;
+  int list_version = 0;
+  std::map<std::tuple<int, int, int, int, int, int, int, double>, std::pair<cudaGraph_t, cudaGraphExec_t>> graph_cache;
+  void clear_graphs() {
+    for (auto& kv : graph_cache) {
+      if (kv.second.second) cudaGraphExecDestroy(kv.second.second);
+      if (kv.second.first) cudaGraphDestroy(kv.second.first);
+    }
+    graph_cache.clear();
+  }
+  ~gbtn_plan() { clear_graphs(); }
   // sequential schedule storage
   DevBuf<int2> d_seq;
   DevBuf<int> d_seq_ptr;
@@ -246,6 +259,47 @@ size_t smem_need(int n, int k, bool sep_bra, size_t elt, int team) {
   return (b + 15) / 16 * 16;
 }
 
+using GraphKey = std::tuple<int, int, int, int, int, int, int, double>;
+
+// maxiter sweeps of `sweep`.  With graphs on (and no per-launch profiling),
+// the first sweep runs as plain launches and the rest are replays of one CUDA
+// graph holding two sweeps -- after two sweeps the double-buffer parity is
+// back where it started, so the same graph serves every pair.  The graph is
+// kept in the plan under `key` (launch parameters, buffer parity, list
+// version) and reused by later calls.
+template <class F>
+void sweep_loop(gbtn_plan* P, int maxiter, const GraphKey& key, F&& sweep) {
+  cudaStream_t s = P->ctx->stream;
+  int it = 0;
+  if (P->graphs && !P->ctx->profiling && maxiter >= 3) {
+    sweep();
+    ++it;
+    auto found = P->graph_cache.find(key);
+    if (found == P->graph_cache.end()) {
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      GBTN_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      try {
+        sweep();
+        sweep();
+      } catch (...) {
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      GBTN_CUDA(cudaStreamEndCapture(s, &g));
+      const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+      if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        GBTN_CUDA(e);
+      }
+      found = P->graph_cache.emplace(key, std::make_pair(g, ge)).first;
+    }
+    for (; it + 2 <= maxiter; it += 2) GBTN_CUDA(cudaGraphLaunch(found->second.second, s));
+  }
+  for (; it < maxiter; ++it) sweep();
+}
+
 // Sweeps of the parallel or coloured schedule in precision T.
 template <typename T>
 void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normalize, DevBuf<T>* msg, const T* fac,
@@ -255,7 +309,8 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
   GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int) * P->nnet, s));
   GBTN_CUDA(cudaMemsetAsync(P->d_iters.p, 0, sizeof(int) * P->nnet, s));
   const int* conv = want_diff ? P->d_conv.p : nullptr;
-  for (int it = 0; it < maxiter; ++it) {
+  const GraphKey key{sizeof(T) == 4 ? 1 : 0, schedule, normalize, want_diff ? 1 : 0, stall, cur, P->list_version, tol};
+  sweep_loop(P, maxiter, key, [&] {
     if (schedule == GBTN_SCHED_PARALLEL) {
       const T* in = msg[cur].p;
       T* out = msg[cur ^ 1].p;
@@ -282,7 +337,7 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
     if (want_diff)
       launch_reduce_diffs(P->nnet, P->d_net_de_ptr.p, P->d_net_de.p, P->d_diffs.p, tol, P->d_conv.p, P->d_iters.p,
                           P->d_mean.p, s, stall, P->d_best.p, P->d_since.p);
-  }
+  });
 }
 
 // Raise the device-side error word (set by a bounded wait that gave up).
@@ -350,6 +405,8 @@ TcList make_tc_list(gbtn_plan* P, const std::vector<int>& verts, std::vector<std
 // Work lists (all vertices, then every colour class) for the split `use`.
 void build_tc_lists(gbtn_plan* P, const std::vector<char>& use) {
   GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));  // no launch still reads the old lists
+  P->clear_graphs();
+  ++P->list_version;
   P->tc_use = use;
   P->tc_lists.clear();
   P->rest_lists.clear();
@@ -478,7 +535,8 @@ void run_sweeps_bf16(gbtn_plan* P, int schedule, int maxiter, double tol, int no
                                 P->d_diffs.p, conv, normalize, want_diff, s);
     }
   };
-  for (int it = 0; it < maxiter; ++it) {
+  const GraphKey key{2, schedule, normalize, want_diff ? 1 : 0, stall, c32, P->list_version, tol};
+  sweep_loop(P, maxiter, key, [&] {
     if (schedule == GBTN_SCHED_PARALLEL) {
       one(0, P->d_msg32[c32].p, P->d_msg32[c32 ^ 1].p);
       c32 ^= 1;
@@ -488,7 +546,7 @@ void run_sweeps_bf16(gbtn_plan* P, int schedule, int maxiter, double tol, int no
     if (want_diff)
       launch_reduce_diffs(P->nnet, P->d_net_de_ptr.p, P->d_net_de.p, P->d_diffs.p, tol, P->d_conv.p, P->d_iters.p,
                           P->d_mean.p, s, stall, P->d_best.p, P->d_since.p);
-  }
+  });
 }
 
 void finish_iters(gbtn_plan* P, bool want_diff, int maxiter, int32_t* iters, double* mean_diff) {
@@ -1037,6 +1095,16 @@ int gbtn_plan_set_tc_policy(gbtn_plan* P, int32_t policy) {
   P->tc_policy = policy;
   P->tc_tuned = false;
   P->tc_tune_best_ms = 0.0;
+  API_CATCH(C)
+}
+
+int gbtn_plan_set_graphs(gbtn_plan* P, int32_t on) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P, "NULL argument");
+  GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));
+  if (!on) P->clear_graphs();
+  P->graphs = on ? 1 : 0;
   API_CATCH(C)
 }
 

@@ -131,6 +131,11 @@ class BeliefPropagationCache:
         self._c(self.lib.gbtn_plan_set_tc_policy(self.handle, _lib.TC_POLICIES[policy]))
         return self
 
+    def set_graphs(self, on=True):
+        """Replay the sweeps of parallel / coloured runs from CUDA graphs."""
+        self._c(self.lib.gbtn_plan_set_graphs(self.handle, 1 if on else 0))
+        return self
+
     def tc_split(self):
         """(is_tc per vertex as a bool array, measured ms of the chosen split)."""
         out = np.zeros(max(self.tn.nv, 1), dtype=np.int32)
