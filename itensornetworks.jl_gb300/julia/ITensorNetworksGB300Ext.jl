@@ -14,16 +14,23 @@
 # site index per vertex, one link per edge and chi <= 8 are supported; other
 # caches fall back to nothing -- they raise, as the library has no CPU path.
 #
+# It also adds `apply(Algorithm("gb300"), gates, psi; maxdim, cutoff, normalize,
+# envs)`, the simple update of src/apply.jl:33-160 on the GPU (FP64 truncated
+# SVD), and a ChainRulesCore rrule for `bp_energy(psi, ops, coefs)`, the BP
+# two-site energy, whose pullback is the library's hand-written adjoint
+# (implicit differentiation at the BP fixed point).
+#
 # Not executed in the environment this file was written in (no Julia
 # toolchain); it documents the binding a maintainer adds.
 module ITensorNetworksGB300Ext
 
 using ITensorNetworks: ITensorNetworks, AbstractBeliefPropagationCache, BeliefPropagationCache,
     messages, set_messages, partitioned_tensornetwork, quotientedges, tensornetwork
-using ITensors: ITensor, Index, inds, commonind, array, itensor, dag, prime
+using ITensors: ITensor, Index, inds, commonind, array, itensor, dag, prime, tags
 using NDTensors: Algorithm, @Algorithm_str
 using NamedGraphs.PartitionedGraphs: QuotientEdge, quotientvertices
 using GB300TensorNetworks: libgbtn
+using ChainRulesCore: ChainRulesCore, NoTangent
 
 const GBTN_OK = Int32(0)
 
@@ -142,6 +149,184 @@ function ITensorNetworks.update(alg::Algorithm"gb300_bp", bpc::BeliefPropagation
         end
     end
     return bpc
+end
+
+
+# ---- simple update (apply / tebd) -------------------------------------------
+
+struct GradOpts
+    mode::Int32
+    maxiter::Int32
+    tol::Float64
+    unroll::Int32
+    checkpoint::Int32
+end
+
+# Ket tensors of a plain ITensorNetwork in the ABI layout (vertex order of
+# `vertices(psi)`, edges with src < dst, legs in each tensor's index order).
+function pack_state(psi)
+    vs = collect(ITensorNetworks.vertices(psi))
+    vid = Dict(v => i - 1 for (i, v) in enumerate(vs))
+    es = collect(ITensorNetworks.edges(psi))
+    links = [commonind(psi[ITensorNetworks.src(e)], psi[ITensorNetworks.dst(e)]) for e in es]
+    eu = Int32[vid[ITensorNetworks.src(e)] for e in es]
+    ev = Int32[vid[ITensorNetworks.dst(e)] for e in es]
+    edim = Int32[length(l) for l in links]
+    sdim, leg_ptr, leg_edge, data, sites = Int32[], Int32[0], Int32[], Float64[], Index[]
+    for v in vs
+        t = psi[v]
+        s = only(filter(i -> !(i in links), inds(t)))
+        ls = filter(i -> i in links, collect(inds(t)))
+        append!(leg_edge, Int32[findfirst(==(l), links) - 1 for l in ls])
+        push!(leg_ptr, length(leg_edge))
+        push!(sdim, length(s))
+        push!(sites, s)
+        append!(data, vec(array(t, s, ls...)))
+    end
+    return (; vs, es, links, eu, ev, edim, sdim, leg_ptr, leg_edge, data, sites)
+end
+
+"""
+    apply(Algorithm("gb300"), gates, psi; maxdim, cutoff=nothing, normalize=true, envs=nothing, callback)
+
+Two-site `gates` (ITensors acting on the site indices of neighbouring vertices)
+applied in order by the GPU simple update; `callback(; singular_values,
+truncation_error)` is called per gate as in src/apply.jl:97-146.  `envs`:
+`nothing` (tebd) or a Dict from QuotientEdge to the converged message.
+"""
+function ITensorNetworks.apply(::Algorithm"gb300", gates::Vector{ITensor}, psi; maxdim, cutoff=nothing,
+                               normalize=true, envs=nothing, callback=(; kws...) -> nothing)
+    p = pack_state(psi)
+    ctx = context()
+    chimax = max(maxdim, maximum(p.edim))
+    eidx = Int32[]
+    gdata = Float64[]
+    for g in gates
+        vs = [v for v in p.vs if !isempty(intersect(inds(g), [p.sites[findfirst(==(v), p.vs)]]))]
+        su, sv = p.sites[findfirst(==(vs[1]), p.vs)], p.sites[findfirst(==(vs[2]), p.vs)]
+        e = findfirst(k -> Set((p.eu[k], p.ev[k])) == Set((findfirst(==(vs[1]), p.vs) - 1,
+                                                              findfirst(==(vs[2]), p.vs) - 1)), eachindex(p.eu))
+        u_first = p.eu[e] == findfirst(==(vs[1]), p.vs) - 1
+        a, b = u_first ? (su, sv) : (sv, su)
+        push!(eidx, e - 1)
+        append!(gdata, vec(array(g, prime(a), prime(b), a, b)))  # row s'_u + du s'_v, column s_u + du s_v
+    end
+    GC.@preserve p eidx gdata begin
+        desc = GraphDesc(length(p.vs), length(p.es), pointer(p.eu), pointer(p.ev), pointer(p.edim),
+            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0)
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ctx, ccall((:gbtn_su_create, libgbtn), Cint, (Ptr{Cvoid}, Ref{GraphDesc}, Int32, Ref{Ptr{Cvoid}}),
+            ctx, desc, chimax, h))
+        try
+            check(ctx, ccall((:gbtn_su_set_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Float64}), h[], p.data))
+            envbuf = C_NULL
+            if envs !== nothing
+                envbuf = zeros(2 * length(p.es) * chimax^2)
+                for (k, e) in enumerate(p.es), (dir, qe) in ((0, e), (1, reverse(e)))
+                    M = array(only(envs[qe]))
+                    c = size(M, 1)
+                    o = (2 * (k - 1) + dir) * chimax^2
+                    envbuf[(o + 1):(o + c * c)] = vec(M)
+                end
+            end
+            n = length(gates)
+            te = zeros(n)
+            sv = zeros(n * maxdim)
+            check(ctx, ccall((:gbtn_su_apply, libgbtn), Cint,
+                (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Float64}, Int32, Ptr{Float64}, Int32, Float64, Int32,
+                 Ptr{Float64}, Ptr{Float64}),
+                h[], n, eidx, gdata, 1, envbuf, maxdim, something(cutoff, -1.0), normalize ? 1 : 0, te, sv))
+            for j in 1:n
+                s = sv[((j - 1) * maxdim + 1):(j * maxdim)]
+                callback(; singular_values=s[s .> 0], truncation_error=te[j])
+            end
+            dims = zeros(Int32, length(p.es))
+            check(ctx, ccall((:gbtn_su_edge_dims, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Int32}), h[], dims))
+            newlinks = [d == length(l) ? l : Index(Int(d), tags(l)) for (d, l) in zip(dims, p.links)]
+            total = sum(Int(p.sdim[i]) * prod(Int(dims[p.leg_edge[q] + 1]) for q in (p.leg_ptr[i] + 1):p.leg_ptr[i + 1];
+                                                 init=1) for i in eachindex(p.vs))
+            flat = Vector{Float64}(undef, total)
+            check(ctx, ccall((:gbtn_su_get_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int64),
+                h[], flat, total))
+            psi = copy(psi)
+            off = 0
+            for (i, v) in enumerate(p.vs)
+                ls = [newlinks[p.leg_edge[q] + 1] for q in (p.leg_ptr[i] + 1):p.leg_ptr[i + 1]]
+                shp = (Int(p.sdim[i]), length.(ls)...)
+                len = prod(shp)
+                psi[v] = itensor(reshape(flat[(off + 1):(off + len)], shp), p.sites[i], ls...)
+                off += len
+            end
+            return psi
+        finally
+            ccall((:gbtn_su_destroy, libgbtn), Cint, (Ptr{Cvoid},), h[])
+        end
+    end
+end
+
+# ---- BP energy and its adjoint (ChainRulesCore) ------------------------------
+
+"""
+    bp_energy(psi, ops, coefs; maxiter=500)
+
+sum_e sum_t coefs[t] <ops[t] (x) ops[t]>_e with BP reduced density matrices of
+the converged (mixed-precision, FP64-refined) messages; ops are d x d matrices.
+"""
+function bp_energy(psi, ops::Vector{Matrix{Float64}}, coefs::Vector{Float64}; maxiter=500)
+    return first(energy_and_grad(psi, ops, coefs; maxiter, want_grad=false))
+end
+
+function energy_and_grad(psi, ops, coefs; maxiter=500, want_grad=true)
+    p = pack_state(psi)
+    ctx = context()
+    opbuf = reduce(vcat, vec.(ops))
+    GC.@preserve p opbuf begin
+        desc = GraphDesc(length(p.vs), length(p.es), pointer(p.eu), pointer(p.ev), pointer(p.edim),
+            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0)
+        plan = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ctx, ccall((:gbtn_plan_create, libgbtn), Cint, (Ptr{Cvoid}, Ref{GraphDesc}, Ref{Ptr{Cvoid}}),
+            ctx, desc, plan))
+        try
+            check(ctx, ccall((:gbtn_set_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Cint),
+                plan[], p.data, C_NULL, 0))
+            opts = BPOpts(1, 3, maxiter, 1, 1e-14, C_NULL, 0, 0.0, 0.0, 0, 0, 0)
+            check(ctx, ccall((:gbtn_bp_run, libgbtn), Cint, (Ptr{Cvoid}, Ref{BPOpts}, Ptr{Int32}, Ptr{Float64}),
+                plan[], opts, C_NULL, C_NULL))
+            E = Ref{Float64}(0.0)
+            if !want_grad
+                check(ctx, ccall((:gbtn_energy2, libgbtn), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Float64},
+                    Ref{Float64}), plan[], length(coefs), coefs, opbuf, E))
+                return (E[], nothing)
+            end
+            grad = similar(p.data)
+            gopts = GradOpts(0, 500, 1e-12, 0, 0)
+            check(ctx, ccall((:gbtn_energy2_grad, libgbtn), Cint,
+                (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Float64}, Ref{GradOpts}, Ref{Float64}, Ptr{Float64},
+                 Ptr{Int32}, Ptr{Float64}),
+                plan[], length(coefs), coefs, opbuf, gopts, E, grad, C_NULL, C_NULL))
+            # unpack dE/dA into one ITensor per vertex (same indices as psi[v])
+            dpsi = Dict{Any, ITensor}()
+            off = 0
+            for (i, v) in enumerate(p.vs)
+                ls = [p.links[p.leg_edge[q] + 1] for q in (p.leg_ptr[i] + 1):p.leg_ptr[i + 1]]
+                shp = (Int(p.sdim[i]), length.(ls)...)
+                len = prod(shp)
+                dpsi[v] = itensor(reshape(grad[(off + 1):(off + len)], shp), p.sites[i], ls...)
+                off += len
+            end
+            return (E[], dpsi)
+        finally
+            ccall((:gbtn_plan_destroy, libgbtn), Cint, (Ptr{Cvoid},), plan[])
+        end
+    end
+end
+
+function ChainRulesCore.rrule(::typeof(bp_energy), psi, ops, coefs; maxiter=500)
+    E, dpsi = energy_and_grad(psi, ops, coefs; maxiter)
+    function bp_energy_pullback(dE)
+        return (NoTangent(), Dict(v => dE * t for (v, t) in dpsi), NoTangent(), NoTangent())
+    end
+    return E, bp_energy_pullback
 end
 
 end
