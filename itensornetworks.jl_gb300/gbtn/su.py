@@ -146,14 +146,42 @@ def checkerboard_edges(Lx, Ly):
 
 
 def tebd(psi: TensorNetwork, gate_of_edge, edge_classes, nsteps, maxdim, cutoff, normalize=True, chi_max=None,
-         state=None):
+         state=None, bp_envs=False, bp_maxiter=30, bp_tol=1e-12, bp_precision="f64"):
     """nsteps Trotter steps: every class of vertex-disjoint edges in order
     (tebd.jl:2-31 with a checkerboard gate order).  Returns the final state and
-    the truncation errors of the last step."""
+    the truncation errors of the last step.
+
+    bp_envs=True is the BP-gauged variant (apply with envs, test/test_apply.jl:30-35,
+    with the cache refreshed inside the loop): before each class the
+    current state's BP messages are computed on the GPU (parallel schedule,
+    at most bp_maxiter sweeps, tol bp_tol) and its gates use them as
+    environments.  Gates of one class touch disjoint vertices, so none of them
+    changes a message another one reads; the refresh between classes picks up
+    the bond dimensions the previous class changed."""
     st = state or SimpleUpdateState(psi, chi_max or maxdim)
+    gates = {e: gate_of_edge(e) for cls in edge_classes for e in cls}
     order = [e for cls in edge_classes for e in cls]
-    gates = [gate_of_edge(e) for e in order]
     te = None
     for _ in range(nsteps):
-        te, _ = st.apply(gates, order, maxdim=maxdim, cutoff=cutoff, normalize=normalize)
+        if not bp_envs:
+            te, _ = st.apply([gates[e] for e in order], order, maxdim=maxdim, cutoff=cutoff, normalize=normalize)
+            continue
+        tes = []
+        for cls in edge_classes:
+            envs = bp_environments(st, maxiter=bp_maxiter, tol=bp_tol, precision=bp_precision)
+            t, _ = st.apply([gates[e] for e in cls], list(cls), envs=envs, maxdim=maxdim, cutoff=cutoff,
+                            normalize=normalize)
+            tes.append(t)
+        te = np.concatenate(tes)
     return st, te
+
+
+def bp_environments(st: SimpleUpdateState, maxiter=30, tol=1e-12, precision="f64"):
+    """Converged BP messages of the state held by ``st`` (one chi x chi matrix
+    per directed edge, current bond dimensions), computed on the GPU."""
+    from .cache import BeliefPropagationCache
+    bpc = BeliefPropagationCache(st.network(), ctx=st.ctx)
+    bpc.update(maxiter=maxiter, tol=tol, schedule="parallel", precision=precision)
+    msgs = bpc.messages()
+    bpc.close()
+    return msgs

@@ -131,3 +131,27 @@ def test_tfim_20x20_chi8_runs_and_lowers_energy():
     # the |+> product state has energy -g = -3 per site; imaginary time lowers it
     assert e_site < -3.0
     assert np.all(np.abs(x) <= 1 + 1e-12)
+
+
+def test_bp_gauged_tebd_matches_oracle():
+    # tebd with BP environments refreshed before every colour class, against the
+    # oracle's BP fixed point and simple update with envs (apply.jl:33-95)
+    Lx, Ly, g_field, dt, steps, maxdim = 3, 3, 3.0, 0.05, 2, 3
+    g = O.square_lattice(Lx, Ly, chi=2)
+    A = O.random_network(g, 17, unit_norm=True)
+    z = [len(l) for l in g.legs]
+    classes = gbtn.checkerboard_edges(Lx, Ly)
+    gate_of = lambda e: gbtn.tfim_gate(dt, g_field, z[g.edges[e][0]], z[g.edges[e][1]])
+    st, te_g = gbtn.tebd(gpu_net(g, A), gate_of, classes, nsteps=steps, maxdim=maxdim, cutoff=1e-12,
+                         chi_max=6, bp_envs=True, bp_maxiter=300, bp_tol=None)
+    gg, B = g, list(A)
+    for _ in range(steps):
+        tes = []
+        for cls in classes:
+            envs, _, _ = O.bp_update(gg, B, O.identity_messages(gg), maxiter=300, schedule="parallel")
+            for e in cls:
+                gg, B, S, t = oracle_gate(gg, B, gate_of(e), e, envs=envs, maxdim=maxdim, cutoff=1e-12)
+                tes.append(t)
+    np.testing.assert_allclose(te_g, tes, rtol=1e-6, atol=1e-12)
+    assert st.edge_dims() == gg.edge_dims
+    assert same_up_to_sign(state(gg, st.network().tensors), state(gg, B), 1e-8)
