@@ -6,7 +6,8 @@ from . import _lib
 from ._lib import Context, GBTNError, InvalidArgument, LibraryNotBuilt, Unsupported, default_context
 from .cache import (BeliefPropagationCache, environment, expect, initialize_cache, inner, loginner, logscalar,
                     message_diff, norm, norm_sqr, normalize, rescale, scalar, update, updated_message)
-from .su import SimpleUpdateState, apply, checkerboard_edges, tebd, tfim_gate
+from .partition import CoarseGraining, PartitionedBPCache, partitioned_cache
+from .su import SimpleUpdateState, apply, bp_environments, checkerboard_edges, tebd, tfim_gate
 from .network import (TensorNetwork, default_edge_sequence, disjoint_union, parallel_edge_sequence,
                       random_network, random_tensors, square_lattice)
 
@@ -15,5 +16,6 @@ __all__ = [
     "Unsupported", "default_context", "default_edge_sequence", "disjoint_union", "environment", "expect",
     "initialize_cache", "inner", "loginner", "logscalar", "message_diff", "norm", "norm_sqr", "normalize",
     "parallel_edge_sequence", "random_network", "random_tensors", "rescale", "scalar", "square_lattice", "update",
-    "updated_message", "SimpleUpdateState", "apply", "checkerboard_edges", "tebd", "tfim_gate",
+    "updated_message", "SimpleUpdateState", "apply", "checkerboard_edges", "tebd", "tfim_gate", "bp_environments",
+    "CoarseGraining", "PartitionedBPCache", "partitioned_cache",
 ]
