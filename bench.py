@@ -131,9 +131,42 @@ def cpu_reference_rate(seconds=10.0, nthreads=0):
     return sweeps * MSGS_PER_NET / el, cores, f"{sweeps} Jacobi sweeps of one 32x32 chi=8 PEPS ({el:.1f} s)"
 
 
+# ---- replica plumbing (one process per GPU, no data-path collective) ----------
+
+def replica_env():
+    """(rank, world size, local rank) from the torchrun environment."""
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def replica_seed(rank):
+    """Seed of a rank's batch: every replica works on its own networks."""
+    return 1000 * rank
+
+
+def reference_runs_on(rank):
+    """The CPU reference arm runs (and prints) on rank 0 only."""
+    return rank == 0
+
+
+def max_over_ranks(x, world, device):
+    """The slowest rank's time (the job's time): all-reduce MAX over ranks."""
+    if world > 1:
+        import torch
+        t = torch.tensor([x], device=device, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        x = float(t.item())
+    return x
+
+
+def aggregate_rate(world, units_per_rank_step, ms_per_step):
+    """Whole-job throughput: the units of every rank / the slowest rank's time."""
+    return world * units_per_rank_step / (ms_per_step * 1e-3)
+
+
 def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    rank, _, _ = replica_env()
+    if not reference_runs_on(rank):
         return
     rates = []
     for _ in range(args.warmup):
@@ -329,16 +362,14 @@ def run_ours(args):
     import gbtn
     from gbtn import _lib
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank, world, local = replica_env()
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     ctx = gbtn.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
-    tn = make_batch(seed0=1000 * rank)
+    tn = make_batch(seed0=replica_seed(rank))
     bpc = gbtn.BeliefPropagationCache(tn, ctx=ctx)
     lib = ctx.lib
     # tensor-core routing of the BF16 phase, chosen by the library's autotuner
@@ -366,12 +397,8 @@ def run_ours(args):
         if world > 1:
             torch.distributed.barrier()
 
-    def max_over_ranks(x):
-        if world > 1:
-            t = torch.tensor([x], device="cuda", dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            x = float(t.item())
-        return x
+    def max_ranks(x):
+        return max_over_ranks(x, world, "cuda")
 
     def timed(precision, steps, warmup):
         """ms per sweep: W untimed sweeps, then K sweeps between CUDA events."""
@@ -382,7 +409,7 @@ def run_ours(args):
         run(steps, precision)
         e1.record(stream)
         barrier()
-        return max_over_ranks(e0.elapsed_time(e1) / steps)
+        return max_ranks(e0.elapsed_time(e1) / steps)
 
     msgs_step = BATCH * MSGS_PER_NET
     # 1. chosen path: BF16 tensor-core sweeps (clocks sampled during the timed region)
@@ -439,7 +466,7 @@ def run_ours(args):
     for _ in range(args.steps):
         e2e_step()
     barrier()
-    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
+    e2e_ms = max_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
 
     # 5. gradient of the BP energy (Heisenberg, 12x12, d=2, chi=6, unit-norm tensors):
     #    mixed-precision BP to convergence + FP64 implicit adjoint, and the
@@ -450,7 +477,7 @@ def run_ours(args):
     # 7. batched BP with uneven shapes (64 networks, L 8..32, chi 2..8)
     batched = batched_uneven_timing(gbtn, ctx, stream, barrier)
 
-    value = world * msgs_step / (ms_bf16 * 1e-3)
+    value = aggregate_rate(world, msgs_step, ms_bf16)
     # algorithmic flops of one tensor-core launch: every routed vertex's k
     # messages of 2 d prod(chi) sum(chi) each, at its own (unpadded) shape
     tc_v = [v for v in range(tn.nv) if is_tc[v]]
@@ -503,7 +530,7 @@ def run_ours(args):
             "batched_uneven": batched,
             "cpu_baseline": {"value": cpu_val, "unit": "msg-updates/s", "cores": cores, "kind": "port",
                              "sample": sample},
-            "e2e": {"value": world * msgs_step / (e2e_ms * 1e-3), "unit": "msg-updates/s",
+            "e2e": {"value": aggregate_rate(world, msgs_step, e2e_ms), "unit": "msg-updates/s",
                     "h2d_bytes_per_step": n_fac * 8, "d2h_bytes_per_step": n_msg * 8},
             "gpu_launches": int(tc_n + simt_n + 2),
             "clocks": clk.summary(),
