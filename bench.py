@@ -468,6 +468,27 @@ def run_ours(args):
     barrier()
     e2e_ms = max_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
 
+    # 4b. message normalisation / gauge scaling (rescale_messages, an HBM-type
+    #     kernel: every message read and written once) on converged messages
+    bpc.init_messages("identity")
+    run(30, "f64")
+    ctx.set_profiling(True)
+    for _ in range(args.warmup):
+        bpc.rescale_messages()
+    ctx.kernel_time(_lib.KCLASS_GAUGE)  # forget the warm-up launches
+    for _ in range(args.steps):
+        bpc.rescale_messages()
+    g_ms, g_n = ctx.kernel_time(_lib.KCLASS_GAUGE)
+    ctx.set_profiling(False)
+    g_launch_ms = g_ms / max(g_n, 1)
+    g_bytes = 2 * n_msg * 8
+    hbm_peak = (json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs")
+                if (ROOT / "MEASURED_PEAKS.json").exists() else None) or 6800.0
+    gauge = {"kernel": "rescale_messages_kernel", "workload": "all messages of the batch (FP64)",
+             "launch_ms": g_launch_ms, "launches": g_n, "algorithmic_bytes": g_bytes,
+             "achieved_gbs": g_bytes / (g_launch_ms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
+             "frac": g_bytes / (g_launch_ms * 1e-3) / 1e9 / hbm_peak}
+
     # 5. gradient of the BP energy (Heisenberg, 12x12, d=2, chi=6, unit-norm tensors):
     #    mixed-precision BP to convergence + FP64 implicit adjoint, and the
     #    checkpointed 30-sweep unrolled variant; seconds per full dE/dA
@@ -528,6 +549,7 @@ def run_ours(args):
             "gradient": grad,
             "simple_update": su,
             "batched_uneven": batched,
+            "gauge_scaling": gauge,
             "cpu_baseline": {"value": cpu_val, "unit": "msg-updates/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": aggregate_rate(world, msgs_step, e2e_ms), "unit": "msg-updates/s",

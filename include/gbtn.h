@@ -118,7 +118,12 @@ int gbtn_abi_version(void);
  * message-kernel launch of the context is bracketed by CUDA events on the
  * context's stream.  gbtn_ctx_kernel_time returns, and forgets, the summed
  * device time and the launch count of one kernel class. */
-enum gbtn_kernel_class { GBTN_KCLASS_TENSOR_CORE = 0, GBTN_KCLASS_SIMT_F32 = 1, GBTN_KCLASS_SIMT_F64 = 2 };
+enum gbtn_kernel_class {
+  GBTN_KCLASS_TENSOR_CORE = 0,
+  GBTN_KCLASS_SIMT_F32 = 1,
+  GBTN_KCLASS_SIMT_F64 = 2,
+  GBTN_KCLASS_GAUGE = 3 /* rescale_messages: message normalisation and gauge scaling */
+};
 int gbtn_ctx_set_profiling(gbtn_ctx* ctx, int on);
 int gbtn_ctx_kernel_time(gbtn_ctx* ctx, int kernel_class, double* total_ms, int64_t* launches);
 

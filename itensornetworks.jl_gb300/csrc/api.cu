@@ -1321,7 +1321,10 @@ int gbtn_rescale_messages(gbtn_plan* P) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P, "NULL plan");
-  if (P->ne) launch_rescale_messages(P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, P->ctx->stream);
+  if (P->ne) {
+    KTimer kt(P->ctx, GBTN_KCLASS_GAUGE);
+    launch_rescale_messages(P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, P->ctx->stream);
+  }
   GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));
   API_CATCH(C)
 }

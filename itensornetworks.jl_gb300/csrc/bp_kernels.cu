@@ -324,13 +324,27 @@ __global__ void reduce_diffs_kernel(const int* __restrict__ net_de_ptr, const in
   }
 }
 
-__global__ void convert_kernel_f64_f32(const double* a, float* b, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
+// Precision conversions: two elements per thread and access (16-byte FP64
+// loads, 8-byte FP32 stores or the reverse), grid-stride, odd tail last.
+__global__ void convert_kernel_f64_f32(const double* __restrict__ a, float* __restrict__ b, long long n) {
+  const long long n2 = n >> 1;
+  const double2* a2 = reinterpret_cast<const double2*>(a);
+  float2* b2 = reinterpret_cast<float2*>(b);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2; i += (long long)gridDim.x * blockDim.x) {
+    const double2 x = a2[i];
+    b2[i] = make_float2((float)x.x, (float)x.y);
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) b[n - 1] = (float)a[n - 1];
 }
-__global__ void convert_kernel_f32_f64(const float* a, double* b, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    b[i] = (double)a[i];
+__global__ void convert_kernel_f32_f64(const float* __restrict__ a, double* __restrict__ b, long long n) {
+  const long long n2 = n >> 1;
+  const float2* a2 = reinterpret_cast<const float2*>(a);
+  double2* b2 = reinterpret_cast<double2*>(b);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2; i += (long long)gridDim.x * blockDim.x) {
+    const float2 x = a2[i];
+    b2[i] = make_double2((double)x.x, (double)x.y);
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) b[n - 1] = (double)a[n - 1];
 }
 __global__ void convert_kernel_f64_bf16(const double* a, __nv_bfloat16* b, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -359,26 +373,53 @@ __global__ void scale_vertices_kernel(int nv, const VDesc* vd, double* fac, doub
   }
 }
 
-// rescale_messages (beliefpropagationcache.jl:121-139), one warp per edge.
+// rescale_messages (beliefpropagationcache.jl:121-139): both messages of an
+// edge normalised, the sign of their inner product moved onto the first, and
+// both scaled by |<m1, m2>|^(-1/2) so the edge scalar is 1.  FP64 is scarce on
+// this part and a warp instruction costs its pipe the same for one edge or
+// eight, so four lanes take an edge (eight edges per warp): each lane keeps
+// its up-to-16 entries of both messages in registers, the three inner
+// products are reduced over the four lanes, and the factors -- three
+// reciprocal square roots -- are formed once per instruction for all eight
+// edges and applied by multiplication.  A warp reads 8 x 4 consecutive FP64
+// values per load (32-byte sectors).
 __global__ void rescale_messages_kernel(int ne, const int* dchi, const long long* msg_off, double* msgs) {
-  const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (e >= ne) return;
-  const int c2 = dchi[2 * e] * dchi[2 * e];
-  double* m1 = msgs + msg_off[2 * e];
-  double* m2 = msgs + msg_off[2 * e + 1];
-  double a0 = lane < c2 ? m1[lane] : 0.0, a1 = lane + 32 < c2 ? m1[lane + 32] : 0.0;
-  double b0 = lane < c2 ? m2[lane] : 0.0, b1 = lane + 32 < c2 ? m2[lane + 32] : 0.0;
-  const double na = sqrt(warp_sum(a0 * a0 + a1 * a1));
-  const double nb = sqrt(warp_sum(b0 * b0 + b1 * b1));
-  a0 /= na; a1 /= na; b0 /= nb; b1 /= nb;
-  double n = warp_sum(a0 * b0 + a1 * b1);
-  const double s = n > 0.0 ? 1.0 : (n < 0.0 ? -1.0 : 0.0);
-  a0 *= s; a1 *= s;
-  n *= s;
-  const double sf = 1.0 / sqrt(n);
-  if (lane < c2) { m1[lane] = sf * a0; m2[lane] = sf * b0; }
-  if (lane + 32 < c2) { m1[lane + 32] = sf * a1; m2[lane + 32] = sf * b1; }
+  const int e = blockIdx.x * (blockDim.x >> 2) + (threadIdx.x >> 2);
+  const int l4 = threadIdx.x & 3;
+  const bool ok = e < ne;  // lanes past the last edge still take part in the shuffles
+  const int c2 = ok ? dchi[2 * e] * dchi[2 * e] : 0;
+  double* m1 = msgs + (ok ? msg_off[2 * e] : 0);
+  double* m2 = msgs + (ok ? msg_off[2 * e + 1] : 0);
+  double a[16], b[16];
+  double na2 = 0.0, nb2 = 0.0, ab = 0.0;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int i = l4 + 4 * j;
+    a[j] = i < c2 ? m1[i] : 0.0;
+    b[j] = i < c2 ? m2[i] : 0.0;
+    na2 = fma(a[j], a[j], na2);
+    nb2 = fma(b[j], b[j], nb2);
+    ab = fma(a[j], b[j], ab);
+  }
+#pragma unroll
+  for (int o = 1; o < 4; o <<= 1) {
+    na2 += __shfl_xor_sync(0xffffffffu, na2, o);
+    nb2 += __shfl_xor_sync(0xffffffffu, nb2, o);
+    ab += __shfl_xor_sync(0xffffffffu, ab, o);
+  }
+  const double ia = rsqrt(na2), ib = rsqrt(nb2);
+  const double n = ab * ia * ib;  // <m1/|m1|, m2/|m2|>
+  const double sg = n > 0.0 ? 1.0 : (n < 0.0 ? -1.0 : 0.0);
+  const double isf = rsqrt(fabs(n));
+  const double ka = sg * isf * ia, kb = isf * ib;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int i = l4 + 4 * j;
+    if (i < c2) {
+      m1[i] = ka * a[j];
+      m2[i] = kb * b[j];
+    }
+  }
 }
 
 __global__ void edge_scalars_kernel(int ne, const int* dchi, const long long* msg_off, const double* msgs, double* out) {
@@ -565,7 +606,7 @@ void launch_scale_vertices(int nv, const VDesc* vd, double* fac, double* bra, co
 }
 void launch_rescale_messages(int ne, const int* dchi, const long long* msg_off, double* msgs, cudaStream_t s) {
   if (ne == 0) return;
-  rescale_messages_kernel<<<(ne + 7) / 8, 256, 0, s>>>(ne, dchi, msg_off, msgs);
+  rescale_messages_kernel<<<(ne + 63) / 64, 256, 0, s>>>(ne, dchi, msg_off, msgs);  // 4 lanes per edge
   GBTN_CUDA(cudaGetLastError());
 }
 void launch_edge_scalars(int ne, const int* dchi, const long long* msg_off, const double* msgs, double* out,

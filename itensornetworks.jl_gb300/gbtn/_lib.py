@@ -23,7 +23,7 @@ ERRORS = {
     6: "GBTN_ERR_NOMEM",
 }
 HOST, DEVICE = 0, 1
-KCLASS_TENSOR_CORE, KCLASS_SIMT_F32, KCLASS_SIMT_F64 = 0, 1, 2
+KCLASS_TENSOR_CORE, KCLASS_SIMT_F32, KCLASS_SIMT_F64, KCLASS_GAUGE = 0, 1, 2, 3
 TC_POLICIES = {"auto": 0, "all": 1, "native": 2, "off": 3}
 SCHED = {"sequential": 0, "parallel": 1, "colored": 2}
 PRECISION = {"f64": 0, "f32": 1, "bf16": 2, "mixed": 3}
