@@ -82,6 +82,15 @@ typedef struct gbtn_graph_desc {
   int32_t separate_bra;          /* 0: bra = conj(ket) (QuadraticFormNetwork);
                                     1: bra tensors are set separately
                                     (LinearFormNetwork / inner(phi, psi)) */
+  int32_t complex_values;        /* 0: real tensors; 1: complex (ComplexF64):
+                                    every tensor, message, RDM and scalar
+                                    array holds interleaved (re, im) doubles,
+                                    twice the element count.  Complex plans run
+                                    the FP64 sweeps (any schedule), environments,
+                                    expect (real part of <O>, O real), vertex
+                                    and edge scalars and logscalar; other entry
+                                    points return GBTN_ERR_UNSUPPORTED.
+                                    (test/test_belief_propagation.jl:18-20) */
 } gbtn_graph_desc;
 
 typedef struct gbtn_bp_opts {
@@ -275,8 +284,9 @@ int gbtn_bp_vjp(gbtn_plan* plan, const double* msg_cot, const gbtn_grad_opts* op
  * call on a device sets that array up (make it before any stream capture);
  * calls that overlap on the GPU share the array and race.  Asynchronous on
  * `stream` (NULL = the legacy default stream).
- * Returns GBTN_ERR_UNSUPPORTED when nv > GBTN_STATIC_MAX_VERTICES or
- * 2*ne > GBTN_STATIC_MAX_DIRECTED_EDGES; a vertex beyond the kernel limits
+ * Returns GBTN_ERR_UNSUPPORTED when nv > GBTN_STATIC_MAX_VERTICES,
+ * 2*ne > GBTN_STATIC_MAX_DIRECTED_EDGES or complex_values is set (real
+ * tensors only); a vertex beyond the kernel limits
  * (degree > 8, chi > 8, d > 8, d*prod(chi) > 8192) is skipped on the device and
  * makes *mean_diff NaN. */
 #define GBTN_STATIC_MAX_VERTICES 16384

@@ -76,6 +76,8 @@ struct gbtn_plan {
   gbtn_ctx* ctx = nullptr;
   int nv = 0, ne = 0, nnet = 1;
   bool sep_bra = false;
+  bool cplx = false;  // complex tensors: arrays hold interleaved (re, im) doubles
+  int es() const { return cplx ? 2 : 1; }  // doubles per element
   long long n_fac = 0, n_msg = 0, n_rdm = 0;
   int ncap = 0, maxdeg = 0;
   std::vector<VDesc> vd;
@@ -139,6 +141,9 @@ struct gbtn_plan {
 };
 
 namespace {
+
+// The interleaved (re, im) doubles of a complex plan's arrays as elements.
+inline zdouble* zptr(double* p) { return reinterpret_cast<zdouble*>(p); }
 
 constexpr int kSmallN = 1024;  // vertices with n <= kSmallN run one per warp
 constexpr int kStallSweeps = 5;  // reduced-precision phases stop at their noise floor
@@ -302,18 +307,19 @@ void sweep_loop(gbtn_plan* P, int maxiter, const GraphKey& key, F&& sweep) {
 
 // Sweeps of the parallel or coloured schedule in precision T.
 template <typename T>
-void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normalize, DevBuf<T>* msg, const T* fac,
+void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normalize, T* msg0, T* msg1, const T* fac,
                 const T* bra, int& cur, int stall = 0) {
   cudaStream_t s = P->ctx->stream;
   const bool want_diff = tol >= 0.0;
   GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int) * P->nnet, s));
   GBTN_CUDA(cudaMemsetAsync(P->d_iters.p, 0, sizeof(int) * P->nnet, s));
   const int* conv = want_diff ? P->d_conv.p : nullptr;
-  const GraphKey key{sizeof(T) == 4 ? 1 : 0, schedule, normalize, want_diff ? 1 : 0, stall, cur, P->list_version, tol};
+  T* msg[2] = {msg0, msg1};
+  const GraphKey key{sizeof(T) == 4 ? 1 : (sizeof(T) == 16 ? 3 : 0), schedule, normalize, want_diff ? 1 : 0, stall, cur, P->list_version, tol};
   sweep_loop(P, maxiter, key, [&] {
     if (schedule == GBTN_SCHED_PARALLEL) {
-      const T* in = msg[cur].p;
-      T* out = msg[cur ^ 1].p;
+      const T* in = msg[cur];
+      T* out = msg[cur ^ 1];
       {
         KTimer kt(P->ctx, sizeof(T) == 4 ? GBTN_KCLASS_SIMT_F32 : GBTN_KCLASS_SIMT_F64, P->lists[0].first.count > 0);
         launch_bp_vertices<T>(P->lists[0].first, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
@@ -327,7 +333,7 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
       cur ^= 1;
     } else {
       for (size_t c = 1; c < P->lists.size(); ++c) {
-        T* m = msg[cur].p;
+        T* m = msg[cur];
         launch_bp_vertices<T>(P->lists[c].first, P->d_vd.p, fac, bra, m, m, P->d_msg_off.p, P->d_diffs.p, conv,
                               normalize, want_diff, s);
         launch_bp_vertices<T>(P->lists[c].second, P->d_vd.p, fac, bra, m, m, P->d_msg_off.p, P->d_diffs.p, conv,
@@ -566,6 +572,12 @@ void finish_iters(gbtn_plan* P, bool want_diff, int maxiter, int32_t* iters, dou
 
 void compute_rdms(gbtn_plan* P) {
   cudaStream_t s = P->ctx->stream;
+  if (P->cplx) {
+    for (const WorkList* wl : {&P->lists[0].first, &P->lists[0].second})
+      launch_vertex_rdms<zdouble>(*wl, P->d_vd.p, zptr(P->d_fac.p), P->sep_bra ? zptr(P->d_bra.p) : nullptr,
+                                  zptr(P->d_msg[P->cur].p), P->d_msg_off.p, P->d_rdm_off.p, zptr(P->d_rdm.p), s);
+    return;
+  }
   launch_vertex_rdms(P->lists[0].first, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p,
                      P->d_msg_off.p, P->d_rdm_off.p, P->d_rdm.p, s);
   launch_vertex_rdms(P->lists[0].second, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p,
@@ -757,6 +769,7 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   P->nv = g->nv;
   P->ne = g->ne;
   P->sep_bra = g->separate_bra != 0;
+  P->cplx = g->complex_values != 0;
   P->nnet = g->vertex_network ? g->n_networks : 1;
   require(P->nnet >= 1, "n_networks must be >= 1");
   P->eu.assign(g->edge_u, g->edge_u + g->ne);
@@ -824,7 +837,8 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
     P->maxdeg = std::max(P->maxdeg, d.k);
     // the FP64 sweep needs its tensors in shared memory
     const int team = n <= kSmallN ? 32 : 256;
-    const size_t need = smem_need((int)n, d.k, P->sep_bra, sizeof(double), team) * (team == 32 ? 4 : 1);
+    const size_t need = smem_need((int)n, d.k, P->sep_bra, P->cplx ? sizeof(zdouble) : sizeof(double), team) *
+                        (team == 32 ? 4 : 1);
     if (need > 227 * 1024) throw Unsupported("vertex tensor too large for the shared-memory kernels");
   }
   for (int e = 0; e < g->ne; ++e) require(seen_count[e] == 2, "every edge must appear once in the legs of each endpoint");
@@ -837,19 +851,20 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   P->d_rdm_off.upload(P->rdm_off, s);
   P->d_dchi.upload(P->dchi, s);
   P->d_dsite.upload(P->dsite, s);
-  P->d_fac.alloc(P->n_fac);
-  GBTN_CUDA(cudaMemsetAsync(P->d_fac.p, 0, sizeof(double) * std::max<long long>(P->n_fac, 1), s));
-  if (P->sep_bra) P->d_bra.alloc(P->n_fac);
-  P->d_msg[0].alloc(std::max<long long>(P->n_msg, 1));
-  P->d_msg[1].alloc(std::max<long long>(P->n_msg, 1));
+  const int es = P->es();
+  P->d_fac.alloc(es * P->n_fac);
+  GBTN_CUDA(cudaMemsetAsync(P->d_fac.p, 0, sizeof(double) * es * std::max<long long>(P->n_fac, 1), s));
+  if (P->sep_bra) P->d_bra.alloc(es * P->n_fac);
+  P->d_msg[0].alloc(es * std::max<long long>(P->n_msg, 1));
+  P->d_msg[1].alloc(es * std::max<long long>(P->n_msg, 1));
   P->d_diffs.alloc(std::max<long long>(2LL * P->ne, 1));
   P->d_mean.alloc(P->nnet);
   P->d_conv.alloc(P->nnet);
   P->d_iters.alloc(P->nnet);
   P->d_since.alloc(P->nnet);
   P->d_best.alloc(P->nnet);
-  P->d_rdm.alloc(std::max<long long>(P->n_rdm, 1));
-  P->d_edge_sc.alloc(std::max(P->ne, 1));
+  P->d_rdm.alloc(es * std::max<long long>(P->n_rdm, 1));
+  P->d_edge_sc.alloc(es * std::max(P->ne, 1));
   P->d_re.alloc(P->nnet);
   P->d_im.alloc(P->nnet);
   P->d_scale.alloc(2 * (size_t)P->nv);
@@ -904,7 +919,7 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   // first reduced-precision run tunes the split, only native vertices use it
   P->ncol = ncol;
   P->tc_cand.assign(g->nv, 0);
-  if (!P->sep_bra && P->n_msg < (1LL << 31))
+  if (!P->sep_bra && !P->cplx && P->n_msg < (1LL << 31))
     for (int v = 0; v < g->nv; ++v) P->tc_cand[v] = tc_paddable(P->vd[v]) ? 1 : 0;
   build_tc_slots(P.get());
   P->d_err.alloc(1);
@@ -914,7 +929,7 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
     for (int v = 0; v < g->nv; ++v) use[v] = P->tc_cand[v] && tc_native(P->vd[v]);
     build_tc_lists(P.get(), use);
   }
-  launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[0].p, GBTN_INIT_IDENTITY, s);
+  launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[0].p, GBTN_INIT_IDENTITY, s, P->cplx);
   GBTN_CUDA(cudaStreamSynchronize(s));
   *out = P.release();
   API_CATCH(ctx)
@@ -939,8 +954,8 @@ int gbtn_set_factors(gbtn_plan* P, const double* ket, const double* bra, int mem
   API_TRY
   require(P && ket, "NULL argument");
   require(!P->sep_bra || bra, "plan has separate_bra: bra tensors are required");
-  copy_in(P, P->d_fac.p, ket, sizeof(double) * P->n_fac, mem);
-  if (P->sep_bra) copy_in(P, P->d_bra.p, bra, sizeof(double) * P->n_fac, mem);
+  copy_in(P, P->d_fac.p, ket, sizeof(double) * P->es() * P->n_fac, mem);
+  if (P->sep_bra) copy_in(P, P->d_bra.p, bra, sizeof(double) * P->es() * P->n_fac, mem);
   P->fac32_valid = false;
   P->zimg_valid = false;
   API_CATCH(C)
@@ -950,7 +965,7 @@ int gbtn_get_factors(gbtn_plan* P, double* ket, int mem) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && ket, "NULL argument");
-  copy_out(P, ket, P->d_fac.p, sizeof(double) * P->n_fac, mem);
+  copy_out(P, ket, P->d_fac.p, sizeof(double) * P->es() * P->n_fac, mem);
   API_CATCH(C)
 }
 
@@ -958,7 +973,7 @@ int gbtn_set_messages(gbtn_plan* P, const double* m, int mem) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && m, "NULL argument");
-  copy_in(P, P->d_msg[P->cur].p, m, sizeof(double) * P->n_msg, mem);
+  copy_in(P, P->d_msg[P->cur].p, m, sizeof(double) * P->es() * P->n_msg, mem);
   API_CATCH(C)
 }
 
@@ -966,7 +981,7 @@ int gbtn_get_messages(gbtn_plan* P, double* m, int mem) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && m, "NULL argument");
-  copy_out(P, m, P->d_msg[P->cur].p, sizeof(double) * P->n_msg, mem);
+  copy_out(P, m, P->d_msg[P->cur].p, sizeof(double) * P->es() * P->n_msg, mem);
   API_CATCH(C)
 }
 
@@ -975,7 +990,7 @@ int gbtn_init_messages(gbtn_plan* P, int kind) {
   API_TRY
   require(P, "NULL plan");
   require(kind == GBTN_INIT_IDENTITY || kind == GBTN_INIT_ONES, "unknown message init");
-  launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, kind, P->ctx->stream);
+  launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, kind, P->ctx->stream, P->cplx);
   API_CATCH(C)
 }
 
@@ -994,6 +1009,7 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
   }
   if (o->precision == GBTN_BF16 && o->schedule == GBTN_SCHED_SEQUENTIAL)
     throw Unsupported("BF16 sweeps run the parallel or coloured schedule");
+  if (P->cplx && o->precision != GBTN_F64) throw Unsupported("complex tensors run the FP64 path");
   if (o->schedule == GBTN_SCHED_SEQUENTIAL) {
     require(o->edge_sequence && o->edge_sequence_len > 0, "SEQUENTIAL needs an edge sequence");
     std::vector<std::vector<int2>> per(P->nnet);
@@ -1017,7 +1033,12 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     for (int n = 0; n < P->nnet; ++n) require(ptr[n + 1] > ptr[n], "edge_sequence misses a network");
     P->d_seq.upload(seq, s);
     P->d_seq_ptr.upload(ptr, s);
-    if (o->precision == GBTN_F64) {
+    if (P->cplx) {
+      launch_bp_sequential<zdouble>(P->nnet, P->d_vd.p, P->d_seq.p, P->d_seq_ptr.p, zptr(P->d_fac.p),
+                                    P->sep_bra ? zptr(P->d_bra.p) : nullptr, zptr(P->d_msg[P->cur].p),
+                                    P->d_msg_off.p, o->maxiter, o->tol, o->normalize, P->d_iters.p, P->d_mean.p,
+                                    P->ncap, P->maxdeg, s);
+    } else if (o->precision == GBTN_F64) {
       launch_bp_sequential<double>(P->nnet, P->d_vd.p, P->d_seq.p, P->d_seq_ptr.p, P->d_fac.p,
                                    P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p, P->d_msg_off.p, o->maxiter,
                                    o->tol, o->normalize, P->d_iters.p, P->d_mean.p, P->ncap, P->maxdeg, s);
@@ -1041,15 +1062,19 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     }
     return GBTN_OK;
   }
-  if (o->precision == GBTN_F64) {
-    run_sweeps<double>(P, o->schedule, o->maxiter, o->tol, o->normalize, P->d_msg, P->d_fac.p,
+  if (P->cplx) {
+    run_sweeps<zdouble>(P, o->schedule, o->maxiter, o->tol, o->normalize, zptr(P->d_msg[0].p), zptr(P->d_msg[1].p),
+                        zptr(P->d_fac.p), P->sep_bra ? zptr(P->d_bra.p) : nullptr, P->cur);
+    finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
+  } else if (o->precision == GBTN_F64) {
+    run_sweeps<double>(P, o->schedule, o->maxiter, o->tol, o->normalize, P->d_msg[0].p, P->d_msg[1].p, P->d_fac.p,
                        P->sep_bra ? P->d_bra.p : nullptr, P->cur);
     finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
   } else if (o->precision == GBTN_F32) {
     ensure_f32(P);
     int c32 = 0;
     launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, s);
-    run_sweeps<float>(P, o->schedule, o->maxiter, o->tol, o->normalize, P->d_msg32, P->d_fac32.p,
+    run_sweeps<float>(P, o->schedule, o->maxiter, o->tol, o->normalize, P->d_msg32[0].p, P->d_msg32[1].p, P->d_fac32.p,
                       P->sep_bra ? P->d_bra32.p : nullptr, c32);
     launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
     finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
@@ -1075,12 +1100,12 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
       const int it16 = o->maxiter_bf16 > 0 ? o->maxiter_bf16 : o->maxiter;
       run_sweeps_bf16(P, o->schedule, it16, tol16, o->normalize, c32, kStallSweeps);
     }
-    run_sweeps<float>(P, o->schedule, it32, tol32, o->normalize, P->d_msg32, P->d_fac32.p,
+    run_sweeps<float>(P, o->schedule, it32, tol32, o->normalize, P->d_msg32[0].p, P->d_msg32[1].p, P->d_fac32.p,
                       P->sep_bra ? P->d_bra32.p : nullptr, c32, kStallSweeps);
     launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
     // FP64 sweeps from the FP32 fixed point until tol (or refine_f64 / maxiter sweeps)
     const int nref = o->refine_f64 > 0 ? std::min(o->refine_f64, o->maxiter) : o->maxiter;
-    run_sweeps<double>(P, o->schedule, nref, o->tol, o->normalize, P->d_msg, P->d_fac.p,
+    run_sweeps<double>(P, o->schedule, nref, o->tol, o->normalize, P->d_msg[0].p, P->d_msg[1].p, P->d_fac.p,
                        P->sep_bra ? P->d_bra.p : nullptr, P->cur);
     finish_iters(P, want_diff, nref, iters, mean_diff);
   }
@@ -1125,6 +1150,7 @@ int gbtn_plan_tc_split(gbtn_plan* P, int32_t* is_tc, double* tuned_ms) {
 int gbtn_updated_message(gbtn_plan* P, int32_t de, double* out) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
+  if (P && P->cplx) throw Unsupported("updated_message of complex networks is not implemented");
   require(P && out, "NULL argument");
   require(de >= 0 && de < 2 * P->ne, "directed edge out of range");
   const int e = de / 2;
@@ -1145,7 +1171,7 @@ int gbtn_vertex_rdms(gbtn_plan* P, double* out) {
   API_TRY
   require(P && out, "NULL argument");
   compute_rdms(P);
-  copy_out(P, out, P->d_rdm.p, sizeof(double) * P->n_rdm, GBTN_HOST);
+  copy_out(P, out, P->d_rdm.p, sizeof(double) * P->es() * P->n_rdm, GBTN_HOST);
   API_CATCH(C)
 }
 
@@ -1168,9 +1194,14 @@ int gbtn_expect1(gbtn_plan* P, const double* ops, int per_vertex, double* out) {
     d_ops.upload(h, s);
   }
   d_res.alloc(P->nv);
-  expect1_kernel<<<(P->nv + 127) / 128, 128, 0, s>>>(P->nv, P->d_rdm_off.p, P->d_rdm.p, P->d_dsite.p, d_ops.p,
-                                                      per_vertex ? d_opoff.p : nullptr, d_res.p);
-  GBTN_CUDA(cudaGetLastError());
+  if (P->cplx) {
+    launch_expect1_z(P->nv, P->d_rdm_off.p, zptr(P->d_rdm.p), P->d_dsite.p, d_ops.p, per_vertex ? d_opoff.p : nullptr,
+                     d_res.p, s);
+  } else {
+    expect1_kernel<<<(P->nv + 127) / 128, 128, 0, s>>>(P->nv, P->d_rdm_off.p, P->d_rdm.p, P->d_dsite.p, d_ops.p,
+                                                        per_vertex ? d_opoff.p : nullptr, d_res.p);
+    GBTN_CUDA(cudaGetLastError());
+  }
   copy_out(P, out, d_res.p, sizeof(double) * P->nv, GBTN_HOST);
   API_CATCH(C)
 }
@@ -1233,6 +1264,7 @@ static void edge_rdms_device(gbtn_plan* P, const int32_t* edges, int32_t n, DevB
 int gbtn_edge_rdms(gbtn_plan* P, const int32_t* edges, int32_t n, double* out) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
+  if (P && P->cplx) throw Unsupported("two-site RDMs of complex networks is not implemented");
   require(P && edges && out && n >= 0, "bad argument");
   if (n == 0) return GBTN_OK;
   DevBuf<double> d_out;
@@ -1251,6 +1283,7 @@ int gbtn_edge_rdms(gbtn_plan* P, const int32_t* edges, int32_t n, double* out) {
 int gbtn_expect2(gbtn_plan* P, const int32_t* edges, int32_t n, const double* op, double* out) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
+  if (P && P->cplx) throw Unsupported("two-site expectation values of complex networks is not implemented");
   require(P && edges && op && out && n >= 0, "bad argument");
   if (n == 0) return GBTN_OK;
   cudaStream_t s = P->ctx->stream;
@@ -1282,14 +1315,17 @@ int gbtn_vertex_scalars(gbtn_plan* P, double* out) {
   API_TRY
   require(P && out, "NULL argument");
   compute_rdms(P);
-  std::vector<double> r(P->n_rdm);
-  copy_out(P, r.data(), P->d_rdm.p, sizeof(double) * P->n_rdm, GBTN_HOST);
-  // trace of each d x d block (a host-side read-out of the device RDMs)
-  for (int v = 0; v < P->nv; ++v) {
-    double z = 0.0;
-    for (int q = 0; q < P->dsite[v]; ++q) z += r[P->rdm_off[v] + q + P->dsite[v] * q];
-    out[v] = z;
-  }
+  const int es = P->es();
+  std::vector<double> r(es * P->n_rdm);
+  copy_out(P, r.data(), P->d_rdm.p, sizeof(double) * es * P->n_rdm, GBTN_HOST);
+  // trace of each d x d block (a host-side read-out of the device RDMs);
+  // complex plans write (re, im) pairs
+  for (int v = 0; v < P->nv; ++v)
+    for (int c = 0; c < es; ++c) {
+      double z = 0.0;
+      for (int q = 0; q < P->dsite[v]; ++q) z += r[es * (P->rdm_off[v] + q + P->dsite[v] * q) + c];
+      out[es * v + c] = z;
+    }
   API_CATCH(C)
 }
 
@@ -1298,8 +1334,12 @@ int gbtn_edge_scalars(gbtn_plan* P, double* out) {
   API_TRY
   require(P && out, "NULL argument");
   if (P->ne == 0) return GBTN_OK;
-  launch_edge_scalars(P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, P->d_edge_sc.p, P->ctx->stream);
-  copy_out(P, out, P->d_edge_sc.p, sizeof(double) * P->ne, GBTN_HOST);
+  if (P->cplx)
+    launch_edge_scalars_z(P->ne, P->d_dchi.p, P->d_msg_off.p, zptr(P->d_msg[P->cur].p), zptr(P->d_edge_sc.p),
+                          P->ctx->stream);
+  else
+    launch_edge_scalars(P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, P->d_edge_sc.p, P->ctx->stream);
+  copy_out(P, out, P->d_edge_sc.p, sizeof(double) * P->es() * P->ne, GBTN_HOST);
   API_CATCH(C)
 }
 
@@ -1309,6 +1349,15 @@ int gbtn_logscalar(gbtn_plan* P, double* re, double* im) {
   require(P && re, "NULL argument");
   cudaStream_t s = P->ctx->stream;
   compute_rdms(P);
+  if (P->cplx) {
+    if (P->ne)
+      launch_edge_scalars_z(P->ne, P->d_dchi.p, P->d_msg_off.p, zptr(P->d_msg[P->cur].p), zptr(P->d_edge_sc.p), s);
+    launch_logscalar_z(P->nnet, P->d_net_v_ptr.p, P->d_net_v.p, P->d_net_e_ptr.p, P->d_net_e.p, P->d_rdm_off.p,
+                       zptr(P->d_rdm.p), P->d_dsite.p, zptr(P->d_edge_sc.p), P->d_re.p, P->d_im.p, s);
+    copy_out(P, re, P->d_re.p, sizeof(double) * P->nnet, GBTN_HOST);
+    if (im) copy_out(P, im, P->d_im.p, sizeof(double) * P->nnet, GBTN_HOST);
+    return GBTN_OK;
+  }
   if (P->ne) launch_edge_scalars(P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, P->d_edge_sc.p, s);
   launch_logscalar(P->nnet, P->d_net_v_ptr.p, P->d_net_v.p, P->d_net_e_ptr.p, P->d_net_e.p, P->d_rdm_off.p,
                    P->d_rdm.p, P->d_dsite.p, P->d_edge_sc.p, P->d_re.p, P->d_im.p, s);
@@ -1320,6 +1369,7 @@ int gbtn_logscalar(gbtn_plan* P, double* re, double* im) {
 int gbtn_rescale_messages(gbtn_plan* P) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
+  if (P && P->cplx) throw Unsupported("rescale_messages of complex networks is not implemented");
   require(P, "NULL plan");
   if (P->ne) {
     KTimer kt(P->ctx, GBTN_KCLASS_GAUGE);
@@ -1332,6 +1382,7 @@ int gbtn_rescale_messages(gbtn_plan* P) {
 int gbtn_rescale_partitions(gbtn_plan* P) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
+  if (P && P->cplx) throw Unsupported("rescale_partitions of complex networks is not implemented");
   require(P, "NULL plan");
   cudaStream_t s = P->ctx->stream;
   compute_rdms(P);
@@ -1379,6 +1430,7 @@ const double* term_ket(Energy2& E, int k) {
 }
 
 void energy_setup(Energy2& E, gbtn_plan* P, int nterms, const double* coef, const double* ops) {
+  if (P->cplx) throw Unsupported("energies and gradients of complex networks are not implemented");
   require(!P->sep_bra, "energies and gradients need bra = conj(ket) (a quadratic-form network)");
   require(nterms >= 1 && coef && ops, "need at least one operator term");
   cudaStream_t s = P->ctx->stream;
@@ -1568,6 +1620,7 @@ int gbtn_bp_vjp(gbtn_plan* P, const double* msg_cot, const gbtn_grad_opts* o, do
                 double* resid) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
+  if (P && P->cplx) throw Unsupported("the BP vector-Jacobian product of complex networks is not implemented");
   require(P && msg_cot && o && grad, "NULL argument");
   require(o->mode == GBTN_GRAD_IMPLICIT, "gbtn_bp_vjp differentiates through the fixed point (IMPLICIT)");
   require(!P->sep_bra, "gradients need bra = conj(ket) (a quadratic-form network)");

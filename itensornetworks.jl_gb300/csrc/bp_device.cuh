@@ -20,6 +20,30 @@ __device__ __forceinline__ void tsync() {
     __syncthreads();
 }
 
+// Arithmetic of the complex FP64 element (zdouble, gbtn_internal.h) that the
+// fiber primitives need.  The bra of the quadratic form is conj(tensor) (dag
+// in the reference), which is the identity for real element types.
+__device__ __forceinline__ zdouble operator+(zdouble a, zdouble b) { return zdouble(a.re + b.re, a.im + b.im); }
+__device__ __forceinline__ zdouble& operator+=(zdouble& a, zdouble b) {
+  a.re += b.re;
+  a.im += b.im;
+  return a;
+}
+// multiply-accumulate a * b + c
+__device__ __forceinline__ float mac(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double mac(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ zdouble mac(zdouble a, zdouble b, zdouble c) {
+  return zdouble(fma(a.re, b.re, fma(-a.im, b.im, c.re)), fma(a.re, b.im, fma(a.im, b.re, c.im)));
+}
+__device__ __forceinline__ float conj_of(float x) { return x; }
+__device__ __forceinline__ double conj_of(double x) { return x; }
+__device__ __forceinline__ zdouble conj_of(zdouble x) { return zdouble(x.re, -x.im); }
+__device__ __forceinline__ float shfl_xor(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ zdouble shfl_xor(zdouble v, int o) {
+  return zdouble(__shfl_xor_sync(0xffffffffu, v.re, o), __shfl_xor_sync(0xffffffffu, v.im, o));
+}
+
 __device__ __forceinline__ double warp_sum(double x) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -42,7 +66,7 @@ __device__ __forceinline__ void warp_reduce_scatter(T (&v)[P2], int lane) {
       if (i < h) {
         T send = upper ? v[i] : v[i + h];
         T keep = upper ? v[i + h] : v[i];
-        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, mask);
+        v[i] = keep + shfl_xor(send, mask);
       }
     }
   }
@@ -67,7 +91,7 @@ __device__ __forceinline__ void absorb_fibers(const T* __restrict__ in, T* __res
     for (int b = 0; b < CHI; ++b) {
       T y = T(0);
 #pragma unroll
-      for (int a = 0; a < CHI; ++a) y = fma(m[b][a], x[a], y);
+      for (int a = 0; a < CHI; ++a) y = mac(m[b][a], x[a], y);
       out[base + b * st] = y;
     }
   }
@@ -111,12 +135,12 @@ __device__ __forceinline__ void close_fibers(const T* __restrict__ t, const T* _
 #pragma unroll
     for (int a = 0; a < CHI; ++a) {
       x[a] = t[base + a * st];
-      y[a] = bra[base + bra_shift + a * st];
+      y[a] = conj_of(bra[base + bra_shift + a * st]);
     }
 #pragma unroll
     for (int a = 0; a < CHI; ++a)
 #pragma unroll
-      for (int b = 0; b < CHI; ++b) acc[b + CHI * a] = fma(y[b], x[a], acc[b + CHI * a]);
+      for (int b = 0; b < CHI; ++b) acc[b + CHI * a] = mac(y[b], x[a], acc[b + CHI * a]);
   }
   const int lane = tid & 31, warp = tid >> 5;
   warp_reduce_scatter<T, P2>(acc, lane);
@@ -184,6 +208,36 @@ __device__ __forceinline__ double finalize_message(const T* res, int chi, const 
     const double na = warp_sum(a0 * a0 + a1 * a1);
     const double nb = warp_sum(o0 * o0 + o1 * o1);
     diff = 1.0 - (dot * dot) / (na * nb);
+  }
+  return diff;
+}
+
+// Complex messages: Frobenius norm sum |x|^2, message_diff with the complex
+// inner product <old, new> (|<a, b>|^2 as in the reference's message_diff).
+template <>
+__device__ __forceinline__ double finalize_message<zdouble>(const zdouble* res, int chi, const zdouble* old,
+                                                            zdouble* out, int normalize, bool want_diff, int lane) {
+  const int P = chi * chi;
+  const zdouble v0 = lane < P ? res[lane] : zdouble(0.0), v1 = lane + 32 < P ? res[lane + 32] : zdouble(0.0);
+  const double nrm2 = warp_sum(v0.re * v0.re + v0.im * v0.im + v1.re * v1.re + v1.im * v1.im);
+  const double sc = (normalize && nrm2 > 0.0) ? 1.0 / sqrt(nrm2) : 1.0;
+  const zdouble n0(v0.re * sc, v0.im * sc), n1(v1.re * sc, v1.im * sc);
+  zdouble o0(0.0), o1(0.0);
+  if (want_diff) {
+    if (lane < P) o0 = old[lane];
+    if (lane + 32 < P) o1 = old[lane + 32];
+  }
+  __syncwarp();
+  if (lane < P) out[lane] = n0;
+  if (lane + 32 < P) out[lane + 32] = n1;
+  double diff = 0.0;
+  if (want_diff) {
+    // <o, n> = sum conj(o) n
+    const double dre = warp_sum(o0.re * n0.re + o0.im * n0.im + o1.re * n1.re + o1.im * n1.im);
+    const double dim = warp_sum(o0.re * n0.im - o0.im * n0.re + o1.re * n1.im - o1.im * n1.re);
+    const double na = warp_sum(n0.re * n0.re + n0.im * n0.im + n1.re * n1.re + n1.im * n1.im);
+    const double nb = warp_sum(o0.re * o0.re + o0.im * o0.im + o1.re * o1.re + o1.im * o1.im);
+    diff = 1.0 - (dre * dre + dim * dim) / (na * nb);
   }
   return diff;
 }

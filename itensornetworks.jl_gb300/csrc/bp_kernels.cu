@@ -229,26 +229,26 @@ __global__ void __launch_bounds__(256)
 
 // rho_v[s', s] for every listed vertex: absorb all incoming messages, CLOSE on
 // the site index.
-template <int TEAM>
+template <typename T, int TEAM>
 __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
     vertex_rdm_kernel(const int* __restrict__ work, int nwork, const VDesc* __restrict__ vd,
-                      const double* __restrict__ fac, const double* __restrict__ bra_g, const double* msgs,
-                      const long long* __restrict__ msg_off, const long long* __restrict__ rdm_off, double* rdm,
+                      const T* __restrict__ fac, const T* __restrict__ bra_g, const T* msgs,
+                      const long long* __restrict__ msg_off, const long long* __restrict__ rdm_off, T* rdm,
                       int ncap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPB = TEAM == 32 ? 4 : 1;
   const int team = threadIdx.x / TEAM, tid = threadIdx.x % TEAM;
-  const size_t tb = team_smem_bytes<double>(ncap, 3, bra_g != nullptr, TEAM);
-  TeamSmem<double> S = carve<double>(smem_raw + team * tb, ncap, 3, bra_g != nullptr, TEAM);
+  const size_t tb = team_smem_bytes<T>(ncap, 3, bra_g != nullptr, TEAM);
+  TeamSmem<T> S = carve<T>(smem_raw + team * tb, ncap, 3, bra_g != nullptr, TEAM);
   for (int w = blockIdx.x * TPB + team; w < nwork; w += gridDim.x * TPB) {
     const int v = work[w];
     load_desc<TEAM>(S.desc, vd + v, tid);
     tsync<TEAM>();
-    load_vertex<double, TEAM>(S, fac, bra_g, msgs, msg_off, -1, tid);
+    load_vertex<T, TEAM>(S, fac, bra_g, msgs, msg_off, -1, tid);
     tsync<TEAM>();
-    const int cur = chain_absorb<double, TEAM>(S, -1, tid);
+    const int cur = chain_absorb<T, TEAM>(S, -1, tid);
     const VDesc& d = *S.desc;
-    close_any<double, TEAM>(d.d, S.buf[cur], S.bra, d.n, 1, 1, 0, 0, S.red, S.res, tid);
+    close_any<T, TEAM>(d.d, S.buf[cur], S.bra, d.n, 1, 1, 0, 0, S.red, S.res, tid);
     for (int i = tid; i < d.d * d.d; i += TEAM) rdm[rdm_off[v] + i] = S.res[i];
     tsync<TEAM>();
   }
@@ -351,13 +351,20 @@ __global__ void convert_kernel_f64_bf16(const double* a, __nv_bfloat16* b, long 
     b[i] = __double2bfloat16(a[i]);
 }
 
-__global__ void fill_messages_kernel(int ndir, const int* dchi, const long long* msg_off, double* msgs, int kind) {
+__global__ void fill_messages_kernel(int ndir, const int* dchi, const long long* msg_off, double* msgs, int kind,
+                                     int cplx) {
   const int de = blockIdx.x;
   if (de >= ndir) return;
   const int c = dchi[de];
   for (int i = threadIdx.x; i < c * c; i += blockDim.x) {
     const int b = i % c, a = i / c;
-    msgs[msg_off[de] + i] = kind == GBTN_INIT_ONES ? 1.0 / c : (a == b ? 1.0 : 0.0);
+    const double x = kind == GBTN_INIT_ONES ? 1.0 / c : (a == b ? 1.0 : 0.0);
+    if (cplx) {
+      msgs[2 * (msg_off[de] + i)] = x;
+      msgs[2 * (msg_off[de] + i) + 1] = 0.0;
+    } else {
+      msgs[msg_off[de] + i] = x;
+    }
   }
 }
 
@@ -433,6 +440,89 @@ __global__ void edge_scalars_kernel(int ne, const int* dchi, const long long* ms
   for (int i = lane; i < c2; i += 32) s += m1[i] * m2[i];
   s = warp_sum(s);
   if (lane == 0) out[e] = s;
+}
+
+// Complex edge scalar sum_i m1[i] m2[i] (the two messages contracted, no
+// conjugation -- ITensors contraction), one warp per edge.
+__global__ void edge_scalars_z_kernel(int ne, const int* dchi, const long long* msg_off, const zdouble* msgs,
+                                      zdouble* out) {
+  const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (e >= ne) return;
+  const int c2 = dchi[2 * e] * dchi[2 * e];
+  const zdouble* m1 = msgs + msg_off[2 * e];
+  const zdouble* m2 = msgs + msg_off[2 * e + 1];
+  double re = 0.0, im = 0.0;
+  for (int i = lane; i < c2; i += 32) {
+    const zdouble a = m1[i], b = m2[i];
+    re = fma(a.re, b.re, fma(-a.im, b.im, re));
+    im = fma(a.re, b.im, fma(a.im, b.re, im));
+  }
+  re = warp_sum(re);
+  im = warp_sum(im);
+  if (lane == 0) out[e] = zdouble(re, im);
+}
+
+// Complex logscalar per network: sum_v Log Z_v - sum_e Log z_e with
+// principal logs (log|z| + i arg z), Z_v = tr rho_v; -Inf on a zero edge scalar.
+__global__ void logscalar_z_kernel(const int* net_v_ptr, const int* net_v, const int* net_e_ptr, const int* net_e,
+                                   const long long* rdm_off, const zdouble* rdm, const int* dsite,
+                                   const zdouble* edge_sc, double* re, double* im) {
+  const int net = blockIdx.x;
+  double lre = 0.0, lim = 0.0, zero_e = 0.0;
+  for (int i = net_v_ptr[net] + threadIdx.x; i < net_v_ptr[net + 1]; i += blockDim.x) {
+    const int v = net_v[i];
+    const int d = dsite[v];
+    double zr = 0.0, zi = 0.0;
+    for (int s = 0; s < d; ++s) {
+      const zdouble x = rdm[rdm_off[v] + s + d * s];
+      zr += x.re;
+      zi += x.im;
+    }
+    lre += 0.5 * log(zr * zr + zi * zi);
+    lim += atan2(zi, zr);
+  }
+  for (int i = net_e_ptr[net] + threadIdx.x; i < net_e_ptr[net + 1]; i += blockDim.x) {
+    const zdouble z = edge_sc[net_e[i]];
+    const double a2 = z.re * z.re + z.im * z.im;
+    zero_e += a2 == 0.0 ? 1.0 : 0.0;
+    lre -= 0.5 * log(a2);
+    lim -= atan2(z.im, z.re);
+  }
+  __shared__ double red[3][32];
+  double vals[3] = {lre, lim, zero_e};
+  for (int q = 0; q < 3; ++q) {
+    const double t = warp_sum(vals[q]);
+    if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot[3] = {0.0, 0.0, 0.0};
+    for (int q = 0; q < 3; ++q)
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot[q] += red[q][w];
+    re[net] = tot[2] > 0.0 ? -INFINITY : tot[0];
+    im[net] = tot[2] > 0.0 ? 0.0 : tot[1];
+  }
+}
+
+// Real part of <O_v> = sum rho[a, b] O[a, b] / tr rho from complex RDMs, O real.
+__global__ void expect1_z_kernel(int nv, const long long* rdm_off, const zdouble* rdm, const int* dsite,
+                                 const double* ops, const long long* op_off, double* out) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int d = dsite[v];
+  const zdouble* r = rdm + rdm_off[v];
+  const double* o = ops + (op_off ? op_off[v] : 0);
+  double nr = 0.0, ni = 0.0, dr = 0.0, di = 0.0;
+  for (int i = 0; i < d * d; ++i) {
+    nr += r[i].re * o[i];
+    ni += r[i].im * o[i];
+  }
+  for (int q = 0; q < d; ++q) {
+    dr += r[q + d * q].re;
+    di += r[q + d * q].im;
+  }
+  out[v] = (nr * dr + ni * di) / (dr * dr + di * di);
 }
 
 // logscalar per network: sum_v log Z_v - sum_e log z_e in FP64, negative
@@ -511,6 +601,9 @@ template void launch_bp_vertices<double>(const WorkList&, const VDesc*, const do
                                          double*, const long long*, double*, const int*, int, int, cudaStream_t);
 template void launch_bp_vertices<float>(const WorkList&, const VDesc*, const float*, const float*, const float*, float*,
                                         const long long*, double*, const int*, int, int, cudaStream_t);
+template void launch_bp_vertices<zdouble>(const WorkList&, const VDesc*, const zdouble*, const zdouble*,
+                                          const zdouble*, zdouble*, const long long*, double*, const int*, int, int,
+                                          cudaStream_t);
 
 template <typename T>
 void launch_bp_sequential(int n_networks, const VDesc* vd, const int2* seq, const int* seq_ptr, const T* fac,
@@ -530,6 +623,9 @@ template void launch_bp_sequential<double>(int, const VDesc*, const int2*, const
                                            cudaStream_t);
 template void launch_bp_sequential<float>(int, const VDesc*, const int2*, const int*, const float*, const float*, float*,
                                           const long long*, int, double, int, int*, double*, int, int, cudaStream_t);
+template void launch_bp_sequential<zdouble>(int, const VDesc*, const int2*, const int*, const zdouble*,
+                                            const zdouble*, zdouble*, const long long*, int, double, int, int*,
+                                            double*, int, int, cudaStream_t);
 
 void launch_reduce_diffs(int n_networks, const int* net_de_ptr, const int* net_de, const double* diffs, double tol,
                          int* converged, int* iters, double* mean_diff, cudaStream_t s, int stall, double* best,
@@ -547,20 +643,48 @@ void launch_updated_message(const VDesc* vd, int v, int leg, const double* fac, 
   GBTN_CUDA(cudaGetLastError());
 }
 
-void launch_vertex_rdms(const WorkList& wl, const VDesc* vd, const double* fac, const double* bra, const double* msgs,
-                        const long long* msg_off, const long long* rdm_off, double* rdm, cudaStream_t s) {
+template <typename T>
+void launch_vertex_rdms(const WorkList& wl, const VDesc* vd, const T* fac, const T* bra, const T* msgs,
+                        const long long* msg_off, const long long* rdm_off, T* rdm, cudaStream_t s) {
   if (wl.count == 0) return;
   if (wl.team == 32) {
-    const size_t sm = 4 * team_smem_bytes<double>(wl.ncap, 3, bra != nullptr, 32);
-    GBTN_CUDA(cudaFuncSetAttribute(vertex_rdm_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    vertex_rdm_kernel<32><<<(wl.count + 3) / 4, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msgs, msg_off,
-                                                              rdm_off, rdm, wl.ncap);
+    const size_t sm = 4 * team_smem_bytes<T>(wl.ncap, 3, bra != nullptr, 32);
+    auto kern = vertex_rdm_kernel<T, 32>;
+    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    kern<<<(wl.count + 3) / 4, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msgs, msg_off, rdm_off, rdm,
+                                              wl.ncap);
   } else {
-    const size_t sm = team_smem_bytes<double>(wl.ncap, 3, bra != nullptr, 256);
-    GBTN_CUDA(cudaFuncSetAttribute(vertex_rdm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    vertex_rdm_kernel<256><<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msgs, msg_off, rdm_off,
-                                                      rdm, wl.ncap);
+    const size_t sm = team_smem_bytes<T>(wl.ncap, 3, bra != nullptr, 256);
+    auto kern = vertex_rdm_kernel<T, 256>;
+    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    kern<<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msgs, msg_off, rdm_off, rdm, wl.ncap);
   }
+  GBTN_CUDA(cudaGetLastError());
+}
+template void launch_vertex_rdms<double>(const WorkList&, const VDesc*, const double*, const double*, const double*,
+                                         const long long*, const long long*, double*, cudaStream_t);
+template void launch_vertex_rdms<zdouble>(const WorkList&, const VDesc*, const zdouble*, const zdouble*,
+                                          const zdouble*, const long long*, const long long*, zdouble*, cudaStream_t);
+
+void launch_edge_scalars_z(int ne, const int* dchi, const long long* msg_off, const zdouble* msgs, zdouble* out,
+                           cudaStream_t s) {
+  if (ne == 0) return;
+  edge_scalars_z_kernel<<<(ne + 7) / 8, 256, 0, s>>>(ne, dchi, msg_off, msgs, out);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_logscalar_z(int n_networks, const int* net_v_ptr, const int* net_v, const int* net_e_ptr,
+                        const int* net_e, const long long* rdm_off, const zdouble* rdm, const int* dsite,
+                        const zdouble* edge_sc, double* re, double* im, cudaStream_t s) {
+  logscalar_z_kernel<<<n_networks, 256, 0, s>>>(net_v_ptr, net_v, net_e_ptr, net_e, rdm_off, rdm, dsite, edge_sc,
+                                                re, im);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_expect1_z(int nv, const long long* rdm_off, const zdouble* rdm, const int* dsite, const double* ops,
+                      const long long* op_off, double* out, cudaStream_t s) {
+  if (nv == 0) return;
+  expect1_z_kernel<<<(nv + 127) / 128, 128, 0, s>>>(nv, rdm_off, rdm, dsite, ops, op_off, out);
   GBTN_CUDA(cudaGetLastError());
 }
 
@@ -594,9 +718,10 @@ void launch_convert_f64_to_bf16(const double* a, __nv_bfloat16* b, long long n, 
   convert_kernel_f64_bf16<<<grid_for(n), 256, 0, s>>>(a, b, n);
   GBTN_CUDA(cudaGetLastError());
 }
-void launch_fill_messages(int ndir, const int* dchi, const long long* msg_off, double* msgs, int kind, cudaStream_t s) {
+void launch_fill_messages(int ndir, const int* dchi, const long long* msg_off, double* msgs, int kind, cudaStream_t s,
+                          int cplx) {
   if (ndir == 0) return;
-  fill_messages_kernel<<<ndir, 64, 0, s>>>(ndir, dchi, msg_off, msgs, kind);
+  fill_messages_kernel<<<ndir, 64, 0, s>>>(ndir, dchi, msg_off, msgs, kind, cplx);
   GBTN_CUDA(cudaGetLastError());
 }
 void launch_scale_vertices(int nv, const VDesc* vd, double* fac, double* bra, const double* scale, cudaStream_t s) {

@@ -20,6 +20,14 @@ constexpr int kMaxSite = 8;       // physical dimension
 constexpr int kMaxOps = 48;       // schedule length per degree
 constexpr int kNumBufs = 4;       // shared-memory tensor buffers (0 = site tensor)
 
+// Complex FP64 element, interleaved (re, im) like numpy complex128 and Julia
+// ComplexF64; its arithmetic lives in bp_device.cuh.
+struct __align__(16) zdouble {
+  double re, im;
+  zdouble() = default;
+  __host__ __device__ constexpr zdouble(double r, double i = 0.0) : re(r), im(i) {}
+};
+
 // Per-vertex descriptor, read by every message / environment kernel.
 struct __align__(16) VDesc {
   long long a_off;          // element offset of the vertex tensor
@@ -100,9 +108,10 @@ void launch_updated_message(const VDesc* vd, int v, int leg, const double* fac, 
                             const double* msgs, const long long* msg_off, double* out, int ncap,
                             cudaStream_t s);
 
-void launch_vertex_rdms(const WorkList& wl, const VDesc* vd, const double* fac, const double* bra,
-                        const double* msgs, const long long* msg_off, const long long* rdm_off,
-                        double* rdm, cudaStream_t s);
+template <typename T>
+void launch_vertex_rdms(const WorkList& wl, const VDesc* vd, const T* fac, const T* bra,
+                        const T* msgs, const long long* msg_off, const long long* rdm_off,
+                        T* rdm, cudaStream_t s);
 
 void launch_edge_halves(const int* jobs /*pairs (v, leg)*/, int njobs, int ncap, int maxdeg,
                         const VDesc* vd, const double* fac, const double* bra, const double* msgs,
@@ -113,7 +122,8 @@ void launch_convert_f64_to_f32(const double* a, float* b, long long n, cudaStrea
 void launch_convert_f32_to_f64(const float* a, double* b, long long n, cudaStream_t s);
 void launch_convert_f64_to_bf16(const double* a, __nv_bfloat16* b, long long n, cudaStream_t s);
 void launch_fill_messages(int ndir, const int* dchi, const long long* msg_off, double* msgs, int kind,
-                          cudaStream_t s);
+                          cudaStream_t s,
+                          int cplx = 0);
 void launch_scale_vertices(int nv, const VDesc* vd, double* fac, double* bra, const double* scale,
                            cudaStream_t s);
 void launch_rescale_messages(int ne, const int* dchi, const long long* msg_off, double* msgs,
@@ -123,6 +133,16 @@ void launch_edge_scalars(int ne, const int* dchi, const long long* msg_off, cons
 void launch_logscalar(int n_networks, const int* net_v_ptr, const int* net_v, const int* net_e_ptr,
                       const int* net_e, const long long* rdm_off, const double* rdm, const int* dsite,
                       const double* edge_sc, double* re, double* im, cudaStream_t s);
+
+// Complex plans: edge scalars sum m_e * m_ebar, log-scalar with principal
+// complex logs, <O> from complex RDMs (real part, O real).
+void launch_edge_scalars_z(int ne, const int* dchi, const long long* msg_off, const zdouble* msgs, zdouble* out,
+                           cudaStream_t s);
+void launch_logscalar_z(int n_networks, const int* net_v_ptr, const int* net_v, const int* net_e_ptr,
+                        const int* net_e, const long long* rdm_off, const zdouble* rdm, const int* dsite,
+                        const zdouble* edge_sc, double* re, double* im, cudaStream_t s);
+void launch_expect1_z(int nv, const long long* rdm_off, const zdouble* rdm, const int* dsite, const double* ops,
+                      const long long* op_off, double* out, cudaStream_t s);
 
 // BF16 tensor-core path (bp_tc.cu): the kernel works on degree-4 vertices with
 // d = 2 and chi = 8; a vertex with d = 2, at most four legs and chi <= 8 is

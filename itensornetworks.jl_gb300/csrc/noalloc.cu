@@ -265,7 +265,8 @@ int gbtn_bp_sweep_static(int device, const gbtn_graph_desc* g, const double* fac
   if (device < 0 || device >= 64) {
     return GBTN_ERR_INVALID;
   }
-  if (g->nv < 1 || g->ne < 0 || g->nv > kStaticMaxVertices || 2LL * g->ne > kStaticMaxDirected) {
+  if (g->nv < 1 || g->ne < 0 || g->nv > kStaticMaxVertices || 2LL * g->ne > kStaticMaxDirected ||
+      g->complex_values) {
     return GBTN_ERR_UNSUPPORTED;
   }
   if (!g->edge_dim || !g->site_dim || !g->leg_ptr || (g->ne > 0 && (!g->edge_u || !g->leg_edge))) {

@@ -827,6 +827,10 @@ extern "C" {
 int gbtn_su_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, int32_t chi_max, gbtn_su** out) {
   if (!ctx || !g || !out) return GBTN_ERR_INVALID;
   *out = nullptr;
+  if (g->complex_values) {
+    gbtn::set_ctx_error(ctx, "the simple update takes real tensors");
+    return GBTN_ERR_UNSUPPORTED;
+  }
   try {
     auto S = std::make_unique<gbtn_su>();
     S->ctx = ctx;

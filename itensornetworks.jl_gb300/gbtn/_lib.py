@@ -64,6 +64,7 @@ class GraphDesc(C.Structure):
         ("vertex_network", C.POINTER(C.c_int32)),
         ("n_networks", C.c_int32),
         ("separate_bra", C.c_int32),
+        ("complex_values", C.c_int32),
     ]
 
 

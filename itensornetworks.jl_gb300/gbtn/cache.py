@@ -36,6 +36,13 @@ class BeliefPropagationCache:
         self.ctx = ctx or _lib.default_context()
         self.lib = self.ctx.lib
         self.separate_bra = bra is not None
+        # complex tensors (ComplexF64): interleaved (re, im) doubles on the device
+        self.complex = tn.is_complex or (bra is not None and any(np.iscomplexobj(t) for t in bra))
+        self.dtype = np.complex128 if self.complex else np.float64
+        if self.complex and not tn.is_complex:
+            tn = tn.copy()
+            tn.tensors = [np.asarray(t, dtype=np.complex128) for t in tn.tensors]
+            self.tn = tn
         desc, keep = tn.graph_desc(separate_bra=self.separate_bra)
         h = C.c_void_p()
         check(self.ctx.handle, self.lib.gbtn_plan_create(self.ctx.handle, C.byref(desc), C.byref(h)))
@@ -52,21 +59,21 @@ class BeliefPropagationCache:
         check(self.ctx.handle, code)
 
     def set_factors(self, ket, bra=None):
-        k = self.tn.flat(ket)
+        k = self.tn.flat([np.asarray(t, dtype=self.dtype) for t in ket])
         if self.separate_bra:
-            b = self.tn.flat(bra)
+            b = self.tn.flat([np.asarray(t, dtype=self.dtype) for t in bra])
             self._c(self.lib.gbtn_set_factors(self.handle, k.ctypes.data, b.ctypes.data, _lib.HOST))
         else:
             self._c(self.lib.gbtn_set_factors(self.handle, k.ctypes.data, None, _lib.HOST))
-        self.tn.tensors = [np.asarray(t, dtype=np.float64) for t in ket]
+        self.tn.tensors = [np.asarray(t, dtype=self.dtype) for t in ket]
 
     def factors(self):
-        out = np.empty(self.n_factor)
+        out = np.empty(self.n_factor, dtype=self.dtype)
         self._c(self.lib.gbtn_get_factors(self.handle, out.ctypes.data, _lib.HOST))
         return self.tn.unflat(out)
 
     def messages(self):
-        out = np.empty(max(self.n_message, 1))
+        out = np.empty(max(self.n_message, 1), dtype=self.dtype)
         self._c(self.lib.gbtn_get_messages(self.handle, out.ctypes.data, _lib.HOST))
         return self.tn.unflat_messages(out)
 
@@ -74,7 +81,8 @@ class BeliefPropagationCache:
         return self.messages()[de]
 
     def set_messages(self, msgs):
-        flat = self.tn.flat_messages(msgs) if isinstance(msgs, (list, tuple)) else np.ascontiguousarray(msgs, dtype=np.float64)
+        flat = (self.tn.flat_messages(msgs, self.complex) if isinstance(msgs, (list, tuple))
+                else np.ascontiguousarray(msgs, dtype=self.dtype))
         self._c(self.lib.gbtn_set_messages(self.handle, flat.ctypes.data, _lib.HOST))
 
     def init_messages(self, kind="identity"):
@@ -167,8 +175,8 @@ class BeliefPropagationCache:
 
     def vertex_rdms(self):
         n = sum(d * d for d in self.tn.site_dims)
-        out = np.empty(n)
-        self._c(self.lib.gbtn_vertex_rdms(self.handle, dptr(out)))
+        out = np.empty(n, dtype=self.dtype)
+        self._c(self.lib.gbtn_vertex_rdms(self.handle, dptr(out.view(np.float64))))
         res, off = [], 0
         for d in self.tn.site_dims:
             res.append(out[off:off + d * d].reshape((d, d), order="F"))
@@ -190,13 +198,13 @@ class BeliefPropagationCache:
         return res
 
     def vertex_scalars(self):
-        out = np.empty(self.tn.nv)
-        self._c(self.lib.gbtn_vertex_scalars(self.handle, dptr(out)))
+        out = np.empty(self.tn.nv, dtype=self.dtype)
+        self._c(self.lib.gbtn_vertex_scalars(self.handle, dptr(out.view(np.float64))))
         return out
 
     def edge_scalars(self):
-        out = np.empty(max(self.tn.ne, 1))
-        self._c(self.lib.gbtn_edge_scalars(self.handle, dptr(out)))
+        out = np.empty(max(self.tn.ne, 1), dtype=self.dtype)
+        self._c(self.lib.gbtn_edge_scalars(self.handle, dptr(out.view(np.float64))))
         return out[:self.tn.ne]
 
     def logscalar(self):

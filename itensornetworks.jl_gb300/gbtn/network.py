@@ -80,10 +80,16 @@ class TensorNetwork:
         return True
 
     # -- storage ---------------------------------------------------------------
+    @property
+    def is_complex(self):
+        """Complex tensors (ComplexF64): the library then stores interleaved
+        (re, im) doubles."""
+        return self.tensors is not None and any(np.iscomplexobj(t) for t in self.tensors)
+
     def flat(self, tensors=None):
         ts = self.tensors if tensors is None else tensors
-        return np.ascontiguousarray(
-            np.concatenate([np.asarray(t, dtype=np.float64).reshape(-1, order="F") for t in ts]))
+        dt = np.complex128 if any(np.iscomplexobj(t) for t in ts) else np.float64
+        return np.ascontiguousarray(np.concatenate([np.asarray(t, dtype=dt).reshape(-1, order="F") for t in ts]))
 
     def unflat(self, flat):
         out, off = [], 0
@@ -104,9 +110,10 @@ class TensorNetwork:
             off += c * c
         return out
 
-    def flat_messages(self, msgs):
-        return np.ascontiguousarray(
-            np.concatenate([np.asarray(m, dtype=np.float64).reshape(-1, order="F") for m in msgs]))
+    def flat_messages(self, msgs, complex_values=None):
+        cplx = any(np.iscomplexobj(m) for m in msgs) if complex_values is None else complex_values
+        dt = np.complex128 if cplx else np.float64
+        return np.ascontiguousarray(np.concatenate([np.asarray(m, dtype=dt).reshape(-1, order="F") for m in msgs]))
 
     def graph_desc(self, separate_bra=False):
         """(GraphDesc, keep-alive arrays) for gbtn_plan_create."""
@@ -132,6 +139,7 @@ class TensorNetwork:
             d.vertex_network = C.cast(None, C.POINTER(C.c_int32))
             d.n_networks = 1
         d.separate_bra = 1 if separate_bra else 0
+        d.complex_values = 1 if self.is_complex else 0
         return d, keep
 
     def copy(self):

@@ -13,6 +13,7 @@
 # converged messages as usual.  Real Float64/Float32 dense tensors with one
 # site index per vertex, one link per edge and chi <= 8 are supported; other
 # caches fall back to nothing -- they raise, as the library has no CPU path.
+# ComplexF64 tensors run the FP64 sweeps (complex_values = 1).
 #
 # It also adds `apply(Algorithm("gb300"), gates, psi; maxdim, cutoff, normalize,
 # envs)`, the simple update of src/apply.jl:33-160 on the GPU (FP64 truncated
@@ -46,6 +47,7 @@ struct GraphDesc
     vertex_network::Ptr{Int32}
     n_networks::Int32
     separate_bra::Int32
+    complex_values::Int32  # 1: ComplexF64 tensors, interleaved (re, im) in the library's arrays
 end
 
 struct BPOpts
@@ -95,7 +97,8 @@ function pack(bpc::BeliefPropagationCache)
     sdim = Int32[]
     leg_ptr = Int32[0]
     leg_edge = Int32[]
-    data = Float64[]
+    cplx = any(pv -> eltype(ket(pv)) <: Complex, pvs)
+    data = cplx ? ComplexF64[] : Float64[]
     for pv in pvs
         t = ket(pv)
         s = only(filter(i -> !(i in links), inds(t)))
@@ -105,7 +108,7 @@ function pack(bpc::BeliefPropagationCache)
         push!(sdim, length(s))
         append!(data, vec(array(t, s, ls...)))  # column-major, site index first
     end
-    return (; pvs, pes, links, eu, ev, edim, sdim, leg_ptr, leg_edge, data)
+    return (; pvs, pes, links, eu, ev, edim, sdim, leg_ptr, leg_edge, data, cplx)
 end
 
 function ITensorNetworks.update(alg::Algorithm"gb300_bp", bpc::BeliefPropagationCache)
@@ -113,12 +116,12 @@ function ITensorNetworks.update(alg::Algorithm"gb300_bp", bpc::BeliefPropagation
     ctx = context()
     GC.@preserve p begin
         desc = GraphDesc(length(p.pvs), length(p.pes), pointer(p.eu), pointer(p.ev), pointer(p.edim),
-            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0)
+            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0, p.cplx ? 1 : 0)
         plan = Ref{Ptr{Cvoid}}(C_NULL)
         check(ctx, ccall((:gbtn_plan_create, libgbtn), Cint, (Ptr{Cvoid}, Ref{GraphDesc}, Ref{Ptr{Cvoid}}),
             ctx, desc, plan))
         try
-            check(ctx, ccall((:gbtn_set_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Cint),
+            check(ctx, ccall((:gbtn_set_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint),
                 plan[], p.data, C_NULL, 0))
             sched = get(alg.kwargs, :schedule, "parallel") == "colored" ? 2 : 1
             prec = Dict("f64" => 0, "f32" => 1, "bf16" => 2, "mixed" => 3)[get(alg.kwargs, :precision, "f64")]
@@ -129,8 +132,8 @@ function ITensorNetworks.update(alg::Algorithm"gb300_bp", bpc::BeliefPropagation
             check(ctx, ccall((:gbtn_bp_run, libgbtn), Cint, (Ptr{Cvoid}, Ref{BPOpts}, Ref{Int32}, Ref{Float64}),
                 plan[], opts, iters, diff))
             nmsg = sum(Int(c)^2 for c in p.edim) * 2
-            flat = Vector{Float64}(undef, nmsg)
-            check(ctx, ccall((:gbtn_get_messages, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Float64}, Cint),
+            flat = Vector{eltype(p.data)}(undef, nmsg)
+            check(ctx, ccall((:gbtn_get_messages, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint),
                 plan[], flat, 0))
             # unpack: directed edge 2e = u->v, 2e+1 = v->u; message M[b, a] with
             # b the bra (primed) link and a the ket link
@@ -213,7 +216,7 @@ function ITensorNetworks.apply(::Algorithm"gb300", gates::Vector{ITensor}, psi; 
     end
     GC.@preserve p eidx gdata begin
         desc = GraphDesc(length(p.vs), length(p.es), pointer(p.eu), pointer(p.ev), pointer(p.edim),
-            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0)
+            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0, 0)
         h = Ref{Ptr{Cvoid}}(C_NULL)
         check(ctx, ccall((:gbtn_su_create, libgbtn), Cint, (Ptr{Cvoid}, Ref{GraphDesc}, Int32, Ref{Ptr{Cvoid}}),
             ctx, desc, chimax, h))
@@ -282,7 +285,7 @@ function energy_and_grad(psi, ops, coefs; maxiter=500, want_grad=true)
     opbuf = reduce(vcat, vec.(ops))
     GC.@preserve p opbuf begin
         desc = GraphDesc(length(p.vs), length(p.es), pointer(p.eu), pointer(p.ev), pointer(p.edim),
-            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0)
+            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0, 0)
         plan = Ref{Ptr{Cvoid}}(C_NULL)
         check(ctx, ccall((:gbtn_plan_create, libgbtn), Cint, (Ptr{Cvoid}, Ref{GraphDesc}, Ref{Ptr{Cvoid}}),
             ctx, desc, plan))

@@ -1,0 +1,98 @@
+"""Complex tensors (ComplexF64, test/test_belief_propagation.jl:18-20) on the
+FP64 path against the oracle, which conjugates the bra and uses the complex
+inner product in message_diff: messages after a fixed number of sweeps to
+1e-10 (every schedule), <Sz> and the complex log-scalar to 1e-10, exactness
+on a tree, inner products with a separate bra.  Paths that take real tensors
+only report GBTN_ERR_UNSUPPORTED."""
+import numpy as np
+import pytest
+
+import bp_oracle as O
+import gbtn
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(lib_built):
+    yield
+
+
+def cnet(g, seed):
+    A = O.random_network(g, seed, dtype=np.complex128, unit_norm=True)
+    tn = gbtn.TensorNetwork(g.nv, g.edges, g.site_dims, g.edge_dims, [a.copy() for a in A])
+    return tn, A
+
+
+@pytest.mark.parametrize("schedule", ["parallel", "colored", "sequential"])
+def test_complex_messages_match_oracle(schedule):
+    # few sweeps: BP on this random complex network does not converge, and its
+    # sequential dynamics amplify rounding differences sweep after sweep
+    g = O.square_lattice(4, 4, chi=3)
+    tn, A = cnet(g, 3)
+    n = 4
+    ref, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=n, schedule=schedule)
+    bpc = gbtn.BeliefPropagationCache(tn).update(maxiter=n, schedule=schedule)
+    got = bpc.messages()
+    assert all(np.iscomplexobj(m) for m in got)
+    err = max(np.max(np.abs(got[de] - ref[de])) for de in range(2 * g.ne))
+    assert err < 1e-10, f"{schedule}: {err:.3e}"
+
+
+def test_complex_expect_logscalar_and_convergence():
+    g = O.square_lattice(5, 4, chi=2)
+    tn, A = cnet(g, 8)
+    # converges (tol bounds 1 - cos^2 of messages) ...
+    conv = gbtn.BeliefPropagationCache(tn).update(maxiter=400, tol=1e-14, schedule="parallel")
+    assert conv.iterations[0] < 400
+    # ... and a fixed, fully converged sweep count is compared at 1e-10
+    bpc = gbtn.BeliefPropagationCache(tn).update(maxiter=400, schedule="parallel")
+    m, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=400, schedule="parallel")
+    sz_ref = np.real(O.expect1(g, A, m, O.SZ))
+    np.testing.assert_allclose(bpc.expect(O.SZ), sz_ref, rtol=0, atol=1e-10 * np.max(np.abs(sz_ref)))
+    ls_ref = O.logscalar(g, A, A, m)
+    ls = bpc.logscalar()
+    assert complex(ls).real == pytest.approx(np.real(ls_ref), rel=1e-10, abs=1e-10)
+    # the imaginary part of a sum of principal logs is defined modulo 2 pi
+    dphi = (complex(ls).imag - np.imag(ls_ref)) / (2 * np.pi)
+    assert abs(dphi - round(dphi)) < 1e-9
+    # Frobenius normalisation leaves the phase of a complex message free: after
+    # many sweeps the messages agree up to a phase each, which vertex scalars
+    # carry and <Sz> and the log-scalar (each message once in a vertex and once
+    # in an edge scalar) do not
+    got = bpc.messages()
+    for de in range(2 * g.ne):
+        assert abs(np.vdot(got[de], m[de])) == pytest.approx(1.0, abs=1e-10)
+    z = bpc.vertex_scalars()
+    assert np.iscomplexobj(z) and z.shape == (g.nv,)
+    np.testing.assert_allclose(np.abs(z), [abs(O.vertex_scalar(g, A, A, m, v)) for v in range(g.nv)], rtol=1e-10)
+
+
+def test_complex_bp_is_exact_on_a_tree():
+    g = O.random_tree(12, 5, chi=3)
+    tn, A = cnet(g, 9)
+    bpc = gbtn.BeliefPropagationCache(tn).update(maxiter=30, schedule="parallel")
+    exact = [np.real(np.sum(O.exact_rdm1(g, A, v) * O.SZ) / np.trace(O.exact_rdm1(g, A, v))) for v in range(g.nv)]
+    np.testing.assert_allclose(bpc.expect(O.SZ), exact, rtol=0, atol=1e-10)
+    assert np.exp(complex(bpc.logscalar())) == pytest.approx(O.exact_scalar(g, A), rel=1e-9)
+
+
+def test_complex_inner_with_separate_bra_on_a_tree():
+    g = O.random_tree(10, 2, chi=2)
+    tn, A = cnet(g, 4)
+    _, B = cnet(g, 5)
+    phi = gbtn.TensorNetwork(g.nv, g.edges, g.site_dims, g.edge_dims, [b.copy() for b in B])
+    val = gbtn.inner(phi, tn, cache_update_kwargs=dict(maxiter=30, schedule="parallel"))
+    assert complex(val) == pytest.approx(complex(O.exact_scalar(g, A, B)), rel=1e-9)
+
+
+def test_complex_paths_outside_fp64_are_unsupported():
+    g = O.square_lattice(3, 3, chi=2)
+    tn, A = cnet(g, 1)
+    bpc = gbtn.BeliefPropagationCache(tn)
+    with pytest.raises(gbtn.Unsupported):
+        bpc.update(maxiter=2, schedule="parallel", precision="bf16")
+    with pytest.raises(gbtn.Unsupported):
+        bpc.edge_rdms()
+    with pytest.raises(gbtn.Unsupported):
+        gbtn.SimpleUpdateState(tn, 4)

@@ -66,8 +66,9 @@ def test_flat_roundtrip():
 
 
 def test_struct_layouts():
-    # GraphDesc: 2 ints, 6 pointers, 1 pointer, 2 ints (x86-64 / aarch64 LP64)
-    assert C.sizeof(_lib.GraphDesc) == 8 + 7 * 8 + 8
+    # GraphDesc: 2 ints, 6 pointers, 1 pointer, 3 ints + padding (x86-64 / aarch64 LP64)
+    assert C.sizeof(_lib.GraphDesc) == 8 + 7 * 8 + 12 + 4
+    assert _lib.GraphDesc.complex_values.offset == 8 + 7 * 8 + 8
     assert C.sizeof(_lib.BPOpts) == 16 + 8 + 8 + 8 + 8 + 8 + 16
 
 
