@@ -295,6 +295,14 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's TMEM lanes
+  // operand descriptors at offset 0 (K-major tiles: LBO 16 B, SBO 1024 B; Z read
+  // MN-major: LBO 8192 B between the two site halves), formed by the issuing thread
+  auto descs = [&](uint64_t& dZk, uint64_t& dZmn, uint64_t& dKT, uint64_t& dT34) {
+    dZk = tc::smem_desc(tc::smem_u32(Z), 16, 1024);
+    dZmn = tc::smem_desc(tc::smem_u32(Z), 8192, 1024);
+    dKT = tc::smem_desc(tc::smem_u32(KT), 16, 1024);
+    dT34 = tc::smem_desc(tc::smem_u32(T34), 16, 1024);
+  };
 
   // thread-0 bookkeeping of the asynchronous work in flight
   uint32_t mma_phase = 0, tma_phase = 0;
@@ -413,18 +421,19 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     __syncthreads();
     if (*abort_flag) break;
 
-    const uint32_t zaddr = tc::smem_u32(Z), ktaddr = tc::smem_u32(KT), t34addr = tc::smem_u32(T34);
     // ---- GEMM1 -> columns [0,64), GEMM1' -> [64,128) (M = 128) ----
+    // descriptors: per-CTA bases (dZk, dZmn, dKT, dT34) plus the operand's
+    // byte offset in 16-byte units (the start-address field of the descriptor)
     if (t == 0) {
       tc::tc_fence_after();
+      uint64_t dZk, dZmn, dKT, dT34;
+      descs(dZk, dZmn, dKT, dT34);
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk)
-        tc::mma_bf16(tmem + 0, tc::smem_desc(zaddr + 32 * kk, 16, 1024), tc::smem_desc(ktaddr + 32 * kk, 16, 1024),
-                     kIdescG1, kk > 0);
+        tc::mma_bf16(tmem + 0, dZk + ((32 * kk) >> 4), dKT + ((32 * kk) >> 4), kIdescG1, kk > 0);
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk)
-        tc::mma_bf16(tmem + 64, tc::smem_desc(zaddr + 2048 * kk, 8192, 1024),
-                     tc::smem_desc(ktaddr + 8192 + 32 * kk, 16, 1024), kIdescG1mn, kk > 0);
+        tc::mma_bf16(tmem + 64, dZmn + ((2048 * kk) >> 4), dKT + ((8192 + 32 * kk) >> 4), kIdescG1mn, kk > 0);
       tc::mma_commit(mma_bar);
       mma_pending = 1;
       *abort_flag = wait_mma() ? 0 : 1;
@@ -453,17 +462,17 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     // ---- GEMM2 -> G34 in columns [0,64), GEMM2' -> G12 in [64,128) (M = 64, K = 128) ----
     if (t == 0) {
       tc::tc_fence_after();
+      uint64_t dZk, dZmn, dKT, dT34;
+      descs(dZk, dZmn, dKT, dT34);
 #pragma unroll
       for (int kk = 0; kk < 8; ++kk) {
-        const uint32_t so = 8192 * (kk >> 2), ko = 32 * (kk & 3);
-        tc::mma_bf16(tmem + 0, tc::smem_desc(ktaddr + so + ko, 16, 1024), tc::smem_desc(zaddr + so + ko, 16, 1024),
-                     kIdescG2, kk > 0);
+        const uint32_t o = (8192 * (kk >> 2) + 32 * (kk & 3)) >> 4;
+        tc::mma_bf16(tmem + 0, dKT + o, dZk + o, kIdescG2, kk > 0);
       }
 #pragma unroll
       for (int kk = 0; kk < 8; ++kk) {
-        const uint32_t so = 8192 * (kk >> 2), ko = 32 * (kk & 3);
-        tc::mma_bf16(tmem + 64, tc::smem_desc(t34addr + so + ko, 16, 1024),
-                     tc::smem_desc(zaddr + 2048 * kk, 8192, 1024), kIdescG2mn, kk > 0);
+        const uint32_t o = (8192 * (kk >> 2) + 32 * (kk & 3)) >> 4;
+        tc::mma_bf16(tmem + 64, dT34 + o, dZmn + ((2048 * kk) >> 4), kIdescG2mn, kk > 0);
       }
       tc::mma_commit(mma_bar);
       mma_pending = 1;
