@@ -343,7 +343,9 @@ __device__ void cta_svd(double* A, int m, int n, double* V, double* sig, SvdBufs
 }
 
 // Householder QR of M (m x n column-major, lda = m): R (r x n, ldr = r) and
-// Q (m x r, ldq = m), r = min(m, n).  M is overwritten; beta: >= n doubles.
+// Q (m x r, ldq = m), r = min(m, n).  M is overwritten by the reflectors
+// (column j holds v_j from row j on; beta_j = 0 marks a skipped reflector);
+// with Q = NULL the reflectors are the result.  beta: >= n doubles.
 // The warp that updates column j + 1 also returns that column's squared norm
 // below row j + 1, so each reflector costs two barriers; Q is accumulated
 // backwards, touching only the columns a reflector changes.
@@ -399,6 +401,10 @@ __device__ void cta_qr(double* M, int m, int n, double* R, double* Q, double* be
     const int row = i % r, col = i / r;
     if (col > row) R[i] = M[(size_t)col * m + row];
     else if (col < row) R[i] = 0.0;
+  }
+  if (!Q) {  // the caller keeps the reflectors and applies them itself
+    __syncthreads();
+    return;
   }
   // Q = H_0 ... H_{r-1} [I; 0]; H_j leaves the columns c < j (still e_c) alone
   for (int i = tid; i < m * r; i += kSuThreads) Q[i] = (i % m == i / m) ? 1.0 : 0.0;
@@ -495,7 +501,9 @@ struct SuArgs {
   double cutoff;
   int normalize;
   int chimax;
-  double* qscratch;          // 2 * kSuMaxN doubles per job
+  double* side_scratch;      // per (job, side): reflectors, beta, R, inverse-sqrt environments, rank
+  double* job_scratch;       // per job: left / right factors, sqrt(S), kept dimension
+  int bmax;                  // bound on theta's rows and columns (shared-memory carve of the SVD)
   double* truncerr;          // [njobs] or NULL
   double* svals;             // [njobs * maxdim] or NULL
   int* status;               // set to 1 when a shape exceeds the kernel limits
@@ -539,62 +547,79 @@ __device__ __forceinline__ void split_index(const SideShape& sh, const int* chi,
   }
 }
 
-__global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
+// Scratch between the three stages of a gate batch (global memory).
+constexpr int kSideRefl = 0;                           // m x r reflectors, lda = m
+constexpr int kSideBeta = kSuMaxN;                     // r reflector coefficients
+constexpr int kSideR = kSideBeta + 64;                 // r x ncol, ldr = r
+constexpr int kSideSI = kSideR + 2048;                 // inverse-sqrt environments, kMaxDeg x 64
+constexpr int kSideMeta = kSideSI + kMaxDeg * 64;      // [0] = r, [1] = status
+constexpr int kSideStride = kSideMeta + 8;
+constexpr int kJobU = 0;                               // left factor, mt x kk (ld mt)
+constexpr int kJobV = kSuMaxTheta * kSuMaxTheta;       // right factor, nt x kk (ld nt)
+constexpr int kJobS = 2 * kSuMaxTheta * kSuMaxTheta;   // sqrt of the kept singular values
+constexpr int kJobMeta = kJobS + kSuMaxTheta;          // [0] = kk, [1] = ok
+constexpr int kJobStride = kJobMeta + 8;
+
+// The gate's site on `side`: shape with the current bond dimensions, and
+// whether the stages' limits hold (uniform over the CTA).
+__device__ bool site_of(const SuArgs& a, const SuJob& job, int side, int& x, SideShape& h) {
+  x = side ? job.v : job.u;
+  side_shape(a, x, side ? job.pv : job.pu, h);
+  const int ce = h.chi[h.p];
+  const int r = min(h.m, h.d * ce);
+  return h.n <= kSuMaxN && h.d * ce <= 32 && h.k <= kMaxDeg && r * h.d <= a.bmax;
+}
+
+// Stage 1, one CTA per (gate, side): square-root environments absorbed,
+// the site matricised as (other legs) x (site, bond) and QR-factorised
+// (Householder, Q kept as reflectors).  Writes R, the reflectors, beta and
+// the inverse-square-root environments to the side's scratch.
+__global__ void __launch_bounds__(kSuThreads, 3) su_qr_kernel(SuArgs a) {
   extern __shared__ __align__(16) double smem[];
-  double* T = smem;                       // kSuMaxN
-  double* W = T + kSuMaxN;                // kSuMaxN
-  double* TH = W + kSuMaxN;               // 64 x 64
-  double* V = TH + kSuMaxTheta * kSuMaxTheta;  // 64 x 64
-  double* RU = V + kSuMaxTheta * kSuMaxTheta;  // 32 x 32
-  double* RV = RU + 1024;                 // 32 x 32
-  double* SI = RV + 1024;                 // 2 sides x kMaxDeg x 64 inverse-sqrt environments
-  double* S = SI + 2 * kMaxDeg * 64;      // 64
-  double* sig = S + 64;                   // 64
-  double* beta = sig + 64;                // 64
+  const int j = blockIdx.x >> 1, side = blockIdx.x & 1, tid = threadIdx.x;
+  if (j >= a.njobs) return;
+  const SuJob job = a.jobs[j];
+  int x;
+  SideShape h;
+  const bool ok = site_of(a, job, side, x, h);
+  double* out = a.side_scratch + (size_t)blockIdx.x * kSideStride;
+  if (!ok) {
+    if (tid == 0) {
+      atomicExch(a.status, 1);
+      out[kSideMeta + 1] = 1.0;
+    }
+    return;
+  }
+  double* W = smem;                       // matricised site (then reflectors), kSuMaxN
+  double* T = W + kSuMaxN;                // site tensor when environments are absorbed, kSuMaxN
+  double* small = T + (a.envs ? kSuMaxN : 0);
+  double* R = small;                      // 1024
+  double* beta = R + 1024;                // 64
   double* red = beta + 64;                // 32
-  double* aux = red + 32;                 // 3 x 64: pivot norms, R diagonal, reflector coefficients
+  double* S = red + 32;                   // 64
+  double* A8 = S + 64;                    // 64: environment matrix
+  double* V8 = A8 + 64;                   // 64
+  double* sig = V8 + 64;                  // 64
+  double* aux = sig + 64;                 // 192
   int* ord = reinterpret_cast<int*>(aux + 192);  // 64
   int* perm = ord + 64;                   // 64
-  __shared__ int s_flag, s_k, s_ok;
-  __shared__ double s_scale;
-  const int tid = threadIdx.x;
-  const int j = blockIdx.x;
-  if (j >= a.njobs) return;
-  SvdBufs sb{W, aux, aux + 64, aux + 128, perm, ord, &s_flag, red};
-  const SuJob job = a.jobs[j];
-  SideShape sh[2];
-  side_shape(a, job.u, job.pu, sh[0]);
-  side_shape(a, job.v, job.pv, sh[1]);
-  const int ce = sh[0].chi[job.pu];
-  if (tid == 0) {
-    int ok = sh[0].n <= kSuMaxN && sh[1].n <= kSuMaxN;
-    for (int x = 0; x < 2; ++x) ok = ok && sh[x].d * ce <= 32 && sh[x].k <= kMaxDeg;
-    const int ru = min(sh[0].m, sh[0].d * ce), rv = min(sh[1].m, sh[1].d * ce);
-    ok = ok && ru * sh[0].d <= kSuMaxTheta && rv * sh[1].d <= kSuMaxTheta;
-    s_ok = ok;
-    if (!ok) atomicExch(a.status, 1);
-  }
-  __syncthreads();
-  if (!s_ok) return;
-  double* R[2] = {RU, RV};
-  int r[2];
-  const int xs[2] = {job.u, job.v};
-  for (int side = 0; side < 2; ++side) {
-    const SideShape& h = sh[side];
-    const int x = xs[side];
-    const double* src = a.tens + a.cap_off[x];
+  __shared__ int s_flag;
+  const double* src = a.tens + a.cap_off[x];
+  const int ce = h.chi[h.p], ncol = h.d * ce;
+  if (a.envs) {
+    SvdBufs sb{W, aux, aux + 64, aux + 128, perm, ord, &s_flag, red};
     for (int i = tid; i < h.n; i += kSuThreads) T[i] = src[i];
     __syncthreads();
     double* cur = T;
     double* nxt = W;
     int st = h.d;
     for (int q = 0; q < h.k; ++q) {
-      if (q != h.p && a.envs) {
+      if (q != h.p) {
         const int f = a.leg_edge[a.leg_ptr[x] + q];
         const int de_in = a.edge_u[f] == x ? 2 * f + 1 : 2 * f;
         const double* env = a.envs + (size_t)de_in * a.chimax * a.chimax;
         sb.work = nxt;
-        cta_env_sqrt(env, h.chi[q], S, SI + (side * kMaxDeg + q) * 64, TH, V, sig, sb);
+        cta_env_sqrt(env, h.chi[q], S, out + kSideSI + q * 64, A8, V8, sig, sb);
         absorb_any<double>(h.chi[q], cur, nxt, h.n, st, S, tid, kSuThreads);
         __syncthreads();
         double* t = cur;
@@ -603,28 +628,77 @@ __global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
       }
       st *= h.chi[q];
     }
-    // matricise: M[row, s + d * bond] (rows = other legs), into the free buffer
-    const int ncol = h.d * ce;
+    if (cur == W) {  // the matricised copy goes to W
+      for (int i = tid; i < h.n; i += kSuThreads) T[i] = W[i];
+      __syncthreads();
+    }
     for (int i = tid; i < h.n; i += kSuThreads) {
       int row, s, b;
       split_index(h, h.chi, i, row, s, b);
-      nxt[row + (size_t)h.m * (s + h.d * b)] = cur[i];
+      W[row + (size_t)h.m * (s + h.d * b)] = T[i];
     }
-    __syncthreads();
-    r[side] = min(h.m, ncol);
-    cta_qr(nxt, h.m, ncol, R[side], cur, beta, red);  // Q into cur
-    double* qs = a.qscratch + ((size_t)j * 2 + side) * kSuMaxN;
-    for (int i = tid; i < h.m * r[side]; i += kSuThreads) qs[i] = cur[i];
-    __syncthreads();
+  } else {
+    for (int i = tid; i < h.n; i += kSuThreads) {
+      int row, s, b;
+      split_index(h, h.chi, i, row, s, b);
+      W[row + (size_t)h.m * (s + h.d * b)] = src[i];
+    }
   }
+  __syncthreads();
+  const int r = min(h.m, ncol);
+  cta_qr(W, h.m, ncol, R, nullptr, beta, red);
+  for (int i = tid; i < h.m * r; i += kSuThreads) out[kSideRefl + i] = W[i];
+  for (int i = tid; i < r * ncol; i += kSuThreads) out[kSideR + i] = R[i];
+  if (tid < r) out[kSideBeta + tid] = beta[tid];
+  if (tid == 0) {
+    out[kSideMeta] = (double)r;
+    out[kSideMeta + 1] = 0.0;
+  }
+}
+
+// Stage 2, one CTA per gate: theta = R_u R_v over the bond with the gate on
+// the two site indices, its SVD and the ITensors truncation.  Writes the kept
+// left and right factors, sqrt(S) and the new bond dimension.
+__global__ void __launch_bounds__(kSuThreads, 2) su_svd_kernel(SuArgs a) {
+  extern __shared__ __align__(16) double smem[];
+  const int j = blockIdx.x, tid = threadIdx.x;
+  if (j >= a.njobs) return;
+  const SuJob job = a.jobs[j];
+  const double* su = a.side_scratch + (size_t)(2 * j) * kSideStride;
+  const double* sv = a.side_scratch + (size_t)(2 * j + 1) * kSideStride;
+  double* out = a.job_scratch + (size_t)j * kJobStride;
+  if (su[kSideMeta + 1] != 0.0 || sv[kSideMeta + 1] != 0.0) {  // a side exceeded the limits
+    if (tid == 0) out[kJobMeta + 1] = 0.0;
+    return;
+  }
+  const int B = a.bmax;
+  double* TH = smem;                      // B x B
+  double* V = TH + B * B;                 // B x B
+  double* W = V + B * B;                  // 2 B x B (theta build, SVD work)
+  double* RU = W + 2 * B * B;             // 1024
+  double* RV = RU + 1024;                 // 1024
+  double* sig = RV + 1024;                // 64
+  double* red = sig + 64;                 // 32
+  double* aux = red + 32;                 // 192
+  int* ord = reinterpret_cast<int*>(aux + 192);  // 64
+  int* perm = ord + 64;                   // 64
+  __shared__ int s_flag, s_k;
+  int xu, xv;
+  SideShape hu, hv;
+  site_of(a, job, 0, xu, hu);
+  site_of(a, job, 1, xv, hv);
+  const int ce = hu.chi[hu.p];
+  const int du = hu.d, dv = hv.d, ru = (int)su[kSideMeta], rv = (int)sv[kSideMeta];
+  for (int i = tid; i < ru * du * ce; i += kSuThreads) RU[i] = su[kSideR + i];
+  for (int i = tid; i < rv * dv * ce; i += kSuThreads) RV[i] = sv[kSideR + i];
+  __syncthreads();
   // theta[(ru, su), (sv, rv)] = sum_e Ru[ru, su + du e] Rv[rv, sv + dv e], then the gate
-  const int du = sh[0].d, dv = sh[1].d, ru = r[0], rv = r[1];
   const int mt = ru * du, nt = dv * rv;
   for (int i = tid; i < mt * nt; i += kSuThreads) {
     const int row = i % mt, col = i / mt;
-    const int iu = row % ru, su = row / ru, sv = col % dv, iv = col / dv;
+    const int iu = row % ru, su_ = row / ru, sv_ = col % dv, iv = col / dv;
     double acc = 0.0;
-    for (int e = 0; e < ce; ++e) acc += RU[iu + ru * (su + du * e)] * RV[iv + rv * (sv + dv * e)];
+    for (int e = 0; e < ce; ++e) acc = fma(RU[iu + ru * (su_ + du * e)], RV[iv + rv * (sv_ + dv * e)], acc);
     W[i] = acc;
   }
   __syncthreads();
@@ -634,9 +708,9 @@ __global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
     const int row = i % mt, col = i / mt;
     const int iu = row % ru, spu = row / ru, spv = col % dv, iv = col / dv;
     double acc = 0.0;
-    for (int sv = 0; sv < dv; ++sv)
-      for (int su = 0; su < du; ++su)
-        acc += G[(spu + du * spv) + D * (su + du * sv)] * W[(iu + ru * su) + mt * (sv + dv * iv)];
+    for (int sv_ = 0; sv_ < dv; ++sv_)
+      for (int su_ = 0; su_ < du; ++su_)
+        acc = fma(G[(spu + du * spv) + D * (su_ + du * sv_)], W[(iu + ru * su_) + mt * (sv_ + dv * iv)], acc);
     TH[i] = acc;
   }
   __syncthreads();
@@ -649,7 +723,7 @@ __global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
     for (int i = tid; i < mt * nt; i += kSuThreads) TH[i] = W[i];
     __syncthreads();
   }
-  sb.work = W;
+  SvdBufs sb{W, aux, aux + 64, aux + 128, perm, ord, &s_flag, red};
   cta_svd(TH, wide ? nt : mt, wide ? mt : nt, V, sig, sb);
   const double* UF = wide ? V : TH;  // left factor, mt x nsv (ld mt)
   const double* VF = wide ? TH : V;  // right factor, nt x nsv (ld nt)
@@ -675,43 +749,92 @@ __global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
     if (a.truncerr) a.truncerr[j] = te / scale;
     if (a.svals)
       for (int i = 0; i < a.maxdim; ++i) a.svals[(size_t)j * a.maxdim + i] = i < n ? sig[i] : 0.0;
+    out[kJobMeta] = (double)n;
+    out[kJobMeta + 1] = 1.0;
+    a.edim[job.e] = n;
   }
   __syncthreads();
   const int kk = s_k;
-  if (tid < kk) sig[tid] = sqrt(sig[tid]);  // sqrt(S), split onto both sites
+  for (int i = tid; i < mt * kk; i += kSuThreads) out[kJobU + i] = UF[i];
+  for (int i = tid; i < nt * kk; i += kSuThreads) out[kJobV + i] = VF[i];
+  if (tid < kk) out[kJobS + tid] = sqrt(sig[tid]);  // sqrt(S), split onto both sites
+}
+
+// Stage 3, one CTA per (gate, side): the new site = Q (U sqrt(S)) (or
+// Q (V sqrt(S)) on the right), Q applied as its reflectors, rearranged to
+// the tensor layout with the new bond dimension, inverse-sqrt environments
+// absorbed back, optionally normalised, written to the site's slot.
+__global__ void __launch_bounds__(kSuThreads, 3) su_rebuild_kernel(SuArgs a) {
+  extern __shared__ __align__(16) double smem[];
+  const int j = blockIdx.x >> 1, side = blockIdx.x & 1, tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  if (j >= a.njobs) return;
+  const double* js = a.job_scratch + (size_t)j * kJobStride;
+  if (js[kJobMeta + 1] == 0.0) return;  // the gate exceeded the limits (status already set)
+  const SuJob job = a.jobs[j];
+  const double* ss = a.side_scratch + (size_t)blockIdx.x * kSideStride;
+  double* Y = smem;                       // m x (d kk), then the tensor
+  double* T = Y + kSuMaxN;                // second buffer when environments are absorbed
+  double* small = T + (a.envs ? kSuMaxN : 0);
+  double* S = small;                      // 64
+  double* red = S + 64;                   // 32
+  __shared__ double s_scale;
+  const int kk = (int)js[kJobMeta];
+  // shape: the other legs as before (edim of this gate's bond already holds kk)
+  SideShape h;
+  const int x = side ? job.v : job.u;
+  side_shape(a, x, side ? job.pv : job.pu, h);
+  int chi2[kMaxDeg];
+  for (int q = 0; q < h.k; ++q) chi2[q] = h.chi[q];
+  chi2[h.p] = kk;
+  const int m = h.m, d = h.d, ncol2 = d * kk;
+  int n2 = d;
+  for (int q = 0; q < h.k; ++q) n2 *= chi2[q];
+  const int r = (int)ss[kSideMeta];
+  // X = U sqrt(S) (rows t, columns s + d b) in the top r rows of Y, zeros below
+  const int du = a.site_dim[job.u], dv = a.site_dim[job.v];
+  const int ru = (int)a.side_scratch[(size_t)(2 * j) * kSideStride + kSideMeta];
+  const int rv = (int)a.side_scratch[(size_t)(2 * j + 1) * kSideStride + kSideMeta];
+  const int mt = ru * du, nt = dv * rv;
+  for (int i = tid; i < m * ncol2; i += kSuThreads) {
+    const int row = i % m, col = i / m, s = col % d, b = col / d;
+    double v = 0.0;
+    if (row < r)
+      v = side == 0 ? js[kJobU + (row + ru * s) + (size_t)mt * b] * js[kJobS + b]
+                    : js[kJobV + (s + dv * row) + (size_t)nt * b] * js[kJobS + b];
+    Y[i] = v;
+  }
   __syncthreads();
-  // reassemble both sites with the new bond dimension kk
-  for (int side = 0; side < 2; ++side) {
-    SideShape h = sh[side];
-    const int x = xs[side];
-    int chi2[kMaxDeg];
-    for (int q = 0; q < h.k; ++q) chi2[q] = h.chi[q];
-    chi2[h.p] = kk;
-    int n2 = h.d;
-    for (int q = 0; q < h.k; ++q) n2 *= chi2[q];
-    const double* qs = a.qscratch + ((size_t)j * 2 + side) * kSuMaxN;
-    for (int i = tid; i < h.m * r[side]; i += kSuThreads) T[i] = qs[i];
+  // Y <- H_0 ... H_{r-1} Y, reflector j from row j on (beta_j = 0: skipped)
+  for (int jr = r - 1; jr >= 0; --jr) {
+    const double bj = ss[kSideBeta + jr];
+    if (bj == 0.0) continue;
+    const double* v = ss + kSideRefl + (size_t)jr * m;
+    for (int c = warp; c < ncol2; c += kSuWarps) {
+      double* y = Y + (size_t)c * m;
+      double w = 0.0;
+      for (int i = jr + lane; i < m; i += 32) w = fma(v[i], y[i], w);
+      w = warp_sum(w) * bj;
+      for (int i = jr + lane; i < m; i += 32) y[i] = fma(-w, v[i], y[i]);
+    }
     __syncthreads();
+  }
+  double* dst = a.tens + a.cap_off[x];
+  if (a.envs) {
+    // tensor layout into T, then the inverse-sqrt environments (T <-> Y)
     for (int i = tid; i < n2; i += kSuThreads) {
       int row, s, b;
       split_index(h, chi2, i, row, s, b);
-      const double sq = sig[b];
-      double acc = 0.0;
-      if (side == 0) {
-        for (int t = 0; t < ru; ++t) acc += T[row + (size_t)h.m * t] * UF[(t + ru * s) + (size_t)mt * b];
-      } else {
-        for (int t = 0; t < rv; ++t) acc += T[row + (size_t)h.m * t] * VF[(s + dv * t) + (size_t)nt * b];
-      }
-      W[i] = acc * sq;
+      T[i] = Y[row + (size_t)m * (s + d * b)];
     }
     __syncthreads();
-    double* cur = W;
-    double* nxt = T;
-    int st = h.d;
+    double* cur = T;
+    double* nxt = Y;
+    int st = d;
     for (int q = 0; q < h.k; ++q) {
-      if (q != h.p && a.envs) {
+      if (q != h.p) {
         const int c = chi2[q];
-        const double* si = SI + (side * kMaxDeg + q) * 64;
+        const double* si = ss + kSideSI + q * 64;
         for (int i = tid; i < c * c; i += kSuThreads) S[(i / c) + c * (i % c)] = si[i];  // transpose
         __syncthreads();
         absorb_any<double>(c, cur, nxt, n2, st, S, tid, kSuThreads);
@@ -722,21 +845,27 @@ __global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
       }
       st *= chi2[q];
     }
-    if (a.normalize) {
-      double s2 = 0.0;
-      for (int i = tid; i < n2; i += kSuThreads) s2 += cur[i] * cur[i];
-      s2 = block_sum(s2, red);
-      if (tid == 0) s_scale = s2 > 0.0 ? 1.0 / sqrt(s2) : 1.0;
-      __syncthreads();
-    } else if (tid == 0) {
-      s_scale = 1.0;
-    }
+    double s2 = 0.0;
+    if (a.normalize)
+      for (int i = tid; i < n2; i += kSuThreads) s2 = fma(cur[i], cur[i], s2);
+    s2 = block_sum(s2, red);
+    if (tid == 0) s_scale = (a.normalize && s2 > 0.0) ? 1.0 / sqrt(s2) : 1.0;
     __syncthreads();
-    double* dst = a.tens + a.cap_off[x];
     for (int i = tid; i < n2; i += kSuThreads) dst[i] = cur[i] * s_scale;
+  } else {
+    // the permutation to the tensor layout keeps the norm: normalise from Y
+    double s2 = 0.0;
+    if (a.normalize)
+      for (int i = tid; i < m * ncol2; i += kSuThreads) s2 = fma(Y[i], Y[i], s2);
+    s2 = block_sum(s2, red);
+    if (tid == 0) s_scale = (a.normalize && s2 > 0.0) ? 1.0 / sqrt(s2) : 1.0;
     __syncthreads();
+    for (int i = tid; i < n2; i += kSuThreads) {
+      int row, s, b;
+      split_index(h, chi2, i, row, s, b);
+      dst[i] = Y[row + (size_t)m * (s + d * b)] * s_scale;
+    }
   }
-  if (tid == 0) a.edim[job.e] = kk;
 }
 
 }  // namespace
@@ -744,21 +873,30 @@ __global__ void __launch_bounds__(kSuThreads, 1) su_gate_kernel(SuArgs a) {
 
 namespace gbtn {
 
-constexpr int kSuMaxNHost = kSuMaxN;
+constexpr size_t kSuSideStride = kSideStride;
+constexpr size_t kSuJobStride = kJobStride;
 
-size_t su_smem_bytes() {
-  return sizeof(double) * (2 * (size_t)kSuMaxN + 2 * (size_t)kSuMaxTheta * kSuMaxTheta + 2 * 1024 +
-                           2 * kMaxDeg * 64 + 64 * 3 + 32 + 192) +
-         sizeof(int) * 128;
+// Shared memory of the three stages.
+size_t su_qr_smem(bool envs) {
+  return sizeof(double) * ((envs ? 2 : 1) * (size_t)kSuMaxN + 1024 + 64 + 32 + 64 * 4 + 192) + sizeof(int) * 128;
 }
-
-void su_prepare(size_t smem) {
-  GBTN_CUDA(cudaFuncSetAttribute(su_gate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+size_t su_svd_smem(int B) {
+  return sizeof(double) * (4 * (size_t)B * B + 2048 + 64 + 32 + 192) + sizeof(int) * 128;
 }
+size_t su_rebuild_smem(bool envs) { return sizeof(double) * ((envs ? 2 : 1) * (size_t)kSuMaxN + 64 + 32); }
 
-void su_launch(const SuArgs& a, size_t smem, cudaStream_t s) {
+void su_launch(const SuArgs& a, cudaStream_t s) {
   if (a.njobs == 0) return;
-  su_gate_kernel<<<a.njobs, kSuThreads, smem, s>>>(a);
+  const bool envs = a.envs != nullptr;
+  const size_t s1 = su_qr_smem(envs), s2 = su_svd_smem(a.bmax), s3 = su_rebuild_smem(envs);
+  GBTN_CUDA(cudaFuncSetAttribute(su_qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1));
+  GBTN_CUDA(cudaFuncSetAttribute(su_svd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+  GBTN_CUDA(cudaFuncSetAttribute(su_rebuild_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s3));
+  su_qr_kernel<<<2 * a.njobs, kSuThreads, s1, s>>>(a);
+  GBTN_CUDA(cudaGetLastError());
+  su_svd_kernel<<<a.njobs, kSuThreads, s2, s>>>(a);
+  GBTN_CUDA(cudaGetLastError());
+  su_rebuild_kernel<<<2 * a.njobs, kSuThreads, s3, s>>>(a);
   GBTN_CUDA(cudaGetLastError());
 }
 
@@ -997,10 +1135,14 @@ int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const doubl
     }
     batches.push_back({start, n_gates});
     maxb = std::max(maxb, n_gates - start);
-    GBTN_CUDA(cudaMalloc(&d_q, sizeof(double) * (size_t)maxb * 2 * gbtn::kSuMaxNHost));
-    std::unique_ptr<double, decltype(&cudaFree)> q_guard(d_q, cudaFree);
-    const size_t smem = gbtn::su_smem_bytes();
-    gbtn::su_prepare(smem);
+    double* d_js = nullptr;
+    GBTN_CUDA(cudaMalloc(&d_q, sizeof(double) * (size_t)maxb * 2 * gbtn::kSuSideStride));
+    GBTN_CUDA(cudaMalloc(&d_js, sizeof(double) * (size_t)maxb * gbtn::kSuJobStride));
+    std::unique_ptr<double, decltype(&cudaFree)> q_guard(d_q, cudaFree), js_guard(d_js, cudaFree);
+    // theta is at most (d_u min(m_u, d_u chi)) x (d_v min(m_v, d_v chi)) <= dmax^2 chi_max
+    int dmax = 1;
+    for (int dd : S->dsite) dmax = std::max(dmax, dd);
+    const int bmax = std::min(64, dmax * dmax * S->chimax);
     GBTN_CUDA(cudaMemsetAsync(S->d_status, 0, sizeof(int), s));
     for (auto& b : batches) {
       SuArgs a{};
@@ -1020,11 +1162,13 @@ int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const doubl
       a.cutoff = cutoff;
       a.normalize = normalize;
       a.chimax = S->chimax;
-      a.qscratch = d_q;
+      a.side_scratch = d_q;
+      a.job_scratch = d_js;
+      a.bmax = bmax;
       a.truncerr = d_te + b.first;
       a.svals = d_sv + (size_t)b.first * md;
       a.status = S->d_status;
-      gbtn::su_launch(a, smem, s);
+      gbtn::su_launch(a, s);
     }
     int status = 0;
     GBTN_CUDA(cudaMemcpyAsync(&status, S->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
