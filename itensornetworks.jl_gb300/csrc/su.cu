@@ -43,7 +43,7 @@ constexpr int kSvdMaxSweeps = 40;
 // relative precision (a few ulps above the rounding of a 64-long FP64 dot)
 // or when either column is below 1e-15 of ||A||_F (rotating rounding noise
 // cannot change the decomposition beyond eps ||A||).
-constexpr double kJacobiTol = 4e-15;
+constexpr double kJacobiTol = 1e-13;
 constexpr double kJacobiTiny = 1e-30;
 
 // FP64 runs at a small fraction of the FP32 rate on this part, and a warp
@@ -70,7 +70,7 @@ __device__ __forceinline__ double block_sum(double x, double* red) {
 
 // Scratch of the SVD: work >= m*n + n*n doubles; cn, rdiag, bet, V-row
 // permutation perm and sort order ord >= n entries; flag and red as in
-// block_sum.
+// block_sum; extra >= 2*n*n doubles.
 struct SvdBufs {
   double* work;
   double* cn;
@@ -80,6 +80,7 @@ struct SvdBufs {
   int* ord;
   int* flag;
   double* red;
+  double* extra;  // >= 2 n^2 doubles: the FP64 re-orthogonalisation of the FP32 rotation
 };
 
 // Sum of x over the 8 lanes of a group (all 32 lanes must take part).
@@ -261,6 +262,87 @@ __device__ void cta_jacobi(double* X, int m, int n, int* flag, double* red) {
   }
 }
 
+// The FP32 stage of the Jacobi SVD: the same tournament on an FP32 copy of
+// the columns of X (m x n), rotations accumulated into V (n x n, set to the
+// identity here), until a sweep finds every pair orthogonal to 2e-6 (a few
+// FP32 roundings above the noise of a 64-long FP32 dot).  Costs the FP64
+// pipe nothing; the FP64 stage then starts from nearly orthogonal columns.
+__device__ void cta_jacobi32(float* X, int m, int n, float* V, int* flag, double* red) {
+  const int tid = threadIdx.x, grp = tid >> 3, gl = tid & 7;
+  for (int i = tid; i < n * n; i += kSuThreads) V[i] = (i % n == i / n) ? 1.f : 0.f;
+  double f = 0.0;
+  for (int i = tid; i < m * n; i += kSuThreads) f += (double)X[i] * (double)X[i];
+  f = block_sum(f, red);
+  const float tiny = (float)(f * kJacobiTiny), tol2 = 4e-12f;
+  const int N = n + (n & 1);
+  const int npair = N / 2;
+  const bool warp_busy = (tid >> 5) * 4 < npair;
+  for (int sweep = 0; sweep < 16; ++sweep) {
+    if (tid == 0) *flag = 0;
+    __syncthreads();
+    for (int r = 0; r < N - 1; ++r) {
+      if (warp_busy) {
+        int p = 0, q = 0;
+        bool act = grp < npair;
+        if (act) {
+          if (grp == 0) {
+            p = N - 1;
+            q = r;
+          } else {
+            p = (r + grp) % (N - 1);
+            q = (r - grp + N - 1) % (N - 1);
+          }
+          if (p > q) {
+            const int t = p;
+            p = q;
+            q = t;
+          }
+          act = q < n;
+        }
+        float* a = X + (size_t)p * m;
+        float* b = X + (size_t)q * m;
+        float al = 0.f, be = 0.f, ga = 0.f;
+        if (act)
+          for (int i = gl; i < m; i += 8) {
+            const float x = a[i], y = b[i];
+            al = fmaf(x, x, al);
+            be = fmaf(y, y, be);
+            ga = fmaf(x, y, ga);
+          }
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+          al += __shfl_xor_sync(0xffffffffu, al, o);
+          be += __shfl_xor_sync(0xffffffffu, be, o);
+          ga += __shfl_xor_sync(0xffffffffu, ga, o);
+        }
+        const bool rot = act && al > tiny && be > tiny && ga * ga > tol2 * al * be;
+        if (rot) {
+          const float inv = 1.0f / fmaxf(al, be);
+          const float d = (be - al) * inv, g = ga * inv;
+          const float t = (d >= 0.f ? 2.f : -2.f) * g / (fabsf(d) + sqrtf(fmaf(d, d, 4.f * g * g)));
+          const float c = rsqrtf(fmaf(t, t, 1.f)), sn = c * t;
+          for (int i = gl; i < m; i += 8) {
+            const float x = a[i], y = b[i];
+            a[i] = fmaf(c, x, -sn * y);
+            b[i] = fmaf(sn, x, c * y);
+          }
+          float* va = V + (size_t)p * n;
+          float* vb = V + (size_t)q * n;
+          for (int i = gl; i < n; i += 8) {
+            const float x = va[i], y = vb[i];
+            va[i] = fmaf(c, x, -sn * y);
+            vb[i] = fmaf(sn, x, c * y);
+          }
+          if (gl == 0) *flag = 1;
+        }
+      }
+      __syncthreads();
+    }
+    if (*flag == 0) break;
+    __syncthreads();
+  }
+}
+
 // SVD of A (m x n, m >= n, lda = m, n <= 64, m <= 64) by one-sided Jacobi
 // preconditioned with a pivoted QR (Drmac and Veselic, SIAM J. Matrix Anal.
 // Appl. 29 (2008)): A P = Q R and Jacobi on the columns of X = R^T give
@@ -283,6 +365,44 @@ __device__ void cta_svd(double* A, int m, int n, double* V, double* sig, SvdBufs
     X[i] = r < c ? A[(size_t)c * m + r] : (r == c ? b.rdiag[r] : 0.0);
   }
   __syncthreads();
+  // FP32 stage on a copy (A's reflectors are no longer needed: X32 and V32
+  // live there), then X <- X Q with Q = V32 (I - E / 2), E = V32^T V32 - I,
+  // orthonormal to O(|E|^2) = O(1e-14), formed in FP64
+  {
+    float* X32 = reinterpret_cast<float*>(A);
+    float* V32 = X32 + n * n;
+    for (int i = tid; i < n * n; i += kSuThreads) X32[i] = (float)X[i];
+    __syncthreads();
+    cta_jacobi32(X32, n, n, V32, b.flag, b.red);
+    double* E = b.extra;
+    double* Q = b.extra + (size_t)n * n;
+    for (int i = tid; i < n * n; i += kSuThreads) V[i] = (double)V32[i];
+    __syncthreads();
+    for (int i = tid; i < n * n; i += kSuThreads) {
+      const int a = i % n, c = i / n;
+      double acc = a == c ? -1.0 : 0.0;
+      for (int k = 0; k < n; ++k) acc = fma(V[k + n * a], V[k + n * c], acc);
+      E[i] = acc;
+    }
+    __syncthreads();
+    for (int i = tid; i < n * n; i += kSuThreads) {
+      const int r = i % n, c = i / n;
+      double acc = 0.0;
+      for (int k = 0; k < n; ++k) acc = fma(V[r + n * k], E[k + n * c], acc);
+      Q[i] = fma(-0.5, acc, V[i]);
+    }
+    __syncthreads();
+    double* XQ = A;
+    for (int i = tid; i < n * n; i += kSuThreads) {
+      const int r = i % n, c = i / n;
+      double acc = 0.0;
+      for (int k = 0; k < n; ++k) acc = fma(X[r + n * k], Q[k + n * c], acc);
+      XQ[i] = acc;
+    }
+    __syncthreads();
+    for (int i = tid; i < n * n; i += kSuThreads) X[i] = XQ[i];
+    __syncthreads();
+  }
   cta_jacobi(X, n, n, b.flag, b.red);
   // sigma = column norms of X, U_x = unit columns (a group per column)
   for (int j0 = 0; j0 < n; j0 += 32) {
@@ -607,7 +727,7 @@ __global__ void __launch_bounds__(kSuThreads, 3) su_qr_kernel(SuArgs a) {
   const double* src = a.tens + a.cap_off[x];
   const int ce = h.chi[h.p], ncol = h.d * ce;
   if (a.envs) {
-    SvdBufs sb{W, aux, aux + 64, aux + 128, perm, ord, &s_flag, red};
+    SvdBufs sb{W, aux, aux + 64, aux + 128, perm, ord, &s_flag, red, nullptr};
     for (int i = tid; i < h.n; i += kSuThreads) T[i] = src[i];
     __syncthreads();
     double* cur = T;
@@ -618,7 +738,8 @@ __global__ void __launch_bounds__(kSuThreads, 3) su_qr_kernel(SuArgs a) {
         const int f = a.leg_edge[a.leg_ptr[x] + q];
         const int de_in = a.edge_u[f] == x ? 2 * f + 1 : 2 * f;
         const double* env = a.envs + (size_t)de_in * a.chimax * a.chimax;
-        sb.work = nxt;
+        sb.work = nxt;                   // free here: m n + n^2 <= 128 doubles used
+        sb.extra = nxt + kSuMaxN / 2;    // 2 n^2 <= 128 doubles
         cta_env_sqrt(env, h.chi[q], S, out + kSideSI + q * 64, A8, V8, sig, sb);
         absorb_any<double>(h.chi[q], cur, nxt, h.n, st, S, tid, kSuThreads);
         __syncthreads();
@@ -677,7 +798,8 @@ __global__ void __launch_bounds__(kSuThreads, 2) su_svd_kernel(SuArgs a) {
   double* W = V + B * B;                  // 2 B x B (theta build, SVD work)
   double* RU = W + 2 * B * B;             // 1024
   double* RV = RU + 1024;                 // 1024
-  double* sig = RV + 1024;                // 64
+  double* XT = RV + 1024;                 // 2 B x B: FP64 re-orthogonalisation in the SVD
+  double* sig = XT + 2 * B * B;           // 64
   double* red = sig + 64;                 // 32
   double* aux = red + 32;                 // 192
   int* ord = reinterpret_cast<int*>(aux + 192);  // 64
@@ -723,7 +845,7 @@ __global__ void __launch_bounds__(kSuThreads, 2) su_svd_kernel(SuArgs a) {
     for (int i = tid; i < mt * nt; i += kSuThreads) TH[i] = W[i];
     __syncthreads();
   }
-  SvdBufs sb{W, aux, aux + 64, aux + 128, perm, ord, &s_flag, red};
+  SvdBufs sb{W, aux, aux + 64, aux + 128, perm, ord, &s_flag, red, XT};
   cta_svd(TH, wide ? nt : mt, wide ? mt : nt, V, sig, sb);
   const double* UF = wide ? V : TH;  // left factor, mt x nsv (ld mt)
   const double* VF = wide ? TH : V;  // right factor, nt x nsv (ld nt)
@@ -881,7 +1003,7 @@ size_t su_qr_smem(bool envs) {
   return sizeof(double) * ((envs ? 2 : 1) * (size_t)kSuMaxN + 1024 + 64 + 32 + 64 * 4 + 192) + sizeof(int) * 128;
 }
 size_t su_svd_smem(int B) {
-  return sizeof(double) * (4 * (size_t)B * B + 2048 + 64 + 32 + 192) + sizeof(int) * 128;
+  return sizeof(double) * (6 * (size_t)B * B + 2048 + 64 + 32 + 192) + sizeof(int) * 128;
 }
 size_t su_rebuild_smem(bool envs) { return sizeof(double) * ((envs ? 2 : 1) * (size_t)kSuMaxN + 64 + 32); }
 
