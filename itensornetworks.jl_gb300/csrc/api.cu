@@ -95,7 +95,9 @@ struct gbtn_plan {
   DevBuf<float> d_msg32[2];
   int cur = 0;  // buffer holding the current messages
   DevBuf<double> d_diffs, d_mean, d_rdm, d_edge_sc, d_re, d_im, d_scale, d_out;
-  DevBuf<int> d_conv, d_iters, d_since;
+  DevBuf<int> d_conv, d_iters, d_since, d_nconv;
+  int* h_nconv = nullptr;  // pinned [2]: converged-network counts read while sweeping
+  cudaEvent_t poll_ev[2] = {nullptr, nullptr};
   DevBuf<double> d_best;
   DevBuf<int> d_net_de_ptr, d_net_de, d_net_v_ptr, d_net_v, d_net_e_ptr, d_net_e;
   // work lists: index 0 = all vertices, 1.. = colour classes; two size classes each
@@ -131,7 +133,12 @@ struct gbtn_plan {
     }
     graph_cache.clear();
   }
-  ~gbtn_plan() { clear_graphs(); }
+  ~gbtn_plan() {
+    clear_graphs();
+    if (h_nconv) cudaFreeHost(h_nconv);
+    for (cudaEvent_t e : poll_ev)
+      if (e) cudaEventDestroy(e);
+  }
   // sequential schedule storage
   DevBuf<int2> d_seq;
   DevBuf<int> d_seq_ptr;
@@ -266,16 +273,39 @@ size_t smem_need(int n, int k, bool sep_bra, size_t elt, int team) {
 
 using GraphKey = std::tuple<int, int, int, int, int, int, int, double>;
 
+// Convergence polling while sweeping.  Each poll queues a 4-byte copy of the
+// converged-network count (kept on the device by reduce_diffs) into pinned
+// memory and records an event, then waits for the PREVIOUS poll's event and
+// reads its count -- so the GPU always has the sweeps since the last poll
+// queued while the host waits, and the loop overshoots convergence by at most
+// two poll periods.
+struct ConvPoll {
+  gbtn_plan* P;
+  int n = 0;
+  explicit ConvPoll(gbtn_plan* p) : P(p) {}
+  bool done() {
+    const int slot = n & 1;
+    GBTN_CUDA(cudaMemcpyAsync(P->h_nconv + slot, P->d_nconv.p, sizeof(int), cudaMemcpyDeviceToHost, P->ctx->stream));
+    GBTN_CUDA(cudaEventRecord(P->poll_ev[slot], P->ctx->stream));
+    if (++n < 2) return false;
+    GBTN_CUDA(cudaEventSynchronize(P->poll_ev[slot ^ 1]));
+    return P->h_nconv[slot ^ 1] >= P->nnet;
+  }
+};
+
 // maxiter sweeps of `sweep`.  With graphs on (and no per-launch profiling),
 // the first sweep runs as plain launches and the rest are replays of one CUDA
 // graph holding two sweeps -- after two sweeps the double-buffer parity is
 // back where it started, so the same graph serves every pair.  The graph is
 // kept in the plan under `key` (launch parameters, buffer parity, list
-// version) and reused by later calls.
+// version) and reused by later calls.  With `poll`, the converged-network
+// count is polled every two sweeps and the loop ends once every network has
+// converged (the remaining sweeps would only carry the messages forward).
 template <class F>
-void sweep_loop(gbtn_plan* P, int maxiter, const GraphKey& key, F&& sweep) {
+void sweep_loop(gbtn_plan* P, int maxiter, const GraphKey& key, F&& sweep, bool poll = false) {
   cudaStream_t s = P->ctx->stream;
   int it = 0;
+  ConvPoll cp(P);
   if (P->graphs && !P->ctx->profiling && maxiter >= 3) {
     sweep();
     ++it;
@@ -300,9 +330,15 @@ void sweep_loop(gbtn_plan* P, int maxiter, const GraphKey& key, F&& sweep) {
       }
       found = P->graph_cache.emplace(key, std::make_pair(g, ge)).first;
     }
-    for (; it + 2 <= maxiter; it += 2) GBTN_CUDA(cudaGraphLaunch(found->second.second, s));
+    for (; it + 2 <= maxiter; it += 2) {
+      GBTN_CUDA(cudaGraphLaunch(found->second.second, s));
+      if (poll && it + 2 < maxiter && cp.done()) return;
+    }
   }
-  for (; it < maxiter; ++it) sweep();
+  for (; it < maxiter; ++it) {
+    sweep();
+    if (poll && (it & 1) && it + 1 < maxiter && cp.done()) return;
+  }
 }
 
 // Sweeps of the parallel or coloured schedule in precision T.
@@ -313,6 +349,7 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
   const bool want_diff = tol >= 0.0;
   GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int) * P->nnet, s));
   GBTN_CUDA(cudaMemsetAsync(P->d_iters.p, 0, sizeof(int) * P->nnet, s));
+  GBTN_CUDA(cudaMemsetAsync(P->d_nconv.p, 0, sizeof(int), s));
   const int* conv = want_diff ? P->d_conv.p : nullptr;
   T* msg[2] = {msg0, msg1};
   const GraphKey key{sizeof(T) == 4 ? 1 : (sizeof(T) == 16 ? 3 : 0), schedule, normalize, want_diff ? 1 : 0, stall, cur, P->list_version, tol};
@@ -342,8 +379,8 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
     }
     if (want_diff)
       launch_reduce_diffs(P->nnet, P->d_net_de_ptr.p, P->d_net_de.p, P->d_diffs.p, tol, P->d_conv.p, P->d_iters.p,
-                          P->d_mean.p, s, stall, P->d_best.p, P->d_since.p);
-  });
+                          P->d_mean.p, s, stall, P->d_best.p, P->d_since.p, P->d_nconv.p);
+  }, want_diff);
 }
 
 // Raise the device-side error word (set by a bounded wait that gave up).
@@ -521,6 +558,7 @@ void run_sweeps_bf16(gbtn_plan* P, int schedule, int maxiter, double tol, int no
   const bool want_diff = tol >= 0.0;
   GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int) * P->nnet, s));
   GBTN_CUDA(cudaMemsetAsync(P->d_iters.p, 0, sizeof(int) * P->nnet, s));
+  GBTN_CUDA(cudaMemsetAsync(P->d_nconv.p, 0, sizeof(int), s));
   const int* conv = want_diff ? P->d_conv.p : nullptr;
   const float* fac = P->d_fac32.p;
   auto one = [&](size_t li, const float* in, float* out) {
@@ -551,8 +589,8 @@ void run_sweeps_bf16(gbtn_plan* P, int schedule, int maxiter, double tol, int no
     }
     if (want_diff)
       launch_reduce_diffs(P->nnet, P->d_net_de_ptr.p, P->d_net_de.p, P->d_diffs.p, tol, P->d_conv.p, P->d_iters.p,
-                          P->d_mean.p, s, stall, P->d_best.p, P->d_since.p);
-  });
+                          P->d_mean.p, s, stall, P->d_best.p, P->d_since.p, P->d_nconv.p);
+  }, want_diff);
 }
 
 void finish_iters(gbtn_plan* P, bool want_diff, int maxiter, int32_t* iters, double* mean_diff) {
@@ -860,6 +898,9 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   P->d_diffs.alloc(std::max<long long>(2LL * P->ne, 1));
   P->d_mean.alloc(P->nnet);
   P->d_conv.alloc(P->nnet);
+  P->d_nconv.alloc(1);
+  GBTN_CUDA(cudaMallocHost(&P->h_nconv, 2 * sizeof(int)));
+  for (cudaEvent_t& e : P->poll_ev) GBTN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   P->d_iters.alloc(P->nnet);
   P->d_since.alloc(P->nnet);
   P->d_best.alloc(P->nnet);

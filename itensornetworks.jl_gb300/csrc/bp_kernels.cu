@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(256)
 // floor of a reduced-precision phase.
 __global__ void reduce_diffs_kernel(const int* __restrict__ net_de_ptr, const int* __restrict__ net_de,
                                     const double* __restrict__ diffs, double tol, int* converged, int* iters,
-                                    double* mean_diff, int stall, double* best, int* since) {
+                                    double* mean_diff, int stall, double* best, int* since, int* n_conv) {
   const int net = blockIdx.x;
   if (converged[net]) return;
   const int b = net_de_ptr[net], e = net_de_ptr[net + 1];
@@ -311,14 +311,18 @@ __global__ void reduce_diffs_kernel(const int* __restrict__ net_de_ptr, const in
       const double mean = t / (double)(e - b);
       iters[net] += 1;
       mean_diff[net] = tol >= 0.0 ? mean : NAN;
-      if (tol >= 0.0 && mean <= tol) converged[net] = 1;
+      int done = tol >= 0.0 && mean <= tol;
       if (stall > 0) {
         if (iters[net] == 1 || mean < 0.9 * best[net]) {
           best[net] = mean;
           since[net] = 0;
         } else if (++since[net] >= stall) {
-          converged[net] = 1;
+          done = 1;
         }
+      }
+      if (done) {
+        converged[net] = 1;
+        if (n_conv) atomicAdd(n_conv, 1);  // the host stops the sweeps once every network is done
       }
     }
   }
@@ -629,9 +633,9 @@ template void launch_bp_sequential<zdouble>(int, const VDesc*, const int2*, cons
 
 void launch_reduce_diffs(int n_networks, const int* net_de_ptr, const int* net_de, const double* diffs, double tol,
                          int* converged, int* iters, double* mean_diff, cudaStream_t s, int stall, double* best,
-                         int* since) {
+                         int* since, int* n_conv) {
   reduce_diffs_kernel<<<n_networks, 256, 0, s>>>(net_de_ptr, net_de, diffs, tol, converged, iters, mean_diff, stall,
-                                                 best, since);
+                                                 best, since, n_conv);
   GBTN_CUDA(cudaGetLastError());
 }
 

@@ -102,7 +102,8 @@ void launch_bp_sequential(int n_networks, const VDesc* vd, const int2* seq, cons
 
 void launch_reduce_diffs(int n_networks, const int* net_de_ptr, const int* net_de, const double* diffs,
                          double tol, int* converged, int* iters, double* mean_diff, cudaStream_t s,
-                         int stall = 0, double* best = nullptr, int* since = nullptr);
+                         int stall = 0, double* best = nullptr, int* since = nullptr,
+                         int* n_conv = nullptr);
 
 void launch_updated_message(const VDesc* vd, int v, int leg, const double* fac, const double* bra,
                             const double* msgs, const long long* msg_off, double* out, int ncap,
