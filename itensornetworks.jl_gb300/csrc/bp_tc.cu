@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     tc::tmem_relinquish();
   }
   if (t == 0) {
-    tc::mbar_init(mma_bar, 1);
+    tc::mbar_init(mma_bar, 2);  // one commit from each MMA issuer
     tc::mbar_init(tma_bar, 1);
     tc::fence_mbar_init();
     *abort_flag = 0;
@@ -424,17 +424,25 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     // ---- GEMM1 -> columns [0,64), GEMM1' -> [64,128) (M = 128) ----
     // descriptors: per-CTA bases (dZk, dZmn, dKT, dT34) plus the operand's
     // byte offset in 16-byte units (the start-address field of the descriptor)
-    if (t == 0) {
+    // Two issuers: thread 0 the GEMM1 chain, thread 32 the GEMM1' chain (separate
+    // accumulators).  A thread waits ~70 cycles per small MMA it issues; two
+    // issuers overlap in the tensor pipe.
+    if (t == 0 || t == 32) {
       tc::tc_fence_after();
       uint64_t dZk, dZmn, dKT, dT34;
       descs(dZk, dZmn, dKT, dT34);
+      if (t == 0) {
 #pragma unroll
-      for (int kk = 0; kk < 4; ++kk)
-        tc::mma_bf16(tmem + 0, dZk + ((32 * kk) >> 4), dKT + ((32 * kk) >> 4), kIdescG1, kk > 0);
+        for (int kk = 0; kk < 4; ++kk)
+          tc::mma_bf16(tmem + 0, dZk + ((32 * kk) >> 4), dKT + ((32 * kk) >> 4), kIdescG1, kk > 0);
+      } else {
 #pragma unroll
-      for (int kk = 0; kk < 4; ++kk)
-        tc::mma_bf16(tmem + 64, dZmn + ((2048 * kk) >> 4), dKT + ((8192 + 32 * kk) >> 4), kIdescG1mn, kk > 0);
+        for (int kk = 0; kk < 4; ++kk)
+          tc::mma_bf16(tmem + 64, dZmn + ((2048 * kk) >> 4), dKT + ((8192 + 32 * kk) >> 4), kIdescG1mn, kk > 0);
+      }
       tc::mma_commit(mma_bar);
+    }
+    if (t == 0) {
       mma_pending = 1;
       *abort_flag = wait_mma() ? 0 : 1;
     }
@@ -460,23 +468,26 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     tc::tc_fence_before();
     __syncthreads();
     // ---- GEMM2 -> G34 in columns [0,64), GEMM2' -> G12 in [64,128) (M = 64, K = 128) ----
-    if (t == 0) {
+    if (t == 0 || t == 32) {
       tc::tc_fence_after();
       uint64_t dZk, dZmn, dKT, dT34;
       descs(dZk, dZmn, dKT, dT34);
+      if (t == 0) {
 #pragma unroll
-      for (int kk = 0; kk < 8; ++kk) {
-        const uint32_t o = (8192 * (kk >> 2) + 32 * (kk & 3)) >> 4;
-        tc::mma_bf16(tmem + 0, dKT + o, dZk + o, kIdescG2, kk > 0);
-      }
+        for (int kk = 0; kk < 8; ++kk) {
+          const uint32_t o = (8192 * (kk >> 2) + 32 * (kk & 3)) >> 4;
+          tc::mma_bf16(tmem + 0, dKT + o, dZk + o, kIdescG2, kk > 0);
+        }
+      } else {
 #pragma unroll
-      for (int kk = 0; kk < 8; ++kk) {
-        const uint32_t o = (8192 * (kk >> 2) + 32 * (kk & 3)) >> 4;
-        tc::mma_bf16(tmem + 64, dT34 + o, dZmn + ((2048 * kk) >> 4), kIdescG2mn, kk > 0);
+        for (int kk = 0; kk < 8; ++kk) {
+          const uint32_t o = (8192 * (kk >> 2) + 32 * (kk & 3)) >> 4;
+          tc::mma_bf16(tmem + 64, dT34 + o, dZmn + ((2048 * kk) >> 4), kIdescG2mn, kk > 0);
+        }
       }
       tc::mma_commit(mma_bar);
-      mma_pending = 1;
     }
+    if (t == 0) mma_pending = 1;
     // the next vertex's incoming messages, ahead of use
     if (nsl >= 0) {
       nm0 = padded_msg(msg_in, nin0, nchi0, e);

@@ -33,6 +33,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
+// One arrival (release at CTA scope) on a barrier initialised with a thread count.
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -63,6 +68,19 @@ __device__ __forceinline__ void tma_load_1d(void* dst_smem, const void* src_gmem
       "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
+
+// ---- 4-byte asynchronous copies (global -> shared) ------------------------------
+// Unlike a load into a register, an outstanding cp.async does not hold up a
+// later bar.sync of the issuing thread.
+__device__ __forceinline__ void cp_async4(void* dst_smem, const void* src_gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst_smem)), "l"(src_gmem) : "memory");
+}
+// Arrive on the barrier once this thread's earlier cp.async copies have landed
+// (counts toward the barrier's expected arrivals).
+__device__ __forceinline__ void cp_async_arrive_noinc(uint64_t* bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // Make generic-proxy shared-memory writes visible to the async proxy (MMA reads).
 __device__ __forceinline__ void fence_proxy_async_smem() {
