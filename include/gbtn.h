@@ -173,6 +173,12 @@ int gbtn_get_factors(gbtn_plan* plan, double* ket, int mem);
 /* Replaces: set_messages! / messages (abstractbeliefpropagationcache.jl:173-191). */
 int gbtn_set_messages(gbtn_plan* plan, const double* msgs, int mem);
 int gbtn_get_messages(gbtn_plan* plan, double* msgs, int mem);
+/* message_diff (abstractbeliefpropagationcache.jl:32-36) of every directed
+   edge from the last sweep that ran with a tolerance (tol >= 0): 2*ne doubles
+   in directed-edge order (NaN before the first such sweep).  A caller that
+   splits one network across processes sums the diffs of the edges it owns
+   (the reference's update loop sums them over the whole sweep, :313-329). */
+int gbtn_get_edge_diffs(gbtn_plan* plan, double* diffs, int mem);
 /* Replaces: identity_messages (src/formnetworks/quadraticformnetwork.jl:96-124);
  * GBTN_INIT_ONES gives all-ones messages of unit Frobenius norm. */
 int gbtn_init_messages(gbtn_plan* plan, int kind);

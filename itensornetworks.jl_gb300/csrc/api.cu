@@ -896,6 +896,8 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   P->d_msg[0].alloc(es * std::max<long long>(P->n_msg, 1));
   P->d_msg[1].alloc(es * std::max<long long>(P->n_msg, 1));
   P->d_diffs.alloc(std::max<long long>(2LL * P->ne, 1));
+  GBTN_CUDA(cudaMemsetAsync(P->d_diffs.p, 0xff, sizeof(double) * std::max<long long>(2LL * P->ne, 1),
+                            P->ctx->stream));  // NaN until a sweep with a tolerance runs
   P->d_mean.alloc(P->nnet);
   P->d_conv.alloc(P->nnet);
   P->d_nconv.alloc(1);
@@ -1023,6 +1025,14 @@ int gbtn_get_messages(gbtn_plan* P, double* m, int mem) {
   API_TRY
   require(P && m, "NULL argument");
   copy_out(P, m, P->d_msg[P->cur].p, sizeof(double) * P->es() * P->n_msg, mem);
+  API_CATCH(C)
+}
+
+int gbtn_get_edge_diffs(gbtn_plan* P, double* d, int mem) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && d, "NULL argument");
+  copy_out(P, d, P->d_diffs.p, sizeof(double) * 2 * (size_t)P->ne, mem);
   API_CATCH(C)
 }
 

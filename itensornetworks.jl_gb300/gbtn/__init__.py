@@ -7,6 +7,7 @@ from ._lib import Context, GBTNError, InvalidArgument, LibraryNotBuilt, Unsuppor
 from .cache import (BeliefPropagationCache, environment, expect, initialize_cache, inner, loginner, logscalar,
                     message_diff, norm, norm_sqr, normalize, rescale, scalar, update, updated_message)
 from .partition import CoarseGraining, PartitionedBPCache, partitioned_cache
+from .sharded import GpuShard, ShardPlan, block_owner, run_distributed, run_local
 from .su import SimpleUpdateState, apply, bp_environments, checkerboard_edges, tebd, tfim_gate
 from .network import (TensorNetwork, default_edge_sequence, disjoint_union, parallel_edge_sequence,
                       random_network, random_tensors, square_lattice)
@@ -17,5 +18,6 @@ __all__ = [
     "initialize_cache", "inner", "loginner", "logscalar", "message_diff", "norm", "norm_sqr", "normalize",
     "parallel_edge_sequence", "random_network", "random_tensors", "rescale", "scalar", "square_lattice", "update",
     "updated_message", "SimpleUpdateState", "apply", "checkerboard_edges", "tebd", "tfim_gate", "bp_environments",
-    "CoarseGraining", "PartitionedBPCache", "partitioned_cache",
+    "CoarseGraining", "PartitionedBPCache", "partitioned_cache", "GpuShard", "ShardPlan", "block_owner",
+    "run_distributed", "run_local",
 ]

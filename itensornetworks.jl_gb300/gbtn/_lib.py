@@ -119,6 +119,7 @@ SIGNATURES = {
     "gbtn_get_factors": (_I, [_P, _P, _I]),
     "gbtn_set_messages": (_I, [_P, _P, _I]),
     "gbtn_get_messages": (_I, [_P, _P, _I]),
+    "gbtn_get_edge_diffs": (_I, [_P, _P, _I]),
     "gbtn_init_messages": (_I, [_P, _I]),
     "gbtn_bp_run": (_I, [_P, C.POINTER(BPOpts), _I32, _D]),
     "gbtn_updated_message": (_I, [_P, C.c_int32, _D]),

@@ -77,6 +77,20 @@ class BeliefPropagationCache:
         self._c(self.lib.gbtn_get_messages(self.handle, out.ctypes.data, _lib.HOST))
         return self.tn.unflat_messages(out)
 
+    def flat_messages(self):
+        """Every message in the ABI layout: directed edges in order, each
+        chi x chi column-major."""
+        out = np.empty(max(self.n_message, 1), dtype=self.dtype)
+        self._c(self.lib.gbtn_get_messages(self.handle, out.ctypes.data, _lib.HOST))
+        return out[:self.n_message]
+
+    def edge_diffs(self):
+        """message_diff of every directed edge from the last sweep run with a
+        tolerance (NaN before the first)."""
+        out = np.empty(max(2 * self.tn.ne, 1))
+        self._c(self.lib.gbtn_get_edge_diffs(self.handle, out.ctypes.data, _lib.HOST))
+        return out[:2 * self.tn.ne]
+
     def message(self, de):
         return self.messages()[de]
 
