@@ -72,6 +72,8 @@ struct HostWork {
 
 }  // namespace
 
+constexpr int kUploadChunks = 8;  // pieces of a host factor upload that overlap the image builds
+
 struct gbtn_plan {
   gbtn_ctx* ctx = nullptr;
   int nv = 0, ne = 0, nnet = 1;
@@ -133,11 +135,18 @@ struct gbtn_plan {
     }
     graph_cache.clear();
   }
+  // overlapped factor upload: copy and image-build streams, one event per chunk
+  cudaStream_t up_copy = nullptr, up_build = nullptr;
+  cudaEvent_t up_ev[kUploadChunks + 1] = {};
   ~gbtn_plan() {
     clear_graphs();
     if (h_nconv) cudaFreeHost(h_nconv);
     for (cudaEvent_t e : poll_ev)
       if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : up_ev)
+      if (e) cudaEventDestroy(e);
+    if (up_copy) cudaStreamDestroy(up_copy);
+    if (up_build) cudaStreamDestroy(up_build);
   }
   // sequential schedule storage
   DevBuf<int2> d_seq;
@@ -249,14 +258,20 @@ void copy_in(gbtn_plan* P, void* dst, const void* src, size_t bytes, int mem) {
   if (mem == GBTN_HOST) GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));
 }
 
-void ensure_f32(gbtn_plan* P) {
-  cudaStream_t s = P->ctx->stream;
+// FP32 message buffers (and room for FP32 factors).
+void ensure_f32_bufs(gbtn_plan* P) {
   if (!P->d_fac32.p) {
     P->d_fac32.alloc(P->n_fac);
     if (P->sep_bra) P->d_bra32.alloc(P->n_fac);
     P->d_msg32[0].alloc(P->n_msg);
     P->d_msg32[1].alloc(P->n_msg);
   }
+}
+
+// FP32 buffers and the FP32 copy of the factors (the FP32 SIMT kernel's input).
+void ensure_f32(gbtn_plan* P) {
+  cudaStream_t s = P->ctx->stream;
+  ensure_f32_bufs(P);
   if (!P->fac32_valid) {
     launch_convert_f64_to_f32(P->d_fac.p, P->d_fac32.p, P->n_fac, s);
     if (P->sep_bra) launch_convert_f64_to_f32(P->d_bra.p, P->d_bra32.p, P->n_fac, s);
@@ -500,6 +515,7 @@ void tune_tc_split(gbtn_plan* P) {
   } else if (P->tc_policy == GBTN_TC_NATIVE) {
     for (int v = 0; v < nv; ++v) use[v] = P->tc_cand[v] && tc_native(P->vd[v]);
   } else if (P->tc_policy == GBTN_TC_AUTO) {
+    ensure_f32(P);  // the timed SIMT launches read the FP32 factors
     std::vector<int> cv;
     for (int v = 0; v < nv; ++v)
       if (P->tc_cand[v]) cv.push_back(v);
@@ -549,6 +565,13 @@ void tune_tc_split(gbtn_plan* P) {
   }
   build_tc_lists(P, use);
   P->tc_tuned = true;
+}
+
+// Does the BF16 sweep run any vertex on the FP32 SIMT kernel?
+bool bf16_has_simt(const gbtn_plan* P) {
+  for (const auto& l : P->rest_lists)
+    if (l.first.count > 0 || l.second.count > 0) return true;
+  return false;
 }
 
 // BF16 sweeps (parallel or coloured): tensor-core kernel on the eligible
@@ -992,15 +1015,59 @@ int gbtn_plan_sizes(const gbtn_plan* P, int64_t* n_factor, int64_t* n_message) {
   return GBTN_OK;
 }
 
+// Host -> device factor upload in kUploadChunks vertex ranges on a copy
+// stream; the BF16 images of each range's tensor-core slots are built on a
+// second stream as soon as the range has landed, so the builds hide under the
+// copy (which the host link bounds).  Slots follow vertex order, so a vertex
+// range owns a contiguous slot range.  Ends synchronised, like every HOST copy.
+void upload_with_images(gbtn_plan* P, const double* ket) {
+  cudaStream_t s = P->ctx->stream;
+  if (!P->up_copy) {
+    GBTN_CUDA(cudaStreamCreateWithFlags(&P->up_copy, cudaStreamNonBlocking));
+    GBTN_CUDA(cudaStreamCreateWithFlags(&P->up_build, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : P->up_ev) GBTN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  // both side streams start after the work already queued on the plan's stream
+  GBTN_CUDA(cudaEventRecord(P->up_ev[kUploadChunks], s));
+  GBTN_CUDA(cudaStreamWaitEvent(P->up_copy, P->up_ev[kUploadChunks], 0));
+  GBTN_CUDA(cudaStreamWaitEvent(P->up_build, P->up_ev[kUploadChunks], 0));
+  int slot = 0;
+  for (int c = 0; c < kUploadChunks; ++c) {
+    const int vb = (int)((long long)P->nv * c / kUploadChunks), ve = (int)((long long)P->nv * (c + 1) / kUploadChunks);
+    const long long fb = vb < P->nv ? P->vd[vb].a_off : P->n_fac;
+    const long long fe = ve < P->nv ? P->vd[ve].a_off : P->n_fac;
+    if (fe > fb)
+      GBTN_CUDA(cudaMemcpyAsync(P->d_fac.p + fb, ket + fb, sizeof(double) * (fe - fb), cudaMemcpyHostToDevice,
+                                P->up_copy));
+    GBTN_CUDA(cudaEventRecord(P->up_ev[c], P->up_copy));
+    const int sb = slot;
+    while (slot < (int)P->tc_slot_vertex.size() && P->tc_slot_vertex[slot] < ve) ++slot;
+    if (slot > sb) {
+      GBTN_CUDA(cudaStreamWaitEvent(P->up_build, P->up_ev[c], 0));
+      launch_build_zimg(P->d_tc_slot_vertex.p + sb, slot - sb, P->d_vd.p, P->d_fac.p, P->d_zimg.p + (size_t)sb * 8192,
+                        P->up_build);
+    }
+  }
+  GBTN_CUDA(cudaEventRecord(P->up_ev[kUploadChunks], P->up_build));
+  GBTN_CUDA(cudaStreamWaitEvent(s, P->up_ev[kUploadChunks], 0));
+  GBTN_CUDA(cudaStreamWaitEvent(s, P->up_ev[kUploadChunks - 1], 0));
+  GBTN_CUDA(cudaStreamSynchronize(s));
+  P->zimg_valid = true;
+}
+
 int gbtn_set_factors(gbtn_plan* P, const double* ket, const double* bra, int mem) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && ket, "NULL argument");
   require(!P->sep_bra || bra, "plan has separate_bra: bra tensors are required");
-  copy_in(P, P->d_fac.p, ket, sizeof(double) * P->es() * P->n_fac, mem);
+  if (mem == GBTN_HOST && P->d_zimg.p && !P->cplx) {
+    upload_with_images(P, ket);  // the plan has run BF16: rebuild its images while the factors arrive
+  } else {
+    copy_in(P, P->d_fac.p, ket, sizeof(double) * P->es() * P->n_fac, mem);
+    P->zimg_valid = false;
+  }
   if (P->sep_bra) copy_in(P, P->d_bra.p, bra, sizeof(double) * P->es() * P->n_fac, mem);
   P->fac32_valid = false;
-  P->zimg_valid = false;
   API_CATCH(C)
 }
 
@@ -1130,10 +1197,11 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
     finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
   } else if (o->precision == GBTN_BF16) {
-    ensure_f32(P);
+    ensure_f32_bufs(P);
     int c32 = 0;
     launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, s);
     tune_tc_split(P);
+    if (bf16_has_simt(P)) ensure_f32(P);  // with every vertex on the tensor cores the FP32 factors go unread
     ensure_zimg(P);
     run_sweeps_bf16(P, o->schedule, o->maxiter, o->tol, o->normalize, c32);
     launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);

@@ -233,3 +233,31 @@ def test_graph_replay_keeps_convergence_bookkeeping():
     assert np.array_equal(out[0][0], out[1][0])
     for de in range(2 * g.ne):
         np.testing.assert_array_equal(out[0][1][de], out[1][1][de])
+
+
+@pytest.mark.parametrize("policy", ["all", "auto"])
+def test_new_factors_after_a_bf16_run_rebuild_the_images(policy):
+    # set_factors on a plan that already ran BF16 uploads the tensors in pieces
+    # and rebuilds the BF16 images as they land; the next sweep must equal a
+    # fresh plan's sweep on the new tensors, bit for bit
+    tn1, _, _ = uneven(9, 41)
+    rng = np.random.default_rng(42)
+    tn2 = gbtn.TensorNetwork(tn1.nv, tn1.edges, tn1.site_dims, tn1.edge_dims,
+                             [rng.standard_normal(np.shape(t)) for t in tn1.tensors])  # same shapes, new values
+    bpc = gbtn.BeliefPropagationCache(tn1).set_tc_policy(policy)
+    bpc.update(maxiter=2, schedule="parallel", precision="bf16")
+    bpc.set_factors(tn2.tensors)
+    bpc.init_messages("identity")
+    bpc.update(maxiter=3, schedule="parallel", precision="bf16")
+    fresh = gbtn.BeliefPropagationCache(tn2).set_tc_policy(policy)
+    fresh.init_messages("identity")
+    fresh.update(maxiter=3, schedule="parallel", precision="bf16")
+    a, b = bpc.messages(), fresh.messages()
+    if policy == "all":
+        for de in range(2 * tn2.ne):
+            np.testing.assert_array_equal(a[de], b[de])
+    else:  # the autotuned split may differ between the two plans; both are BF16-accurate
+        for de in range(2 * tn2.ne):
+            np.testing.assert_allclose(a[de], b[de], rtol=0, atol=3e-2)
+    np.testing.assert_array_equal(np.concatenate([t.ravel() for t in bpc.factors()]),
+                                  np.concatenate([np.asarray(t).ravel() for t in tn2.tensors]))
