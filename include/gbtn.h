@@ -82,14 +82,17 @@ typedef struct gbtn_graph_desc {
   int32_t separate_bra;          /* 0: bra = conj(ket) (QuadraticFormNetwork);
                                     1: bra tensors are set separately
                                     (LinearFormNetwork / inner(phi, psi)) */
-  int32_t complex_values;        /* 0: real tensors; 1: complex (ComplexF64):
-                                    every tensor, message, RDM and scalar
-                                    array holds interleaved (re, im) doubles,
-                                    twice the element count.  Complex plans run
-                                    the FP64 sweeps (any schedule), environments,
-                                    expect (real part of <O>, O real), vertex
-                                    and edge scalars and logscalar; other entry
-                                    points return GBTN_ERR_UNSUPPORTED.
+  int32_t complex_values;        /* 0: real tensors; 1: complex: every
+                                    tensor, message, RDM and scalar array
+                                    holds interleaved (re, im) doubles, twice
+                                    the element count.  Complex plans run
+                                    sweeps in FP64 (ComplexF64), FP32
+                                    (ComplexF32 arithmetic) or MIXED (FP32
+                                    sweeps, then FP64 ones), any schedule;
+                                    environments, expect (real part of <O>,
+                                    O real), vertex and edge scalars and
+                                    logscalar.  BF16 sweeps and the other
+                                    entry points return GBTN_ERR_UNSUPPORTED.
                                     (test/test_belief_propagation.jl:18-20) */
 } gbtn_graph_desc;
 

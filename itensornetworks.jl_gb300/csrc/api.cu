@@ -160,6 +160,14 @@ namespace {
 
 // The interleaved (re, im) doubles of a complex plan's arrays as elements.
 inline zdouble* zptr(double* p) { return reinterpret_cast<zdouble*>(p); }
+inline zfloat* zfptr(float* p) { return reinterpret_cast<zfloat*>(p); }
+
+// element type -> (graph-cache tag, FP32 kernel class?)
+template <typename T> struct ElemTraits;
+template <> struct ElemTraits<double> { static constexpr int tag = 0; static constexpr bool f32 = false; };
+template <> struct ElemTraits<float> { static constexpr int tag = 1; static constexpr bool f32 = true; };
+template <> struct ElemTraits<zdouble> { static constexpr int tag = 3; static constexpr bool f32 = false; };
+template <> struct ElemTraits<zfloat> { static constexpr int tag = 4; static constexpr bool f32 = true; };
 
 constexpr int kSmallN = 1024;  // vertices with n <= kSmallN run one per warp
 constexpr int kStallSweeps = 5;  // reduced-precision phases stop at their noise floor
@@ -260,11 +268,11 @@ void copy_in(gbtn_plan* P, void* dst, const void* src, size_t bytes, int mem) {
 
 // FP32 message buffers (and room for FP32 factors).
 void ensure_f32_bufs(gbtn_plan* P) {
-  if (!P->d_fac32.p) {
-    P->d_fac32.alloc(P->n_fac);
-    if (P->sep_bra) P->d_bra32.alloc(P->n_fac);
-    P->d_msg32[0].alloc(P->n_msg);
-    P->d_msg32[1].alloc(P->n_msg);
+  if (!P->d_fac32.p) {  // floats per element: 1, or 2 for complex networks (zfloat)
+    P->d_fac32.alloc(P->es() * P->n_fac);
+    if (P->sep_bra) P->d_bra32.alloc(P->es() * P->n_fac);
+    P->d_msg32[0].alloc(P->es() * P->n_msg);
+    P->d_msg32[1].alloc(P->es() * P->n_msg);
   }
 }
 
@@ -273,8 +281,8 @@ void ensure_f32(gbtn_plan* P) {
   cudaStream_t s = P->ctx->stream;
   ensure_f32_bufs(P);
   if (!P->fac32_valid) {
-    launch_convert_f64_to_f32(P->d_fac.p, P->d_fac32.p, P->n_fac, s);
-    if (P->sep_bra) launch_convert_f64_to_f32(P->d_bra.p, P->d_bra32.p, P->n_fac, s);
+    launch_convert_f64_to_f32(P->d_fac.p, P->d_fac32.p, P->es() * P->n_fac, s);
+    if (P->sep_bra) launch_convert_f64_to_f32(P->d_bra.p, P->d_bra32.p, P->es() * P->n_fac, s);
     P->fac32_valid = true;
   }
 }
@@ -367,18 +375,18 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
   GBTN_CUDA(cudaMemsetAsync(P->d_nconv.p, 0, sizeof(int), s));
   const int* conv = want_diff ? P->d_conv.p : nullptr;
   T* msg[2] = {msg0, msg1};
-  const GraphKey key{sizeof(T) == 4 ? 1 : (sizeof(T) == 16 ? 3 : 0), schedule, normalize, want_diff ? 1 : 0, stall, cur, P->list_version, tol};
+  const GraphKey key{ElemTraits<T>::tag, schedule, normalize, want_diff ? 1 : 0, stall, cur, P->list_version, tol};
   sweep_loop(P, maxiter, key, [&] {
     if (schedule == GBTN_SCHED_PARALLEL) {
       const T* in = msg[cur];
       T* out = msg[cur ^ 1];
       {
-        KTimer kt(P->ctx, sizeof(T) == 4 ? GBTN_KCLASS_SIMT_F32 : GBTN_KCLASS_SIMT_F64, P->lists[0].first.count > 0);
+        KTimer kt(P->ctx, ElemTraits<T>::f32 ? GBTN_KCLASS_SIMT_F32 : GBTN_KCLASS_SIMT_F64, P->lists[0].first.count > 0);
         launch_bp_vertices<T>(P->lists[0].first, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
                               normalize, want_diff, s);
       }
       {
-        KTimer kt(P->ctx, sizeof(T) == 4 ? GBTN_KCLASS_SIMT_F32 : GBTN_KCLASS_SIMT_F64, P->lists[0].second.count > 0);
+        KTimer kt(P->ctx, ElemTraits<T>::f32 ? GBTN_KCLASS_SIMT_F32 : GBTN_KCLASS_SIMT_F64, P->lists[0].second.count > 0);
         launch_bp_vertices<T>(P->lists[0].second, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
                               normalize, want_diff, s);
       }
@@ -1127,7 +1135,8 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
   }
   if (o->precision == GBTN_BF16 && o->schedule == GBTN_SCHED_SEQUENTIAL)
     throw Unsupported("BF16 sweeps run the parallel or coloured schedule");
-  if (P->cplx && o->precision != GBTN_F64) throw Unsupported("complex tensors run the FP64 path");
+  if (P->cplx && o->precision == GBTN_BF16)
+    throw Unsupported("complex tensors have no tensor-core (BF16) path: use f32, mixed or f64");
   if (o->schedule == GBTN_SCHED_SEQUENTIAL) {
     require(o->edge_sequence && o->edge_sequence_len > 0, "SEQUENTIAL needs an edge sequence");
     std::vector<std::vector<int2>> per(P->nnet);
@@ -1151,11 +1160,19 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     for (int n = 0; n < P->nnet; ++n) require(ptr[n + 1] > ptr[n], "edge_sequence misses a network");
     P->d_seq.upload(seq, s);
     P->d_seq_ptr.upload(ptr, s);
-    if (P->cplx) {
+    if (P->cplx && o->precision == GBTN_F64) {
       launch_bp_sequential<zdouble>(P->nnet, P->d_vd.p, P->d_seq.p, P->d_seq_ptr.p, zptr(P->d_fac.p),
                                     P->sep_bra ? zptr(P->d_bra.p) : nullptr, zptr(P->d_msg[P->cur].p),
                                     P->d_msg_off.p, o->maxiter, o->tol, o->normalize, P->d_iters.p, P->d_mean.p,
                                     P->ncap, P->maxdeg, s);
+    } else if (P->cplx) {
+      ensure_f32(P);
+      launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, 2 * P->n_msg, s);
+      launch_bp_sequential<zfloat>(P->nnet, P->d_vd.p, P->d_seq.p, P->d_seq_ptr.p, zfptr(P->d_fac32.p),
+                                   P->sep_bra ? zfptr(P->d_bra32.p) : nullptr, zfptr(P->d_msg32[0].p),
+                                   P->d_msg_off.p, o->maxiter, o->tol, o->normalize, P->d_iters.p, P->d_mean.p,
+                                   P->ncap, P->maxdeg, s);
+      launch_convert_f32_to_f64(P->d_msg32[0].p, P->d_msg[P->cur].p, 2 * P->n_msg, s);
     } else if (o->precision == GBTN_F64) {
       launch_bp_sequential<double>(P->nnet, P->d_vd.p, P->d_seq.p, P->d_seq_ptr.p, P->d_fac.p,
                                    P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p, P->d_msg_off.p, o->maxiter,
@@ -1180,10 +1197,29 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     }
     return GBTN_OK;
   }
-  if (P->cplx) {
+  if (P->cplx && o->precision == GBTN_F64) {
     run_sweeps<zdouble>(P, o->schedule, o->maxiter, o->tol, o->normalize, zptr(P->d_msg[0].p), zptr(P->d_msg[1].p),
                         zptr(P->d_fac.p), P->sep_bra ? zptr(P->d_bra.p) : nullptr, P->cur);
     finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
+  } else if (P->cplx) {  // complex FP32 sweeps (F32), then FP64 ones (MIXED): no tensor-core phase
+    ensure_f32(P);
+    int c32 = 0;
+    launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, 2 * P->n_msg, s);
+    const bool mixed = o->precision == GBTN_MIXED;
+    const double tol32 = mixed ? (o->tol_f32 > 0 ? o->tol_f32 : 1e-13) : o->tol;
+    const int it32 = mixed && o->maxiter_f32 > 0 ? o->maxiter_f32 : o->maxiter;
+    run_sweeps<zfloat>(P, o->schedule, it32, tol32, o->normalize, zfptr(P->d_msg32[0].p), zfptr(P->d_msg32[1].p),
+                       zfptr(P->d_fac32.p), P->sep_bra ? zfptr(P->d_bra32.p) : nullptr, c32,
+                       mixed ? kStallSweeps : 0);
+    launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, 2 * P->n_msg, s);
+    if (mixed) {
+      const int nref = o->refine_f64 > 0 ? std::min(o->refine_f64, o->maxiter) : o->maxiter;
+      run_sweeps<zdouble>(P, o->schedule, nref, o->tol, o->normalize, zptr(P->d_msg[0].p), zptr(P->d_msg[1].p),
+                          zptr(P->d_fac.p), P->sep_bra ? zptr(P->d_bra.p) : nullptr, P->cur);
+      finish_iters(P, want_diff, nref, iters, mean_diff);
+    } else {
+      finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
+    }
   } else if (o->precision == GBTN_F64) {
     run_sweeps<double>(P, o->schedule, o->maxiter, o->tol, o->normalize, P->d_msg[0].p, P->d_msg[1].p, P->d_fac.p,
                        P->sep_bra ? P->d_bra.p : nullptr, P->cur);

@@ -29,19 +29,32 @@ __device__ __forceinline__ zdouble& operator+=(zdouble& a, zdouble b) {
   a.im += b.im;
   return a;
 }
+__device__ __forceinline__ zfloat operator+(zfloat a, zfloat b) { return zfloat(a.re + b.re, a.im + b.im); }
+__device__ __forceinline__ zfloat& operator+=(zfloat& a, zfloat b) {
+  a.re += b.re;
+  a.im += b.im;
+  return a;
+}
 // multiply-accumulate a * b + c
 __device__ __forceinline__ float mac(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double mac(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ zdouble mac(zdouble a, zdouble b, zdouble c) {
   return zdouble(fma(a.re, b.re, fma(-a.im, b.im, c.re)), fma(a.re, b.im, fma(a.im, b.re, c.im)));
 }
+__device__ __forceinline__ zfloat mac(zfloat a, zfloat b, zfloat c) {
+  return zfloat(fmaf(a.re, b.re, fmaf(-a.im, b.im, c.re)), fmaf(a.re, b.im, fmaf(a.im, b.re, c.im)));
+}
 __device__ __forceinline__ float conj_of(float x) { return x; }
 __device__ __forceinline__ double conj_of(double x) { return x; }
 __device__ __forceinline__ zdouble conj_of(zdouble x) { return zdouble(x.re, -x.im); }
+__device__ __forceinline__ zfloat conj_of(zfloat x) { return zfloat(x.re, -x.im); }
 __device__ __forceinline__ float shfl_xor(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 __device__ __forceinline__ double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 __device__ __forceinline__ zdouble shfl_xor(zdouble v, int o) {
   return zdouble(__shfl_xor_sync(0xffffffffu, v.re, o), __shfl_xor_sync(0xffffffffu, v.im, o));
+}
+__device__ __forceinline__ zfloat shfl_xor(zfloat v, int o) {
+  return zfloat(__shfl_xor_sync(0xffffffffu, v.re, o), __shfl_xor_sync(0xffffffffu, v.im, o));
 }
 
 __device__ __forceinline__ double warp_sum(double x) {
@@ -237,6 +250,38 @@ __device__ __forceinline__ double finalize_message<zdouble>(const zdouble* res, 
     const double dim = warp_sum(o0.re * n0.im - o0.im * n0.re + o1.re * n1.im - o1.im * n1.re);
     const double na = warp_sum(n0.re * n0.re + n0.im * n0.im + n1.re * n1.re + n1.im * n1.im);
     const double nb = warp_sum(o0.re * o0.re + o0.im * o0.im + o1.re * o1.re + o1.im * o1.im);
+    diff = 1.0 - (dre * dre + dim * dim) / (na * nb);
+  }
+  return diff;
+}
+
+// Complex FP32 messages: as the complex FP64 case, with the norm, the scale
+// and message_diff evaluated in FP64 and the result stored as FP32 pairs.
+template <>
+__device__ __forceinline__ double finalize_message<zfloat>(const zfloat* res, int chi, const zfloat* old, zfloat* out,
+                                                           int normalize, bool want_diff, int lane) {
+  const int P = chi * chi;
+  const zfloat r0 = lane < P ? res[lane] : zfloat(0.f), r1 = lane + 32 < P ? res[lane + 32] : zfloat(0.f);
+  const double v0r = r0.re, v0i = r0.im, v1r = r1.re, v1i = r1.im;
+  const double nrm2 = warp_sum(v0r * v0r + v0i * v0i + v1r * v1r + v1i * v1i);
+  const double sc = (normalize && nrm2 > 0.0) ? 1.0 / sqrt(nrm2) : 1.0;
+  const zfloat n0((float)(v0r * sc), (float)(v0i * sc)), n1((float)(v1r * sc), (float)(v1i * sc));
+  zfloat o0(0.f), o1(0.f);
+  if (want_diff) {
+    if (lane < P) o0 = old[lane];
+    if (lane + 32 < P) o1 = old[lane + 32];
+  }
+  __syncwarp();
+  if (lane < P) out[lane] = n0;
+  if (lane + 32 < P) out[lane + 32] = n1;
+  double diff = 0.0;
+  if (want_diff) {
+    const double a0r = n0.re, a0i = n0.im, a1r = n1.re, a1i = n1.im;
+    const double b0r = o0.re, b0i = o0.im, b1r = o1.re, b1i = o1.im;
+    const double dre = warp_sum(b0r * a0r + b0i * a0i + b1r * a1r + b1i * a1i);
+    const double dim = warp_sum(b0r * a0i - b0i * a0r + b1r * a1i - b1i * a1r);
+    const double na = warp_sum(a0r * a0r + a0i * a0i + a1r * a1r + a1i * a1i);
+    const double nb = warp_sum(b0r * b0r + b0i * b0i + b1r * b1r + b1i * b1i);
     diff = 1.0 - (dre * dre + dim * dim) / (na * nb);
   }
   return diff;

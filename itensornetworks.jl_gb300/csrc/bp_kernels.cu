@@ -608,6 +608,8 @@ template void launch_bp_vertices<float>(const WorkList&, const VDesc*, const flo
 template void launch_bp_vertices<zdouble>(const WorkList&, const VDesc*, const zdouble*, const zdouble*,
                                           const zdouble*, zdouble*, const long long*, double*, const int*, int, int,
                                           cudaStream_t);
+template void launch_bp_vertices<zfloat>(const WorkList&, const VDesc*, const zfloat*, const zfloat*, const zfloat*,
+                                         zfloat*, const long long*, double*, const int*, int, int, cudaStream_t);
 
 template <typename T>
 void launch_bp_sequential(int n_networks, const VDesc* vd, const int2* seq, const int* seq_ptr, const T* fac,
@@ -630,6 +632,9 @@ template void launch_bp_sequential<float>(int, const VDesc*, const int2*, const 
 template void launch_bp_sequential<zdouble>(int, const VDesc*, const int2*, const int*, const zdouble*,
                                             const zdouble*, zdouble*, const long long*, int, double, int, int*,
                                             double*, int, int, cudaStream_t);
+template void launch_bp_sequential<zfloat>(int, const VDesc*, const int2*, const int*, const zfloat*, const zfloat*,
+                                           zfloat*, const long long*, int, double, int, int*, double*, int, int,
+                                           cudaStream_t);
 
 void launch_reduce_diffs(int n_networks, const int* net_de_ptr, const int* net_de, const double* diffs, double tol,
                          int* converged, int* iters, double* mean_diff, cudaStream_t s, int stall, double* best,

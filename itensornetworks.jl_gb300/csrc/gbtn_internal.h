@@ -28,6 +28,14 @@ struct __align__(16) zdouble {
   __host__ __device__ constexpr zdouble(double r, double i = 0.0) : re(r), im(i) {}
 };
 
+// Complex FP32 element (the FP32 SIMT path of complex networks): interleaved
+// (re, im) floats.
+struct __align__(8) zfloat {
+  float re, im;
+  zfloat() = default;
+  __host__ __device__ constexpr zfloat(float r, float i = 0.f) : re(r), im(i) {}
+};
+
 // Per-vertex descriptor, read by every message / environment kernel.
 struct __align__(16) VDesc {
   long long a_off;          // element offset of the vertex tensor
@@ -88,7 +96,7 @@ struct WorkList {
   int team = 32;              // threads per vertex (32 or 256)
 };
 
-// Kernel launchers (bp_kernels.cu).  T = double or float.
+// Kernel launchers (bp_kernels.cu).  T = double, float, zdouble or zfloat.
 template <typename T>
 void launch_bp_vertices(const WorkList& wl, const VDesc* vd, const T* fac, const T* bra,
                         const T* msg_in, T* msg_out, const long long* msg_off, double* diffs,

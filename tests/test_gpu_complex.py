@@ -1,9 +1,13 @@
-"""Complex tensors (ComplexF64, test/test_belief_propagation.jl:18-20) on the
-FP64 path against the oracle, which conjugates the bra and uses the complex
-inner product in message_diff: messages after a fixed number of sweeps to
-1e-10 (every schedule), <Sz> and the complex log-scalar to 1e-10, exactness
-on a tree, inner products with a separate bra.  Paths that take real tensors
-only report GBTN_ERR_UNSUPPORTED."""
+"""Complex tensors (ComplexF32 / ComplexF64, test/test_belief_propagation.jl:18-20)
+against the oracle, which conjugates the bra and uses the complex inner
+product in message_diff.  FP64 path: messages after a fixed number of sweeps
+to 1e-10 (every schedule), <Sz> and the complex log-scalar to 1e-10,
+exactness on a tree, inner products with a separate bra.  FP32 path (complex
+FP32 elements, the ComplexF32 case): messages after a fixed number of sweeps
+to 1e-5 (parallel, coloured; 5e-5 sequential, whose updates compound within
+a sweep; FP32 keeps 24 significant bits); the mixed pipeline
+(complex FP32 sweeps, then FP64 ones to tol) reaches the FP64 fixed point to
+1e-10.  Paths that take real tensors only report GBTN_ERR_UNSUPPORTED."""
 import numpy as np
 import pytest
 
@@ -84,6 +88,39 @@ def test_complex_inner_with_separate_bra_on_a_tree():
     phi = gbtn.TensorNetwork(g.nv, g.edges, g.site_dims, g.edge_dims, [b.copy() for b in B])
     val = gbtn.inner(phi, tn, cache_update_kwargs=dict(maxiter=30, schedule="parallel"))
     assert complex(val) == pytest.approx(complex(O.exact_scalar(g, A, B)), rel=1e-9)
+
+
+@pytest.mark.parametrize("schedule", ["parallel", "colored", "sequential"])
+def test_complex_fp32_messages_match_oracle(schedule):
+    g = O.square_lattice(4, 4, chi=3)
+    tn, A = cnet(g, 3)
+    n = 4
+    ref, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=n, schedule=schedule)
+    bpc = gbtn.BeliefPropagationCache(tn).update(maxiter=n, schedule=schedule, precision="f32")
+    got = bpc.messages()
+    err = max(np.max(np.abs(got[de] - ref[de])) for de in range(2 * g.ne))
+    # in a sequential sweep each update feeds the next, so FP32 rounding
+    # compounds along the 48-message chain of this (non-converging) network
+    tol = 5e-5 if schedule == "sequential" else 1e-5
+    assert err < tol, f"{schedule}: {err:.3e}"
+    assert err > 1e-12  # the sweeps really ran in FP32
+
+
+def test_complex_mixed_reaches_the_fp64_fixed_point():
+    g = O.square_lattice(5, 4, chi=2)
+    tn, A = cnet(g, 8)
+    m, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=400, schedule="parallel")
+    sz_ref = np.real(O.expect1(g, A, m, O.SZ))
+    # FP32 sweeps to their noise floor, then a full FP64 phase: the FP64 fixed point
+    bpc = gbtn.BeliefPropagationCache(tn).update(maxiter=400, schedule="parallel", precision="mixed")
+    np.testing.assert_allclose(bpc.expect(O.SZ), sz_ref, rtol=0, atol=1e-10 * np.max(np.abs(sz_ref)))
+    got = bpc.messages()
+    for de in range(2 * g.ne):  # equal up to each message's free phase
+        assert abs(np.vdot(got[de], m[de])) == pytest.approx(1.0, abs=1e-10)
+    # stopped at tol 1e-14 (message angles ~1e-7): within the 1e-6 bar, like plain FP64 at the same tol
+    mix = gbtn.BeliefPropagationCache(tn).update(maxiter=400, tol=1e-14, schedule="parallel", precision="mixed")
+    assert mix.iterations[0] < 400 and mix.mean_diff[0] <= 1e-14
+    np.testing.assert_allclose(mix.expect(O.SZ), sz_ref, rtol=0, atol=1e-6 * np.max(np.abs(sz_ref)))
 
 
 def test_complex_paths_outside_fp64_are_unsupported():
