@@ -89,10 +89,12 @@ typedef struct gbtn_graph_desc {
                                     sweeps in FP64 (ComplexF64), FP32
                                     (ComplexF32 arithmetic) or MIXED (FP32
                                     sweeps, then FP64 ones), any schedule;
-                                    environments, expect (real part of <O>,
-                                    O real), vertex and edge scalars and
-                                    logscalar.  BF16 sweeps and the other
-                                    entry points return GBTN_ERR_UNSUPPORTED.
+                                    environments, one- and two-site RDMs,
+                                    expect / expect2 (real part of <O>, O
+                                    real), vertex and edge scalars,
+                                    logscalar and rescale_messages.  BF16
+                                    sweeps and the other entry points return
+                                    GBTN_ERR_UNSUPPORTED.
                                     (test/test_belief_propagation.jl:18-20) */
 } gbtn_graph_desc;
 

@@ -670,9 +670,15 @@ __global__ void expect1_kernel(int nv, const long long* rdm_off, const double* r
 }
 
 // rho[(s'u, s'v), (su, sv)] = sum_{b,a} Ru[s'u, su, b, a] Rv[s'v, sv, b, a]
+// (the shared link's bra and ket indices contracted directly, no conjugation)
+__device__ __forceinline__ double rdm_mac(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ zdouble rdm_mac(zdouble a, zdouble b, zdouble c) {
+  return zdouble(fma(a.re, b.re, fma(-a.im, b.im, c.re)), fma(a.re, b.im, fma(a.im, b.re, c.im)));
+}
+template <typename T>
 __global__ void edge_rdm_combine_kernel(int nedges, const int* du_, const int* dv_, const int* chi_,
-                                        const long long* hu_off, const long long* hv_off, const double* halves,
-                                        const long long* out_off, double* out) {
+                                        const long long* hu_off, const long long* hv_off, const T* halves,
+                                        const long long* out_off, T* out) {
   const int j = blockIdx.x;
   if (j >= nedges) return;
   const int du = du_[j], dv = dv_[j], c2 = chi_[j] * chi_[j];
@@ -680,12 +686,32 @@ __global__ void edge_rdm_combine_kernel(int nedges, const int* du_, const int* d
   for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) {
     const int row = idx % D, col = idx / D;
     const int spu = row % du, spv = row / du, su = col % du, sv = col / du;
-    const double* ru = halves + hu_off[j] + (long long)(spu + du * su) * c2;
-    const double* rv = halves + hv_off[j] + (long long)(spv + dv * sv) * c2;
-    double acc = 0.0;
-    for (int i = 0; i < c2; ++i) acc += ru[i] * rv[i];
+    const T* ru = halves + hu_off[j] + (long long)(spu + du * su) * c2;
+    const T* rv = halves + hv_off[j] + (long long)(spv + dv * sv) * c2;
+    T acc = T(0.0);
+    for (int i = 0; i < c2; ++i) acc = rdm_mac(ru[i], rv[i], acc);
     out[out_off[j] + idx] = acc;
   }
+}
+
+// Complex two-site RDMs (interleaved pairs): the real part of
+// sum rho O / tr rho for a real operator O.
+__global__ void expect2_z_kernel(int nedges, const long long* rdm_off, const int* D_, const zdouble* rdm,
+                                 const double* op, double* out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nedges) return;
+  const int D = D_[j];
+  const zdouble* r = rdm + rdm_off[j];
+  double nr = 0.0, ni = 0.0, dr = 0.0, di = 0.0;
+  for (int i = 0; i < D * D; ++i) {
+    nr += r[i].re * op[i];
+    ni += r[i].im * op[i];
+  }
+  for (int q = 0; q < D; ++q) {
+    dr += r[q + D * q].re;
+    di += r[q + D * q].im;
+  }
+  out[j] = (nr * dr + ni * di) / (dr * dr + di * di);
 }
 
 __global__ void expect2_kernel(int nedges, const long long* rdm_off, const int* D_, const double* rdm, const double* op,
@@ -1399,9 +1425,15 @@ static void edge_rdms_device(gbtn_plan* P, const int32_t* edges, int32_t n, DevB
   }
   P->d_jobs.upload(jobs, s);
   P->d_half_off.upload(hoff, s);
-  P->d_halves.alloc(std::max<long long>(off, 1));
-  launch_edge_halves(P->d_jobs.p, 2 * n, P->ncap, P->maxdeg, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr,
-                     P->d_msg[P->cur].p, P->d_msg_off.p, P->d_halves.p, P->d_half_off.p, s);
+  P->d_halves.alloc(std::max<long long>(P->es() * off, 1));
+  if (P->cplx)
+    launch_edge_halves<zdouble>(P->d_jobs.p, 2 * n, P->ncap, P->maxdeg, P->d_vd.p, zptr(P->d_fac.p),
+                                P->sep_bra ? zptr(P->d_bra.p) : nullptr, zptr(P->d_msg[P->cur].p), P->d_msg_off.p,
+                                zptr(P->d_halves.p), P->d_half_off.p, s);
+  else
+    launch_edge_halves<double>(P->d_jobs.p, 2 * n, P->ncap, P->maxdeg, P->d_vd.p, P->d_fac.p,
+                               P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p, P->d_msg_off.p, P->d_halves.p,
+                               P->d_half_off.p, s);
   DevBuf<int> d_du, d_dv, d_ch;
   DevBuf<long long> d_hu, d_hv, d_oo;
   d_du.upload(du, s);
@@ -1410,8 +1442,13 @@ static void edge_rdms_device(gbtn_plan* P, const int32_t* edges, int32_t n, DevB
   d_hu.upload(hu, s);
   d_hv.upload(hv, s);
   d_oo.upload(out_off, s);
-  d_out.alloc(std::max<long long>(ooff, 1));
-  edge_rdm_combine_kernel<<<n, 128, 0, s>>>(n, d_du.p, d_dv.p, d_ch.p, d_hu.p, d_hv.p, P->d_halves.p, d_oo.p, d_out.p);
+  d_out.alloc(std::max<long long>(P->es() * ooff, 1));
+  if (P->cplx)
+    edge_rdm_combine_kernel<zdouble><<<n, 128, 0, s>>>(n, d_du.p, d_dv.p, d_ch.p, d_hu.p, d_hv.p, zptr(P->d_halves.p),
+                                                       d_oo.p, zptr(d_out.p));
+  else
+    edge_rdm_combine_kernel<double><<<n, 128, 0, s>>>(n, d_du.p, d_dv.p, d_ch.p, d_hu.p, d_hv.p, P->d_halves.p,
+                                                      d_oo.p, d_out.p);
   GBTN_CUDA(cudaGetLastError());
   GBTN_CUDA(cudaStreamSynchronize(s));
 }
@@ -1419,7 +1456,6 @@ static void edge_rdms_device(gbtn_plan* P, const int32_t* edges, int32_t n, DevB
 int gbtn_edge_rdms(gbtn_plan* P, const int32_t* edges, int32_t n, double* out) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
-  if (P && P->cplx) throw Unsupported("two-site RDMs of complex networks is not implemented");
   require(P && edges && out && n >= 0, "bad argument");
   if (n == 0) return GBTN_OK;
   DevBuf<double> d_out;
@@ -1431,14 +1467,13 @@ int gbtn_edge_rdms(gbtn_plan* P, const int32_t* edges, int32_t n, double* out) {
     const long long D = (long long)P->dsite[P->eu[e]] * P->dsite[P->ev[e]];
     tot += D * D;
   }
-  copy_out(P, out, d_out.p, sizeof(double) * tot, GBTN_HOST);
+  copy_out(P, out, d_out.p, sizeof(double) * P->es() * tot, GBTN_HOST);
   API_CATCH(C)
 }
 
 int gbtn_expect2(gbtn_plan* P, const int32_t* edges, int32_t n, const double* op, double* out) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
-  if (P && P->cplx) throw Unsupported("two-site expectation values of complex networks is not implemented");
   require(P && edges && op && out && n >= 0, "bad argument");
   if (n == 0) return GBTN_OK;
   cudaStream_t s = P->ctx->stream;
@@ -1459,7 +1494,10 @@ int gbtn_expect2(gbtn_plan* P, const int32_t* edges, int32_t n, const double* op
   std::vector<double> hop(op, op + D[0] * D[0]);
   d_op.upload(hop, s);
   d_res.alloc(n);
-  expect2_kernel<<<(n + 127) / 128, 128, 0, s>>>(n, d_oo.p, d_D.p, d_rdm.p, d_op.p, d_res.p);
+  if (P->cplx)
+    expect2_z_kernel<<<(n + 127) / 128, 128, 0, s>>>(n, d_oo.p, d_D.p, zptr(d_rdm.p), d_op.p, d_res.p);
+  else
+    expect2_kernel<<<(n + 127) / 128, 128, 0, s>>>(n, d_oo.p, d_D.p, d_rdm.p, d_op.p, d_res.p);
   GBTN_CUDA(cudaGetLastError());
   copy_out(P, out, d_res.p, sizeof(double) * n, GBTN_HOST);
   API_CATCH(C)
@@ -1524,11 +1562,13 @@ int gbtn_logscalar(gbtn_plan* P, double* re, double* im) {
 int gbtn_rescale_messages(gbtn_plan* P) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
-  if (P && P->cplx) throw Unsupported("rescale_messages of complex networks is not implemented");
   require(P, "NULL plan");
   if (P->ne) {
     KTimer kt(P->ctx, GBTN_KCLASS_GAUGE);
-    launch_rescale_messages(P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, P->ctx->stream);
+    if (P->cplx)
+      launch_rescale_messages_z(P->ne, P->d_dchi.p, P->d_msg_off.p, zptr(P->d_msg[P->cur].p), P->ctx->stream);
+    else
+      launch_rescale_messages(P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, P->ctx->stream);
   }
   GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));
   API_CATCH(C)
@@ -1537,6 +1577,9 @@ int gbtn_rescale_messages(gbtn_plan* P) {
 int gbtn_rescale_partitions(gbtn_plan* P) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
+  // With the bra taken as conj(ket), scale factors come in conjugate pairs and
+  // change a partition scalar only by |c|^2: a complex partition scalar
+  // cannot be brought to 1 without separate ket and bra tensors.
   if (P && P->cplx) throw Unsupported("rescale_partitions of complex networks is not implemented");
   require(P, "NULL plan");
   cudaStream_t s = P->ctx->stream;

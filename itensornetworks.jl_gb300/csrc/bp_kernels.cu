@@ -257,27 +257,28 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
 // Half of a two-site RDM: for job (v, p), R[s', s, b, a] with every incoming
 // message of v except the one on leg p absorbed, stored at
 // half[(s' + d*s)*chi*chi + b + chi*a].
+template <typename T>
 __global__ void __launch_bounds__(256)
     edge_half_kernel(const int2* __restrict__ jobs, int njobs, const VDesc* __restrict__ vd,
-                     const double* __restrict__ fac, const double* __restrict__ bra_g, const double* msgs,
-                     const long long* __restrict__ msg_off, double* halves, const long long* __restrict__ half_off,
+                     const T* __restrict__ fac, const T* __restrict__ bra_g, const T* msgs,
+                     const long long* __restrict__ msg_off, T* halves, const long long* __restrict__ half_off,
                      int ncap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TEAM = 256;
   const int tid = threadIdx.x;
-  TeamSmem<double> S = carve<double>(smem_raw, ncap, 3, bra_g != nullptr, TEAM);
+  TeamSmem<T> S = carve<T>(smem_raw, ncap, 3, bra_g != nullptr, TEAM);
   for (int j = blockIdx.x; j < njobs; j += gridDim.x) {
     const int2 jb = jobs[j];
     load_desc<TEAM>(S.desc, vd + jb.x, tid);
     __syncthreads();
-    load_vertex<double, TEAM>(S, fac, bra_g, msgs, msg_off, jb.y, tid);
+    load_vertex<T, TEAM>(S, fac, bra_g, msgs, msg_off, jb.y, tid);
     __syncthreads();
-    const int cur = chain_absorb<double, TEAM>(S, jb.y, tid);
+    const int cur = chain_absorb<T, TEAM>(S, jb.y, tid);
     const VDesc& d = *S.desc;
     const int chi = d.chi[jb.y];
     for (int s = 0; s < d.d; ++s)
       for (int sp = 0; sp < d.d; ++sp) {
-        close_any<double, TEAM>(chi, S.buf[cur], S.bra, d.n, d.st[jb.y], d.d, s, sp - s, S.red, S.res, tid);
+        close_any<T, TEAM>(chi, S.buf[cur], S.bra, d.n, d.st[jb.y], d.d, s, sp - s, S.red, S.res, tid);
         for (int i = tid; i < chi * chi; i += TEAM) halves[half_off[j] + (long long)(sp + d.d * s) * chi * chi + i] = S.res[i];
         __syncthreads();
       }
@@ -430,6 +431,49 @@ __global__ void rescale_messages_kernel(int ne, const int* dchi, const long long
       m1[i] = ka * a[j];
       m2[i] = kb * b[j];
     }
+  }
+}
+
+// Complex messages (rescale_messages, beliefpropagationcache.jl:121-139):
+// normalise both, n = sum m1 m2 (no conjugation), and when n is real fix the
+// sign of m1 (n -> |n|); then multiply both by the principal n^(-1/2).  One
+// warp per edge; the complex networks this serves are not bandwidth-bound.
+__global__ void rescale_messages_z_kernel(int ne, const int* dchi, const long long* msg_off, zdouble* msgs) {
+  const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (e >= ne) return;
+  const int c2 = dchi[2 * e] * dchi[2 * e];
+  zdouble* m1 = msgs + msg_off[2 * e];
+  zdouble* m2 = msgs + msg_off[2 * e + 1];
+  double na2 = 0.0, nb2 = 0.0, pr = 0.0, pi = 0.0;
+  for (int i = lane; i < c2; i += 32) {
+    const zdouble a = m1[i], b = m2[i];
+    na2 += a.re * a.re + a.im * a.im;
+    nb2 += b.re * b.re + b.im * b.im;
+    pr += a.re * b.re - a.im * b.im;
+    pi += a.re * b.im + a.im * b.re;
+  }
+  na2 = warp_sum(na2);
+  nb2 = warp_sum(nb2);
+  pr = warp_sum(pr);
+  pi = warp_sum(pi);
+  const double ia = 1.0 / sqrt(na2), ib = 1.0 / sqrt(nb2);
+  double nr = pr * ia * ib, ni = pi * ia * ib;  // n = <m1/|m1|, m2/|m2|>
+  double sg = 1.0;
+  if (ni == 0.0) {  // isreal(n): m1 *= sign(n), n *= sign(n)
+    sg = nr > 0.0 ? 1.0 : (nr < 0.0 ? -1.0 : 0.0);
+    nr *= sg;
+  }
+  // principal square root of n, then its reciprocal
+  const double mod = sqrt(nr * nr + ni * ni);
+  const double sr = sqrt(0.5 * (mod + nr)), si = copysign(sqrt(0.5 * (mod - nr)), ni);
+  const double sm2 = sr * sr + si * si;
+  const double fr = sr / sm2, fi = -si / sm2;  // n^(-1/2)
+  const zdouble ka(sg * ia * fr, sg * ia * fi), kb(ib * fr, ib * fi);
+  for (int i = lane; i < c2; i += 32) {
+    const zdouble a = m1[i], b = m2[i];
+    m1[i] = zdouble(ka.re * a.re - ka.im * a.im, ka.re * a.im + ka.im * a.re);
+    m2[i] = zdouble(kb.re * b.re - kb.im * b.im, kb.re * b.im + kb.im * b.re);
   }
 }
 
@@ -697,17 +741,21 @@ void launch_expect1_z(int nv, const long long* rdm_off, const zdouble* rdm, cons
   GBTN_CUDA(cudaGetLastError());
 }
 
-void launch_edge_halves(const int* jobs, int njobs, int ncap, int maxdeg, const VDesc* vd, const double* fac,
-                        const double* bra, const double* msgs, const long long* msg_off, double* halves,
-                        const long long* half_off, cudaStream_t s) {
+template <typename T>
+void launch_edge_halves(const int* jobs, int njobs, int ncap, int maxdeg, const VDesc* vd, const T* fac, const T* bra,
+                        const T* msgs, const long long* msg_off, T* halves, const long long* half_off, cudaStream_t s) {
   (void)maxdeg;
   if (njobs == 0) return;
-  const size_t sm = team_smem_bytes<double>(ncap, 3, bra != nullptr, 256);
-  GBTN_CUDA(cudaFuncSetAttribute(edge_half_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  edge_half_kernel<<<njobs, 256, sm, s>>>(reinterpret_cast<const int2*>(jobs), njobs, vd, fac, bra, msgs, msg_off,
-                                          halves, half_off, ncap);
+  const size_t sm = team_smem_bytes<T>(ncap, 3, bra != nullptr, 256);
+  GBTN_CUDA(cudaFuncSetAttribute(edge_half_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  edge_half_kernel<T><<<njobs, 256, sm, s>>>(reinterpret_cast<const int2*>(jobs), njobs, vd, fac, bra, msgs, msg_off,
+                                             halves, half_off, ncap);
   GBTN_CUDA(cudaGetLastError());
 }
+template void launch_edge_halves<double>(const int*, int, int, int, const VDesc*, const double*, const double*,
+                                         const double*, const long long*, double*, const long long*, cudaStream_t);
+template void launch_edge_halves<zdouble>(const int*, int, int, int, const VDesc*, const zdouble*, const zdouble*,
+                                          const zdouble*, const long long*, zdouble*, const long long*, cudaStream_t);
 
 static int grid_for(long long n) {
   long long b = (n + 255) / 256;
@@ -738,6 +786,11 @@ void launch_scale_vertices(int nv, const VDesc* vd, double* fac, double* bra, co
   scale_vertices_kernel<<<nv, 256, 0, s>>>(nv, vd, fac, bra, scale);
   GBTN_CUDA(cudaGetLastError());
 }
+void launch_rescale_messages_z(int ne, const int* dchi, const long long* msg_off, zdouble* msgs, cudaStream_t s) {
+  rescale_messages_z_kernel<<<(ne + 7) / 8, 256, 0, s>>>(ne, dchi, msg_off, msgs);
+  GBTN_CUDA(cudaGetLastError());
+}
+
 void launch_rescale_messages(int ne, const int* dchi, const long long* msg_off, double* msgs, cudaStream_t s) {
   if (ne == 0) return;
   rescale_messages_kernel<<<(ne + 63) / 64, 256, 0, s>>>(ne, dchi, msg_off, msgs);  // 4 lanes per edge

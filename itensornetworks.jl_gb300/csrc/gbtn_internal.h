@@ -122,9 +122,10 @@ void launch_vertex_rdms(const WorkList& wl, const VDesc* vd, const T* fac, const
                         const T* msgs, const long long* msg_off, const long long* rdm_off,
                         T* rdm, cudaStream_t s);
 
+template <typename T>
 void launch_edge_halves(const int* jobs /*pairs (v, leg)*/, int njobs, int ncap, int maxdeg,
-                        const VDesc* vd, const double* fac, const double* bra, const double* msgs,
-                        const long long* msg_off, double* halves /* per job d*d*chi*chi */,
+                        const VDesc* vd, const T* fac, const T* bra, const T* msgs,
+                        const long long* msg_off, T* halves /* per job d*d*chi*chi */,
                         const long long* half_off, cudaStream_t s);
 
 void launch_convert_f64_to_f32(const double* a, float* b, long long n, cudaStream_t s);
@@ -135,6 +136,7 @@ void launch_fill_messages(int ndir, const int* dchi, const long long* msg_off, d
                           int cplx = 0);
 void launch_scale_vertices(int nv, const VDesc* vd, double* fac, double* bra, const double* scale,
                            cudaStream_t s);
+void launch_rescale_messages_z(int ne, const int* dchi, const long long* msg_off, zdouble* msgs, cudaStream_t s);
 void launch_rescale_messages(int ne, const int* dchi, const long long* msg_off, double* msgs,
                              cudaStream_t s);
 void launch_edge_scalars(int ne, const int* dchi, const long long* msg_off, const double* msgs,

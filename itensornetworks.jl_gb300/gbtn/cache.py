@@ -203,8 +203,8 @@ class BeliefPropagationCache:
             return []
         es = np.ascontiguousarray(edges, dtype=np.int32)
         Ds = [self.tn.site_dims[self.tn.edges[e][0]] * self.tn.site_dims[self.tn.edges[e][1]] for e in edges]
-        out = np.empty(sum(D * D for D in Ds))
-        self._c(self.lib.gbtn_edge_rdms(self.handle, iptr(es), len(edges), dptr(out)))
+        out = np.empty(sum(D * D for D in Ds), dtype=self.dtype)
+        self._c(self.lib.gbtn_edge_rdms(self.handle, iptr(es), len(edges), dptr(out.view(np.float64))))
         res, off = [], 0
         for D in Ds:
             res.append(out[off:off + D * D].reshape((D, D), order="F"))

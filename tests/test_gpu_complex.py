@@ -7,7 +7,10 @@ FP32 elements, the ComplexF32 case): messages after a fixed number of sweeps
 to 1e-5 (parallel, coloured; 5e-5 sequential, whose updates compound within
 a sweep; FP32 keeps 24 significant bits); the mixed pipeline
 (complex FP32 sweeps, then FP64 ones to tol) reaches the FP64 fixed point to
-1e-10.  Paths that take real tensors only report GBTN_ERR_UNSUPPORTED."""
+1e-10.  Two-site RDMs and <O_u O_v> (1e-10, RDMs compared after trace
+normalisation since each message keeps a free phase) and rescale_messages
+(1e-12, edge scalars 1) are complex too.  Paths that take real tensors only
+report GBTN_ERR_UNSUPPORTED."""
 import numpy as np
 import pytest
 
@@ -130,6 +133,38 @@ def test_complex_paths_outside_fp64_are_unsupported():
     with pytest.raises(gbtn.Unsupported):
         bpc.update(maxiter=2, schedule="parallel", precision="bf16")
     with pytest.raises(gbtn.Unsupported):
-        bpc.edge_rdms()
+        bpc.rescale_partitions()
     with pytest.raises(gbtn.Unsupported):
         gbtn.SimpleUpdateState(tn, 4)
+
+
+def test_complex_two_site_rdms_and_expect2():
+    g = O.square_lattice(4, 3, chi=2)
+    tn, A = cnet(g, 12)
+    bpc = gbtn.BeliefPropagationCache(tn).update(maxiter=200, schedule="parallel")
+    m, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=200, schedule="parallel")
+    rho = bpc.edge_rdms()
+    zz = np.kron(O.SZ, O.SZ)
+    for e in range(g.ne):
+        ref = O.edge_rdm(g, A, A, m, e)
+        # each message carries a free phase: compare the normalised RDMs
+        r, rr = rho[e] / np.trace(rho[e]), ref / np.trace(ref)
+        assert np.iscomplexobj(rho[e])
+        np.testing.assert_allclose(r, rr, rtol=0, atol=1e-10)
+    got = bpc.expect2(zz)
+    ref = np.real(O.expect2(g, A, m, zz))
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-10 * np.max(np.abs(ref)))
+
+
+def test_complex_rescale_messages_matches_oracle():
+    g = O.square_lattice(4, 4, chi=3)
+    tn, A = cnet(g, 6)
+    bpc = gbtn.BeliefPropagationCache(tn).update(maxiter=3, schedule="parallel")
+    before = bpc.messages()
+    bpc.rescale_messages()
+    got = bpc.messages()
+    ref = O.rescale_messages(g, before)
+    err = max(np.max(np.abs(got[de] - ref[de])) for de in range(2 * g.ne))
+    assert err < 1e-12, err
+    # every edge scalar <m_e, m_ebar> (no conjugation) is now 1
+    np.testing.assert_allclose(bpc.edge_scalars(), np.ones(g.ne), rtol=0, atol=1e-12)
