@@ -10,10 +10,12 @@
 # C-ABI layout (include/gbtn.h), runs the sweeps on the GPU and writes the
 # messages back into the cache, so `expect`, `environment`, `scalar`,
 # `logscalar`, `inner`, `norm` and `normalize` keep their signatures and read
-# converged messages as usual.  Real Float64/Float32 dense tensors with one
-# site index per vertex, one link per edge and chi <= 8 are supported; other
-# caches fall back to nothing -- they raise, as the library has no CPU path.
-# ComplexF64 tensors run the FP64 sweeps (complex_values = 1).
+# converged messages as usual.  Dense Float64, Float32, ComplexF64 and
+# ComplexF32 tensors with one site index per vertex and one link per edge are
+# supported; other caches raise, as the library has no CPU path.  The default
+# precision follows the element type (FP64 for Float64 / ComplexF64, FP32 for
+# Float32 / ComplexF32); complex tensors (complex_values = 1) run the FP64,
+# FP32 or mixed sweeps, not the BF16 tensor-core one.
 #
 # It also adds `apply(Algorithm("gb300"), gates, psi; maxdim, cutoff, normalize,
 # envs)`, the simple update of src/apply.jl:33-160 on the GPU (FP64 truncated
@@ -124,7 +126,9 @@ function ITensorNetworks.update(alg::Algorithm"gb300_bp", bpc::BeliefPropagation
             check(ctx, ccall((:gbtn_set_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint),
                 plan[], p.data, C_NULL, 0))
             sched = get(alg.kwargs, :schedule, "parallel") == "colored" ? 2 : 1
-            prec = Dict("f64" => 0, "f32" => 1, "bf16" => 2, "mixed" => 3)[get(alg.kwargs, :precision, "f64")]
+            single = all(pv -> real(eltype(ket(pv))) === Float32, p.pvs)
+            prec = Dict("f64" => 0, "f32" => 1, "bf16" => 2, "mixed" => 3)[get(alg.kwargs, :precision,
+                single ? "f32" : "f64")]
             tol = something(get(alg.kwargs, :tol, nothing), -1.0)
             opts = BPOpts(sched, prec, alg.kwargs.maxiter, 1, tol, C_NULL, 0, 0.0, 0.0, 0, 0, 0)
             iters = Ref{Int32}(0)
