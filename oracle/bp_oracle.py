@@ -413,7 +413,9 @@ def bp_update(g, A, msgs, *, B=None, maxiter, tol=None, schedule="sequential",
                     msgs[de] = new[de]
         else:
             raise ValueError(schedule)
-        mean_diff = diff / len(edge_sequence)
+        # an empty sequence divides 0 by 0: NaN, never <= tol, so the loop runs
+        # maxiter no-op iterations (abstractbeliefpropagationcache.jl:320)
+        mean_diff = diff / len(edge_sequence) if len(edge_sequence) else float("nan")
         if tol is not None and mean_diff <= tol:
             break
     return msgs, it, mean_diff
