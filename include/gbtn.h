@@ -233,7 +233,12 @@ int gbtn_rescale_partitions(gbtn_plan* plan);
 /* Replaces: the network state updated by apply(o, psi; envs, maxdim, cutoff,
  * normalize) (src/apply.jl:97-160, simple_update_bp :33-95) and tebd
  * (src/tebd.jl:2-31).  Site tensors keep their current bond dimensions, which
- * grow up to chi_max; the graph descriptor's edge_dim gives the initial ones. */
+ * grow up to chi_max; the graph descriptor's edge_dim gives the initial ones.
+ * With complex_values set in the descriptor, tensors, gates and environments
+ * are interleaved (re, im) doubles (ComplexF64; e.g. the RandomUnitary gates
+ * of test/test_apply.jl), run by a one-kernel complex path limited to site
+ * tensors of <= 4096 elements (also with the bond at chi_max) and theta
+ * <= 32 x 32; larger gates report GBTN_ERR_UNSUPPORTED. */
 typedef struct gbtn_su gbtn_su;
 int gbtn_su_create(gbtn_ctx* ctx, const gbtn_graph_desc* desc, int32_t chi_max, gbtn_su** out);
 int gbtn_su_destroy(gbtn_su* su);

@@ -993,6 +993,452 @@ __global__ void __launch_bounds__(kSuThreads, 3) su_rebuild_kernel(SuArgs a) {
 }  // namespace
 }  // namespace gbtn
 
+// ---------------------------------------------------------------------------
+// Complex tensors (ComplexF64): the same gate, one CTA per gate in one launch.
+// apply.jl's simple_update_bp with complex arithmetic: Hermitian square roots
+// of the environments (V f(lambda) V^H), Householder reflectors
+// H = I - beta v v^H, theta without conjugation, a one-sided Jacobi SVD with
+// complex rotations, the right factor sqrt(S) V^H, and the inverse-square-root
+// environments absorbed conjugated on the other index, as
+// tensordot(T, conj(s), axes=(leg, 0)).  Limits: site tensors (also with the
+// bond at chi_max) <= 4096 elements, theta <= 32 x 32.
+// ---------------------------------------------------------------------------
+namespace gbtn {
+namespace {
+
+constexpr int kSuZMaxN = 4096;
+constexpr int kSuZMaxTheta = 32;
+constexpr int kZSide = kSuZMaxN + kMaxDeg * 64;  // zdouble per (gate, side) of global scratch
+
+__device__ __forceinline__ zdouble zmul(zdouble a, zdouble b) {
+  return zdouble(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+__device__ __forceinline__ zdouble zcmul(zdouble a, zdouble b) {  // conj(a) b
+  return zdouble(a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re);
+}
+__device__ __forceinline__ zdouble zscale(double s, zdouble a) { return zdouble(s * a.re, s * a.im); }
+__device__ __forceinline__ zdouble zsub(zdouble a, zdouble b) { return zdouble(a.re - b.re, a.im - b.im); }
+__device__ __forceinline__ double zabs2(zdouble a) { return a.re * a.re + a.im * a.im; }
+__device__ __forceinline__ zdouble zwarp_sum(zdouble x) { return zdouble(warp_sum(x.re), warp_sum(x.im)); }
+
+// One-sided Jacobi SVD of X (m x n, m, n <= 32, ld m) with complex rotations:
+// for the pair (i, j) with alpha = |x_i|^2, beta = |x_j|^2, gamma = x_i^H x_j
+// = |gamma| e^{i phi}, zeta = (beta - alpha) / (2 |gamma|),
+// t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)), c = 1 / sqrt(1 + t^2), s = c t:
+//   x_i <- c x_i - s e^{-i phi} x_j,   x_j <- s e^{i phi} x_i + c x_j
+// (the same on the columns of V, which starts as the identity), which makes
+// the pair orthogonal.  Pairs in round-robin rounds of n/2 disjoint pairs, one
+// warp per pair, one row per lane.  On return the columns of X are U S,
+// sig their norms and ord the descending order.
+__device__ void cta_zjacobi(zdouble* X, int m, int n, zdouble* V, double* sig, int* ord, int* flag) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < n * n; i += kSuThreads) V[i] = zdouble(i % n == i / n ? 1.0 : 0.0);
+  __syncthreads();
+  const int n2 = n + (n & 1);
+  for (int sweep = 0; sweep < kSvdMaxSweeps; ++sweep) {
+    if (tid == 0) *flag = 0;
+    __syncthreads();
+    for (int r = 0; r < n2 - 1; ++r) {
+      for (int k = warp; k < n2 / 2; k += kSuWarps) {
+        const int a = k == 0 ? r : (r + k) % (n2 - 1);
+        const int b = k == 0 ? n2 - 1 : (r - k + n2 - 1) % (n2 - 1);
+        const int i = min(a, b), j = max(a, b);
+        if (j >= n) continue;  // the padding column of an odd n
+        const zdouble xi = lane < m ? X[lane + m * i] : zdouble(0.0);
+        const zdouble xj = lane < m ? X[lane + m * j] : zdouble(0.0);
+        const double al = warp_sum(zabs2(xi)), be = warp_sum(zabs2(xj));
+        const zdouble ga = zwarp_sum(zcmul(xi, xj));
+        const double ag = sqrt(zabs2(ga));
+        if (ag > kJacobiTol * sqrt(al * be) && al > kJacobiTiny && be > kJacobiTiny) {
+          const double z = (be - al) / (2.0 * ag);
+          const double t = (z >= 0.0 ? 1.0 : -1.0) / (fabs(z) + sqrt(1.0 + z * z));
+          const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+          const zdouble se(s * ga.re / ag, s * ga.im / ag), sec(se.re, -se.im);
+          if (lane < m) {
+            X[lane + m * i] = zsub(zscale(c, xi), zmul(sec, xj));
+            X[lane + m * j] = zmul(se, xi) + zscale(c, xj);
+          }
+          if (lane < n) {
+            const zdouble vi = V[lane + n * i], vj = V[lane + n * j];
+            V[lane + n * i] = zsub(zscale(c, vi), zmul(sec, vj));
+            V[lane + n * j] = zmul(se, vi) + zscale(c, vj);
+          }
+          if (lane == 0) *flag = 1;
+        }
+      }
+      __syncthreads();
+    }
+    const int rotated = *flag;
+    __syncthreads();
+    if (!rotated) break;
+  }
+  for (int i = warp; i < n; i += kSuWarps) {
+    const zdouble x = lane < m ? X[lane + m * i] : zdouble(0.0);
+    const double s2 = warp_sum(zabs2(x));
+    if (lane == 0) sig[i] = sqrt(s2);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int i = 0; i < n; ++i) ord[i] = i;
+    for (int i = 1; i < n; ++i) {  // stable insertion sort, descending
+      const int o = ord[i];
+      int q = i;
+      while (q > 0 && sig[ord[q - 1]] < sig[o]) {
+        ord[q] = ord[q - 1];
+        --q;
+      }
+      ord[q] = o;
+    }
+  }
+  __syncthreads();
+}
+
+// sqrt and inverse sqrt of the Hermitian part of a chi x chi message
+// (map_eigvals, apply.jl:9-25): eigenvalues sorted by magnitude, the tail
+// whose summed magnitude is within 10 eps of the total dropped.
+__device__ void cta_zenv_sqrt(const zdouble* env, int chi, zdouble* S, zdouble* Si, zdouble* A, zdouble* V,
+                              double* sig, int* ord, int* flag) {
+  const int tid = threadIdx.x;
+  for (int i = tid; i < chi * chi; i += kSuThreads) {
+    const int b = i % chi, a = i / chi;
+    const zdouble x = env[b + chi * a], y = env[a + chi * b];
+    A[i] = zdouble(0.5 * (x.re + y.re), 0.5 * (x.im - y.im));
+  }
+  __syncthreads();
+  cta_zjacobi(A, chi, chi, V, sig, ord, flag);
+  __shared__ int s_keep;
+  if (tid == 0) {
+    double tot = 0.0;
+    for (int j = 0; j < chi; ++j) tot += sig[j];
+    if (tot == 0.0) tot = 1.0;
+    int k = chi;
+    double disc = 0.0;
+    while (k > 1 && disc + sig[ord[k - 1]] <= 10.0 * 2.220446049250313e-16 * tot) {
+      disc += sig[ord[k - 1]];
+      --k;
+    }
+    s_keep = k;
+  }
+  __syncthreads();
+  const int k = s_keep;
+  for (int i = tid; i < chi * chi; i += kSuThreads) {
+    const int b = i % chi, a = i / chi;
+    zdouble s(0.0), si(0.0);
+    for (int q = 0; q < k; ++q) {
+      const int o = ord[q];
+      const zdouble vv = zmul(V[b + chi * o], zdouble(V[a + chi * o].re, -V[a + chi * o].im));
+      const double e = sqrt(sig[o]);
+      s = s + zscale(e, vv);
+      si = si + zscale(1.0 / e, vv);
+    }
+    S[i] = s;
+    Si[i] = si;
+  }
+  __syncthreads();
+}
+
+// Householder QR of W (m x n, ld m), r = min(m, n) reflectors: column j of W
+// becomes v_j (v_j[j] = x_j + e^{i arg x_j} |x|), beta[j] = 1 / (|x| (|x| + |x_j|))
+// (0 for a zero column), R (r x n, ld r) the upper triangle, R_jj = -e^{i arg x_j} |x|.
+__device__ void cta_zqr(zdouble* W, int m, int n, zdouble* R, double* beta, double* red) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int r = min(m, n);
+  for (int i = tid; i < r * n; i += kSuThreads) R[i] = zdouble(0.0);
+  __shared__ double s_beta;
+  for (int j = 0; j < r; ++j) {
+    double s2 = 0.0;
+    for (int i = j + tid; i < m; i += kSuThreads) s2 += zabs2(W[i + (size_t)m * j]);
+    s2 = block_sum(s2, red);
+    if (tid == 0) {
+      const double al = sqrt(s2);
+      const zdouble x0 = W[j + (size_t)m * j];
+      const double a0 = sqrt(zabs2(x0));
+      if (al == 0.0) {
+        s_beta = 0.0;
+        R[j + r * j] = zdouble(0.0);
+      } else {
+        const zdouble ph = a0 > 0.0 ? zdouble(x0.re / a0, x0.im / a0) : zdouble(1.0);
+        W[j + (size_t)m * j] = x0 + zscale(al, ph);
+        s_beta = 1.0 / (al * (al + a0));
+        R[j + r * j] = zscale(-al, ph);
+      }
+      beta[j] = s_beta;
+    }
+    __syncthreads();
+    const double bj = s_beta;
+    for (int c = j + 1 + warp; c < n; c += kSuWarps) {
+      zdouble* y = W + (size_t)m * c;
+      if (bj != 0.0) {
+        const zdouble* v = W + (size_t)m * j;
+        zdouble w(0.0);
+        for (int i = j + lane; i < m; i += 32) w = w + zcmul(v[i], y[i]);
+        w = zscale(bj, zwarp_sum(w));
+        for (int i = j + lane; i < m; i += 32) y[i] = zsub(y[i], zmul(w, v[i]));
+      }
+      if (lane == 0) R[j + r * c] = y[j];
+    }
+    __syncthreads();
+  }
+}
+
+// Y (m x nc, ld m) <- H_0 ... H_{r-1} Y with the reflectors of cta_zqr.
+__device__ void cta_zapply_q(const zdouble* refl, const double* beta, int m, int r, zdouble* Y, int nc) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int jr = r - 1; jr >= 0; --jr) {
+    const double bj = beta[jr];
+    if (bj != 0.0) {
+      const zdouble* v = refl + (size_t)jr * m;
+      for (int c = warp; c < nc; c += kSuWarps) {
+        zdouble* y = Y + (size_t)c * m;
+        zdouble w(0.0);
+        for (int i = jr + lane; i < m; i += 32) w = w + zcmul(v[i], y[i]);
+        w = zscale(bj, zwarp_sum(w));
+        for (int i = jr + lane; i < m; i += 32) y[i] = zsub(y[i], zmul(w, v[i]));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__device__ bool zsite_of(const SuArgs& a, const SuJob& job, int side, int& x, SideShape& h) {
+  x = side ? job.v : job.u;
+  side_shape(a, x, side ? job.pv : job.pu, h);
+  const int ce = h.chi[h.p];
+  const int r = min(h.m, h.d * ce);
+  return h.n <= kSuZMaxN && h.m * h.d * a.chimax <= kSuZMaxN && h.d * ce <= 32 && r * h.d <= kSuZMaxTheta &&
+         h.k <= kMaxDeg;
+}
+
+__global__ void __launch_bounds__(kSuThreads, 1) su_gate_z_kernel(SuArgs a, zdouble* zscr) {
+  extern __shared__ __align__(16) double smem[];
+  zdouble* B0 = reinterpret_cast<zdouble*>(smem);
+  zdouble* B1 = B0 + kSuZMaxN;
+  zdouble* RS[2] = {B1 + kSuZMaxN, B1 + kSuZMaxN + 1024};  // R of each side, r x (d chi)
+  zdouble* EM = RS[1] + 1024;                              // 64: environment work
+  zdouble* EV = EM + 64;                                   // 64
+  zdouble* ES = EV + 64;                                   // 64: sqrt(env), then the rebuild's matrix
+  zdouble* UU = ES + 64;                                   // 32 x 8: kept left factor
+  zdouble* VV = UU + 256;                                  // 32 x 8: kept right factor
+  double* sig = reinterpret_cast<double*>(VV + 256);       // 64
+  double* sq = sig + 64;                                   // 64: sqrt of the kept singular values
+  double* beta = sq + 64;                                  // 2 x 32
+  double* red = beta + 64;                                 // 32
+  int* ord = reinterpret_cast<int*>(red + 32);             // 64
+  __shared__ int s_flag, s_k;
+  __shared__ double s_scale;
+  const int j = blockIdx.x, tid = threadIdx.x;
+  if (j >= a.njobs) return;
+  const SuJob job = a.jobs[j];
+  int xs[2];
+  SideShape hs[2];
+  const bool ok0 = zsite_of(a, job, 0, xs[0], hs[0]), ok1 = zsite_of(a, job, 1, xs[1], hs[1]);
+  if (!ok0 || !ok1) {
+    if (tid == 0) atomicExch(a.status, 1);
+    return;
+  }
+  zdouble* tens = reinterpret_cast<zdouble*>(a.tens);
+  const zdouble* envs = reinterpret_cast<const zdouble*>(a.envs);
+  zdouble* gscr = zscr + (size_t)j * 2 * kZSide;
+  const int ce = hs[0].chi[hs[0].p];
+  int rr[2];
+  // ---- per side: sqrt environments, matricise, QR ----
+  for (int side = 0; side < 2; ++side) {
+    const SideShape& h = hs[side];
+    const int x = xs[side];
+    zdouble* refl = gscr + side * kZSide;
+    zdouble* sis = refl + kSuZMaxN;
+    const zdouble* src = tens + a.cap_off[x];
+    for (int i = tid; i < h.n; i += kSuThreads) B0[i] = src[i];
+    __syncthreads();
+    zdouble* cur = B0;
+    zdouble* nxt = B1;
+    if (envs) {
+      int st = h.d;
+      for (int q = 0; q < h.k; ++q) {
+        if (q != h.p) {
+          const int f = a.leg_edge[a.leg_ptr[x] + q];
+          const int de_in = a.edge_u[f] == x ? 2 * f + 1 : 2 * f;
+          cta_zenv_sqrt(envs + (size_t)de_in * a.chimax * a.chimax, h.chi[q], ES, sis + q * 64, EM, EV, sig, ord,
+                        &s_flag);
+          absorb_any<zdouble>(h.chi[q], cur, nxt, h.n, st, ES, tid, kSuThreads);
+          __syncthreads();
+          zdouble* t = cur;
+          cur = nxt;
+          nxt = t;
+        }
+        st *= h.chi[q];
+      }
+    }
+    for (int i = tid; i < h.n; i += kSuThreads) {
+      int row, s, b;
+      split_index(h, h.chi, i, row, s, b);
+      nxt[row + (size_t)h.m * (s + h.d * b)] = cur[i];
+    }
+    __syncthreads();
+    const int ncol = h.d * ce, r = min(h.m, ncol);
+    cta_zqr(nxt, h.m, ncol, RS[side], beta + 32 * side, red);
+    for (int i = tid; i < h.m * r; i += kSuThreads) refl[i] = nxt[i];
+    rr[side] = r;
+    __syncthreads();
+  }
+  // ---- theta = R_u R_v over the bond, then the gate ----
+  const int du = hs[0].d, dv = hs[1].d, ru = rr[0], rv = rr[1];
+  const int mt = ru * du, nt = dv * rv;
+  const zdouble* RU = RS[0];
+  const zdouble* RV = RS[1];
+  for (int i = tid; i < mt * nt; i += kSuThreads) {
+    const int row = i % mt, col = i / mt;
+    const int iu = row % ru, su_ = row / ru, sv_ = col % dv, iv = col / dv;
+    zdouble acc(0.0);
+    for (int e = 0; e < ce; ++e) acc = mac(RU[iu + ru * (su_ + du * e)], RV[iv + rv * (sv_ + dv * e)], acc);
+    B1[i] = acc;
+  }
+  __syncthreads();
+  const zdouble* G = reinterpret_cast<const zdouble*>(a.gates) + (size_t)a.gate_stride * j;
+  const int D = du * dv;
+  const bool wide = mt < nt;
+  for (int i = tid; i < mt * nt; i += kSuThreads) {
+    const int row = i % mt, col = i / mt;
+    const int iu = row % ru, spu = row / ru, spv = col % dv, iv = col / dv;
+    zdouble acc(0.0);
+    for (int sv_ = 0; sv_ < dv; ++sv_)
+      for (int su_ = 0; su_ < du; ++su_)
+        acc = mac(G[(spu + du * spv) + D * (su_ + du * sv_)], B1[(iu + ru * su_) + mt * (sv_ + dv * iv)], acc);
+    if (wide)  // decompose theta^H (rows >= columns); its factors swap roles
+      B0[col + nt * row] = zdouble(acc.re, -acc.im);
+    else
+      B0[i] = acc;
+  }
+  __syncthreads();
+  const int M = wide ? nt : mt, N = wide ? mt : nt;
+  cta_zjacobi(B0, M, N, B1, sig, ord, &s_flag);
+  // theta = U S V^H: not wide, U = columns of B0 / sig, V = B1; wide (theta^H =
+  // U' S V'^H), U = V' = B1 and V = U' = columns of B0 / sig
+  if (tid == 0) {
+    const int nsv = N;
+    int n = nsv;
+    double te = 0.0, scale = 0.0;
+    for (int i = 0; i < nsv; ++i) scale += sig[i] * sig[i];
+    if (a.maxdim > 0)
+      while (n > a.maxdim) {
+        te += sig[ord[n - 1]] * sig[ord[n - 1]];
+        --n;
+      }
+    if (scale == 0.0) scale = 1.0;
+    if (a.cutoff >= 0.0)
+      while (n > 1 && te + sig[ord[n - 1]] * sig[ord[n - 1]] <= a.cutoff * scale) {
+        te += sig[ord[n - 1]] * sig[ord[n - 1]];
+        --n;
+      }
+    if (n < 1) n = 1;
+    s_k = n;
+    if (a.truncerr) a.truncerr[j] = te / scale;
+    if (a.svals)
+      for (int i = 0; i < a.maxdim; ++i) a.svals[(size_t)j * a.maxdim + i] = i < n ? sig[ord[i]] : 0.0;
+    a.edim[job.e] = n;
+  }
+  __syncthreads();
+  const int kk = s_k;
+  for (int i = tid; i < mt * kk; i += kSuThreads) {
+    const int row = i % mt, b = i / mt, o = ord[b];
+    const double sg = sig[o] > 0.0 ? sig[o] : 1.0;
+    UU[i] = wide ? B1[row + mt * o] : zscale(1.0 / sg, B0[row + mt * o]);
+  }
+  for (int i = tid; i < nt * kk; i += kSuThreads) {
+    const int row = i % nt, b = i / nt, o = ord[b];
+    const double sg = sig[o] > 0.0 ? sig[o] : 1.0;
+    VV[i] = wide ? zscale(1.0 / sg, B0[row + nt * o]) : B1[row + nt * o];
+  }
+  if (tid < kk) sq[tid] = sqrt(sig[ord[tid]]);
+  __syncthreads();
+  // ---- rebuild each side: Q (core), layout, inverse-sqrt environments, normalise ----
+  for (int side = 0; side < 2; ++side) {
+    const SideShape& h = hs[side];
+    const int x = xs[side];
+    const zdouble* refl = gscr + side * kZSide;
+    const zdouble* sis = refl + kSuZMaxN;
+    int chi2[kMaxDeg];
+    for (int q = 0; q < h.k; ++q) chi2[q] = h.chi[q];
+    chi2[h.p] = kk;
+    const int m = h.m, d = h.d, nc = d * kk, r = rr[side];
+    int n2 = d;
+    for (int q = 0; q < h.k; ++q) n2 *= chi2[q];
+    // core: left U sqrt(S) [(t, s), b]; right (sqrt(S) V^H)^T: conj(V)[(s, t), b] sqrt(S)
+    for (int i = tid; i < m * nc; i += kSuThreads) {
+      const int row = i % m, col = i / m, s = col % d, b = col / d;
+      zdouble v(0.0);
+      if (row < r) {
+        if (side == 0) {
+          v = zscale(sq[b], UU[(row + ru * s) + mt * b]);
+        } else {
+          const zdouble w = VV[(s + dv * row) + nt * b];
+          v = zscale(sq[b], zdouble(w.re, -w.im));
+        }
+      }
+      B0[i] = v;
+    }
+    __syncthreads();
+    cta_zapply_q(refl, beta + 32 * side, m, r, B0, nc);
+    for (int i = tid; i < n2; i += kSuThreads) {
+      int row, s, b;
+      split_index(h, chi2, i, row, s, b);
+      B1[i] = B0[row + (size_t)m * (s + d * b)];
+    }
+    __syncthreads();
+    zdouble* cur = B1;
+    zdouble* nxt = B0;
+    if (envs) {
+      int st = d;
+      for (int q = 0; q < h.k; ++q) {
+        if (q != h.p) {
+          const int c = chi2[q];
+          const zdouble* si = sis + q * 64;
+          // out[b] = sum_a in[a] conj(Si[a, b]): the matrix conj(Si)^T
+          for (int i = tid; i < c * c; i += kSuThreads) {
+            const int bb = i % c, aa = i / c;
+            const zdouble w = si[aa + c * bb];
+            ES[i] = zdouble(w.re, -w.im);
+          }
+          __syncthreads();
+          absorb_any<zdouble>(c, cur, nxt, n2, st, ES, tid, kSuThreads);
+          __syncthreads();
+          zdouble* t = cur;
+          cur = nxt;
+          nxt = t;
+        }
+        st *= chi2[q];
+      }
+    }
+    double s2 = 0.0;
+    if (a.normalize)
+      for (int i = tid; i < n2; i += kSuThreads) s2 += zabs2(cur[i]);
+    s2 = block_sum(s2, red);
+    if (tid == 0) s_scale = (a.normalize && s2 > 0.0) ? 1.0 / sqrt(s2) : 1.0;
+    __syncthreads();
+    zdouble* dst = tens + a.cap_off[x];
+    for (int i = tid; i < n2; i += kSuThreads) dst[i] = zscale(s_scale, cur[i]);
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+size_t su_z_smem() {
+  return sizeof(zdouble) * (2 * (size_t)kSuZMaxN + 2048 + 3 * 64 + 512) + sizeof(double) * (64 * 3 + 32) +
+         sizeof(int) * 64;
+}
+constexpr size_t kSuZScratch = 2 * (size_t)kZSide;  // zdouble per gate
+
+void su_launch_z(const SuArgs& a, zdouble* zscr, cudaStream_t s) {
+  if (a.njobs == 0) return;
+  const size_t sm = su_z_smem();
+  GBTN_CUDA(cudaFuncSetAttribute(su_gate_z_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  su_gate_z_kernel<<<a.njobs, kSuThreads, sm, s>>>(a, zscr);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+}  // namespace gbtn
+
 namespace gbtn {
 
 constexpr size_t kSuSideStride = kSideStride;
@@ -1032,6 +1478,8 @@ struct gbtn_su {
   gbtn_ctx* ctx = nullptr;
   cudaStream_t stream = nullptr;
   int nv = 0, ne = 0, chimax = 0;
+  bool cplx = false;  // complex tensors: interleaved (re, im) doubles
+  int es() const { return cplx ? 2 : 1; }
   std::vector<int> eu, ev, leg_ptr, leg_edge, dsite, edim;
   std::vector<long long> cap_off;
   long long cap_total = 0;
@@ -1087,13 +1535,10 @@ extern "C" {
 int gbtn_su_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, int32_t chi_max, gbtn_su** out) {
   if (!ctx || !g || !out) return GBTN_ERR_INVALID;
   *out = nullptr;
-  if (g->complex_values) {
-    gbtn::set_ctx_error(ctx, "the simple update takes real tensors");
-    return GBTN_ERR_UNSUPPORTED;
-  }
   try {
     auto S = std::make_unique<gbtn_su>();
     S->ctx = ctx;
+    S->cplx = g->complex_values != 0;
     S->stream = gbtn::ctx_stream(ctx);
     S->nv = g->nv;
     S->ne = g->ne;
@@ -1130,8 +1575,9 @@ int gbtn_su_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, int32_t chi_max, gbt
     S->d_cap_off = dev_upload(S->cap_off, S->stream);
     std::vector<int> zero(1, 0);
     S->d_status = dev_upload(zero, S->stream);
-    GBTN_CUDA(cudaMalloc(&S->d_tens, sizeof(double) * std::max<long long>(S->cap_total, 1)));
-    GBTN_CUDA(cudaMemsetAsync(S->d_tens, 0, sizeof(double) * std::max<long long>(S->cap_total, 1), S->stream));
+    GBTN_CUDA(cudaMalloc(&S->d_tens, sizeof(double) * S->es() * std::max<long long>(S->cap_total, 1)));
+    GBTN_CUDA(cudaMemsetAsync(S->d_tens, 0, sizeof(double) * S->es() * std::max<long long>(S->cap_total, 1),
+                              S->stream));
     GBTN_CUDA(cudaStreamSynchronize(S->stream));
     *out = S.release();
     return GBTN_OK;
@@ -1167,8 +1613,8 @@ int gbtn_su_set_factors(gbtn_su* S, const double* ket) {
     long long off = 0;
     for (int v = 0; v < S->nv; ++v) {
       const long long n = su_size(S, v);
-      GBTN_CUDA(cudaMemcpyAsync(S->d_tens + S->cap_off[v], ket + off, sizeof(double) * n, cudaMemcpyHostToDevice,
-                                S->stream));
+      GBTN_CUDA(cudaMemcpyAsync(S->d_tens + S->es() * S->cap_off[v], ket + S->es() * off,
+                                sizeof(double) * S->es() * n, cudaMemcpyHostToDevice, S->stream));
       off += n;
     }
     GBTN_CUDA(cudaStreamSynchronize(S->stream));
@@ -1184,12 +1630,12 @@ int gbtn_su_get_factors(gbtn_su* S, double* ket, int64_t capacity) {
     su_pull_dims(S);
     long long tot = 0;
     for (int v = 0; v < S->nv; ++v) tot += su_size(S, v);
-    if (tot > capacity) return su_fail(S, GBTN_ERR_INVALID, "simple update: output buffer too small");
+    if (S->es() * tot > capacity) return su_fail(S, GBTN_ERR_INVALID, "simple update: output buffer too small");
     long long off = 0;
     for (int v = 0; v < S->nv; ++v) {
       const long long n = su_size(S, v);
-      GBTN_CUDA(cudaMemcpyAsync(ket + off, S->d_tens + S->cap_off[v], sizeof(double) * n, cudaMemcpyDeviceToHost,
-                                S->stream));
+      GBTN_CUDA(cudaMemcpyAsync(ket + S->es() * off, S->d_tens + S->es() * S->cap_off[v],
+                                sizeof(double) * S->es() * n, cudaMemcpyDeviceToHost, S->stream));
       off += n;
     }
     GBTN_CUDA(cudaStreamSynchronize(S->stream));
@@ -1221,15 +1667,16 @@ int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const doubl
       if (j == 0) D = dd;
       if (per_gate && dd != D) return su_fail(S, GBTN_ERR_INVALID, "simple update: per-gate operators need equal sizes");
     }
-    const long long gsz = (long long)D * D;
+    const long long gsz = (long long)D * D;  // elements (complex plans: interleaved pairs)
+    const int es = S->es();
     double* d_gates = nullptr;
-    GBTN_CUDA(cudaMalloc(&d_gates, sizeof(double) * gsz * (per_gate ? n_gates : 1)));
+    GBTN_CUDA(cudaMalloc(&d_gates, sizeof(double) * es * gsz * (per_gate ? n_gates : 1)));
     std::unique_ptr<double, decltype(&cudaFree)> g_guard(d_gates, cudaFree);
-    GBTN_CUDA(cudaMemcpyAsync(d_gates, gates, sizeof(double) * gsz * (per_gate ? n_gates : 1),
+    GBTN_CUDA(cudaMemcpyAsync(d_gates, gates, sizeof(double) * es * gsz * (per_gate ? n_gates : 1),
                               cudaMemcpyHostToDevice, s));
     double* d_envs = nullptr;
     if (envs) {
-      const long long ne2 = 2LL * S->ne * S->chimax * S->chimax;
+      const long long ne2 = es * 2LL * S->ne * S->chimax * S->chimax;
       GBTN_CUDA(cudaMalloc(&d_envs, sizeof(double) * std::max<long long>(ne2, 1)));
       GBTN_CUDA(cudaMemcpyAsync(d_envs, envs, sizeof(double) * ne2, cudaMemcpyHostToDevice, s));
     }
@@ -1258,8 +1705,12 @@ int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const doubl
     batches.push_back({start, n_gates});
     maxb = std::max(maxb, n_gates - start);
     double* d_js = nullptr;
-    GBTN_CUDA(cudaMalloc(&d_q, sizeof(double) * (size_t)maxb * 2 * gbtn::kSuSideStride));
-    GBTN_CUDA(cudaMalloc(&d_js, sizeof(double) * (size_t)maxb * gbtn::kSuJobStride));
+    if (S->cplx) {  // per gate: both sides' reflectors and inverse-sqrt environments
+      GBTN_CUDA(cudaMalloc(&d_q, sizeof(gbtn::zdouble) * (size_t)maxb * gbtn::kSuZScratch));
+    } else {
+      GBTN_CUDA(cudaMalloc(&d_q, sizeof(double) * (size_t)maxb * 2 * gbtn::kSuSideStride));
+      GBTN_CUDA(cudaMalloc(&d_js, sizeof(double) * (size_t)maxb * gbtn::kSuJobStride));
+    }
     std::unique_ptr<double, decltype(&cudaFree)> q_guard(d_q, cudaFree), js_guard(d_js, cudaFree);
     // theta is at most (d_u min(m_u, d_u chi)) x (d_v min(m_v, d_v chi)) <= dmax^2 chi_max
     int dmax = 1;
@@ -1278,8 +1729,8 @@ int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const doubl
       a.cap_off = S->d_cap_off;
       a.tens = S->d_tens;
       a.envs = d_envs;
-      a.gates = d_gates + (per_gate ? gsz * b.first : 0);
-      a.gate_stride = per_gate ? gsz : 0;
+      a.gates = d_gates + (per_gate ? es * gsz * b.first : 0);
+      a.gate_stride = per_gate ? gsz : 0;  // elements
       a.maxdim = md;
       a.cutoff = cutoff;
       a.normalize = normalize;
@@ -1290,7 +1741,10 @@ int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const doubl
       a.truncerr = d_te + b.first;
       a.svals = d_sv + (size_t)b.first * md;
       a.status = S->d_status;
-      gbtn::su_launch(a, s);
+      if (S->cplx)
+        gbtn::su_launch_z(a, reinterpret_cast<gbtn::zdouble*>(d_q), s);
+      else
+        gbtn::su_launch(a, s);
     }
     int status = 0;
     GBTN_CUDA(cudaMemcpyAsync(&status, S->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1298,7 +1752,11 @@ int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const doubl
     GBTN_CUDA(cudaMemcpyAsync(te.data(), d_te, sizeof(double) * n_gates, cudaMemcpyDeviceToHost, s));
     GBTN_CUDA(cudaMemcpyAsync(sv.data(), d_sv, sizeof(double) * sv.size(), cudaMemcpyDeviceToHost, s));
     GBTN_CUDA(cudaStreamSynchronize(s));
-    if (status) return su_fail(S, GBTN_ERR_UNSUPPORTED, "simple update: a gate exceeds the kernel limits (site tensor > 8192 elements or theta > 64 x 64)");
+    if (status)
+      return su_fail(S, GBTN_ERR_UNSUPPORTED,
+                     S->cplx ? "simple update: a gate exceeds the complex kernel's limits (site tensor, also with the "
+                               "bond at chi_max, > 4096 elements, or theta > 32 x 32)"
+                             : "simple update: a gate exceeds the kernel limits (site tensor > 8192 elements or theta > 64 x 64)");
     if (truncerr) std::copy(te.begin(), te.end(), truncerr);
     if (svals)
       for (int j = 0; j < n_gates; ++j)

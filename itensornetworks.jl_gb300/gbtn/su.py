@@ -4,7 +4,8 @@
 ``chi_max`` as two-site gates are applied.  Gates are (du*dv) x (du*dv)
 matrices acting on an edge (u, v) = network.edges[e], row s'_u + du*s'_v,
 column s_u + du*s_v.  Every numerical step (sqrt environments, QR, gate, SVD,
-truncation, reassembly) runs in libgbtn in FP64."""
+truncation, reassembly) runs in libgbtn in FP64; complex networks (complex
+tensors, gates or environments, e.g. random unitaries) run complex FP64."""
 from __future__ import annotations
 
 import ctypes as C
@@ -17,19 +18,22 @@ from .network import TensorNetwork
 
 
 class SimpleUpdateState:
-    def __init__(self, tn: TensorNetwork, chi_max: int, ctx=None):
+    def __init__(self, tn: TensorNetwork, chi_max: int, ctx=None, complex_values=None):
         if tn.tensors is None:
             raise ValueError("the network has no tensors")
         self.ctx = ctx or _lib.default_context()
         self.lib = self.ctx.lib
         self.tn = tn.copy()
+        self.complex = tn.is_complex if complex_values is None else bool(complex_values)
+        self.dtype = np.complex128 if self.complex else np.float64
+        self.tn.tensors = [np.asarray(t, dtype=self.dtype) for t in self.tn.tensors]
         self.chi_max = int(chi_max)
         desc, keep = self.tn.graph_desc()
         h = C.c_void_p()
         check(self.ctx.handle, self.lib.gbtn_su_create(self.ctx.handle, C.byref(desc), self.chi_max, C.byref(h)))
         self.handle = h
         flat = self.tn.flat()
-        check(self.ctx.handle, self.lib.gbtn_su_set_factors(self.handle, dptr(flat)))
+        check(self.ctx.handle, self.lib.gbtn_su_set_factors(self.handle, dptr(flat.view(np.float64))))
 
     def edge_dims(self):
         out = np.zeros(max(self.tn.ne, 1), dtype=np.int32)
@@ -42,8 +46,9 @@ class SimpleUpdateState:
         net = TensorNetwork(self.tn.nv, self.tn.edges, self.tn.site_dims, dims, None, self.tn.legs,
                             self.tn.vertex_network, self.tn.n_networks)
         n = sum(net.size(v) for v in range(net.nv))
-        out = np.empty(max(n, 1))
-        check(self.ctx.handle, self.lib.gbtn_su_get_factors(self.handle, dptr(out), n))
+        out = np.empty(max(n, 1), dtype=self.dtype)
+        buf = out.view(np.float64)
+        check(self.ctx.handle, self.lib.gbtn_su_get_factors(self.handle, dptr(buf), buf.size))
         net.tensors = net.unflat(out[:n])
         return net
 
@@ -54,23 +59,26 @@ class SimpleUpdateState:
         edges = np.ascontiguousarray(edges, dtype=np.int32)
         n = len(edges)
         shared = not isinstance(gates, (list, tuple))
-        if shared:
-            g = np.ascontiguousarray(np.asarray(gates, float).reshape(-1, order="F"))
-        else:
-            g = np.ascontiguousarray(np.concatenate([np.asarray(x, float).reshape(-1, order="F") for x in gates]))
+        glist = [gates] if shared else list(gates)
+        if not self.complex and (any(np.iscomplexobj(x) for x in glist)
+                                 or (envs is not None and any(np.iscomplexobj(m) for m in envs))):
+            raise ValueError("complex gates or environments need a complex state (complex_values=True)")
+        dt = self.dtype
+        g = np.ascontiguousarray(np.concatenate([np.asarray(x, dt).reshape(-1, order="F") for x in glist]))
         env_arr = None
         if envs is not None:
             cm = self.chi_max
-            env_arr = np.zeros(2 * self.tn.ne * cm * cm)
+            env_arr = np.zeros(2 * self.tn.ne * cm * cm, dtype=dt)
             for de, m in enumerate(envs):
                 c = m.shape[0]
-                env_arr[de * cm * cm:de * cm * cm + c * c] = np.asarray(m, float).reshape(-1, order="F")
+                env_arr[de * cm * cm:de * cm * cm + c * c] = np.asarray(m, dt).reshape(-1, order="F")
         md = int(maxdim) if maxdim else self.chi_max
         te = np.zeros(max(n, 1))
         sv = np.zeros(max(n * md, 1))
         check(self.ctx.handle, self.lib.gbtn_su_apply(
-            self.handle, n, iptr(edges), dptr(g), 0 if shared else 1,
-            None if env_arr is None else dptr(env_arr), md, -1.0 if cutoff is None else float(cutoff),
+            self.handle, n, iptr(edges), dptr(g.view(np.float64)), 0 if shared else 1,
+            None if env_arr is None else dptr(env_arr.view(np.float64)), md,
+            -1.0 if cutoff is None else float(cutoff),
             1 if normalize else 0, dptr(te), dptr(sv)))
         return te[:n], sv[:n * md].reshape(n, md)
 
@@ -93,7 +101,8 @@ def apply(gate, psi: TensorNetwork, edge, envs=None, maxdim=None, cutoff=None, n
     singular_values= and truncation_error= like the reference's callback."""
     cm = chi_max or max([maxdim or 0] + list(psi.edge_dims) + [psi.site_dims[0] * max(psi.edge_dims or [1])])
     cm = min(cm, 8)
-    st = SimpleUpdateState(psi, cm)
+    cplx = psi.is_complex or np.iscomplexobj(gate) or (envs is not None and any(np.iscomplexobj(m) for m in envs))
+    st = SimpleUpdateState(psi, cm, complex_values=cplx)
     te, sv = st.apply(gate, [edge], envs=envs, maxdim=maxdim or cm, cutoff=cutoff, normalize=normalize)
     if callback is not None:
         k = int(np.count_nonzero(sv[0]))

@@ -135,7 +135,7 @@ def test_complex_paths_outside_fp64_are_unsupported():
     with pytest.raises(gbtn.Unsupported):
         bpc.rescale_partitions()
     with pytest.raises(gbtn.Unsupported):
-        gbtn.SimpleUpdateState(tn, 4)
+        bpc.energy2([(1.0, O.SZ)])
 
 
 def test_complex_two_site_rdms_and_expect2():
