@@ -170,8 +170,9 @@ struct GradOpts
 end
 
 # Ket tensors of a plain ITensorNetwork in the ABI layout (vertex order of
-# `vertices(psi)`, edges with src < dst, legs in each tensor's index order).
-function pack_state(psi)
+# `vertices(psi)`, edges with src < dst, legs in each tensor's index order),
+# as ComplexF64 when `cplx` (interleaved pairs in the library) else Float64.
+function pack_state(psi; cplx=false)
     vs = collect(ITensorNetworks.vertices(psi))
     vid = Dict(v => i - 1 for (i, v) in enumerate(vs))
     es = collect(ITensorNetworks.edges(psi))
@@ -179,7 +180,8 @@ function pack_state(psi)
     eu = Int32[vid[ITensorNetworks.src(e)] for e in es]
     ev = Int32[vid[ITensorNetworks.dst(e)] for e in es]
     edim = Int32[length(l) for l in links]
-    sdim, leg_ptr, leg_edge, data, sites = Int32[], Int32[0], Int32[], Float64[], Index[]
+    sdim, leg_ptr, leg_edge, sites = Int32[], Int32[0], Int32[], Index[]
+    data = cplx ? ComplexF64[] : Float64[]
     for v in vs
         t = psi[v]
         s = only(filter(i -> !(i in links), inds(t)))
@@ -200,14 +202,20 @@ Two-site `gates` (ITensors acting on the site indices of neighbouring vertices)
 applied in order by the GPU simple update; `callback(; singular_values,
 truncation_error)` is called per gate as in src/apply.jl:97-146.  `envs`:
 `nothing` (tebd) or a Dict from QuotientEdge to the converged message.
+Complex gates (e.g. `op("RandomUnitary", ...)`), states or environments run
+the library's complex path (complex_values = 1).
 """
 function ITensorNetworks.apply(::Algorithm"gb300", gates::Vector{ITensor}, psi; maxdim, cutoff=nothing,
                                normalize=true, envs=nothing, callback=(; kws...) -> nothing)
-    p = pack_state(psi)
+    cplx = any(g -> eltype(g) <: Complex, gates) ||
+           any(v -> eltype(psi[v]) <: Complex, ITensorNetworks.vertices(psi)) ||
+           (envs !== nothing && any(m -> eltype(only(m)) <: Complex, values(envs)))
+    T = cplx ? ComplexF64 : Float64
+    p = pack_state(psi; cplx)
     ctx = context()
     chimax = max(maxdim, maximum(p.edim))
     eidx = Int32[]
-    gdata = Float64[]
+    gdata = T[]
     for g in gates
         vs = [v for v in p.vs if !isempty(intersect(inds(g), [p.sites[findfirst(==(v), p.vs)]]))]
         su, sv = p.sites[findfirst(==(vs[1]), p.vs)], p.sites[findfirst(==(vs[2]), p.vs)]
@@ -220,15 +228,15 @@ function ITensorNetworks.apply(::Algorithm"gb300", gates::Vector{ITensor}, psi; 
     end
     GC.@preserve p eidx gdata begin
         desc = GraphDesc(length(p.vs), length(p.es), pointer(p.eu), pointer(p.ev), pointer(p.edim),
-            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0, 0)
+            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0, cplx ? 1 : 0)
         h = Ref{Ptr{Cvoid}}(C_NULL)
         check(ctx, ccall((:gbtn_su_create, libgbtn), Cint, (Ptr{Cvoid}, Ref{GraphDesc}, Int32, Ref{Ptr{Cvoid}}),
             ctx, desc, chimax, h))
         try
-            check(ctx, ccall((:gbtn_su_set_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Float64}), h[], p.data))
+            check(ctx, ccall((:gbtn_su_set_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), h[], p.data))
             envbuf = C_NULL
             if envs !== nothing
-                envbuf = zeros(2 * length(p.es) * chimax^2)
+                envbuf = zeros(T, 2 * length(p.es) * chimax^2)
                 for (k, e) in enumerate(p.es), (dir, qe) in ((0, e), (1, reverse(e)))
                     M = array(only(envs[qe]))
                     c = size(M, 1)
@@ -240,7 +248,7 @@ function ITensorNetworks.apply(::Algorithm"gb300", gates::Vector{ITensor}, psi; 
             te = zeros(n)
             sv = zeros(n * maxdim)
             check(ctx, ccall((:gbtn_su_apply, libgbtn), Cint,
-                (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Float64}, Int32, Ptr{Float64}, Int32, Float64, Int32,
+                (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Cvoid}, Int32, Ptr{Cvoid}, Int32, Float64, Int32,
                  Ptr{Float64}, Ptr{Float64}),
                 h[], n, eidx, gdata, 1, envbuf, maxdim, something(cutoff, -1.0), normalize ? 1 : 0, te, sv))
             for j in 1:n
@@ -252,9 +260,9 @@ function ITensorNetworks.apply(::Algorithm"gb300", gates::Vector{ITensor}, psi; 
             newlinks = [d == length(l) ? l : Index(Int(d), tags(l)) for (d, l) in zip(dims, p.links)]
             total = sum(Int(p.sdim[i]) * prod(Int(dims[p.leg_edge[q] + 1]) for q in (p.leg_ptr[i] + 1):p.leg_ptr[i + 1];
                                                  init=1) for i in eachindex(p.vs))
-            flat = Vector{Float64}(undef, total)
-            check(ctx, ccall((:gbtn_su_get_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int64),
-                h[], flat, total))
+            flat = Vector{T}(undef, total)
+            check(ctx, ccall((:gbtn_su_get_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Int64),
+                h[], flat, cplx ? 2 * total : total))
             psi = copy(psi)
             off = 0
             for (i, v) in enumerate(p.vs)
