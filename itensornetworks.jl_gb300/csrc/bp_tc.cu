@@ -33,7 +33,8 @@
 //
 // Per vertex: one 16 KB TMA bulk copy of the pre-swizzled BF16 image of Z,
 // 24 tcgen05.mma instructions (4.2 MFLOP) accumulating in FP32 in TMEM (128
-// columns: D1 | D1', then G34 | G12), two MMA round trips, seven CTA barriers,
+// columns: D1 | D1', then G34 | G12) issued by two threads (one per
+// accumulator chain), two MMA round trips, seven CTA barriers,
 // 128 threads.  Four CTAs share an SM (53 KB of shared memory each; the
 // Kronecker products and then T12 share one region), the next vertex's Z is
 // copied while the current one finishes and its messages are loaded into
