@@ -60,8 +60,9 @@ constexpr int kOffT34 = 32768;     // T34 as two 8 KB tiles (s = 0, 1)
 constexpr int kOffPart = 49152;    // cross-warp partial sums: 2 pairs x 4 warps x 64 FP32
 constexpr int kOffMsg = kOffPart + 2048;  // 4 x 64 FP32 incoming messages
 constexpr int kOffRes = kOffMsg + 1024;   // 4 x 64 FP32 outgoing messages
-constexpr int kOffBar = kOffRes + 1024;   // mma bar, TMA bar
-constexpr int kOffTmem = kOffBar + 16;
+constexpr int kOffRec = kOffRes + 1024;   // 3 x 64 B: records of this vertex and the next two (TMA)
+constexpr int kOffBar = kOffRec + 192;    // mma bar, TMA bar, 3 record bars
+constexpr int kOffTmem = kOffBar + 40;
 constexpr int kOffFlag = kOffTmem + 4;
 constexpr int kSmemUsed = kOffFlag + 4;
 constexpr int kSmemBytes = kSmemUsed + 1024;  // room to align the base
@@ -261,6 +262,9 @@ __device__ __forceinline__ void pair_epilogue(uint32_t taddr, const float* Mx, c
 
 // One CTA walks recs[blockIdx.x], recs[blockIdx.x + gridDim.x], ... (one
 // record per vertex of the work list, in list order; Z at zimg + slot * 8192).
+// The records arrive by 64-byte bulk copies two vertices ahead into a ring
+// of three, so no thread reads a record from global memory: a load still in
+// flight would hold up the next CTA barrier.
 // err (device) receives GBTN_ERR_TIMEOUT when a bounded wait gives up; the CTA
 // then drains its own copy and MMAs in flight, frees its TMEM and returns.
 __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
@@ -275,8 +279,10 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
   float* PART = reinterpret_cast<float*>(sm + kOffPart);
   float* MSG = reinterpret_cast<float*>(sm + kOffMsg);
   float* RES = reinterpret_cast<float*>(sm + kOffRes);
+  const TcRec* REC = reinterpret_cast<const TcRec*>(sm + kOffRec);
   uint64_t* mma_bar = reinterpret_cast<uint64_t*>(sm + kOffBar);
   uint64_t* tma_bar = mma_bar + 1;
+  uint64_t* rec_bar = mma_bar + 2;  // [3]
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kOffTmem);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(sm + kOffFlag);
 
@@ -288,6 +294,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
   if (t == 0) {
     tc::mbar_init(mma_bar, 2);  // one commit from each MMA issuer
     tc::mbar_init(tma_bar, 1);
+    for (int k = 0; k < 3; ++k) tc::mbar_init(rec_bar + k, 1);
     tc::fence_mbar_init();
     *abort_flag = 0;
   }
@@ -329,25 +336,55 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     }
     return ok;
   };
+  // record i of this CTA's walk goes to ring entry i % 3 (use i / 3)
+  int rec_pending[3] = {0, 0, 0};
+  uint32_t rec_par[3] = {0, 0, 0};
+  auto issue_rec = [&](int i, int wv) {
+    const int k = i % 3;
+    tc::mbar_expect_tx(rec_bar + k, (uint32_t)sizeof(TcRec));
+    tc::tma_load_1d(sm + kOffRec + k * sizeof(TcRec), recs + wv, (uint32_t)sizeof(TcRec), rec_bar + k);
+    rec_pending[k] = 1;
+    rec_par[k] = (uint32_t)(i / 3) & 1;
+  };
+  auto wait_rec = [&](int i) -> bool {
+    const int k = i % 3;
+    const bool ok = tc::mbar_wait(rec_bar + k, rec_par[k], kWaitNs);
+    if (ok) rec_pending[k] = 0;
+    return ok;
+  };
 
   const int q0 = t, q1 = t + 128;  // this thread's entries of the 4 x 64 message block
   const int e = t & 63;
+  const int G = gridDim.x;
   int w = blockIdx.x;
   float cm0 = 0.f, cm1 = 0.f;  // current vertex's incoming-message entries q0, q1
   int cnet = 0;
-  if (w < nwork) {
-    const TcRec* r = recs + w;
-    if (t == 0) issue_z(r->slot);
-    cnet = r->net;
-    const int c4 = r->chi4;
-    cm0 = padded_msg(msg_in, r->in_off[q0 >> 6], rec_chi(c4, q0 >> 6), e);
-    cm1 = padded_msg(msg_in, r->in_off[q1 >> 6], rec_chi(c4, q1 >> 6), e);
+  if (t == 0 && w < nwork) {
+    issue_rec(0, w);
+    if (w + G < nwork) issue_rec(1, w + G);
+    const bool ok = wait_rec(0);
+    *abort_flag = ok ? 0 : 1;
+    if (ok) issue_z(REC[0].slot);
   }
-  for (; w < nwork; w += gridDim.x) {
-    const TcRec* cr = recs + w;
-    const int out_off_w = cr->out_off[warp];
-    const int out_de_w = cr->out_de[warp];
-    const int cchi4 = cr->chi4;
+  __syncthreads();
+  const bool started = !*abort_flag;  // read by every thread after the barrier: uniform
+  if (w < nwork && started) {
+    const TcRec& r = REC[0];
+    cnet = r.net;
+    const int c4 = r.chi4;
+    cm0 = padded_msg(msg_in, r.in_off[q0 >> 6], rec_chi(c4, q0 >> 6), e);
+    cm1 = padded_msg(msg_in, r.in_off[q1 >> 6], rec_chi(c4, q1 >> 6), e);
+  }
+  // a wait that gives up inside the loop is seen by every thread after the next barrier
+  for (int it = 0; started && w < nwork; w += G, ++it) {
+    const TcRec& cr = REC[it % 3];  // this vertex (complete since the previous iteration)
+    const TcRec& nr = REC[(it + 1) % 3];
+    const int wn = w + G;
+    // the next vertex's record must be here before the barrier below makes it visible
+    if (t == 0 && wn < nwork && !wait_rec(it + 1)) *abort_flag = 1;
+    const int out_off_w = cr.out_off[warp];
+    const int out_de_w = cr.out_de[warp];
+    const int cchi4 = cr.chi4;
     const int chi_w = rec_chi(cchi4, warp);
     // the previous outgoing message of this warp's leg (message_diff), loaded now, used last
     float old0 = 0.f, old1 = 0.f;
@@ -356,37 +393,26 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
       if (b < chi_w && a0 < chi_w) old0 = msg_in[out_off_w + b + chi_w * a0];
       if (b < chi_w && a0 + 4 < chi_w) old1 = msg_in[out_off_w + b + chi_w * (a0 + 4)];
     }
-    // next vertex: record now, messages later in this iteration
-    const int wn = w + gridDim.x;
-    int nsl = -1, nin0 = 0, nin1 = 0, nnet = 0, nchi0 = 8, nchi1 = 8;
-    if (wn < nwork) {
-      const TcRec* nr = recs + wn;
-      nsl = nr->slot;
-      nin0 = nr->in_off[q0 >> 6];
-      nin1 = nr->in_off[q1 >> 6];
-      nnet = nr->net;
-      const int n4 = nr->chi4;
-      nchi0 = rec_chi(n4, q0 >> 6);
-      nchi1 = rec_chi(n4, q1 >> 6);
-    }
     float nm0 = 0.f, nm1 = 0.f;
 
     if (converged && converged[cnet]) {  // network done: carry its messages forward
       const int p0 = q0 >> 6, p1 = q1 >> 6;
       const int c0 = rec_chi(cchi4, p0), c1 = rec_chi(cchi4, p1);
-      if (e < c0 * c0) msg_out[cr->out_off[p0] + e] = msg_in[cr->out_off[p0] + e];
-      if (e < c1 * c1) msg_out[cr->out_off[p1] + e] = msg_in[cr->out_off[p1] + e];
-      if (t == 0) {
+      if (e < c0 * c0) msg_out[cr.out_off[p0] + e] = msg_in[cr.out_off[p0] + e];
+      if (e < c1 * c1) msg_out[cr.out_off[p1] + e] = msg_in[cr.out_off[p1] + e];
+      if (t == 0 && !*abort_flag) {
         const bool ok = wait_z();
         *abort_flag = ok ? 0 : 1;
-        if (ok && nsl >= 0) issue_z(nsl);
+        if (ok && wn < nwork) issue_z(nr.slot);
       }
       __syncthreads();
       if (*abort_flag) break;
-      if (nsl >= 0) {
-        cm0 = padded_msg(msg_in, nin0, nchi0, e);
-        cm1 = padded_msg(msg_in, nin1, nchi1, e);
-        cnet = nnet;
+      // every thread is past the previous vertex: its ring entry takes the one after next
+      if (t == 0 && wn + G < nwork) issue_rec(it + 2, wn + G);
+      if (wn < nwork) {
+        cm0 = padded_msg(msg_in, nr.in_off[q0 >> 6], rec_chi(nr.chi4, q0 >> 6), e);
+        cm1 = padded_msg(msg_in, nr.in_off[q1 >> 6], rec_chi(nr.chi4, q1 >> 6), e);
+        cnet = nr.net;
       }
       continue;
     }
@@ -394,6 +420,19 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     MSG[q0] = cm0;
     MSG[q1] = cm1;
     __syncthreads();
+    if (*abort_flag) break;
+    // every thread is past the previous vertex: its ring entry takes the one after next
+    if (t == 0 && wn + G < nwork) issue_rec(it + 2, wn + G);
+    int nsl = -1, nin0 = 0, nin1 = 0, nnet = 0, nchi0 = 8, nchi1 = 8;
+    if (wn < nwork) {
+      nsl = nr.slot;
+      nin0 = nr.in_off[q0 >> 6];
+      nin1 = nr.in_off[q1 >> 6];
+      nnet = nr.net;
+      const int n4 = nr.chi4;
+      nchi0 = rec_chi(n4, q0 >> 6);
+      nchi1 = rec_chi(n4, q1 >> 6);
+    }
     {
       // Kronecker products: threads 0-63 build K12 = M1 (x) M2, 64-127 K34 = M3 (x) M4;
       // row n = b_a + 8 b_b, column k = a_a + 8 a_b (16-byte chunk a_b), value M_a[b_a,a_a] M_b[b_b,a_b]
@@ -523,11 +562,16 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     cnet = nnet;
   }
 
-  // drain: after a timeout, wait (bounded) for this CTA's own copy and MMAs
-  if (t == 0 && *abort_flag) {
-    atomicExch(err, (int)GBTN_ERR_TIMEOUT);
-    if (tma_pending) wait_z();
-    if (mma_pending) wait_mma();
+  // drain: after a timeout, wait (bounded) for this CTA's own copies and MMAs;
+  // record copies issued for vertices the walk did not reach land before exit
+  if (t == 0) {
+    if (*abort_flag) {
+      atomicExch(err, (int)GBTN_ERR_TIMEOUT);
+      if (tma_pending) wait_z();
+      if (mma_pending) wait_mma();
+    }
+    for (int k = 0; k < 3; ++k)
+      if (rec_pending[k]) tc::mbar_wait(rec_bar + k, rec_par[k], kWaitNs);
   }
   tc::tc_fence_before();
   __syncthreads();
