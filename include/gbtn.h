@@ -89,7 +89,8 @@ typedef struct gbtn_graph_desc {
                                     sweeps in FP64 (ComplexF64), FP32
                                     (ComplexF32 arithmetic) or MIXED (FP32
                                     sweeps, then FP64 ones), any schedule;
-                                    environments, one- and two-site RDMs,
+                                    environments, updated_message, one- and
+                                    two-site RDMs,
                                     expect / expect2 (real part of <O>, O
                                     real), vertex and edge scalars,
                                     logscalar and rescale_messages.  BF16

@@ -1339,7 +1339,6 @@ int gbtn_plan_tc_split(gbtn_plan* P, int32_t* is_tc, double* tuned_ms) {
 int gbtn_updated_message(gbtn_plan* P, int32_t de, double* out) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
-  if (P && P->cplx) throw Unsupported("updated_message of complex networks is not implemented");
   require(P && out, "NULL argument");
   require(de >= 0 && de < 2 * P->ne, "directed edge out of range");
   const int e = de / 2;
@@ -1348,10 +1347,15 @@ int gbtn_updated_message(gbtn_plan* P, int32_t de, double* out) {
   for (int p = 0; p < P->vd[v].k; ++p)
     if (P->vd[v].out_de[p] == de) leg = p;
   const int c = P->dchi[de];
-  P->d_out.alloc(c * c);
-  launch_updated_message(P->d_vd.p, v, leg, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p,
-                         P->d_msg_off.p, P->d_out.p, P->ncap, P->ctx->stream);
-  copy_out(P, out, P->d_out.p, sizeof(double) * c * c, GBTN_HOST);
+  P->d_out.alloc(P->es() * c * c);
+  if (P->cplx)
+    launch_updated_message<zdouble>(P->d_vd.p, v, leg, zptr(P->d_fac.p), P->sep_bra ? zptr(P->d_bra.p) : nullptr,
+                                    zptr(P->d_msg[P->cur].p), P->d_msg_off.p, zptr(P->d_out.p), P->ncap,
+                                    P->ctx->stream);
+  else
+    launch_updated_message<double>(P->d_vd.p, v, leg, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr,
+                                   P->d_msg[P->cur].p, P->d_msg_off.p, P->d_out.p, P->ncap, P->ctx->stream);
+  copy_out(P, out, P->d_out.p, sizeof(double) * P->es() * c * c, GBTN_HOST);
   API_CATCH(C)
 }
 

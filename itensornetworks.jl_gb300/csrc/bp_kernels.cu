@@ -205,22 +205,23 @@ __global__ void __launch_bounds__(256)
 }
 
 // One message, FP64, written to out without touching the cache.
+template <typename T>
 __global__ void __launch_bounds__(256)
-    updated_message_kernel(const VDesc* __restrict__ vd, int v, int leg, const double* __restrict__ fac,
-                           const double* __restrict__ bra_g, const double* msgs, const long long* msg_off,
-                           double* out, int ncap) {
+    updated_message_kernel(const VDesc* __restrict__ vd, int v, int leg, const T* __restrict__ fac,
+                           const T* __restrict__ bra_g, const T* msgs, const long long* msg_off, T* out,
+                           int ncap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TEAM = 256;
   const int tid = threadIdx.x;
-  TeamSmem<double> S = carve<double>(smem_raw, ncap, 3, bra_g != nullptr, TEAM);
+  TeamSmem<T> S = carve<T>(smem_raw, ncap, 3, bra_g != nullptr, TEAM);
   load_desc<TEAM>(S.desc, vd + v, tid);
   __syncthreads();
-  load_vertex<double, TEAM>(S, fac, bra_g, msgs, msg_off, leg, tid);
+  load_vertex<T, TEAM>(S, fac, bra_g, msgs, msg_off, leg, tid);
   __syncthreads();
-  const int cur = chain_absorb<double, TEAM>(S, leg, tid);
+  const int cur = chain_absorb<T, TEAM>(S, leg, tid);
   const VDesc& d = *S.desc;
-  close_any<double, TEAM>(d.chi[leg], S.buf[cur], S.bra, d.n, d.st[leg], 1, 0, 0, S.red, S.res, tid);
-  if (tid < 32) finalize_message<double>(S.res, d.chi[leg], out, out, 1, false, tid);
+  close_any<T, TEAM>(d.chi[leg], S.buf[cur], S.bra, d.n, d.st[leg], 1, 0, 0, S.red, S.res, tid);
+  if (tid < 32) finalize_message<T>(S.res, d.chi[leg], out, out, 1, false, tid);
 }
 
 // ---------------------------------------------------------------------------
@@ -688,13 +689,18 @@ void launch_reduce_diffs(int n_networks, const int* net_de_ptr, const int* net_d
   GBTN_CUDA(cudaGetLastError());
 }
 
-void launch_updated_message(const VDesc* vd, int v, int leg, const double* fac, const double* bra, const double* msgs,
-                            const long long* msg_off, double* out, int ncap, cudaStream_t s) {
-  const size_t sm = team_smem_bytes<double>(ncap, 3, bra != nullptr, 256);
-  GBTN_CUDA(cudaFuncSetAttribute(updated_message_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  updated_message_kernel<<<1, 256, sm, s>>>(vd, v, leg, fac, bra, msgs, msg_off, out, ncap);
+template <typename T>
+void launch_updated_message(const VDesc* vd, int v, int leg, const T* fac, const T* bra, const T* msgs,
+                            const long long* msg_off, T* out, int ncap, cudaStream_t s) {
+  const size_t sm = team_smem_bytes<T>(ncap, 3, bra != nullptr, 256);
+  GBTN_CUDA(cudaFuncSetAttribute(updated_message_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  updated_message_kernel<T><<<1, 256, sm, s>>>(vd, v, leg, fac, bra, msgs, msg_off, out, ncap);
   GBTN_CUDA(cudaGetLastError());
 }
+template void launch_updated_message<double>(const VDesc*, int, int, const double*, const double*, const double*,
+                                             const long long*, double*, int, cudaStream_t);
+template void launch_updated_message<zdouble>(const VDesc*, int, int, const zdouble*, const zdouble*, const zdouble*,
+                                              const long long*, zdouble*, int, cudaStream_t);
 
 template <typename T>
 void launch_vertex_rdms(const WorkList& wl, const VDesc* vd, const T* fac, const T* bra, const T* msgs,

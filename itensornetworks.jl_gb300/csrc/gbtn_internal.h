@@ -113,9 +113,9 @@ void launch_reduce_diffs(int n_networks, const int* net_de_ptr, const int* net_d
                          int stall = 0, double* best = nullptr, int* since = nullptr,
                          int* n_conv = nullptr);
 
-void launch_updated_message(const VDesc* vd, int v, int leg, const double* fac, const double* bra,
-                            const double* msgs, const long long* msg_off, double* out, int ncap,
-                            cudaStream_t s);
+template <typename T>
+void launch_updated_message(const VDesc* vd, int v, int leg, const T* fac, const T* bra, const T* msgs,
+                            const long long* msg_off, T* out, int ncap, cudaStream_t s);
 
 template <typename T>
 void launch_vertex_rdms(const WorkList& wl, const VDesc* vd, const T* fac, const T* bra,

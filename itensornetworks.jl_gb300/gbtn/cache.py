@@ -39,6 +39,11 @@ class BeliefPropagationCache:
         # complex tensors (ComplexF64): interleaved (re, im) doubles on the device
         self.complex = tn.is_complex or (bra is not None and any(np.iscomplexobj(t) for t in bra))
         self.dtype = np.complex128 if self.complex else np.float64
+        # element type the messages are reported in (the reference's messages
+        # keep the tensors' eltype: Float32, Float64, ComplexF32, ComplexF64)
+        ts = list(tn.tensors) + (list(bra) if bra is not None else [])
+        single = all(np.asarray(t).dtype in (np.float32, np.complex64) for t in ts)
+        self.elt = np.dtype((np.complex64 if self.complex else np.float32) if single else self.dtype)
         if self.complex and not tn.is_complex:
             tn = tn.copy()
             tn.tensors = [np.asarray(t, dtype=np.complex128) for t in tn.tensors]
@@ -75,7 +80,7 @@ class BeliefPropagationCache:
     def messages(self):
         out = np.empty(max(self.n_message, 1), dtype=self.dtype)
         self._c(self.lib.gbtn_get_messages(self.handle, out.ctypes.data, _lib.HOST))
-        return self.tn.unflat_messages(out)
+        return [m.astype(self.elt, copy=False) for m in self.tn.unflat_messages(out)]
 
     def flat_messages(self):
         """Every message in the ABI layout: directed edges in order, each
@@ -167,9 +172,9 @@ class BeliefPropagationCache:
 
     def updated_message(self, de):
         c = self.tn.edge_dims[de // 2]
-        out = np.empty(c * c)
-        self._c(self.lib.gbtn_updated_message(self.handle, int(de), dptr(out)))
-        return out.reshape((c, c), order="F")
+        out = np.empty(c * c, dtype=self.dtype)
+        self._c(self.lib.gbtn_updated_message(self.handle, int(de), dptr(out.view(np.float64))))
+        return out.reshape((c, c), order="F").astype(self.elt, copy=False)
 
     # -- environments and scalars ---------------------------------------------
     def environment(self, verts):
@@ -337,10 +342,11 @@ def updated_message(bpc, de):
 
 
 def message_diff(a, b):
-    """1 - |<a/|a|, b/|b|>|^2 (host-side helper on two message matrices)."""
-    a = np.asarray(a, float)
-    b = np.asarray(b, float)
-    return 1.0 - float(np.vdot(a / np.linalg.norm(a), b / np.linalg.norm(b))) ** 2
+    """1 - |<a/|a|, b/|b|>|^2 (host-side helper on two message matrices, real
+    or complex; abstractbeliefpropagationcache.jl:32-36)."""
+    a = np.asarray(a, np.complex128 if np.iscomplexobj(a) or np.iscomplexobj(b) else np.float64)
+    b = np.asarray(b, a.dtype)
+    return 1.0 - abs(np.vdot(a / np.linalg.norm(a), b / np.linalg.norm(b))) ** 2
 
 
 def _cache_for(tn, cache, update_cache, cache_update_kwargs, bra=None):
