@@ -143,9 +143,10 @@ function ITensorNetworks.update(alg::Algorithm"gb300_bp", bpc::BeliefPropagation
             # b the bra (primed) link and a the ket link
             off = 0
             new = Dict{QuotientEdge, Vector{ITensor}}()
+            elt = promote_type((eltype(ket(pv)) for pv in p.pvs)...)  # messages keep the tensors' eltype
             for (e, pe) in enumerate(p.pes), (dir, qe) in ((0, pe), (1, reverse(pe)))
                 c = Int(p.edim[e])
-                M = reshape(flat[(off + 1):(off + c * c)], c, c)
+                M = convert(Matrix{elt}, reshape(flat[(off + 1):(off + c * c)], c, c))
                 off += c * c
                 l = p.links[e]
                 new[qe] = [itensor(M, dag(prime(l)), l)]
