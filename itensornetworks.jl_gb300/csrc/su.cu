@@ -45,6 +45,14 @@ constexpr int kSvdMaxSweeps = 40;
 // cannot change the decomposition beyond eps ||A||).
 constexpr double kJacobiTol = 1e-13;
 constexpr double kJacobiTiny = 1e-30;
+// Noise bound of the Jacobi stage of a gate's SVD (n singular values, relative
+// cutoff on sigma^2): pairs of columns both at or below skip_rel * ||theta||^2
+// are not rotated.  Those columns sum to at most n * skip_rel <= cutoff / 2 of
+// the total, so the cutoff discards every one of them whatever maxdim did
+// first; no cutoff (< 0) or a zero cutoff keeps the full Jacobi.
+__host__ __device__ inline double svd_skip_rel(double cutoff, int n) {
+  return cutoff > 0.0 ? fmin(1e-16, 0.5 * cutoff / (double)n) : 0.0;
+}
 
 // FP64 runs at a small fraction of the FP32 rate on this part, and a warp
 // instruction costs the FP64 pipe the same whether one lane or 32 are active,
@@ -192,13 +200,19 @@ __device__ void cta_qrcp(double* A, int m, int n, SvdBufs& b) {
 // tangent is used (the transformation stays orthogonal), and the FP64
 // stopping test decides the accuracy.  Sweeps stop when a sweep rotates
 // nothing.  The rotations are not accumulated: the caller recovers the right
-// factor from the rotated columns.
-__device__ void cta_jacobi(double* X, int m, int n, int* flag, double* red) {
+// factor from the rotated columns.  A pair whose squared norms are both at or
+// below skip_rel * ||X||_F^2 is left alone: at the end every pair that is not
+// orthogonal has both columns below that bound, so a caller whose truncation
+// is sure to discard all such columns (n * skip_rel well inside its relative
+// cutoff) loses nothing, and the sweeps spent orthogonalising noise columns of
+// a rank-deficient theta against each other are saved; skip_rel = 0 keeps
+// every column exact.
+__device__ void cta_jacobi(double* X, int m, int n, int* flag, double* red, double skip_rel) {
   const int tid = threadIdx.x, grp = tid >> 3, gl = tid & 7;
   double f = 0.0;
   for (int i = tid; i < m * n; i += kSuThreads) f = fma(X[i], X[i], f);
   f = block_sum(f, red);
-  const double tiny = f * kJacobiTiny, tol2 = kJacobiTol * kJacobiTol;
+  const double tiny = f * kJacobiTiny, tol2 = kJacobiTol * kJacobiTol, small = f * skip_rel;
   const int N = n + (n & 1);  // players of the round-robin (one dummy when n is odd)
   const int npair = N / 2;
   const bool warp_busy = (tid >> 5) * 4 < npair;  // warp-uniform
@@ -237,7 +251,7 @@ __device__ void cta_jacobi(double* X, int m, int n, int* flag, double* red) {
         al = group8_sum(al);
         be = group8_sum(be);
         ga = group8_sum(ga);
-        const bool rot = act && al > tiny && be > tiny && ga * ga > tol2 * al * be;
+        const bool rot = act && al > tiny && be > tiny && fmax(al, be) > small && ga * ga > tol2 * al * be;
         if (__any_sync(0xffffffffu, rot)) {
           // tan of the angle: 2 g sgn(d) / (|d| + sqrt(d^2 + 4 g^2)), d = (be - al) / mx, g = ga / mx
           const float inv = 1.0f / (float)fmax(al, be);
@@ -352,8 +366,9 @@ __device__ void cta_jacobi32(float* X, int m, int n, float* V, int* flag, double
 // columns of A hold U (zero where sigma = 0), V (n x n, ldv = n) the right
 // singular vectors, sig[n] the singular values, all in descending order of
 // sig.  U is accurate to eps ||A|| / sigma per column, which is the accuracy
-// of the reconstruction U S V^T that the callers use.
-__device__ void cta_svd(double* A, int m, int n, double* V, double* sig, SvdBufs& b) {
+// of the reconstruction U S V^T that the callers use.  skip_rel is passed to
+// the FP64 Jacobi stage (0: every singular triplet exact).
+__device__ void cta_svd(double* A, int m, int n, double* V, double* sig, SvdBufs& b, double skip_rel = 0.0) {
   const int tid = threadIdx.x, grp = tid >> 3, gl = tid & 7;
   double* A0 = b.work;                  // m x n copy of the input
   double* X = b.work + (size_t)m * n;   // n x n
@@ -403,7 +418,7 @@ __device__ void cta_svd(double* A, int m, int n, double* V, double* sig, SvdBufs
     for (int i = tid; i < n * n; i += kSuThreads) X[i] = XQ[i];
     __syncthreads();
   }
-  cta_jacobi(X, n, n, b.flag, b.red);
+  cta_jacobi(X, n, n, b.flag, b.red, skip_rel);
   // sigma = column norms of X, U_x = unit columns (a group per column)
   for (int j0 = 0; j0 < n; j0 += 32) {
     const int j = j0 + grp;
@@ -846,7 +861,7 @@ __global__ void __launch_bounds__(kSuThreads, 2) su_svd_kernel(SuArgs a) {
     __syncthreads();
   }
   SvdBufs sb{W, aux, aux + 64, aux + 128, perm, ord, &s_flag, red, XT};
-  cta_svd(TH, wide ? nt : mt, wide ? mt : nt, V, sig, sb);
+  cta_svd(TH, wide ? nt : mt, wide ? mt : nt, V, sig, sb, svd_skip_rel(a.cutoff, min(mt, nt)));
   const double* UF = wide ? V : TH;  // left factor, mt x nsv (ld mt)
   const double* VF = wide ? TH : V;  // right factor, nt x nsv (ld nt)
   if (tid == 0) {
@@ -1029,10 +1044,20 @@ __device__ __forceinline__ zdouble zwarp_sum(zdouble x) { return zdouble(warp_su
 // (the same on the columns of V, which starts as the identity), which makes
 // the pair orthogonal.  Pairs in round-robin rounds of n/2 disjoint pairs, one
 // warp per pair, one row per lane.  On return the columns of X are U S,
-// sig their norms and ord the descending order.
-__device__ void cta_zjacobi(zdouble* X, int m, int n, zdouble* V, double* sig, int* ord, int* flag) {
+// sig their norms and ord the descending order.  Pairs whose squared norms are
+// both at or below skip_rel * ||X||_F^2 are not rotated (as in the real
+// Jacobi: for callers whose truncation discards all such columns).
+__device__ void cta_zjacobi(zdouble* X, int m, int n, zdouble* V, double* sig, int* ord, int* flag,
+                            double skip_rel) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int i = tid; i < n * n; i += kSuThreads) V[i] = zdouble(i % n == i / n ? 1.0 : 0.0);
+  double small = 0.0;
+  if (skip_rel > 0.0) {  // every warp forms ||X||_F^2 itself (m <= 32 rows, one per lane)
+    double f = 0.0;
+    if (lane < m)
+      for (int c = 0; c < n; ++c) f += zabs2(X[lane + m * c]);
+    small = warp_sum(f) * skip_rel;
+  }
   __syncthreads();
   const int n2 = n + (n & 1);
   for (int sweep = 0; sweep < kSvdMaxSweeps; ++sweep) {
@@ -1049,7 +1074,7 @@ __device__ void cta_zjacobi(zdouble* X, int m, int n, zdouble* V, double* sig, i
         const double al = warp_sum(zabs2(xi)), be = warp_sum(zabs2(xj));
         const zdouble ga = zwarp_sum(zcmul(xi, xj));
         const double ag = sqrt(zabs2(ga));
-        if (ag > kJacobiTol * sqrt(al * be) && al > kJacobiTiny && be > kJacobiTiny) {
+        if (ag > kJacobiTol * sqrt(al * be) && al > kJacobiTiny && be > kJacobiTiny && fmax(al, be) > small) {
           const double z = (be - al) / (2.0 * ag);
           const double t = (z >= 0.0 ? 1.0 : -1.0) / (fabs(z) + sqrt(1.0 + z * z));
           const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
@@ -1105,7 +1130,7 @@ __device__ void cta_zenv_sqrt(const zdouble* env, int chi, zdouble* S, zdouble* 
     A[i] = zdouble(0.5 * (x.re + y.re), 0.5 * (x.im - y.im));
   }
   __syncthreads();
-  cta_zjacobi(A, chi, chi, V, sig, ord, flag);
+  cta_zjacobi(A, chi, chi, V, sig, ord, flag, 0.0);
   __shared__ int s_keep;
   if (tid == 0) {
     double tot = 0.0;
@@ -1311,7 +1336,7 @@ __global__ void __launch_bounds__(kSuThreads, 1) su_gate_z_kernel(SuArgs a, zdou
   }
   __syncthreads();
   const int M = wide ? nt : mt, N = wide ? mt : nt;
-  cta_zjacobi(B0, M, N, B1, sig, ord, &s_flag);
+  cta_zjacobi(B0, M, N, B1, sig, ord, &s_flag, svd_skip_rel(a.cutoff, N));
   // theta = U S V^H: not wide, U = columns of B0 / sig, V = B1; wide (theta^H =
   // U' S V'^H), U = V' = B1 and V = U' = columns of B0 / sig
   if (tid == 0) {
