@@ -507,12 +507,23 @@ def run_ours(args):
                                  for v in tc_v))
     n_tc_native = sum(1 for v in tc_v if len(tn.legs[v]) == 4)
     mma_flops_vertex = 2 * (2 * 128 * 64 * 64) + 2 * (2 * 64 * 64 * 128)  # GEMM1, GEMM1', GEMM2, GEMM2'
+    # compulsory bytes of one launch: every routed vertex's BF16 tensor at its
+    # own (unpadded) shape, and each of its incoming and outgoing FP32 messages once
+    alg_bytes_launch = float(sum(2 * tn.size(v) + 2 * 4 * sum(tn.edge_dims[e] ** 2 for e in tn.legs[v])
+                                 for v in tc_v))
     tc_launch_ms = tc_ms / max(tc_n, 1)
     achieved = alg_flops_launch / (tc_launch_ms * 1e-3) / 1e12
+    achieved_gbs = alg_bytes_launch / (tc_launch_ms * 1e-3) / 1e9
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("bf16_tflops")
     peak_src = "measured burst" if peak else "fallback"
     peak = peak or 1900.0
+    hbm_src = "measured" if peaks.get("hbm_gbs") else "fallback"
+    # the binding roof: the arithmetic intensity (flops per compulsory byte) is
+    # below the ridge point of the two peaks, so HBM caps the kernel first
+    intensity = alg_flops_launch / max(alg_bytes_launch, 1.0)
+    ridge = peak * 1e12 / (hbm_peak * 1e9)
+    bound = "hbm" if intensity < ridge else "tensor"
     traffic = None
     tfile = ROOT / "profiles" / "tc_vertex_kernel_traffic.json"
     if tfile.exists():
@@ -534,18 +545,30 @@ def run_ours(args):
                 "tol": args.solve_tol, "fp64_ms": fp64_ms, "fp64_sweeps": int(np.max(fp64_it)),
                 "mixed_ms": mix_ms, "mixed_final_fp64_sweeps": int(np.max(mix_it)),
                 "speedup": fp64_ms / mix_ms, "mixed_max_rel_err_sz": max(per_net)},
-            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "tc_vertex_kernel", "launch_ms": tc_launch_ms, "launches": tc_n,
-                         "other_kernels_ms_per_sweep": {"simt_f32": simt_ms / max(args.steps, 1)},
-                         "units_per_launch": n_tc, "unit_kind": "vertex (all outgoing messages)",
-                         "alg_flops_per_launch": alg_flops_launch,
-                         "alg_flops_per_unit": alg_flops_launch / max(n_tc, 1),
-                         "tc_split": {"policy": "auto", "tensor_core_vertices": n_tc,
-                                      "of_which_degree4": n_tc_native, "simt_vertices": tn.nv - n_tc,
-                                      "tuned_split_ms": tune_ms},
-                         "mma_tflops": n_tc * mma_flops_vertex / (tc_launch_ms * 1e-3) / 1e12,
-                         "note": f"algorithmic FP flops of the routed vertices (unpadded shapes) / event-timed kernel duration, of {peak_src} bf16 peak"},
+            "roofline": dict(
+                {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                 "frac": achieved_gbs / hbm_peak, "traffic": traffic}
+                if bound == "hbm" else
+                {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                 "frac": achieved / peak, "traffic": traffic},
+                **{"kernel": "tc_vertex_kernel", "launch_ms": tc_launch_ms, "launches": tc_n,
+                   "other_kernels_ms_per_sweep": {"simt_f32": simt_ms / max(args.steps, 1)},
+                   "units_per_launch": n_tc, "unit_kind": "vertex (all outgoing messages)",
+                   "alg_bytes_per_launch": alg_bytes_launch, "alg_bytes_per_unit": alg_bytes_launch / max(n_tc, 1),
+                   "alg_flops_per_launch": alg_flops_launch,
+                   "alg_flops_per_unit": alg_flops_launch / max(n_tc, 1),
+                   "intensity_flop_per_byte": intensity, "ridge_flop_per_byte": ridge,
+                   "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                           "frac": achieved_gbs / hbm_peak},
+                   "tensor": {"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                              "mma_issued_tflops": n_tc * mma_flops_vertex / (tc_launch_ms * 1e-3) / 1e12},
+                   "tc_split": {"policy": "auto", "tensor_core_vertices": n_tc,
+                                "of_which_degree4": n_tc_native, "simt_vertices": tn.nv - n_tc,
+                                "tuned_split_ms": tune_ms},
+                   "note": (f"algorithmic bytes and flops of the routed vertices at their unpadded shapes / "
+                            f"event-timed kernel duration; bound = the roof the intensity meets first "
+                            f"({hbm_src} HBM copy bandwidth, {peak_src} bf16 peak); traffic = ncu DRAM "
+                            f"bytes per vertex (padded images) x vertices")}),
             "gradient": grad,
             "simple_update": su,
             "batched_uneven": batched,

@@ -75,6 +75,37 @@ def test_single_gate_matches_oracle(e):
     assert same_up_to_sign(state(g2, out.tensors), state(g2, B), 1e-9)
 
 
+def rank2_bond(g, A, e, seed):
+    """Make edge e (dimension 4) carry rank 2: A[u]'s leg on e is projected
+    onto a random 2-dimensional subspace."""
+    u = g.edges[e][0]
+    pu = g.legs[u].index(e)
+    P = np.random.default_rng(seed).standard_normal((2, g.edge_dims[e]))
+    B = list(A)
+    B[u] = np.moveaxis(np.tensordot(A[u], P.T @ P, axes=([1 + pu], [0])), -1, 1 + pu)
+    return B
+
+
+@pytest.mark.parametrize("e", [2, 6])
+def test_rank_deficient_theta_keeps_exactly_its_rank(e):
+    # a product gate on a bond of rank 2: theta (8 x 8 after the QRs) has rank
+    # 2, so maxdim 4 with a relative cutoff keeps two values and discards the
+    # six noise columns, which the FP64 Jacobi leaves unrotated among themselves
+    g = O.square_lattice(3, 3, chi=4)
+    A = rank2_bond(g, O.random_network(g, 77), e, e)
+    rng = np.random.default_rng(10 + e)
+    gate = np.kron(rng.standard_normal((2, 2)), rng.standard_normal((2, 2)))
+    g2, B, S, te = oracle_gate(g, A, gate, e, maxdim=4, cutoff=1e-12)
+    assert g2.edge_dims[e] == 2
+    st = gbtn.SimpleUpdateState(gpu_net(g, A), chi_max=4)
+    te_g, sv = st.apply(gate, [e], maxdim=4, cutoff=1e-12, normalize=True)
+    assert st.edge_dims()[e] == 2
+    np.testing.assert_allclose(sv[0][:2], S, rtol=1e-10)
+    assert np.all(sv[0][2:] == 0.0)
+    assert te_g[0] == pytest.approx(te, abs=1e-14)
+    assert same_up_to_sign(state(g2, st.network().tensors), state(g2, B), 1e-9)
+
+
 def test_single_gate_with_bp_environment():
     g = O.square_lattice(3, 3, chi=3)
     A = O.random_network(g, 5)

@@ -105,6 +105,28 @@ def test_complex_state_and_gate_sequence_without_environments():
     assert overlap(state(gg, st.network().tensors), state(gg, B)) == pytest.approx(1.0, abs=1e-9)
 
 
+@pytest.mark.parametrize("e", [2, 6])
+def test_rank_deficient_complex_theta_keeps_exactly_its_rank(e):
+    # a product of single-site unitaries on a bond of dimension 4 that carries
+    # rank 2: two values kept, the noise columns discarded by the cutoff
+    g = O.square_lattice(3, 3, chi=4)
+    A = O.random_network(g, 31, dtype=np.complex128)
+    u = g.edges[e][0]
+    pu = g.legs[u].index(e)
+    rng = np.random.default_rng(e)
+    P = rng.standard_normal((2, 4)) + 1j * rng.standard_normal((2, 4))
+    A[u] = np.moveaxis(np.tensordot(A[u], P.conj().T @ P, axes=([1 + pu], [0])), -1, 1 + pu)
+    gate = np.kron(random_unitary(20 + e, 2), random_unitary(30 + e, 2))
+    g2, B, S, te = oracle_gate(g, A, gate, e, maxdim=4, cutoff=1e-12)
+    assert g2.edge_dims[e] == 2
+    st = gbtn.SimpleUpdateState(gpu_net(g, A), chi_max=4)
+    te_g, sv = st.apply(gate, [e], maxdim=4, cutoff=1e-12, normalize=True)
+    assert st.edge_dims()[e] == 2
+    np.testing.assert_allclose(sv[0][:2], S, rtol=1e-10)
+    assert te_g[0] == pytest.approx(te, abs=1e-14)
+    assert overlap(state(g2, st.network().tensors), state(g2, B)) == pytest.approx(1.0, abs=1e-9)
+
+
 def test_complex_gates_need_a_complex_state_and_fit_the_kernel():
     g = O.square_lattice(3, 3, chi=2)
     A = O.random_network(g, 2)
