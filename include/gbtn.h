@@ -93,8 +93,9 @@ typedef struct gbtn_graph_desc {
                                     two-site RDMs,
                                     expect / expect2 (real part of <O>, O
                                     real), vertex and edge scalars,
-                                    logscalar and rescale_messages.  BF16
-                                    sweeps and the other entry points return
+                                    logscalar, rescale_messages and
+                                    rescale_partitions.  BF16 sweeps and the
+                                    energy / gradient entry points return
                                     GBTN_ERR_UNSUPPORTED.
                                     (test/test_belief_propagation.jl:18-20) */
 } gbtn_graph_desc;
@@ -227,7 +228,12 @@ int gbtn_logscalar(gbtn_plan* plan, double* re, double* im);
 /* Replaces: rescale_messages (beliefpropagationcache.jl:121-139). */
 int gbtn_rescale_messages(gbtn_plan* plan);
 /* Replaces: rescale_partitions on ket+bra vertices (abstractbeliefpropagationcache.jl:349-379,
- * normalize.jl:77): every vertex scalar becomes 1. */
+ * normalize.jl:77): every vertex scalar becomes 1.  Both tensors are divided
+ * by their norms, then with r = z^(-1/2) (principal root) of the partition
+ * scalar z and s = sign(z) for a real z (else 1) the ket is scaled by s*r and
+ * the bra by s*s*r, as in the reference (whose partitions list the bra first).
+ * With bra = conj(ket) only the ket is scaled: a real network with a negative
+ * z gets NaN tensors, and a complex one keeps the scalar's phase z/|z|. */
 int gbtn_rescale_partitions(gbtn_plan* plan);
 
 /* ---- simple update / apply (FP64) ------------------------------------------- */

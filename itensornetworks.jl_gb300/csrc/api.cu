@@ -772,6 +772,100 @@ __global__ void partition_scale_kernel(int nv, const VDesc* vd, const double* fa
   }
 }
 
+// Complex partition scale factors (abstractbeliefpropagationcache.jl:349-379).
+// With z' = Z / (|ket| |bra|), r = z'^(-1/2) (principal root) and s = sign(z')
+// when z' has an exactly zero imaginary part, else 1, the reference weights the
+// first vertex of the partition by s * (s * r) and the others by s * r.  The
+// partition lists the bra first (the form network is the disjoint union of
+// operator, bra and ket, formnetworks/bilinearformnetwork.jl:34-38), so the ket
+// takes s * r and the bra s * s * r; the stored bra is conjugated by every
+// contraction, so it is scaled by the conjugate.  With a shared bra only the
+// ket is scaled: the returned ket is the reference's and the partition scalar
+// becomes z'/|z'| (1 for the real positive scalars of <psi|psi>).  scale: four
+// doubles per vertex, (ket re, ket im, bra re, bra im), norms divided in.
+// fac, bra: interleaved (re, im) doubles; rdm_off in complex elements.
+__global__ void partition_scale_z_kernel(int nv, const VDesc* vd, const double* fac, const double* bra,
+                                         const long long* rdm_off, const double* rdm, double* scale) {
+  const int v = blockIdx.x;
+  const long long off = 2 * vd[v].a_off;
+  const int n = 2 * vd[v].n, d = vd[v].d;
+  double nk = 0.0, nb = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    nk += fac[off + i] * fac[off + i];
+    if (bra) nb += bra[off + i] * bra[off + i];
+  }
+  __shared__ double r1[32], r2[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    nk += __shfl_xor_sync(0xffffffffu, nk, o);
+    nb += __shfl_xor_sync(0xffffffffu, nb, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    r1[threadIdx.x >> 5] = nk;
+    r2[threadIdx.x >> 5] = nb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += r1[w];
+      b += r2[w];
+    }
+    const double normk = sqrt(a);
+    const double normb = bra ? sqrt(b) : normk;
+    double zr = 0.0, zi = 0.0;
+    for (int q = 0; q < d; ++q) {
+      zr += rdm[2 * (rdm_off[v] + q + d * q)];
+      zi += rdm[2 * (rdm_off[v] + q + d * q) + 1];
+    }
+    zr /= normk * normb;
+    zi /= normk * normb;
+    // principal square root w of z' (w.re >= 0; the branch cut on the negative
+    // real axis follows the sign of the zero imaginary part), then r = 1 / w
+    const double m = hypot(zr, zi);
+    const double h = sqrt(0.5 * (m + fabs(zr)));
+    double wr, wi;
+    if (zr >= 0.0) {
+      wr = h;
+      wi = h > 0.0 ? zi / (2.0 * h) : 0.0;
+    } else {
+      wr = fabs(zi) / (2.0 * h);
+      wi = copysign(h, zi);
+    }
+    const double w2 = wr * wr + wi * wi;
+    const double rr = w2 > 0.0 ? wr / w2 : INFINITY, ri = w2 > 0.0 ? -wi / w2 : 0.0;
+    const double sg = zi == 0.0 ? (zr > 0.0 ? 1.0 : (zr < 0.0 ? -1.0 : 0.0)) : 1.0;
+    scale[4 * v] = sg * rr / normk;
+    scale[4 * v + 1] = sg * ri / normk;
+    if (bra) {
+      scale[4 * v + 2] = sg * sg * rr / normb;
+      scale[4 * v + 3] = -sg * sg * ri / normb;
+    } else {
+      scale[4 * v + 2] = 1.0;
+      scale[4 * v + 3] = 0.0;
+    }
+  }
+}
+
+// fac_v *= (scale[4v], scale[4v+1]), bra_v *= (scale[4v+2], scale[4v+3]) in
+// complex arithmetic (interleaved (re, im) doubles).
+__global__ void scale_vertices_z_kernel(int nv, const VDesc* vd, double* fac, double* bra, const double* scale) {
+  const int v = blockIdx.x;
+  if (v >= nv) return;
+  const long long off = 2 * vd[v].a_off;
+  const int n = vd[v].n;
+  const double kr = scale[4 * v], ki = scale[4 * v + 1], br = scale[4 * v + 2], bi = scale[4 * v + 3];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double x = fac[off + 2 * i], y = fac[off + 2 * i + 1];
+    fac[off + 2 * i] = x * kr - y * ki;
+    fac[off + 2 * i + 1] = x * ki + y * kr;
+    if (bra) {
+      const double p = bra[off + 2 * i], q = bra[off + 2 * i + 1];
+      bra[off + 2 * i] = p * br - q * bi;
+      bra[off + 2 * i + 1] = p * bi + q * br;
+    }
+  }
+}
+
 namespace gbtn {
 cudaStream_t ctx_stream(gbtn_ctx* c) { return c->stream; }
 void set_ctx_error(gbtn_ctx* c, const char* msg) { set_err(c, msg); }
@@ -967,7 +1061,7 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   P->d_edge_sc.alloc(es * std::max(P->ne, 1));
   P->d_re.alloc(P->nnet);
   P->d_im.alloc(P->nnet);
-  P->d_scale.alloc(2 * (size_t)P->nv);
+  P->d_scale.alloc(2 * es * (size_t)P->nv);  // (ket, bra) factors per vertex, complex for complex plans
 
   // per-network bookkeeping (parallel-sequence order of directed edges)
   std::vector<std::vector<int>> nde(P->nnet), nvv(P->nnet), nee(P->nnet);
@@ -1589,13 +1683,21 @@ int gbtn_rescale_messages(gbtn_plan* P) {
 int gbtn_rescale_partitions(gbtn_plan* P) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
-  // With the bra taken as conj(ket), scale factors come in conjugate pairs and
-  // change a partition scalar only by |c|^2: a complex partition scalar
-  // cannot be brought to 1 without separate ket and bra tensors.
-  if (P && P->cplx) throw Unsupported("rescale_partitions of complex networks is not implemented");
   require(P, "NULL plan");
   cudaStream_t s = P->ctx->stream;
   compute_rdms(P);
+  if (P->cplx) {
+    partition_scale_z_kernel<<<P->nv, 256, 0, s>>>(P->nv, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr,
+                                                    P->d_rdm_off.p, P->d_rdm.p, P->d_scale.p);
+    GBTN_CUDA(cudaGetLastError());
+    scale_vertices_z_kernel<<<P->nv, 256, 0, s>>>(P->nv, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr,
+                                                   P->d_scale.p);
+    GBTN_CUDA(cudaGetLastError());
+    P->fac32_valid = false;
+    P->zimg_valid = false;
+    GBTN_CUDA(cudaStreamSynchronize(s));
+    return GBTN_OK;
+  }
   partition_scale_kernel<<<P->nv, 256, 0, s>>>(P->nv, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr,
                                               P->d_rdm_off.p, P->d_rdm.p, P->d_scale.p);
   GBTN_CUDA(cudaGetLastError());

@@ -515,17 +515,30 @@ def rescale_messages(g, msgs):
     return msgs
 
 
-def rescale_partitions(g, A, msgs):
+def rescale_partitions(g, A, msgs, B=None):
     """Scale each ket (and its bra) so every vertex scalar is 1
     (abstractbeliefpropagationcache.jl:349-379 restricted to the ket and bra
-    vertices, normalize.jl:77): divide by the tensor norm, then by the square
-    root of the partition scalar computed with the divided tensors."""
-    out = []
+    vertices, normalize.jl:77): divide both tensors by their norms, compute the
+    partition scalar z with the divided tensors, take r = z^(-1/2) (principal
+    root) and s = sign(z) when z is real (for a complex z: an exactly zero
+    imaginary part), else 1.  The reference weights the first vertex of the
+    partition by s * (s * r) and the others by s * r; the partition lists the bra
+    before the ket, because the form network is disjoint_union(operator, bra,
+    ket) (formnetworks/bilinearformnetwork.jl:34-38) and partitions group the
+    vertices in that order (abstractformnetwork.jl:89-91).  So the ket takes
+    s * r and the bra conj(B_v) takes s * s * r.  With B = None the bra is
+    conj(A) and only the kets are returned; with B the rescaled (A, B)."""
+    out, outb = [], []
     for v in range(g.nv):
         a = A[v] / np.linalg.norm(A[v])
-        z = np.trace(contract_partition(g, {v: a}, {v: a}, msgs, v, open_site=True))
-        out.append(a * z ** -0.5)
-    return out
+        b = a if B is None else B[v] / np.linalg.norm(B[v])
+        z = np.trace(contract_partition(g, {v: a}, {v: b}, msgs, v, open_site=True))
+        real = np.isrealobj(z) or np.imag(z) == 0
+        sg = np.sign(np.real(z)) if real else 1.0
+        r = z ** -0.5
+        out.append(a * (sg * r))
+        outb.append(b * np.conj(sg * sg * r))  # the contraction conjugates B
+    return out if B is None else (out, outb)
 
 
 def normalize_bp(g, A, msgs):

@@ -133,9 +133,54 @@ def test_complex_paths_outside_fp64_are_unsupported():
     with pytest.raises(gbtn.Unsupported):
         bpc.update(maxiter=2, schedule="parallel", precision="bf16")
     with pytest.raises(gbtn.Unsupported):
-        bpc.rescale_partitions()
-    with pytest.raises(gbtn.Unsupported):
         bpc.energy2([(1.0, O.SZ)])
+
+
+def test_complex_rescale_partitions_and_normalize_match_the_oracle():
+    # normalize(alg="bp") of a complex state: messages rescaled, then every ket
+    # divided by its norm and scaled by z^(-1/2) of its partition scalar.  Ten
+    # sweeps: on random complex tensors BP amplifies the rounding-level
+    # anti-Hermitian part of the messages (1e-15 after ten sweeps, O(1) after a
+    # hundred), after which the messages and partition scalars carry free phases
+    kw = dict(maxiter=10, schedule="parallel")
+    g = O.square_lattice(4, 3, chi=2)
+    tn, A = cnet(g, 21)
+    bpc = gbtn.BeliefPropagationCache(tn).update(**kw)
+    msgs = bpc.messages()
+    bpc.rescale()
+    ref, ref_msgs = O.normalize_bp(g, A, msgs)
+    got = bpc.factors()
+    for v in range(g.nv):
+        np.testing.assert_allclose(got[v], ref[v], rtol=0, atol=1e-12 * np.max(np.abs(ref[v])))
+    # the shared bra carries conj of the ket's factor: each partition scalar
+    # keeps only its phase, and it is real and positive for <psi|psi>
+    vs = bpc.vertex_scalars()
+    np.testing.assert_allclose(np.abs(vs), 1.0, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(vs, 1.0, rtol=0, atol=1e-10)
+    # the module-level normalize returns the same kets, and its BP norm is 1
+    out = gbtn.normalize(tn, cache_update_kwargs=kw)
+    for v in range(g.nv):
+        np.testing.assert_allclose(out.tensors[v], ref[v], rtol=0, atol=1e-12 * np.max(np.abs(ref[v])))
+    n2 = gbtn.norm_sqr(out, cache_update_kwargs=kw)
+    assert abs(n2 - 1.0) < 1e-10
+
+
+def test_complex_rescale_partitions_with_a_separate_bra():
+    # <phi|psi> with complex phi != psi: the ket takes s*r and the bra s*s*r,
+    # which brings every partition scalar to 1 whatever its phase
+    g = O.square_lattice(3, 3, chi=2)
+    tn, A = cnet(g, 5)
+    _, B = cnet(g, 6)
+    bpc = gbtn.BeliefPropagationCache(tn, bra=B).update(maxiter=100, schedule="parallel")
+    msgs = bpc.messages()
+    bpc.rescale_partitions()
+    ref_k, ref_b = O.rescale_partitions(g, A, msgs, B)
+    got = bpc.factors()
+    for v in range(g.nv):
+        np.testing.assert_allclose(got[v], ref_k[v], rtol=0, atol=1e-12 * np.max(np.abs(ref_k[v])))
+        z = np.trace(O.contract_partition(g, {v: ref_k[v]}, {v: ref_b[v]}, msgs, v, open_site=True))
+        assert abs(z - 1.0) < 1e-12
+    np.testing.assert_allclose(bpc.vertex_scalars(), 1.0, rtol=0, atol=1e-12)
 
 
 def test_complex_two_site_rdms_and_expect2():
