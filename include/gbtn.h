@@ -232,8 +232,11 @@ int gbtn_rescale_messages(gbtn_plan* plan);
  * by their norms, then with r = z^(-1/2) (principal root) of the partition
  * scalar z and s = sign(z) for a real z (else 1) the ket is scaled by s*r and
  * the bra by s*s*r, as in the reference (whose partitions list the bra first).
- * With bra = conj(ket) only the ket is scaled: a real network with a negative
- * z gets NaN tensors, and a complex one keeps the scalar's phase z/|z|. */
+ * With bra = conj(ket) only the ket is scaled (a real network with a negative
+ * z gets NaN tensors); for complex tensors the remaining phases z/|z| are then
+ * moved onto the messages, which carry a free phase (m_{u->v} by e^{i psi},
+ * m_{v->u} by e^{-i psi} on the edges of a spanning forest, which keeps every
+ * edge scalar), so vertex scalars become 1 as in the reference. */
 int gbtn_rescale_partitions(gbtn_plan* plan);
 
 /* ---- simple update / apply (FP64) ------------------------------------------- */

@@ -866,6 +866,101 @@ __global__ void scale_vertices_z_kernel(int nv, const VDesc* vd, double* fac, do
   }
 }
 
+// m_de *= (f[2 de], f[2 de + 1]) in complex arithmetic, one block per directed edge.
+__global__ void scale_messages_z_kernel(int nde, const int* dchi, const long long* msg_off, const double* f,
+                                        double* msgs) {
+  const int de = blockIdx.x;
+  if (de >= nde) return;
+  const double fr = f[2 * de], fi = f[2 * de + 1];
+  if (fr == 1.0 && fi == 0.0) return;
+  const int chi = dchi[de];  // per directed edge
+  for (int i = threadIdx.x; i < chi * chi; i += blockDim.x) {
+    const long long k = 2 * (msg_off[de] + i);
+    const double x = msgs[k], y = msgs[k + 1];
+    msgs[k] = x * fr - y * fi;
+    msgs[k + 1] = x * fi + y * fr;
+  }
+}
+
+namespace {
+
+// Complex plans with bra = conj(ket): after the kets are scaled, partition v's
+// scalar is z_v = e^{i phi_v} (the reference reaches 1 by scaling its bra with
+// the unconjugated factor, which a shared bra cannot take).  Every message
+// carries a free phase, and m_{u->v} *= e^{i psi}, m_{v->u} *= e^{-i psi}
+// keeps every edge scalar <m_e, m_ebar> while it multiplies z_v by e^{i psi}
+// and z_u by e^{-i psi}.  psi set on the edges of a breadth-first spanning
+// forest, children before parents, brings every z_v to 1 but the roots'.
+// Each root keeps the phase of the product of its component's z_v: 1 up to
+// rounding when the component's BP estimate of <psi|psi> (invariant under
+// message phases) is real and positive.
+void move_partition_phases(gbtn_plan* P) {
+  constexpr double kTwoPi = 6.283185307179586;
+  cudaStream_t s = P->ctx->stream;
+  compute_rdms(P);
+  std::vector<double> r(2 * P->n_rdm);
+  copy_out(P, r.data(), P->d_rdm.p, sizeof(double) * 2 * P->n_rdm, GBTN_HOST);
+  std::vector<double> phi(P->nv);
+  for (int v = 0; v < P->nv; ++v) {
+    double zr = 0.0, zi = 0.0;
+    for (int q = 0; q < P->dsite[v]; ++q) {
+      zr += r[2 * (P->rdm_off[v] + q + P->dsite[v] * q)];
+      zi += r[2 * (P->rdm_off[v] + q + P->dsite[v] * q) + 1];
+    }
+    if (!std::isfinite(zr) || !std::isfinite(zi) || (zr == 0.0 && zi == 0.0)) return;  // nothing to move
+    phi[v] = std::atan2(zi, zr);
+  }
+  std::vector<std::vector<int>> adj(P->nv);
+  for (int e = 0; e < P->ne; ++e) {
+    adj[P->eu[e]].push_back(e);
+    adj[P->ev[e]].push_back(e);
+  }
+  std::vector<int> order, parent(P->nv, -1);
+  std::vector<char> seen(P->nv, 0);
+  order.reserve(P->nv);
+  for (int root = 0; root < P->nv; ++root) {
+    if (seen[root]) continue;
+    seen[root] = 1;
+    size_t head = order.size();
+    order.push_back(root);
+    while (head < order.size()) {
+      const int v = order[head++];
+      for (int e : adj[v]) {
+        const int w = P->eu[e] == v ? P->ev[e] : P->eu[e];
+        if (seen[w]) continue;
+        seen[w] = 1;
+        parent[w] = e;
+        order.push_back(w);
+      }
+    }
+  }
+  std::vector<double> acc(P->nv, 0.0), f(4 * (size_t)P->ne);
+  for (int de = 0; de < 2 * P->ne; ++de) {
+    f[2 * de] = 1.0;
+    f[2 * de + 1] = 0.0;
+  }
+  for (int k = (int)order.size() - 1; k >= 0; --k) {
+    const int v = order[k], e = parent[v];
+    if (e < 0) continue;
+    const int p = P->eu[e] == v ? P->ev[e] : P->eu[e];
+    const double ps = std::remainder(-phi[v] - acc[v], kTwoPi);  // onto m_{p->v}; -ps onto m_{v->p}
+    const int de_in = P->eu[e] == p ? 2 * e : 2 * e + 1;
+    f[2 * de_in] = std::cos(ps);
+    f[2 * de_in + 1] = std::sin(ps);
+    f[2 * (de_in ^ 1)] = std::cos(ps);
+    f[2 * (de_in ^ 1) + 1] = -std::sin(ps);
+    acc[p] -= ps;
+  }
+  DevBuf<double> d_f;
+  d_f.upload(f, s);
+  scale_messages_z_kernel<<<2 * P->ne, 64, 0, s>>>(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, d_f.p,
+                                                   P->d_msg[P->cur].p);
+  GBTN_CUDA(cudaGetLastError());
+  GBTN_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace
+
 namespace gbtn {
 cudaStream_t ctx_stream(gbtn_ctx* c) { return c->stream; }
 void set_ctx_error(gbtn_ctx* c, const char* msg) { set_err(c, msg); }
@@ -1695,6 +1790,7 @@ int gbtn_rescale_partitions(gbtn_plan* P) {
     GBTN_CUDA(cudaGetLastError());
     P->fac32_valid = false;
     P->zimg_valid = false;
+    if (!P->sep_bra && P->ne > 0) move_partition_phases(P);
     GBTN_CUDA(cudaStreamSynchronize(s));
     return GBTN_OK;
   }

@@ -465,9 +465,13 @@ __global__ void rescale_messages_z_kernel(int ne, const int* dchi, const long lo
     sg = nr > 0.0 ? 1.0 : (nr < 0.0 ? -1.0 : 0.0);
     nr *= sg;
   }
-  // principal square root of n, then its reciprocal
+  // principal square root of n, then its reciprocal: the larger component from
+  // sqrt((|n| + |Re n|) / 2), the other as Im n / (2 * it), so that neither
+  // cancels (|n| + Re n loses digits when n is near the negative real axis)
   const double mod = sqrt(nr * nr + ni * ni);
-  const double sr = sqrt(0.5 * (mod + nr)), si = copysign(sqrt(0.5 * (mod - nr)), ni);
+  const double h = sqrt(0.5 * (mod + fabs(nr)));
+  const double sr = nr >= 0.0 ? h : (h > 0.0 ? fabs(ni) / (2.0 * h) : 0.0);
+  const double si = nr >= 0.0 ? (h > 0.0 ? ni / (2.0 * h) : 0.0) : copysign(h, ni);
   const double sm2 = sr * sr + si * si;
   const double fr = sr / sm2, fi = -si / sm2;  // n^(-1/2)
   const zdouble ka(sg * ia * fr, sg * ia * fi), kb(ib * fr, ib * fi);

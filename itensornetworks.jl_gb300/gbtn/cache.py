@@ -32,6 +32,10 @@ class BeliefPropagationCache:
     def __init__(self, tn: TensorNetwork, messages=None, bra=None, ctx=None):
         if tn.tensors is None:
             raise ValueError("the network has no tensors")
+        # the cache's own network object: set_factors and rescale_partitions
+        # replace its tensor list, never the caller's (rescale and normalize
+        # return new networks, as in the reference)
+        tn = tn.shallow_copy()
         self.tn = tn
         self.ctx = ctx or _lib.default_context()
         self.lib = self.ctx.lib

@@ -142,6 +142,13 @@ class TensorNetwork:
         d.complex_values = 1 if self.is_complex else 0
         return d, keep
 
+    def shallow_copy(self):
+        """A new network object sharing the tensor arrays: replacing its tensor
+        list leaves this one untouched."""
+        ts = None if self.tensors is None else list(self.tensors)
+        return TensorNetwork(self.nv, self.edges, self.site_dims, self.edge_dims, ts,
+                             [list(l) for l in self.legs], self.vertex_network, self.n_networks)
+
     def copy(self):
         ts = None if self.tensors is None else [t.copy() for t in self.tensors]
         return TensorNetwork(self.nv, self.edges, self.site_dims, self.edge_dims, ts,

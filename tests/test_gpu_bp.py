@@ -169,7 +169,9 @@ def test_rescale_gives_unit_scalars():
     bpc.rescale()
     np.testing.assert_allclose(bpc.edge_scalars(), 1.0, rtol=1e-12)
     np.testing.assert_allclose(bpc.vertex_scalars(), 1.0, rtol=1e-12)
+    assert all(np.array_equal(t, a) for t, a in zip(tn.tensors, A))  # the input network is not rescaled
     psi = gbtn.normalize(tn, cache_update_kwargs=dict(maxiter=20))
+    assert all(np.array_equal(t, a) for t, a in zip(tn.tensors, A))
     assert gbtn.scalar(psi, cache_update_kwargs=dict(maxiter=20)) == pytest.approx(1.0, rel=1e-10)
 
 

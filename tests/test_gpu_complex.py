@@ -138,11 +138,11 @@ def test_complex_paths_outside_fp64_are_unsupported():
 
 def test_complex_rescale_partitions_and_normalize_match_the_oracle():
     # normalize(alg="bp") of a complex state: messages rescaled, then every ket
-    # divided by its norm and scaled by z^(-1/2) of its partition scalar.  Ten
-    # sweeps: on random complex tensors BP amplifies the rounding-level
-    # anti-Hermitian part of the messages (1e-15 after ten sweeps, O(1) after a
-    # hundred), after which the messages and partition scalars carry free phases
-    kw = dict(maxiter=10, schedule="parallel")
+    # divided by its norm and scaled by z^(-1/2) of its partition scalar.  On
+    # random complex tensors BP amplifies rounding-level message phases about
+    # threefold per sweep, so after 40 sweeps the partition scalars carry O(1)
+    # phases; the library moves them onto the (phase-free) messages
+    kw = dict(maxiter=40, schedule="parallel")
     g = O.square_lattice(4, 3, chi=2)
     tn, A = cnet(g, 21)
     bpc = gbtn.BeliefPropagationCache(tn).update(**kw)
@@ -152,12 +152,13 @@ def test_complex_rescale_partitions_and_normalize_match_the_oracle():
     got = bpc.factors()
     for v in range(g.nv):
         np.testing.assert_allclose(got[v], ref[v], rtol=0, atol=1e-12 * np.max(np.abs(ref[v])))
-    # the shared bra carries conj of the ket's factor: each partition scalar
-    # keeps only its phase, and it is real and positive for <psi|psi>
-    vs = bpc.vertex_scalars()
-    np.testing.assert_allclose(np.abs(vs), 1.0, rtol=0, atol=1e-12)
-    np.testing.assert_allclose(vs, 1.0, rtol=0, atol=1e-10)
-    # the module-level normalize returns the same kets, and its BP norm is 1
+    # every vertex and edge scalar 1, as in the reference's cache
+    np.testing.assert_allclose(bpc.vertex_scalars(), 1.0, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(bpc.edge_scalars(), 1.0, rtol=0, atol=1e-12)
+    # the caller's network is left alone (rescale returns a new one) ...
+    assert all(np.array_equal(t, a) for t, a in zip(tn.tensors, A))
+    # ... so the module-level normalize runs the same sweeps from the same
+    # tensors and returns the same kets, with BP norm 1
     out = gbtn.normalize(tn, cache_update_kwargs=kw)
     for v in range(g.nv):
         np.testing.assert_allclose(out.tensors[v], ref[v], rtol=0, atol=1e-12 * np.max(np.abs(ref[v])))

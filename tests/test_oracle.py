@@ -83,7 +83,7 @@ def test_product_state_bp_exact():
 
 
 def test_normalize_gives_unit_scalars():
-    # test_normalize.jl:96-132
+    # test_normalize.jl:30-66 (a real state here; the ComplexF32 one runs on the GPU path)
     g = O.square_lattice(3, 2, chi=2)
     A = O.random_network(g, 1234)
     m, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=20)
