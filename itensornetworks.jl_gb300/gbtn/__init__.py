@@ -8,7 +8,8 @@ from .cache import (BeliefPropagationCache, environment, expect, initialize_cach
                     message_diff, norm, norm_sqr, normalize, rescale, scalar, update, updated_message)
 from .partition import CoarseGraining, PartitionedBPCache, partitioned_cache
 from .sharded import GpuShard, ShardPlan, block_owner, run_distributed, run_local
-from .su import SimpleUpdateState, apply, bp_environments, checkerboard_edges, tebd, tfim_gate
+from .su import SimpleUpdateState, apply, bp_environments, checkerboard_edges, tebd, tebd_gates, tfim_gate
+from .opsum import OpSum, group_terms, trotter2_gates
 from .network import (TensorNetwork, default_edge_sequence, disjoint_union, parallel_edge_sequence,
                       random_network, random_tensors, square_lattice)
 
@@ -19,5 +20,5 @@ __all__ = [
     "parallel_edge_sequence", "random_network", "random_tensors", "rescale", "scalar", "square_lattice", "update",
     "updated_message", "SimpleUpdateState", "apply", "checkerboard_edges", "tebd", "tfim_gate", "bp_environments",
     "CoarseGraining", "PartitionedBPCache", "partitioned_cache", "GpuShard", "ShardPlan", "block_owner",
-    "run_distributed", "run_local",
+    "run_distributed", "run_local", "tebd_gates", "OpSum", "group_terms", "trotter2_gates",
 ]

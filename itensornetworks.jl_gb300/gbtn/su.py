@@ -154,8 +154,20 @@ def checkerboard_edges(Lx, Ly):
     return classes
 
 
-def tebd(psi: TensorNetwork, gate_of_edge, edge_classes, nsteps, maxdim, cutoff, normalize=True, chi_max=None,
-         state=None, bp_envs=False, bp_maxiter=30, bp_tol=1e-12, bp_precision="f64"):
+def tebd(*args, **kwargs):
+    """Two forms.  ``tebd(H, psi, beta=, dbeta=, maxdim=, cutoff=,
+    print_frequency=10, ortho=False)`` with an OpSum H is the reference's
+    signature (src/tebd.jl:2-31; see gbtn.opsum) and returns the evolved network.
+    ``tebd(psi, gate_of_edge, edge_classes, nsteps, maxdim, cutoff, ...)`` runs
+    precomputed two-site gates class by class (tebd_gates)."""
+    from .opsum import OpSum, tebd_opsum
+    if args and isinstance(args[0], OpSum):
+        return tebd_opsum(*args, **kwargs)
+    return tebd_gates(*args, **kwargs)
+
+
+def tebd_gates(psi: TensorNetwork, gate_of_edge, edge_classes, nsteps, maxdim, cutoff, normalize=True, chi_max=None,
+               state=None, bp_envs=False, bp_maxiter=30, bp_tol=1e-12, bp_precision="f64"):
     """nsteps Trotter steps: every class of vertex-disjoint edges in order
     (tebd.jl:2-31 with a checkerboard gate order).  Returns the final state and
     the truncation errors of the last step.

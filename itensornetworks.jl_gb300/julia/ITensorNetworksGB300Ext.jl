@@ -19,7 +19,8 @@
 #
 # It also adds `apply(Algorithm("gb300"), gates, psi; maxdim, cutoff, normalize,
 # envs)`, the simple update of src/apply.jl:33-160 on the GPU (FP64 truncated
-# SVD), and a ChainRulesCore rrule for `bp_energy(psi, ops, coefs)`, the BP
+# SVD), `tebd(Algorithm("gb300"), ℋ, ψ; β, Δβ, maxdim, cutoff)` over it (src/tebd.jl),
+# and a ChainRulesCore rrule for `bp_energy(psi, ops, coefs)`, the BP
 # two-site energy, whose pullback is the library's hand-written adjoint
 # (implicit differentiation at the BP fixed point).
 #
@@ -29,7 +30,7 @@ module ITensorNetworksGB300Ext
 
 using ITensorNetworks: ITensorNetworks, AbstractBeliefPropagationCache, BeliefPropagationCache,
     messages, set_messages, partitioned_tensornetwork, quotientedges, tensornetwork
-using ITensors: ITensor, Index, inds, commonind, array, itensor, dag, prime, tags
+using ITensors: ITensors, ITensor, Index, inds, commonind, array, itensor, dag, prime, tags
 using NDTensors: Algorithm, @Algorithm_str
 using NamedGraphs.PartitionedGraphs: QuotientEdge, quotientvertices
 using GB300TensorNetworks: libgbtn
@@ -278,6 +279,30 @@ function ITensorNetworks.apply(::Algorithm"gb300", gates::Vector{ITensor}, psi; 
             ccall((:gbtn_su_destroy, libgbtn), Cint, (Ptr{Cvoid},), h[])
         end
     end
+end
+
+"""
+    tebd(Algorithm("gb300"), ℋ, ψ; β, Δβ, maxdim, cutoff, print_frequency=10, ortho=false)
+
+src/tebd.jl:2-31 with the gate list applied by the GPU simple update: the
+gates are the caller's ITensors `exp(-Δβ * ℋ; alg=Trotter{2}())`, so they are
+the reference's; each of the `Int(β ÷ Δβ)` steps is one
+`apply(Algorithm("gb300"), gates, ψ; maxdim, cutoff, normalize=true)`.  The
+terms of ℋ must be grouped per edge (two-site gates), as the reference's test
+does with `group_terms`; `ortho=true` (tree_orthogonalize) is not provided.
+"""
+function ITensorNetworks.tebd(::Algorithm"gb300", ℋ, ψ; β, Δβ, maxdim, cutoff, print_frequency=10,
+                              ortho=false)
+    ortho && error("tebd(Algorithm(\"gb300\"), ...; ortho=true): tree_orthogonalize is not provided by libgbtn")
+    𝒰 = exp(-Δβ * ℋ; alg=ITensors.Trotter{2}())
+    u⃗ = Vector{ITensor}(𝒰, ITensorNetworks.siteinds(ψ))
+    all(g -> length(inds(g)) == 4, u⃗) ||
+        error("tebd(Algorithm(\"gb300\")): every gate must act on the two sites of an edge (group the terms per edge)")
+    for step in 1:Int(β ÷ Δβ)
+        step % print_frequency == 0 && @show step, (step - 1) * Δβ, β
+        ψ = ITensorNetworks.apply(Algorithm("gb300"), u⃗, ψ; maxdim, cutoff, normalize=true)
+    end
+    return ψ
 end
 
 # ---- BP energy and its adjoint (ChainRulesCore) ------------------------------

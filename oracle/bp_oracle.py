@@ -25,6 +25,8 @@ bra conj(A_v) per site partition):
   ``abstractbeliefpropagationcache.jl:397-412``
 * rescale / normalize       ``beliefpropagationcache.jl:121-139``,
   ``abstractbeliefpropagationcache.jl:349-395``, ``src/normalize.jl:63-80``
+* tebd                      ``src/tebd.jl:2-31`` (Trotter{2} gates, Strang
+  splitting), ``test/utils.jl:174-192,239-246`` (Ising model, group_terms)
 * simple update (apply)     ``src/apply.jl:9-146`` with ITensors' truncation
   rule restated in :func:`truncate_spectrum`.
 
@@ -546,6 +548,88 @@ def normalize_bp(g, A, msgs):
     partitions (normalize.jl:63-80).  Returns (new site tensors, messages)."""
     msgs = rescale_messages(g, msgs)
     return rescale_partitions(g, A, msgs), msgs
+
+
+# ----------------------------------------------------------------------------
+# tebd(H, psi; beta, dbeta, maxdim, cutoff) with a second-order Trotter product
+# ----------------------------------------------------------------------------
+
+# ITensors' "S=1/2" operators in the basis (up, down): S = sigma / 2
+SPIN_HALF = {
+    "Id": np.eye(2),
+    "Sz": np.diag([0.5, -0.5]),
+    "Sx": np.array([[0.0, 0.5], [0.5, 0.0]]),
+    "Sy": np.array([[0.0, -0.5j], [0.5j, 0.0]]),
+    "S+": np.array([[0.0, 1.0], [0.0, 0.0]]),
+    "S-": np.array([[0.0, 0.0], [1.0, 0.0]]),
+}
+
+
+def ising_terms(g, J1=-1.0, h=0.0):
+    """The Ising model of the reference's tests (test/utils.jl:174-192, J2 = 0):
+    J1 Sz Sz on every edge in edge order, then h Sx on every vertex.  Terms are
+    (coefficient, [(operator, vertex), ...])."""
+    terms = [(J1, [("Sz", u), ("Sz", v)]) for (u, v) in g.edges]
+    terms += [(h, [("Sx", v)]) for v in range(g.nv)]
+    return terms
+
+
+def group_terms(terms, g):
+    """test/utils.jl:239-246: every term joins the group of the first edge (in
+    edge order) holding all its sites; groups keep the order in which their
+    edges first appear among the terms.  Returns [(edge, [terms])]."""
+    groups = {}
+    for t in terms:
+        sites = {v for _, v in t[1]}
+        e = next(k for k, (u, v) in enumerate(g.edges) if sites <= {u, v})
+        groups.setdefault(e, []).append(t)
+    return list(groups.items())
+
+
+def group_matrix(g, e, terms):
+    """Sum of the terms as a (du dv) x (du dv) matrix on edge e = (u, v), row
+    s'_u + du s'_v (the gate convention of simple_update)."""
+    u, v = g.edges[e]
+    H = 0
+    for c, ops in terms:
+        Ou, Ov = np.eye(2), np.eye(2)
+        for name, x in ops:  # a product as written: op1 op2 ... on each site
+            if x == u:
+                Ou = Ou @ SPIN_HALF[name]
+            else:
+                Ov = Ov @ SPIN_HALF[name]
+        H = H + c * np.kron(Ov, Ou)  # row index s'_u + 2 s'_v
+    return H
+
+
+def trotter2_gates(g, groups, dbeta):
+    """exp(-dbeta H) as a symmetric second-order Trotter product (Strang
+    splitting, the published form of ITensors' Trotter{2}): exp(-dbeta/2 h_k)
+    for the groups in order, then in reverse order.  Returns [(edge, gate)]."""
+    half = []
+    for e, terms in groups:
+        h = group_matrix(g, e, terms)
+        w, U = np.linalg.eigh(h)  # the terms are Hermitian
+        half.append((e, (U * np.exp(-0.5 * dbeta * w)) @ U.conj().T))
+    return half + half[::-1]
+
+
+def tebd(g, A, groups, beta, dbeta, maxdim, cutoff):
+    """tebd.jl:2-31 with ortho = false: int(beta / dbeta) (floor) steps, each
+    applying the Trotter gates one by one with normalize = true and no
+    environments (apply.jl:148-160 -> simple_update_bp without envs).
+    Returns (graph with the new bond dimensions, tensors)."""
+    g = Graph(g.nv, g.edges, g.site_dims, list(g.edge_dims), [list(l) for l in g.legs])
+    A = [a.copy() for a in A]
+    seq = trotter2_gates(g, groups, dbeta)
+    for _ in range(int(beta // dbeta)):
+        for e, gate in seq:
+            u, v = g.edges[e]
+            pu, pv = g.legs[u].index(e), g.legs[v].index(e)
+            Au, Av, _, _ = simple_update(gate, A[u], A[v], pu, pv, {}, {}, maxdim=maxdim, cutoff=cutoff)
+            A[u], A[v] = Au / np.linalg.norm(Au), Av / np.linalg.norm(Av)
+            g.edge_dims[e] = Au.shape[pu + 1]
+    return g, A
 
 
 # ----------------------------------------------------------------------------
