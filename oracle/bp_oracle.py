@@ -20,6 +20,7 @@ bra conj(A_v) per site partition):
 * identity messages         ``src/formnetworks/quadraticformnetwork.jl:96-124``
 * forest-cover edge order   ``src/edge_sequences.jl:32-47``
 * environment / expect      ``src/caches/beliefpropagationcache.jl:100-105``,
+  exact environment ``src/environment.jl:6-20``,
   ``src/expect.jl:5-19``; two-site RDM ``test/test_belief_propagation.jl:64-91``
 * region scalars, logscalar ``beliefpropagationcache.jl:107-119``,
   ``abstractbeliefpropagationcache.jl:397-412``
@@ -657,6 +658,31 @@ def exact_rdm1(g, A, v, B=None):
             sp = s
         ops += [A[w], [s] + [ket_link[e] for e in g.legs[w]]]
         ops += [np.conj(B[w]), [sp] + [bra_link[e] for e in g.legs[w]]]
+    return np.einsum(*ops, out, optimize="greedy")
+
+
+def exact_environment(g, A, v, B=None):
+    """Exact environment of vertex v in <B|A> (environment(qf, [v]; alg =
+    "exact"), environment.jl:6-20): every other ket and bra tensor contracted,
+    v's links left open.  Index order: v's bra links, then its ket links (leg
+    order); the site indices of v meet through the identity operator, which is
+    left out."""
+    B = A if B is None else B
+    nid = [0]
+
+    def new():
+        nid[0] += 1
+        return nid[0]
+    ket_link = {e: new() for e in range(g.ne)}
+    bra_link = {e: new() for e in range(g.ne)}
+    ops = []
+    for w in range(g.nv):
+        if w == v:
+            continue
+        s = new()
+        ops += [A[w], [s] + [ket_link[e] for e in g.legs[w]]]
+        ops += [np.conj(B[w]), [s] + [bra_link[e] for e in g.legs[w]]]
+    out = [bra_link[e] for e in g.legs[v]] + [ket_link[e] for e in g.legs[v]]
     return np.einsum(*ops, out, optimize="greedy")
 
 
