@@ -26,11 +26,24 @@ rank), :class:`GpuShard` runs one rank's block through the library, and two
 drivers move the boundary messages: :func:`run_local` (every block in one
 process, exchange by copies -- one GPU or a test) and :func:`run_distributed`
 (one block per process, torch.distributed point-to-point sends and an
-all-reduce; NCCL between GPUs, gloo on the host)."""
+all-reduce; NCCL between GPUs, gloo on the host).
+
+Both drivers move boundary messages through torch tensors on an exchange
+device.  On a GPU (``device="cuda"``, the default with NCCL) a block's messages
+are copied device to device out of the library into one tensor, the entries of
+each cut edge are gathered there and sent with NCCL, and the received entries
+are scattered back before the copy into the library.  The library runs on
+torch's current stream meanwhile, so the copies, gathers, NCCL waits and sweeps
+are ordered on one stream and no message crosses the host.  On the host
+(gloo, or a test double of a block) the same steps run on CPU tensors."""
 from __future__ import annotations
+
+import ctypes as C
+from contextlib import contextmanager
 
 import numpy as np
 
+from . import _lib
 from .network import TensorNetwork
 
 
@@ -124,8 +137,74 @@ class GpuShard:
     def set_messages(self, flat):
         self.bpc.set_messages(np.ascontiguousarray(flat))
 
+    # -- device-resident exchange ------------------------------------------------
+    def message_count(self):
+        return self.bpc.n_message
+
+    def is_complex(self):
+        return self.bpc.complex
+
+    def messages_to(self, buf):
+        """Copy the block's flat messages into ``buf``, a contiguous CUDA tensor
+        of message_count() elements (device to device, on the context's stream)."""
+        self.bpc._c(self.bpc.lib.gbtn_get_messages(self.bpc.handle, C.c_void_p(buf.data_ptr()), _lib.DEVICE))
+
+    def messages_from(self, buf):
+        self.bpc._c(self.bpc.lib.gbtn_set_messages(self.bpc.handle, C.c_void_p(buf.data_ptr()), _lib.DEVICE))
+
+    @contextmanager
+    def on_stream(self, stream_ptr):
+        """Run the library on ``stream_ptr`` (a raw cudaStream_t) inside the block."""
+        ctx = self.bpc.ctx
+        old = ctx.stream
+        ctx.set_stream(stream_ptr)
+        try:
+            yield
+        finally:
+            ctx.set_stream(old)
+
     def close(self):
         self.bpc.close()
+
+
+class _Exchange:
+    """A block's messages as one torch tensor on the exchange device, with the
+    flat entry indices of its cut edges there."""
+
+    def __init__(self, shard, device):
+        import torch
+        self.torch = torch
+        self.shard = shard
+        self.device = device
+        plan = shard.plan
+        self.on_gpu = device.type == "cuda"
+        if self.on_gpu:
+            dt = torch.complex128 if shard.is_complex() else torch.float64
+            self.buf = torch.empty(max(shard.message_count(), 1), dtype=dt, device=device)
+        else:
+            self.buf = None
+        self.send = {q: torch.as_tensor(np.asarray(i, dtype=np.int64), device=device) for q, i in plan.send.items()}
+        self.recv = {q: torch.as_tensor(np.asarray(i, dtype=np.int64), device=device) for q, i in plan.recv.items()}
+
+    def pull(self):
+        """The block's current messages into the exchange tensor."""
+        if self.on_gpu:
+            self.shard.messages_to(self.buf)
+        else:
+            self.buf = self.torch.from_numpy(np.array(self.shard.get_messages()))
+        return self.buf
+
+    def push(self):
+        if self.on_gpu:
+            self.shard.messages_from(self.buf)
+        else:
+            self.shard.set_messages(self.buf.numpy())
+
+    def outgoing(self, q):
+        return self.buf.index_select(0, self.send[q])
+
+    def incoming(self, q, values):
+        self.buf.index_copy_(0, self.recv[q], values)
 
 
 def _finish_sweep(shard, diffs):
@@ -136,74 +215,119 @@ def _finish_sweep(shard, diffs):
     return float(d.sum()), int(d.size)
 
 
-def run_local(shards, maxiter, tol=None, init="identity"):
+def _exchange_device(device):
+    import torch
+    return torch.device(device) if device is not None else torch.device("cpu")
+
+
+@contextmanager
+def _library_on_torch_stream(shards, device):
+    """GPU blocks run on torch's current stream while the exchange uses it."""
+    if device.type != "cuda":
+        yield
+        return
+    import torch
+    stream = torch.cuda.current_stream(device).cuda_stream
+    with _nested([s.on_stream(stream) for s in shards if hasattr(s, "on_stream")]):
+        yield
+
+
+@contextmanager
+def _nested(cms):
+    if not cms:
+        yield
+        return
+    with cms[0]:
+        with _nested(cms[1:]):
+            yield
+
+
+def run_local(shards, maxiter, tol=None, init="identity", device=None):
     """Jacobi sweeps of every block in this process, boundary messages copied
-    between the blocks after each sweep.  Returns (sweeps run, last mean diff)."""
+    between the blocks after each sweep (on ``device``: "cpu" by default,
+    "cuda" for GPU blocks exchanged on the device).  Returns (sweeps run, last
+    mean diff)."""
     if maxiter is None or maxiter < 1:
         raise ValueError("You need to specify a number of iterations for BP!")
-    by_rank = {s.plan.rank: s for s in shards}
-    for s in shards:
-        s.init_messages(init)
+    dev = _exchange_device(device)
+    ex = {s.plan.rank: _Exchange(s, dev) for s in shards}
     mean = float("nan")
     it = 0
-    for it in range(1, maxiter + 1):
-        tot, cnt = 0.0, 0
-        flats = {}
+    with _library_on_torch_stream(shards, dev):
         for s in shards:
-            d = s.sweep(tol is not None)
-            a, b = _finish_sweep(s, d)
-            tot, cnt = tot + a, cnt + b
-            flats[s.plan.rank] = s.get_messages()
-        for s in shards:
-            f = flats[s.plan.rank].copy()
-            for q, idx in s.plan.recv.items():
-                f[idx] = flats[q][by_rank[q].plan.send[s.plan.rank]]
-            s.set_messages(f)
-        if tol is not None:
-            mean = tot / max(cnt, 1)
-            if mean <= tol:
-                break
+            s.init_messages(init)
+        for it in range(1, maxiter + 1):
+            tot, cnt = 0.0, 0
+            for s in shards:
+                d = s.sweep(tol is not None)
+                a, b = _finish_sweep(s, d)
+                tot, cnt = tot + a, cnt + b
+            for r in ex:  # every block's new messages before any is overwritten (Jacobi)
+                ex[r].pull()
+            if len(ex) > 1:
+                vals = {(r, q): ex[q].outgoing(r) for r in ex for q in ex[r].recv}
+                for (r, q), v in vals.items():
+                    ex[r].incoming(q, v)
+            for r in ex:
+                ex[r].push()
+            if tol is not None:
+                mean = tot / max(cnt, 1)
+                if mean <= tol:
+                    break
     return it, mean
 
 
-def run_distributed(shard, maxiter, tol=None, init="identity", group=None):
+def run_distributed(shard, maxiter, tol=None, init="identity", group=None, device=None):
     """This process's block, exchanging boundary messages with the blocks of
     the other ranks of ``group`` (torch.distributed point-to-point sends, one
-    all-reduce per sweep when ``tol`` is given).  Returns (sweeps run, last
-    mean diff), identical on every rank."""
+    all-reduce per sweep when ``tol`` is given).  The exchange tensors live on
+    ``device``: by default the GPU with NCCL and the host with other backends.
+    Returns (sweeps run, last mean diff), identical on every rank."""
     import torch
     import torch.distributed as dist
 
     if maxiter is None or maxiter < 1:
         raise ValueError("You need to specify a number of iterations for BP!")
+    if device is None:
+        device = f"cuda:{shard.bpc.ctx.device}" if str(dist.get_backend(group)) == "nccl" else "cpu"
+    dev = _exchange_device(device)
     plan = shard.plan
-    shard.init_messages(init)
+    ex = _Exchange(shard, dev)
+    cplx = ex.on_gpu and shard.is_complex()
+
+    def wire(t):  # complex entries travel as (re, im) pairs of doubles
+        return torch.view_as_real(t) if cplx else t
+
     mean = float("nan")
     it = 0
-    for it in range(1, maxiter + 1):
-        d = shard.sweep(tol is not None)
-        flat = shard.get_messages()
-        ops, inbox = [], {}
-        for q in plan.neighbours:
-            if q in plan.send:
-                ops.append(dist.P2POp(dist.isend, torch.from_numpy(np.ascontiguousarray(flat[plan.send[q]])), q,
-                                      group))
-            if q in plan.recv:
-                inbox[q] = torch.empty(len(plan.recv[q]), dtype=torch.float64)
-                ops.append(dist.P2POp(dist.irecv, inbox[q], q, group))
-        if ops:
-            for r in dist.batch_isend_irecv(ops):
-                r.wait()
-        for q, buf in inbox.items():
-            flat[plan.recv[q]] = buf.numpy()
-        shard.set_messages(flat)
-        if tol is not None:
-            a, b = _finish_sweep(shard, d)
-            t = torch.tensor([a, float(b)], dtype=torch.float64)
-            dist.all_reduce(t, group=group)
-            mean = float(t[0]) / max(float(t[1]), 1.0)
-            if mean <= tol:
-                break
+    with _library_on_torch_stream([shard], dev):
+        shard.init_messages(init)
+        for it in range(1, maxiter + 1):
+            d = shard.sweep(tol is not None)
+            ex.pull()
+            ops, inbox, keep = [], {}, []
+            for q in plan.neighbours:
+                if q in ex.send:
+                    out = ex.outgoing(q)
+                    keep.append(out)
+                    ops.append(dist.P2POp(dist.isend, wire(out), q, group))
+                if q in ex.recv:
+                    inbox[q] = torch.empty(len(plan.recv[q]), dtype=ex.buf.dtype, device=dev)
+                    ops.append(dist.P2POp(dist.irecv, wire(inbox[q]), q, group))
+            if ops:
+                for r in dist.batch_isend_irecv(ops):
+                    r.wait()
+            for q, buf in inbox.items():
+                ex.incoming(q, buf)
+            ex.push()
+            if tol is not None:
+                a, b = _finish_sweep(shard, d)
+                t = torch.tensor([a, float(b)], dtype=torch.float64, device=dev)
+                dist.all_reduce(t, group=group)
+                tot, cnt = t.tolist()
+                mean = tot / max(cnt, 1.0)
+                if mean <= tol:
+                    break
     return it, mean
 
 

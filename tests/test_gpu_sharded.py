@@ -26,13 +26,16 @@ def _unsplit_gpu(tn, sweeps, tol=None):
     return bpc
 
 
+@pytest.mark.parametrize("device", ["cpu", "cuda"])
 @pytest.mark.parametrize("blocks", [(2, 1), (2, 2), (3, 2)])
-def test_split_gpu_sweeps_match_unsplit(blocks):
+def test_split_gpu_sweeps_match_unsplit(blocks, device):
+    # device "cuda": boundary messages gathered and scattered in device tensors
+    # (the NCCL path's data movement) with the library on torch's stream
     L, sweeps = 8, 10
     tn = gbtn.random_network(gbtn.square_lattice(L, L, chi=3), 21)
     owner = block_owner(L, *blocks)
     shards = [GpuShard(ShardPlan(tn, owner, r)) for r in range(blocks[0] * blocks[1])]
-    it, _ = run_local(shards, maxiter=sweeps)
+    it, _ = run_local(shards, maxiter=sweeps, device=device)
     ref = _unsplit_gpu(tn, sweeps).messages()
     got = {}
     for s in shards:
@@ -43,11 +46,12 @@ def test_split_gpu_sweeps_match_unsplit(blocks):
     assert err <= 1e-12, err
 
 
-def test_split_gpu_convergence_matches_unsplit():
+@pytest.mark.parametrize("device", ["cpu", "cuda"])
+def test_split_gpu_convergence_matches_unsplit(device):
     L, tol = 8, 1e-10
     tn = gbtn.random_network(gbtn.square_lattice(L, L, chi=2), 4)
     shards = [GpuShard(ShardPlan(tn, block_owner(L, 2, 2), r)) for r in range(4)]
-    it, mean = run_local(shards, maxiter=200, tol=tol)
+    it, mean = run_local(shards, maxiter=200, tol=tol, device=device)
     for s in shards:
         s.close()
     ref = _unsplit_gpu(tn, 200, tol)
