@@ -45,6 +45,12 @@ constexpr int kSvdMaxSweeps = 40;
 // cannot change the decomposition beyond eps ||A||).
 constexpr double kJacobiTol = 1e-13;
 constexpr double kJacobiTiny = 1e-30;
+// A sweep whose rotations all had couplings |g| / sqrt(a b) at or below this
+// ends the FP64 Jacobi: each rotation leaves its pair coupled to about 1e-7 of
+// its coupling (the FP32 tangent), and later rotations of the sweep couple
+// pairs again only by products of two couplings, so every coupling left is
+// about 1e-14, below kJacobiTol, and the next sweep would rotate nothing.
+constexpr double kJacobiLastSweep = 1e-7;
 // Noise bound of the Jacobi stage of a gate's SVD (n singular values, relative
 // cutoff on sigma^2): pairs of columns both at or below skip_rel * ||theta||^2
 // are not rotated.  Those columns sum to at most n * skip_rel <= cutoff / 2 of
@@ -206,13 +212,15 @@ __device__ void cta_qrcp(double* A, int m, int n, SvdBufs& b) {
 // is sure to discard all such columns (n * skip_rel well inside its relative
 // cutoff) loses nothing, and the sweeps spent orthogonalising noise columns of
 // a rank-deficient theta against each other are saved; skip_rel = 0 keeps
-// every column exact.
+// every column exact.  Sweeps also stop after one whose couplings were all at
+// or below kJacobiLastSweep (flag bit 1 marks a larger one).
 __device__ void cta_jacobi(double* X, int m, int n, int* flag, double* red, double skip_rel) {
   const int tid = threadIdx.x, grp = tid >> 3, gl = tid & 7;
   double f = 0.0;
   for (int i = tid; i < m * n; i += kSuThreads) f = fma(X[i], X[i], f);
   f = block_sum(f, red);
   const double tiny = f * kJacobiTiny, tol2 = kJacobiTol * kJacobiTol, small = f * skip_rel;
+  const double last2 = kJacobiLastSweep * kJacobiLastSweep;
   const int N = n + (n & 1);  // players of the round-robin (one dummy when n is odd)
   const int npair = N / 2;
   const bool warp_busy = (tid >> 5) * 4 < npair;  // warp-uniform
@@ -265,13 +273,13 @@ __device__ void cta_jacobi(double* X, int m, int n, int* flag, double* red, doub
               a[i] = fma(c, x, -s * y);
               b[i] = fma(s, x, c * y);
             }
-            if (gl == 0) *flag = 1;
+            if (gl == 0) atomicOr(flag, ga * ga > last2 * al * be ? 3 : 1);
           }
         }
       }
       __syncthreads();
     }
-    if (*flag == 0) break;
+    if ((*flag & 2) == 0) break;  // nothing rotated, or only couplings the next sweep would not see
     __syncthreads();
   }
 }
