@@ -2,8 +2,11 @@
 // two-site gates (simple_update_bp, src/apply.jl:33-95; apply, :97-146), and
 // the gate batches of tebd (src/tebd.jl:2-31).
 //
-// One CTA (256 threads) per gate; the gates of one launch touch disjoint
-// vertices, so they commute with each other and run concurrently.  Per gate:
+// A batch of consecutive gates on disjoint vertices (they commute) runs as
+// three launches: su_qr_kernel (one CTA per gate side: steps 1-2),
+// su_svd_kernel (one CTA per gate: steps 3-5) and su_rebuild_kernel (one CTA
+// per gate side: step 6); complex gates or tensors run the whole gate in one
+// CTA (su_gate_z_kernel).  Per gate:
 //   1. sqrt / inverse-sqrt of every environment message on the other legs of
 //      both sites (Hermitian eigen-decomposition, eigenvalues below 10 eps of
 //      the total magnitude dropped -- map_eigvals, apply.jl:9-25);
@@ -11,8 +14,11 @@
 //      (other legs) x (site, bond) with Householder reflectors: psi = Q R;
 //   3. theta = R_u R_v over the bond, the gate applied on the two site indices;
 //   4. SVD of theta: pivoted QR, then one-sided Jacobi on R^T (columns
-//      rotated in round-robin pairs, eight lanes per pair), singular values
-//      sorted in descending order;
+//      rotated in round-robin pairs, eight lanes per pair): sweeps in FP32 to
+//      2e-6, a first-order FP64 re-orthogonalisation of their rotation, then
+//      FP64 sweeps that skip pairs of noise columns the cutoff discards and
+//      stop after a sweep of couplings below 1e-7; singular values sorted in
+//      descending order;
 //   5. truncation by the rule of ITensors' svd: at most maxdim values, then drop
 //      from the tail while the discarded sum of squares stays within
 //      cutoff * sum of squares (at least one value kept); truncation error =
