@@ -25,7 +25,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import check, dptr, iptr
-from .network import TensorNetwork, default_edge_sequence, parallel_edge_sequence
+from .network import TensorNetwork, default_edge_sequence
 
 
 class BeliefPropagationCache:
