@@ -84,6 +84,17 @@ def test_library_builds_and_exports_every_declared_symbol(lib_built):
     assert set(_lib.SIGNATURES) == set(declared)
 
 
+def test_no_library_or_no_gpu_fails_loudly(lib_built, tmp_path):
+    # the product has no CPU path: a missing libgbtn.so raises on load, and a
+    # machine without a usable GPU raises when the context is made
+    with pytest.raises(gbtn.LibraryNotBuilt):
+        _lib.load(tmp_path / "libgbtn.so")
+    import torch
+    if not torch.cuda.is_available():
+        with pytest.raises(gbtn.GBTNError):
+            gbtn.Context(0)
+
+
 def test_missing_maxiter_on_loopy_graph_raises_before_gpu():
     class Fake(gbtn.BeliefPropagationCache):
         def __init__(self, tn):
