@@ -141,6 +141,15 @@ enum gbtn_kernel_class {
   GBTN_KCLASS_GAUGE = 3 /* rescale_messages: message normalisation and gauge scaling */
 };
 int gbtn_ctx_set_profiling(gbtn_ctx* ctx, int on);
+/* Failure-detection test of the bounded device waits.  on = 1 makes every
+ * tensor-core image copy launched afterwards (any context of the process;
+ * CUDA graphs captured before keep their launches) expect 16 bytes more than it
+ * delivers: the copy lands, its mbarrier never completes, the kernel's 1 s
+ * bounded wait gives up, the CTA drains its own copies, frees its TMEM and
+ * returns, and the BF16 sweep returns GBTN_ERR_TIMEOUT (the plan and context
+ * stay usable).  No fault, trap or hang.  on = 0 (the default) restores
+ * normal operation.  Not for production use. */
+int gbtn_ctx_test_wait_timeout(gbtn_ctx* ctx, int on);
 int gbtn_ctx_kernel_time(gbtn_ctx* ctx, int kernel_class, double* total_ms, int64_t* launches);
 
 /* ---- plan (BeliefPropagationCache storage) ------------------------------ */

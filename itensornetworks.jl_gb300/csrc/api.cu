@@ -1015,6 +1015,14 @@ int gbtn_ctx_set_profiling(gbtn_ctx* ctx, int on) {
   return GBTN_OK;
 }
 
+int gbtn_ctx_test_wait_timeout(gbtn_ctx* ctx, int on) {
+  gbtn_ctx* C = ctx;
+  API_TRY
+  require(ctx, "NULL context");
+  gbtn::tc_set_test_extra_tx(on ? 16u : 0u);
+  API_CATCH(C)
+}
+
 int gbtn_ctx_kernel_time(gbtn_ctx* ctx, int kernel_class, double* total_ms, int64_t* launches) {
   API_TRY
   require(ctx && total_ms && launches, "NULL argument");

@@ -53,6 +53,12 @@ constexpr uint32_t kZElems = 8192;
 constexpr uint32_t kZBytes = kZElems * 2;
 constexpr uint64_t kWaitNs = 1000000000ull;  // 1 s bound on every wait
 
+// Failure-detection test (gbtn_ctx_test_wait_timeout): bytes added to the
+// transaction count each image copy's mbarrier expects, passed to every
+// launch.  Nonzero, the copy lands but the barrier never completes, so the
+// bounded wait gives up and the sweep reports a timeout; 0 in normal use.
+unsigned int g_tc_test_extra_tx = 0;
+
 // shared-memory carve-up (bytes from a 1024-aligned base)
 constexpr int kOffZ = 0;           // 16 KB: Z image (TMA destination)
 constexpr int kOffKT = 16384;      // K12 | K34 (2 x 8 KB), then T12 as two 8 KB tiles (s = 0, 1)
@@ -270,7 +276,8 @@ __device__ __forceinline__ void pair_epilogue(uint32_t taddr, const float* Mx, c
 __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     tc_vertex_kernel(const TcRec* __restrict__ recs, int nwork, const __nv_bfloat16* __restrict__ zimg,
                      const float* msg_in,
-                     float* msg_out, double* diffs, const int* converged, int normalize, int want_diff, int* err) {
+                     float* msg_out, double* diffs, const int* converged, int normalize, int want_diff, int* err,
+                     unsigned int extra_tx) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* Z = sm + kOffZ;
@@ -316,7 +323,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
   uint32_t mma_phase = 0, tma_phase = 0;
   int tma_pending = 0, mma_pending = 0;
   auto issue_z = [&](int slot) {
-    tc::mbar_expect_tx(tma_bar, kZBytes);
+    tc::mbar_expect_tx(tma_bar, kZBytes + extra_tx);
     tc::tma_load_1d(Z, zimg + (size_t)slot * kZElems, kZBytes, tma_bar);
     tma_pending = 1;
   };
@@ -654,6 +661,8 @@ void launch_build_zimg(const int* slot_vertex, int nslot, const VDesc* vd, const
   GBTN_CUDA(cudaGetLastError());
 }
 
+void tc_set_test_extra_tx(unsigned int bytes) { g_tc_test_extra_tx = bytes; }
+
 void launch_tc_vertices(const TcRec* recs, int nwork, const __nv_bfloat16* zimg,
                         const float* msg_in, float* msg_out, double* diffs, const int* converged, int normalize,
                         int want_diff, int* err, cudaStream_t s) {
@@ -668,7 +677,7 @@ void launch_tc_vertices(const TcRec* recs, int nwork, const __nv_bfloat16* zimg,
   const int slots = kTcBlocksPerSm * nsm;
   const int grid = nwork < slots ? nwork : slots;
   tc_vertex_kernel<<<grid, kTcThreads, kSmemBytes, s>>>(recs, nwork, zimg, msg_in, msg_out, diffs,
-                                                         converged, normalize, want_diff, err);
+                                                         converged, normalize, want_diff, err, g_tc_test_extra_tx);
   GBTN_CUDA(cudaGetLastError());
 }
 

@@ -177,6 +177,8 @@ bool tc_paddable(const VDesc& d);  // d = 2, 1 <= degree <= 4, chi <= 8
 TcRec tc_record(const VDesc& d, const std::vector<long long>& msg_off);
 void launch_build_zimg(const int* slot_vertex, int nslot, const VDesc* vd, const double* fac, __nv_bfloat16* zimg,
                        cudaStream_t s);
+// Failure-detection test: extra bytes each tensor-core image copy's barrier expects.
+void tc_set_test_extra_tx(unsigned int bytes);
 void launch_tc_vertices(const TcRec* recs, int nwork, const __nv_bfloat16* zimg,
                         const float* msg_in, float* msg_out, double* diffs, const int* converged, int normalize,
                         int want_diff, int* err, cudaStream_t s);

@@ -108,6 +108,7 @@ SIGNATURES = {
     "gbtn_ctx_set_stream": (_I, [_P, _P]),
     "gbtn_ctx_get_stream": (_P, [_P]),
     "gbtn_ctx_set_profiling": (_I, [_P, _I]),
+    "gbtn_ctx_test_wait_timeout": (_I, [_P, _I]),
     "gbtn_ctx_kernel_time": (_I, [_P, _I, _D, C.POINTER(C.c_int64)]),
     "gbtn_plan_create": (_I, [_P, C.POINTER(GraphDesc), C.POINTER(_P)]),
     "gbtn_plan_destroy": (_I, [_P]),
