@@ -1060,7 +1060,8 @@ __device__ __forceinline__ zdouble zwarp_sum(zdouble x) { return zdouble(warp_su
 // warp per pair, one row per lane.  On return the columns of X are U S,
 // sig their norms and ord the descending order.  Pairs whose squared norms are
 // both at or below skip_rel * ||X||_F^2 are not rotated (as in the real
-// Jacobi: for callers whose truncation discards all such columns).
+// Jacobi: for callers whose truncation discards all such columns).  Sweeps
+// stop after one whose couplings were all at or below kJacobiLastSweep.
 __device__ void cta_zjacobi(zdouble* X, int m, int n, zdouble* V, double* sig, int* ord, int* flag,
                             double skip_rel) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1102,14 +1103,14 @@ __device__ void cta_zjacobi(zdouble* X, int m, int n, zdouble* V, double* sig, i
             V[lane + n * i] = zsub(zscale(c, vi), zmul(sec, vj));
             V[lane + n * j] = zmul(se, vi) + zscale(c, vj);
           }
-          if (lane == 0) *flag = 1;
+          if (lane == 0) atomicOr(flag, ag * ag > kJacobiLastSweep * kJacobiLastSweep * al * be ? 3 : 1);
         }
       }
       __syncthreads();
     }
     const int rotated = *flag;
     __syncthreads();
-    if (!rotated) break;
+    if ((rotated & 2) == 0) break;  // nothing rotated, or only couplings the next sweep would not see
   }
   for (int i = warp; i < n; i += kSuWarps) {
     const zdouble x = lane < m ? X[lane + m * i] : zdouble(0.0);
