@@ -531,6 +531,7 @@ def run_ours(args):
         traffic = tj["dram_bytes_per_vertex"] * n_tc
     if rank == 0:
         cpu_val, cores, sample = cpu_reference_rate(seconds=10.0)
+        cpu1_val, _, sample1 = cpu_reference_rate(seconds=3.0, nthreads=1)
         line = {
             "metric": "bp_msg_updates_per_s", "value": value, "unit": "msg-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_bf16, "higher_is_better": True,
@@ -574,7 +575,9 @@ def run_ours(args):
             "batched_uneven": batched,
             "gauge_scaling": gauge,
             "cpu_baseline": {"value": cpu_val, "unit": "msg-updates/s", "cores": cores, "kind": "port",
-                             "sample": sample},
+                             "sample": sample,
+                             "single_core": {"value": cpu1_val, "unit": "msg-updates/s", "cores": 1,
+                                             "sample": sample1}},
             "e2e": {"value": aggregate_rate(world, msgs_step, e2e_ms), "unit": "msg-updates/s",
                     "h2d_bytes_per_step": n_fac * 8, "d2h_bytes_per_step": n_msg * 8},
             "gpu_launches": int(tc_n + simt_n + 2),
