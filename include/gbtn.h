@@ -58,7 +58,9 @@ enum gbtn_schedule { GBTN_SCHED_SEQUENTIAL = 0, GBTN_SCHED_PARALLEL = 1, GBTN_SC
 
 /* Arithmetic of the message contractions.  MIXED runs BF16 tensor-core
  * sweeps (FP32 accumulation), then FP32 sweeps, then FP64 sweeps, each phase
- * started from the previous phase's fixed point. */
+ * started from the previous phase's fixed point.  BF16 and MIXED run the
+ * PARALLEL and COLORED schedules (SEQUENTIAL returns GBTN_ERR_UNSUPPORTED);
+ * FP32 and FP64 run all three. */
 enum gbtn_precision { GBTN_F64 = 0, GBTN_F32 = 1, GBTN_BF16 = 2, GBTN_MIXED = 3 };
 
 enum gbtn_message_init { GBTN_INIT_IDENTITY = 0, GBTN_INIT_ONES = 1 };

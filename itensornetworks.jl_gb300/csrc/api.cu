@@ -1358,16 +1358,10 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
   }
   if (o->precision == GBTN_BF16 && o->schedule == GBTN_SCHED_SEQUENTIAL)
     throw Unsupported("BF16 sweeps run the parallel or coloured schedule");
+  if (o->precision == GBTN_MIXED && o->schedule == GBTN_SCHED_SEQUENTIAL)
+    throw Unsupported("the mixed BF16 -> FP32 -> FP64 pipeline runs the parallel or coloured schedule");
   if (P->cplx && o->precision == GBTN_BF16)
     throw Unsupported("complex tensors have no tensor-core (BF16) path: use f32, mixed or f64");
-  if (P->ne == 0) {  // nothing to sweep: maxiter no-op iterations, mean diff 0/0 = NaN (never <= tol), as the
-                     // reference's update loop on an empty edge sequence (abstractbeliefpropagationcache.jl:313-329)
-    for (int n = 0; n < P->nnet; ++n) {
-      if (iters) iters[n] = o->maxiter;
-      if (mean_diff) mean_diff[n] = NAN;
-    }
-    return GBTN_OK;
-  }
   if (o->schedule == GBTN_SCHED_SEQUENTIAL) {
     require(o->edge_sequence && o->edge_sequence_len > 0, "SEQUENTIAL needs an edge sequence");
     std::vector<std::vector<int2>> per(P->nnet);

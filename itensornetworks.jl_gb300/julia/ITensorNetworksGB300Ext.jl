@@ -6,7 +6,9 @@
 # `[extensions] ITensorNetworksGB300Ext = "GB300TensorNetworks"`).
 #
 # It adds the algorithm "gb300_bp": `update(bpc; alg="gb300_bp", maxiter, tol,
-# schedule, precision)` packs the cache's partitioned tensor network into the
+# schedule, edge_sequence, precision)` (the reference's defaults: sequential
+# sweeps in default_bp_edge_sequence order, maxiter 1 on trees and required
+# otherwise) packs the cache's partitioned tensor network into the
 # C-ABI layout (include/gbtn.h), runs the sweeps on the GPU and writes the
 # messages back into the cache, so `expect`, `environment`, `scalar`,
 # `logscalar`, `inner`, `norm` and `normalize` keep their signatures and read
@@ -32,6 +34,7 @@ using ITensorNetworks: ITensorNetworks, AbstractBeliefPropagationCache, BeliefPr
     messages, set_messages, partitioned_tensornetwork, quotientedges, tensornetwork
 using ITensors: ITensors, ITensor, Index, inds, commonind, array, itensor, dag, prime, tags
 using NDTensors: Algorithm, @Algorithm_str
+using Graphs: src, dst
 using NamedGraphs.PartitionedGraphs: QuotientEdge, quotientvertices
 using GB300TensorNetworks: libgbtn
 using ChainRulesCore: ChainRulesCore, NoTangent
@@ -84,24 +87,34 @@ function context()
     return CTX[]
 end
 
-# Pack the ket layer of a QuadraticFormNetwork cache: vertex order =
+# Pack the ket and bra layers of a form-network cache: vertex order =
 # partitions, edges = quotient edges (src < dst), legs in each ket tensor's
-# index order after the site index.
+# index order after the site index.  The bra layer holds dag(phi) (with its
+# site and link indices mapped); the library conjugates the bra it is given,
+# so it receives phi = conj(bra), in the ket's leg order.  When phi equals the
+# ket everywhere (a QuadraticFormNetwork) the plan shares the bra
+# (separate_bra = 0), which keeps the tensor-core path; otherwise (inner(phi,
+# psi), a BilinearFormNetwork with the identity operator) both layers are
+# passed.  Operator tensors are taken to be identities.
 function pack(bpc::BeliefPropagationCache)
     pvs = collect(quotientvertices(bpc))
     vid = Dict(pv => i - 1 for (i, pv) in enumerate(pvs))
     pes = collect(quotientedges(bpc))
     tn = tensornetwork(bpc)
     ket(pv) = tn[(parent(pv), "ket")]
+    bra(pv) = tn[(parent(pv), "bra")]
     eu = Int32[vid[src(pe)] for pe in pes]
     ev = Int32[vid[dst(pe)] for pe in pes]
     links = [commonind(ket(src(pe)), ket(dst(pe))) for pe in pes]
+    blinks = [commonind(bra(src(pe)), bra(dst(pe))) for pe in pes]
     edim = Int32[length(l) for l in links]
     sdim = Int32[]
     leg_ptr = Int32[0]
     leg_edge = Int32[]
-    cplx = any(pv -> eltype(ket(pv)) <: Complex, pvs)
+    cplx = any(pv -> eltype(ket(pv)) <: Complex || eltype(bra(pv)) <: Complex, pvs)
     data = cplx ? ComplexF64[] : Float64[]
+    bdata = similar(data)
+    shared = true
     for pv in pvs
         t = ket(pv)
         s = only(filter(i -> !(i in links), inds(t)))
@@ -109,9 +122,18 @@ function pack(bpc::BeliefPropagationCache)
         append!(leg_edge, Int32[findfirst(==(l), links) - 1 for l in ls])
         push!(leg_ptr, length(leg_edge))
         push!(sdim, length(s))
-        append!(data, vec(array(t, s, ls...)))  # column-major, site index first
+        kv = vec(array(t, s, ls...))  # column-major, site index first
+        append!(data, kv)
+        tb = bra(pv)
+        sb = only(filter(i -> !(i in blinks), inds(tb)))
+        lbs = [blinks[findfirst(==(l), links)] for l in ls]  # the bra's links in the ket's leg order
+        bv = conj.(vec(array(tb, sb, lbs...)))
+        shared &= bv == kv
+        append!(bdata, bv)
     end
-    return (; pvs, pes, links, eu, ev, edim, sdim, leg_ptr, leg_edge, data, cplx)
+    # messages keep the tensors' element type (Float32, Float64, ComplexF32, ComplexF64)
+    elt = promote_type((eltype(ket(pv)) for pv in pvs)..., (eltype(bra(pv)) for pv in pvs)...)
+    return (; pvs, vid, pes, links, eu, ev, edim, sdim, leg_ptr, leg_edge, data, bdata, shared, cplx, elt)
 end
 
 function ITensorNetworks.update(alg::Algorithm"gb300_bp", bpc::BeliefPropagationCache)
@@ -119,23 +141,38 @@ function ITensorNetworks.update(alg::Algorithm"gb300_bp", bpc::BeliefPropagation
     ctx = context()
     GC.@preserve p begin
         desc = GraphDesc(length(p.pvs), length(p.pes), pointer(p.eu), pointer(p.ev), pointer(p.edim),
-            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0, p.cplx ? 1 : 0)
+            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, p.shared ? 0 : 1,
+            p.cplx ? 1 : 0)
         plan = Ref{Ptr{Cvoid}}(C_NULL)
         check(ctx, ccall((:gbtn_plan_create, libgbtn), Cint, (Ptr{Cvoid}, Ref{GraphDesc}, Ref{Ptr{Cvoid}}),
             ctx, desc, plan))
         try
             check(ctx, ccall((:gbtn_set_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint),
-                plan[], p.data, C_NULL, 0))
-            sched = get(alg.kwargs, :schedule, "parallel") == "colored" ? 2 : 1
-            single = all(pv -> real(eltype(ket(pv))) === Float32, p.pvs)
+                plan[], p.data, p.shared ? C_NULL : pointer(p.bdata), 0))
+            # the reference's defaults: sequential sweeps in the forest-cover order
+            # (default_bp_edge_sequence), maxiter 1 on trees and required otherwise
+            sched = Dict("sequential" => 0, "parallel" => 1, "colored" => 2)[get(alg.kwargs, :schedule,
+                "sequential")]
+            maxiter = get(alg.kwargs, :maxiter, ITensorNetworks.default_bp_maxiter(bpc))
+            isnothing(maxiter) && error("You need to specify a number of iterations for BP!")
+            seq = Int32[]
+            if sched == 0
+                de = Dict((p.eu[k], p.ev[k]) => Int32(2 * (k - 1)) for k in eachindex(p.pes))
+                for qe in get(alg.kwargs, :edge_sequence, ITensorNetworks.default_bp_edge_sequence(bpc))
+                    a, b = Int32(p.vid[src(qe)]), Int32(p.vid[dst(qe)])
+                    push!(seq, haskey(de, (a, b)) ? de[(a, b)] : de[(b, a)] + Int32(1))
+                end
+            end
+            single = real(p.elt) === Float32
             prec = Dict("f64" => 0, "f32" => 1, "bf16" => 2, "mixed" => 3)[get(alg.kwargs, :precision,
                 single ? "f32" : "f64")]
             tol = something(get(alg.kwargs, :tol, nothing), -1.0)
-            opts = BPOpts(sched, prec, alg.kwargs.maxiter, 1, tol, C_NULL, 0, 0.0, 0.0, 0, 0, 0)
+            opts = BPOpts(sched, prec, maxiter, 1, tol, isempty(seq) ? C_NULL : pointer(seq), length(seq),
+                0.0, 0.0, 0, 0, 0)
             iters = Ref{Int32}(0)
             diff = Ref{Float64}(0.0)
-            check(ctx, ccall((:gbtn_bp_run, libgbtn), Cint, (Ptr{Cvoid}, Ref{BPOpts}, Ref{Int32}, Ref{Float64}),
-                plan[], opts, iters, diff))
+            GC.@preserve seq check(ctx, ccall((:gbtn_bp_run, libgbtn), Cint,
+                (Ptr{Cvoid}, Ref{BPOpts}, Ref{Int32}, Ref{Float64}), plan[], opts, iters, diff))
             nmsg = sum(Int(c)^2 for c in p.edim) * 2
             flat = Vector{eltype(p.data)}(undef, nmsg)
             check(ctx, ccall((:gbtn_get_messages, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint),
@@ -144,7 +181,7 @@ function ITensorNetworks.update(alg::Algorithm"gb300_bp", bpc::BeliefPropagation
             # b the bra (primed) link and a the ket link
             off = 0
             new = Dict{QuotientEdge, Vector{ITensor}}()
-            elt = promote_type((eltype(ket(pv)) for pv in p.pvs)...)  # messages keep the tensors' eltype
+            elt = p.elt
             for (e, pe) in enumerate(p.pes), (dir, qe) in ((0, pe), (1, reverse(pe)))
                 c = Int(p.edim[e])
                 M = convert(Matrix{elt}, reshape(flat[(off + 1):(off + c * c)], c, c))
