@@ -1287,6 +1287,7 @@ void upload_with_images(gbtn_plan* P, const double* ket) {
 }
 
 int gbtn_set_factors(gbtn_plan* P, const double* ket, const double* bra, int mem) {
+  const gbtn::NvtxRange nvtx_range("gbtn_set_factors");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && ket, "NULL argument");
@@ -1311,6 +1312,7 @@ int gbtn_get_factors(gbtn_plan* P, double* ket, int mem) {
 }
 
 int gbtn_set_messages(gbtn_plan* P, const double* m, int mem) {
+  const gbtn::NvtxRange nvtx_range("gbtn_set_messages");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && m, "NULL argument");
@@ -1319,6 +1321,7 @@ int gbtn_set_messages(gbtn_plan* P, const double* m, int mem) {
 }
 
 int gbtn_get_messages(gbtn_plan* P, double* m, int mem) {
+  const gbtn::NvtxRange nvtx_range("gbtn_get_messages");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && m, "NULL argument");
@@ -1344,6 +1347,7 @@ int gbtn_init_messages(gbtn_plan* P, int kind) {
 }
 
 int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mean_diff) {
+  const gbtn::NvtxRange nvtx_range("gbtn_bp_run");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && o, "NULL argument");
@@ -1560,6 +1564,7 @@ int gbtn_vertex_rdms(gbtn_plan* P, double* out) {
 }
 
 int gbtn_expect1(gbtn_plan* P, const double* ops, int per_vertex, double* out) {
+  const gbtn::NvtxRange nvtx_range("gbtn_expect1");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && ops && out, "NULL argument");
@@ -1657,6 +1662,7 @@ static void edge_rdms_device(gbtn_plan* P, const int32_t* edges, int32_t n, DevB
 }
 
 int gbtn_edge_rdms(gbtn_plan* P, const int32_t* edges, int32_t n, double* out) {
+  const gbtn::NvtxRange nvtx_range("gbtn_edge_rdms");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && edges && out && n >= 0, "bad argument");
@@ -1740,6 +1746,7 @@ int gbtn_edge_scalars(gbtn_plan* P, double* out) {
 }
 
 int gbtn_logscalar(gbtn_plan* P, double* re, double* im) {
+  const gbtn::NvtxRange nvtx_range("gbtn_logscalar");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && re, "NULL argument");
@@ -1763,6 +1770,7 @@ int gbtn_logscalar(gbtn_plan* P, double* re, double* im) {
 }
 
 int gbtn_rescale_messages(gbtn_plan* P) {
+  const gbtn::NvtxRange nvtx_range("gbtn_rescale_messages");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P, "NULL plan");
@@ -1778,6 +1786,7 @@ int gbtn_rescale_messages(gbtn_plan* P) {
 }
 
 int gbtn_rescale_partitions(gbtn_plan* P) {
+  const gbtn::NvtxRange nvtx_range("gbtn_rescale_partitions");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P, "NULL plan");
@@ -1948,6 +1957,7 @@ int gbtn_energy2(gbtn_plan* P, int32_t nterms, const double* coef, const double*
 
 int gbtn_energy2_grad(gbtn_plan* P, int32_t nterms, const double* coef, const double* ops, const gbtn_grad_opts* o,
                       double* energy, double* grad, int32_t* iters, double* resid) {
+  const gbtn::NvtxRange nvtx_range("gbtn_energy2_grad");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && o && grad, "NULL argument");
@@ -2028,6 +2038,7 @@ int gbtn_energy2_grad(gbtn_plan* P, int32_t nterms, const double* coef, const do
 
 int gbtn_bp_vjp(gbtn_plan* P, const double* msg_cot, const gbtn_grad_opts* o, double* grad, int32_t* iters,
                 double* resid) {
+  const gbtn::NvtxRange nvtx_range("gbtn_bp_vjp");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   if (P && P->cplx) throw Unsupported("the BP vector-Jacobian product of complex networks is not implemented");

@@ -11,6 +11,21 @@
 
 #include "../../include/gbtn.h"
 
+#include <nvtx3/nvToolsExt.h>
+
+namespace gbtn {
+
+// NVTX range named after a C entry point, for profiler timelines (nsys, ncu
+// NVTX filters); a no-op unless a profiling tool is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
+}  // namespace gbtn
+
 namespace gbtn {
 
 // Limits of the compiled kernels.

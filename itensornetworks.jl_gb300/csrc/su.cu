@@ -1688,6 +1688,7 @@ int gbtn_su_get_factors(gbtn_su* S, double* ket, int64_t capacity) {
 int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
                   const double* envs, int32_t maxdim, double cutoff, int32_t normalize, double* truncerr,
                   double* svals) {
+  const gbtn::NvtxRange nvtx_range("gbtn_su_apply");
   if (!S || n_gates < 0 || (n_gates > 0 && (!edges || !gates))) return GBTN_ERR_INVALID;
   if (n_gates == 0) return GBTN_OK;
   try {
