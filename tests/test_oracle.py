@@ -201,3 +201,68 @@ def test_c_restatement_matches_oracle(schedule):
                                     schedule, seq if schedule == "sequential" else None, 15, tol=1e-300, nthreads=2)
     np.testing.assert_allclose(mc, O.flatten_messages(g, m), rtol=1e-12, atol=1e-14)
     assert itc == it
+
+
+def test_rescale_partitions_with_a_separate_bra_gives_unit_scalars():
+    # abstractbeliefpropagationcache.jl:349-379 with ket and bra vertices
+    # (the bra first in each partition): every partition scalar becomes 1 --
+    # complex tensors with an independent bra (any phase), and real tensors
+    # with positive scalars (a negative real scalar has no real square root:
+    # the reference raises a DomainError there, the oracle returns NaN)
+    for dtype, seed_b in ((np.complex128, 4), (np.float64, 3)):
+        g = O.square_lattice(3, 3, chi=2)
+        A = O.random_network(g, 3, dtype=dtype)
+        B = O.random_network(g, seed_b, dtype=dtype)
+        m, _, _ = O.bp_update(g, A, O.identity_messages(g), B=B, maxiter=30, schedule="parallel")
+        k, b = O.rescale_partitions(g, A, m, B)
+        for v in range(g.nv):
+            z = np.trace(O.contract_partition(g, {v: k[v]}, {v: b[v]}, m, v, open_site=True))
+            assert abs(z - 1.0) < 1e-12
+
+
+def test_exact_environment_equals_bp_messages_on_a_tree():
+    # environment(qf, [v]; alg="exact") against the BP environment on a tree
+    # (test_forms.jl:59-73): the product of the incoming messages, normalised
+    g = O.comb_tree(3, 3, chi=2)
+    A = O.random_network(g, 7)
+    m, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=1)
+    for v in range(g.nv):
+        k = len(g.legs[v])
+        ops = []
+        for p, e in enumerate(g.legs[v]):
+            de = 2 * e if g.edges[e][1] == v else 2 * e + 1
+            ops += [m[de], [p, k + p]]
+        env_bp = np.einsum(*ops, list(range(2 * k)))
+        env_ex = O.exact_environment(g, A, v)
+        np.testing.assert_allclose(env_bp / np.linalg.norm(env_bp), env_ex / np.linalg.norm(env_ex),
+                                   rtol=0, atol=1e-12)
+
+
+def test_trotter_tebd_lowers_the_ising_energy():
+    # tebd.jl:2-31 on the Ising model of test_tebd.jl (2 x 3, h = 0.1, all up,
+    # beta 2, dbeta 0.2, maxdim 2): the energy goes down, towards the exact
+    # ground energy, and the Trotter list is a palindrome of half steps
+    g = O.square_lattice(2, 3, chi=1)
+    terms = O.ising_terms(g, h=0.1)
+    groups = O.group_terms(terms, g)
+    seq = O.trotter2_gates(g, groups, 0.2)
+    assert [e for e, _ in seq] == [e for e, _ in groups] + [e for e, _ in groups][::-1]
+    up = np.array([1.0, 0.0])
+    A = [up.reshape((2,) + (1,) * len(g.legs[v])) for v in range(g.nv)]
+
+    def energy(gg, T):
+        ops = []
+        for v in range(gg.nv):
+            ops += [T[v], [v] + [20 + e for e in gg.legs[v]]]
+        psi = np.einsum(*ops, list(range(gg.nv)), optimize=True)
+        psi = psi / np.linalg.norm(psi)
+        E = 0.0
+        for c, tops in terms:
+            phi = psi
+            for name, x in reversed(tops):
+                phi = np.moveaxis(np.tensordot(O.SPIN_HALF[name], phi, axes=([1], [x])), 0, x)
+            E += c * float(np.real(np.vdot(psi, phi)))
+        return E
+    g2, B = O.tebd(g, A, groups, beta=2.0, dbeta=0.2, maxdim=2, cutoff=1e-8)
+    assert max(g2.edge_dims) <= 2
+    assert energy(g2, B) < energy(g, A) - 1e-3
