@@ -244,7 +244,9 @@ int gbtn_rescale_messages(gbtn_plan* plan);
  * scalar z and s = sign(z) for a real z (else 1) the ket is scaled by s*r and
  * the bra by s*s*r, as in the reference (whose partitions list the bra first).
  * With bra = conj(ket) only the ket is scaled (a real network with a negative
- * z gets NaN tensors); for complex tensors the remaining phases z/|z| are then
+ * z gets NaN tensors; with a separate real bra, where the reference raises a
+ * DomainError, the sign goes on the bra and the scalar still becomes 1); for
+ * complex tensors the remaining phases z/|z| are then
  * moved onto the messages, which carry a free phase (m_{u->v} by e^{i psi},
  * m_{v->u} by e^{-i psi} on the edges of a spanning forest, which keeps every
  * edge scalar), so vertex scalars become 1 as in the reference. */
