@@ -4,8 +4,9 @@ Python mirror of ITensorNetworks.jl's BP interface over the C ABI of
 libgbtn.so (include/gbtn.h).  Every numerical step runs on the GPU."""
 from . import _lib
 from ._lib import Context, GBTNError, InvalidArgument, LibraryNotBuilt, Unsupported, default_context
-from .cache import (BeliefPropagationCache, environment, expect, initialize_cache, inner, loginner, logscalar,
-                    message_diff, norm, norm_sqr, normalize, rescale, scalar, update, updated_message)
+from .cache import (BeliefPropagationCache, edge_scalars, environment, expect, identity_messages, initialize_cache,
+                    inner, loginner, logscalar, message, message_diff, messages, norm, norm_sqr, normalize, rescale,
+                    scalar, update, update_factor, update_factors, updated_message, vertex_scalars)
 from .partition import CoarseGraining, PartitionedBPCache, partitioned_cache
 from .sharded import GpuShard, ShardPlan, block_owner, run_distributed, run_local
 from .su import SimpleUpdateState, apply, bp_environments, checkerboard_edges, tebd, tebd_gates, tfim_gate
@@ -20,5 +21,6 @@ __all__ = [
     "parallel_edge_sequence", "random_network", "random_tensors", "rescale", "scalar", "square_lattice", "update",
     "updated_message", "SimpleUpdateState", "apply", "checkerboard_edges", "tebd", "tfim_gate", "bp_environments",
     "CoarseGraining", "PartitionedBPCache", "partitioned_cache", "GpuShard", "ShardPlan", "block_owner",
-    "run_distributed", "run_local", "tebd_gates", "OpSum", "group_terms", "trotter2_gates",
+    "run_distributed", "run_local", "tebd_gates", "OpSum", "group_terms", "trotter2_gates", "edge_scalars",
+    "identity_messages", "message", "messages", "update_factor", "update_factors", "vertex_scalars",
 ]

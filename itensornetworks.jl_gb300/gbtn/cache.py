@@ -72,9 +72,36 @@ class BeliefPropagationCache:
         if self.separate_bra:
             b = self.tn.flat([np.asarray(t, dtype=self.dtype) for t in bra])
             self._c(self.lib.gbtn_set_factors(self.handle, k.ctypes.data, b.ctypes.data, _lib.HOST))
+            self.bra_tensors = [np.asarray(t, dtype=self.dtype) for t in bra]
         else:
             self._c(self.lib.gbtn_set_factors(self.handle, k.ctypes.data, None, _lib.HOST))
         self.tn.tensors = [np.asarray(t, dtype=self.dtype) for t in ket]
+
+    def update_factors(self, factors, bra_factors=None):
+        """update_factors(bpc, factors) (abstractbeliefpropagationcache.jl:158-165):
+        ``factors`` maps vertices to new site tensors of the same shape (and,
+        for a cache with a separate bra, ``bra_factors`` the bra's); the
+        messages are kept.  One upload of all tensors.  Unlike the reference,
+        which returns a copy, the cache is updated in place and returned."""
+        def merged(current, new):
+            out = list(current)
+            for v, t in dict(new or {}).items():
+                t = np.asarray(t)
+                if not 0 <= int(v) < self.tn.nv:
+                    raise _lib.InvalidArgument(1, f"vertex {v} is not in the network")
+                if tuple(t.shape) != tuple(self.tn.shape(int(v))):
+                    raise _lib.InvalidArgument(
+                        1, f"factor of vertex {v} has shape {tuple(t.shape)}, expected {tuple(self.tn.shape(int(v)))}")
+                out[int(v)] = t
+            return out
+        ket = merged(self.tn.tensors, factors)
+        bra = merged(self.bra_tensors, bra_factors) if self.separate_bra else None
+        self.set_factors(ket, bra)
+        return self
+
+    def update_factor(self, vertex, factor, bra_factor=None):
+        """update_factor(bpc, vertex, factor) (:167-171) for one vertex."""
+        return self.update_factors({vertex: factor}, None if bra_factor is None else {vertex: bra_factor})
 
     def factors(self):
         out = np.empty(self.n_factor, dtype=self.dtype)
@@ -376,6 +403,40 @@ def expect(psi, op, vertices=None, alg="bp", cache=None, update_cache=None, cach
 
 def environment(bpc, verts):
     return bpc.environment(verts)
+
+
+# Functions of a cache under the reference's names (the reference calls them
+# with the cache as first argument; abstractbeliefpropagationcache.jl:83-97,
+# 158-175, beliefpropagationcache.jl:107-119).
+def messages(bpc):
+    return bpc.messages()
+
+
+def message(bpc, directed_edge):
+    return bpc.message(directed_edge)
+
+
+def vertex_scalars(bpc):
+    return bpc.vertex_scalars()
+
+
+def edge_scalars(bpc):
+    return bpc.edge_scalars()
+
+
+def update_factor(bpc, vertex, factor):
+    return bpc.update_factor(vertex, factor)
+
+
+def update_factors(bpc, factors):
+    return bpc.update_factors(factors)
+
+
+def identity_messages(tn):
+    """The initial messages of a quadratic form (quadraticformnetwork.jl:96-124):
+    the chi x chi identity delta(dag(k'), k) on every directed edge, in
+    directed-edge order."""
+    return [np.eye(tn.edge_dims[de // 2]) for de in range(2 * tn.ne)]
 
 
 def logscalar(tn, alg="bp", cache=None, update_cache=None, cache_update_kwargs=None, bra=None):

@@ -56,10 +56,12 @@ def test_belief_propagation_as_the_reference(elt):
     new = rng.standard_normal(tn.shape(0))
     if np.iscomplexobj(np.zeros(1, elt)):
         new = new + 1j * rng.standard_normal(tn.shape(0))
-    ts = list(tn.tensors)
-    ts[0] = new.astype(elt)
-    bpc.set_factors(ts)
-    np.testing.assert_array_equal(bpc.factors()[0], ts[0].astype(bpc.dtype))
+    before = bpc.factors()
+    gbtn.update_factor(bpc, 0, new.astype(elt))
+    after = bpc.factors()
+    np.testing.assert_array_equal(after[0], new.astype(elt).astype(bpc.dtype))
+    for v in range(1, tn.nv):
+        np.testing.assert_array_equal(after[v], before[v])
     bpc.update(maxiter=25, tol=eps, precision=precision(elt))
     msgs = bpc.messages()
     for de in range(2 * tn.ne):

@@ -102,3 +102,38 @@ def test_missing_maxiter_on_loopy_graph_raises_before_gpu():
     bpc = Fake(gbtn.random_network(square_lattice(3, 3), 1))
     with pytest.raises(gbtn.InvalidArgument, match="number of iterations"):
         bpc.update()
+
+
+def test_update_factors_and_reference_named_functions():
+    # update_factor / update_factors (abstractbeliefpropagationcache.jl:158-171)
+    # through a cache double whose upload is recorded instead of run
+    class Recording(gbtn.BeliefPropagationCache):
+        def __init__(self, tn, bra=None):
+            self.tn = tn
+            self.separate_bra = bra is not None
+            self.dtype = np.float64
+            self.bra_tensors = bra
+            self.uploads = []
+
+        def set_factors(self, ket, bra=None):
+            self.uploads.append((ket, bra))
+            self.tn.tensors = ket
+
+    tn = gbtn.random_network(square_lattice(3, 2), 4)
+    old = list(tn.tensors)
+    bpc = Recording(tn)
+    new = np.ones(tn.shape(2))
+    assert gbtn.update_factor(bpc, 2, new) is bpc
+    ket, bra = bpc.uploads[-1]
+    assert bra is None and ket[2] is new and all(ket[v] is old[v] for v in range(tn.nv) if v != 2)
+    with pytest.raises(gbtn.InvalidArgument):
+        bpc.update_factor(1, np.ones((3, 3)))
+    with pytest.raises(gbtn.InvalidArgument):
+        bpc.update_factors({tn.nv: new})
+    sep = Recording(gbtn.random_network(square_lattice(3, 2), 5), bra=list(old))
+    sep.update_factor(0, np.zeros(tn.shape(0)), bra_factor=np.ones(tn.shape(0)))
+    ket, bra = sep.uploads[-1]
+    assert np.all(ket[0] == 0) and np.all(bra[0] == 1) and bra[1] is old[1]
+    ids = gbtn.identity_messages(tn)
+    ref = O.identity_messages(O.square_lattice(3, 2))
+    assert len(ids) == 2 * tn.ne and all(np.array_equal(a, b) for a, b in zip(ids, ref))
