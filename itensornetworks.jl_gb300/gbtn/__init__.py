@@ -5,8 +5,9 @@ libgbtn.so (include/gbtn.h).  Every numerical step runs on the GPU."""
 from . import _lib
 from ._lib import Context, GBTNError, InvalidArgument, LibraryNotBuilt, Unsupported, default_context
 from .cache import (BeliefPropagationCache, edge_scalars, environment, expect, identity_messages, initialize_cache,
-                    inner, loginner, logscalar, message, message_diff, messages, norm, norm_sqr, normalize, rescale,
-                    scalar, update, update_factor, update_factors, updated_message, vertex_scalars)
+                    inner, loginner, logscalar, message, message_diff, messages, norm, norm_sqr, normalize,
+                    region_scalar, rescale, scalar, scalar_factors_quotient, update, update_factor, update_factors,
+                    updated_message, vertex_scalars)
 from .partition import CoarseGraining, PartitionedBPCache, partitioned_cache
 from .sharded import GpuShard, ShardPlan, block_owner, run_distributed, run_local
 from .su import SimpleUpdateState, apply, bp_environments, checkerboard_edges, tebd, tebd_gates, tfim_gate
@@ -23,4 +24,5 @@ __all__ = [
     "CoarseGraining", "PartitionedBPCache", "partitioned_cache", "GpuShard", "ShardPlan", "block_owner",
     "run_distributed", "run_local", "tebd_gates", "OpSum", "group_terms", "trotter2_gates", "edge_scalars",
     "identity_messages", "message", "messages", "update_factor", "update_factors", "vertex_scalars",
+    "region_scalar", "scalar_factors_quotient",
 ]

@@ -428,6 +428,21 @@ def update_factor(bpc, vertex, factor):
     return bpc.update_factor(vertex, factor)
 
 
+def region_scalar(bpc, vertex=None, edge=None):
+    """region_scalar(bpc, pv) / region_scalar(bpc, pe) (beliefpropagationcache.jl:107-119):
+    the partition scalar of a vertex (its tensors with all incoming messages)
+    or the scalar <m_e, m_ebar> of an edge; give exactly one of the two."""
+    if (vertex is None) == (edge is None):
+        raise ValueError("give a vertex or an edge")
+    return bpc.vertex_scalars()[vertex] if edge is None else bpc.edge_scalars()[edge]
+
+
+def scalar_factors_quotient(bpc):
+    """(vertex scalars, edge scalars), the factors of the BP estimate
+    prod_v Z_v / prod_e <m_e, m_ebar> (abstractbeliefpropagationcache.jl:95-97)."""
+    return bpc.vertex_scalars(), bpc.edge_scalars()
+
+
 def update_factors(bpc, factors):
     return bpc.update_factors(factors)
 

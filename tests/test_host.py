@@ -137,3 +137,22 @@ def test_update_factors_and_reference_named_functions():
     ids = gbtn.identity_messages(tn)
     ref = O.identity_messages(O.square_lattice(3, 2))
     assert len(ids) == 2 * tn.ne and all(np.array_equal(a, b) for a, b in zip(ids, ref))
+
+
+def test_region_scalars_read_the_vertex_and_edge_scalars():
+    class Scalars(gbtn.BeliefPropagationCache):
+        def __init__(self):
+            pass
+
+        def vertex_scalars(self):
+            return np.array([2.0, 3.0, 5.0])
+
+        def edge_scalars(self):
+            return np.array([7.0, 11.0])
+
+    bpc = Scalars()
+    assert gbtn.region_scalar(bpc, vertex=1) == 3.0 and gbtn.region_scalar(bpc, edge=1) == 11.0
+    with pytest.raises(ValueError):
+        gbtn.region_scalar(bpc)
+    vs, es = gbtn.scalar_factors_quotient(bpc)
+    assert list(vs) == [2.0, 3.0, 5.0] and list(es) == [7.0, 11.0]
