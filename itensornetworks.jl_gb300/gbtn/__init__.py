@@ -4,7 +4,8 @@ Python mirror of ITensorNetworks.jl's BP interface over the C ABI of
 libgbtn.so (include/gbtn.h).  Every numerical step runs on the GPU."""
 from . import _lib
 from ._lib import Context, GBTNError, InvalidArgument, LibraryNotBuilt, Unsupported, default_context
-from .cache import (BeliefPropagationCache, edge_scalars, environment, expect, identity_messages, initialize_cache,
+from .cache import (BeliefPropagationCache, default_bp_maxiter, edge_scalars, environment, expect, factors,
+                    identity_messages, incoming_messages, initialize_cache,
                     inner, loginner, logscalar, message, message_diff, messages, norm, norm_sqr, normalize,
                     region_scalar, rescale, scalar, scalar_factors_quotient, update, update_factor, update_factors,
                     updated_message, vertex_scalars)
@@ -24,5 +25,5 @@ __all__ = [
     "CoarseGraining", "PartitionedBPCache", "partitioned_cache", "GpuShard", "ShardPlan", "block_owner",
     "run_distributed", "run_local", "tebd_gates", "OpSum", "group_terms", "trotter2_gates", "edge_scalars",
     "identity_messages", "message", "messages", "update_factor", "update_factors", "vertex_scalars",
-    "region_scalar", "scalar_factors_quotient",
+    "region_scalar", "scalar_factors_quotient", "incoming_messages", "factors", "default_bp_maxiter",
 ]

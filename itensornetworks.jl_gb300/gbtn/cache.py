@@ -428,6 +428,29 @@ def update_factor(bpc, vertex, factor):
     return bpc.update_factor(vertex, factor)
 
 
+def incoming_messages(bpc, verts, ignore_edges=()):
+    """incoming_messages(bpc, partition_vertices; ignore_edges)
+    (abstractbeliefpropagationcache.jl:99-107): the messages on directed edges
+    entering ``verts`` from outside, except the directed edges listed in
+    ``ignore_edges``, as (directed edge, message) pairs."""
+    skip = set(int(d) for d in ignore_edges)
+    incoming, _ = bpc.environment(list(verts))
+    return [(de, m) for de, m in incoming if de not in skip]
+
+
+def factors(bpc, verts=None):
+    """factors(bpc, verts) (abstractbeliefpropagationcache.jl:75-81): the site
+    tensors of ``verts`` (all vertices when None), read back from the device."""
+    ts = bpc.factors()
+    return ts if verts is None else [ts[int(v)] for v in verts]
+
+
+def default_bp_maxiter(bpc):
+    """1 on a tree, None (maxiter required) on a loopy graph
+    (abstractbeliefpropagationcache.jl:38-41)."""
+    return bpc.default_maxiter()
+
+
 def region_scalar(bpc, vertex=None, edge=None):
     """region_scalar(bpc, pv) / region_scalar(bpc, pe) (beliefpropagationcache.jl:107-119):
     the partition scalar of a vertex (its tensors with all incoming messages)

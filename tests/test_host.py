@@ -156,3 +156,29 @@ def test_region_scalars_read_the_vertex_and_edge_scalars():
         gbtn.region_scalar(bpc)
     vs, es = gbtn.scalar_factors_quotient(bpc)
     assert list(vs) == [2.0, 3.0, 5.0] and list(es) == [7.0, 11.0]
+
+
+def test_incoming_messages_factors_and_default_maxiter():
+    tn = gbtn.random_network(square_lattice(3, 2), 6)
+
+    class Msgs(gbtn.BeliefPropagationCache):
+        def __init__(self, tn):
+            self.tn = tn
+
+        def messages(self):
+            return [np.full((c, c), float(de)) for de, c in
+                    ((de, self.tn.edge_dims[de // 2]) for de in range(2 * self.tn.ne))]
+
+        def factors(self):
+            return list(self.tn.tensors)
+
+    bpc = Msgs(tn)
+    v = 4
+    inc = gbtn.incoming_messages(bpc, [v])
+    want = sorted(tn.directed(e, tn.other(v, e)) for e in tn.legs[v])
+    assert sorted(de for de, _ in inc) == want
+    assert all(np.all(m == de) for de, m in inc)
+    assert sorted(de for de, _ in gbtn.incoming_messages(bpc, [v], ignore_edges=[want[0]])) == want[1:]
+    assert all(a is b for a, b in zip(gbtn.factors(bpc, [1, 3]), [tn.tensors[1], tn.tensors[3]]))
+    assert gbtn.default_bp_maxiter(bpc) is None  # a loopy grid: maxiter is required
+    assert gbtn.default_bp_maxiter(Msgs(gbtn.random_network(square_lattice(4, 1), 1))) == 1
