@@ -272,6 +272,12 @@ class BeliefPropagationCache:
         return f(ls) if not isinstance(ls, list) else [f(x) for x in ls]
 
     def expect(self, op, per_vertex=False):
+        """<O_v> per vertex: ``op`` is a d x d matrix O[s', s], a list of them
+        (per_vertex), or the name of a real S=1/2 operator ("Sz", "Sx", "S+",
+        "S-", "Id") as in the reference's expect(psi, "Sz")."""
+        if isinstance(op, str):
+            from .opsum import named_operator
+            op, per_vertex = named_operator(op, self.tn), False
         out = np.empty(self.tn.nv)
         if per_vertex:
             ops = np.ascontiguousarray(np.concatenate([np.asarray(o, float).reshape(-1, order="F") for o in op]))
@@ -393,7 +399,8 @@ def _cache_for(tn, cache, update_cache, cache_update_kwargs, bra=None):
 
 def expect(psi, op, vertices=None, alg="bp", cache=None, update_cache=None, cache_update_kwargs=None):
     """<psi|O_v|psi>/<psi|psi> on every vertex (expect.jl:58-109); ``op`` is a
-    d x d matrix O[s', s].  Returns a numpy array (or the subset ``vertices``)."""
+    d x d matrix O[s', s] or the name of a real S=1/2 operator ("Sz").  Returns
+    a numpy array (or the subset ``vertices``)."""
     if alg != "bp":
         raise ValueError("only alg='bp' runs on the GPU")
     cache = _cache_for(psi, cache, update_cache, cache_update_kwargs)

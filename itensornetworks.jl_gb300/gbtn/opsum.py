@@ -33,6 +33,22 @@ SPIN_HALF_OPS = {
 }
 
 
+def named_operator(name, tn: TensorNetwork):
+    """The matrix O[s', s] of a named S=1/2 operator for expect(psi, "Sz")
+    (expect.jl:21-41): every site of ``tn`` must have dimension 2, and the
+    operator must be real (the library reports the real part of <O> for a real
+    O; "Sy" is imaginary)."""
+    if name not in SPIN_HALF_OPS:
+        raise ValueError(f"unknown operator {name!r} (S=1/2 sites: {sorted(SPIN_HALF_OPS)})")
+    if any(d != 2 for d in tn.site_dims):
+        raise ValueError(f"operator {name!r} acts on spin-1/2 sites; this network has site dimensions "
+                         f"{sorted(set(tn.site_dims))}")
+    op = SPIN_HALF_OPS[name]
+    if np.iscomplexobj(op):
+        raise ValueError(f"operator {name!r} is complex: pass its matrix to a complex-aware contraction instead")
+    return np.asarray(op, dtype=float)
+
+
 class OpSum:
     """A sum of products of named one-site operators.  Each term is stored as
     (coefficient, ((name, vertex), ...)); ``groups`` (set by group_terms) is a

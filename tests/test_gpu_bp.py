@@ -39,6 +39,7 @@ def test_c1_sequential_f64_golden():
     np.testing.assert_allclose(tn.flat_messages(bpc.messages()), GOLD["c1__msgs"], rtol=0, atol=1e-12)
     sz = bpc.expect(O.SZ)
     np.testing.assert_allclose(sz, GOLD["c1__sz"], rtol=1e-10, atol=1e-14)
+    np.testing.assert_array_equal(bpc.expect("Sz"), sz)  # expect(psi, "Sz") by name, as the reference
     assert bpc.logscalar() == pytest.approx(float(GOLD["c1__logscalar"]), rel=1e-12)
     assert list(bpc.iterations) == [20]
 

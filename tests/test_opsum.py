@@ -47,3 +47,17 @@ def test_terms_parse_like_opsum_tuples():
     far = gbtn.OpSum([(1.0, "Sz", 0, "Sz", 3)])  # a diagonal pair: no edge holds both sites
     with pytest.raises(ValueError):
         gbtn.group_terms(far, tn)
+
+
+def test_named_operators_for_expect():
+    tn = gbtn.square_lattice(2, 2, chi=1)
+    from gbtn.opsum import named_operator
+    np.testing.assert_array_equal(named_operator("Sz", tn), np.diag([0.5, -0.5]))
+    np.testing.assert_array_equal(named_operator("S+", tn), [[0.0, 1.0], [0.0, 0.0]])  # S+|dn> = |up>: O[up, dn]
+    with pytest.raises(ValueError):
+        named_operator("Sy", tn)  # imaginary: the library reports real parts of real operators
+    with pytest.raises(ValueError):
+        named_operator("Sq", tn)
+    t3 = gbtn.TensorNetwork(tn.nv, tn.edges, [3, 2, 2, 2], tn.edge_dims)
+    with pytest.raises(ValueError):
+        named_operator("Sz", t3)
