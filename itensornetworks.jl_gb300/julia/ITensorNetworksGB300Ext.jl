@@ -32,7 +32,8 @@ module ITensorNetworksGB300Ext
 
 using ITensorNetworks: ITensorNetworks, AbstractBeliefPropagationCache, BeliefPropagationCache,
     messages, set_messages, partitioned_tensornetwork, quotientedges, tensornetwork
-using ITensors: ITensors, ITensor, Index, inds, commonind, array, itensor, dag, prime, tags
+using ITensors: ITensors, ITensor, Index, inds, commonind, hascommoninds, array, itensor, dag, prime, tags
+using LinearAlgebra: norm
 using NDTensors: Algorithm, @Algorithm_str
 using Graphs: src, dst
 using NamedGraphs.PartitionedGraphs: QuotientEdge, quotientvertices
@@ -238,7 +239,8 @@ end
     apply(Algorithm("gb300"), gates, psi; maxdim, cutoff=nothing, normalize=true, envs=nothing, callback)
 
 Two-site `gates` (ITensors acting on the site indices of neighbouring vertices)
-applied in order by the GPU simple update; `callback(; singular_values,
+applied in order by the GPU simple update, one-site gates contracted into their
+site tensor on the host (src/apply.jl:107-116); `callback(; singular_values,
 truncation_error)` is called per gate as in src/apply.jl:97-146.  `envs`:
 `nothing` (tebd) or a Dict from QuotientEdge to the converged message.
 Complex gates (e.g. `op("RandomUnitary", ...)`), states or environments run
@@ -246,6 +248,28 @@ the library's complex path (complex_values = 1).
 """
 function ITensorNetworks.apply(::Algorithm"gb300", gates::Vector{ITensor}, psi; maxdim, cutoff=nothing,
                                normalize=true, envs=nothing, callback=(; kws...) -> nothing)
+    # one-site gates act on their site tensor on the host, as the reference's
+    # apply does (src/apply.jl:107-116); the runs of two-site gates between
+    # them go to the GPU in order
+    if any(g -> length(inds(g)) == 2, gates)
+        run = ITensor[]
+        flush!(psi) = isempty(run) ? psi :
+            ITensorNetworks.apply(Algorithm("gb300"), copy(run), psi; maxdim, cutoff, normalize, envs, callback)
+        for g in gates
+            if length(inds(g)) == 2
+                psi = flush!(psi)
+                empty!(run)
+                v = only(filter(w -> hascommoninds(g, psi[w]), collect(ITensorNetworks.vertices(psi))))
+                t = ITensors.apply(g, psi[v])
+                normalize && (t ./= norm(t))
+                psi = copy(psi)
+                psi[v] = t
+            else
+                push!(run, g)
+            end
+        end
+        return flush!(psi)
+    end
     cplx = any(g -> eltype(g) <: Complex, gates) ||
            any(v -> eltype(psi[v]) <: Complex, ITensorNetworks.vertices(psi)) ||
            (envs !== nothing && any(m -> eltype(only(m)) <: Complex, values(envs)))
@@ -325,16 +349,16 @@ src/tebd.jl:2-31 with the gate list applied by the GPU simple update: the
 gates are the caller's ITensors `exp(-Δβ * ℋ; alg=Trotter{2}())`, so they are
 the reference's; each of the `Int(β ÷ Δβ)` steps is one
 `apply(Algorithm("gb300"), gates, ψ; maxdim, cutoff, normalize=true)`.  The
-terms of ℋ must be grouped per edge (two-site gates), as the reference's test
-does with `group_terms`; `ortho=true` (tree_orthogonalize) is not provided.
+gates act on the two sites of an edge (on the GPU) or on one site (on the host,
+as the reference's apply); `ortho=true` (tree_orthogonalize) is not provided.
 """
 function ITensorNetworks.tebd(::Algorithm"gb300", ℋ, ψ; β, Δβ, maxdim, cutoff, print_frequency=10,
                               ortho=false)
     ortho && error("tebd(Algorithm(\"gb300\"), ...; ortho=true): tree_orthogonalize is not provided by libgbtn")
     𝒰 = exp(-Δβ * ℋ; alg=ITensors.Trotter{2}())
     u⃗ = Vector{ITensor}(𝒰, ITensorNetworks.siteinds(ψ))
-    all(g -> length(inds(g)) == 4, u⃗) ||
-        error("tebd(Algorithm(\"gb300\")): every gate must act on the two sites of an edge (group the terms per edge)")
+    all(g -> length(inds(g)) in (2, 4), u⃗) ||
+        error("tebd(Algorithm(\"gb300\")): gates act on one site or on the two sites of an edge")
     for step in 1:Int(β ÷ Δβ)
         step % print_frequency == 0 && @show step, (step - 1) * Δβ, β
         ψ = ITensorNetworks.apply(Algorithm("gb300"), u⃗, ψ; maxdim, cutoff, normalize=true)
