@@ -61,3 +61,31 @@ def test_named_operators_for_expect():
     t3 = gbtn.TensorNetwork(tn.nv, tn.edges, [3, 2, 2, 2], tn.edge_dims)
     with pytest.raises(ValueError):
         named_operator("Sz", t3)
+
+
+def test_complex_terms_give_the_oracle_gates():
+    # Sy is imaginary: an XY model with a field makes complex Hermitian edge
+    # terms, and its Trotter gates exp(-dbeta/2 h) are complex
+    tn = gbtn.square_lattice(3, 2, chi=1)
+    g = O.square_lattice(3, 2, chi=1)
+    H = gbtn.OpSum()
+    terms = []
+    for (u, v) in tn.edges:
+        for name in ("Sx", "Sy"):
+            H += (0.7, name, u, name, v)
+            terms.append((0.7, [(name, u), (name, v)]))
+    for v in range(tn.nv):
+        H += (0.3, "Sz", v)
+        terms.append((0.3, [("Sz", v)]))
+    a = gbtn.trotter2_gates(gbtn.group_terms(H, tn), tn, 0.1)
+    b = O.trotter2_gates(g, O.group_terms(terms, g), 0.1)
+    assert [e for e, _ in a] == [e for e, _ in b]
+    for (_, x), (_, y) in zip(a, b):
+        np.testing.assert_allclose(x, y, rtol=0, atol=1e-14)
+    # Sx Sx + Sy Sy is real (the imaginary parts cancel), so these gates are real
+    assert not any(np.iscomplexobj(x) and np.any(np.imag(x)) for _, x in a)
+    # S+ S- is real but not Hermitian, Sy Sz is imaginary: the gate (a general
+    # matrix exponential, no Hermitian assumption) is complex
+    Hc = gbtn.OpSum([(1.0, "S+", 0, "S-", 1), (1.0, "Sy", 0, "Sz", 1)])
+    h = gbtn.trotter2_gates(gbtn.group_terms(Hc, tn), tn, 0.2)[0][1]
+    assert np.iscomplexobj(h) and np.any(np.imag(h))
