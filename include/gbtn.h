@@ -320,14 +320,21 @@ int gbtn_bp_vjp(gbtn_plan* plan, const double* msg_cot, const gbtn_grad_opts* op
  * including the arrays inside *dev_graph (the struct itself stays on the
  * host), is DEVICE memory owned by the caller; the library allocates
  * nothing and keeps its scratch in a fixed ~1.2 MiB device array.  The first
- * call on a device sets that array up (make it before any stream capture);
- * calls that overlap on the GPU share the array and race.  Asynchronous on
- * `stream` (NULL = the legacy default stream).
+ * call on a device sets that array up (make it before any stream capture; a
+ * set-up that fails returns GBTN_ERR_CUDA and is tried again by the next
+ * call); calls that overlap on the GPU share the array and race.
+ * Asynchronous on `stream` (NULL = the legacy default stream).
  * Returns GBTN_ERR_UNSUPPORTED when nv > GBTN_STATIC_MAX_VERTICES,
- * 2*ne > GBTN_STATIC_MAX_DIRECTED_EDGES or complex_values is set (real
- * tensors only); a vertex beyond the kernel limits
- * (degree > 8, chi > 8, d > 8, d*prod(chi) > 8192) is skipped on the device and
- * makes *mean_diff NaN. */
+ * 2*ne > GBTN_STATIC_MAX_DIRECTED_EDGES, complex_values is set (real
+ * tensors only) or separate_bra is set (the bra is always the ket here).
+ * The descriptor is checked on the device, since the call does not wait for
+ * the GPU: a vertex beyond the kernel limits (degree > 8, chi > 8, d > 8,
+ * d*prod(chi) > 8192) or one that fails a structural check (leg_ptr
+ * decreasing or not starting at 0, a leg edge outside 0..ne-1 or not incident
+ * to the vertex, a dimension < 1) is skipped without reading out of bounds:
+ * its outgoing entries of msg_out are left unwritten (they keep whatever the
+ * buffer held) and *mean_diff becomes NaN, while every other vertex's
+ * messages are computed as usual.  The call itself still returns GBTN_OK. */
 #define GBTN_STATIC_MAX_VERTICES 16384
 #define GBTN_STATIC_MAX_DIRECTED_EDGES 65536
 int gbtn_bp_sweep_static(int device, const gbtn_graph_desc* dev_graph, const double* factors,

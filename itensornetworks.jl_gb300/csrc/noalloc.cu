@@ -92,19 +92,49 @@ __device__ void block_scan(int n, long long* out, F size_of) {
   __syncthreads();
 }
 
-// Offsets of every vertex tensor and every message; status 0.
+// Structural checks of one vertex of a caller's device descriptor, made on the
+// device before any array is indexed with a value read from the descriptor:
+// leg_ptr non-decreasing with at most kMaxDeg legs, every leg edge in
+// 0..ne-1 with v as one of its endpoints, bond and site dimensions >= 1.
+// leg_edge is read only inside [leg_ptr[v], leg_ptr[v+1]), which the caller
+// sizes (its length is leg_ptr[nv]).
+__device__ __forceinline__ bool vertex_valid(const gbtn_graph_desc& g, int v) {
+  const int b = g.leg_ptr[v], e_ = g.leg_ptr[v + 1];
+  if (b < 0 || e_ < b || e_ - b > gbtn::kMaxDeg || g.site_dim[v] < 1) return false;
+  for (int q = b; q < e_; ++q) {
+    const int e = g.leg_edge[q];
+    if (e < 0 || e >= g.ne) return false;
+    if (g.edge_dim[e] < 1) return false;
+    if (g.edge_u[e] != v && g.edge_v[e] != v) return false;
+  }
+  return true;
+}
+
+// Offsets of every vertex tensor and every message; status 0, or 1 when the
+// descriptor fails a structural check (the offending sizes count as 0).
 __global__ void __launch_bounds__(kThreads) static_prep_kernel(gbtn_graph_desc g, unsigned char* base) {
   Scratch S = view(base);
-  if (threadIdx.x == 0) *S.status = 0;
+  __shared__ int s_bad;
+  if (threadIdx.x == 0) s_bad = g.leg_ptr[0] != 0;
+  __syncthreads();
   block_scan(g.nv, S.voff, [&](int v) -> long long {
+    if (!vertex_valid(g, v)) {
+      s_bad = 1;
+      return 0;
+    }
     long long n = g.site_dim[v];
     for (int q = g.leg_ptr[v]; q < g.leg_ptr[v + 1]; ++q) n *= g.edge_dim[g.leg_edge[q]];
     return n;
   });
   block_scan(2 * g.ne, S.moff, [&](int de) -> long long {
     const long long c = g.edge_dim[de >> 1];
+    if (c < 1) {
+      s_bad = 1;
+      return 0;
+    }
     return c * c;
   });
+  if (threadIdx.x == 0) *S.status = s_bad;
 }
 
 __device__ __forceinline__ void absorb_leg(const double* in, double* out, int n, int st, int chi, const double* M) {
@@ -161,21 +191,23 @@ __global__ void __launch_bounds__(kThreads)
   Scratch S = view(base);
   const int v = blockIdx.x;
   if (threadIdx.x == 0) {
-    const int k = g.leg_ptr[v + 1] - g.leg_ptr[v];
+    int ok = vertex_valid(g, v);
+    const int k = ok ? g.leg_ptr[v + 1] - g.leg_ptr[v] : 0;
     const int d = g.site_dim[v];
     const long long n = S.voff[v + 1] - S.voff[v];
-    int ok = k <= gbtn::kMaxDeg && d >= 1 && d <= gbtn::kMaxSite && n <= kStaticMaxN;
+    ok = ok && d <= gbtn::kMaxSite && n <= kStaticMaxN;
     long long st = d;
     for (int p = 0; ok && p < k; ++p) {
       const int e = g.leg_edge[g.leg_ptr[v] + p];
       const int c = g.edge_dim[e];
-      ok = ok && c >= 1 && c <= gbtn::kMaxChi;
+      ok = ok && c <= gbtn::kMaxChi;
       s_chi[p] = c;
       s_st[p] = (int)st;
       st *= c;
       s_out[p] = g.edge_u[e] == v ? 2 * e : 2 * e + 1;
       s_in[p] = s_out[p] ^ 1;
     }
+    ok = ok && st == n;  // the offsets agree with this vertex's own shape
     s_k = k;
     s_n = (int)n;
     s_aoff = S.voff[v];
@@ -246,12 +278,31 @@ __global__ void __launch_bounds__(kThreads) static_mean_kernel(int ndir, unsigne
 
 constexpr size_t kSweepSmem = sizeof(double) * (3 * (size_t)kStaticMaxN + gbtn::kMaxDeg * 64 + kThreads + 64);
 
+// Per-device set-up: the scratch array's device address and the sweep
+// kernel's shared-memory limit.  A set-up that fails (for example a first
+// call made during a stream capture) is retried by the next call.
 struct DeviceSetup {
-  std::once_flag once;
+  std::mutex mu;
   unsigned char* ptr = nullptr;
-  cudaError_t err = cudaSuccess;
+  bool done = false;
 };
 DeviceSetup g_setup[64];
+
+cudaError_t setup_device(DeviceSetup& ds) {
+  std::lock_guard<std::mutex> lock(ds.mu);
+  if (ds.done) return cudaSuccess;
+  unsigned char* p = nullptr;
+  cudaError_t err = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_sweep_scratch);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(static_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
+  if (err != cudaSuccess || !p) {
+    cudaGetLastError();  // a failed set-up leaves no sticky error for the caller's next launch
+    return err != cudaSuccess ? err : cudaErrorInvalidSymbol;
+  }
+  ds.ptr = p;
+  ds.done = true;
+  return cudaSuccess;
+}
 
 }  // namespace
 
@@ -266,10 +317,10 @@ int gbtn_bp_sweep_static(int device, const gbtn_graph_desc* g, const double* fac
     return GBTN_ERR_INVALID;
   }
   if (g->nv < 1 || g->ne < 0 || g->nv > kStaticMaxVertices || 2LL * g->ne > kStaticMaxDirected ||
-      g->complex_values) {
+      g->complex_values || g->separate_bra) {
     return GBTN_ERR_UNSUPPORTED;
   }
-  if (!g->edge_dim || !g->site_dim || !g->leg_ptr || (g->ne > 0 && (!g->edge_u || !g->leg_edge))) {
+  if (!g->site_dim || !g->leg_ptr || (g->ne > 0 && (!g->edge_dim || !g->edge_u || !g->edge_v || !g->leg_edge))) {
     return GBTN_ERR_INVALID;
   }
   int prev = 0;
@@ -280,13 +331,8 @@ int gbtn_bp_sweep_static(int device, const gbtn_graph_desc* g, const double* fac
     return GBTN_ERR_CUDA;
   }
   DeviceSetup& ds = g_setup[device];
-  std::call_once(ds.once, [&] {
-    ds.err = cudaGetSymbolAddress(reinterpret_cast<void**>(&ds.ptr), g_sweep_scratch);
-    if (ds.err == cudaSuccess)
-      ds.err = cudaFuncSetAttribute(static_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
-  });
   int rc = GBTN_OK;
-  if (ds.err != cudaSuccess || !ds.ptr) {
+  if (setup_device(ds) != cudaSuccess) {
     rc = GBTN_ERR_CUDA;
   } else {
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);

@@ -182,3 +182,20 @@ def test_incoming_messages_factors_and_default_maxiter():
     assert all(a is b for a, b in zip(gbtn.factors(bpc, [1, 3]), [tn.tensors[1], tn.tensors[3]]))
     assert gbtn.default_bp_maxiter(bpc) is None  # a loopy grid: maxiter is required
     assert gbtn.default_bp_maxiter(Msgs(gbtn.random_network(square_lattice(4, 1), 1))) == 1
+
+
+def test_static_sweep_refusals_before_any_device_access(lib_built):
+    """gbtn_bp_sweep_static refuses, on the host and before touching a device,
+    more vertices than its fixed scratch holds and a descriptor with separate
+    bra tensors (it always contracts the ket with its own conjugate)."""
+    lib = _lib.load()
+    buf = C.c_void_p(1)
+    d = _lib.GraphDesc()
+    d.nv, d.ne = 16385, 0  # GBTN_STATIC_MAX_VERTICES + 1
+    assert lib.gbtn_bp_sweep_static(0, C.byref(d), buf, buf, buf, buf, None) == 3  # GBTN_ERR_UNSUPPORTED
+    d = _lib.GraphDesc()
+    d.nv, d.ne, d.separate_bra = 4, 0, 1
+    assert lib.gbtn_bp_sweep_static(0, C.byref(d), buf, buf, buf, buf, None) == 3
+    d = _lib.GraphDesc()
+    d.nv, d.ne, d.complex_values = 4, 0, 1
+    assert lib.gbtn_bp_sweep_static(0, C.byref(d), buf, buf, buf, buf, None) == 3
