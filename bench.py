@@ -1,19 +1,23 @@
 """Benchmark of the BP hot path: belief-propagation message updates per second.
 
 Workload (default): a batch of 16 independent 32x32 open PEPS, d=2, chi=8,
-i.i.d. N(0,1) site tensors (seeded), all-edges-at-once (Jacobi) sweeps.  One
-step = one sweep over the whole batch = 16 * 3968 directed-edge message
-updates.  The chosen path runs the contractions in BF16 on the tensor cores
-(FP32 accumulation, FP64 normalisation); the plain FP64 and the FP32 paths
-are measured beside it, and the mixed pipeline (BF16 -> FP32 -> FP64
-refinement) is timed to convergence against the plain FP64 path with its
-<Sz> error.  The BF16 tensor images of the batch take 236 MB, the FP32 copies
-486 MB and the FP64 tensors 972 MB -- all larger than L2 (129 MB), so no L2
-flush is needed between steps.
+i.i.d. N(0,1) site tensors (seeds 0..15), all-edges-at-once (Jacobi) sweeps.
+One step = one accuracy-matched solve of the whole batch from identity
+messages: the mixed pipeline (BF16 tensor-core sweeps, FP32 sweeps, then
+double-FP32 refinement sweeps with FP64 normalisation) until every network's
+mean message diff is <= 1e-14.  ``value`` = message updates the solve ran
+(sweeps of every phase x 63,488 directed edges) / solve time; the line also
+carries the plain FP64 GPU path's time to the same tolerance (the speed-up),
+the max relative <Sz> error against the FP64 oracle's converged fixed point
+(tests/golden/peps32x32_chi8_batch16.npz), the per-sweep rate of every
+arithmetic and each kernel's share of the solve.  The BF16 images of the
+batch take 236 MB, the FP64 tensors 972 MB -- larger than L2 (129 MB), so no
+L2 flush is needed between steps.
 
-Output: one JSON line (rank 0).  ``--impl reference`` times the CPU
-restatement of the reference's per-edge update (FP64, all host threads) on a
-bounded sample of the same workload."""
+Output: one JSON line (rank 0).  ``--impl reference`` times the C
+restatement of the reference's per-edge update (FP64, all host threads) on
+FP64 Jacobi sweeps of the same 16-network batch, one sweep per step.
+"""
 from __future__ import annotations
 
 import argparse
@@ -105,30 +109,49 @@ class ClockSampler:
 
 
 def make_batch(seed0=0):
-    import gbtn
-    nets = [gbtn.random_network(gbtn.square_lattice(L, L, chi=CHI, d=D), seed0 + k) for k in range(BATCH)]
-    return gbtn.disjoint_union(nets)
+    from gbtn import workloads
+    return workloads.peps_batch(BATCH, L, CHI, D, seed0)[0]
 
 
-def cpu_reference_rate(seconds=10.0, nthreads=0):
-    """Messages/s of the C restatement (FP64, OpenMP over directed edges) on
-    one 32x32 chi=8 network, Jacobi sweeps, until ``seconds`` elapsed."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import bp_oracle as O
-    import build_oracle
-    g = O.square_lattice(L, L, chi=CHI, d=D)
-    A = O.flatten_tensors(O.random_network(g, 0))
-    m0 = O.flatten_messages(g, O.identity_messages(g))
-    build_oracle.run(g, A, m0, "parallel", None, 1, nthreads=nthreads)  # warm-up
-    sweeps, t0 = 0, time.perf_counter()
-    while True:
-        build_oracle.run(g, A, m0, "parallel", None, 1, nthreads=nthreads)
-        sweeps += 1
-        el = time.perf_counter() - t0
-        if el >= seconds:
-            break
-    cores = nthreads or os.cpu_count()
-    return sweeps * MSGS_PER_NET / el, cores, f"{sweeps} Jacobi sweeps of one 32x32 chi=8 PEPS ({el:.1f} s)"
+def config_dict(world=1):
+    """The workload, identical for both arms."""
+    return {"workload": f"bp_solve_{BATCH}x_peps32x32_d2_chi8", "batch": BATCH, "L": L, "chi": CHI, "d": D,
+            "schedule": "parallel (Jacobi)", "tol": 1e-14, "init": "identity messages",
+            "l2": "inputs larger than L2 (fp64 tensors 972 MB)", "parallelism": f"replicas{world}"}
+
+
+class CpuReference:
+    """The C restatement of the reference's per-edge update (FP64, OpenMP over
+    directed edges) on the first `nets` networks of the batch, FP64 Jacobi
+    sweeps from identity messages."""
+
+    def __init__(self, nets=None, nthreads=0):
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import bp_oracle as O
+        import build_oracle
+        self.run_c = build_oracle.run
+        tn = make_batch()
+        self.nets = BATCH if nets is None else nets
+        nv, ne = self.nets * L * L, self.nets * 2 * L * (L - 1)
+        self.g = O.Graph(nv, tn.edges[:ne], tn.site_dims[:nv], tn.edge_dims[:ne], [list(l) for l in tn.legs[:nv]])
+        self.A = tn.flat()[:sum(tn.size(v) for v in range(nv))]
+        self.m0 = O.flatten_messages(self.g, O.identity_messages(self.g))
+        self.nthreads = nthreads
+        self.cores = nthreads or os.cpu_count()
+
+    def sweep_s(self):
+        t0 = time.perf_counter()
+        self.run_c(self.g, self.A, self.m0, "parallel", None, 1, nthreads=self.nthreads)
+        return time.perf_counter() - t0
+
+    def rate(self, seconds):
+        """msg-updates/s over sweeps until `seconds` elapsed (at least one)."""
+        sweeps, el = 0, 0.0
+        while sweeps == 0 or el < seconds:
+            el += self.sweep_s()
+            sweeps += 1
+        return (sweeps * self.nets * MSGS_PER_NET / el,
+                f"{sweeps} FP64 Jacobi sweeps of {self.nets} 32x32 chi=8 PEPS ({el:.1f} s, {self.cores} threads)")
 
 
 # ---- replica plumbing (one process per GPU, no data-path collective) ----------
@@ -168,48 +191,56 @@ def run_reference(args):
     rank, _, _ = replica_env()
     if not reference_runs_on(rank):
         return
-    rates = []
+    ref = CpuReference()
     for _ in range(args.warmup):
-        cpu_reference_rate(seconds=0.5)
-    for _ in range(args.steps):
-        r, cores, sample = cpu_reference_rate(seconds=2.0)
-        rates.append(r)
-    val = float(np.mean(rates))
+        ref.sweep_s()
+    times = [ref.sweep_s() for _ in range(args.steps)]  # one FP64 sweep of the whole batch per step
+    val = BATCH * MSGS_PER_NET * len(times) / sum(times)
+    sample = f"per step one FP64 Jacobi sweep of the {BATCH} networks ({np.mean(times):.2f} s, {ref.cores} threads)"
     line = {"impl": "reference", "metric": "bp_msg_updates_per_s", "value": val, "unit": "msg-updates/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * BATCH * MSGS_PER_NET / val, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"bp_sweep_{BATCH}x_peps32x32_d2_chi8", "batch": BATCH, "L": L, "chi": CHI, "d": D,
-                       "schedule": "parallel", "l2": "inputs larger than L2"},
-            "cpu_baseline": {"value": val, "unit": "msg-updates/s", "cores": cores, "kind": "port",
-                             "sample": "per step: " + sample},
+            "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_dict(args.gpus),
+            "cpu_baseline": {"value": val, "unit": "msg-updates/s", "cores": ref.cores, "kind": "port",
+                             "sample": sample},
             "e2e": {"value": val, "unit": "msg-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def oracle_sz_error(sz, fixture, sizes):
+    """Max over networks of max|<Sz> - oracle| / max|oracle| (the oracle's
+    converged fixed point from tests/golden; None when the fixture is absent)."""
+    f = ROOT / "tests" / "golden" / fixture
+    if not f.exists():
+        return None
+    ref = np.load(f)["sz"]
+    if len(ref) != len(sz):
+        return None
+    worst, off = 0.0, 0
+    for n in sizes:
+        a, b = ref[off:off + n], sz[off:off + n]
+        worst = max(worst, float(np.max(np.abs(b - a)) / np.max(np.abs(a))))
+        off += n
+    return worst
 
 
 def batched_uneven_timing(gbtn, ctx, stream, barrier, nnet=64, sweeps=20, seed=7):
     """Batched BP with uneven shapes: nnet independent square PEPS, side
     lengths ~ U{8..32}, per-edge bond dimensions ~ U{2..8}, d = 2, N(0,1)
     tensors, one plan.  Parallel sweeps in BF16 (tensor-core split chosen by
-    the autotuner, sweeps replayed from CUDA graphs; also timed without
-    graphs) and in plain FP64, msg-updates/s each; then the mixed pipeline and
-    plain FP64 to convergence from the same start, max relative error of
-    <Sz> per network."""
+    the autotuner, sweeps replayed from CUDA graphs), DF32 and plain FP64,
+    msg-updates/s each; then the mixed pipeline and plain FP64 to convergence
+    from the same start, max relative error of <Sz> per network against the
+    FP64 oracle's fixed point (tests/golden/uneven64_sz.npz)."""
     import torch
-    rng = np.random.default_rng(seed)
-    nets = []
-    for k in range(nnet):
-        Lk = int(rng.integers(8, 33))
-        ne = 2 * Lk * (Lk - 1)
-        dims = [int(x) for x in rng.integers(2, 9, size=ne)]
-        nets.append(gbtn.random_network(gbtn.square_lattice(Lk, Lk, d=2, edge_dims=dims), 5000 + k))
-    tn = gbtn.disjoint_union(nets)
+    from gbtn import workloads
+    tn, nets = workloads.uneven_batch(nnet, seed)
     msgs = 2 * tn.ne
     bpc = gbtn.BeliefPropagationCache(tn, ctx=ctx)
     is_tc, tune_ms = bpc.tc_split()
 
-    def ms_per_sweep(precision, graphs, n):
-        bpc.set_graphs(graphs)
+    def ms_per_sweep(precision, n):
+        bpc.set_graphs(True)
         bpc.init_messages("identity")
         bpc.update(maxiter=3, schedule="parallel", precision=precision)
         barrier()
@@ -220,36 +251,34 @@ def batched_uneven_timing(gbtn, ctx, stream, barrier, nnet=64, sweeps=20, seed=7
         barrier()
         return e0.elapsed_time(e1) / n
 
-    ms16g = ms_per_sweep("bf16", True, sweeps)
-    ms16 = ms_per_sweep("bf16", False, sweeps)
-    ms64 = ms_per_sweep("f64", True, max(4, sweeps // 4))
+    ms16 = ms_per_sweep("bf16", sweeps)
+    msdf = ms_per_sweep("df32", max(4, sweeps // 4))
+    ms64 = ms_per_sweep("f64", max(4, sweeps // 4))
     sz_op = np.array([[0.5, 0.0], [0.0, -0.5]])
+    sizes = [n.nv for n in nets]
 
-    def solve(precision, **kw):
+    def solve(precision):
         bpc.set_graphs(True)
         bpc.init_messages("identity")
         barrier()
         t0 = time.perf_counter()
-        bpc.update(maxiter=400, tol=1e-14, schedule="parallel", precision=precision, **kw)
+        bpc.update(maxiter=400, tol=1e-14, schedule="parallel", precision=precision)
         barrier()
-        return (time.perf_counter() - t0) * 1e3, bpc.expect(sz_op)
+        return (time.perf_counter() - t0) * 1e3, bpc.expect(sz_op), bpc.phase_sweeps()
 
-    t64, sz64 = solve("f64")
-    tmix, szmix = solve("mixed", refine_f64=2)
-    errs, off = [], 0
-    for net in nets:
-        a, b = sz64[off:off + net.nv], szmix[off:off + net.nv]
-        errs.append(float(np.max(np.abs(b - a)) / np.max(np.abs(a))))
-        off += net.nv
+    solve("mixed")  # warm-up (graphs captured)
+    t64, sz64, ph64 = solve("f64")
+    tmix, szmix, phmix = solve("mixed")
     out = {"workload": f"bp_batch_{nnet}x_peps_L8-32_chi2-8_d2", "networks": nnet, "vertices": tn.nv,
            "msgs_per_sweep": msgs,
-           "bf16_graph_ms_per_sweep": ms16g, "bf16_ms_per_sweep": ms16, "fp64_ms_per_sweep": ms64,
-           "bf16_msg_updates_per_s": msgs / (ms16g * 1e-3), "fp64_msg_updates_per_s": msgs / (ms64 * 1e-3),
-           "chosen_over_fp64_per_sweep": ms64 / ms16g,
+           "ms_per_sweep": {"bf16": ms16, "df32": msdf, "f64": ms64},
+           "bf16_msg_updates_per_s": msgs / (ms16 * 1e-3), "fp64_msg_updates_per_s": msgs / (ms64 * 1e-3),
            "tc_split": {"tensor_core_vertices": int(is_tc.sum()), "simt_vertices": int(tn.nv - is_tc.sum()),
                         "tuned_split_ms": tune_ms},
-           "time_to_solution": {"tol": 1e-14, "fp64_ms": t64, "mixed_ms": tmix, "speedup": t64 / tmix,
-                                "mixed_max_rel_err_sz": max(errs)}}
+           "time_to_solution": {"tol": 1e-14, "fp64_ms": t64, "fp64_sweeps": ph64["f64"], "mixed_ms": tmix,
+                                "mixed_phase_sweeps": phmix, "speedup": t64 / tmix,
+                                "mixed_max_rel_err_sz_vs_oracle": oracle_sz_error(szmix, "uneven64_sz.npz", sizes),
+                                "fp64_max_rel_err_sz_vs_oracle": oracle_sz_error(sz64, "uneven64_sz.npz", sizes)}}
     bpc.close()
     return out
 
@@ -371,26 +400,14 @@ def run_ours(args):
     stream = torch.cuda.ExternalStream(ctx.stream)
     tn = make_batch(seed0=replica_seed(rank))
     bpc = gbtn.BeliefPropagationCache(tn, ctx=ctx)
+    bpc.set_graphs(True)
     lib = ctx.lib
     # tensor-core routing of the BF16 phase, chosen by the library's autotuner
     # (timed on these vertices before the warm-up)
     is_tc, tune_ms = bpc.tc_split()
-
-    def run(n, precision, tol=None, **mixed):
-        o = _lib.BPOpts()
-        o.schedule, o.precision, o.maxiter, o.normalize = 1, _lib.PRECISION[precision], n, 1
-        o.tol = -1.0 if tol is None else tol
-        o.edge_sequence = C.cast(None, C.POINTER(C.c_int32))
-        o.tol_bf16 = mixed.get("tol_bf16", 0.0)
-        o.tol_f32 = mixed.get("tol_f32", 0.0)
-        o.refine_f64 = mixed.get("refine_f64", 0)
-        if tol is None:
-            _lib.check(ctx.handle, lib.gbtn_bp_run(bpc.handle, C.byref(o), None, None))
-            return None
-        it = np.zeros(tn.n_networks, dtype=np.int32)
-        md = np.zeros(tn.n_networks)
-        _lib.check(ctx.handle, lib.gbtn_bp_run(bpc.handle, C.byref(o), _lib.iptr(it), _lib.dptr(md)))
-        return it
+    sz_op = np.array([[0.5, 0.0], [0.0, -0.5]])
+    msgs_step = BATCH * MSGS_PER_NET
+    sizes = [L * L] * BATCH
 
     def barrier():
         torch.cuda.synchronize()
@@ -400,64 +417,88 @@ def run_ours(args):
     def max_ranks(x):
         return max_over_ranks(x, world, "cuda")
 
-    def timed(precision, steps, warmup):
-        """ms per sweep: W untimed sweeps, then K sweeps between CUDA events."""
-        run(warmup, precision)
-        barrier()
+    def solve(precision):
+        bpc.init_messages("identity")
+        bpc.update(maxiter=args.solve_maxiter, tol=args.solve_tol, schedule="parallel", precision=precision)
+
+    def sweeps_of_last_run():
+        ph = bpc.phase_sweeps()
+        return ph, sum(ph.values())
+
+    # 1. the step: an accuracy-matched mixed solve of the batch (W warm-up, K timed;
+    #    CUDA events on the library's stream, clocks sampled during the timed region)
+    for _ in range(args.warmup):
+        solve("mixed")
+    barrier()
+    with ClockSampler(local) as clk:
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        run(steps, precision)
+        for _ in range(args.steps):
+            solve("mixed")
         e1.record(stream)
         barrier()
-        return max_ranks(e0.elapsed_time(e1) / steps)
+    ms_step = max_ranks(e0.elapsed_time(e1) / args.steps)
+    phases, sweeps_step = sweeps_of_last_run()
+    sz_mixed = bpc.expect(sz_op)
+    err_mixed = oracle_sz_error(sz_mixed, "peps32x32_chi8_batch16.npz", sizes) if rank == 0 else None
+    updates_step = sweeps_step * msgs_step
 
-    msgs_step = BATCH * MSGS_PER_NET
-    # 1. chosen path: BF16 tensor-core sweeps (clocks sampled during the timed region)
-    with ClockSampler(local) as clk:
-        ms_bf16 = timed("bf16", args.steps, args.warmup)
-    ms_f32 = timed("f32", args.steps, args.warmup)
-    ms_f64 = timed("f64", max(2, args.steps // 2), 1)
+    # 2. the plain FP64 GPU path to the same tolerance from the same start
+    solve("f64")
+    barrier()
+    e0.record(stream)
+    solve("f64")
+    e1.record(stream)
+    barrier()
+    fp64_ms = max_ranks(e0.elapsed_time(e1))
+    fp64_sweeps = bpc.phase_sweeps()["f64"]
+    err_fp64 = (oracle_sz_error(bpc.expect(sz_op), "peps32x32_chi8_batch16.npz", sizes) if rank == 0 else None)
 
-    # 2. the dominant kernel's own duration, CUDA events around every launch
+    # 3. kernel shares of one mixed solve (CUDA events around every launch)
     ctx.set_profiling(True)
-    run(args.steps, "bf16")
+    solve("mixed")
+    barrier()
+    kcls = {"tc_vertex_kernel (bf16)": _lib.KCLASS_TENSOR_CORE, "bp_vertex_kernel<float>": _lib.KCLASS_SIMT_F32,
+            "bp_vertex_kernel<df32>": _lib.KCLASS_SIMT_DF32, "bp_vertex_kernel<double>": _lib.KCLASS_SIMT_F64}
+    kt = {name: ctx.kernel_time(k) for name, k in kcls.items()}
+    ctx.set_profiling(False)
+    k_total = sum(ms for ms, _ in kt.values()) or 1.0
+    shares = {name: {"ms": ms, "launches": n, "share_of_kernel_time": ms / k_total} for name, (ms, n) in kt.items()}
+
+    # 4. per-sweep rate of every arithmetic (K sweeps between CUDA events; the
+    #    tensor-core kernel's own launch time for its roofline)
+    def per_sweep(precision, n):
+        bpc.init_messages("identity")
+        bpc.update(maxiter=max(3, args.warmup), schedule="parallel", precision=precision)
+        barrier()
+        e0.record(stream)
+        bpc.update(maxiter=n, schedule="parallel", precision=precision)
+        e1.record(stream)
+        barrier()
+        return max_ranks(e0.elapsed_time(e1) / n)
+
+    ms_bf16 = per_sweep("bf16", args.steps)
+    ms_f32 = per_sweep("f32", args.steps)
+    ms_df32 = per_sweep("df32", max(3, args.steps // 2))
+    ms_f64 = per_sweep("f64", max(2, args.steps // 4))
+    ctx.set_profiling(True)
+    bpc.update(maxiter=args.steps, schedule="parallel", precision="bf16")
     barrier()
     tc_ms, tc_n = ctx.kernel_time(_lib.KCLASS_TENSOR_CORE)
-    simt_ms, simt_n = ctx.kernel_time(_lib.KCLASS_SIMT_F32)
+    ctx.kernel_time(_lib.KCLASS_SIMT_F32)
     ctx.set_profiling(False)
 
-    # 3. time to solution: plain FP64 vs the mixed pipeline, same start, same tol
-    sz_op = np.array([[0.5, 0.0], [0.0, -0.5]])
-
-    def solve(precision, **kw):
-        bpc.init_messages("identity")
-        barrier()
-        t0 = time.perf_counter()
-        it = run(args.solve_maxiter, precision, tol=args.solve_tol, **kw)
-        barrier()
-        return (time.perf_counter() - t0) * 1e3, it
-
-    fp64_ms, fp64_it = solve("f64")
-    sz64 = bpc.expect(sz_op)
-    mix_ms, mix_it = solve("mixed", refine_f64=2)
-    szmix = bpc.expect(sz_op)
-    per_net = []
-    for k in range(BATCH):
-        a = sz64[k * L * L:(k + 1) * L * L]
-        b = szmix[k * L * L:(k + 1) * L * L]
-        per_net.append(float(np.max(np.abs(b - a)) / np.max(np.abs(a))))
-
-    # 4. end to end through the public API: pinned host tensors -> device, one
-    #    BF16 sweep (tensor images rebuilt from the new tensors), all messages back
-    n_fac, n_msg = bpc.n_factor, bpc.n_message
+    # 5. end to end through the public API: pinned host tensors -> device, the
+    #    mixed solve, <Sz> of every site back to the host
+    n_fac = bpc.n_factor
     host_fac = torch.from_numpy(tn.flat()).pin_memory()
-    host_msg = torch.empty(n_msg, dtype=torch.float64).pin_memory()
+    host_op = np.ascontiguousarray(sz_op.reshape(-1, order="F"))
+    host_sz = np.zeros(tn.nv)
 
     def e2e_step():
         _lib.check(ctx.handle, lib.gbtn_set_factors(bpc.handle, C.c_void_p(host_fac.data_ptr()), None, _lib.HOST))
-        bpc.init_messages("identity")
-        run(1, "bf16")
-        _lib.check(ctx.handle, lib.gbtn_get_messages(bpc.handle, C.c_void_p(host_msg.data_ptr()), _lib.HOST))
+        solve("mixed")
+        _lib.check(ctx.handle, lib.gbtn_expect1(bpc.handle, _lib.dptr(host_op), 0, _lib.dptr(host_sz)))
 
     for _ in range(args.warmup):
         e2e_step()
@@ -468,10 +509,7 @@ def run_ours(args):
     barrier()
     e2e_ms = max_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
 
-    # 4b. message normalisation / gauge scaling (rescale_messages, an HBM-type
-    #     kernel: every message read and written once) on converged messages
-    bpc.init_messages("identity")
-    run(30, "f64")
+    # 6. message normalisation / gauge scaling (rescale_messages, HBM-type) on converged messages
     ctx.set_profiling(True)
     for _ in range(args.warmup):
         bpc.rescale_messages()
@@ -480,108 +518,88 @@ def run_ours(args):
         bpc.rescale_messages()
     g_ms, g_n = ctx.kernel_time(_lib.KCLASS_GAUGE)
     ctx.set_profiling(False)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs") or 6800.0
+    hbm_src = "measured" if peaks.get("hbm_gbs") else "fallback"
     g_launch_ms = g_ms / max(g_n, 1)
-    g_bytes = 2 * n_msg * 8
-    hbm_peak = (json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs")
-                if (ROOT / "MEASURED_PEAKS.json").exists() else None) or 6800.0
-    gauge = {"kernel": "rescale_messages_kernel", "workload": "all messages of the batch (FP64)",
-             "launch_ms": g_launch_ms, "launches": g_n, "algorithmic_bytes": g_bytes,
+    g_bytes = 2 * bpc.n_message * 8
+    gauge = {"kernel": "rescale_messages_kernel", "launch_ms": g_launch_ms, "algorithmic_bytes": g_bytes,
              "achieved_gbs": g_bytes / (g_launch_ms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
              "frac": g_bytes / (g_launch_ms * 1e-3) / 1e9 / hbm_peak}
 
-    # 5. gradient of the BP energy (Heisenberg, 12x12, d=2, chi=6, unit-norm tensors):
-    #    mixed-precision BP to convergence + FP64 implicit adjoint, and the
-    #    checkpointed 30-sweep unrolled variant; seconds per full dE/dA
+    # 7. the other configurations: gradient (c5), simple update (c4), uneven batch (c3)
     grad = gradient_timing(gbtn, ctx, barrier, rank)
-    # 6. simple update (TFIM, 20x20, 200 steps)
     su = simple_update_timing(gbtn, ctx, barrier, rank)
-    # 7. batched BP with uneven shapes (64 networks, L 8..32, chi 2..8)
     batched = batched_uneven_timing(gbtn, ctx, stream, barrier)
 
-    value = aggregate_rate(world, msgs_step, ms_bf16)
-    # algorithmic flops of one tensor-core launch: every routed vertex's k
-    # messages of 2 d prod(chi) sum(chi) each, at its own (unpadded) shape
+    # roofline of the tensor-core kernel: algorithmic flops and compulsory bytes of
+    # the routed vertices at their own (unpadded) shapes / its event-timed launch
     tc_v = [v for v in range(tn.nv) if is_tc[v]]
     n_tc = len(tc_v)
-    alg_flops_launch = float(sum(len(tn.legs[v]) * 2.0 * tn.size(v) * sum(tn.edge_dims[e] for e in tn.legs[v])
-                                 for v in tc_v))
-    n_tc_native = sum(1 for v in tc_v if len(tn.legs[v]) == 4)
-    mma_flops_vertex = 2 * (2 * 128 * 64 * 64) + 2 * (2 * 64 * 64 * 128)  # GEMM1, GEMM1', GEMM2, GEMM2'
-    # compulsory bytes of one launch: every routed vertex's BF16 tensor at its
-    # own (unpadded) shape, and each of its incoming and outgoing FP32 messages once
-    alg_bytes_launch = float(sum(2 * tn.size(v) + 2 * 4 * sum(tn.edge_dims[e] ** 2 for e in tn.legs[v])
-                                 for v in tc_v))
+    alg_flops = float(sum(len(tn.legs[v]) * 2.0 * tn.size(v) * sum(tn.edge_dims[e] for e in tn.legs[v])
+                          for v in tc_v))
+    alg_bytes = float(sum(2 * tn.size(v) + 2 * 4 * sum(tn.edge_dims[e] ** 2 for e in tn.legs[v]) for v in tc_v))
     tc_launch_ms = tc_ms / max(tc_n, 1)
-    achieved = alg_flops_launch / (tc_launch_ms * 1e-3) / 1e12
-    achieved_gbs = alg_bytes_launch / (tc_launch_ms * 1e-3) / 1e9
-    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-    peak = peaks.get("bf16_tflops")
-    peak_src = "measured burst" if peak else "fallback"
-    peak = peak or 1900.0
-    hbm_src = "measured" if peaks.get("hbm_gbs") else "fallback"
-    # the binding roof: the arithmetic intensity (flops per compulsory byte) is
-    # below the ridge point of the two peaks, so HBM caps the kernel first
-    intensity = alg_flops_launch / max(alg_bytes_launch, 1.0)
-    ridge = peak * 1e12 / (hbm_peak * 1e9)
-    bound = "hbm" if intensity < ridge else "tensor"
+    achieved_tf = alg_flops / (tc_launch_ms * 1e-3) / 1e12
+    achieved_gbs = alg_bytes / (tc_launch_ms * 1e-3) / 1e9
+    bf16_peak = peaks.get("bf16_tflops") or 1900.0
+    bf16_src = "measured burst" if peaks.get("bf16_tflops") else "fallback"
+    intensity = alg_flops / max(alg_bytes, 1.0)
+    ridge = bf16_peak * 1e12 / (hbm_peak * 1e9)
     traffic = None
     tfile = ROOT / "profiles" / "tc_vertex_kernel_traffic.json"
     if tfile.exists():
-        tj = json.loads(tfile.read_text())
-        traffic = tj["dram_bytes_per_vertex"] * n_tc
+        traffic = json.loads(tfile.read_text())["dram_bytes_per_vertex"] * n_tc
+    mma_flops_vertex = 2 * (2 * 128 * 64 * 64) + 2 * (2 * 64 * 64 * 128)
+    if intensity < ridge:
+        roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved_gbs / hbm_peak, "traffic": traffic}
+    else:
+        roof = {"bound": "tensor", "achieved": achieved_tf, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": achieved_tf / bf16_peak, "traffic": traffic}
+    roof.update({"kernel": "tc_vertex_kernel", "launch_ms": tc_launch_ms, "units_per_launch": n_tc,
+                 "unit_kind": "vertex", "alg_bytes_per_unit": alg_bytes / max(n_tc, 1),
+                 "alg_flops_per_unit": alg_flops / max(n_tc, 1), "intensity": intensity, "ridge": ridge,
+                 "tensor_frac": achieved_tf / bf16_peak,
+                 "mma_issued_tflops": n_tc * mma_flops_vertex / (tc_launch_ms * 1e-3) / 1e12,
+                 "peaks": f"{hbm_src} hbm, {bf16_src} bf16"})
     if rank == 0:
-        cpu_val, cores, sample = cpu_reference_rate(seconds=10.0)
-        cpu1_val, _, sample1 = cpu_reference_rate(seconds=3.0, nthreads=1)
+        cpu = CpuReference()
+        cpu_val, sample = cpu.rate(10.0)
+        cpu1_val, sample1 = CpuReference(nets=1, nthreads=1).rate(3.0)
+        value = aggregate_rate(world, updates_step, ms_step)
         line = {
             "metric": "bp_msg_updates_per_s", "value": value, "unit": "msg-updates/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_bf16, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-            "config": {"workload": f"bp_sweep_{BATCH}x_peps32x32_d2_chi8", "batch": BATCH, "L": L, "chi": CHI, "d": D,
-                       "schedule": "parallel (Jacobi)",
-                       "chosen_path": "bf16 tcgen05 contractions (vertices padded to degree 4, chi 8; autotuned split with fp32 simt), fp32 accumulation",
-                       "l2": "inputs larger than L2 (bf16 images 236 MB)", "parallelism": f"replicas{world}"},
-            "paths_ms_per_sweep": {"bf16_tensor_core": ms_bf16, "f32_simt": ms_f32, "f64_simt": ms_f64},
-            "chosen_over_fp64_per_sweep": ms_f64 / ms_bf16,
-            "time_to_solution": {
-                "tol": args.solve_tol, "fp64_ms": fp64_ms, "fp64_sweeps": int(np.max(fp64_it)),
-                "mixed_ms": mix_ms, "mixed_final_fp64_sweeps": int(np.max(mix_it)),
-                "speedup": fp64_ms / mix_ms, "mixed_max_rel_err_sz": max(per_net)},
-            "roofline": dict(
-                {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                 "frac": achieved_gbs / hbm_peak, "traffic": traffic}
-                if bound == "hbm" else
-                {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                 "frac": achieved / peak, "traffic": traffic},
-                **{"kernel": "tc_vertex_kernel", "launch_ms": tc_launch_ms, "launches": tc_n,
-                   "other_kernels_ms_per_sweep": {"simt_f32": simt_ms / max(args.steps, 1)},
-                   "units_per_launch": n_tc, "unit_kind": "vertex (all outgoing messages)",
-                   "alg_bytes_per_launch": alg_bytes_launch, "alg_bytes_per_unit": alg_bytes_launch / max(n_tc, 1),
-                   "alg_flops_per_launch": alg_flops_launch,
-                   "alg_flops_per_unit": alg_flops_launch / max(n_tc, 1),
-                   "intensity_flop_per_byte": intensity, "ridge_flop_per_byte": ridge,
-                   "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                           "frac": achieved_gbs / hbm_peak},
-                   "tensor": {"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                              "mma_issued_tflops": n_tc * mma_flops_vertex / (tc_launch_ms * 1e-3) / 1e12},
-                   "tc_split": {"policy": "auto", "tensor_core_vertices": n_tc,
-                                "of_which_degree4": n_tc_native, "simt_vertices": tn.nv - n_tc,
-                                "tuned_split_ms": tune_ms},
-                   "note": (f"algorithmic bytes and flops of the routed vertices at their unpadded shapes / "
-                            f"event-timed kernel duration; bound = the roof the intensity meets first "
-                            f"({hbm_src} HBM copy bandwidth, {peak_src} bf16 peak); traffic = ncu DRAM "
-                            f"bytes per vertex (padded images) x vertices")}),
-            "gradient": grad,
-            "simple_update": su,
-            "batched_uneven": batched,
-            "gauge_scaling": gauge,
-            "cpu_baseline": {"value": cpu_val, "unit": "msg-updates/s", "cores": cores, "kind": "port",
-                             "sample": sample,
-                             "single_core": {"value": cpu1_val, "unit": "msg-updates/s", "cores": 1,
-                                             "sample": sample1}},
-            "e2e": {"value": aggregate_rate(world, msgs_step, e2e_ms), "unit": "msg-updates/s",
-                    "h2d_bytes_per_step": n_fac * 8, "d2h_bytes_per_step": n_msg * 8},
-            "gpu_launches": int(tc_n + simt_n + 2),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32+df32", "data": "synthetic",
+            "config": config_dict(world),
+            "time_to_solution": {"tol": args.solve_tol, "mixed_ms": ms_step, "fp64_ms": fp64_ms,
+                                 "speedup": fp64_ms / ms_step, "mixed_phase_sweeps": phases,
+                                 "fp64_sweeps": fp64_sweeps,
+                                 "mixed_max_rel_err_sz_vs_oracle": err_mixed,
+                                 "fp64_max_rel_err_sz_vs_oracle": err_fp64},
+            "e2e": {"value": aggregate_rate(world, updates_step, e2e_ms), "unit": "msg-updates/s",
+                    "ms_per_step": e2e_ms, "h2d_bytes_per_step": n_fac * 8, "d2h_bytes_per_step": tn.nv * 8},
+            # own kernels per timed solve: the message kernels counted above, one
+            # convergence reduction per sweep, message conversions and the init
+            "gpu_launches": int(sum(n for _, n in kt.values()) + sweeps_step + 4) * args.steps,
             "clocks": clk.summary(),
+            "roofline": roof,
+            "cpu_baseline": {"value": cpu_val, "unit": "msg-updates/s", "cores": cpu.cores, "kind": "port",
+                             "sample": sample,
+                             "single_core": {"value": cpu1_val, "cores": 1, "sample": sample1}},
+            "chosen_path": ("mixed: bf16 tcgen05 sweeps (fp32 accumulation, autotuned split with fp32 simt), "
+                            "fp32 simt sweeps, double-fp32 refinement sweeps; norms and diffs fp64"),
+            "value_definition": "message updates the solve ran (every phase's sweeps x 63488) / solve time",
+            "fp64_equivalent_msg_updates_per_s": aggregate_rate(world, fp64_sweeps * msgs_step, ms_step),
+            "kernel_shares_of_mixed_solve": shares,
+            "paths_ms_per_sweep": {"bf16_tensor_core": ms_bf16, "f32_simt": ms_f32, "df32_simt": ms_df32,
+                                   "f64_simt": ms_f64},
+            "tc_split": {"tensor_core_vertices": n_tc, "simt_vertices": tn.nv - n_tc, "tuned_split_ms": tune_ms},
+            "gauge_scaling": gauge,
+            "batched_uneven": batched,
+            "simple_update": su,
+            "gradient": grad,
         }
         print(json.dumps(line))
     bpc.close()

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define GBTN_ABI_VERSION 1
+#define GBTN_ABI_VERSION 2
 
 enum gbtn_status {
   GBTN_OK = 0,
@@ -57,11 +57,17 @@ enum gbtn_mem { GBTN_HOST = 0, GBTN_DEVICE = 1 };
 enum gbtn_schedule { GBTN_SCHED_SEQUENTIAL = 0, GBTN_SCHED_PARALLEL = 1, GBTN_SCHED_COLORED = 2 };
 
 /* Arithmetic of the message contractions.  MIXED runs BF16 tensor-core
- * sweeps (FP32 accumulation), then FP32 sweeps, then FP64 sweeps, each phase
- * started from the previous phase's fixed point.  BF16 and MIXED run the
- * PARALLEL and COLORED schedules (SEQUENTIAL returns GBTN_ERR_UNSUPPORTED);
- * FP32 and FP64 run all three. */
-enum gbtn_precision { GBTN_F64 = 0, GBTN_F32 = 1, GBTN_BF16 = 2, GBTN_MIXED = 3 };
+ * sweeps (FP32 accumulation), then FP32 sweeps, then refinement sweeps (DF32
+ * by default, or FP64: gbtn_bp_opts.refine), each phase started from the
+ * previous phase's fixed point.  DF32 is double-FP32 arithmetic (a value is
+ * the unevaluated sum of two floats, ~48 significant bits, on the FP32 pipe)
+ * on FP64 tensors and messages, with message norms and diffs in FP64.  BF16,
+ * DF32 and MIXED run the PARALLEL and COLORED schedules (SEQUENTIAL returns
+ * GBTN_ERR_UNSUPPORTED); FP32 and FP64 run all three.  Complex plans have no
+ * BF16 or DF32 path: their MIXED pipeline is FP32 then FP64. */
+enum gbtn_precision { GBTN_F64 = 0, GBTN_F32 = 1, GBTN_BF16 = 2, GBTN_MIXED = 3, GBTN_DF32 = 4 };
+/* Refinement arithmetic of MIXED after its FP32 phase. */
+enum gbtn_refine { GBTN_REFINE_DF32 = 0, GBTN_REFINE_F64 = 1 };
 
 enum gbtn_message_init { GBTN_INIT_IDENTITY = 0, GBTN_INIT_ONES = 1 };
 
@@ -118,8 +124,11 @@ typedef struct gbtn_bp_opts {
   double tol_f32;                /* default 1e-13 */
   int32_t maxiter_bf16;          /* default maxiter */
   int32_t maxiter_f32;           /* default maxiter */
-  int32_t refine_f64;            /* cap on the FP64 sweeps after FP32 (they stop
-                                    at tol), default maxiter */
+  int32_t refine_f64;            /* cap on the refinement sweeps after FP32
+                                    (they stop at tol), default maxiter */
+  int32_t refine;                /* gbtn_refine, default DF32 */
+  int32_t confirm_f64;           /* FP64 sweeps after a DF32 refinement
+                                    (they stop at tol), default 0 */
 } gbtn_bp_opts;
 
 /* ---- context ----------------------------------------------------------- */
@@ -140,7 +149,8 @@ enum gbtn_kernel_class {
   GBTN_KCLASS_TENSOR_CORE = 0,
   GBTN_KCLASS_SIMT_F32 = 1,
   GBTN_KCLASS_SIMT_F64 = 2,
-  GBTN_KCLASS_GAUGE = 3 /* rescale_messages: message normalisation and gauge scaling */
+  GBTN_KCLASS_GAUGE = 3, /* rescale_messages: message normalisation and gauge scaling */
+  GBTN_KCLASS_SIMT_DF32 = 4
 };
 int gbtn_ctx_set_profiling(gbtn_ctx* ctx, int on);
 /* Failure-detection test of the bounded device waits.  on = 1 makes every
@@ -208,6 +218,12 @@ int gbtn_init_messages(gbtn_plan* plan, int kind);
  * network, the sweeps run and sum(diff)/len(sequence) of the last sweep
  * (NaN when tol < 0). */
 int gbtn_bp_run(gbtn_plan* plan, const gbtn_bp_opts* opts, int32_t* iters, double* mean_diff);
+/* Instrumentation (no counterpart in the reference): the sweeps each phase of
+ * the last gbtn_bp_run took, the most over the plan's networks:
+ * sweeps[0..3] = BF16, FP32, refinement (DF32 or FP64), FP64 confirmation
+ * (0 for a phase that did not run; a single-precision run counts in its
+ * own slot, FP64 in slot 3). */
+int gbtn_plan_phase_sweeps(gbtn_plan* plan, int32_t sweeps[4]);
 /* Replaces: updated_message(bpc, edge) (abstractbeliefpropagationcache.jl:225-239,
  * 254-261): the normalised new message of one directed edge, FP64, written to
  * out (chi*chi) without changing the cache. */

@@ -9,6 +9,7 @@
 #include <memory>
 #include <mutex>
 #include <numeric>
+#include <type_traits>
 
 #include "gbtn_internal.h"
 
@@ -148,6 +149,9 @@ struct gbtn_plan {
     if (up_copy) cudaStreamDestroy(up_copy);
     if (up_build) cudaStreamDestroy(up_build);
   }
+  // sweeps per phase of the last run (max over networks): BF16, FP32, refinement, FP64
+  DevBuf<int> d_phase_iters;  // 4 x nnet
+  int phase_fixed[4] = {0, 0, 0, 0};  // sweeps of a phase run without a tolerance (all of its maxiter)
   // sequential schedule storage
   DevBuf<int2> d_seq;
   DevBuf<int> d_seq_ptr;
@@ -162,12 +166,27 @@ namespace {
 inline zdouble* zptr(double* p) { return reinterpret_cast<zdouble*>(p); }
 inline zfloat* zfptr(float* p) { return reinterpret_cast<zfloat*>(p); }
 
-// element type -> (graph-cache tag, FP32 kernel class?)
+// Arithmetic tag of the double-FP32 sweeps (FP64 storage, df32 arithmetic).
+struct DF32 {};
+
+// arithmetic -> (graph-cache tag, kernel class of the profiling API)
 template <typename T> struct ElemTraits;
-template <> struct ElemTraits<double> { static constexpr int tag = 0; static constexpr bool f32 = false; };
-template <> struct ElemTraits<float> { static constexpr int tag = 1; static constexpr bool f32 = true; };
-template <> struct ElemTraits<zdouble> { static constexpr int tag = 3; static constexpr bool f32 = false; };
-template <> struct ElemTraits<zfloat> { static constexpr int tag = 4; static constexpr bool f32 = true; };
+template <> struct ElemTraits<double> { static constexpr int tag = 0; static constexpr int kcls = GBTN_KCLASS_SIMT_F64; };
+template <> struct ElemTraits<float> { static constexpr int tag = 1; static constexpr int kcls = GBTN_KCLASS_SIMT_F32; };
+template <> struct ElemTraits<zdouble> { static constexpr int tag = 3; static constexpr int kcls = GBTN_KCLASS_SIMT_F64; };
+template <> struct ElemTraits<zfloat> { static constexpr int tag = 4; static constexpr int kcls = GBTN_KCLASS_SIMT_F32; };
+template <> struct ElemTraits<DF32> { static constexpr int tag = 5; static constexpr int kcls = GBTN_KCLASS_SIMT_DF32; };
+
+// One vertex-kernel launch in arithmetic A on storage T (A = T except for DF32).
+template <typename T, typename A>
+void launch_vertices(const WorkList& wl, const VDesc* vd, const T* fac, const T* bra, const T* in, T* out,
+                     const long long* msg_off, double* diffs, const int* conv, int normalize, int want_diff,
+                     cudaStream_t s) {
+  if constexpr (std::is_same<A, DF32>::value)
+    launch_bp_vertices_df32(wl, vd, fac, bra, in, out, msg_off, diffs, conv, normalize, want_diff, s);
+  else
+    launch_bp_vertices<T>(wl, vd, fac, bra, in, out, msg_off, diffs, conv, normalize, want_diff, s);
+}
 
 constexpr int kSmallN = 1024;  // vertices with n <= kSmallN run one per warp
 constexpr int kStallSweeps = 5;  // reduced-precision phases stop at their noise floor
@@ -364,8 +383,8 @@ void sweep_loop(gbtn_plan* P, int maxiter, const GraphKey& key, F&& sweep, bool 
   }
 }
 
-// Sweeps of the parallel or coloured schedule in precision T.
-template <typename T>
+// Sweeps of the parallel or coloured schedule on storage T in arithmetic A.
+template <typename T, typename A = T>
 void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normalize, T* msg0, T* msg1, const T* fac,
                 const T* bra, int& cur, int stall = 0) {
   cudaStream_t s = P->ctx->stream;
@@ -375,28 +394,29 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
   GBTN_CUDA(cudaMemsetAsync(P->d_nconv.p, 0, sizeof(int), s));
   const int* conv = want_diff ? P->d_conv.p : nullptr;
   T* msg[2] = {msg0, msg1};
-  const GraphKey key{ElemTraits<T>::tag, schedule, normalize, want_diff ? 1 : 0, stall, cur, P->list_version, tol};
+  const GraphKey key{ElemTraits<A>::tag, schedule, normalize, want_diff ? 1 : 0, stall, cur, P->list_version, tol};
+  constexpr int kcls = ElemTraits<A>::kcls;
   sweep_loop(P, maxiter, key, [&] {
     if (schedule == GBTN_SCHED_PARALLEL) {
       const T* in = msg[cur];
       T* out = msg[cur ^ 1];
       {
-        KTimer kt(P->ctx, ElemTraits<T>::f32 ? GBTN_KCLASS_SIMT_F32 : GBTN_KCLASS_SIMT_F64, P->lists[0].first.count > 0);
-        launch_bp_vertices<T>(P->lists[0].first, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
+        KTimer kt(P->ctx, kcls, P->lists[0].first.count > 0);
+        launch_vertices<T, A>(P->lists[0].first, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
                               normalize, want_diff, s);
       }
       {
-        KTimer kt(P->ctx, ElemTraits<T>::f32 ? GBTN_KCLASS_SIMT_F32 : GBTN_KCLASS_SIMT_F64, P->lists[0].second.count > 0);
-        launch_bp_vertices<T>(P->lists[0].second, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
+        KTimer kt(P->ctx, kcls, P->lists[0].second.count > 0);
+        launch_vertices<T, A>(P->lists[0].second, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
                               normalize, want_diff, s);
       }
       cur ^= 1;
     } else {
       for (size_t c = 1; c < P->lists.size(); ++c) {
         T* m = msg[cur];
-        launch_bp_vertices<T>(P->lists[c].first, P->d_vd.p, fac, bra, m, m, P->d_msg_off.p, P->d_diffs.p, conv,
+        launch_vertices<T, A>(P->lists[c].first, P->d_vd.p, fac, bra, m, m, P->d_msg_off.p, P->d_diffs.p, conv,
                               normalize, want_diff, s);
-        launch_bp_vertices<T>(P->lists[c].second, P->d_vd.p, fac, bra, m, m, P->d_msg_off.p, P->d_diffs.p, conv,
+        launch_vertices<T, A>(P->lists[c].second, P->d_vd.p, fac, bra, m, m, P->d_msg_off.p, P->d_diffs.p, conv,
                               normalize, want_diff, s);
       }
     }
@@ -637,6 +657,12 @@ void finish_iters(gbtn_plan* P, bool want_diff, int maxiter, int32_t* iters, dou
   GBTN_CUDA(cudaStreamSynchronize(s));
   if (iters) std::copy(it.begin(), it.end(), iters);
   if (mean_diff) std::copy(md.begin(), md.end(), mean_diff);
+}
+
+// Keep the per-network sweep counts of the phase that just ran (slot 0-3).
+void record_phase(gbtn_plan* P, int slot) {
+  GBTN_CUDA(cudaMemcpyAsync(P->d_phase_iters.p + (size_t)slot * P->nnet, P->d_iters.p, sizeof(int) * P->nnet,
+                            cudaMemcpyDeviceToDevice, P->ctx->stream));
 }
 
 void compute_rdms(gbtn_plan* P) {
@@ -1158,6 +1184,8 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   GBTN_CUDA(cudaMallocHost(&P->h_nconv, 2 * sizeof(int)));
   for (cudaEvent_t& e : P->poll_ev) GBTN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   P->d_iters.alloc(P->nnet);
+  P->d_phase_iters.alloc(4 * (size_t)P->nnet);
+  GBTN_CUDA(cudaMemsetAsync(P->d_phase_iters.p, 0, sizeof(int) * 4 * P->nnet, s));
   P->d_since.alloc(P->nnet);
   P->d_best.alloc(P->nnet);
   P->d_rdm.alloc(es * std::max<long long>(P->n_rdm, 1));
@@ -1353,7 +1381,11 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
   require(P && o, "NULL argument");
   require(o->maxiter >= 1, "You need to specify a number of iterations for BP!");
   require(o->schedule >= 0 && o->schedule <= 2, "unknown schedule");
-  require(o->precision >= 0 && o->precision <= 3, "unknown precision");
+  require(o->precision >= 0 && o->precision <= 4, "unknown precision");
+  require(o->refine == GBTN_REFINE_DF32 || o->refine == GBTN_REFINE_F64, "unknown refinement arithmetic");
+  require(o->confirm_f64 >= 0, "confirm_f64 must be >= 0");
+  for (int& f : P->phase_fixed) f = 0;
+  GBTN_CUDA(cudaMemsetAsync(P->d_phase_iters.p, 0, sizeof(int) * 4 * P->nnet, P->ctx->stream));
   cudaStream_t s = P->ctx->stream;
   const bool want_diff = o->tol >= 0.0;
   if (P->ne == 0) {
@@ -1364,8 +1396,12 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     throw Unsupported("BF16 sweeps run the parallel or coloured schedule");
   if (o->precision == GBTN_MIXED && o->schedule == GBTN_SCHED_SEQUENTIAL)
     throw Unsupported("the mixed BF16 -> FP32 -> FP64 pipeline runs the parallel or coloured schedule");
+  if (o->precision == GBTN_DF32 && o->schedule == GBTN_SCHED_SEQUENTIAL)
+    throw Unsupported("double-FP32 sweeps run the parallel or coloured schedule");
   if (P->cplx && o->precision == GBTN_BF16)
     throw Unsupported("complex tensors have no tensor-core (BF16) path: use f32, mixed or f64");
+  if (P->cplx && o->precision == GBTN_DF32)
+    throw Unsupported("complex tensors have no double-FP32 path: use f32, mixed or f64");
   if (o->schedule == GBTN_SCHED_SEQUENTIAL) {
     require(o->edge_sequence && o->edge_sequence_len > 0, "SEQUENTIAL needs an edge sequence");
     std::vector<std::vector<int2>> per(P->nnet);
@@ -1426,9 +1462,17 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     }
     return GBTN_OK;
   }
+  // phase slots of gbtn_plan_phase_sweeps: 0 BF16, 1 FP32, 2 refinement, 3 FP64
+  auto phase_done = [&](int slot, double phase_tol, int sweeps_run) {
+    if (phase_tol >= 0.0)
+      record_phase(P, slot);  // the reduction kernel counted each network's sweeps
+    else
+      P->phase_fixed[slot] = sweeps_run;  // no convergence test: every sweep ran
+  };
   if (P->cplx && o->precision == GBTN_F64) {
     run_sweeps<zdouble>(P, o->schedule, o->maxiter, o->tol, o->normalize, zptr(P->d_msg[0].p), zptr(P->d_msg[1].p),
                         zptr(P->d_fac.p), P->sep_bra ? zptr(P->d_bra.p) : nullptr, P->cur);
+    phase_done(3, o->tol, o->maxiter);
     finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
   } else if (P->cplx) {  // complex FP32 sweeps (F32), then FP64 ones (MIXED): no tensor-core phase
     ensure_f32(P);
@@ -1440,11 +1484,13 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     run_sweeps<zfloat>(P, o->schedule, it32, tol32, o->normalize, zfptr(P->d_msg32[0].p), zfptr(P->d_msg32[1].p),
                        zfptr(P->d_fac32.p), P->sep_bra ? zfptr(P->d_bra32.p) : nullptr, c32,
                        mixed ? kStallSweeps : 0);
+    phase_done(1, tol32, it32);
     launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, 2 * P->n_msg, s);
     if (mixed) {
       const int nref = o->refine_f64 > 0 ? std::min(o->refine_f64, o->maxiter) : o->maxiter;
       run_sweeps<zdouble>(P, o->schedule, nref, o->tol, o->normalize, zptr(P->d_msg[0].p), zptr(P->d_msg[1].p),
                           zptr(P->d_fac.p), P->sep_bra ? zptr(P->d_bra.p) : nullptr, P->cur);
+      phase_done(2, o->tol, nref);
       finish_iters(P, want_diff, nref, iters, mean_diff);
     } else {
       finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
@@ -1452,6 +1498,12 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
   } else if (o->precision == GBTN_F64) {
     run_sweeps<double>(P, o->schedule, o->maxiter, o->tol, o->normalize, P->d_msg[0].p, P->d_msg[1].p, P->d_fac.p,
                        P->sep_bra ? P->d_bra.p : nullptr, P->cur);
+    phase_done(3, o->tol, o->maxiter);
+    finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
+  } else if (o->precision == GBTN_DF32) {
+    run_sweeps<double, DF32>(P, o->schedule, o->maxiter, o->tol, o->normalize, P->d_msg[0].p, P->d_msg[1].p,
+                             P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->cur);
+    phase_done(2, o->tol, o->maxiter);
     finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
   } else if (o->precision == GBTN_F32) {
     ensure_f32(P);
@@ -1459,6 +1511,7 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, s);
     run_sweeps<float>(P, o->schedule, o->maxiter, o->tol, o->normalize, P->d_msg32[0].p, P->d_msg32[1].p, P->d_fac32.p,
                       P->sep_bra ? P->d_bra32.p : nullptr, c32);
+    phase_done(1, o->tol, o->maxiter);
     launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
     finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
   } else if (o->precision == GBTN_BF16) {
@@ -1469,9 +1522,10 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     if (bf16_has_simt(P)) ensure_f32(P);  // with every vertex on the tensor cores the FP32 factors go unread
     ensure_zimg(P);
     run_sweeps_bf16(P, o->schedule, o->maxiter, o->tol, o->normalize, c32);
+    phase_done(0, o->tol, o->maxiter);
     launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
     finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
-  } else {  // MIXED: BF16 tensor-core phase, FP32 phase, then FP64 refinement
+  } else {  // MIXED: BF16 tensor-core phase, FP32 phase, then DF32 (or FP64) refinement
     ensure_f32(P);
     int c32 = 0;
     const double tol32 = o->tol_f32 > 0 ? o->tol_f32 : 1e-13;
@@ -1483,15 +1537,49 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
       const double tol16 = o->tol_bf16 > 0 ? o->tol_bf16 : 1e-6;
       const int it16 = o->maxiter_bf16 > 0 ? o->maxiter_bf16 : o->maxiter;
       run_sweeps_bf16(P, o->schedule, it16, tol16, o->normalize, c32, kStallSweeps);
+      phase_done(0, tol16, it16);
     }
     run_sweeps<float>(P, o->schedule, it32, tol32, o->normalize, P->d_msg32[0].p, P->d_msg32[1].p, P->d_fac32.p,
                       P->sep_bra ? P->d_bra32.p : nullptr, c32, kStallSweeps);
+    phase_done(1, tol32, it32);
     launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
-    // FP64 sweeps from the FP32 fixed point until tol (or refine_f64 / maxiter sweeps)
+    // refinement sweeps from the FP32 fixed point until tol (or refine_f64 / maxiter sweeps)
     const int nref = o->refine_f64 > 0 ? std::min(o->refine_f64, o->maxiter) : o->maxiter;
-    run_sweeps<double>(P, o->schedule, nref, o->tol, o->normalize, P->d_msg[0].p, P->d_msg[1].p, P->d_fac.p,
-                       P->sep_bra ? P->d_bra.p : nullptr, P->cur);
-    finish_iters(P, want_diff, nref, iters, mean_diff);
+    if (o->refine == GBTN_REFINE_F64) {
+      run_sweeps<double>(P, o->schedule, nref, o->tol, o->normalize, P->d_msg[0].p, P->d_msg[1].p, P->d_fac.p,
+                         P->sep_bra ? P->d_bra.p : nullptr, P->cur);
+      phase_done(2, o->tol, nref);
+      finish_iters(P, want_diff, nref, iters, mean_diff);
+    } else {
+      run_sweeps<double, DF32>(P, o->schedule, nref, o->tol, o->normalize, P->d_msg[0].p, P->d_msg[1].p,
+                               P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->cur);
+      phase_done(2, o->tol, nref);
+      if (o->confirm_f64 > 0) {
+        const int nc = std::min(o->confirm_f64, o->maxiter);
+        run_sweeps<double>(P, o->schedule, nc, o->tol, o->normalize, P->d_msg[0].p, P->d_msg[1].p, P->d_fac.p,
+                           P->sep_bra ? P->d_bra.p : nullptr, P->cur);
+        phase_done(3, o->tol, nc);
+        finish_iters(P, want_diff, nc, iters, mean_diff);
+      } else {
+        finish_iters(P, want_diff, nref, iters, mean_diff);
+      }
+    }
+  }
+  API_CATCH(C)
+}
+
+int gbtn_plan_phase_sweeps(gbtn_plan* P, int32_t* sweeps) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && sweeps, "NULL argument");
+  std::vector<int> it(4 * (size_t)P->nnet);
+  GBTN_CUDA(cudaMemcpyAsync(it.data(), P->d_phase_iters.p, sizeof(int) * it.size(), cudaMemcpyDeviceToHost,
+                            P->ctx->stream));
+  GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));
+  for (int k = 0; k < 4; ++k) {
+    int m = P->phase_fixed[k];
+    for (int n = 0; n < P->nnet; ++n) m = std::max(m, it[(size_t)k * P->nnet + n]);
+    sweeps[k] = m;
   }
   API_CATCH(C)
 }

@@ -4,6 +4,8 @@
 // shared-memory carve-up.  Included by bp_kernels.cu and adjoint.cu.
 #pragma once
 
+#include <type_traits>
+
 #include "gbtn_internal.h"
 
 namespace gbtn {
@@ -35,6 +37,74 @@ __device__ __forceinline__ zfloat& operator+=(zfloat& a, zfloat b) {
   a.im += b.im;
   return a;
 }
+// Double-FP32 element ("double-float"): the unevaluated sum hi + lo of two
+// floats, about 48 significant bits, carried on the FP32 pipe.  GB300's FP32
+// pipe issues 64 times the FP64 rate, so the refinement sweeps that need more
+// than FP32 accuracy run in this arithmetic (tensors and messages stay FP64 in
+// HBM and are split on load; norms and message diffs are formed in FP64).
+// The operations are the error-free transformations of Knuth (TwoSum) and
+// Dekker (1971) / Ogita, Rump & Oishi (2005) (the product error from one FMA):
+//   mac(a, b, c): p = a.hi b.hi exactly split into p + e by an FMA, the cross
+//   terms a.hi b.lo + a.lo b.hi folded into e, then TwoSum(c.hi, p) with the
+//   low parts summed into the error word.  mac leaves (hi, lo) unnormalised
+//   (|lo| may exceed half an ulp of hi); settle() renormalises with a
+//   FastTwoSum before a value is stored or reused as an operand.
+struct __align__(8) df32 {
+  float hi, lo;
+  df32() = default;
+  __host__ __device__ constexpr df32(float h, float l = 0.f) : hi(h), lo(l) {}
+};
+
+__device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ df32 settle(df32 a) {
+  const float s = __fadd_rn(a.hi, a.lo);
+  return df32(s, __fsub_rn(a.lo, __fsub_rn(s, a.hi)));
+}
+__device__ __forceinline__ df32 operator+(df32 a, df32 b) {
+  float s, e;
+  df_two_sum(a.hi, b.hi, s, e);
+  return settle(df32(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo))));
+}
+__device__ __forceinline__ df32& operator+=(df32& a, df32 b) {
+  a = a + b;
+  return a;
+}
+__device__ __forceinline__ df32 mac(df32 a, df32 b, df32 c) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  float s, t;
+  df_two_sum(c.hi, p, s, t);
+  return df32(s, __fadd_rn(__fadd_rn(t, e), c.lo));
+}
+__device__ __forceinline__ df32 conj_of(df32 x) { return x; }
+__device__ __forceinline__ df32 shfl_xor(df32 v, int o) {
+  return df32(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
+}
+__device__ __forceinline__ df32 df_from_double(double x) {
+  const float h = __double2float_rn(x);
+  return df32(h, __double2float_rn(x - (double)h));
+}
+__device__ __forceinline__ double df_to_double(df32 a) { return (double)a.hi + (double)a.lo; }
+
+// Storage element -> arithmetic element (identity unless the arithmetic is df32).
+template <typename T, typename S>
+__device__ __forceinline__ T to_elem(S x) {
+  if constexpr (std::is_same<T, df32>::value)
+    return df_from_double(x);
+  else
+    return x;
+}
+template <typename T>
+__device__ __forceinline__ T settle(T x) {
+  return x;
+}
+
 // multiply-accumulate a * b + c
 __device__ __forceinline__ float mac(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double mac(double a, double b, double c) { return fma(a, b, c); }
@@ -105,7 +175,7 @@ __device__ __forceinline__ void absorb_fibers(const T* __restrict__ in, T* __res
       T y = T(0);
 #pragma unroll
       for (int a = 0; a < CHI; ++a) y = mac(m[b][a], x[a], y);
-      out[base + b * st] = y;
+      out[base + b * st] = settle(y);
     }
   }
 }
@@ -287,6 +357,34 @@ __device__ __forceinline__ double finalize_message<zfloat>(const zfloat* res, in
   return diff;
 }
 
+// Double-FP32 arithmetic with FP64 storage: the result is formed in FP64
+// (hi + lo), normalised and compared with the old FP64 message in FP64.
+__device__ __forceinline__ double finalize_message_df(const df32* res, int chi, const double* old, double* out,
+                                                      int normalize, bool want_diff, int lane) {
+  const int P = chi * chi;
+  const double v0 = lane < P ? df_to_double(res[lane]) : 0.0;
+  const double v1 = lane + 32 < P ? df_to_double(res[lane + 32]) : 0.0;
+  const double nrm2 = warp_sum(v0 * v0 + v1 * v1);
+  const double sc = (normalize && nrm2 > 0.0) ? 1.0 / sqrt(nrm2) : 1.0;
+  const double n0 = v0 * sc, n1 = v1 * sc;
+  double o0 = 0.0, o1 = 0.0;
+  if (want_diff) {
+    if (lane < P) o0 = old[lane];
+    if (lane + 32 < P) o1 = old[lane + 32];
+  }
+  __syncwarp();
+  if (lane < P) out[lane] = n0;
+  if (lane + 32 < P) out[lane + 32] = n1;
+  double diff = 0.0;
+  if (want_diff) {
+    const double dot = warp_sum(n0 * o0 + n1 * o1);
+    const double na = warp_sum(n0 * n0 + n1 * n1);
+    const double nb = warp_sum(o0 * o0 + o1 * o1);
+    diff = 1.0 - (dot * dot) / (na * nb);
+  }
+  return diff;
+}
+
 // Shared-memory carve-up of one team.
 template <typename T>
 struct TeamSmem {
@@ -338,21 +436,22 @@ __device__ __forceinline__ void load_desc(VDesc* dst, const VDesc* src, int tid)
 
 // Load the tensor (and bra) of a vertex and its incoming messages (all legs,
 // or all but skip_leg) into shared memory.
-template <typename T, int TEAM>
-__device__ __forceinline__ void load_vertex(const TeamSmem<T>& S, const T* fac, const T* bra_g, const T* msgs,
+// S is the storage type in HBM (T, or double under df32 arithmetic).
+template <typename T, int TEAM, typename S = T>
+__device__ __forceinline__ void load_vertex(const TeamSmem<T>& Sm, const S* fac, const S* bra_g, const S* msgs,
                                             const long long* msg_off, int skip_leg, int tid) {
-  const VDesc& d = *S.desc;
-  const T* a = fac + d.a_off;
-  for (int i = tid; i < d.n; i += TEAM) S.buf[0][i] = a[i];
+  const VDesc& d = *Sm.desc;
+  const S* a = fac + d.a_off;
+  for (int i = tid; i < d.n; i += TEAM) Sm.buf[0][i] = to_elem<T>(a[i]);
   if (bra_g) {
-    const T* b = bra_g + d.a_off;
-    for (int i = tid; i < d.n; i += TEAM) S.bra[i] = b[i];
+    const S* b = bra_g + d.a_off;
+    for (int i = tid; i < d.n; i += TEAM) Sm.bra[i] = to_elem<T>(b[i]);
   }
   for (int p = 0; p < d.k; ++p) {
     if (p == skip_leg) continue;
     const int c2 = d.chi[p] * d.chi[p];
-    const T* m = msgs + msg_off[d.in_de[p]];
-    for (int i = tid; i < c2; i += TEAM) S.msg[p * 64 + i] = m[i];
+    const S* m = msgs + msg_off[d.in_de[p]];
+    for (int i = tid; i < c2; i += TEAM) Sm.msg[p * 64 + i] = to_elem<T>(m[i]);
   }
 }
 

@@ -86,22 +86,24 @@ void upload_schedules(const DeviceSched& s) { GBTN_CUDA(cudaMemcpyToSymbol(c_sch
 // outgoing messages from msg_in into msg_out.
 // ---------------------------------------------------------------------------
 
-template <typename T, int TEAM>
+// T is the arithmetic, S the storage in HBM (S = T, or double for the
+// double-FP32 refinement sweeps, whose tensors and messages stay FP64).
+template <typename T, int TEAM, typename S = T>
 __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
     bp_vertex_kernel(const int* __restrict__ work, int nwork, const VDesc* __restrict__ vd,
-                     const T* __restrict__ fac, const T* __restrict__ bra_g, const T* msg_in, T* msg_out,
+                     const S* __restrict__ fac, const S* __restrict__ bra_g, const S* msg_in, S* msg_out,
                      const long long* __restrict__ msg_off, double* diffs, const int* converged,
                      int normalize, int want_diff, int ncap, int nbuf) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPB = TEAM == 32 ? 4 : 1;
   const int team = threadIdx.x / TEAM, tid = threadIdx.x % TEAM, lane = tid & 31;
   const size_t tb = team_smem_bytes<T>(ncap, nbuf, bra_g != nullptr, TEAM);
-  TeamSmem<T> S = carve<T>(smem_raw + team * tb, ncap, nbuf, bra_g != nullptr, TEAM);
+  TeamSmem<T> Sm = carve<T>(smem_raw + team * tb, ncap, nbuf, bra_g != nullptr, TEAM);
   for (int w = blockIdx.x * TPB + team; w < nwork; w += gridDim.x * TPB) {
     const int v = work[w];
-    load_desc<TEAM>(S.desc, vd + v, tid);
+    load_desc<TEAM>(Sm.desc, vd + v, tid);
     tsync<TEAM>();
-    const VDesc& d = *S.desc;
+    const VDesc& d = *Sm.desc;
     if (converged && converged[d.net]) {
       if (msg_in != msg_out) {
         for (int p = 0; p < d.k; ++p) {
@@ -113,7 +115,7 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
       tsync<TEAM>();
       continue;
     }
-    load_vertex<T, TEAM>(S, fac, bra_g, msg_in, msg_off, -1, tid);
+    load_vertex<T, TEAM, S>(Sm, fac, bra_g, msg_in, msg_off, -1, tid);
     tsync<TEAM>();
     const int k = d.k;
     const int len = c_sched.len[k];
@@ -122,15 +124,18 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
       const int leg = op.leg;
       const int chi = d.chi[leg], st = d.st[leg];
       if (op.type == 0) {
-        absorb_any<T>(chi, S.buf[op.src], S.buf[op.dst], d.n, st, S.msg + leg * 64, tid, TEAM);
+        absorb_any<T>(chi, Sm.buf[op.src], Sm.buf[op.dst], d.n, st, Sm.msg + leg * 64, tid, TEAM);
         tsync<TEAM>();
       } else {
-        close_any<T, TEAM>(chi, S.buf[op.src], S.bra, d.n, st, 1, 0, 0, S.red, S.res, tid);
+        close_any<T, TEAM>(chi, Sm.buf[op.src], Sm.bra, d.n, st, 1, 0, 0, Sm.red, Sm.res, tid);
         if (tid < 32) {
           const int de = d.out_de[leg];
           const long long off = msg_off[de];
-          const double df = finalize_message<T>(S.res, chi, msg_in + off, msg_out + off, normalize,
-                                                want_diff != 0, lane);
+          double df;
+          if constexpr (std::is_same<T, df32>::value)
+            df = finalize_message_df(Sm.res, chi, msg_in + off, msg_out + off, normalize, want_diff != 0, lane);
+          else
+            df = finalize_message<T>(Sm.res, chi, msg_in + off, msg_out + off, normalize, want_diff != 0, lane);
           if (want_diff && lane == 0) diffs[de] = df;
         }
         tsync<TEAM>();
@@ -643,6 +648,28 @@ void launch_bp_vertices(const WorkList& wl, const VDesc* vd, const T* fac, const
   } else {
     const size_t sm = team_smem_bytes<T>(wl.ncap, nbuf, bra != nullptr, 256);
     auto kern = bp_vertex_kernel<T, 256>;
+    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    kern<<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
+                                   normalize, want_diff, wl.ncap, nbuf);
+  }
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_bp_vertices_df32(const WorkList& wl, const VDesc* vd, const double* fac, const double* bra,
+                             const double* msg_in, double* msg_out, const long long* msg_off, double* diffs,
+                             const int* converged, int normalize, int want_diff, cudaStream_t s) {
+  if (wl.count == 0) return;
+  const int nbuf = wl.maxdeg <= 4 ? 3 : kNumBufs;
+  if (wl.team == 32) {
+    const size_t sm = 4 * team_smem_bytes<df32>(wl.ncap, nbuf, bra != nullptr, 32);
+    auto kern = bp_vertex_kernel<df32, 32, double>;
+    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const int blocks = (wl.count + 3) / 4;
+    kern<<<blocks, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
+                                 normalize, want_diff, wl.ncap, nbuf);
+  } else {
+    const size_t sm = team_smem_bytes<df32>(wl.ncap, nbuf, bra != nullptr, 256);
+    auto kern = bp_vertex_kernel<df32, 256, double>;
     GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     kern<<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
                                    normalize, want_diff, wl.ncap, nbuf);

@@ -117,6 +117,11 @@ void launch_bp_vertices(const WorkList& wl, const VDesc* vd, const T* fac, const
                         const T* msg_in, T* msg_out, const long long* msg_off, double* diffs,
                         const int* converged, int normalize, int want_diff, cudaStream_t s);
 
+// Double-FP32 arithmetic (bp_device.cuh, df32) on FP64 tensors and messages.
+void launch_bp_vertices_df32(const WorkList& wl, const VDesc* vd, const double* fac, const double* bra,
+                             const double* msg_in, double* msg_out, const long long* msg_off, double* diffs,
+                             const int* converged, int normalize, int want_diff, cudaStream_t s);
+
 template <typename T>
 void launch_bp_sequential(int n_networks, const VDesc* vd, const int2* seq, const int* seq_ptr,
                           const T* fac, const T* bra, T* msgs, const long long* msg_off,

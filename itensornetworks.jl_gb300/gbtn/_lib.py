@@ -23,10 +23,11 @@ ERRORS = {
     6: "GBTN_ERR_NOMEM",
 }
 HOST, DEVICE = 0, 1
-KCLASS_TENSOR_CORE, KCLASS_SIMT_F32, KCLASS_SIMT_F64, KCLASS_GAUGE = 0, 1, 2, 3
+KCLASS_TENSOR_CORE, KCLASS_SIMT_F32, KCLASS_SIMT_F64, KCLASS_GAUGE, KCLASS_SIMT_DF32 = 0, 1, 2, 3, 4
 TC_POLICIES = {"auto": 0, "all": 1, "native": 2, "off": 3}
 SCHED = {"sequential": 0, "parallel": 1, "colored": 2}
-PRECISION = {"f64": 0, "f32": 1, "bf16": 2, "mixed": 3}
+PRECISION = {"f64": 0, "f32": 1, "bf16": 2, "mixed": 3, "df32": 4}
+REFINE = {"df32": 0, "f64": 1}
 INIT = {"identity": 0, "ones": 1}
 
 
@@ -82,6 +83,8 @@ class BPOpts(C.Structure):
         ("maxiter_bf16", C.c_int32),
         ("maxiter_f32", C.c_int32),
         ("refine_f64", C.c_int32),
+        ("refine", C.c_int32),
+        ("confirm_f64", C.c_int32),
     ]
 
 
@@ -123,6 +126,7 @@ SIGNATURES = {
     "gbtn_get_edge_diffs": (_I, [_P, _P, _I]),
     "gbtn_init_messages": (_I, [_P, _I]),
     "gbtn_bp_run": (_I, [_P, C.POINTER(BPOpts), _I32, _D]),
+    "gbtn_plan_phase_sweeps": (_I, [_P, _I32]),
     "gbtn_updated_message": (_I, [_P, C.c_int32, _D]),
     "gbtn_vertex_rdms": (_I, [_P, _D]),
     "gbtn_expect1": (_I, [_P, _D, _I, _D]),

@@ -172,6 +172,8 @@ class BeliefPropagationCache:
         o.maxiter_bf16 = int(mixed.get("maxiter_bf16", 0))
         o.maxiter_f32 = int(mixed.get("maxiter_f32", 0))
         o.refine_f64 = int(mixed.get("refine_f64", 0))
+        o.refine = _lib.REFINE[mixed.get("refine", "df32")]
+        o.confirm_f64 = int(mixed.get("confirm_f64", 0))
         it = np.zeros(self.tn.n_networks, dtype=np.int32)
         md = np.zeros(self.tn.n_networks)
         self._c(self.lib.gbtn_bp_run(self.handle, C.byref(o), iptr(it), dptr(md)))
@@ -181,6 +183,13 @@ class BeliefPropagationCache:
                 if tol is not None and md[n] <= tol:
                     print(f"BP converged to desired precision after {it[n]} iterations.")
         return self
+
+    def phase_sweeps(self):
+        """Sweeps of each phase of the last update (most over the networks):
+        {"bf16", "f32", "refine", "f64"}; 0 for a phase that did not run."""
+        out = np.zeros(4, dtype=np.int32)
+        self._c(self.lib.gbtn_plan_phase_sweeps(self.handle, iptr(out)))
+        return dict(zip(("bf16", "f32", "refine", "f64"), (int(x) for x in out)))
 
     def set_tc_policy(self, policy):
         """Tensor-core routing of the BF16 phase: "auto" (timed on this plan's

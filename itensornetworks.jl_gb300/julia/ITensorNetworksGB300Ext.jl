@@ -70,6 +70,8 @@ struct BPOpts
     maxiter_bf16::Int32
     maxiter_f32::Int32
     refine_f64::Int32
+    refine::Int32       # 0: double-FP32 refinement (default), 1: FP64
+    confirm_f64::Int32  # FP64 sweeps after a double-FP32 refinement
 end
 
 function check(ctx, code)
@@ -165,11 +167,11 @@ function ITensorNetworks.update(alg::Algorithm"gb300_bp", bpc::BeliefPropagation
                 end
             end
             single = real(p.elt) === Float32
-            prec = Dict("f64" => 0, "f32" => 1, "bf16" => 2, "mixed" => 3)[get(alg.kwargs, :precision,
-                single ? "f32" : "f64")]
+            prec = Dict("f64" => 0, "f32" => 1, "bf16" => 2, "mixed" => 3, "df32" => 4)[get(alg.kwargs,
+                :precision, single ? "f32" : "f64")]
             tol = something(get(alg.kwargs, :tol, nothing), -1.0)
             opts = BPOpts(sched, prec, maxiter, 1, tol, isempty(seq) ? C_NULL : pointer(seq), length(seq),
-                0.0, 0.0, 0, 0, 0)
+                0.0, 0.0, 0, 0, 0, 0, 0)
             iters = Ref{Int32}(0)
             diff = Ref{Float64}(0.0)
             GC.@preserve seq check(ctx, ccall((:gbtn_bp_run, libgbtn), Cint,
@@ -391,7 +393,7 @@ function energy_and_grad(psi, ops, coefs; maxiter=500, want_grad=true)
         try
             check(ctx, ccall((:gbtn_set_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Cint),
                 plan[], p.data, C_NULL, 0))
-            opts = BPOpts(1, 3, maxiter, 1, 1e-14, C_NULL, 0, 0.0, 0.0, 0, 0, 0)
+            opts = BPOpts(1, 3, maxiter, 1, 1e-14, C_NULL, 0, 0.0, 0.0, 0, 0, 0, 0, 0)
             check(ctx, ccall((:gbtn_bp_run, libgbtn), Cint, (Ptr{Cvoid}, Ref{BPOpts}, Ptr{Int32}, Ptr{Float64}),
                 plan[], opts, C_NULL, C_NULL))
             E = Ref{Float64}(0.0)

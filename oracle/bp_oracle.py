@@ -826,3 +826,61 @@ def kron2(a, b):
     """Two-site operator with row index s'_u + du*s'_v: O = b (x) a in numpy's
     kron (first-site index fastest)."""
     return np.kron(b, a)
+
+
+# ----------------------------------------------------------------------------
+# Rounding model of the BF16 tensor-core message update
+# ----------------------------------------------------------------------------
+
+def bf16_round(x):
+    """Round float64 (or float32) values to the nearest bfloat16 (8 significant
+    bits, ties to even), returned as float64.  Exact for the normal range."""
+    x = np.asarray(x, dtype=np.float64)
+    m, e = np.frexp(x)  # x = m 2^e, 0.5 <= |m| < 1
+    return np.ldexp(np.rint(m * 256.0) / 256.0, e)
+
+
+def tc_bf16_messages(g, A, msgs, v):
+    """Outgoing messages of vertex v as the BF16 tensor-core sweep computes
+    them (d = 2, degree <= 4, chi <= 8; real tensors, bra = ket): the same
+    contraction as :func:`updated_message`, evaluated through the kernel's two
+    pairs of two-leg environments with BF16 roundings at the kernel's points --
+    site tensor rounded to BF16; incoming messages stored as FP32; Kronecker
+    products of two messages formed in FP32 and rounded to BF16; the
+    half-contracted tensors T12 / T34 rounded to BF16 before the second
+    product.  Sums are taken in float64 (the kernel accumulates in FP32), so
+    the result differs from the kernel's by FP32 accumulation error and the
+    rare BF16 rounding it flips.  Returns {directed edge: normalised chi x chi
+    message}."""
+    k = len(g.legs[v])
+    assert k <= 4 and g.site_dims[v] == 2
+    shape = list(A[v].shape) + [1] * (4 - k)
+    Z = bf16_round(np.asarray(A[v], dtype=np.float64).reshape(shape, order="F"))
+    M = []
+    for p in range(4):
+        if p < k:
+            e = g.legs[v][p]
+            M.append(np.asarray(msgs[g.directed(e, g.other(v, e))], dtype=np.float32))
+        else:
+            M.append(np.ones((1, 1), dtype=np.float32))
+
+    def kron(Ma, Mb):  # K[b_a, b_b, a_a, a_b] = bf16(fp32(Ma[b_a, a_a] * Mb[b_b, a_b]))
+        prod = Ma[:, None, :, None] * Mb[None, :, None, :]  # float32 products
+        return bf16_round(prod.astype(np.float32))
+
+    K12, K34 = kron(M[0], M[1]), kron(M[2], M[3])
+    T12 = bf16_round(np.einsum("sxyzw,bcxy->szwbc", Z, K12))
+    T34 = bf16_round(np.einsum("sxyzw,uvzw->sxyuv", Z, K34))
+    G34 = np.einsum("szwbc,sbcuv->zwuv", T12, Z)  # [a3, a4, b3, b4]
+    G12 = np.einsum("sxyuv,sbcuv->xybc", T34, Z)  # [a1, a2, b1, b2]
+    M64 = [m.astype(np.float64) for m in M]
+    outs = [np.einsum("xybc,cy->bx", G12, M64[1]),   # leg 0: [b1, a1]
+            np.einsum("xybc,bx->cy", G12, M64[0]),   # leg 1: [b2, a2]
+            np.einsum("zwuv,vw->uz", G34, M64[3]),   # leg 2: [b3, a3]
+            np.einsum("zwuv,uz->vw", G34, M64[2])]   # leg 3: [b4, a4]
+    res = {}
+    for p in range(k):
+        m = outs[p]
+        nrm = np.linalg.norm(m)
+        res[g.directed(g.legs[v][p], v)] = m / nrm if nrm != 0 else m
+    return res

@@ -2,12 +2,16 @@
 
 Tolerances: one BF16 sweep from the same input messages agrees with the FP64
 sweep to 3e-2 absolute on unit-norm messages (BF16 keeps 8 significant bits;
-a layout or descriptor error shows up as O(0.1-1) differences); messages of
+a layout or descriptor error shows up as O(0.1-1) differences; the tighter
+check against the oracle's BF16 rounding model is in
+test_gpu_oracle_configs.py); messages of
 vertices outside the tensor-core class run FP32 and agree to 1e-5.  Vertices
 padded to the kernel's shape (boundary legs, bond dimensions below 8, leaves)
 meet the same 3e-2 and keep their compact shapes.  The mixed
 pipeline (BF16 -> FP32 -> FP64) meets <= 1e-6 max relative error in <Sz>
 after two FP64 sweeps and 1e-10 after a full FP64 phase."""
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -72,10 +76,12 @@ def test_bf16_colored_schedule_matches_fp64():
 
 
 def test_mixed_pipeline_accuracy_on_32x32_chi8():
-    # the target shape: 32x32, d=2, chi=8, N(0,1) tensors
+    # the target shape: 32x32, d=2, chi=8, N(0,1) tensors (seed 11); the
+    # reference <Sz> is the oracle's converged fixed point (C restatement of
+    # the reference's sweep, tests/golden/make_large_fixtures.py)
     tn, g, A = pair(32, 11)
-    ref = gbtn.BeliefPropagationCache(tn).update(maxiter=300, schedule="parallel", precision="f64")
-    sz_ref = ref.expect(O.SZ)
+    fx = np.load(Path(__file__).resolve().parent / "golden" / "peps32x32_chi8_batch16.npz")
+    sz_ref = fx["sz"][11 * 1024:12 * 1024]
     scale = np.max(np.abs(sz_ref))
     b16 = gbtn.BeliefPropagationCache(tn).update(maxiter=300, tol=1e-7, schedule="parallel", precision="bf16")
     err16 = np.max(np.abs(b16.expect(O.SZ) - sz_ref)) / scale

@@ -65,11 +65,28 @@ def test_flat_roundtrip():
     np.testing.assert_array_equal(tn.flat_messages(tn.unflat_messages(tn.flat_messages(msgs))), tn.flat_messages(msgs))
 
 
-def test_struct_layouts():
-    # GraphDesc: 2 ints, 6 pointers, 1 pointer, 3 ints + padding (x86-64 / aarch64 LP64)
-    assert C.sizeof(_lib.GraphDesc) == 8 + 7 * 8 + 12 + 4
-    assert _lib.GraphDesc.complex_values.offset == 8 + 7 * 8 + 8
-    assert C.sizeof(_lib.BPOpts) == 16 + 8 + 8 + 8 + 8 + 8 + 16
+def test_struct_layouts(tmp_path):
+    """The ctypes mirrors of the ABI structs have the C compiler's sizes and
+    field offsets (a C program compiled against include/gbtn.h prints them)."""
+    structs = {"gbtn_graph_desc": _lib.GraphDesc, "gbtn_bp_opts": _lib.BPOpts, "gbtn_grad_opts": _lib.GradOpts}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbtn.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("  return 0;\n}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", str(_lib.INCLUDE), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        a, b, c = ln.split()
+        got[(a, b)] = int(c)
+    for cname, cls in structs.items():
+        assert got[(cname, "size")] == C.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
 
 
 def test_library_builds_and_exports_every_declared_symbol(lib_built):
@@ -80,7 +97,7 @@ def test_library_builds_and_exports_every_declared_symbol(lib_built):
     missing = [s for s in declared if s not in exported]
     assert not missing, missing
     lib = _lib.load()
-    assert lib.gbtn_abi_version() == 1
+    assert lib.gbtn_abi_version() == 2
     assert set(_lib.SIGNATURES) == set(declared)
 
 
