@@ -150,7 +150,8 @@ enum gbtn_kernel_class {
   GBTN_KCLASS_SIMT_F32 = 1,
   GBTN_KCLASS_SIMT_F64 = 2,
   GBTN_KCLASS_GAUGE = 3, /* rescale_messages: message normalisation and gauge scaling */
-  GBTN_KCLASS_SIMT_DF32 = 4
+  GBTN_KCLASS_SIMT_DF32 = 4,
+  GBTN_KCLASS_LARGE = 5 /* global-memory path of vertices beyond the shared-memory kernels */
 };
 int gbtn_ctx_set_profiling(gbtn_ctx* ctx, int on);
 /* Failure-detection test of the bounded device waits.  on = 1 makes every

@@ -149,6 +149,23 @@ struct gbtn_plan {
     if (up_copy) cudaStreamDestroy(up_copy);
     if (up_build) cudaStreamDestroy(up_build);
   }
+  // global-memory path (bp_large.cu) for vertices beyond the shared-memory
+  // kernels: per work list (0 = all, 1.. = colour classes), waves of vertices
+  // of one degree whose scratch buffers fit kLargeWaveBytes together
+  struct LargeWave {
+    int k = 0, count = 0, max_tiles = 0, max_chi = 0;
+    long long vstride = 0, scratch_elems = 0;
+    std::vector<int> verts;
+    DevBuf<int> d_verts;
+    DevBuf<long long> d_off;
+  };
+  std::vector<char> is_large;
+  bool has_large = false;
+  std::vector<std::vector<std::unique_ptr<LargeWave>>> large_lists;
+  long long large_scratch_elems = 0, large_partial_elems = 0;
+  DevBuf<double> d_large_scratch, d_large_partial;  // sized in elements of the plan's widest arithmetic
+  DevBuf<int> d_iota;                               // vertex ids 0..nv-1 (single-vertex waves)
+  DevBuf<long long> d_zero_off;                     // scratch offset 0
   // sweeps per phase of the last run (max over networks): BF16, FP32, refinement, FP64
   DevBuf<int> d_phase_iters;  // 4 x nnet
   int phase_fixed[4] = {0, 0, 0, 0};  // sweeps of a phase run without a tolerance (all of its maxiter)
@@ -176,6 +193,14 @@ template <> struct ElemTraits<float> { static constexpr int tag = 1; static cons
 template <> struct ElemTraits<zdouble> { static constexpr int tag = 3; static constexpr int kcls = GBTN_KCLASS_SIMT_F64; };
 template <> struct ElemTraits<zfloat> { static constexpr int tag = 4; static constexpr int kcls = GBTN_KCLASS_SIMT_F32; };
 template <> struct ElemTraits<DF32> { static constexpr int tag = 5; static constexpr int kcls = GBTN_KCLASS_SIMT_DF32; };
+
+// Large-path arithmetic code of (storage T, arithmetic A).
+template <typename T, typename A> struct ArithOf;
+template <> struct ArithOf<double, double> { static constexpr int value = kArithF64; };
+template <> struct ArithOf<float, float> { static constexpr int value = kArithF32; };
+template <> struct ArithOf<double, DF32> { static constexpr int value = kArithDF32; };
+template <> struct ArithOf<zdouble, zdouble> { static constexpr int value = kArithZ64; };
+template <> struct ArithOf<zfloat, zfloat> { static constexpr int value = kArithZ32; };
 
 // One vertex-kernel launch in arithmetic A on storage T (A = T except for DF32).
 template <typename T, typename A>
@@ -250,11 +275,34 @@ void require(bool c, const std::string& m) {
   if (!c) throw InvalidArg(m);
 }
 
-WorkList make_list(gbtn_plan* P, const std::vector<int>& verts, int team,
+WorkList make_list(gbtn_plan* P, const std::vector<int>& verts_in, int team,
                    std::vector<std::unique_ptr<DevBuf<int>>>* store = nullptr) {
+  // size classes: team 32 up to 128, 256, 512, 1024 elements; team 256 up to
+  // 2048, 4096, 8192, 16384, ... (one launch each, shared memory per class)
+  std::vector<int> verts = verts_in;
+  std::stable_sort(verts.begin(), verts.end(), [&](int a, int b) { return P->vd[a].n < P->vd[b].n; });
   WorkList w;
   w.count = (int)verts.size();
   w.team = team;
+  long long bound = team == 32 ? 128 : 2048;
+  for (int i = 0; i < w.count;) {
+    while (P->vd[verts[i]].n > bound) bound *= 2;
+    const bool last = w.nsub == kMaxSub - 1;  // the last class takes every remaining vertex
+    int j = i;
+    int ncap = 0, maxdeg = 0;
+    while (j < w.count && (last || P->vd[verts[j]].n <= bound)) {
+      ncap = std::max(ncap, P->vd[verts[j]].n);
+      maxdeg = std::max(maxdeg, P->vd[verts[j]].k);
+      ++j;
+    }
+    w.sub_begin[w.nsub] = i;
+    w.sub_count[w.nsub] = j - i;
+    w.sub_ncap[w.nsub] = ncap;
+    w.sub_maxdeg[w.nsub] = maxdeg;
+    w.nsub++;
+    i = j;
+    bound *= 2;
+  }
   for (int v : verts) {
     w.ncap = std::max(w.ncap, P->vd[v].n);
     w.maxdeg = std::max(w.maxdeg, P->vd[v].k);
@@ -269,7 +317,10 @@ WorkList make_list(gbtn_plan* P, const std::vector<int>& verts, int team,
 std::pair<WorkList, WorkList> split_list(gbtn_plan* P, const std::vector<int>& verts,
                                          std::vector<std::unique_ptr<DevBuf<int>>>* store = nullptr) {
   std::vector<int> small, large;
-  for (int v : verts) (P->vd[v].n <= kSmallN ? small : large).push_back(v);
+  for (int v : verts) {
+    if (!P->is_large.empty() && P->is_large[v]) continue;  // the global-memory path takes these
+    (P->vd[v].n <= kSmallN ? small : large).push_back(v);
+  }
   return {make_list(P, small, 32, store), make_list(P, large, 256, store)};
 }
 
@@ -383,6 +434,9 @@ void sweep_loop(gbtn_plan* P, int maxiter, const GraphKey& key, F&& sweep, bool 
   }
 }
 
+void run_large(gbtn_plan* P, size_t li, int arith, const void* fac, const void* bra, const void* in, void* out,
+               const int* conv, int normalize, int want_diff, cudaStream_t s);
+
 // Sweeps of the parallel or coloured schedule on storage T in arithmetic A.
 template <typename T, typename A = T>
 void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normalize, T* msg0, T* msg1, const T* fac,
@@ -410,6 +464,10 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
         launch_vertices<T, A>(P->lists[0].second, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
                               normalize, want_diff, s);
       }
+      {
+        KTimer kt(P->ctx, GBTN_KCLASS_LARGE, P->has_large);
+        run_large(P, 0, ArithOf<T, A>::value, fac, bra, in, out, conv, normalize, want_diff, s);
+      }
       cur ^= 1;
     } else {
       for (size_t c = 1; c < P->lists.size(); ++c) {
@@ -418,6 +476,7 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
                               normalize, want_diff, s);
         launch_vertices<T, A>(P->lists[c].second, P->d_vd.p, fac, bra, m, m, P->d_msg_off.p, P->d_diffs.p, conv,
                               normalize, want_diff, s);
+        run_large(P, c, ArithOf<T, A>::value, fac, bra, m, m, conv, normalize, want_diff, s);
       }
     }
     if (want_diff)
@@ -597,6 +656,7 @@ void tune_tc_split(gbtn_plan* P) {
 
 // Does the BF16 sweep run any vertex on the FP32 SIMT kernel?
 bool bf16_has_simt(const gbtn_plan* P) {
+  if (P->has_large) return true;  // large vertices run the FP32 global-memory path
   for (const auto& l : P->rest_lists)
     if (l.first.count > 0 || l.second.count > 0) return true;
   return false;
@@ -629,6 +689,7 @@ void run_sweeps_bf16(gbtn_plan* P, int schedule, int maxiter, double tol, int no
       launch_bp_vertices<float>(P->rest_lists[li].second, P->d_vd.p, fac, nullptr, in, out, P->d_msg_off.p,
                                 P->d_diffs.p, conv, normalize, want_diff, s);
     }
+    run_large(P, li, kArithF32, fac, nullptr, in, out, conv, normalize, want_diff, s);
   };
   const GraphKey key{2, schedule, normalize, want_diff ? 1 : 0, stall, c32, P->list_version, tol};
   sweep_loop(P, maxiter, key, [&] {
@@ -665,18 +726,256 @@ void record_phase(gbtn_plan* P, int slot) {
                             cudaMemcpyDeviceToDevice, P->ctx->stream));
 }
 
+constexpr long long kLargeWaveBytes = 1LL << 30;  // scratch of one wave of large vertices
+
+// Tiles and partial-sum elements of the fibers of one leg (p < 0: the site index).
+void large_leg_cost(const VDesc& d, int p, int& tiles, long long& partial) {
+  const int chi = p >= 0 ? d.chi[p] : d.d, st = p >= 0 ? d.st[p] : 1;
+  const LegTiling g = leg_tiling(d.n, st, chi);
+  tiles = g.ntl * g.ntj;
+  partial = (long long)tiles * chi * chi;
+}
+
+// Scratch buffers of a large vertex: the schedule's, and at least two for the
+// absorb chains of environments, updated_message and the sequential schedule.
+int large_nbuf(const gbtn_ctx* C, int k) { return std::max(C->sched.nbuf[k], 3) - 1; }
+
+// Waves of the large vertices among `verts`, grouped by degree.
+std::vector<std::unique_ptr<gbtn_plan::LargeWave>> build_large_waves(gbtn_plan* P, const std::vector<int>& verts) {
+  std::vector<std::unique_ptr<gbtn_plan::LargeWave>> out;
+  const long long elt = P->cplx ? 16 : 8;
+  for (int k = 0; k <= kMaxDeg; ++k) {
+    std::unique_ptr<gbtn_plan::LargeWave> w;
+    long long bytes = 0;
+    auto flush = [&] {
+      if (!w || w->count == 0) return;
+      std::vector<long long> off;
+      long long o = 0;
+      for (int v : w->verts) {
+        off.push_back(o);
+        o += (long long)large_nbuf(P->ctx, k) * P->vd[v].n;
+      }
+      w->scratch_elems = o;
+      w->d_verts.upload(w->verts, P->ctx->stream);
+      w->d_off.upload(off, P->ctx->stream);
+      P->large_scratch_elems = std::max(P->large_scratch_elems, o);
+      P->large_partial_elems = std::max(P->large_partial_elems, w->vstride * w->count);
+      out.push_back(std::move(w));
+    };
+    for (int v : verts) {
+      if (!P->is_large[v] || P->vd[v].k != k) continue;
+      const VDesc& d = P->vd[v];
+      int mt = 0, mc = 0;
+      long long vs = 0;
+      for (int p = -1; p < d.k; ++p) {
+        int t;
+        long long pe;
+        large_leg_cost(d, p, t, pe);
+        mt = std::max(mt, t);
+        vs = std::max(vs, pe);
+        if (p >= 0) mc = std::max(mc, d.chi[p]);
+      }
+      const long long need = ((long long)large_nbuf(P->ctx, k) * d.n + vs) * elt;
+      if (w && (bytes + need > kLargeWaveBytes || w->count >= 65535)) {
+        flush();
+        w.reset();
+        bytes = 0;
+      }
+      if (!w) {
+        w = std::make_unique<gbtn_plan::LargeWave>();
+        w->k = k;
+      }
+      w->verts.push_back(v);
+      w->count++;
+      w->max_tiles = std::max(w->max_tiles, mt);
+      w->max_chi = std::max(w->max_chi, mc);
+      w->vstride = std::max(w->vstride, vs);
+      bytes += need;
+    }
+    flush();
+  }
+  return out;
+}
+
+// Scratch and partial sums of one vertex processed alone (updated_message and
+// the sequential schedule of plans with large vertices take any vertex).
+void reserve_single_vertex(gbtn_plan* P) {
+  for (int v = 0; v < P->nv; ++v) {
+    const VDesc& d = P->vd[v];
+    long long vs = 0;
+    for (int p = -1; p < d.k; ++p) {
+      int t;
+      long long pe;
+      large_leg_cost(d, p, t, pe);
+      vs = std::max(vs, pe);
+    }
+    P->large_scratch_elems = std::max(P->large_scratch_elems, (long long)large_nbuf(P->ctx, d.k) * d.n);
+    P->large_partial_elems = std::max(P->large_partial_elems, vs);
+  }
+}
+
+void ensure_large_bufs(gbtn_plan* P) {
+  const size_t dbl = P->cplx ? 2 : 1;  // doubles per element of the widest arithmetic
+  if (!P->d_large_scratch.p && P->large_scratch_elems > 0) P->d_large_scratch.alloc(dbl * P->large_scratch_elems);
+  if (!P->d_large_partial.p && P->large_partial_elems > 0) P->d_large_partial.alloc(dbl * P->large_partial_elems);
+}
+
+LargeArgs<double> large_args(const gbtn_plan::LargeWave& w, const gbtn_plan* P, const void* fac, const void* bra,
+                             const void* msgs) {
+  LargeArgs<double> a;
+  a.verts = w.d_verts.p;
+  a.buf_off = w.d_off.p;
+  a.vd = P->d_vd.p;
+  a.fac = static_cast<const double*>(fac);
+  a.bra = static_cast<const double*>(bra);
+  a.msgs = static_cast<const double*>(msgs);
+  a.msg_off = P->d_msg_off.p;
+  return a;
+}
+
+// Every outgoing message of the large vertices of work list li, in arithmetic
+// `arith` (storage: double, float, zdouble or zfloat arrays).
+void run_large(gbtn_plan* P, size_t li, int arith, const void* fac, const void* bra, const void* in, void* out,
+               const int* conv, int normalize, int want_diff, cudaStream_t s) {
+  if (!P->has_large || li >= P->large_lists.size()) return;
+  ensure_large_bufs(P);
+  for (const auto& w : P->large_lists[li]) {
+    const LargeArgs<double> a = large_args(*w, P, fac, bra, in);
+    const int len = P->ctx->sched.len[w->k];
+    for (int i = 0; i < len; ++i)
+      launch_large_op_any(arith, a, w->count, w->max_tiles, w->max_chi, P->ctx->sched.ops[w->k][i],
+                          P->d_large_scratch.p, P->d_large_partial.p, w->vstride, in, out, P->d_diffs.p, conv,
+                          normalize, want_diff, s);
+  }
+}
+
+// The absorb chain of every leg but `skip` (ping-pong between scratch buffers
+// 1 and 2, from the site tensor); returns the buffer holding the result.
+int large_chain(const VDesc& d, int skip, std::vector<SchedOp>& ops) {
+  int cur = 0;
+  for (int p = 0; p < d.k; ++p) {
+    if (p == skip) continue;
+    const int nxt = cur == 1 ? 2 : 1;
+    ops.push_back({0, (int8_t)cur, (int8_t)nxt, (int8_t)p});
+    cur = nxt;
+  }
+  return cur;
+}
+
+// One-site RDMs of the large vertices (FP64 or complex FP64).
+void large_rdms(gbtn_plan* P, const double* fac, const double* bra, const double* msgs, double* rdm) {
+  if (!P->has_large) return;
+  ensure_large_bufs(P);
+  cudaStream_t s = P->ctx->stream;
+  const int arith = P->cplx ? kArithZ64 : kArithF64;
+  for (const auto& w : P->large_lists[0]) {
+    const LargeArgs<double> a = large_args(*w, P, fac, bra, msgs);
+    std::vector<SchedOp> ops;
+    const int src = large_chain(P->vd[w->verts[0]], -1, ops);
+    for (const SchedOp& op : ops)
+      launch_large_op_any(arith, a, w->count, w->max_tiles, w->max_chi, op, P->d_large_scratch.p,
+                          P->d_large_partial.p, w->vstride, msgs, nullptr, nullptr, nullptr, 0, 0, s);
+    launch_large_rdm_any(arith, a, w->count, w->max_tiles, src, P->d_large_scratch.p, P->d_large_partial.p,
+                         w->vstride, rdm, P->d_rdm_off.p, s);
+  }
+}
+
+// One message of a vertex through the global-memory path: the absorb chain of
+// every other leg, CLOSE on `leg`, normalised into out + msg_off[out_de]
+// (message_diff into diffs when want_diff).  Used for single messages of large
+// vertices and by the sequential schedule of plans that hold large vertices.
+void large_one_message(gbtn_plan* P, int arith, int v, int leg, const void* fac, const void* bra, const void* msgs,
+                       void* out, int normalize, int want_diff, cudaStream_t s) {
+  ensure_large_bufs(P);
+  const VDesc& d = P->vd[v];
+  gbtn_plan::LargeWave w;
+  w.count = 1;
+  for (int p = -1; p < d.k; ++p) {
+    int t;
+    long long pe;
+    large_leg_cost(d, p, t, pe);
+    w.max_tiles = std::max(w.max_tiles, t);
+    w.vstride = std::max(w.vstride, pe);
+    if (p >= 0) w.max_chi = std::max(w.max_chi, d.chi[p]);
+  }
+  LargeArgs<double> a = large_args(w, P, fac, bra, msgs);
+  a.verts = P->d_iota.p + v;
+  a.buf_off = P->d_zero_off.p;
+  std::vector<SchedOp> ops;
+  const int src = large_chain(d, leg, ops);
+  ops.push_back({1, (int8_t)src, 0, (int8_t)leg});
+  for (const SchedOp& op : ops)
+    launch_large_op_any(arith, a, 1, w.max_tiles, w.max_chi, op, P->d_large_scratch.p, P->d_large_partial.p,
+                        w.vstride, msgs, out, P->d_diffs.p, nullptr, normalize, want_diff, s);
+}
+
+// The sequential schedule of a plan that holds large vertices: every message
+// of the sequence in order through the global-memory path (one vertex at a
+// time, each update seeing every earlier one, in place), FP64 or FP32 (complex
+// ones too); per sweep the mean diff of each network's sequence is tested on
+// the host (abstractbeliefpropagationcache.jl:272-287, 313-329).  Latency-bound:
+// a few launches per message.
+void run_sequential_large(gbtn_plan* P, const gbtn_bp_opts* o, const std::vector<std::vector<int2>>& per,
+                          int32_t* iters, double* mean_diff) {
+  cudaStream_t s = P->ctx->stream;
+  const bool want_diff = o->tol >= 0.0;
+  const bool f32 = o->precision == GBTN_F32;
+  const int arith = P->cplx ? (f32 ? kArithZ32 : kArithZ64) : (f32 ? kArithF32 : kArithF64);
+  const void* fac = P->d_fac.p;
+  const void* bra = P->sep_bra ? P->d_bra.p : nullptr;
+  void* msgs = P->d_msg[P->cur].p;
+  if (f32) {
+    ensure_f32(P);
+    launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->es() * P->n_msg, s);
+    fac = P->d_fac32.p;
+    bra = P->sep_bra ? P->d_bra32.p : nullptr;
+    msgs = P->d_msg32[0].p;
+  }
+  std::vector<int> it(P->nnet, 0);
+  std::vector<double> md(P->nnet, NAN);
+  std::vector<char> done(P->nnet, 0);
+  std::vector<double> diffs(2 * (size_t)P->ne);
+  for (int sweep = 1; sweep <= o->maxiter; ++sweep) {
+    bool any = false;
+    for (int n = 0; n < P->nnet; ++n) {
+      if (done[n]) continue;
+      any = true;
+      for (const int2& e : per[n]) large_one_message(P, arith, e.x, e.y, fac, bra, msgs, msgs, o->normalize,
+                                                     want_diff ? 1 : 0, s);
+      it[n] = sweep;
+    }
+    if (!any) break;
+    if (!want_diff) continue;
+    GBTN_CUDA(cudaMemcpyAsync(diffs.data(), P->d_diffs.p, sizeof(double) * diffs.size(), cudaMemcpyDeviceToHost, s));
+    GBTN_CUDA(cudaStreamSynchronize(s));
+    for (int n = 0; n < P->nnet; ++n) {
+      if (done[n]) continue;
+      double sum = 0.0;
+      for (const int2& e : per[n]) sum += diffs[P->vd[e.x].out_de[e.y]];
+      md[n] = sum / (double)per[n].size();
+      if (md[n] <= o->tol) done[n] = 1;
+    }
+  }
+  if (f32) launch_convert_f32_to_f64(P->d_msg32[0].p, P->d_msg[P->cur].p, P->es() * P->n_msg, s);
+  GBTN_CUDA(cudaStreamSynchronize(s));
+  if (iters) std::copy(it.begin(), it.end(), iters);
+  if (mean_diff) std::copy(md.begin(), md.end(), mean_diff);
+}
+
 void compute_rdms(gbtn_plan* P) {
   cudaStream_t s = P->ctx->stream;
   if (P->cplx) {
     for (const WorkList* wl : {&P->lists[0].first, &P->lists[0].second})
       launch_vertex_rdms<zdouble>(*wl, P->d_vd.p, zptr(P->d_fac.p), P->sep_bra ? zptr(P->d_bra.p) : nullptr,
                                   zptr(P->d_msg[P->cur].p), P->d_msg_off.p, P->d_rdm_off.p, zptr(P->d_rdm.p), s);
+    large_rdms(P, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p, P->d_rdm.p);
     return;
   }
   launch_vertex_rdms(P->lists[0].first, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p,
                      P->d_msg_off.p, P->d_rdm_off.p, P->d_rdm.p, s);
   launch_vertex_rdms(P->lists[0].second, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p,
                      P->d_msg_off.p, P->d_rdm_off.p, P->d_rdm.p, s);
+  large_rdms(P, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p, P->d_rdm.p);
 }
 
 }  // namespace
@@ -1097,7 +1396,8 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   if (g->vertex_network) P->vnet.assign(g->vertex_network, g->vertex_network + g->nv);
   for (int v = 0; v < g->nv; ++v) {
     require(P->vnet[v] >= 0 && P->vnet[v] < P->nnet, "vertex_network out of range");
-    require(P->dsite[v] >= 1 && P->dsite[v] <= kMaxSite, "site dimension must be in 1..8");
+    require(P->dsite[v] >= 1, "site dimension must be >= 1");
+    if (P->dsite[v] > kMaxSiteLarge) throw Unsupported("site dimension must be in 1..64");
   }
   P->dchi.resize(2 * (size_t)g->ne);
   for (int e = 0; e < g->ne; ++e) {
@@ -1105,7 +1405,8 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
     require(u >= 0 && u < g->nv && v >= 0 && v < g->nv, "edge endpoint out of range");
     require(u != v, "self loops are not allowed");
     require(P->vnet[u] == P->vnet[v], "edge joins two different networks");
-    if (c < 1 || c > kMaxChi) throw Unsupported("bond dimension must be in 1..8");
+    require(c >= 1, "bond dimension must be >= 1");
+    if (c > kMaxChiLarge) throw Unsupported("bond dimension must be in 1..64");
     P->dchi[2 * e] = P->dchi[2 * e + 1] = c;
   }
   // messages
@@ -1120,6 +1421,7 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   require(g->leg_ptr[0] == 0, "leg_ptr[0] must be 0");
   std::vector<int> seen_count(g->ne, 0);
   P->vd.resize(g->nv);
+  P->is_large.assign(g->nv, 0);
   off = 0;
   long long roff = 0;
   P->rdm_off.resize(g->nv);
@@ -1145,19 +1447,27 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
       d.out_de[p] = fwd ? 2 * e : 2 * e + 1;
       d.in_de[p] = fwd ? 2 * e + 1 : 2 * e;
     }
-    if (n > (1 << 20)) throw Unsupported("vertex tensor above 2^20 elements");
+    if (n > kMaxLargeN) throw Unsupported("vertex tensor above 2^28 elements");
     d.n = (int)n;
     P->vd[v] = d;
     off += n;
     P->rdm_off[v] = roff;
     roff += (long long)d.d * d.d;
-    P->ncap = std::max(P->ncap, d.d == 0 ? 0 : (int)n);
     P->maxdeg = std::max(P->maxdeg, d.k);
-    // the FP64 sweep needs its tensors in shared memory
-    const int team = n <= kSmallN ? 32 : 256;
-    const size_t need = smem_need((int)n, d.k, P->sep_bra, P->cplx ? sizeof(zdouble) : sizeof(double), team) *
-                        (team == 32 ? 4 : 1);
-    if (need > 227 * 1024) throw Unsupported("vertex tensor too large for the shared-memory kernels");
+    // the shared-memory kernels hold the whole tensor (FP64 or complex FP64,
+    // three or four buffers) and bond / site dimensions <= 8; the rest runs
+    // the global-memory path
+    bool large = d.d > kMaxSite || n > (1 << 20);
+    for (int p = 0; p < d.k; ++p) large = large || d.chi[p] > kMaxChi;
+    if (!large) {
+      const int team = n <= kSmallN ? 32 : 256;
+      const size_t need = smem_need((int)n, d.k, P->sep_bra, P->cplx ? sizeof(zdouble) : sizeof(double), team) *
+                          (team == 32 ? 4 : 1);
+      large = need > 227 * 1024;
+    }
+    P->is_large[v] = large ? 1 : 0;
+    P->has_large = P->has_large || large;
+    if (!large) P->ncap = std::max(P->ncap, (int)n);
   }
   for (int e = 0; e < g->ne; ++e) require(seen_count[e] == 2, "every edge must appear once in the legs of each endpoint");
   P->n_fac = off;
@@ -1218,6 +1528,10 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
   std::vector<int> all(g->nv);
   std::iota(all.begin(), all.end(), 0);
   P->lists.push_back(split_list(P.get(), all));
+  P->large_lists.push_back(build_large_waves(P.get(), all));
+  P->d_iota.upload(all, s);
+  P->d_zero_off.upload(std::vector<long long>(1, 0), s);
+  if (P->has_large) reserve_single_vertex(P.get());
   std::vector<std::vector<int>> nbrs(g->nv);
   for (int e = 0; e < g->ne; ++e) {
     nbrs[P->eu[e]].push_back(P->ev[e]);
@@ -1239,6 +1553,7 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, gbtn_plan** out) {
     for (int v = 0; v < g->nv; ++v)
       if (P->color[v] == c) vs.push_back(v);
     P->lists.push_back(split_list(P.get(), vs));
+    P->large_lists.push_back(build_large_waves(P.get(), vs));
   }
   // tensor-core candidates: one swizzled BF16 image slot each; until the
   // first reduced-precision run tunes the split, only native vertices use it
@@ -1423,6 +1738,10 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
       ptr.push_back((int)seq.size());
     }
     for (int n = 0; n < P->nnet; ++n) require(ptr[n + 1] > ptr[n], "edge_sequence misses a network");
+    if (P->has_large) {
+      run_sequential_large(P, o, per, iters, mean_diff);
+      return GBTN_OK;
+    }
     P->d_seq.upload(seq, s);
     P->d_seq_ptr.upload(ptr, s);
     if (P->cplx && o->precision == GBTN_F64) {
@@ -1630,6 +1949,15 @@ int gbtn_updated_message(gbtn_plan* P, int32_t de, double* out) {
   for (int p = 0; p < P->vd[v].k; ++p)
     if (P->vd[v].out_de[p] == de) leg = p;
   const int c = P->dchi[de];
+  if (P->is_large[v]) {
+    // global-memory path: the message lands at its own offset of a message-sized buffer
+    DevBuf<double> tmp;
+    tmp.alloc(P->es() * std::max<long long>(P->n_msg, 1));
+    large_one_message(P, P->cplx ? kArithZ64 : kArithF64, v, leg, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr,
+                      P->d_msg[P->cur].p, tmp.p, 1, 0, P->ctx->stream);
+    copy_out(P, out, tmp.p + P->es() * P->msg_off[de], sizeof(double) * P->es() * c * c, GBTN_HOST);
+    return GBTN_OK;
+  }
   P->d_out.alloc(P->es() * c * c);
   if (P->cplx)
     launch_updated_message<zdouble>(P->d_vd.p, v, leg, zptr(P->d_fac.p), P->sep_bra ? zptr(P->d_bra.p) : nullptr,
@@ -1696,6 +2024,9 @@ static void edge_rdms_device(gbtn_plan* P, const int32_t* edges, int32_t n, DevB
     const int e = edges[j];
     require(e >= 0 && e < P->ne, "edge out of range");
     const int u = P->eu[e], v = P->ev[e];
+    if (P->is_large[u] || P->is_large[v])
+      throw Unsupported("two-site RDMs are computed for vertices of the shared-memory kernels only "
+                        "(bond and site dimensions <= 8)");
     int pu = -1, pv = -1;
     for (int p = 0; p < P->vd[u].k; ++p)
       if (P->vd[u].out_de[p] == 2 * e) pu = p;
@@ -1867,7 +2198,8 @@ int gbtn_rescale_messages(gbtn_plan* P) {
     if (P->cplx)
       launch_rescale_messages_z(P->ne, P->d_dchi.p, P->d_msg_off.p, zptr(P->d_msg[P->cur].p), P->ctx->stream);
     else
-      launch_rescale_messages(P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, P->ctx->stream);
+      launch_rescale_messages(P->ne, P->d_dchi.p, P->d_msg_off.p, P->d_msg[P->cur].p, P->ctx->stream,
+                              *std::max_element(P->dchi.begin(), P->dchi.end()));
   }
   GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));
   API_CATCH(C)
@@ -2035,6 +2367,10 @@ extern "C" {
 int gbtn_energy2(gbtn_plan* P, int32_t nterms, const double* coef, const double* ops, double* energy) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
+  require(P, "NULL plan");
+  if (P->has_large)
+    throw Unsupported("energies and gradients take vertices of the shared-memory kernels only (bond and site "
+                      "dimensions <= 8)");
   require(P && energy, "NULL argument");
   Energy2 E;
   energy_setup(E, P, nterms, coef, ops);
@@ -2048,6 +2384,10 @@ int gbtn_energy2_grad(gbtn_plan* P, int32_t nterms, const double* coef, const do
   const gbtn::NvtxRange nvtx_range("gbtn_energy2_grad");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
+  require(P, "NULL plan");
+  if (P->has_large)
+    throw Unsupported("energies and gradients take vertices of the shared-memory kernels only (bond and site "
+                      "dimensions <= 8)");
   require(P && o && grad, "NULL argument");
   require(o->mode == GBTN_GRAD_IMPLICIT || o->mode == GBTN_GRAD_UNROLLED, "unknown gradient mode");
   cudaStream_t s = P->ctx->stream;
@@ -2129,6 +2469,10 @@ int gbtn_bp_vjp(gbtn_plan* P, const double* msg_cot, const gbtn_grad_opts* o, do
   const gbtn::NvtxRange nvtx_range("gbtn_bp_vjp");
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
+  require(P, "NULL plan");
+  if (P->has_large)
+    throw Unsupported("energies and gradients take vertices of the shared-memory kernels only (bond and site "
+                      "dimensions <= 8)");
   if (P && P->cplx) throw Unsupported("the BP vector-Jacobian product of complex networks is not implemented");
   require(P && msg_cot && o && grad, "NULL argument");
   require(o->mode == GBTN_GRAD_IMPLICIT, "gbtn_bp_vjp differentiates through the fixed point (IMPLICIT)");

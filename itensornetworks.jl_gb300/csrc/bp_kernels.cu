@@ -633,10 +633,12 @@ __global__ void logscalar_kernel(const int* net_v_ptr, const int* net_v, const i
 // ---------------------------------------------------------------------------
 
 template <typename T>
-void launch_bp_vertices(const WorkList& wl, const VDesc* vd, const T* fac, const T* bra, const T* msg_in, T* msg_out,
-                        const long long* msg_off, double* diffs, const int* converged, int normalize, int want_diff,
-                        cudaStream_t s) {
-  if (wl.count == 0) return;
+void launch_bp_vertices(const WorkList& wl_all, const VDesc* vd, const T* fac, const T* bra, const T* msg_in,
+                        T* msg_out, const long long* msg_off, double* diffs, const int* converged, int normalize,
+                        int want_diff, cudaStream_t s) {
+  for (int c = 0; c < wl_all.nsubs(); ++c) {
+  const WorkList wl = wl_all.sub(c);
+  if (wl.count == 0) continue;
   const int nbuf = wl.maxdeg <= 4 ? 3 : kNumBufs;
   if (wl.team == 32) {
     const size_t sm = 4 * team_smem_bytes<T>(wl.ncap, nbuf, bra != nullptr, 32);
@@ -653,12 +655,15 @@ void launch_bp_vertices(const WorkList& wl, const VDesc* vd, const T* fac, const
                                    normalize, want_diff, wl.ncap, nbuf);
   }
   GBTN_CUDA(cudaGetLastError());
+  }
 }
 
-void launch_bp_vertices_df32(const WorkList& wl, const VDesc* vd, const double* fac, const double* bra,
+void launch_bp_vertices_df32(const WorkList& wl_all, const VDesc* vd, const double* fac, const double* bra,
                              const double* msg_in, double* msg_out, const long long* msg_off, double* diffs,
                              const int* converged, int normalize, int want_diff, cudaStream_t s) {
-  if (wl.count == 0) return;
+  for (int c = 0; c < wl_all.nsubs(); ++c) {
+  const WorkList wl = wl_all.sub(c);
+  if (wl.count == 0) continue;
   const int nbuf = wl.maxdeg <= 4 ? 3 : kNumBufs;
   if (wl.team == 32) {
     const size_t sm = 4 * team_smem_bytes<df32>(wl.ncap, nbuf, bra != nullptr, 32);
@@ -675,6 +680,7 @@ void launch_bp_vertices_df32(const WorkList& wl, const VDesc* vd, const double* 
                                    normalize, want_diff, wl.ncap, nbuf);
   }
   GBTN_CUDA(cudaGetLastError());
+  }
 }
 
 template void launch_bp_vertices<double>(const WorkList&, const VDesc*, const double*, const double*, const double*,
@@ -828,9 +834,43 @@ void launch_rescale_messages_z(int ne, const int* dchi, const long long* msg_off
   GBTN_CUDA(cudaGetLastError());
 }
 
-void launch_rescale_messages(int ne, const int* dchi, const long long* msg_off, double* msgs, cudaStream_t s) {
+// rescale_messages for bond dimensions above 8: one warp per edge, strided
+// over the chi^2 entries (the same factors as rescale_messages_kernel).
+__global__ void rescale_messages_wide_kernel(int ne, const int* dchi, const long long* msg_off, double* msgs) {
+  const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (e >= ne) return;
+  const int c2 = dchi[2 * e] * dchi[2 * e];
+  double* m1 = msgs + msg_off[2 * e];
+  double* m2 = msgs + msg_off[2 * e + 1];
+  double na2 = 0.0, nb2 = 0.0, ab = 0.0;
+  for (int i = lane; i < c2; i += 32) {
+    const double a = m1[i], b = m2[i];
+    na2 = fma(a, a, na2);
+    nb2 = fma(b, b, nb2);
+    ab = fma(a, b, ab);
+  }
+  na2 = warp_sum(na2);
+  nb2 = warp_sum(nb2);
+  ab = warp_sum(ab);
+  const double ia = rsqrt(na2), ib = rsqrt(nb2);
+  const double n = ab * ia * ib;
+  const double sg = n > 0.0 ? 1.0 : (n < 0.0 ? -1.0 : 0.0);
+  const double isf = rsqrt(fabs(n));
+  const double ka = sg * isf * ia, kb = isf * ib;
+  for (int i = lane; i < c2; i += 32) {
+    m1[i] *= ka;
+    m2[i] *= kb;
+  }
+}
+
+void launch_rescale_messages(int ne, const int* dchi, const long long* msg_off, double* msgs, cudaStream_t s,
+                             int max_chi) {
   if (ne == 0) return;
-  rescale_messages_kernel<<<(ne + 63) / 64, 256, 0, s>>>(ne, dchi, msg_off, msgs);  // 4 lanes per edge
+  if (max_chi <= 8)
+    rescale_messages_kernel<<<(ne + 63) / 64, 256, 0, s>>>(ne, dchi, msg_off, msgs);  // 4 lanes per edge
+  else
+    rescale_messages_wide_kernel<<<(ne + 7) / 8, 256, 0, s>>>(ne, dchi, msg_off, msgs);
   GBTN_CUDA(cudaGetLastError());
 }
 void launch_edge_scalars(int ne, const int* dchi, const long long* msg_off, const double* msgs, double* out,

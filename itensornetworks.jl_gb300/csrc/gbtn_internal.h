@@ -103,12 +103,33 @@ struct Timeout : std::runtime_error {
   } while (0)
 
 // Launch parameters of a batch of vertices processed by one message kernel.
+// The vertices are sorted by tensor size and cut into size classes (up to
+// kMaxSub sub-ranges, one launch each), so that a class of small tensors gets
+// shared memory, and resident blocks, for its own largest tensor only.
+constexpr int kMaxSub = 8;
 struct WorkList {
   int* d_vertices = nullptr;  // device list of vertex ids
   int count = 0;
   int ncap = 0;               // largest n in the list
   int maxdeg = 0;
   int team = 32;              // threads per vertex (32 or 256)
+  int nsub = 0;               // size classes: [sub_begin[i], sub_begin[i] + sub_count[i])
+  int sub_begin[kMaxSub] = {};
+  int sub_count[kMaxSub] = {};
+  int sub_ncap[kMaxSub] = {};
+  int sub_maxdeg[kMaxSub] = {};
+  // The list restricted to size class i (the whole list when it has none).
+  WorkList sub(int i) const {
+    WorkList w = *this;
+    w.nsub = 0;
+    if (nsub == 0) return w;
+    w.d_vertices = d_vertices + sub_begin[i];
+    w.count = sub_count[i];
+    w.ncap = sub_ncap[i];
+    w.maxdeg = sub_maxdeg[i];
+    return w;
+  }
+  int nsubs() const { return nsub == 0 ? 1 : nsub; }
 };
 
 // Kernel launchers (bp_kernels.cu).  T = double, float, zdouble or zfloat.
@@ -121,6 +142,65 @@ void launch_bp_vertices(const WorkList& wl, const VDesc* vd, const T* fac, const
 void launch_bp_vertices_df32(const WorkList& wl, const VDesc* vd, const double* fac, const double* bra,
                              const double* msg_in, double* msg_out, const long long* msg_off, double* diffs,
                              const int* converged, int normalize, int want_diff, cudaStream_t s);
+
+// Global-memory path for vertices beyond the shared-memory kernels
+// (bp_large.cu): bond and site dimensions up to 64, tensors up to 2^28
+// elements, intermediates in a scratch area in HBM, one launch per schedule
+// step over a wave of vertices of one degree.
+constexpr int kMaxChiLarge = 64;
+constexpr int kMaxSiteLarge = 64;
+constexpr long long kMaxLargeN = 1LL << 28;
+constexpr int kTile = 4096;  // elements of one staged tile
+// Arithmetic of a large-path launch (the storage is double, float, zdouble or
+// zfloat; double under DF32).
+enum { kArithF64 = 0, kArithF32 = 1, kArithDF32 = 2, kArithZ64 = 3, kArithZ32 = 4 };
+
+// Tiles of the fibers of one leg (stride st, dimension chi) of a tensor of n
+// elements: a tile covers leg indices [l0, l0 + Lt) of R consecutive outer
+// rows (each st * chi elements), contiguous runs of memory of at most kTile.
+struct LegTiling {
+  int Lt, R, ntl, ntj;
+  long long nouter;
+};
+__host__ __device__ inline LegTiling leg_tiling(int n, int st, int chi) {
+  LegTiling g;
+  const long long sc = (long long)st * chi;
+  g.nouter = n / sc;
+  if (sc <= kTile) {
+    g.Lt = st;
+    g.R = (int)(kTile / sc < g.nouter ? kTile / sc : g.nouter);
+    g.ntl = 1;
+    g.ntj = (int)((g.nouter + g.R - 1) / g.R);
+  } else {
+    const int lt = kTile / chi;
+    g.Lt = lt < st ? lt : st;
+    g.R = 1;
+    g.ntl = (st + g.Lt - 1) / g.Lt;
+    g.ntj = (int)g.nouter;
+  }
+  return g;
+}
+
+template <typename S>
+struct LargeArgs {
+  const int* verts;         // wave vertex ids
+  const long long* buf_off; // element offset of each wave vertex's scratch buffers
+  const VDesc* vd;
+  const S* fac;
+  const S* bra;             // NULL: bra = conj(fac)
+  const S* msgs;            // incoming messages
+  const long long* msg_off;
+};
+// One schedule step (ABSORB, or CLOSE + normalisation into msg_out) for a
+// wave; msg_old is the message array of the previous values (message_diff).
+void launch_large_op_any(int arith, const LargeArgs<double>& a, int nverts, int max_tiles, int max_chi,
+                         const SchedOp& op, void* scratch, void* partial, long long vstride, const void* msg_old,
+                         void* msg_out, double* diffs, const int* converged, int normalize, int want_diff,
+                         cudaStream_t s);
+// CLOSE on the site index of buffer src: rho_v[s', s] into rdm (FP64 or complex FP64).
+void launch_large_rdm_any(int arith, const LargeArgs<double>& a, int nverts, int max_tiles, int src, void* scratch,
+                          void* partial, long long vstride, void* rdm, const long long* rdm_off, cudaStream_t s);
+size_t large_elem_size(int arith);
 
 template <typename T>
 void launch_bp_sequential(int n_networks, const VDesc* vd, const int2* seq, const int* seq_ptr,
@@ -158,7 +238,7 @@ void launch_scale_vertices(int nv, const VDesc* vd, double* fac, double* bra, co
                            cudaStream_t s);
 void launch_rescale_messages_z(int ne, const int* dchi, const long long* msg_off, zdouble* msgs, cudaStream_t s);
 void launch_rescale_messages(int ne, const int* dchi, const long long* msg_off, double* msgs,
-                             cudaStream_t s);
+                             cudaStream_t s, int max_chi = 8);
 void launch_edge_scalars(int ne, const int* dchi, const long long* msg_off, const double* msgs,
                          double* out, cudaStream_t s);
 void launch_logscalar(int n_networks, const int* net_v_ptr, const int* net_v, const int* net_e_ptr,

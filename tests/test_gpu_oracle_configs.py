@@ -91,7 +91,7 @@ def test_tfim_20x20_200_steps_against_oracle():
     np.testing.assert_allclose(te, fx["truncerr_last_step"], rtol=1e-5, atol=1e-14)
     net = st.network()
     st.close()
-    bpc = gbtn.BeliefPropagationCache(net).update(maxiter=300, schedule="parallel")
+    bpc = gbtn.BeliefPropagationCache(net).update(maxiter=int(fx["bp_sweeps"]), schedule="parallel")
     x = bpc.expect(O.PX)
     zz = bpc.expect2(np.kron(O.PZ, O.PZ))
     energy = (-zz.sum() - g_field * x.sum()) / net.nv
