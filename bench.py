@@ -483,6 +483,20 @@ def run_ours(args):
     ms_f32 = per_sweep("f32", args.steps)
     ms_df32 = per_sweep("df32", max(3, args.steps // 2))
     ms_f64 = per_sweep("f64", max(2, args.steps // 4))
+
+    # the reference's default schedule: sequential sweeps in the forest-cover
+    # order, run as waves of independent messages
+    def per_sweep_seq(precision, n):
+        bpc.init_messages("identity")
+        bpc.update(maxiter=2, schedule="sequential", precision=precision)
+        barrier()
+        e0.record(stream)
+        bpc.update(maxiter=n, schedule="sequential", precision=precision)
+        e1.record(stream)
+        barrier()
+        return max_ranks(e0.elapsed_time(e1) / n)
+
+    seq_ms = {p: per_sweep_seq(p, 3) for p in ("f32", "df32", "f64")}
     ctx.set_profiling(True)
     bpc.update(maxiter=args.steps, schedule="parallel", precision="bf16")
     barrier()
@@ -597,6 +611,8 @@ def run_ours(args):
             "kernel_shares_of_mixed_solve": shares,
             "paths_ms_per_sweep": {"bf16_tensor_core": ms_bf16, "f32_simt": ms_f32, "df32_simt": ms_df32,
                                    "f64_simt": ms_f64},
+            "sequential_schedule": {"ms_per_sweep": seq_ms,
+                                    "msg_updates_per_s": {p: msgs_step / (ms * 1e-3) for p, ms in seq_ms.items()}},
             "tc_split": {"tensor_core_vertices": n_tc, "simt_vertices": tn.nv - n_tc, "tuned_split_ms": tune_ms},
             "gauge_scaling": gauge,
             "batched_uneven": batched,

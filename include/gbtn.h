@@ -119,7 +119,7 @@ typedef struct gbtn_bp_opts {
                                       not allowed; give the full sequence) */
   /* MIXED only: per-phase limits; zeros select the defaults.  The BF16 and
      FP32 phases also stop at their noise floor: when a network's mean diff
-     has not dropped below 0.9x its best value for 5 sweeps. */
+     has not dropped below 0.9x its best value for 3 sweeps. */
   double tol_bf16;               /* default 1e-6 */
   double tol_f32;                /* default 1e-13 */
   int32_t maxiter_bf16;          /* default maxiter */
@@ -174,6 +174,13 @@ int gbtn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* desc, gbtn_plan** out
 int gbtn_plan_destroy(gbtn_plan* plan);
 /* Element counts of the concatenated tensor and message arrays. */
 int gbtn_plan_sizes(const gbtn_plan* plan, int64_t* n_factor, int64_t* n_message);
+/* Instrumentation (no counterpart in the reference): how often the plan's
+ * arrays crossed the host boundary since it was made: counts[0] tensor
+ * uploads (gbtn_set_factors), [1] message uploads (gbtn_set_messages),
+ * [2] message read-backs (gbtn_get_messages), [3] tensor read-backs
+ * (gbtn_get_factors).  A caller that keeps one plan for update, expect,
+ * logscalar and normalize sees one tensor upload and no message traffic. */
+int gbtn_plan_counters(const gbtn_plan* plan, int64_t counts[4]);
 /* Tensor-core routing of the BF16 phase (no counterpart in the reference,
  * which contracts every vertex the same way; the "autotuner keyed on chi, d
  * and degree").  Vertices with d = 2, at most four legs and chi <= 8 can run

@@ -166,12 +166,19 @@ struct gbtn_plan {
   DevBuf<double> d_large_scratch, d_large_partial;  // sized in elements of the plan's widest arithmetic
   DevBuf<int> d_iota;                               // vertex ids 0..nv-1 (single-vertex waves)
   DevBuf<long long> d_zero_off;                     // scratch offset 0
+  // sequential schedule in waves: the per-network sequences the waves were cut
+  // for, and per wave the jobs of small (team 32) and larger (team 256) vertices
+  std::vector<int> wave_key;  // per network: its length, then (vertex, leg) pairs
+  std::vector<std::pair<WaveJobs, WaveJobs>> waves;
+  DevBuf<int4> d_wave_jobs;
+  DevBuf<int> d_wave_ptr, d_wave_iota;
+  DevBuf<double> d_pos_diffs;
+  int wave_version = 0;
+  // host <-> device traffic of the plan's arrays (gbtn_plan_counters)
+  long long cnt_fac_up = 0, cnt_msg_up = 0, cnt_msg_down = 0, cnt_fac_down = 0;
   // sweeps per phase of the last run (max over networks): BF16, FP32, refinement, FP64
   DevBuf<int> d_phase_iters;  // 4 x nnet
   int phase_fixed[4] = {0, 0, 0, 0};  // sweeps of a phase run without a tolerance (all of its maxiter)
-  // sequential schedule storage
-  DevBuf<int2> d_seq;
-  DevBuf<int> d_seq_ptr;
   DevBuf<int> d_jobs;
   DevBuf<long long> d_half_off;
   DevBuf<double> d_halves;
@@ -214,7 +221,9 @@ void launch_vertices(const WorkList& wl, const VDesc* vd, const T* fac, const T*
 }
 
 constexpr int kSmallN = 1024;  // vertices with n <= kSmallN run one per warp
-constexpr int kStallSweeps = 5;  // reduced-precision phases stop at their noise floor
+// Reduced-precision phases stop at their noise floor: after this many sweeps
+// without a new best mean diff below 0.9x the previous one.
+constexpr int kStallSweeps = 3;
 
 // Brackets one kernel launch with CUDA events when the context profiles.
 struct KTimer {
@@ -907,6 +916,114 @@ void large_one_message(gbtn_plan* P, int arith, int v, int leg, const void* fac,
   for (const SchedOp& op : ops)
     launch_large_op_any(arith, a, 1, w.max_tiles, w.max_chi, op, P->d_large_scratch.p, P->d_large_partial.p,
                         w.vstride, msgs, out, P->d_diffs.p, nullptr, normalize, want_diff, s);
+}
+
+// Cut the per-network sequences into waves.  A job (one message) goes to the
+// first wave after every job it depends on in sequence order: the last writer
+// of each message it reads (read after write), the readers since the last
+// write of the message it writes (write after read) and that last writer
+// (write after write).  Networks are independent, so wave l holds level l of
+// every network.
+void build_waves(gbtn_plan* P, const std::vector<std::vector<int2>>& per) {
+  std::vector<int> key;
+  for (const auto& l : per) {
+    key.push_back((int)l.size());
+    for (const int2& jb : l) {
+      key.push_back(jb.x);
+      key.push_back(jb.y);
+    }
+  }
+  if (!P->waves.empty() && key == P->wave_key) return;
+  GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));  // no launch still reads the old job lists
+  std::vector<std::vector<int4>> small, big;
+  std::vector<int> ptr(1, 0);
+  int pos = 0;
+  for (int n = 0; n < (int)per.size(); ++n) {
+    std::map<int, int> last_write, last_read;
+    for (const int2& jb : per[n]) {
+      const VDesc& d = P->vd[jb.x];
+      const int de = d.out_de[jb.y];
+      int l = 0;
+      for (int p = 0; p < d.k; ++p) {
+        if (p == jb.y) continue;
+        auto w = last_write.find(d.in_de[p]);
+        if (w != last_write.end()) l = std::max(l, w->second + 1);
+      }
+      auto r = last_read.find(de);
+      if (r != last_read.end()) l = std::max(l, r->second + 1);
+      auto w = last_write.find(de);
+      if (w != last_write.end()) l = std::max(l, w->second + 1);
+      last_write[de] = l;
+      last_read.erase(de);
+      for (int p = 0; p < d.k; ++p) {
+        if (p == jb.y) continue;
+        int& lr = last_read.emplace(d.in_de[p], l).first->second;
+        lr = std::max(lr, l);
+      }
+      auto& lv = d.n <= kSmallN ? small : big;
+      if ((int)lv.size() <= l) {
+        small.resize(l + 1);
+        big.resize(l + 1);
+      }
+      (d.n <= kSmallN ? small : big)[l].push_back(make_int4(jb.x, jb.y, pos, n));
+      ++pos;
+    }
+    ptr.push_back(pos);
+  }
+  std::vector<int4> all;
+  std::vector<std::pair<size_t, int>> spans;  // (offset, count) per wave and class
+  for (size_t l = 0; l < small.size(); ++l)
+    for (auto* lv : {&small[l], &big[l]}) {
+      spans.push_back({all.size(), (int)lv->size()});
+      all.insert(all.end(), lv->begin(), lv->end());
+    }
+  if (all.empty()) all.push_back(make_int4(0, 0, 0, 0));
+  P->d_wave_jobs.upload(all, P->ctx->stream);
+  P->d_wave_ptr.upload(ptr, P->ctx->stream);
+  std::vector<int> iota(std::max(pos, 1));
+  std::iota(iota.begin(), iota.end(), 0);
+  P->d_wave_iota.upload(iota, P->ctx->stream);
+  P->d_pos_diffs.alloc(std::max(pos, 1));
+  P->waves.clear();
+  for (size_t l = 0; l < small.size(); ++l) {
+    std::pair<WaveJobs, WaveJobs> w;
+    for (int c = 0; c < 2; ++c) {
+      WaveJobs& j = c == 0 ? w.first : w.second;
+      const auto& sp = spans[2 * l + c];
+      j.d_jobs = P->d_wave_jobs.p + sp.first;
+      j.count = sp.second;
+      j.team = c == 0 ? 32 : 256;
+      for (const int4& jb : c == 0 ? small[l] : big[l]) j.ncap = std::max(j.ncap, P->vd[jb.x].n);
+    }
+    P->waves.push_back(w);
+  }
+  P->wave_key = key;
+  P->wave_version++;
+  P->clear_graphs();
+}
+
+// Sweeps of the sequential schedule as waves (see build_waves), in place on
+// msgs, in arithmetic `arith`; per-network convergence as the other schedules.
+void run_waves(gbtn_plan* P, int arith, const void* fac, const void* bra, void* msgs, const gbtn_bp_opts* o) {
+  cudaStream_t s = P->ctx->stream;
+  const bool want_diff = o->tol >= 0.0;
+  GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int) * P->nnet, s));
+  GBTN_CUDA(cudaMemsetAsync(P->d_iters.p, 0, sizeof(int) * P->nnet, s));
+  GBTN_CUDA(cudaMemsetAsync(P->d_nconv.p, 0, sizeof(int), s));
+  const int* conv = want_diff ? P->d_conv.p : nullptr;
+  const GraphKey key{20 + arith, GBTN_SCHED_SEQUENTIAL, o->normalize, want_diff ? 1 : 0, 0, P->wave_version,
+                     P->list_version, o->tol};
+  sweep_loop(P, o->maxiter, key, [&] {
+    for (const auto& w : P->waves) {
+      launch_bp_wave_any(arith, w.first, P->d_vd.p, fac, bra, msgs, P->d_msg_off.p, P->d_pos_diffs.p, conv,
+                         o->normalize, want_diff, s);
+      launch_bp_wave_any(arith, w.second, P->d_vd.p, fac, bra, msgs, P->d_msg_off.p, P->d_pos_diffs.p, conv,
+                         o->normalize, want_diff, s);
+    }
+    if (want_diff)
+      launch_reduce_diffs(P->nnet, P->d_wave_ptr.p, P->d_wave_iota.p, P->d_pos_diffs.p, o->tol, P->d_conv.p,
+                          P->d_iters.p, P->d_mean.p, s, 0, P->d_best.p, P->d_since.p, P->d_nconv.p);
+  }, want_diff);
 }
 
 // The sequential schedule of a plan that holds large vertices: every message
@@ -1635,6 +1752,7 @@ int gbtn_set_factors(gbtn_plan* P, const double* ket, const double* bra, int mem
   API_TRY
   require(P && ket, "NULL argument");
   require(!P->sep_bra || bra, "plan has separate_bra: bra tensors are required");
+  P->cnt_fac_up++;
   if (mem == GBTN_HOST && P->d_zimg.p && !P->cplx) {
     upload_with_images(P, ket);  // the plan has run BF16: rebuild its images while the factors arrive
   } else {
@@ -1650,6 +1768,7 @@ int gbtn_get_factors(gbtn_plan* P, double* ket, int mem) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && ket, "NULL argument");
+  P->cnt_fac_down++;
   copy_out(P, ket, P->d_fac.p, sizeof(double) * P->es() * P->n_fac, mem);
   API_CATCH(C)
 }
@@ -1659,6 +1778,7 @@ int gbtn_set_messages(gbtn_plan* P, const double* m, int mem) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && m, "NULL argument");
+  P->cnt_msg_up++;
   copy_in(P, P->d_msg[P->cur].p, m, sizeof(double) * P->es() * P->n_msg, mem);
   API_CATCH(C)
 }
@@ -1668,6 +1788,7 @@ int gbtn_get_messages(gbtn_plan* P, double* m, int mem) {
   gbtn_ctx* C = P ? P->ctx : nullptr;
   API_TRY
   require(P && m, "NULL argument");
+  P->cnt_msg_down++;
   copy_out(P, m, P->d_msg[P->cur].p, sizeof(double) * P->es() * P->n_msg, mem);
   API_CATCH(C)
 }
@@ -1711,8 +1832,8 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     throw Unsupported("BF16 sweeps run the parallel or coloured schedule");
   if (o->precision == GBTN_MIXED && o->schedule == GBTN_SCHED_SEQUENTIAL)
     throw Unsupported("the mixed BF16 -> FP32 -> FP64 pipeline runs the parallel or coloured schedule");
-  if (o->precision == GBTN_DF32 && o->schedule == GBTN_SCHED_SEQUENTIAL)
-    throw Unsupported("double-FP32 sweeps run the parallel or coloured schedule");
+  if (o->precision == GBTN_DF32 && o->schedule == GBTN_SCHED_SEQUENTIAL && P->has_large)
+    throw Unsupported("double-FP32 sequential sweeps take vertices of the shared-memory kernels only");
   if (P->cplx && o->precision == GBTN_BF16)
     throw Unsupported("complex tensors have no tensor-core (BF16) path: use f32, mixed or f64");
   if (P->cplx && o->precision == GBTN_DF32)
@@ -1742,43 +1863,21 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
       run_sequential_large(P, o, per, iters, mean_diff);
       return GBTN_OK;
     }
-    P->d_seq.upload(seq, s);
-    P->d_seq_ptr.upload(ptr, s);
-    if (P->cplx && o->precision == GBTN_F64) {
-      launch_bp_sequential<zdouble>(P->nnet, P->d_vd.p, P->d_seq.p, P->d_seq_ptr.p, zptr(P->d_fac.p),
-                                    P->sep_bra ? zptr(P->d_bra.p) : nullptr, zptr(P->d_msg[P->cur].p),
-                                    P->d_msg_off.p, o->maxiter, o->tol, o->normalize, P->d_iters.p, P->d_mean.p,
-                                    P->ncap, P->maxdeg, s);
-    } else if (P->cplx) {
+    // waves of independent messages, in sequence order (see build_waves)
+    build_waves(P, per);
+    const void* bra = nullptr;
+    if (o->precision == GBTN_F32) {
       ensure_f32(P);
-      launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, 2 * P->n_msg, s);
-      launch_bp_sequential<zfloat>(P->nnet, P->d_vd.p, P->d_seq.p, P->d_seq_ptr.p, zfptr(P->d_fac32.p),
-                                   P->sep_bra ? zfptr(P->d_bra32.p) : nullptr, zfptr(P->d_msg32[0].p),
-                                   P->d_msg_off.p, o->maxiter, o->tol, o->normalize, P->d_iters.p, P->d_mean.p,
-                                   P->ncap, P->maxdeg, s);
-      launch_convert_f32_to_f64(P->d_msg32[0].p, P->d_msg[P->cur].p, 2 * P->n_msg, s);
-    } else if (o->precision == GBTN_F64) {
-      launch_bp_sequential<double>(P->nnet, P->d_vd.p, P->d_seq.p, P->d_seq_ptr.p, P->d_fac.p,
-                                   P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p, P->d_msg_off.p, o->maxiter,
-                                   o->tol, o->normalize, P->d_iters.p, P->d_mean.p, P->ncap, P->maxdeg, s);
+      launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->es() * P->n_msg, s);
+      if (P->sep_bra) bra = P->d_bra32.p;
+      run_waves(P, P->cplx ? kArithZ32 : kArithF32, P->d_fac32.p, bra, P->d_msg32[0].p, o);
+      launch_convert_f32_to_f64(P->d_msg32[0].p, P->d_msg[P->cur].p, P->es() * P->n_msg, s);
     } else {
-      ensure_f32(P);
-      launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, s);
-      launch_bp_sequential<float>(P->nnet, P->d_vd.p, P->d_seq.p, P->d_seq_ptr.p, P->d_fac32.p,
-                                  P->sep_bra ? P->d_bra32.p : nullptr, P->d_msg32[0].p, P->d_msg_off.p, o->maxiter,
-                                  o->tol, o->normalize, P->d_iters.p, P->d_mean.p, P->ncap, P->maxdeg, s);
-      launch_convert_f32_to_f64(P->d_msg32[0].p, P->d_msg[P->cur].p, P->n_msg, s);
+      if (P->sep_bra) bra = P->d_bra.p;
+      const int arith = P->cplx ? kArithZ64 : (o->precision == GBTN_DF32 ? kArithDF32 : kArithF64);
+      run_waves(P, arith, P->d_fac.p, bra, P->d_msg[P->cur].p, o);
     }
-    // the sequential kernel reports iterations itself
-    if (iters || mean_diff) {
-      std::vector<int> it(P->nnet);
-      std::vector<double> md(P->nnet);
-      GBTN_CUDA(cudaMemcpyAsync(it.data(), P->d_iters.p, sizeof(int) * P->nnet, cudaMemcpyDeviceToHost, s));
-      GBTN_CUDA(cudaMemcpyAsync(md.data(), P->d_mean.p, sizeof(double) * P->nnet, cudaMemcpyDeviceToHost, s));
-      GBTN_CUDA(cudaStreamSynchronize(s));
-      if (iters) std::copy(it.begin(), it.end(), iters);
-      if (mean_diff) std::copy(md.begin(), md.end(), mean_diff);
-    }
+    finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
     return GBTN_OK;
   }
   // phase slots of gbtn_plan_phase_sweeps: 0 BF16, 1 FP32, 2 refinement, 3 FP64
@@ -1885,6 +1984,15 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     }
   }
   API_CATCH(C)
+}
+
+int gbtn_plan_counters(const gbtn_plan* P, int64_t* counts) {
+  if (!P || !counts) return GBTN_ERR_INVALID;
+  counts[0] = P->cnt_fac_up;
+  counts[1] = P->cnt_msg_up;
+  counts[2] = P->cnt_msg_down;
+  counts[3] = P->cnt_fac_down;
+  return GBTN_OK;
 }
 
 int gbtn_plan_phase_sweeps(gbtn_plan* P, int32_t* sweeps) {

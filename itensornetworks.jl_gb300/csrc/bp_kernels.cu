@@ -145,9 +145,9 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
 }
 
 // ---------------------------------------------------------------------------
-// Sequential schedule: one block per network walks its edge sequence for all
-// sweeps, each update seeing every earlier one; convergence is tested on the
-// device after every sweep (abstractbeliefpropagationcache.jl:272-287,313-329).
+// Sequential schedule: waves of messages that do not depend on one another,
+// each update seeing every earlier one; convergence is tested on the device
+// after every sweep (abstractbeliefpropagationcache.jl:272-287,313-329).
 // ---------------------------------------------------------------------------
 
 // Compute the message leaving v on leg p from the loaded vertex: absorb every
@@ -166,46 +166,46 @@ __device__ __forceinline__ int chain_absorb(const TeamSmem<T>& S, int skip_leg, 
   return cur;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256)
-    bp_sequential_kernel(const VDesc* __restrict__ vd, const int2* __restrict__ seq, const int* __restrict__ seq_ptr,
-                         const T* __restrict__ fac, const T* __restrict__ bra_g, T* msgs,
-                         const long long* __restrict__ msg_off, int maxiter, double tol, int normalize,
-                         int* iters, double* mean_diff, int ncap) {
+// One wave of the sequential schedule: every job (vertex, leg, sequence
+// position, network) computes one message in place from the current messages
+// (absorb chain of the other legs, CLOSE on the leg, normalisation) and
+// records its message_diff at its sequence position.  The host cuts the
+// sequence into waves so that no job of a wave reads or writes a message that
+// another job of the same wave writes, and every job comes after the jobs it
+// depends on in sequence order (read-after-write, write-after-read and
+// write-after-write on the messages): the waves in order give the strictly
+// sequential result (abstractbeliefpropagationcache.jl:272-287).
+template <typename T, int TEAM, typename S = T>
+__global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
+    bp_wave_kernel(const int4* __restrict__ jobs, int njobs, const VDesc* __restrict__ vd, const S* __restrict__ fac,
+                   const S* __restrict__ bra_g, S* msgs, const long long* __restrict__ msg_off, double* pos_diffs,
+                   const int* converged, int normalize, int want_diff, int ncap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int TEAM = 256;
-  const int tid = threadIdx.x, lane = tid & 31;
-  const int net = blockIdx.x;
-  TeamSmem<T> S = carve<T>(smem_raw, ncap, 3, bra_g != nullptr, TEAM);
-  __shared__ int s_stop;
-  const int begin = seq_ptr[net], end = seq_ptr[net + 1];
-  const bool want_diff = tol >= 0.0;
-  for (int it = 1; it <= maxiter; ++it) {
-    double sum = 0.0;
-    for (int i = begin; i < end; ++i) {
-      const int2 e = seq[i];
-      load_desc<TEAM>(S.desc, vd + e.x, tid);
-      __syncthreads();
-      load_vertex<T, TEAM>(S, fac, bra_g, msgs, msg_off, e.y, tid);
-      __syncthreads();
-      const int cur = chain_absorb<T, TEAM>(S, e.y, tid);
-      const VDesc& d = *S.desc;
-      close_any<T, TEAM>(d.chi[e.y], S.buf[cur], S.bra, d.n, d.st[e.y], 1, 0, 0, S.red, S.res, tid);
-      if (tid < 32) {
-        const long long off = msg_off[d.out_de[e.y]];
-        const double df = finalize_message<T>(S.res, d.chi[e.y], msgs + off, msgs + off, normalize, want_diff, lane);
-        sum += df;  // meaningful on tid 0 only
-      }
-      __syncthreads();
+  constexpr int TPB = TEAM == 32 ? 4 : 1;
+  const int team = threadIdx.x / TEAM, tid = threadIdx.x % TEAM, lane = tid & 31;
+  const size_t tb = team_smem_bytes<T>(ncap, 3, bra_g != nullptr, TEAM);
+  TeamSmem<T> Sm = carve<T>(smem_raw + team * tb, ncap, 3, bra_g != nullptr, TEAM);
+  for (int w = blockIdx.x * TPB + team; w < njobs; w += gridDim.x * TPB) {
+    const int4 jb = jobs[w];  // (vertex, leg, sequence position, network)
+    if (converged && converged[jb.w]) continue;  // uniform over the team
+    load_desc<TEAM>(Sm.desc, vd + jb.x, tid);
+    tsync<TEAM>();
+    load_vertex<T, TEAM, S>(Sm, fac, bra_g, msgs, msg_off, jb.y, tid);
+    tsync<TEAM>();
+    const int cur = chain_absorb<T, TEAM>(Sm, jb.y, tid);
+    const VDesc& d = *Sm.desc;
+    const int chi = d.chi[jb.y];
+    close_any<T, TEAM>(chi, Sm.buf[cur], Sm.bra, d.n, d.st[jb.y], 1, 0, 0, Sm.red, Sm.res, tid);
+    if (tid < 32) {
+      S* m = msgs + msg_off[d.out_de[jb.y]];
+      double df;
+      if constexpr (std::is_same<T, df32>::value)
+        df = finalize_message_df(Sm.res, chi, m, m, normalize, want_diff != 0, lane);
+      else
+        df = finalize_message<T>(Sm.res, chi, m, m, normalize, want_diff != 0, lane);
+      if (want_diff && lane == 0) pos_diffs[jb.z] = df;
     }
-    if (tid == 0) {
-      const double mean = sum / (double)(end - begin);
-      iters[net] = it;
-      mean_diff[net] = want_diff ? mean : NAN;
-      s_stop = (want_diff && mean <= tol) ? 1 : 0;
-    }
-    __syncthreads();
-    if (s_stop) break;
+    tsync<TEAM>();
   }
 }
 
@@ -693,30 +693,56 @@ template void launch_bp_vertices<zdouble>(const WorkList&, const VDesc*, const z
 template void launch_bp_vertices<zfloat>(const WorkList&, const VDesc*, const zfloat*, const zfloat*, const zfloat*,
                                          zfloat*, const long long*, double*, const int*, int, int, cudaStream_t);
 
-template <typename T>
-void launch_bp_sequential(int n_networks, const VDesc* vd, const int2* seq, const int* seq_ptr, const T* fac,
-                          const T* bra, T* msgs, const long long* msg_off, int maxiter, double tol, int normalize,
-                          int* iters, double* mean_diff, int ncap, int maxdeg, cudaStream_t s) {
-  (void)maxdeg;
-  const size_t sm = team_smem_bytes<T>(ncap, 3, bra != nullptr, 256);
-  auto kern = bp_sequential_kernel<T>;
-  GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  kern<<<n_networks, 256, sm, s>>>(vd, seq, seq_ptr, fac, bra, msgs, msg_off, maxiter, tol, normalize, iters, mean_diff,
-                                   ncap);
+template <typename T, typename S>
+void launch_bp_wave(const WaveJobs& wj, const VDesc* vd, const S* fac, const S* bra, S* msgs, const long long* msg_off,
+                    double* pos_diffs, const int* converged, int normalize, int want_diff, cudaStream_t s) {
+  if (wj.count == 0) return;
+  if (wj.team == 32) {
+    const size_t sm = 4 * team_smem_bytes<T>(wj.ncap, 3, bra != nullptr, 32);
+    auto kern = bp_wave_kernel<T, 32, S>;
+    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    kern<<<(wj.count + 3) / 4, 128, sm, s>>>(wj.d_jobs, wj.count, vd, fac, bra, msgs, msg_off, pos_diffs, converged,
+                                              normalize, want_diff, wj.ncap);
+  } else {
+    const size_t sm = team_smem_bytes<T>(wj.ncap, 3, bra != nullptr, 256);
+    auto kern = bp_wave_kernel<T, 256, S>;
+    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    kern<<<wj.count, 256, sm, s>>>(wj.d_jobs, wj.count, vd, fac, bra, msgs, msg_off, pos_diffs, converged, normalize,
+                                   want_diff, wj.ncap);
+  }
   GBTN_CUDA(cudaGetLastError());
 }
 
-template void launch_bp_sequential<double>(int, const VDesc*, const int2*, const int*, const double*, const double*,
-                                           double*, const long long*, int, double, int, int*, double*, int, int,
-                                           cudaStream_t);
-template void launch_bp_sequential<float>(int, const VDesc*, const int2*, const int*, const float*, const float*, float*,
-                                          const long long*, int, double, int, int*, double*, int, int, cudaStream_t);
-template void launch_bp_sequential<zdouble>(int, const VDesc*, const int2*, const int*, const zdouble*,
-                                            const zdouble*, zdouble*, const long long*, int, double, int, int*,
-                                            double*, int, int, cudaStream_t);
-template void launch_bp_sequential<zfloat>(int, const VDesc*, const int2*, const int*, const zfloat*, const zfloat*,
-                                           zfloat*, const long long*, int, double, int, int*, double*, int, int,
-                                           cudaStream_t);
+void launch_bp_wave_any(int arith, const WaveJobs& wj, const VDesc* vd, const void* fac, const void* bra, void* msgs,
+                        const long long* msg_off, double* pos_diffs, const int* converged, int normalize,
+                        int want_diff, cudaStream_t s) {
+  switch (arith) {
+    case kArithF64:
+      launch_bp_wave<double, double>(wj, vd, static_cast<const double*>(fac), static_cast<const double*>(bra),
+                                     static_cast<double*>(msgs), msg_off, pos_diffs, converged, normalize, want_diff, s);
+      break;
+    case kArithF32:
+      launch_bp_wave<float, float>(wj, vd, static_cast<const float*>(fac), static_cast<const float*>(bra),
+                                   static_cast<float*>(msgs), msg_off, pos_diffs, converged, normalize, want_diff, s);
+      break;
+    case kArithDF32:
+      launch_bp_wave<df32, double>(wj, vd, static_cast<const double*>(fac), static_cast<const double*>(bra),
+                                   static_cast<double*>(msgs), msg_off, pos_diffs, converged, normalize, want_diff, s);
+      break;
+    case kArithZ64:
+      launch_bp_wave<zdouble, zdouble>(wj, vd, static_cast<const zdouble*>(fac), static_cast<const zdouble*>(bra),
+                                       static_cast<zdouble*>(msgs), msg_off, pos_diffs, converged, normalize,
+                                       want_diff, s);
+      break;
+    case kArithZ32:
+      launch_bp_wave<zfloat, zfloat>(wj, vd, static_cast<const zfloat*>(fac), static_cast<const zfloat*>(bra),
+                                     static_cast<zfloat*>(msgs), msg_off, pos_diffs, converged, normalize, want_diff,
+                                     s);
+      break;
+    default:
+      throw std::logic_error("wave kernel: unknown arithmetic");
+  }
+}
 
 void launch_reduce_diffs(int n_networks, const int* net_de_ptr, const int* net_de, const double* diffs, double tol,
                          int* converged, int* iters, double* mean_diff, cudaStream_t s, int stall, double* best,

@@ -202,11 +202,19 @@ void launch_large_rdm_any(int arith, const LargeArgs<double>& a, int nverts, int
                           void* partial, long long vstride, void* rdm, const long long* rdm_off, cudaStream_t s);
 size_t large_elem_size(int arith);
 
-template <typename T>
-void launch_bp_sequential(int n_networks, const VDesc* vd, const int2* seq, const int* seq_ptr,
-                          const T* fac, const T* bra, T* msgs, const long long* msg_off,
-                          int maxiter, double tol, int normalize, int* iters, double* mean_diff,
-                          int ncap, int maxdeg, cudaStream_t s);
+// One wave of the sequential schedule (bp_kernels.cu): jobs (vertex, leg,
+// sequence position, network), one message each, in place; team 32 (four jobs
+// per block) or 256 threads per job, shared memory for tensors of ncap elements.
+struct WaveJobs {
+  const int4* d_jobs = nullptr;
+  int count = 0;
+  int team = 32;
+  int ncap = 0;
+};
+void launch_bp_wave_any(int arith, const WaveJobs& wj, const VDesc* vd, const void* fac, const void* bra, void* msgs,
+                        const long long* msg_off, double* pos_diffs, const int* converged, int normalize,
+                        int want_diff, cudaStream_t s);
+
 
 void launch_reduce_diffs(int n_networks, const int* net_de_ptr, const int* net_de, const double* diffs,
                          double tol, int* converged, int* iters, double* mean_diff, cudaStream_t s,

@@ -127,6 +127,7 @@ SIGNATURES = {
     "gbtn_init_messages": (_I, [_P, _I]),
     "gbtn_bp_run": (_I, [_P, C.POINTER(BPOpts), _I32, _D]),
     "gbtn_plan_phase_sweeps": (_I, [_P, _I32]),
+    "gbtn_plan_counters": (_I, [_P, C.POINTER(C.c_int64)]),
     "gbtn_updated_message": (_I, [_P, C.c_int32, _D]),
     "gbtn_vertex_rdms": (_I, [_P, _D]),
     "gbtn_expect1": (_I, [_P, _D, _I, _D]),

@@ -13,7 +13,9 @@ the per-link identities, and the Frobenius norm and message_diff do not see
 the fusion.  The coarse tensors are contracted once here (the partition
 contraction the reference repeats in every update); sweeps, environments and
 scalars run on the GPU through the ordinary cache, within its limits
-(fused site dimension <= 8, fused bond dimension <= 8).
+(fused site and bond dimensions <= 64; above 8 they run the global-memory
+path, so square blocks of four sites at chi = 2 and columns of up to six
+sites at d = chi = 2 are in reach).
 
 Fusion order: the sites of a partition in the order given, the first fastest;
 the crossing edges of a neighbouring pair by ascending edge id, the first

@@ -5,7 +5,18 @@
 # extension (weakdep GB300TensorNetworks in ITensorNetworks' Project.toml,
 # `[extensions] ITensorNetworksGB300Ext = "GB300TensorNetworks"`).
 #
-# It adds the algorithm "gb300_bp": `update(bpc; alg="gb300_bp", maxiter, tol,
+# Its main type is `GB300BeliefPropagationCache <: AbstractBeliefPropagationCache`
+# (the interface of src/caches/abstractbeliefpropagationcache.jl:44-69), made by
+# `initialize_cache(Algorithm("gb300_bp"), tn)` and so picked up by every
+# `alg`+`cache!` entry point of the reference (expect.jl:21-41,
+# environment.jl:21-39, contract.jl:41-58, normalize.jl:63-80).  It keeps one
+# library plan alive for its whole life: the tensors are uploaded once (again
+# only after `bpc[v] = t`), the messages stay on the GPU between `update`,
+# `expect`, `logscalar`, `region_scalar`, `rescale` and `normalize`, and a
+# host copy of the messages is made only when `messages(bpc)` or
+# `environment(bpc, verts)` asks for ITensors.
+#
+# For a plain BeliefPropagationCache it also adds `update(bpc; alg="gb300_bp", maxiter, tol,
 # schedule, edge_sequence, precision)` (the reference's defaults: sequential
 # sweeps in default_bp_edge_sequence order, maxiter 1 on trees and required
 # otherwise) packs the cache's partitioned tensor network into the
@@ -31,12 +42,17 @@
 module ITensorNetworksGB300Ext
 
 using ITensorNetworks: ITensorNetworks, AbstractBeliefPropagationCache, BeliefPropagationCache,
-    messages, set_messages, partitioned_tensornetwork, quotientedges, tensornetwork
+    QuadraticFormNetwork, messages, set_messages, partitioned_tensornetwork, quotientedges, tensornetwork,
+    ket_vertex, bra_vertex
+using DataGraphs: DataGraphs
+using Dictionaries: Dictionary, set!
+using ITensors: Op
 using ITensors: ITensors, ITensor, Index, inds, commonind, hascommoninds, array, itensor, dag, prime, tags
-using LinearAlgebra: norm
+using LinearAlgebra: LinearAlgebra, norm
 using NDTensors: Algorithm, @Algorithm_str
 using Graphs: src, dst
-using NamedGraphs.PartitionedGraphs: QuotientEdge, quotientvertices
+using NamedGraphs.PartitionedGraphs: PartitionedGraphs, PartitionedGraph, QuotientEdge, QuotientVertex,
+    quotientvertices, quotient_graph, unpartitioned_graph
 using GB300TensorNetworks: libgbtn
 using ChainRulesCore: ChainRulesCore, NoTangent
 
@@ -200,6 +216,298 @@ function ITensorNetworks.update(alg::Algorithm"gb300_bp", bpc::BeliefPropagation
     return bpc
 end
 
+
+# ---- the GPU-resident cache ----------------------------------------------------
+
+# One library plan and the host-side maps of a packed form network; the
+# finalizer frees the device storage.
+mutable struct GB300Plan
+    handle::Ptr{Cvoid}
+    p::Any          # pack(): vertex and edge maps, leg order, host tensor arrays
+    uploaded::Bool  # the device tensors match the cache's
+end
+
+function GB300Plan(p)
+    ctx = context()
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve p begin
+        desc = GraphDesc(length(p.pvs), length(p.pes), pointer(p.eu), pointer(p.ev), pointer(p.edim),
+            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, p.shared ? 0 : 1,
+            p.cplx ? 1 : 0)
+        check(ctx, ccall((:gbtn_plan_create, libgbtn), Cint, (Ptr{Cvoid}, Ref{GraphDesc}, Ref{Ptr{Cvoid}}),
+            ctx, desc, h))
+    end
+    plan = GB300Plan(h[], p, false)
+    finalizer(plan) do x
+        x.handle == C_NULL || ccall((:gbtn_plan_destroy, libgbtn), Cint, (Ptr{Cvoid},), x.handle)
+        x.handle = C_NULL
+    end
+    return plan
+end
+
+"""
+    GB300BeliefPropagationCache
+
+A BP cache whose messages live on the GPU (libgbtn plan).  Implements the
+reference's cache interface (abstractbeliefpropagationcache.jl:44-69) and is
+updated in place: `update` returns the same object.
+"""
+struct GB300BeliefPropagationCache{V, PV, PTN} <: AbstractBeliefPropagationCache{V, PV}
+    partitioned_tensornetwork::PTN
+    plan::GB300Plan
+    host_messages::Base.RefValue{Any}  # Dictionary mirrored from the device, nothing when stale
+end
+
+function GB300BeliefPropagationCache(ptn::PTN, plan::GB300Plan) where {PTN}
+    V = eltype(ITensorNetworks.vertices(ptn))
+    PV = eltype(quotientvertices(ptn))
+    return GB300BeliefPropagationCache{V, PV, PTN}(ptn, plan, Ref{Any}(nothing))
+end
+
+ITensorNetworks.partitioned_tensornetwork(bpc::GB300BeliefPropagationCache) = bpc.partitioned_tensornetwork
+ITensorNetworks.default_update_alg(::GB300BeliefPropagationCache) = "gb300_bp"
+ITensorNetworks.default_message_update_alg(::GB300BeliefPropagationCache) = "contract"
+ITensorNetworks.partitions(bpc::GB300BeliefPropagationCache) = quotientvertices(bpc.partitioned_tensornetwork)
+PartitionedGraphs.quotientedges(bpc::GB300BeliefPropagationCache) = quotientedges(bpc.partitioned_tensornetwork)
+function PartitionedGraphs.partitioned_vertices(bpc::GB300BeliefPropagationCache)
+    return PartitionedGraphs.partitioned_vertices(bpc.partitioned_tensornetwork)
+end
+function ITensorNetworks.default_bp_maxiter(bpc::GB300BeliefPropagationCache)
+    return ITensorNetworks.default_bp_maxiter(quotient_graph(bpc.partitioned_tensornetwork))
+end
+function ITensorNetworks.default_bp_edge_sequence(bpc::GB300BeliefPropagationCache)
+    return ITensorNetworks.default_edge_sequence(bpc.partitioned_tensornetwork)
+end
+
+# bpc[v] = t (update_factor): the tensor network changes on the host and the
+# device copy is refreshed before the next library call.
+function DataGraphs.set_vertex_data!(bpc::GB300BeliefPropagationCache, value, vertex)
+    DataGraphs.set_vertex_data!(tensornetwork(bpc), value, vertex)
+    bpc.plan.uploaded = false
+    return bpc
+end
+
+# Upload the tensors once, and again only after they changed.
+function device_plan(bpc::GB300BeliefPropagationCache)
+    plan = bpc.plan
+    if !plan.uploaded
+        p = pack(bpc)  # the current tensors, same vertex / edge / leg order as the plan
+        plan.p = merge(plan.p, (; data=p.data, bdata=p.bdata))
+        GC.@preserve p check(context(), ccall((:gbtn_set_factors, libgbtn), Cint,
+            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint), plan.handle, p.data,
+            plan.p.shared ? C_NULL : pointer(p.bdata), 0))
+        plan.uploaded = true
+    end
+    return plan.handle
+end
+
+function ITensorNetworks.initialize_cache(alg::Algorithm"gb300_bp", tn;
+                                          partitioned_vertices=ITensorNetworks.default_partitioned_vertices(tn),
+                                          messages=nothing)
+    ptn = PartitionedGraph(tn, partitioned_vertices)
+    bpc = GB300BeliefPropagationCache(ptn, GB300Plan(pack_ptn(ptn)))
+    h = device_plan(bpc)
+    if isnothing(messages)
+        check(context(), ccall((:gbtn_init_messages, libgbtn), Cint, (Ptr{Cvoid}, Cint), h, 0))  # identity
+    else
+        ITensorNetworks.set_messages!(bpc, messages)
+    end
+    return bpc
+end
+
+function Base.copy(bpc::GB300BeliefPropagationCache)
+    ptn = copy(bpc.partitioned_tensornetwork)
+    new = GB300BeliefPropagationCache(ptn, GB300Plan(bpc.plan.p))
+    flat = device_messages(bpc)
+    check(context(), ccall((:gbtn_set_messages, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint),
+        device_plan(new), flat, 0))
+    return new
+end
+
+function device_messages(bpc::GB300BeliefPropagationCache)
+    p = bpc.plan.p
+    flat = Vector{eltype(p.data)}(undef, 2 * sum(Int(c)^2 for c in p.edim; init=0))
+    check(context(), ccall((:gbtn_get_messages, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint),
+        device_plan(bpc), flat, 0))
+    return flat
+end
+
+# messages(bpc): ITensors made from the device messages (one host copy per
+# state; directed edge 2e = u->v, 2e+1 = v->u; M[b, a], b the bra link)
+function ITensorNetworks.messages(bpc::GB300BeliefPropagationCache)
+    isnothing(bpc.host_messages[]) || return bpc.host_messages[]
+    p = bpc.plan.p
+    flat = device_messages(bpc)
+    out = Dictionary{QuotientEdge, Vector{ITensor}}()
+    off = 0
+    for (e, pe) in enumerate(p.pes), qe in (pe, reverse(pe))
+        c = Int(p.edim[e])
+        M = convert(Matrix{p.elt}, reshape(flat[(off + 1):(off + c * c)], c, c))
+        off += c * c
+        set!(out, qe, [itensor(M, dag(prime(p.links[e])), p.links[e])])
+    end
+    bpc.host_messages[] = out
+    return out
+end
+
+function ITensorNetworks.set_messages!(bpc::GB300BeliefPropagationCache, ms)
+    p = bpc.plan.p
+    flat = similar(p.data, 2 * sum(Int(c)^2 for c in p.edim; init=0))
+    off = 0
+    for (e, pe) in enumerate(p.pes), qe in (pe, reverse(pe))
+        c = Int(p.edim[e])
+        flat[(off + 1):(off + c * c)] = vec(array(only(ms[qe]), dag(prime(p.links[e])), p.links[e]))
+        off += c * c
+    end
+    check(context(), ccall((:gbtn_set_messages, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint),
+        device_plan(bpc), flat, 0))
+    bpc.host_messages[] = nothing
+    return bpc
+end
+
+function ITensorNetworks.set_default_kwargs(alg::Algorithm"gb300_bp", bpc::GB300BeliefPropagationCache)
+    maxiter = get(alg.kwargs, :maxiter, ITensorNetworks.default_bp_maxiter(bpc))
+    edge_sequence = get(alg.kwargs, :edge_sequence, ITensorNetworks.default_bp_edge_sequence(bpc))
+    return Algorithm("gb300_bp"; maxiter, edge_sequence, tol=get(alg.kwargs, :tol, nothing),
+        schedule=get(alg.kwargs, :schedule, "sequential"), precision=get(alg.kwargs, :precision, nothing),
+        verbose=get(alg.kwargs, :verbose, false))
+end
+
+# update(::Algorithm"bp") with the sweeps on the GPU; the cache is updated in
+# place and returned (abstractbeliefpropagationcache.jl:313-337)
+function ITensorNetworks.update(alg::Algorithm"gb300_bp", bpc::GB300BeliefPropagationCache)
+    p = bpc.plan.p
+    maxiter = alg.kwargs.maxiter
+    isnothing(maxiter) && error("You need to specify a number of iterations for BP!")
+    sched = Dict("sequential" => 0, "parallel" => 1, "colored" => 2)[alg.kwargs.schedule]
+    seq = Int32[]
+    if sched == 0
+        de = Dict((p.eu[k], p.ev[k]) => Int32(2 * (k - 1)) for k in eachindex(p.pes))
+        for qe in alg.kwargs.edge_sequence
+            a, b = Int32(p.vid[src(qe)]), Int32(p.vid[dst(qe)])
+            push!(seq, haskey(de, (a, b)) ? de[(a, b)] : de[(b, a)] + Int32(1))
+        end
+    end
+    single = real(p.elt) === Float32
+    prec = Dict("f64" => 0, "f32" => 1, "bf16" => 2, "mixed" => 3, "df32" => 4)[something(alg.kwargs.precision,
+        single ? "f32" : "f64")]
+    tol = something(alg.kwargs.tol, -1.0)
+    opts = BPOpts(sched, prec, maxiter, 1, tol, isempty(seq) ? C_NULL : pointer(seq), length(seq),
+        0.0, 0.0, 0, 0, 0, 0, 0)
+    iters = Ref{Int32}(0)
+    diff = Ref{Float64}(0.0)
+    GC.@preserve seq check(context(), ccall((:gbtn_bp_run, libgbtn), Cint,
+        (Ptr{Cvoid}, Ref{BPOpts}, Ref{Int32}, Ref{Float64}), device_plan(bpc), opts, iters, diff))
+    if alg.kwargs.verbose && tol >= 0 && diff[] <= tol
+        println("BP converged to desired precision after $(iters[]) iterations.")
+    end
+    bpc.host_messages[] = nothing
+    return bpc
+end
+
+function ITensorNetworks.environment(bpc::GB300BeliefPropagationCache, verts::Vector; kwargs...)
+    pvs = ITensorNetworks.quotientvertices(bpc, verts)
+    ms = ITensorNetworks.incoming_messages(bpc, pvs; kwargs...)
+    central = ITensorNetworks.factors(bpc, setdiff(ITensorNetworks.vertices(bpc, pvs), verts))
+    return vcat(ms, central)
+end
+
+# region scalars from the device: tr(rho_v) per partition, <m_e, m_ebar> per edge
+function device_scalars(bpc::GB300BeliefPropagationCache, which::Symbol)
+    p = bpc.plan.p
+    n = which === :vertex ? length(p.pvs) : length(p.pes)
+    out = Vector{p.cplx ? ComplexF64 : Float64}(undef, max(n, 1))
+    f = which === :vertex ? :gbtn_vertex_scalars : :gbtn_edge_scalars
+    check(context(), ccall((f, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), device_plan(bpc), out))
+    return out
+end
+function ITensorNetworks.region_scalar(bpc::GB300BeliefPropagationCache, pv::QuotientVertex; kwargs...)
+    return device_scalars(bpc, :vertex)[bpc.plan.p.vid[pv] + 1]
+end
+function ITensorNetworks.region_scalar(bpc::GB300BeliefPropagationCache, pe::QuotientEdge; kwargs...)
+    p = bpc.plan.p
+    k = findfirst(e -> e == pe || e == reverse(pe), p.pes)
+    return device_scalars(bpc, :edge)[k]
+end
+function ITensorNetworks.vertex_scalars(bpc::GB300BeliefPropagationCache, pvs=ITensorNetworks.partitions(bpc);
+                                        kwargs...)
+    vs = device_scalars(bpc, :vertex)
+    return [vs[bpc.plan.p.vid[pv] + 1] for pv in pvs]
+end
+
+# logscalar(bpc) (abstractbeliefpropagationcache.jl:397-408), FP64 on the device
+function ITensorNetworks.logscalar(bpc::GB300BeliefPropagationCache)
+    re, im = Ref{Float64}(0.0), Ref{Float64}(0.0)
+    check(context(), ccall((:gbtn_logscalar, libgbtn), Cint, (Ptr{Cvoid}, Ref{Float64}, Ref{Float64}),
+        device_plan(bpc), re, im))
+    return im[] == 0 ? re[] : complex(re[], im[])
+end
+
+# rescale(bpc; verts) = rescale_messages then rescale_partitions
+# (abstractbeliefpropagationcache.jl:349-395) on the device; the rescaled
+# tensors are read back into the cache's network (normalize.jl:63-80 returns
+# its ket network).
+function ITensorNetworks.rescale(bpc::GB300BeliefPropagationCache; kwargs...)
+    h = device_plan(bpc)
+    check(context(), ccall((:gbtn_rescale_messages, libgbtn), Cint, (Ptr{Cvoid},), h))
+    check(context(), ccall((:gbtn_rescale_partitions, libgbtn), Cint, (Ptr{Cvoid},), h))
+    p = bpc.plan.p
+    flat = similar(p.data)
+    check(context(), ccall((:gbtn_get_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint), h, flat, 0))
+    tn = tensornetwork(bpc)
+    off = 0
+    for (i, pv) in enumerate(p.pvs)
+        v = parent(pv)
+        t = tn[(v, "ket")]
+        s = only(filter(j -> !(j in p.links), inds(t)))
+        ls = filter(j -> j in p.links, collect(inds(t)))
+        len = length(t)
+        knew = itensor(convert(Array{eltype(t)}, reshape(flat[(off + 1):(off + len)], length(s), length.(ls)...)),
+            s, ls...)
+        off += len
+        DataGraphs.set_vertex_data!(tn, knew, (v, "ket"))
+        DataGraphs.set_vertex_data!(tn, dag(prime(knew)), (v, "bra"))
+    end
+    bpc.plan.uploaded = true  # the device already holds these tensors
+    bpc.host_messages[] = nothing
+    return bpc
+end
+
+# expect(alg, psi, ops; cache!) (expect.jl:21-41) with every one-site <O_v> =
+# tr(rho_v O)/tr(rho_v) from the device (gbtn_expect1)
+function ITensorNetworks.expect(alg::Algorithm"gb300_bp", ψ::ITensorNetworks.AbstractITensorNetwork, ops;
+                                (cache!)=nothing, update_cache=isnothing(cache!), cache_update_kwargs=(;),
+                                cache_construction_kwargs=(;), kwargs...)
+    ψIψ = QuadraticFormNetwork(ψ)
+    if isnothing(cache!)
+        cache! = Ref(ITensorNetworks.initialize_cache(alg, ψIψ; cache_construction_kwargs...))
+    end
+    update_cache && (cache![] = ITensorNetworks.update(cache![]; cache_update_kwargs...))
+    bpc = cache![]
+    p = bpc.plan.p
+    out = Float64[]
+    for o in (ops isa Op ? [ops] : ops)
+        v = only(o.sites)
+        i = p.vid[only(filter(pv -> parent(pv) == v, p.pvs))]
+        s = ITensorNetworks.siteinds(ψ)[v] |> only
+        M = zeros(Float64, sum(Int(d)^2 for d in p.sdim))
+        offs = cumsum(vcat(0, Int.(p.sdim) .^ 2))
+        for (j, d) in enumerate(p.sdim)  # identity elsewhere; only vertex i is read
+            M[(offs[j] + 1):offs[j + 1]] = vec(Matrix{Float64}(LinearAlgebra.I, Int(d), Int(d)))
+        end
+        M[(offs[i + 1] + 1):offs[i + 2]] = vec(real(array(ITensors.op(o.which_op, s), prime(s), s)))
+        res = zeros(Float64, length(p.pvs))
+        check(context(), ccall((:gbtn_expect1, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Float64}, Cint, Ptr{Float64}),
+            device_plan(bpc), M, 1, res))
+        push!(out, res[i + 1])
+    end
+    return ops isa Op ? only(out) : out
+end
+
+# Pack a partitioned form network (one site partition per vertex: its ket,
+# operator and bra) in the ABI layout; same as pack(bpc) for a cache.
+pack_ptn(ptn) = pack(BeliefPropagationCache(ptn))
+pack(bpc::GB300BeliefPropagationCache) = pack_ptn(bpc.partitioned_tensornetwork)
 
 # ---- simple update (apply / tebd) -------------------------------------------
 

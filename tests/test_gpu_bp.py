@@ -183,7 +183,7 @@ def test_argument_errors_map_to_reference_errors():
         bpc.update()
     with pytest.raises(gbtn.InvalidArgument):
         bpc.update(maxiter=2, edge_sequence=[0, 1, 999])
-    big = gbtn.random_network(gbtn.square_lattice(2, 2, chi=9), 1)
+    big = gbtn.random_network(gbtn.square_lattice(2, 2, chi=65), 1)  # bond dimensions run up to 64
     with pytest.raises(gbtn.Unsupported):
         gbtn.BeliefPropagationCache(big)
 

@@ -173,6 +173,9 @@ def test_shapes_beyond_the_kernels_are_unsupported():
     star9 = gbtn.random_network(gbtn.TensorNetwork(10, [(0, k) for k in range(1, 10)], [2] * 10, [2] * 9), 1)
     with pytest.raises(gbtn.Unsupported, match="degree"):
         gbtn.BeliefPropagationCache(star9)
-    big = gbtn.random_network(gbtn.square_lattice(3, 3, chi=8, d=4), 2)  # centre: 4 * 8^4 = 16384 entries
-    with pytest.raises(gbtn.Unsupported):
+    big = gbtn.random_network(gbtn.square_lattice(2, 2, chi=2, d=65), 2)  # site dimensions run up to 64
+    with pytest.raises(gbtn.Unsupported, match="site dimension"):
         gbtn.BeliefPropagationCache(big)
+    # a tensor the shared-memory kernels cannot hold runs the global-memory path
+    ok = gbtn.random_network(gbtn.square_lattice(3, 3, chi=8, d=4), 2)  # centre: 4 * 8^4 = 16384 entries
+    gbtn.BeliefPropagationCache(ok).update(maxiter=2, schedule="parallel").close()

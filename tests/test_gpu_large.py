@@ -113,6 +113,5 @@ def test_large_complex_f64_sweep():
 
 
 def test_refused_beyond_the_large_path():
-    g = O.square_lattice(2, 2, chi=65)
-    with pytest.raises(gbtn.Unsupported):
-        gbtn.BeliefPropagationCache(gbtn.TensorNetwork(g.nv, g.edges, g.site_dims, g.edge_dims))
+    with pytest.raises(gbtn.Unsupported, match="bond dimension"):
+        gbtn.BeliefPropagationCache(gbtn.random_network(gbtn.square_lattice(2, 2, chi=65), 1))

@@ -84,8 +84,10 @@ def test_column_partitioned_bp_is_exact_oracle(L):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("L", [2, 3])
+@pytest.mark.parametrize("L", [2, 3, 4])
 def test_column_partitioned_bp_is_exact_gpu(lib_built, L):
+    # L = 4: fused site dimension 16 and crossing bonds of dimension 16 run the
+    # global-memory path (test/test_expect.jl:28-39 uses columns of the grid)
     tn, g, A = grid(L, 2, 10 + L)
     pc = gbtn.partitioned_cache(tn, columns(L)).update(maxiter=20, schedule="parallel")
     exact, nrm = exact_sz_and_norm(g, A)
@@ -107,4 +109,26 @@ def test_domino_partitions_on_a_loopy_grid_gpu(lib_built):
     rdms = cg.site_rdms([O.vertex_rdm(gc, cg.coarse.tensors, cg.coarse.tensors, m, i) for i in range(gc.nv)])
     ref = [np.sum(r * O.SZ) / np.trace(r) for r in rdms]
     np.testing.assert_allclose(pc.expect(O.SZ), ref, rtol=1e-10, atol=1e-12)
+    pc.close()
+
+
+@pytest.mark.gpu
+def test_square_block_partitions_on_a_loopy_grid_gpu(lib_built):
+    # 6x6 grid in 2x2 blocks: a loopy 3x3 partition graph with fused site
+    # dimension 16 and crossing bonds of dimension 4, against the oracle's BP
+    # on the same coarse network
+    L = 6
+    tn, g, A = grid(L, 2, 47)
+    parts = [[i + L * j, i + 1 + L * j, i + L * (j + 1), i + 1 + L * (j + 1)]
+             for j in range(0, L, 2) for i in range(0, L, 2)]
+    pc = gbtn.partitioned_cache(tn, parts).update(maxiter=200, schedule="parallel")
+    cg = pc.cg
+    assert set(cg.coarse.site_dims) == {16} and set(cg.coarse.edge_dims) == {4}
+    gc = as_graph(cg.coarse)
+    m, _, _ = O.bp_update(gc, cg.coarse.tensors, O.identity_messages(gc), maxiter=200, schedule="parallel")
+    rdms = cg.site_rdms([O.vertex_rdm(gc, cg.coarse.tensors, cg.coarse.tensors, m, i) for i in range(gc.nv)])
+    ref = [np.sum(r * O.SZ) / np.trace(r) for r in rdms]
+    np.testing.assert_allclose(pc.expect(O.SZ), ref, rtol=1e-10, atol=1e-12)
+    assert pc.logscalar() == pytest.approx(float(np.real(O.logscalar(gc, cg.coarse.tensors, cg.coarse.tensors, m))),
+                                           rel=1e-10)
     pc.close()
