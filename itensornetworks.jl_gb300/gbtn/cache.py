@@ -160,8 +160,12 @@ class BeliefPropagationCache:
         o.tol = -1.0 if tol is None else float(tol)
         seq = None
         if schedule == "sequential":
-            seq = np.ascontiguousarray(default_edge_sequence(self.tn) if edge_sequence is None else edge_sequence,
-                                       dtype=np.int32)
+            if edge_sequence is None:
+                if getattr(self, "_default_seq", None) is None:  # the graph is fixed for the cache's life
+                    self._default_seq = np.ascontiguousarray(default_edge_sequence(self.tn), dtype=np.int32)
+                seq = self._default_seq
+            else:
+                seq = np.ascontiguousarray(edge_sequence, dtype=np.int32)
             o.edge_sequence = iptr(seq)
             o.edge_sequence_len = len(seq)
         else:

@@ -4,7 +4,7 @@ product in message_diff.  FP64 path: messages after a fixed number of sweeps
 to 1e-10 (every schedule), <Sz> and the complex log-scalar to 1e-10,
 exactness on a tree, inner products with a separate bra.  FP32 path (complex
 FP32 elements, the ComplexF32 case): messages after a fixed number of sweeps
-to 1e-5 (parallel, coloured; 5e-5 sequential, whose updates compound within
+to 1e-5 (parallel, coloured; 2e-5 after two sequential sweeps, whose updates compound within
 a sweep; FP32 keeps 24 significant bits); the mixed pipeline
 (complex FP32 sweeps, then FP64 ones to tol) reaches the FP64 fixed point to
 1e-10.  Two-site RDMs and <O_u O_v> (1e-10, RDMs compared after trace
@@ -97,14 +97,17 @@ def test_complex_inner_with_separate_bra_on_a_tree():
 def test_complex_fp32_messages_match_oracle(schedule):
     g = O.square_lattice(4, 4, chi=3)
     tn, A = cnet(g, 3)
-    n = 4
+    # in a sequential sweep each update feeds the next, and on this
+    # non-converging network FP32 rounding grows along the chain: a complex64
+    # emulation of the sweep with FP32-level perturbations of the summation
+    # order ends 1.5e-5 to 2.6e-3 from the FP64 result after four sweeps,
+    # below 2e-7 after one and 4e-6 after two -- so two sweeps, 2e-5
+    n = 2 if schedule == "sequential" else 4
     ref, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=n, schedule=schedule)
     bpc = gbtn.BeliefPropagationCache(tn).update(maxiter=n, schedule=schedule, precision="f32")
     got = bpc.messages()
     err = max(np.max(np.abs(got[de] - ref[de])) for de in range(2 * g.ne))
-    # in a sequential sweep each update feeds the next, so FP32 rounding
-    # compounds along the 48-message chain of this (non-converging) network
-    tol = 5e-5 if schedule == "sequential" else 1e-5
+    tol = 2e-5 if schedule == "sequential" else 1e-5
     assert err < tol, f"{schedule}: {err:.3e}"
     assert err > 1e-12  # the sweeps really ran in FP32
 

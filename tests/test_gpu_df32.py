@@ -99,8 +99,9 @@ def test_mixed_default_refinement_is_df32_and_converges():
 
 def test_df32_refused_where_it_has_no_path():
     g = O.square_lattice(3, 3, chi=2)
-    A = O.random_network(g, 1)
-    bpc = gbtn.BeliefPropagationCache(net(g, A))
+    # sequential double-FP32 sweeps on a plan with a vertex of the global-memory path
+    gl = O.square_lattice(3, 3, chi=10)
+    bpc = gbtn.BeliefPropagationCache(net(gl, O.random_network(gl, 1)))
     with pytest.raises(gbtn.Unsupported):
         bpc.update(maxiter=2, schedule="sequential", precision="df32")
     bpc.close()
