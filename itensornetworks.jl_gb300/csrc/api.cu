@@ -366,10 +366,13 @@ void ensure_f32(gbtn_plan* P) {
   }
 }
 
+// Shared memory of one team of the SIMT kernels for a tensor of n elements
+// (padded layout: one unused element per 32, see spos in bp_device.cuh).
 size_t smem_need(int n, int k, bool sep_bra, size_t elt, int team) {
   const int nbuf = k <= 4 ? 3 : kNumBufs;
+  const size_t np = (size_t)n + (n >> 5) + 1;
   size_t b = (sizeof(VDesc) + 15) / 16 * 16;
-  b += elt * ((size_t)n * (nbuf + (sep_bra ? 1 : 0)) + kMaxDeg * 64 + (team / 32) * 64 + 64);
+  b += elt * (np * (nbuf + (sep_bra ? 1 : 0)) + kMaxDeg * 64 + (team / 32) * 64 + 64);
   return (b + 15) / 16 * 16;
 }
 

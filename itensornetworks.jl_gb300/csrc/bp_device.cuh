@@ -155,7 +155,21 @@ __device__ __forceinline__ void warp_reduce_scatter(T (&v)[P2], int lane) {
   }
 }
 
-template <typename T, int CHI>
+// Shared-memory position of tensor element i.  With PAD one unused element
+// follows every 32: the fibers of the innermost legs (strides 2 and 16 at
+// d = 2, chi = 8) then spread a warp over many banks instead of 2-4 (an
+// 8-way conflict on leg 0 without it).  padded_len(n) elements hold a padded
+// tensor of n elements.
+template <bool PAD>
+__device__ __forceinline__ int spos(int i) {
+  if constexpr (PAD)
+    return i + (i >> 5);
+  else
+    return i;
+}
+__host__ __device__ inline int padded_len(int n) { return n + (n >> 5) + 1; }
+
+template <typename T, int CHI, bool PAD = false>
 __device__ __forceinline__ void absorb_fibers(const T* __restrict__ in, T* __restrict__ out, int n, int st,
                                               const T* __restrict__ M, int tid, int nth) {
   T m[CHI][CHI];
@@ -169,29 +183,29 @@ __device__ __forceinline__ void absorb_fibers(const T* __restrict__ in, T* __res
     const int base = lo + (f - lo) * CHI;
     T x[CHI];
 #pragma unroll
-    for (int a = 0; a < CHI; ++a) x[a] = in[base + a * st];
+    for (int a = 0; a < CHI; ++a) x[a] = in[spos<PAD>(base + a * st)];
 #pragma unroll
     for (int b = 0; b < CHI; ++b) {
       T y = T(0);
 #pragma unroll
       for (int a = 0; a < CHI; ++a) y = mac(m[b][a], x[a], y);
-      out[base + b * st] = settle(y);
+      out[spos<PAD>(base + b * st)] = settle(y);
     }
   }
 }
 
-template <typename T>
+template <typename T, bool PAD = false>
 __device__ __forceinline__ void absorb_any(int chi, const T* in, T* out, int n, int st, const T* M, int tid,
                                            int nth) {
   switch (chi) {
-    case 1: absorb_fibers<T, 1>(in, out, n, st, M, tid, nth); break;
-    case 2: absorb_fibers<T, 2>(in, out, n, st, M, tid, nth); break;
-    case 3: absorb_fibers<T, 3>(in, out, n, st, M, tid, nth); break;
-    case 4: absorb_fibers<T, 4>(in, out, n, st, M, tid, nth); break;
-    case 5: absorb_fibers<T, 5>(in, out, n, st, M, tid, nth); break;
-    case 6: absorb_fibers<T, 6>(in, out, n, st, M, tid, nth); break;
-    case 7: absorb_fibers<T, 7>(in, out, n, st, M, tid, nth); break;
-    case 8: absorb_fibers<T, 8>(in, out, n, st, M, tid, nth); break;
+    case 1: absorb_fibers<T, 1, PAD>(in, out, n, st, M, tid, nth); break;
+    case 2: absorb_fibers<T, 2, PAD>(in, out, n, st, M, tid, nth); break;
+    case 3: absorb_fibers<T, 3, PAD>(in, out, n, st, M, tid, nth); break;
+    case 4: absorb_fibers<T, 4, PAD>(in, out, n, st, M, tid, nth); break;
+    case 5: absorb_fibers<T, 5, PAD>(in, out, n, st, M, tid, nth); break;
+    case 6: absorb_fibers<T, 6, PAD>(in, out, n, st, M, tid, nth); break;
+    case 7: absorb_fibers<T, 7, PAD>(in, out, n, st, M, tid, nth); break;
+    case 8: absorb_fibers<T, 8, PAD>(in, out, n, st, M, tid, nth); break;
     default: break;
   }
 }
@@ -200,7 +214,7 @@ constexpr int kRedStride = 64;  // per-warp slot of the close reduction (CHI <= 
 
 // CLOSE over fibers ff = fib_add + fib_mul*f of leg (st, CHI); result
 // res[b + CHI*a] = sum bra[base+shift+b*st] * t[base+a*st] (team-wide sum).
-template <typename T, int CHI, int TEAM>
+template <typename T, int CHI, int TEAM, bool PAD = false>
 __device__ __forceinline__ void close_fibers(const T* __restrict__ t, const T* __restrict__ bra, int n, int st,
                                              int fib_mul, int fib_add, int bra_shift, T* red, T* res,
                                              int tid) {
@@ -217,8 +231,8 @@ __device__ __forceinline__ void close_fibers(const T* __restrict__ t, const T* _
     T x[CHI], y[CHI];
 #pragma unroll
     for (int a = 0; a < CHI; ++a) {
-      x[a] = t[base + a * st];
-      y[a] = conj_of(bra[base + bra_shift + a * st]);
+      x[a] = t[spos<PAD>(base + a * st)];
+      y[a] = conj_of(bra[spos<PAD>(base + bra_shift + a * st)]);
     }
 #pragma unroll
     for (int a = 0; a < CHI; ++a)
@@ -248,18 +262,18 @@ __device__ __forceinline__ void close_fibers(const T* __restrict__ t, const T* _
   tsync<TEAM>();
 }
 
-template <typename T, int TEAM>
+template <typename T, int TEAM, bool PAD = false>
 __device__ __forceinline__ void close_any(int chi, const T* t, const T* bra, int n, int st, int fib_mul,
                                           int fib_add, int bra_shift, T* red, T* res, int tid) {
   switch (chi) {
-    case 1: close_fibers<T, 1, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 2: close_fibers<T, 2, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 3: close_fibers<T, 3, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 4: close_fibers<T, 4, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 5: close_fibers<T, 5, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 6: close_fibers<T, 6, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 7: close_fibers<T, 7, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 8: close_fibers<T, 8, TEAM>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 1: close_fibers<T, 1, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 2: close_fibers<T, 2, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 3: close_fibers<T, 3, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 4: close_fibers<T, 4, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 5: close_fibers<T, 5, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 6: close_fibers<T, 6, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 7: close_fibers<T, 7, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 8: close_fibers<T, 8, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
     default: break;
   }
 }
@@ -437,15 +451,15 @@ __device__ __forceinline__ void load_desc(VDesc* dst, const VDesc* src, int tid)
 // Load the tensor (and bra) of a vertex and its incoming messages (all legs,
 // or all but skip_leg) into shared memory.
 // S is the storage type in HBM (T, or double under df32 arithmetic).
-template <typename T, int TEAM, typename S = T>
+template <typename T, int TEAM, typename S = T, bool PAD = false>
 __device__ __forceinline__ void load_vertex(const TeamSmem<T>& Sm, const S* fac, const S* bra_g, const S* msgs,
                                             const long long* msg_off, int skip_leg, int tid) {
   const VDesc& d = *Sm.desc;
   const S* a = fac + d.a_off;
-  for (int i = tid; i < d.n; i += TEAM) Sm.buf[0][i] = to_elem<T>(a[i]);
+  for (int i = tid; i < d.n; i += TEAM) Sm.buf[0][spos<PAD>(i)] = to_elem<T>(a[i]);
   if (bra_g) {
     const S* b = bra_g + d.a_off;
-    for (int i = tid; i < d.n; i += TEAM) Sm.bra[i] = to_elem<T>(b[i]);
+    for (int i = tid; i < d.n; i += TEAM) Sm.bra[spos<PAD>(i)] = to_elem<T>(b[i]);
   }
   for (int p = 0; p < d.k; ++p) {
     if (p == skip_leg) continue;

@@ -97,8 +97,8 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPB = TEAM == 32 ? 4 : 1;
   const int team = threadIdx.x / TEAM, tid = threadIdx.x % TEAM, lane = tid & 31;
-  const size_t tb = team_smem_bytes<T>(ncap, nbuf, bra_g != nullptr, TEAM);
-  TeamSmem<T> Sm = carve<T>(smem_raw + team * tb, ncap, nbuf, bra_g != nullptr, TEAM);
+  const size_t tb = team_smem_bytes<T>(padded_len(ncap), nbuf, bra_g != nullptr, TEAM);
+  TeamSmem<T> Sm = carve<T>(smem_raw + team * tb, padded_len(ncap), nbuf, bra_g != nullptr, TEAM);
   for (int w = blockIdx.x * TPB + team; w < nwork; w += gridDim.x * TPB) {
     const int v = work[w];
     load_desc<TEAM>(Sm.desc, vd + v, tid);
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
       tsync<TEAM>();
       continue;
     }
-    load_vertex<T, TEAM, S>(Sm, fac, bra_g, msg_in, msg_off, -1, tid);
+    load_vertex<T, TEAM, S, true>(Sm, fac, bra_g, msg_in, msg_off, -1, tid);
     tsync<TEAM>();
     const int k = d.k;
     const int len = c_sched.len[k];
@@ -124,10 +124,10 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
       const int leg = op.leg;
       const int chi = d.chi[leg], st = d.st[leg];
       if (op.type == 0) {
-        absorb_any<T>(chi, Sm.buf[op.src], Sm.buf[op.dst], d.n, st, Sm.msg + leg * 64, tid, TEAM);
+        absorb_any<T, true>(chi, Sm.buf[op.src], Sm.buf[op.dst], d.n, st, Sm.msg + leg * 64, tid, TEAM);
         tsync<TEAM>();
       } else {
-        close_any<T, TEAM>(chi, Sm.buf[op.src], Sm.bra, d.n, st, 1, 0, 0, Sm.red, Sm.res, tid);
+        close_any<T, TEAM, true>(chi, Sm.buf[op.src], Sm.bra, d.n, st, 1, 0, 0, Sm.red, Sm.res, tid);
         if (tid < 32) {
           const int de = d.out_de[leg];
           const long long off = msg_off[de];
@@ -159,7 +159,7 @@ __device__ __forceinline__ int chain_absorb(const TeamSmem<T>& S, int skip_leg, 
   for (int j = 0; j < d.k; ++j) {
     if (j == skip_leg) continue;
     const int nxt = cur == 1 ? 2 : 1;
-    absorb_any<T>(d.chi[j], S.buf[cur], S.buf[nxt], d.n, d.st[j], S.msg + j * 64, tid, TEAM);
+    absorb_any<T, true>(d.chi[j], S.buf[cur], S.buf[nxt], d.n, d.st[j], S.msg + j * 64, tid, TEAM);
     tsync<TEAM>();
     cur = nxt;
   }
@@ -183,19 +183,19 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPB = TEAM == 32 ? 4 : 1;
   const int team = threadIdx.x / TEAM, tid = threadIdx.x % TEAM, lane = tid & 31;
-  const size_t tb = team_smem_bytes<T>(ncap, 3, bra_g != nullptr, TEAM);
-  TeamSmem<T> Sm = carve<T>(smem_raw + team * tb, ncap, 3, bra_g != nullptr, TEAM);
+  const size_t tb = team_smem_bytes<T>(padded_len(ncap), 3, bra_g != nullptr, TEAM);
+  TeamSmem<T> Sm = carve<T>(smem_raw + team * tb, padded_len(ncap), 3, bra_g != nullptr, TEAM);
   for (int w = blockIdx.x * TPB + team; w < njobs; w += gridDim.x * TPB) {
     const int4 jb = jobs[w];  // (vertex, leg, sequence position, network)
     if (converged && converged[jb.w]) continue;  // uniform over the team
     load_desc<TEAM>(Sm.desc, vd + jb.x, tid);
     tsync<TEAM>();
-    load_vertex<T, TEAM, S>(Sm, fac, bra_g, msgs, msg_off, jb.y, tid);
+    load_vertex<T, TEAM, S, true>(Sm, fac, bra_g, msgs, msg_off, jb.y, tid);
     tsync<TEAM>();
     const int cur = chain_absorb<T, TEAM>(Sm, jb.y, tid);
     const VDesc& d = *Sm.desc;
     const int chi = d.chi[jb.y];
-    close_any<T, TEAM>(chi, Sm.buf[cur], Sm.bra, d.n, d.st[jb.y], 1, 0, 0, Sm.red, Sm.res, tid);
+    close_any<T, TEAM, true>(chi, Sm.buf[cur], Sm.bra, d.n, d.st[jb.y], 1, 0, 0, Sm.red, Sm.res, tid);
     if (tid < 32) {
       S* m = msgs + msg_off[d.out_de[jb.y]];
       double df;
@@ -218,14 +218,14 @@ __global__ void __launch_bounds__(256)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TEAM = 256;
   const int tid = threadIdx.x;
-  TeamSmem<T> S = carve<T>(smem_raw, ncap, 3, bra_g != nullptr, TEAM);
+  TeamSmem<T> S = carve<T>(smem_raw, padded_len(ncap), 3, bra_g != nullptr, TEAM);
   load_desc<TEAM>(S.desc, vd + v, tid);
   __syncthreads();
-  load_vertex<T, TEAM>(S, fac, bra_g, msgs, msg_off, leg, tid);
+  load_vertex<T, TEAM, T, true>(S, fac, bra_g, msgs, msg_off, leg, tid);
   __syncthreads();
   const int cur = chain_absorb<T, TEAM>(S, leg, tid);
   const VDesc& d = *S.desc;
-  close_any<T, TEAM>(d.chi[leg], S.buf[cur], S.bra, d.n, d.st[leg], 1, 0, 0, S.red, S.res, tid);
+  close_any<T, TEAM, true>(d.chi[leg], S.buf[cur], S.bra, d.n, d.st[leg], 1, 0, 0, S.red, S.res, tid);
   if (tid < 32) finalize_message<T>(S.res, d.chi[leg], out, out, 1, false, tid);
 }
 
@@ -244,17 +244,17 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPB = TEAM == 32 ? 4 : 1;
   const int team = threadIdx.x / TEAM, tid = threadIdx.x % TEAM;
-  const size_t tb = team_smem_bytes<T>(ncap, 3, bra_g != nullptr, TEAM);
-  TeamSmem<T> S = carve<T>(smem_raw + team * tb, ncap, 3, bra_g != nullptr, TEAM);
+  const size_t tb = team_smem_bytes<T>(padded_len(ncap), 3, bra_g != nullptr, TEAM);
+  TeamSmem<T> S = carve<T>(smem_raw + team * tb, padded_len(ncap), 3, bra_g != nullptr, TEAM);
   for (int w = blockIdx.x * TPB + team; w < nwork; w += gridDim.x * TPB) {
     const int v = work[w];
     load_desc<TEAM>(S.desc, vd + v, tid);
     tsync<TEAM>();
-    load_vertex<T, TEAM>(S, fac, bra_g, msgs, msg_off, -1, tid);
+    load_vertex<T, TEAM, T, true>(S, fac, bra_g, msgs, msg_off, -1, tid);
     tsync<TEAM>();
     const int cur = chain_absorb<T, TEAM>(S, -1, tid);
     const VDesc& d = *S.desc;
-    close_any<T, TEAM>(d.d, S.buf[cur], S.bra, d.n, 1, 1, 0, 0, S.red, S.res, tid);
+    close_any<T, TEAM, true>(d.d, S.buf[cur], S.bra, d.n, 1, 1, 0, 0, S.red, S.res, tid);
     for (int i = tid; i < d.d * d.d; i += TEAM) rdm[rdm_off[v] + i] = S.res[i];
     tsync<TEAM>();
   }
@@ -272,19 +272,19 @@ __global__ void __launch_bounds__(256)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TEAM = 256;
   const int tid = threadIdx.x;
-  TeamSmem<T> S = carve<T>(smem_raw, ncap, 3, bra_g != nullptr, TEAM);
+  TeamSmem<T> S = carve<T>(smem_raw, padded_len(ncap), 3, bra_g != nullptr, TEAM);
   for (int j = blockIdx.x; j < njobs; j += gridDim.x) {
     const int2 jb = jobs[j];
     load_desc<TEAM>(S.desc, vd + jb.x, tid);
     __syncthreads();
-    load_vertex<T, TEAM>(S, fac, bra_g, msgs, msg_off, jb.y, tid);
+    load_vertex<T, TEAM, T, true>(S, fac, bra_g, msgs, msg_off, jb.y, tid);
     __syncthreads();
     const int cur = chain_absorb<T, TEAM>(S, jb.y, tid);
     const VDesc& d = *S.desc;
     const int chi = d.chi[jb.y];
     for (int s = 0; s < d.d; ++s)
       for (int sp = 0; sp < d.d; ++sp) {
-        close_any<T, TEAM>(chi, S.buf[cur], S.bra, d.n, d.st[jb.y], d.d, s, sp - s, S.red, S.res, tid);
+        close_any<T, TEAM, true>(chi, S.buf[cur], S.bra, d.n, d.st[jb.y], d.d, s, sp - s, S.red, S.res, tid);
         for (int i = tid; i < chi * chi; i += TEAM) halves[half_off[j] + (long long)(sp + d.d * s) * chi * chi + i] = S.res[i];
         __syncthreads();
       }
@@ -641,14 +641,14 @@ void launch_bp_vertices(const WorkList& wl_all, const VDesc* vd, const T* fac, c
   if (wl.count == 0) continue;
   const int nbuf = wl.maxdeg <= 4 ? 3 : kNumBufs;
   if (wl.team == 32) {
-    const size_t sm = 4 * team_smem_bytes<T>(wl.ncap, nbuf, bra != nullptr, 32);
+    const size_t sm = 4 * team_smem_bytes<T>(padded_len(wl.ncap), nbuf, bra != nullptr, 32);
     auto kern = bp_vertex_kernel<T, 32>;
     GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const int blocks = (wl.count + 3) / 4;
     kern<<<blocks, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
                                  normalize, want_diff, wl.ncap, nbuf);
   } else {
-    const size_t sm = team_smem_bytes<T>(wl.ncap, nbuf, bra != nullptr, 256);
+    const size_t sm = team_smem_bytes<T>(padded_len(wl.ncap), nbuf, bra != nullptr, 256);
     auto kern = bp_vertex_kernel<T, 256>;
     GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     kern<<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
@@ -666,14 +666,14 @@ void launch_bp_vertices_df32(const WorkList& wl_all, const VDesc* vd, const doub
   if (wl.count == 0) continue;
   const int nbuf = wl.maxdeg <= 4 ? 3 : kNumBufs;
   if (wl.team == 32) {
-    const size_t sm = 4 * team_smem_bytes<df32>(wl.ncap, nbuf, bra != nullptr, 32);
+    const size_t sm = 4 * team_smem_bytes<df32>(padded_len(wl.ncap), nbuf, bra != nullptr, 32);
     auto kern = bp_vertex_kernel<df32, 32, double>;
     GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const int blocks = (wl.count + 3) / 4;
     kern<<<blocks, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
                                  normalize, want_diff, wl.ncap, nbuf);
   } else {
-    const size_t sm = team_smem_bytes<df32>(wl.ncap, nbuf, bra != nullptr, 256);
+    const size_t sm = team_smem_bytes<df32>(padded_len(wl.ncap), nbuf, bra != nullptr, 256);
     auto kern = bp_vertex_kernel<df32, 256, double>;
     GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     kern<<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
@@ -698,13 +698,13 @@ void launch_bp_wave(const WaveJobs& wj, const VDesc* vd, const S* fac, const S* 
                     double* pos_diffs, const int* converged, int normalize, int want_diff, cudaStream_t s) {
   if (wj.count == 0) return;
   if (wj.team == 32) {
-    const size_t sm = 4 * team_smem_bytes<T>(wj.ncap, 3, bra != nullptr, 32);
+    const size_t sm = 4 * team_smem_bytes<T>(padded_len(wj.ncap), 3, bra != nullptr, 32);
     auto kern = bp_wave_kernel<T, 32, S>;
     GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     kern<<<(wj.count + 3) / 4, 128, sm, s>>>(wj.d_jobs, wj.count, vd, fac, bra, msgs, msg_off, pos_diffs, converged,
                                               normalize, want_diff, wj.ncap);
   } else {
-    const size_t sm = team_smem_bytes<T>(wj.ncap, 3, bra != nullptr, 256);
+    const size_t sm = team_smem_bytes<T>(padded_len(wj.ncap), 3, bra != nullptr, 256);
     auto kern = bp_wave_kernel<T, 256, S>;
     GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     kern<<<wj.count, 256, sm, s>>>(wj.d_jobs, wj.count, vd, fac, bra, msgs, msg_off, pos_diffs, converged, normalize,
@@ -755,7 +755,7 @@ void launch_reduce_diffs(int n_networks, const int* net_de_ptr, const int* net_d
 template <typename T>
 void launch_updated_message(const VDesc* vd, int v, int leg, const T* fac, const T* bra, const T* msgs,
                             const long long* msg_off, T* out, int ncap, cudaStream_t s) {
-  const size_t sm = team_smem_bytes<T>(ncap, 3, bra != nullptr, 256);
+  const size_t sm = team_smem_bytes<T>(padded_len(ncap), 3, bra != nullptr, 256);
   GBTN_CUDA(cudaFuncSetAttribute(updated_message_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   updated_message_kernel<T><<<1, 256, sm, s>>>(vd, v, leg, fac, bra, msgs, msg_off, out, ncap);
   GBTN_CUDA(cudaGetLastError());
@@ -770,13 +770,13 @@ void launch_vertex_rdms(const WorkList& wl, const VDesc* vd, const T* fac, const
                         const long long* msg_off, const long long* rdm_off, T* rdm, cudaStream_t s) {
   if (wl.count == 0) return;
   if (wl.team == 32) {
-    const size_t sm = 4 * team_smem_bytes<T>(wl.ncap, 3, bra != nullptr, 32);
+    const size_t sm = 4 * team_smem_bytes<T>(padded_len(wl.ncap), 3, bra != nullptr, 32);
     auto kern = vertex_rdm_kernel<T, 32>;
     GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     kern<<<(wl.count + 3) / 4, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msgs, msg_off, rdm_off, rdm,
                                               wl.ncap);
   } else {
-    const size_t sm = team_smem_bytes<T>(wl.ncap, 3, bra != nullptr, 256);
+    const size_t sm = team_smem_bytes<T>(padded_len(wl.ncap), 3, bra != nullptr, 256);
     auto kern = vertex_rdm_kernel<T, 256>;
     GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     kern<<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msgs, msg_off, rdm_off, rdm, wl.ncap);
@@ -815,7 +815,7 @@ void launch_edge_halves(const int* jobs, int njobs, int ncap, int maxdeg, const 
                         const T* msgs, const long long* msg_off, T* halves, const long long* half_off, cudaStream_t s) {
   (void)maxdeg;
   if (njobs == 0) return;
-  const size_t sm = team_smem_bytes<T>(ncap, 3, bra != nullptr, 256);
+  const size_t sm = team_smem_bytes<T>(padded_len(ncap), 3, bra != nullptr, 256);
   GBTN_CUDA(cudaFuncSetAttribute(edge_half_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   edge_half_kernel<T><<<njobs, 256, sm, s>>>(reinterpret_cast<const int2*>(jobs), njobs, vd, fac, bra, msgs, msg_off,
                                              halves, half_off, ncap);
