@@ -335,6 +335,58 @@ int gbtn_energy2_grad(gbtn_plan* plan, int32_t n_terms, const double* coef, cons
 int gbtn_bp_vjp(gbtn_plan* plan, const double* msg_cot, const gbtn_grad_opts* opts, double* grad, int32_t* iters,
                 double* resid);
 
+/* ---- charge-conserving (QN) block-sparse networks ------------------------ */
+/* Replaces: BP on QN-conserving ITensors (ITensors' conserve_qns = true, e.g.
+ * the QN-graded loopy network of test/test_belief_propagation.jl:103-116).
+ * Every index carries sectors of one U(1) charge: the sectors of a link are
+ * contiguous ranges of its dense index (sec_dim of them, in order, summing to
+ * edge_dim), likewise those of a site index.  A vertex tensor is nonzero only
+ * in the blocks whose charges balance its flux:
+ *   charge(site sector) + sum_{legs into v} q - sum_{legs out of v} q = flux[v],
+ * where a link's sector charge q is counted out of edge_u[e] and into
+ * edge_v[e].  Messages of such a network stay block-diagonal in the link
+ * sectors, so the plan stores only the nonzero blocks of the tensors and the
+ * diagonal sector blocks of the messages, and contracts block by block.
+ * Real FP64 tensors; sector dimensions <= 8, degree <= 8; the sectors of one
+ * index carry distinct charges (merge equal-charge sectors first). */
+typedef struct gbtn_qn_desc {
+  const int32_t* edge_sec_ptr;    /* [ne+1] CSR offsets into sec_dim / sec_charge */
+  const int32_t* sec_dim;         /* link sector dimensions */
+  const int32_t* sec_charge;      /* link sector charges (out of edge_u, into edge_v) */
+  const int32_t* site_sec_ptr;    /* [nv+1] CSR offsets into site_sec_dim / site_sec_charge */
+  const int32_t* site_sec_dim;    /* site sector dimensions */
+  const int32_t* site_sec_charge; /* site sector charges */
+  const int32_t* flux;            /* [nv] flux of every vertex tensor */
+} gbtn_qn_desc;
+typedef struct gbtn_qn_plan gbtn_qn_plan;
+/* Replaces: BeliefPropagationCache / initialize_cache for a QN network. */
+int gbtn_qn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* desc, const gbtn_qn_desc* qn, gbtn_qn_plan** out);
+int gbtn_qn_plan_destroy(gbtn_qn_plan* plan);
+/* Counts: nonzero blocks, their elements, and the elements of the sector-packed messages. */
+int gbtn_qn_plan_sizes(const gbtn_qn_plan* plan, int32_t* n_blocks, int64_t* n_block_elems, int64_t* n_message);
+/* The blocks in storage order: for block i, blocks[i*10 + 0] = vertex,
+ * [i*10 + 1] = its site sector, [i*10 + 2 + p] = its sector on leg p (-1 past
+ * the degree); offsets[i] = its first element.  A block is a dense tensor of
+ * shape (site sector dim, leg sector dims...) in column-major order. */
+int gbtn_qn_blocks(const gbtn_qn_plan* plan, int32_t* blocks, int64_t* offsets);
+/* Replaces: bpc[v] = tensor for every vertex (update_factors). */
+int gbtn_qn_set_blocks(gbtn_qn_plan* plan, const double* data, int mem);
+/* Replaces: identity_messages (quadraticformnetwork.jl:96-124): the identity in every sector block. */
+int gbtn_qn_init_messages(gbtn_qn_plan* plan);
+/* Sector-packed messages: directed edge after directed edge (2e = u -> v),
+ * within one the sector blocks of its link in order, each dim x dim M[b, a]
+ * column-major (the dense message is block-diagonal with these blocks). */
+int gbtn_qn_set_messages(gbtn_qn_plan* plan, const double* msgs, int mem);
+int gbtn_qn_get_messages(gbtn_qn_plan* plan, double* msgs, int mem);
+/* Replaces: update(bpc; maxiter, tol) with the parallel (Jacobi) schedule;
+ * message_diff and its mean as the dense plan (abstractbeliefpropagationcache.jl:32-36, 313-329). */
+int gbtn_qn_bp_run(gbtn_qn_plan* plan, int32_t maxiter, double tol, int32_t* iters, double* mean_diff);
+/* Replaces: the one-site environments of expect (expect.jl:5-19): dense
+ * rho_v[s', s] (d x d, block-diagonal in the site sectors) per vertex. */
+int gbtn_qn_vertex_rdms(gbtn_qn_plan* plan, double* out);
+/* Replaces: logscalar(bpc) (abstractbeliefpropagationcache.jl:397-408). */
+int gbtn_qn_logscalar(gbtn_qn_plan* plan, double* re, double* im);
+
 /* ---- allocation-free sweep ------------------------------------------------ */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory when they need a message update (a framework capturing its stream

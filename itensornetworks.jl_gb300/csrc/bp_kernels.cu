@@ -166,6 +166,88 @@ __device__ __forceinline__ int chain_absorb(const TeamSmem<T>& S, int skip_leg, 
   return cur;
 }
 
+// ---------------------------------------------------------------------------
+// Block-sparse (U(1)-graded) networks: one job per nonzero sector block of a
+// vertex tensor.  Messages of a charge-conserving network stay block-diagonal
+// in the link sectors (flux zero), so absorbing them keeps every leg of a
+// block in its sector, and the bra block that closes a block has the same
+// sectors as the ket block.  A block's share of the outgoing message on leg p
+// (sector sigma_p) is therefore the dense update of the block alone, with the
+// sector blocks of its incoming messages; the shares of all blocks with the
+// same sector are added by qn_finalize (bp_qn.cu), which then normalises the
+// whole message.  Block descriptor fields: a_off / n / d / k / chi / st as a
+// vertex (d = site-sector dimension, chi = sector dimensions), in_de[p] = the
+// incoming (directed edge, sector) message id, out_de[p] = the block's
+// partial slot for leg p, net = its reduced-density-matrix slot.
+// mode 0: every outgoing share (the shared-prefix schedule); mode 1: the
+// block's share of rho_v (all legs absorbed, CLOSE on the site index).
+// ---------------------------------------------------------------------------
+template <int TEAM>
+__global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
+    qn_block_kernel(const int* __restrict__ work, int nwork, const VDesc* __restrict__ bd,
+                    const double* __restrict__ blocks, const double* __restrict__ msg_in,
+                    const long long* __restrict__ sec_off, double* __restrict__ partial,
+                    const long long* __restrict__ part_off, int mode, int ncap, int nbuf) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int TPB = TEAM == 32 ? 4 : 1;
+  const int team = threadIdx.x / TEAM, tid = threadIdx.x % TEAM;
+  const size_t tb = team_smem_bytes<double>(padded_len(ncap), nbuf, false, TEAM);
+  TeamSmem<double> Sm = carve<double>(smem_raw + team * tb, padded_len(ncap), nbuf, false, TEAM);
+  for (int w = blockIdx.x * TPB + team; w < nwork; w += gridDim.x * TPB) {
+    load_desc<TEAM>(Sm.desc, bd + work[w], tid);
+    tsync<TEAM>();
+    const VDesc& d = *Sm.desc;
+    load_vertex<double, TEAM, double, true>(Sm, blocks, nullptr, msg_in, sec_off, -1, tid);
+    tsync<TEAM>();
+    if (mode == 1) {
+      const int cur = chain_absorb<double, TEAM>(Sm, -1, tid);
+      close_any<double, TEAM, true>(d.d, Sm.buf[cur], Sm.bra, d.n, 1, 1, 0, 0, Sm.red, Sm.res, tid);
+      double* out = partial + part_off[d.net];
+      for (int i = tid; i < d.d * d.d; i += TEAM) out[i] = Sm.res[i];
+      tsync<TEAM>();
+      continue;
+    }
+    const int k = d.k;
+    const int len = c_sched.len[k];
+    for (int i = 0; i < len; ++i) {
+      const SchedOp op = c_sched.ops[k][i];
+      const int leg = op.leg;
+      const int chi = d.chi[leg], st = d.st[leg];
+      if (op.type == 0) {
+        absorb_any<double, true>(chi, Sm.buf[op.src], Sm.buf[op.dst], d.n, st, Sm.msg + leg * 64, tid, TEAM);
+        tsync<TEAM>();
+      } else {
+        close_any<double, TEAM, true>(chi, Sm.buf[op.src], Sm.bra, d.n, st, 1, 0, 0, Sm.red, Sm.res, tid);
+        double* out = partial + part_off[d.out_de[leg]];
+        for (int j = tid; j < chi * chi; j += TEAM) out[j] = Sm.res[j];
+        tsync<TEAM>();
+      }
+    }
+  }
+}
+
+void launch_qn_blocks(const WorkList& wl_all, const VDesc* bd, const double* blocks, const double* msg_in,
+                      const long long* sec_off, double* partial, const long long* part_off, int mode,
+                      cudaStream_t s) {
+  for (int c = 0; c < wl_all.nsubs(); ++c) {
+    const WorkList wl = wl_all.sub(c);
+    if (wl.count == 0) continue;
+    const int nbuf = wl.maxdeg <= 4 ? 3 : kNumBufs;
+    if (wl.team == 32) {
+      const size_t sm = 4 * team_smem_bytes<double>(padded_len(wl.ncap), nbuf, false, 32);
+      GBTN_CUDA(cudaFuncSetAttribute(qn_block_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      qn_block_kernel<32><<<(wl.count + 3) / 4, 128, sm, s>>>(wl.d_vertices, wl.count, bd, blocks, msg_in, sec_off,
+                                                              partial, part_off, mode, wl.ncap, nbuf);
+    } else {
+      const size_t sm = team_smem_bytes<double>(padded_len(wl.ncap), nbuf, false, 256);
+      GBTN_CUDA(cudaFuncSetAttribute(qn_block_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      qn_block_kernel<256><<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, bd, blocks, msg_in, sec_off, partial,
+                                                     part_off, mode, wl.ncap, nbuf);
+    }
+    GBTN_CUDA(cudaGetLastError());
+  }
+}
+
 // One wave of the sequential schedule: every job (vertex, leg, sequence
 // position, network) computes one message in place from the current messages
 // (absorb chain of the other legs, CLOSE on the leg, normalisation) and

@@ -202,6 +202,13 @@ void launch_large_rdm_any(int arith, const LargeArgs<double>& a, int nverts, int
                           void* partial, long long vstride, void* rdm, const long long* rdm_off, cudaStream_t s);
 size_t large_elem_size(int arith);
 
+// Block-sparse networks (bp_kernels.cu): the share of every listed sector
+// block in its outgoing messages (mode 0) or in rho_v (mode 1), unnormalised,
+// into partial + part_off[slot]; the sums and normalisation are in bp_qn.cu.
+void launch_qn_blocks(const WorkList& wl, const VDesc* bd, const double* blocks, const double* msg_in,
+                      const long long* sec_off, double* partial, const long long* part_off, int mode,
+                      cudaStream_t s);
+
 // One wave of the sequential schedule (bp_kernels.cu): jobs (vertex, leg,
 // sequence position, network), one message each, in place; team 32 (four jobs
 // per block) or 256 threads per job, shared memory for tensors of ncap elements.

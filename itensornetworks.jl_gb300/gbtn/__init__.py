@@ -13,6 +13,7 @@ from .partition import CoarseGraining, PartitionedBPCache, partitioned_cache
 from .sharded import GpuShard, ShardPlan, block_owner, run_distributed, run_local
 from .su import SimpleUpdateState, apply, bp_environments, checkerboard_edges, tebd, tebd_gates, tfim_gate
 from .opsum import OpSum, group_terms, trotter2_gates
+from .qn import QNBeliefPropagationCache, QNNetwork, random_qn_network
 from .network import (TensorNetwork, default_edge_sequence, disjoint_union, parallel_edge_sequence,
                       random_network, random_tensors, square_lattice)
 
@@ -26,4 +27,5 @@ __all__ = [
     "run_distributed", "run_local", "tebd_gates", "OpSum", "group_terms", "trotter2_gates", "edge_scalars",
     "identity_messages", "message", "messages", "update_factor", "update_factors", "vertex_scalars",
     "region_scalar", "scalar_factors_quotient", "incoming_messages", "factors", "default_bp_maxiter",
+    "QNBeliefPropagationCache", "QNNetwork", "random_qn_network",
 ]

@@ -88,6 +88,18 @@ class BPOpts(C.Structure):
     ]
 
 
+class QNDesc(C.Structure):
+    _fields_ = [
+        ("edge_sec_ptr", C.POINTER(C.c_int32)),
+        ("sec_dim", C.POINTER(C.c_int32)),
+        ("sec_charge", C.POINTER(C.c_int32)),
+        ("site_sec_ptr", C.POINTER(C.c_int32)),
+        ("site_sec_dim", C.POINTER(C.c_int32)),
+        ("site_sec_charge", C.POINTER(C.c_int32)),
+        ("flux", C.POINTER(C.c_int32)),
+    ]
+
+
 class GradOpts(C.Structure):
     _fields_ = [
         ("mode", C.c_int32),
@@ -148,6 +160,17 @@ SIGNATURES = {
     "gbtn_energy2_grad": (_I, [_P, C.c_int32, _D, _D, C.POINTER(GradOpts), _D, _D, _I32, _D]),
     "gbtn_bp_vjp": (_I, [_P, _D, C.POINTER(GradOpts), _D, _I32, _D]),
     "gbtn_bp_sweep_static": (_I, [_I, C.POINTER(GraphDesc), _P, _P, _P, _P, _P]),
+    "gbtn_qn_plan_create": (_I, [_P, C.POINTER(GraphDesc), C.POINTER(QNDesc), C.POINTER(_P)]),
+    "gbtn_qn_plan_destroy": (_I, [_P]),
+    "gbtn_qn_plan_sizes": (_I, [_P, _I32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "gbtn_qn_blocks": (_I, [_P, _I32, C.POINTER(C.c_int64)]),
+    "gbtn_qn_set_blocks": (_I, [_P, _P, _I]),
+    "gbtn_qn_init_messages": (_I, [_P]),
+    "gbtn_qn_set_messages": (_I, [_P, _P, _I]),
+    "gbtn_qn_get_messages": (_I, [_P, _P, _I]),
+    "gbtn_qn_bp_run": (_I, [_P, C.c_int32, C.c_double, _I32, _D]),
+    "gbtn_qn_vertex_rdms": (_I, [_P, _D]),
+    "gbtn_qn_logscalar": (_I, [_P, _D, _D]),
 }
 
 

@@ -1,0 +1,110 @@
+"""Charge-conserving (QN) block-sparse networks on the GPU against the dense
+FP64 oracle.
+
+A U(1)-graded network is expanded to dense tensors (zero outside the blocks
+that balance each vertex's flux) for the oracle; the library stores and
+contracts only the blocks.  BP from identity messages keeps the messages
+block-diagonal in the link sectors, so the library's sector-block messages,
+expanded, must equal the oracle's dense messages: 1e-12 on unit-norm FP64
+messages, 1e-10 relative on <Sz> and the log-scalar.  The reference's QN
+regression case (test/test_belief_propagation.jl:103-116: a loopy 4-cycle of
+S=1/2 sites, a product state, BP scalar finite and nonzero) is restated."""
+import numpy as np
+import pytest
+
+import bp_oracle as O
+import gbtn
+
+pytestmark = pytest.mark.gpu
+
+UP_DOWN = [(1, 1), (-1, 1)]  # S=1/2 site: charge 2 Sz of |up>, |down>
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(lib_built):
+    yield
+
+
+def oracle_graph(tn):
+    return O.Graph(tn.nv, tn.edges, tn.site_dims, tn.edge_dims, tn.legs)
+
+
+def random_u1_lattice(Lx, Ly, seed):
+    tn = gbtn.square_lattice(Lx, Ly, chi=4)
+    links = [[(-1, 1), (0, 2), (1, 1)]] * tn.ne
+    sites = [UP_DOWN] * tn.nv
+    flux = [1 if (v % Lx + v // Lx) % 2 else -1 for v in range(tn.nv)]
+    return gbtn.random_qn_network(tn, links, sites, flux, seed, unit_norm=True)
+
+
+@pytest.mark.parametrize("L", [(3, 3), (4, 4), (5, 3)])
+def test_qn_bp_matches_dense_oracle(L):
+    q = random_u1_lattice(*L, seed=10 + L[0])
+    tn = q.tn
+    g = oracle_graph(tn)
+    A = tn.tensors
+    m, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=25, schedule="parallel")
+    # the premise: dense BP keeps the messages block-diagonal in the link sectors
+    for de in range(2 * g.ne):
+        e = de // 2
+        for c1, a1, b1 in gbtn.QNNetwork._ranges(q.link_sectors[e]):
+            for c2, a2, b2 in gbtn.QNNetwork._ranges(q.link_sectors[e]):
+                if c1 != c2:
+                    assert np.max(np.abs(m[de][a1:b1, a2:b2])) < 1e-14
+    bpc = gbtn.QNBeliefPropagationCache(q)
+    assert bpc.n_block_elems < sum(tn.size(v) for v in range(tn.nv))  # only the allowed blocks are stored
+    bpc.update(maxiter=25)
+    got = bpc.messages()
+    assert max(float(np.max(np.abs(got[de] - m[de]))) for de in range(2 * g.ne)) <= 1e-12
+    sz = bpc.expect(O.SZ)
+    ref = O.expect1(g, A, m, O.SZ)
+    np.testing.assert_allclose(sz, ref, rtol=1e-10, atol=1e-13)
+    assert bpc.logscalar() == pytest.approx(float(np.real(O.logscalar(g, A, A, m))), rel=1e-10)
+    # and the dense plan on the expanded tensors agrees
+    dense = gbtn.BeliefPropagationCache(tn).update(maxiter=25, schedule="parallel")
+    assert max(float(np.max(np.abs(dense.messages()[de] - got[de]))) for de in range(2 * g.ne)) <= 1e-12
+    dense.close()
+    bpc.close()
+
+
+def test_qn_convergence_and_diff():
+    q = random_u1_lattice(4, 4, seed=3)
+    g = oracle_graph(q.tn)
+    m, it, md = O.bp_update(g, q.tn.tensors, O.identity_messages(g), maxiter=200, tol=1e-12, schedule="parallel")
+    bpc = gbtn.QNBeliefPropagationCache(q).update(maxiter=200, tol=1e-12)
+    assert abs(bpc.iterations - it) <= 1
+    assert max(float(np.max(np.abs(bpc.messages()[de] - m[de]))) for de in range(2 * g.ne)) <= 1e-6
+    bpc.close()
+
+
+def test_qn_graded_loopy_product_state_scalar():
+    # test/test_belief_propagation.jl:109-116: a 4-cycle of S=1/2 sites with
+    # conserved Sz, the product state up/down by site parity, BP scalar of
+    # <psi|psi> from identity messages: finite, nonzero (and exactly 1 here)
+    tn = gbtn.square_lattice(2, 2, chi=1)
+    up, dn = np.array([1.0, 0.0]), np.array([0.0, 1.0])
+    flux, ts = [], []
+    for v in range(tn.nv):
+        i, j = v % 2, v // 2
+        odd = (i + j + 2) % 2 == 1
+        ts.append((up if odd else dn).reshape((2,) + (1,) * len(tn.legs[v])))
+        flux.append(1 if odd else -1)
+    tn.tensors = ts
+    q = gbtn.QNNetwork(tn, [[(0, 1)]] * tn.ne, [UP_DOWN] * tn.nv, flux)
+    bpc = gbtn.QNBeliefPropagationCache(q).update(maxiter=25)
+    n2 = bpc.scalar()
+    assert np.isfinite(n2) and n2 != 0
+    assert n2 == pytest.approx(O.exact_scalar(oracle_graph(tn), ts), rel=1e-12)
+    np.testing.assert_allclose(bpc.expect(O.SZ), [0.5 if f > 0 else -0.5 for f in flux], atol=1e-14)
+    bpc.close()
+
+
+def test_qn_refusals():
+    tn = gbtn.square_lattice(2, 2, chi=2)
+    q = gbtn.random_qn_network(tn, [[(0, 1), (0, 1)]] * tn.ne, [UP_DOWN] * tn.nv, [1, -1, -1, 1], 1)
+    with pytest.raises(gbtn.Unsupported, match="distinct charges"):
+        gbtn.QNBeliefPropagationCache(q)
+    tn9 = gbtn.square_lattice(2, 2, chi=9)
+    q9 = gbtn.random_qn_network(tn9, [[(0, 9)]] * tn9.ne, [UP_DOWN] * tn9.nv, [1, 1, 1, 1], 1)
+    with pytest.raises(gbtn.Unsupported, match="sector dimensions"):
+        gbtn.QNBeliefPropagationCache(q9)
