@@ -283,6 +283,43 @@ def batched_uneven_timing(gbtn, ctx, stream, barrier, nnet=64, sweeps=20, seed=7
     return out
 
 
+def qn_timing(gbtn, ctx, stream, barrier, L=24, sweeps=10):
+    """Charge-conserving (U(1)) block-sparse network: an L x L PEPS with
+    S=1/2 sites (charges +-1), links of dimension 8 in sectors of charge
+    -1, 0, +1 (dimensions 2, 4, 2), fluxes alternating by site parity, N(0,1)
+    entries in the allowed blocks.  FP64 parallel sweeps of the block-sparse
+    plan against the dense plan on the same tensors expanded with zeros."""
+    import torch
+    tn = gbtn.square_lattice(L, L, chi=8)
+    links = [[(-1, 2), (0, 4), (1, 2)]] * tn.ne
+    flux = [1 if (v % L + v // L) % 2 else -1 for v in range(tn.nv)]
+    q = gbtn.random_qn_network(tn, links, [[(1, 1), (-1, 1)]] * tn.nv, flux, 11, unit_norm=True)
+
+    def ms(update):
+        update(2)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        update(sweeps)
+        e1.record(stream)
+        barrier()
+        return e0.elapsed_time(e1) / sweeps
+
+    qc = gbtn.QNBeliefPropagationCache(q, ctx=ctx)
+    dc = gbtn.BeliefPropagationCache(q.tn, ctx=ctx)
+    ms_qn = ms(lambda n: qc.update(maxiter=n))
+    ms_dense = ms(lambda n: dc.update(maxiter=n, schedule="parallel", precision="f64"))
+    err = max(float(np.max(np.abs(a - b))) for a, b in zip(qc.messages(), dc.messages()))
+    out = {"workload": f"u1_peps{L}x{L}_chi8_sectors2-4-2_d2", "fp64_ms_per_sweep_block_sparse": ms_qn,
+           "fp64_ms_per_sweep_dense": ms_dense, "speedup": ms_dense / ms_qn,
+           "stored_elements_block_sparse": qc.n_block_elems,
+           "stored_elements_dense": int(sum(q.tn.size(v) for v in range(tn.nv))),
+           "max_message_difference_vs_dense": err}
+    qc.close()
+    dc.close()
+    return out
+
+
 def gradient_timing(gbtn, ctx, barrier, rank, Lg=12, chig=6, reps=3):
     """Seconds per gradient of the BP Heisenberg energy on an Lg x Lg PEPS."""
     from gbtn.operators import HEISENBERG
@@ -547,6 +584,7 @@ def run_ours(args):
     grad = gradient_timing(gbtn, ctx, barrier, rank)
     su = simple_update_timing(gbtn, ctx, barrier, rank)
     batched = batched_uneven_timing(gbtn, ctx, stream, barrier)
+    qn = qn_timing(gbtn, ctx, stream, barrier)
 
     # roofline of the tensor-core kernel: algorithmic flops and compulsory bytes of
     # the routed vertices at their own (unpadded) shapes / its event-timed launch
@@ -616,6 +654,7 @@ def run_ours(args):
             "tc_split": {"tensor_core_vertices": n_tc, "simt_vertices": tn.nv - n_tc, "tuned_split_ms": tune_ms},
             "gauge_scaling": gauge,
             "batched_uneven": batched,
+            "qn_block_sparse": qn,
             "simple_update": su,
             "gradient": grad,
         }

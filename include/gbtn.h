@@ -335,6 +335,23 @@ int gbtn_energy2_grad(gbtn_plan* plan, int32_t n_terms, const double* coef, cons
 int gbtn_bp_vjp(gbtn_plan* plan, const double* msg_cot, const gbtn_grad_opts* opts, double* grad, int32_t* iters,
                 double* resid);
 
+/* Gradients of the BP log-norm and of one-site expectation values with
+ * respect to every site tensor (no counterpart in the reference, which has no
+ * automatic differentiation), at the messages in the plan, which must be a
+ * converged fixed point: the direct derivatives (messages held) plus the
+ * implicit part through the fixed point (the adjoint BP solve of
+ * gbtn_bp_vjp; opts may be NULL for its defaults, mode is ignored).
+ *   gbtn_logscalar_grad: value[n] = Re logscalar of network n
+ *     (abstractbeliefpropagationcache.jl:397-408) and grad = d/dA of the sum;
+ *   gbtn_expect1_grad: value[n] = sum_v <O_v> over network n's vertices
+ *     (expect.jl:5-19, one d x d operator O[s', s] for all) and its gradient.
+ * Real FP64 quadratic-form plans whose vertices all have a link and fit the
+ * shared-memory kernels; others return GBTN_ERR_UNSUPPORTED. */
+int gbtn_logscalar_grad(gbtn_plan* plan, const gbtn_grad_opts* opts, double* value, double* grad, int32_t* iters,
+                        double* resid);
+int gbtn_expect1_grad(gbtn_plan* plan, const double* op, const gbtn_grad_opts* opts, double* value, double* grad,
+                      int32_t* iters, double* resid);
+
 /* ---- charge-conserving (QN) block-sparse networks ------------------------ */
 /* Replaces: BP on QN-conserving ITensors (ITensors' conserve_qns = true, e.g.
  * the QN-graded loopy network of test/test_belief_propagation.jl:103-116).

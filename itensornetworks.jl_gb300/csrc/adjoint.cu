@@ -269,6 +269,89 @@ void launch_site_op(int nv, const VDesc* vd, const double* fac, const double* op
   GBTN_CUDA(cudaGetLastError());
 }
 
+// Vertex terms of the log-norm and of one-site expectation values, as
+// contractions of an unnormalised outgoing message with the incoming one on
+// the same leg (leg 0 of every vertex): the full contraction of a partition is
+// D_v = <F_{v->w}, m_{w->v}> (region_scalar, beliefpropagationcache.jl:107-113),
+// and with O applied to the ket N_v = <F^O_{v->w}, m_{w->v}> = tr(rho_v O).
+// One warp per vertex (degree >= 1).
+//   mode 0 (log-norm, logscalar abstractbeliefpropagationcache.jl:397-408):
+//     val[v] = log|D_v|; cotangent of F_{v->w}: m_{w->v} / D_v (into ci);
+//     g[w->v] += F_{v->w} / D_v.
+//   mode 1 (expect, expect.jl:5-19): val[v] = N_v / D_v; cotangents
+//     co (of F^O_{v->w}) = m / D_v and ci (of F_{v->w}) = -N_v / D_v^2 m;
+//     g[w->v] += F^O / D_v - N_v / D_v^2 F.
+__global__ void vertex_term_cot_kernel(int nv, const VDesc* __restrict__ vd, const long long* __restrict__ msg_off,
+                                       const double* __restrict__ msgs, const double* __restrict__ F,
+                                       const double* __restrict__ FO, int mode, double* ci, double* co, double* g,
+                                       double* val) {
+  const int v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (v >= nv) return;
+  const VDesc& d = vd[v];
+  const int c2 = d.chi[0] * d.chi[0];
+  const long long oo = msg_off[d.out_de[0]], oi = msg_off[d.in_de[0]];
+  double dd = 0.0, nn = 0.0;
+  for (int i = lane; i < c2; i += 32) {
+    dd = fma(F[oo + i], msgs[oi + i], dd);
+    if (mode == 1) nn = fma(FO[oo + i], msgs[oi + i], nn);
+  }
+  dd = warp_sum(dd);
+  nn = warp_sum(nn);
+  const double inv = 1.0 / dd;
+  if (mode == 0) {
+    for (int i = lane; i < c2; i += 32) {
+      ci[oo + i] = msgs[oi + i] * inv;
+      g[oi + i] += F[oo + i] * inv;
+    }
+    if (lane == 0) val[v] = log(fabs(dd));
+  } else {
+    const double r = nn * inv * inv;
+    for (int i = lane; i < c2; i += 32) {
+      co[oo + i] = msgs[oi + i] * inv;
+      ci[oo + i] = -r * msgs[oi + i];
+      g[oi + i] += FO[oo + i] * inv - r * F[oo + i];
+    }
+    if (lane == 0) val[v] = nn * inv;
+  }
+}
+
+// Edge terms of the log-norm: z_e = <m_e, m_ebar>, val[e] = log|z_e|,
+// g[e] -= m_ebar / z_e and g[ebar] -= m_e / z_e.  One warp per edge.
+__global__ void edge_term_cot_kernel(int ne, const int* __restrict__ dchi, const long long* __restrict__ msg_off,
+                                     const double* __restrict__ msgs, double* g, double* val) {
+  const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (e >= ne) return;
+  const int c2 = dchi[2 * e] * dchi[2 * e];
+  const long long o1 = msg_off[2 * e], o2 = msg_off[2 * e + 1];
+  double z = 0.0;
+  for (int i = lane; i < c2; i += 32) z = fma(msgs[o1 + i], msgs[o2 + i], z);
+  z = warp_sum(z);
+  const double inv = 1.0 / z;
+  for (int i = lane; i < c2; i += 32) {
+    const double a = msgs[o1 + i], b = msgs[o2 + i];
+    g[o1 + i] -= b * inv;
+    g[o2 + i] -= a * inv;
+  }
+  if (lane == 0) val[e] = log(fabs(z));
+}
+
+void launch_vertex_term_cot(int nv, const VDesc* vd, const long long* msg_off, const double* msgs, const double* F,
+                            const double* FO, int mode, double* ci, double* co, double* g, double* val,
+                            cudaStream_t s) {
+  if (nv == 0) return;
+  vertex_term_cot_kernel<<<(nv + 7) / 8, 256, 0, s>>>(nv, vd, msg_off, msgs, F, FO, mode, ci, co, g, val);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_edge_term_cot(int ne, const int* dchi, const long long* msg_off, const double* msgs, double* g,
+                          double* val, cudaStream_t s) {
+  if (ne == 0) return;
+  edge_term_cot_kernel<<<(ne + 7) / 8, 256, 0, s>>>(ne, dchi, msg_off, msgs, g, val);
+  GBTN_CUDA(cudaGetLastError());
+}
+
 void launch_norm_vjp(int ndir, const int* dchi, const long long* msg_off, const double* f, const double* nbar,
                      double* fbar, cudaStream_t s) {
   if (ndir == 0) return;

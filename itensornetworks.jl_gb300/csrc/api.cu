@@ -2575,6 +2575,118 @@ int gbtn_energy2_grad(gbtn_plan* P, int32_t nterms, const double* coef, const do
   API_CATCH(C)
 }
 
+}  // extern "C"
+
+namespace {
+
+// Checks shared by the scalar gradients (real FP64 quadratic form, every
+// vertex with a link, shared-memory vertices).
+void scalar_grad_checks(gbtn_plan* P) {
+  if (P->has_large)
+    throw Unsupported("energies and gradients take vertices of the shared-memory kernels only (bond and site "
+                      "dimensions <= 8)");
+  if (P->cplx) throw Unsupported("gradients of complex networks are not implemented");
+  require(!P->sep_bra, "gradients need bra = conj(ket) (a quadratic-form network)");
+  for (int v = 0; v < P->nv; ++v)
+    if (P->vd[v].k < 1) throw Unsupported("gradients take vertices with at least one link");
+  if (vertex_vjp_smem(P->ncap) > 227 * 1024) throw Unsupported("vertex tensor too large for the adjoint kernels");
+}
+
+// Per-network sums of per-vertex (and, when ev is given, minus per-edge) values.
+void net_sums(gbtn_plan* P, const DevBuf<double>& vv, const DevBuf<double>* ev, double* out) {
+  std::vector<double> hv(P->nv), he(std::max(P->ne, 1));
+  copy_out(P, hv.data(), vv.p, sizeof(double) * P->nv, GBTN_HOST);
+  if (ev && P->ne) copy_out(P, he.data(), ev->p, sizeof(double) * P->ne, GBTN_HOST);
+  std::vector<double> acc(P->nnet, 0.0);
+  for (int v = 0; v < P->nv; ++v) acc[P->vnet[v]] += hv[v];
+  if (ev)
+    for (int e = 0; e < P->ne; ++e) acc[P->vnet[P->eu[e]]] -= he[e];
+  std::copy(acc.begin(), acc.end(), out);
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbtn_logscalar_grad(gbtn_plan* P, const gbtn_grad_opts* o, double* value, double* grad, int32_t* iters,
+                        double* resid) {
+  const gbtn::NvtxRange nvtx_range("gbtn_logscalar_grad");
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && grad, "NULL argument");
+  scalar_grad_checks(P);
+  cudaStream_t s = P->ctx->stream;
+  const long long nm = std::max<long long>(P->n_msg, 1), nf = std::max<long long>(P->n_fac, 1);
+  DevBuf<double> F, ci, g, dgrad, vval, eval;
+  DevBuf<int> allv;
+  std::vector<int> all(P->nv);
+  std::iota(all.begin(), all.end(), 0);
+  allv.upload(all, s);
+  F.alloc(nm);
+  ci.alloc(nm);
+  g.alloc(nm);
+  dgrad.alloc(nf);
+  vval.alloc(P->nv);
+  eval.alloc(std::max(P->ne, 1));
+  GBTN_CUDA(cudaMemsetAsync(ci.p, 0, sizeof(double) * nm, s));
+  GBTN_CUDA(cudaMemsetAsync(g.p, 0, sizeof(double) * nm, s));
+  GBTN_CUDA(cudaMemsetAsync(dgrad.p, 0, sizeof(double) * nf, s));
+  const double* m = P->d_msg[P->cur].p;
+  raw_forward(P, P->d_fac.p, nullptr, m, F.p, 0);
+  launch_vertex_term_cot(P->nv, P->d_vd.p, P->d_msg_off.p, m, F.p, nullptr, 0, ci.p, nullptr, g.p, vval.p, s);
+  launch_edge_term_cot(P->ne, P->d_dchi.p, P->d_msg_off.p, m, g.p, eval.p, s);
+  launch_vertex_vjp(allv.p, P->nv, P->d_vd.p, P->d_fac.p, P->d_fac.p, m, ci.p, P->d_msg_off.p, nullptr, g.p,
+                    dgrad.p, P->ncap, s);
+  implicit_adjoint(P, allv.p, m, g.p, dgrad.p, o && o->maxiter > 0 ? o->maxiter : 500,
+                   o && o->tol > 0 ? o->tol : 1e-12, iters, resid);
+  copy_out(P, grad, dgrad.p, sizeof(double) * P->n_fac, GBTN_HOST);
+  if (value) net_sums(P, vval, &eval, value);
+  API_CATCH(C)
+}
+
+int gbtn_expect1_grad(gbtn_plan* P, const double* op, const gbtn_grad_opts* o, double* value, double* grad,
+                      int32_t* iters, double* resid) {
+  const gbtn::NvtxRange nvtx_range("gbtn_expect1_grad");
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P && op && grad, "NULL argument");
+  scalar_grad_checks(P);
+  const int d = P->dsite[0];
+  for (int v = 0; v < P->nv; ++v) require(P->dsite[v] == d, "all vertices must share the site dimension of the operator");
+  cudaStream_t s = P->ctx->stream;
+  const long long nm = std::max<long long>(P->n_msg, 1), nf = std::max<long long>(P->n_fac, 1);
+  DevBuf<double> dop, ketO, F, FO, ci, co, g, dgrad, vval;
+  DevBuf<int> allv;
+  std::vector<int> all(P->nv);
+  std::iota(all.begin(), all.end(), 0);
+  allv.upload(all, s);
+  dop.upload(std::vector<double>(op, op + (size_t)d * d), s);
+  ketO.alloc(nf);
+  F.alloc(nm);
+  FO.alloc(nm);
+  ci.alloc(nm);
+  co.alloc(nm);
+  g.alloc(nm);
+  dgrad.alloc(nf);
+  vval.alloc(P->nv);
+  for (DevBuf<double>* b : {&ci, &co, &g}) GBTN_CUDA(cudaMemsetAsync(b->p, 0, sizeof(double) * nm, s));
+  GBTN_CUDA(cudaMemsetAsync(dgrad.p, 0, sizeof(double) * nf, s));
+  const double* m = P->d_msg[P->cur].p;
+  launch_site_op(P->nv, P->d_vd.p, P->d_fac.p, dop.p, ketO.p, s);
+  raw_forward(P, P->d_fac.p, nullptr, m, F.p, 0);
+  raw_forward(P, ketO.p, P->d_fac.p, m, FO.p, 0);
+  launch_vertex_term_cot(P->nv, P->d_vd.p, P->d_msg_off.p, m, F.p, FO.p, 1, ci.p, co.p, g.p, vval.p, s);
+  launch_vertex_vjp(allv.p, P->nv, P->d_vd.p, P->d_fac.p, P->d_fac.p, m, ci.p, P->d_msg_off.p, nullptr, g.p,
+                    dgrad.p, P->ncap, s);
+  launch_vertex_vjp(allv.p, P->nv, P->d_vd.p, ketO.p, P->d_fac.p, m, co.p, P->d_msg_off.p, dop.p, g.p, dgrad.p,
+                    P->ncap, s);
+  implicit_adjoint(P, allv.p, m, g.p, dgrad.p, o && o->maxiter > 0 ? o->maxiter : 500,
+                   o && o->tol > 0 ? o->tol : 1e-12, iters, resid);
+  copy_out(P, grad, dgrad.p, sizeof(double) * P->n_fac, GBTN_HOST);
+  if (value) net_sums(P, vval, nullptr, value);
+  API_CATCH(C)
+}
+
 int gbtn_bp_vjp(gbtn_plan* P, const double* msg_cot, const gbtn_grad_opts* o, double* grad, int32_t* iters,
                 double* resid) {
   const gbtn::NvtxRange nvtx_range("gbtn_bp_vjp");

@@ -312,6 +312,11 @@ void launch_energy_cot(int ndir, const int* dchi, const long long* msg_off, cons
 void launch_energy_terms(int ne, int nterms, const double* coef, const double* t, double* Ee, double* scale,
                          cudaStream_t s);
 void launch_net_sum(int nnet, const int* net_e_ptr, const int* net_e, const double* Ee, double* out, cudaStream_t s);
+void launch_vertex_term_cot(int nv, const VDesc* vd, const long long* msg_off, const double* msgs, const double* F,
+                            const double* FO, int mode, double* ci, double* co, double* g, double* val,
+                            cudaStream_t s);
+void launch_edge_term_cot(int ne, const int* dchi, const long long* msg_off, const double* msgs, double* g,
+                          double* val, cudaStream_t s);
 void launch_axpy_resid(long long n, const double* a, const double* b, const double* old, double* y, double* acc,
                        cudaStream_t s);
 

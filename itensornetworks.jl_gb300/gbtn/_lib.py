@@ -160,6 +160,8 @@ SIGNATURES = {
     "gbtn_energy2_grad": (_I, [_P, C.c_int32, _D, _D, C.POINTER(GradOpts), _D, _D, _I32, _D]),
     "gbtn_bp_vjp": (_I, [_P, _D, C.POINTER(GradOpts), _D, _I32, _D]),
     "gbtn_bp_sweep_static": (_I, [_I, C.POINTER(GraphDesc), _P, _P, _P, _P, _P]),
+    "gbtn_logscalar_grad": (_I, [_P, C.POINTER(GradOpts), _D, _D, _I32, _D]),
+    "gbtn_expect1_grad": (_I, [_P, _D, C.POINTER(GradOpts), _D, _D, _I32, _D]),
     "gbtn_qn_plan_create": (_I, [_P, C.POINTER(GraphDesc), C.POINTER(QNDesc), C.POINTER(_P)]),
     "gbtn_qn_plan_destroy": (_I, [_P]),
     "gbtn_qn_plan_sizes": (_I, [_P, _I32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
