@@ -372,7 +372,7 @@ size_t smem_need(int n, int k, bool sep_bra, size_t elt, int team) {
   const int nbuf = k <= 4 ? 3 : kNumBufs;
   const size_t np = (size_t)n + (n >> 5) + 1;
   size_t b = (sizeof(VDesc) + 15) / 16 * 16;
-  b += elt * (np * (nbuf + (sep_bra ? 1 : 0)) + kMaxDeg * 64 + (team / 32) * 64 + 64);
+  b += elt * (np * (nbuf + (sep_bra ? 1 : 0)) + team_tail_elems(team));
   return (b + 15) / 16 * 16;
 }
 

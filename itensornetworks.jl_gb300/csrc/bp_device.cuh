@@ -399,7 +399,11 @@ __device__ __forceinline__ double finalize_message_df(const df32* res, int chi, 
   return diff;
 }
 
-// Shared-memory carve-up of one team.
+// Shared-memory carve-up of one team.  A team of several warps keeps one
+// close result per leg (res: kMaxDeg x 64) and finalises them together after
+// its last schedule step; a one-warp team finalises each as it is closed
+// (res: 64).  old holds the previous outgoing messages (storage type, read by
+// message_diff), loaded with the vertex so that no finalisation waits on HBM.
 template <typename T>
 struct TeamSmem {
   VDesc* desc;
@@ -407,7 +411,8 @@ struct TeamSmem {
   T* bra;
   T* msg;  // kMaxDeg x 64
   T* red;  // (TEAM/32) x kRedStride
-  T* res;  // 64
+  T* res;  // kMaxDeg x 64 (TEAM > 32) or 64
+  T* old;  // kMaxDeg x 64 elements of T's size (holding the storage type)
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -415,7 +420,7 @@ __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a -
 template <typename T>
 __host__ __device__ inline size_t team_smem_bytes(int ncap, int nbuf, bool sep_bra, int team) {
   size_t b = align_up(sizeof(VDesc), 16);
-  b += sizeof(T) * ((size_t)ncap * (nbuf + (sep_bra ? 1 : 0)) + kMaxDeg * 64 + (team / 32) * kRedStride + 64);
+  b += sizeof(T) * ((size_t)ncap * (nbuf + (sep_bra ? 1 : 0)) + team_tail_elems(team));
   return align_up(b, 16);
 }
 
@@ -437,6 +442,8 @@ __device__ __forceinline__ TeamSmem<T> carve(unsigned char* p, int ncap, int nbu
   s.red = q;
   q += (team / 32) * kRedStride;
   s.res = q;
+  q += team > 32 ? kMaxDeg * 64 : 64;
+  s.old = q;
   return s;
 }
 
@@ -456,7 +463,16 @@ __device__ __forceinline__ void load_vertex(const TeamSmem<T>& Sm, const S* fac,
                                             const long long* msg_off, int skip_leg, int tid) {
   const VDesc& d = *Sm.desc;
   const S* a = fac + d.a_off;
-  for (int i = tid; i < d.n; i += TEAM) Sm.buf[0][spos<PAD>(i)] = to_elem<T>(a[i]);
+  // four loads in flight per thread before their stores
+  int i = tid;
+  for (; i + 3 * TEAM < d.n; i += 4 * TEAM) {
+    const S x0 = a[i], x1 = a[i + TEAM], x2 = a[i + 2 * TEAM], x3 = a[i + 3 * TEAM];
+    Sm.buf[0][spos<PAD>(i)] = to_elem<T>(x0);
+    Sm.buf[0][spos<PAD>(i + TEAM)] = to_elem<T>(x1);
+    Sm.buf[0][spos<PAD>(i + 2 * TEAM)] = to_elem<T>(x2);
+    Sm.buf[0][spos<PAD>(i + 3 * TEAM)] = to_elem<T>(x3);
+  }
+  for (; i < d.n; i += TEAM) Sm.buf[0][spos<PAD>(i)] = to_elem<T>(a[i]);
   if (bra_g) {
     const S* b = bra_g + d.a_off;
     for (int i = tid; i < d.n; i += TEAM) Sm.bra[spos<PAD>(i)] = to_elem<T>(b[i]);
@@ -466,6 +482,20 @@ __device__ __forceinline__ void load_vertex(const TeamSmem<T>& Sm, const S* fac,
     const int c2 = d.chi[p] * d.chi[p];
     const S* m = msgs + msg_off[d.in_de[p]];
     for (int i = tid; i < c2; i += TEAM) Sm.msg[p * 64 + i] = to_elem<T>(m[i]);
+  }
+}
+
+// The current outgoing messages of a vertex (the "old" side of message_diff)
+// into Sm.old, in their storage type.
+template <typename T, int TEAM, typename S>
+__device__ __forceinline__ void load_old_messages(const TeamSmem<T>& Sm, const S* msgs, const long long* msg_off,
+                                                  int tid) {
+  const VDesc& d = *Sm.desc;
+  S* o = reinterpret_cast<S*>(Sm.old);
+  for (int p = 0; p < d.k; ++p) {
+    const int c2 = d.chi[p] * d.chi[p];
+    const S* m = msgs + msg_off[d.out_de[p]];
+    for (int i = tid; i < c2; i += TEAM) o[p * 64 + i] = m[i];
   }
 }
 

@@ -116,9 +116,22 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
       continue;
     }
     load_vertex<T, TEAM, S, true>(Sm, fac, bra_g, msg_in, msg_off, -1, tid);
+    if (want_diff) load_old_messages<T, TEAM, S>(Sm, msg_in, msg_off, tid);
     tsync<TEAM>();
     const int k = d.k;
     const int len = c_sched.len[k];
+    // normalise leg p's close result, write it, and record message_diff against Sm.old
+    auto finalize = [&](int p, const T* res) {
+      const int de = d.out_de[p];
+      const long long off = msg_off[de];
+      const S* old = reinterpret_cast<const S*>(Sm.old) + p * 64;
+      double df;
+      if constexpr (std::is_same<T, df32>::value)
+        df = finalize_message_df(res, d.chi[p], old, msg_out + off, normalize, want_diff != 0, lane);
+      else
+        df = finalize_message<T>(res, d.chi[p], old, msg_out + off, normalize, want_diff != 0, lane);
+      if (want_diff && lane == 0) diffs[de] = df;
+    };
     for (int i = 0; i < len; ++i) {
       const SchedOp op = c_sched.ops[k][i];
       const int leg = op.leg;
@@ -126,20 +139,19 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
       if (op.type == 0) {
         absorb_any<T, true>(chi, Sm.buf[op.src], Sm.buf[op.dst], d.n, st, Sm.msg + leg * 64, tid, TEAM);
         tsync<TEAM>();
+      } else if constexpr (TEAM > 32) {
+        // the result waits in its leg's slot; close_fibers ends with a team barrier
+        close_any<T, TEAM, true>(chi, Sm.buf[op.src], Sm.bra, d.n, st, 1, 0, 0, Sm.red, Sm.res + leg * 64, tid);
       } else {
         close_any<T, TEAM, true>(chi, Sm.buf[op.src], Sm.bra, d.n, st, 1, 0, 0, Sm.red, Sm.res, tid);
-        if (tid < 32) {
-          const int de = d.out_de[leg];
-          const long long off = msg_off[de];
-          double df;
-          if constexpr (std::is_same<T, df32>::value)
-            df = finalize_message_df(Sm.res, chi, msg_in + off, msg_out + off, normalize, want_diff != 0, lane);
-          else
-            df = finalize_message<T>(Sm.res, chi, msg_in + off, msg_out + off, normalize, want_diff != 0, lane);
-          if (want_diff && lane == 0) diffs[de] = df;
-        }
+        finalize(leg, Sm.res);
         tsync<TEAM>();
       }
+    }
+    if constexpr (TEAM > 32) {
+      // every leg's message at once, one warp each
+      for (int p = tid >> 5; p < k; p += TEAM / 32) finalize(p, Sm.res + p * 64);
+      tsync<TEAM>();
     }
   }
 }

@@ -64,6 +64,15 @@ struct __align__(16) VDesc {
   int out_de[kMaxDeg];      // directed edge leaving v on leg p
 };
 
+// Shared-memory elements of a SIMT team beyond its tensor buffers: incoming
+// messages (kMaxDeg x 64), the close reduction ((team / 32) x 64), close
+// results (kMaxDeg x 64 for a team of several warps, else 64) and the
+// previous outgoing messages (kMaxDeg x 64).
+__host__ __device__ inline constexpr size_t team_tail_elems(int team) {
+  return (size_t)kMaxDeg * 64 + (size_t)(team / 32) * 64 + (team > 32 ? (size_t)kMaxDeg * 64 : 64) +
+         (size_t)kMaxDeg * 64;
+}
+
 // One step of a vertex schedule: ABSORB src->dst on leg, or CLOSE src on leg.
 struct SchedOp {
   int8_t type;  // 0 absorb, 1 close

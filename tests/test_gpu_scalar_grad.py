@@ -59,8 +59,11 @@ def unit_directions(A, seed):
 
 
 def cache(g, A):
+    """Every sweep runs (no tolerance): a mean message diff of 1e-15 still
+    leaves ~3e-8 in the messages (the diff is quadratic in the error), which
+    the log-norm, stationary at the fixed point, does not see but <O> does."""
     tn = gbtn.TensorNetwork(g.nv, g.edges, g.site_dims, g.edge_dims, [a.copy() for a in A])
-    return gbtn.BeliefPropagationCache(tn).update(maxiter=SWEEPS, tol=1e-15, schedule="parallel")
+    return gbtn.BeliefPropagationCache(tn).update(maxiter=SWEEPS, schedule="parallel")
 
 
 CASES = {
@@ -113,7 +116,7 @@ def test_batched_gradients_are_per_network():
     A1, A2 = O.random_network(g1, 5, unit_norm=True), O.random_network(g2, 6, unit_norm=True)
     t1 = gbtn.TensorNetwork(g1.nv, g1.edges, g1.site_dims, g1.edge_dims, [a.copy() for a in A1])
     t2 = gbtn.TensorNetwork(g2.nv, g2.edges, g2.site_dims, g2.edge_dims, [a.copy() for a in A2])
-    both = gbtn.BeliefPropagationCache(gbtn.disjoint_union([t1, t2])).update(maxiter=SWEEPS, tol=1e-15, schedule="parallel")
+    both = gbtn.BeliefPropagationCache(gbtn.disjoint_union([t1, t2])).update(maxiter=SWEEPS, schedule="parallel")
     vals, G = both.logscalar_grad(tol=1e-14)
     v1, G1 = cache(g1, A1).logscalar_grad(tol=1e-14)
     v2, G2 = cache(g2, A2).logscalar_grad(tol=1e-14)
