@@ -82,6 +82,31 @@ __device__ __forceinline__ df32 mac(df32 a, df32 b, df32 c) {
   df_two_sum(c.hi, p, s, t);
   return df32(s, __fadd_rn(__fadd_rn(t, e), c.lo));
 }
+// Two independent df32 values per register pair, for the packed FP32x2
+// instructions: the same operations as mac() and settle(), each component
+// rounded exactly as there.  A difference x - y is the FMA y * (-1) + x (one
+// rounding, as __fsub_rn); the product error is carried negated, en = -e, so
+// that no operand needs a negation of its own.
+struct df32x2 {
+  float2 hi, lo;
+};
+__device__ __forceinline__ float2 sub2(float2 x, float2 y) { return __ffma2_rn(y, make_float2(-1.f, -1.f), x); }
+// a * (bh + bl) + c for a pair a, c and one value b given with its negation (nbh, nbl)
+__device__ __forceinline__ df32x2 mac2(const df32x2& a, float2 bh, float2 nbh, float2 nbl, const df32x2& c) {
+  const float2 p = __fmul2_rn(a.hi, bh);
+  float2 en = __ffma2_rn(a.hi, nbh, p);
+  en = __ffma2_rn(a.hi, nbl, en);
+  en = __ffma2_rn(a.lo, nbh, en);
+  const float2 s = __fadd2_rn(c.hi, p);
+  const float2 bb = sub2(s, c.hi);
+  const float2 t = __fadd2_rn(sub2(c.hi, sub2(s, bb)), sub2(p, bb));
+  return df32x2{s, __fadd2_rn(sub2(t, en), c.lo)};
+}
+__device__ __forceinline__ df32x2 settle2(const df32x2& a) {
+  const float2 s = __fadd2_rn(a.hi, a.lo);
+  return df32x2{s, sub2(a.lo, sub2(s, a.hi))};
+}
+
 __device__ __forceinline__ df32 conj_of(df32 x) { return x; }
 __device__ __forceinline__ df32 shfl_xor(df32 v, int o) {
   return df32(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
@@ -169,9 +194,85 @@ __device__ __forceinline__ int spos(int i) {
 }
 __host__ __device__ inline int padded_len(int n) { return n + (n >> 5) + 1; }
 
-template <typename T, int CHI, bool PAD = false>
+// FP32 fibers use the packed FP32x2 FMA (two outputs b, b + 1 per
+// instruction, each component rounded as one fmaf, in the same order).
+template <int CHI, bool PAD>
+__device__ __forceinline__ void absorb_fibers_f32x2(const float* __restrict__ in, float* __restrict__ out, int n,
+                                                    int st, const float* __restrict__ M, int tid, int nth) {
+  constexpr int H = (CHI + 1) / 2;
+  float2 m[H][CHI];
+#pragma unroll
+  for (int h = 0; h < H; ++h)
+#pragma unroll
+    for (int a = 0; a < CHI; ++a)
+      m[h][a] = make_float2(M[2 * h + CHI * a], 2 * h + 1 < CHI ? M[2 * h + 1 + CHI * a] : 0.f);
+  const int nfib = n / CHI;
+  for (int f = tid; f < nfib; f += nth) {
+    const int lo = f % st;
+    const int base = lo + (f - lo) * CHI;
+    float x[CHI];
+#pragma unroll
+    for (int a = 0; a < CHI; ++a) x[a] = in[spos<PAD>(base + a * st)];
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      float2 y = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int a = 0; a < CHI; ++a) y = __ffma2_rn(m[h][a], make_float2(x[a], x[a]), y);
+      out[spos<PAD>(base + 2 * h * st)] = y.x;
+      if (2 * h + 1 < CHI) out[spos<PAD>(base + (2 * h + 1) * st)] = y.y;
+    }
+  }
+}
+
+// df32 fibers: outputs b, b + 1 as one df32x2 (mac2, settle2).  Taken by
+// one-warp teams (PACK); a 256-thread team, one block per SM, keeps the
+// scalar loop, whose eight independent chains per fiber hide the FP32
+// latency better than four packed ones (measured on both kinds of vertex).
+template <int CHI, bool PAD>
+__device__ __forceinline__ void absorb_fibers_df32x2(const df32* __restrict__ in, df32* __restrict__ out, int n,
+                                                     int st, const df32* __restrict__ M, int tid, int nth) {
+  constexpr int H = (CHI + 1) / 2;
+  df32x2 m[H][CHI];
+#pragma unroll
+  for (int h = 0; h < H; ++h)
+#pragma unroll
+    for (int a = 0; a < CHI; ++a) {
+      const df32 u = M[2 * h + CHI * a];
+      const df32 w = 2 * h + 1 < CHI ? M[2 * h + 1 + CHI * a] : df32(0.f);
+      m[h][a] = df32x2{make_float2(u.hi, w.hi), make_float2(u.lo, w.lo)};
+    }
+  const int nfib = n / CHI;
+  for (int f = tid; f < nfib; f += nth) {
+    const int lo = f % st;
+    const int base = lo + (f - lo) * CHI;
+    df32 x[CHI];
+#pragma unroll
+    for (int a = 0; a < CHI; ++a) x[a] = in[spos<PAD>(base + a * st)];
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      df32x2 y{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+      for (int a = 0; a < CHI; ++a)
+        y = mac2(m[h][a], make_float2(x[a].hi, x[a].hi), make_float2(-x[a].hi, -x[a].hi),
+                 make_float2(-x[a].lo, -x[a].lo), y);
+      y = settle2(y);
+      out[spos<PAD>(base + 2 * h * st)] = df32(y.hi.x, y.lo.x);
+      if (2 * h + 1 < CHI) out[spos<PAD>(base + (2 * h + 1) * st)] = df32(y.hi.y, y.lo.y);
+    }
+  }
+}
+
+template <typename T, int CHI, bool PAD = false, bool PACK = false>
 __device__ __forceinline__ void absorb_fibers(const T* __restrict__ in, T* __restrict__ out, int n, int st,
                                               const T* __restrict__ M, int tid, int nth) {
+  if constexpr (std::is_same<T, float>::value && CHI > 1) {
+    absorb_fibers_f32x2<CHI, PAD>(in, out, n, st, M, tid, nth);
+    return;
+  }
+  if constexpr (std::is_same<T, df32>::value && CHI > 1 && PACK) {
+    absorb_fibers_df32x2<CHI, PAD>(in, out, n, st, M, tid, nth);
+    return;
+  }
   T m[CHI][CHI];
 #pragma unroll
   for (int b = 0; b < CHI; ++b)
@@ -194,18 +295,18 @@ __device__ __forceinline__ void absorb_fibers(const T* __restrict__ in, T* __res
   }
 }
 
-template <typename T, bool PAD = false>
+template <typename T, bool PAD = false, bool PACK = false>
 __device__ __forceinline__ void absorb_any(int chi, const T* in, T* out, int n, int st, const T* M, int tid,
                                            int nth) {
   switch (chi) {
-    case 1: absorb_fibers<T, 1, PAD>(in, out, n, st, M, tid, nth); break;
-    case 2: absorb_fibers<T, 2, PAD>(in, out, n, st, M, tid, nth); break;
-    case 3: absorb_fibers<T, 3, PAD>(in, out, n, st, M, tid, nth); break;
-    case 4: absorb_fibers<T, 4, PAD>(in, out, n, st, M, tid, nth); break;
-    case 5: absorb_fibers<T, 5, PAD>(in, out, n, st, M, tid, nth); break;
-    case 6: absorb_fibers<T, 6, PAD>(in, out, n, st, M, tid, nth); break;
-    case 7: absorb_fibers<T, 7, PAD>(in, out, n, st, M, tid, nth); break;
-    case 8: absorb_fibers<T, 8, PAD>(in, out, n, st, M, tid, nth); break;
+    case 1: absorb_fibers<T, 1, PAD, PACK>(in, out, n, st, M, tid, nth); break;
+    case 2: absorb_fibers<T, 2, PAD, PACK>(in, out, n, st, M, tid, nth); break;
+    case 3: absorb_fibers<T, 3, PAD, PACK>(in, out, n, st, M, tid, nth); break;
+    case 4: absorb_fibers<T, 4, PAD, PACK>(in, out, n, st, M, tid, nth); break;
+    case 5: absorb_fibers<T, 5, PAD, PACK>(in, out, n, st, M, tid, nth); break;
+    case 6: absorb_fibers<T, 6, PAD, PACK>(in, out, n, st, M, tid, nth); break;
+    case 7: absorb_fibers<T, 7, PAD, PACK>(in, out, n, st, M, tid, nth); break;
+    case 8: absorb_fibers<T, 8, PAD, PACK>(in, out, n, st, M, tid, nth); break;
     default: break;
   }
 }
@@ -214,7 +315,7 @@ constexpr int kRedStride = 64;  // per-warp slot of the close reduction (CHI <= 
 
 // CLOSE over fibers ff = fib_add + fib_mul*f of leg (st, CHI); result
 // res[b + CHI*a] = sum bra[base+shift+b*st] * t[base+a*st] (team-wide sum).
-template <typename T, int CHI, int TEAM, bool PAD = false>
+template <typename T, int CHI, int TEAM, bool PAD = false, bool PACK = false>
 __device__ __forceinline__ void close_fibers(const T* __restrict__ t, const T* __restrict__ bra, int n, int st,
                                              int fib_mul, int fib_add, int bra_shift, T* red, T* res,
                                              int tid) {
@@ -224,20 +325,93 @@ __device__ __forceinline__ void close_fibers(const T* __restrict__ t, const T* _
 #pragma unroll
   for (int i = 0; i < P2; ++i) acc[i] = T(0);
   const int nfib = n / (CHI * fib_mul);
-  for (int f = tid; f < nfib; f += TEAM) {
+  // fiber ff of leg (st, CHI) -> its first element
+  auto fiber_base = [&](int f) {
     const int ff = fib_add + fib_mul * f;
     const int lo = ff % st;
-    const int base = lo + (ff - lo) * CHI;
-    T x[CHI], y[CHI];
+    return lo + (ff - lo) * CHI;
+  };
+  if constexpr (std::is_same<T, float>::value && CHI % 2 == 0) {
+    // packed FP32x2 accumulators: pair (h, a) holds entries 2h + CHI a and 2h + 1 + CHI a,
+    // each updated by the same fmaf sequence as the scalar loop
+    constexpr int H = CHI / 2;
+    float2 acc2[H][CHI];
 #pragma unroll
-    for (int a = 0; a < CHI; ++a) {
-      x[a] = t[spos<PAD>(base + a * st)];
-      y[a] = conj_of(bra[spos<PAD>(base + bra_shift + a * st)]);
+    for (int h = 0; h < H; ++h)
+#pragma unroll
+      for (int a = 0; a < CHI; ++a) acc2[h][a] = make_float2(0.f, 0.f);
+    for (int f = tid; f < nfib; f += TEAM) {
+      const int base = fiber_base(f);
+      float x[CHI];
+      float2 y2[H];
+#pragma unroll
+      for (int a = 0; a < CHI; ++a) x[a] = t[spos<PAD>(base + a * st)];
+#pragma unroll
+      for (int h = 0; h < H; ++h)
+        y2[h] = make_float2(bra[spos<PAD>(base + bra_shift + 2 * h * st)],
+                            bra[spos<PAD>(base + bra_shift + (2 * h + 1) * st)]);
+#pragma unroll
+      for (int a = 0; a < CHI; ++a) {
+        const float2 xa = make_float2(x[a], x[a]);
+#pragma unroll
+        for (int h = 0; h < H; ++h) acc2[h][a] = __ffma2_rn(y2[h], xa, acc2[h][a]);
+      }
     }
 #pragma unroll
-    for (int a = 0; a < CHI; ++a)
+    for (int h = 0; h < H; ++h)
 #pragma unroll
-      for (int b = 0; b < CHI; ++b) acc[b + CHI * a] = mac(y[b], x[a], acc[b + CHI * a]);
+      for (int a = 0; a < CHI; ++a) {
+        acc[2 * h + CHI * a] = acc2[h][a].x;
+        acc[2 * h + 1 + CHI * a] = acc2[h][a].y;
+      }
+  } else if constexpr (std::is_same<T, df32>::value && CHI % 2 == 0 && PACK) {
+    constexpr int H = CHI / 2;
+    df32x2 acc2[H][CHI];
+#pragma unroll
+    for (int h = 0; h < H; ++h)
+#pragma unroll
+      for (int a = 0; a < CHI; ++a) acc2[h][a] = df32x2{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    for (int f = tid; f < nfib; f += TEAM) {
+      const int base = fiber_base(f);
+      df32 x[CHI];
+      df32x2 y2[H];
+#pragma unroll
+      for (int a = 0; a < CHI; ++a) x[a] = t[spos<PAD>(base + a * st)];
+#pragma unroll
+      for (int h = 0; h < H; ++h) {
+        const df32 u = bra[spos<PAD>(base + bra_shift + 2 * h * st)];
+        const df32 w = bra[spos<PAD>(base + bra_shift + (2 * h + 1) * st)];
+        y2[h] = df32x2{make_float2(u.hi, w.hi), make_float2(u.lo, w.lo)};
+      }
+#pragma unroll
+      for (int a = 0; a < CHI; ++a) {
+        const float2 bh = make_float2(x[a].hi, x[a].hi);
+        const float2 nbh = make_float2(-x[a].hi, -x[a].hi), nbl = make_float2(-x[a].lo, -x[a].lo);
+#pragma unroll
+        for (int h = 0; h < H; ++h) acc2[h][a] = mac2(y2[h], bh, nbh, nbl, acc2[h][a]);
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < H; ++h)
+#pragma unroll
+      for (int a = 0; a < CHI; ++a) {
+        acc[2 * h + CHI * a] = df32(acc2[h][a].hi.x, acc2[h][a].lo.x);
+        acc[2 * h + 1 + CHI * a] = df32(acc2[h][a].hi.y, acc2[h][a].lo.y);
+      }
+  } else {
+    for (int f = tid; f < nfib; f += TEAM) {
+      const int base = fiber_base(f);
+      T x[CHI], y[CHI];
+#pragma unroll
+      for (int a = 0; a < CHI; ++a) {
+        x[a] = t[spos<PAD>(base + a * st)];
+        y[a] = conj_of(bra[spos<PAD>(base + bra_shift + a * st)]);
+      }
+#pragma unroll
+      for (int a = 0; a < CHI; ++a)
+#pragma unroll
+        for (int b = 0; b < CHI; ++b) acc[b + CHI * a] = mac(y[b], x[a], acc[b + CHI * a]);
+    }
   }
   const int lane = tid & 31, warp = tid >> 5;
   warp_reduce_scatter<T, P2>(acc, lane);
@@ -262,18 +436,18 @@ __device__ __forceinline__ void close_fibers(const T* __restrict__ t, const T* _
   tsync<TEAM>();
 }
 
-template <typename T, int TEAM, bool PAD = false>
+template <typename T, int TEAM, bool PAD = false, bool PACK = false>
 __device__ __forceinline__ void close_any(int chi, const T* t, const T* bra, int n, int st, int fib_mul,
                                           int fib_add, int bra_shift, T* red, T* res, int tid) {
   switch (chi) {
-    case 1: close_fibers<T, 1, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 2: close_fibers<T, 2, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 3: close_fibers<T, 3, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 4: close_fibers<T, 4, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 5: close_fibers<T, 5, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 6: close_fibers<T, 6, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 7: close_fibers<T, 7, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
-    case 8: close_fibers<T, 8, TEAM, PAD>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 1: close_fibers<T, 1, TEAM, PAD, PACK>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 2: close_fibers<T, 2, TEAM, PAD, PACK>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 3: close_fibers<T, 3, TEAM, PAD, PACK>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 4: close_fibers<T, 4, TEAM, PAD, PACK>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 5: close_fibers<T, 5, TEAM, PAD, PACK>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 6: close_fibers<T, 6, TEAM, PAD, PACK>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 7: close_fibers<T, 7, TEAM, PAD, PACK>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
+    case 8: close_fibers<T, 8, TEAM, PAD, PACK>(t, bra, n, st, fib_mul, fib_add, bra_shift, red, res, tid); break;
     default: break;
   }
 }

@@ -137,13 +137,13 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
       const int leg = op.leg;
       const int chi = d.chi[leg], st = d.st[leg];
       if (op.type == 0) {
-        absorb_any<T, true>(chi, Sm.buf[op.src], Sm.buf[op.dst], d.n, st, Sm.msg + leg * 64, tid, TEAM);
+        absorb_any<T, true, TEAM == 32>(chi, Sm.buf[op.src], Sm.buf[op.dst], d.n, st, Sm.msg + leg * 64, tid, TEAM);
         tsync<TEAM>();
       } else if constexpr (TEAM > 32) {
         // the result waits in its leg's slot; close_fibers ends with a team barrier
         close_any<T, TEAM, true>(chi, Sm.buf[op.src], Sm.bra, d.n, st, 1, 0, 0, Sm.red, Sm.res + leg * 64, tid);
       } else {
-        close_any<T, TEAM, true>(chi, Sm.buf[op.src], Sm.bra, d.n, st, 1, 0, 0, Sm.red, Sm.res, tid);
+        close_any<T, TEAM, true, true>(chi, Sm.buf[op.src], Sm.bra, d.n, st, 1, 0, 0, Sm.red, Sm.res, tid);
         finalize(leg, Sm.res);
         tsync<TEAM>();
       }
