@@ -362,6 +362,39 @@ def gradient_timing(gbtn, ctx, barrier, rank, Lg=12, chig=6, reps=3):
     return out
 
 
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64 (nominal; no measured FP64 figure is available)
+
+
+def su_step_flops(net, order):
+    """Algorithmic FP64 flops of one simple-update step (every gate of `order` on
+    the network's current shapes, no environments): per side the Householder QR
+    of the (other legs) x (site, bond) matrix, 2 m c^2 - 2 c^3 / 3 with
+    c = d chi_bond; theta = R_u R_v and the gate; the SVD of theta with thin
+    U and V by the Golub-Reinsch count 14 m n^2 + 8 n^3 (Golub & Van Loan);
+    per side the reflectors applied to the kept columns, 4 m r k."""
+    tot = 0.0
+    for e in order:
+        u, v = net.edges[e]
+        ce = net.edge_dims[e]
+        sides = []
+        for x in (u, v):
+            d = net.site_dims[x]
+            n = d * int(np.prod([net.edge_dims[q] for q in net.legs[x]]))
+            m = n // (d * ce)
+            c = d * ce
+            r = min(m, c)
+            tot += 2.0 * m * c * c - 2.0 * c ** 3 / 3.0
+            sides.append((d, m, r))
+        (du, mu, ru), (dv, mv, rv) = sides
+        mt, nt = ru * du, rv * dv
+        tot += 2.0 * mt * nt * ce + 2.0 * mt * nt * du * dv
+        big, small = max(mt, nt), min(mt, nt)
+        tot += 14.0 * big * small * small + 8.0 * small ** 3
+        k = min(small, ce)
+        tot += 4.0 * mu * ru * k + 4.0 * mv * rv * k
+    return tot
+
+
 def simple_update_timing(gbtn, ctx, barrier, rank, Ls=20, steps=200, g_field=3.0, dt=0.01, chi_max=8):
     """TFIM imaginary-time evolution by simple update: H = -sum ZZ - g sum X on an
     Ls x Ls open lattice from |+>, gates exp(-dt h_e) in checkerboard order,
@@ -393,9 +426,15 @@ def simple_update_timing(gbtn, ctx, barrier, rank, Ls=20, steps=200, g_field=3.0
     pz = np.array([[1.0, 0.0], [0.0, -1.0]])
     x = bpc.expect(px)
     zz = bpc.expect2(np.kron(pz, pz))
+    step_flops = su_step_flops(net, order)
+    fp64 = {"flops_per_step": step_flops, "achieved_tflops": step_flops / last_step_s / 1e12,
+            "peak_tflops": FP64_NOMINAL_TFLOPS, "peak_source": "nominal",
+            "frac": step_flops / last_step_s / 1e12 / FP64_NOMINAL_TFLOPS,
+            "count": "Householder QRs, theta and gate, SVD with thin U/V by the Golub-Reinsch count, "
+                     "reflectors applied; the last step's shapes and time"}
     out = {"workload": f"tfim_{Ls}x{Ls}_g{g_field}_dt{dt}_{steps}steps_chimax{chi_max}_cutoff1e-10",
            "gate_updates_per_s": steps * len(order) / el, "total_s": el,
-           "gate_updates_per_s_at_chi8": len(order) / last_step_s,
+           "gate_updates_per_s_at_chi8": len(order) / last_step_s, "fp64_roofline": fp64,
            "max_bond_dim": max(st.edge_dims()), "x_per_site": float(np.mean(x)),
            "energy_per_site": float((-zz.sum() - g_field * x.sum()) / tn.nv)}
     if rank == 0:
