@@ -195,6 +195,22 @@ int gbtn_plan_counters(const gbtn_plan* plan, int64_t counts[4]);
 enum gbtn_tc_policy { GBTN_TC_AUTO = 0, GBTN_TC_ALL = 1, GBTN_TC_NATIVE = 2, GBTN_TC_OFF = 3 };
 int gbtn_plan_set_tc_policy(gbtn_plan* plan, int32_t policy);
 int gbtn_plan_tc_split(gbtn_plan* plan, int32_t* is_tc, double* tuned_ms);
+
+/* SIMT team widths (no counterpart in the reference).  Before the first
+ * parallel or coloured sweeps of each arithmetic, the plan times the vertex
+ * kernel with 32 (four vertices per block), 128 and 256 threads per vertex on
+ * up to 2048 vertices of every size class of its own network (vertex size n
+ * up to a power of two; CUDA events, best of two) and keeps the fastest width
+ * per class -- the results equal those of any width up to rounding in the
+ * close reductions.  gbtn_plan_set_simt_tuning(plan, mode) forgets the
+ * choices; mode 0 restores the fixed rule (32 threads up to n = 1024, else
+ * 256), 1 (the default) measures again at the next run, and 32, 128 or 256
+ * takes that width for every class whose shared memory allows it.  gbtn_plan_simt_teams writes the
+ * width chosen for arithmetic `arith` (0 FP64, 1 FP32, 2 df32, 3 complex FP64,
+ * 4 complex FP32) into teams[k] for the classes n <= 2^k, k < 32 (0: not
+ * measured). */
+int gbtn_plan_set_simt_tuning(gbtn_plan* plan, int32_t on);
+int gbtn_plan_simt_teams(const gbtn_plan* plan, int32_t arith, int32_t teams[32]);
 /* CUDA graphs for the parallel / coloured sweeps (no counterpart in the
  * reference): with on = 1, a run of three or more sweeps launches its first
  * sweep directly and replays the rest from a CUDA graph of two sweeps, kept

@@ -119,6 +119,11 @@ struct gbtn_plan {
   std::vector<char> tc_cand, tc_use;
   int tc_policy = GBTN_TC_AUTO;
   bool tc_tuned = false;
+  // SIMT team width per arithmetic and size class (0: the fixed rule), measured
+  // before the first parallel or coloured sweeps of each arithmetic
+  int simt_tuning = 1;
+  bool team_tuned[5] = {};
+  int team_pick[5][32] = {};
   int ncol = 0;
   double tc_tune_best_ms = 0.0;
   DevBuf<int> d_tc_slot_vertex, d_err;
@@ -449,6 +454,76 @@ void sweep_loop(gbtn_plan* P, int maxiter, const GraphKey& key, F&& sweep, bool 
 void run_large(gbtn_plan* P, size_t li, int arith, const void* fac, const void* bra, const void* in, void* out,
                const int* conv, int normalize, int want_diff, cudaStream_t s);
 
+// A work list carrying the measured team widths of arithmetic `arith`.
+WorkList picked(const WorkList& w, const gbtn_plan* P, int arith) {
+  WorkList c = w;
+  c.pick = P->team_pick[arith];
+  return c;
+}
+
+// The measured autotuner of the SIMT sweeps, keyed on the vertex shapes: for
+// every size class of the parallel work lists (vertex size n up to a power of
+// two, which with the degree fixes chi^k d), time one launch of each team
+// width that fits shared memory -- 32 (four vertices per block), 128 or 256
+// threads per vertex -- on up to 2048 of the class's own vertices with CUDA
+// events (best of two after a warm-up), and keep the fastest for that class.
+// The launches read `in` and write `out` (a message buffer the next sweep
+// overwrites), with no convergence flags.
+template <typename T, typename A>
+void tune_teams(gbtn_plan* P, const T* fac, const T* bra, const T* in, T* out) {
+  constexpr int arith = ArithOf<T, A>::value;
+  if (P->team_tuned[arith]) return;
+  P->team_tuned[arith] = true;
+  if (!P->simt_tuning) return;
+  cudaStream_t s = P->ctx->stream;
+  const size_t elt = std::is_same<A, DF32>::value ? 8 : sizeof(T);
+  cudaEvent_t e0, e1;
+  GBTN_CUDA(cudaEventCreate(&e0));
+  GBTN_CUDA(cudaEventCreate(&e1));
+  bool changed = false;
+  for (const WorkList* lst : {&P->lists[0].first, &P->lists[0].second}) {
+    for (int c = 0; c < lst->nsubs(); ++c) {
+      WorkList w = lst->sub(c);
+      if (w.count == 0) continue;
+      const int key = WorkList::class_key(w.ncap);
+      if (P->team_pick[arith][key] != 0) continue;  // tuned on another list's class of this size
+      w.count = std::min(w.count, 2048);
+      float best = 0.f;
+      int best_team = 0;
+      for (int team : {32, 128, 256}) {
+        const size_t sm = smem_need(w.ncap, w.maxdeg, bra != nullptr, elt, team) * (team == 32 ? 4 : 1);
+        if (sm > 227 * 1024) continue;
+        if (P->simt_tuning != 1) {  // one width forced wherever it fits
+          if (team == P->simt_tuning) best_team = team;
+          continue;
+        }
+        w.team = team;
+        float t = 0.f;
+        for (int rep = 0; rep < 3; ++rep) {
+          GBTN_CUDA(cudaEventRecord(e0, s));
+          launch_vertices<T, A>(w, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, nullptr, 1, 1, s);
+          GBTN_CUDA(cudaEventRecord(e1, s));
+          GBTN_CUDA(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          GBTN_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          if (rep == 1 || (rep == 2 && ms < t)) t = ms;
+        }
+        if (best_team == 0 || t < best) {
+          best = t;
+          best_team = team;
+        }
+      }
+      if (best_team != 0) {
+        P->team_pick[arith][key] = best_team;
+        changed = true;
+      }
+    }
+  }
+  GBTN_CUDA(cudaEventDestroy(e0));
+  GBTN_CUDA(cudaEventDestroy(e1));
+  if (changed) ++P->list_version;  // graphs captured before the choice are stale
+}
+
 // Sweeps of the parallel or coloured schedule on storage T in arithmetic A.
 template <typename T, typename A = T>
 void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normalize, T* msg0, T* msg1, const T* fac,
@@ -460,6 +535,8 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
   GBTN_CUDA(cudaMemsetAsync(P->d_nconv.p, 0, sizeof(int), s));
   const int* conv = want_diff ? P->d_conv.p : nullptr;
   T* msg[2] = {msg0, msg1};
+  constexpr int arith = ArithOf<T, A>::value;
+  tune_teams<T, A>(P, fac, bra, msg[cur], msg[cur ^ 1]);
   const GraphKey key{ElemTraits<A>::tag, schedule, normalize, want_diff ? 1 : 0, stall, cur, P->list_version, tol};
   constexpr int kcls = ElemTraits<A>::kcls;
   sweep_loop(P, maxiter, key, [&] {
@@ -468,13 +545,13 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
       T* out = msg[cur ^ 1];
       {
         KTimer kt(P->ctx, kcls, P->lists[0].first.count > 0);
-        launch_vertices<T, A>(P->lists[0].first, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
-                              normalize, want_diff, s);
+        launch_vertices<T, A>(picked(P->lists[0].first, P, arith), P->d_vd.p, fac, bra, in, out, P->d_msg_off.p,
+                              P->d_diffs.p, conv, normalize, want_diff, s);
       }
       {
         KTimer kt(P->ctx, kcls, P->lists[0].second.count > 0);
-        launch_vertices<T, A>(P->lists[0].second, P->d_vd.p, fac, bra, in, out, P->d_msg_off.p, P->d_diffs.p, conv,
-                              normalize, want_diff, s);
+        launch_vertices<T, A>(picked(P->lists[0].second, P, arith), P->d_vd.p, fac, bra, in, out, P->d_msg_off.p,
+                              P->d_diffs.p, conv, normalize, want_diff, s);
       }
       {
         KTimer kt(P->ctx, GBTN_KCLASS_LARGE, P->has_large);
@@ -484,10 +561,10 @@ void run_sweeps(gbtn_plan* P, int schedule, int maxiter, double tol, int normali
     } else {
       for (size_t c = 1; c < P->lists.size(); ++c) {
         T* m = msg[cur];
-        launch_vertices<T, A>(P->lists[c].first, P->d_vd.p, fac, bra, m, m, P->d_msg_off.p, P->d_diffs.p, conv,
-                              normalize, want_diff, s);
-        launch_vertices<T, A>(P->lists[c].second, P->d_vd.p, fac, bra, m, m, P->d_msg_off.p, P->d_diffs.p, conv,
-                              normalize, want_diff, s);
+        launch_vertices<T, A>(picked(P->lists[c].first, P, arith), P->d_vd.p, fac, bra, m, m, P->d_msg_off.p,
+                              P->d_diffs.p, conv, normalize, want_diff, s);
+        launch_vertices<T, A>(picked(P->lists[c].second, P, arith), P->d_vd.p, fac, bra, m, m, P->d_msg_off.p,
+                              P->d_diffs.p, conv, normalize, want_diff, s);
         run_large(P, c, ArithOf<T, A>::value, fac, bra, m, m, conv, normalize, want_diff, s);
       }
     }
@@ -2033,6 +2110,27 @@ int gbtn_plan_set_graphs(gbtn_plan* P, int32_t on) {
   if (!on) P->clear_graphs();
   P->graphs = on ? 1 : 0;
   API_CATCH(C)
+}
+
+int gbtn_plan_set_simt_tuning(gbtn_plan* P, int32_t on) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  API_TRY
+  require(P, "NULL argument");
+  GBTN_CUDA(cudaStreamSynchronize(P->ctx->stream));
+  require(on == 0 || on == 1 || on == 32 || on == 128 || on == 256, "SIMT tuning mode must be 0, 1, 32, 128 or 256");
+  P->simt_tuning = on;
+  for (int a = 0; a < 5; ++a) {
+    P->team_tuned[a] = false;
+    for (int k = 0; k < 32; ++k) P->team_pick[a][k] = 0;
+  }
+  ++P->list_version;
+  API_CATCH(C)
+}
+
+int gbtn_plan_simt_teams(const gbtn_plan* P, int32_t arith, int32_t* teams) {
+  if (!P || !teams || arith < 0 || arith > 4) return GBTN_ERR_INVALID;
+  for (int k = 0; k < 32; ++k) teams[k] = P->team_pick[arith][k];
+  return GBTN_OK;
 }
 
 int gbtn_plan_tc_split(gbtn_plan* P, int32_t* is_tc, double* tuned_ms) {

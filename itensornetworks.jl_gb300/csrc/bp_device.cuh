@@ -162,12 +162,17 @@ __device__ __forceinline__ double warp_sum(double x) {
 // warp-wide sums of entries [L*P2/32, (L+1)*P2/32) in v[0 .. P2/32).
 template <typename T, int P2>
 __device__ __forceinline__ void warp_reduce_scatter(T (&v)[P2], int lane) {
+  // step s (lane bit 4 - s): while more than one value is left, each lane keeps
+  // the half its lane bit selects and adds its partner's copy of that half;
+  // with one value left, a plain butterfly sum over the remaining lane bits
 #pragma unroll
   for (int step = 0; step < 5; ++step) {
-    constexpr int dummy = 0;
-    (void)dummy;
     const int h = P2 >> (step + 1);
     const int mask = 16 >> step;
+    if (h == 0) {
+      v[0] = v[0] + shfl_xor(v[0], mask);
+      continue;
+    }
     const bool upper = (lane & mask) != 0;
 #pragma unroll
     for (int i = 0; i < P2 / 2; ++i) {
@@ -320,7 +325,8 @@ __device__ __forceinline__ void close_fibers(const T* __restrict__ t, const T* _
                                              int fib_mul, int fib_add, int bra_shift, T* red, T* res,
                                              int tid) {
   constexpr int P = CHI * CHI;
-  constexpr int P2 = P <= 32 ? 32 : 64;
+  // accumulators padded to a power of two (the reduce-scatter's shape)
+  constexpr int P2 = P <= 1 ? 1 : P <= 4 ? 4 : P <= 16 ? 16 : P <= 32 ? 32 : 64;
   T acc[P2];
 #pragma unroll
   for (int i = 0; i < P2; ++i) acc[i] = T(0);
@@ -415,16 +421,26 @@ __device__ __forceinline__ void close_fibers(const T* __restrict__ t, const T* _
   }
   const int lane = tid & 31, warp = tid >> 5;
   warp_reduce_scatter<T, P2>(acc, lane);
-  constexpr int PER = P2 / 32;
+  // lane l now holds entries (l * PER, ...) for P2 >= 32; for P2 < 32 the top
+  // log2(P2) lane bits select the entry and every lane of a group holds it
+  constexpr int PER = P2 >= 32 ? P2 / 32 : 1;
+  constexpr int SHIFT = P2 >= 32 ? 0 : (P2 == 1 ? 5 : P2 == 4 ? 3 : 1);
+  const bool writer = (lane & ((1 << SHIFT) - 1)) == 0;
+  const int first = P2 >= 32 ? lane * PER : (lane >> SHIFT);
   if constexpr (TEAM == 32) {
+    if (writer) {
 #pragma unroll
-    for (int j = 0; j < PER; ++j) {
-      const int o = lane * PER + j;
-      if (o < P) res[o] = acc[j];
+      for (int j = 0; j < PER; ++j) {
+        const int o = first + j;
+        if (o < P) res[o] = acc[j];
+      }
     }
   } else {
+    if (writer) {
 #pragma unroll
-    for (int j = 0; j < PER; ++j) red[warp * kRedStride + lane * PER + j] = acc[j];
+      for (int j = 0; j < PER; ++j)
+        if (first + j < P) red[warp * kRedStride + first + j] = acc[j];
+    }
     __syncthreads();
     for (int o = tid; o < P; o += TEAM) {
       T s = T(0);

@@ -89,7 +89,7 @@ void upload_schedules(const DeviceSched& s) { GBTN_CUDA(cudaMemcpyToSymbol(c_sch
 // T is the arithmetic, S the storage in HBM (S = T, or double for the
 // double-FP32 refinement sweeps, whose tensors and messages stay FP64).
 template <typename T, int TEAM, typename S = T>
-__global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
+__global__ void __launch_bounds__(TEAM == 32 ? 128 : TEAM)
     bp_vertex_kernel(const int* __restrict__ work, int nwork, const VDesc* __restrict__ vd,
                      const S* __restrict__ fac, const S* __restrict__ bra_g, const S* msg_in, S* msg_out,
                      const long long* __restrict__ msg_off, double* diffs, const int* converged,
@@ -726,55 +726,53 @@ __global__ void logscalar_kernel(const int* net_v_ptr, const int* net_v, const i
 // Launchers
 // ---------------------------------------------------------------------------
 
-template <typename T>
-void launch_bp_vertices(const WorkList& wl_all, const VDesc* vd, const T* fac, const T* bra, const T* msg_in,
-                        T* msg_out, const long long* msg_off, double* diffs, const int* converged, int normalize,
-                        int want_diff, cudaStream_t s) {
-  for (int c = 0; c < wl_all.nsubs(); ++c) {
-  const WorkList wl = wl_all.sub(c);
-  if (wl.count == 0) continue;
+// One size class of a vertex list with its team width: 32 (four vertices per
+// 128-thread block), 128 or 256 threads per vertex.  T is the arithmetic, S
+// the storage.
+template <typename T, typename S>
+void launch_vertex_class(const WorkList& wl, const VDesc* vd, const S* fac, const S* bra, const S* msg_in, S* msg_out,
+                         const long long* msg_off, double* diffs, const int* converged, int normalize, int want_diff,
+                         cudaStream_t s) {
+  if (wl.count == 0) return;
   const int nbuf = wl.maxdeg <= 4 ? 3 : kNumBufs;
+  const int np = padded_len(wl.ncap);
   if (wl.team == 32) {
-    const size_t sm = 4 * team_smem_bytes<T>(padded_len(wl.ncap), nbuf, bra != nullptr, 32);
-    auto kern = bp_vertex_kernel<T, 32>;
+    const size_t sm = 4 * team_smem_bytes<T>(np, nbuf, bra != nullptr, 32);
+    auto kern = bp_vertex_kernel<T, 32, S>;
     GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    const int blocks = (wl.count + 3) / 4;
-    kern<<<blocks, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
-                                 normalize, want_diff, wl.ncap, nbuf);
+    kern<<<(wl.count + 3) / 4, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs,
+                                             converged, normalize, want_diff, wl.ncap, nbuf);
+  } else if (wl.team == 128) {
+    const size_t sm = team_smem_bytes<T>(np, nbuf, bra != nullptr, 128);
+    auto kern = bp_vertex_kernel<T, 128, S>;
+    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    kern<<<wl.count, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
+                                   normalize, want_diff, wl.ncap, nbuf);
   } else {
-    const size_t sm = team_smem_bytes<T>(padded_len(wl.ncap), nbuf, bra != nullptr, 256);
-    auto kern = bp_vertex_kernel<T, 256>;
+    const size_t sm = team_smem_bytes<T>(np, nbuf, bra != nullptr, 256);
+    auto kern = bp_vertex_kernel<T, 256, S>;
     GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     kern<<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
                                    normalize, want_diff, wl.ncap, nbuf);
   }
   GBTN_CUDA(cudaGetLastError());
-  }
+}
+
+template <typename T>
+void launch_bp_vertices(const WorkList& wl_all, const VDesc* vd, const T* fac, const T* bra, const T* msg_in,
+                        T* msg_out, const long long* msg_off, double* diffs, const int* converged, int normalize,
+                        int want_diff, cudaStream_t s) {
+  for (int c = 0; c < wl_all.nsubs(); ++c)
+    launch_vertex_class<T, T>(wl_all.sub(c), vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged, normalize,
+                              want_diff, s);
 }
 
 void launch_bp_vertices_df32(const WorkList& wl_all, const VDesc* vd, const double* fac, const double* bra,
                              const double* msg_in, double* msg_out, const long long* msg_off, double* diffs,
                              const int* converged, int normalize, int want_diff, cudaStream_t s) {
-  for (int c = 0; c < wl_all.nsubs(); ++c) {
-  const WorkList wl = wl_all.sub(c);
-  if (wl.count == 0) continue;
-  const int nbuf = wl.maxdeg <= 4 ? 3 : kNumBufs;
-  if (wl.team == 32) {
-    const size_t sm = 4 * team_smem_bytes<df32>(padded_len(wl.ncap), nbuf, bra != nullptr, 32);
-    auto kern = bp_vertex_kernel<df32, 32, double>;
-    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    const int blocks = (wl.count + 3) / 4;
-    kern<<<blocks, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
-                                 normalize, want_diff, wl.ncap, nbuf);
-  } else {
-    const size_t sm = team_smem_bytes<df32>(padded_len(wl.ncap), nbuf, bra != nullptr, 256);
-    auto kern = bp_vertex_kernel<df32, 256, double>;
-    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    kern<<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
-                                   normalize, want_diff, wl.ncap, nbuf);
-  }
-  GBTN_CUDA(cudaGetLastError());
-  }
+  for (int c = 0; c < wl_all.nsubs(); ++c)
+    launch_vertex_class<df32, double>(wl_all.sub(c), vd, fac, bra, msg_in, msg_out, msg_off, diffs, converged,
+                                      normalize, want_diff, s);
 }
 
 template void launch_bp_vertices<double>(const WorkList&, const VDesc*, const double*, const double*, const double*,

@@ -127,16 +127,28 @@ struct WorkList {
   int sub_count[kMaxSub] = {};
   int sub_ncap[kMaxSub] = {};
   int sub_maxdeg[kMaxSub] = {};
-  // The list restricted to size class i (the whole list when it has none).
+  // Measured team width per size class (host table indexed by class_key(ncap);
+  // 0 or no table: the list's own team).
+  const int* pick = nullptr;
+  // The list restricted to size class i (the whole list when it has none),
+  // with its measured team width when one was chosen.
   WorkList sub(int i) const {
     WorkList w = *this;
     w.nsub = 0;
-    if (nsub == 0) return w;
-    w.d_vertices = d_vertices + sub_begin[i];
-    w.count = sub_count[i];
-    w.ncap = sub_ncap[i];
-    w.maxdeg = sub_maxdeg[i];
+    if (nsub != 0) {
+      w.d_vertices = d_vertices + sub_begin[i];
+      w.count = sub_count[i];
+      w.ncap = sub_ncap[i];
+      w.maxdeg = sub_maxdeg[i];
+    }
+    if (pick && pick[class_key(w.ncap)] != 0) w.team = pick[class_key(w.ncap)];
     return w;
+  }
+  // ceil(log2(n)): the size class a vertex count falls in (classes are powers of two)
+  static int class_key(int n) {
+    int k = 0;
+    while ((1 << k) < n && k < 30) ++k;
+    return k;
   }
   int nsubs() const { return nsub == 0 ? 1 : nsub; }
 };

@@ -130,6 +130,8 @@ SIGNATURES = {
     "gbtn_plan_sizes": (_I, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "gbtn_plan_set_tc_policy": (_I, [_P, C.c_int32]),
     "gbtn_plan_tc_split": (_I, [_P, _I32, _D]),
+    "gbtn_plan_set_simt_tuning": (_I, [_P, C.c_int32]),
+    "gbtn_plan_simt_teams": (_I, [_P, C.c_int32, _I32]),
     "gbtn_plan_set_graphs": (_I, [_P, C.c_int32]),
     "gbtn_set_factors": (_I, [_P, _P, _P, _I]),
     "gbtn_get_factors": (_I, [_P, _P, _I]),

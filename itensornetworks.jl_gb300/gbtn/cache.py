@@ -202,6 +202,21 @@ class BeliefPropagationCache:
         self._c(self.lib.gbtn_plan_set_tc_policy(self.handle, _lib.TC_POLICIES[policy]))
         return self
 
+    def set_simt_tuning(self, mode=True):
+        """SIMT team width per size class: True = measured (default), False =
+        the fixed rule, 32 / 128 / 256 = that width wherever it fits."""
+        m = {True: 1, False: 0}.get(mode, mode) if isinstance(mode, bool) else int(mode)
+        self._c(self.lib.gbtn_plan_set_simt_tuning(self.handle, m))
+        return self
+
+    def simt_teams(self, precision="f64"):
+        """{n_bound: team} chosen for an arithmetic ("f64", "f32", "df32",
+        "z64", "z32"), n_bound = 2^k for every measured size class."""
+        arith = {"f64": 0, "f32": 1, "df32": 2, "z64": 3, "z32": 4}[precision]
+        out = np.zeros(32, dtype=np.int32)
+        self._c(self.lib.gbtn_plan_simt_teams(self.handle, arith, iptr(out)))
+        return {1 << k: int(t) for k, t in enumerate(out) if t}
+
     def set_graphs(self, on=True):
         """Replay the sweeps of parallel / coloured runs from CUDA graphs."""
         self._c(self.lib.gbtn_plan_set_graphs(self.handle, 1 if on else 0))
