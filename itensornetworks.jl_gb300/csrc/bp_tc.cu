@@ -79,12 +79,6 @@ constexpr uint32_t kIdescG1mn = tc::idesc_bf16(128, 64, 1, 0);
 constexpr uint32_t kIdescG2 = tc::idesc_bf16(64, 64, 0, 0);
 constexpr uint32_t kIdescG2mn = tc::idesc_bf16(64, 64, 0, 1);
 
-__device__ __forceinline__ double tc_warp_sum(double x) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-  return x;
-}
-
 // 32 lanes x 32 bits, 32 consecutive columns per thread; the values are valid
 // after tmem_wait_ld (several loads may be in flight before one wait).
 __device__ __forceinline__ void tmem_ld_x32(uint32_t taddr, uint32_t (&r)[32]) {
@@ -150,9 +144,14 @@ __device__ __forceinline__ int rec_chi(int chi4, int p) { return (chi4 >> (8 * p
 
 // Normalise one 8 x 8 message held by a warp (two values per lane), store its
 // compact chi x chi part as FP32, and (want_diff) return
-// message_diff(new, old) (abstractbeliefpropagationcache.jl:32-36) against
-// the previous message's entries o0, o1 (same positions, zero outside
-// chi x chi), accumulated in FP64.  Entries outside chi x chi are exact zeros.
+// message_diff(new, old) = 1 - <a, b>^2 / (|a|^2 |b|^2)
+// (abstractbeliefpropagationcache.jl:32-36) against the previous message's
+// entries o0, o1 (same positions, zero outside chi x chi).  It is formed in
+// FP32 as s - s^2 / 4 with s = |a/|a| - b/|b||^2 (= 2 - 2 cos, so
+// s - s^2 / 4 = 1 - cos^2 for either sign of cos): no cancellation, so the
+// diff keeps FP32's relative accuracy however small it is, and the FP64 pipe,
+// which three FP64 warp reductions per message kept as busy as the whole
+// contraction, is not used.  Entries outside chi x chi are exact zeros.
 __device__ __forceinline__ double tc_finalize(const float* res, float o0, float o1, float* out, int chi, int normalize,
                                               bool want_diff, int lane) {
   const float x0 = res[lane], x1 = res[lane + 32];
@@ -168,11 +167,18 @@ __device__ __forceinline__ double tc_finalize(const float* res, float o0, float 
   if (v1) out[i1] = n1;
   double diff = 0.0;
   if (want_diff) {
-    const double a0d = n0, a1d = n1, b0 = o0, b1 = o1;
-    const double dot = tc_warp_sum(a0d * b0 + a1d * b1);
-    const double na = tc_warp_sum(a0d * a0d + a1d * a1d);
-    const double nb = tc_warp_sum(b0 * b0 + b1 * b1);
-    diff = 1.0 - (dot * dot) / (na * nb);
+    float na = fmaf(n0, n0, n1 * n1), nb = fmaf(o0, o0, o1 * o1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      na += __shfl_xor_sync(0xffffffffu, na, o);
+      nb += __shfl_xor_sync(0xffffffffu, nb, o);
+    }
+    const float ia = rsqrtf(na), ib = rsqrtf(nb);
+    const float d0 = fmaf(n0, ia, -o0 * ib), d1 = fmaf(n1, ia, -o1 * ib);
+    float sd = fmaf(d0, d0, d1 * d1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
+    diff = (double)fmaf(-0.25f * sd, sd, sd);
   }
   return diff;
 }

@@ -269,3 +269,20 @@ def test_new_factors_after_a_bf16_run_rebuild_the_images(policy):
             np.testing.assert_allclose(a[de], b[de], rtol=0, atol=3e-2)
     np.testing.assert_array_equal(np.concatenate([t.ravel() for t in bpc.factors()]),
                                   np.concatenate([np.asarray(t).ravel() for t in tn2.tensors]))
+
+
+def test_bf16_message_diffs_match_the_fp64_formula():
+    # the tensor-core kernel forms message_diff in FP32 as s - s^2/4 with
+    # s = |a^ - b^|^2; on the FP32 messages themselves it equals the reference's
+    # 1 - <a,b>^2 / (|a|^2 |b|^2) evaluated in FP64 to FP32's relative accuracy
+    tn, g, A = uneven(6, 41)
+    bpc = gbtn.BeliefPropagationCache(tn).set_tc_policy("all")
+    bpc.update(maxiter=3, schedule="parallel", precision="bf16")
+    before = bpc.messages()
+    bpc.update(maxiter=1, tol=0.0, schedule="parallel", precision="bf16")
+    after = bpc.messages()
+    got = bpc.edge_diffs()
+    want = np.array([O.message_diff(after[de].astype(np.float64), before[de].astype(np.float64))
+                     for de in range(2 * g.ne)])
+    assert np.all(want > 0)
+    np.testing.assert_allclose(got, want, rtol=1e-4, atol=1e-10)
