@@ -704,12 +704,16 @@ def run_ours(args):
 
 def run_sweeps_only(args):
     """A few parallel sweeps of the batch in one arithmetic and nothing else:
-    the command the ncu captures of one message kernel run (--sweeps-only)."""
+    the command the ncu captures of one message kernel run (--sweeps-only).
+    The sweeps compute message diffs as the solve does (a tolerance no sweep
+    reaches), and take the fixed SIMT team rule so that the launch sequence is
+    the same on every run (the measured choice for this batch is the same
+    widths: 256 threads for the chi = 8 interior)."""
     import gbtn
     ctx = gbtn.Context(0)
     tn = make_batch()
-    bpc = gbtn.BeliefPropagationCache(tn, ctx=ctx)
-    bpc.update(maxiter=args.warmup + args.steps, schedule="parallel", precision=args.sweeps_only)
+    bpc = gbtn.BeliefPropagationCache(tn, ctx=ctx).set_simt_tuning(False)
+    bpc.update(maxiter=args.warmup + args.steps, tol=1e-300, schedule="parallel", precision=args.sweeps_only)
     bpc.messages()  # waits for the sweeps
     bpc.close()
     ctx.close()
