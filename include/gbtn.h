@@ -347,7 +347,8 @@ int gbtn_energy2_grad(gbtn_plan* plan, int32_t n_terms, const double* coef, cons
                       const gbtn_grad_opts* opts, double* energy, double* grad, int32_t* iters, double* resid);
 /* Vector-Jacobian product through the BP fixed point: given dL/dm for the
  * converged messages (n_message values), the gradient dL/dA (n_factor values)
- * by implicit differentiation (opts->mode must be IMPLICIT). */
+ * by implicit differentiation (opts->mode must be IMPLICIT).  Complex plans:
+ * both are dL/dRe + i dL/dIm of a real loss L, interleaved (re, im). */
 int gbtn_bp_vjp(gbtn_plan* plan, const double* msg_cot, const gbtn_grad_opts* opts, double* grad, int32_t* iters,
                 double* resid);
 
@@ -361,8 +362,11 @@ int gbtn_bp_vjp(gbtn_plan* plan, const double* msg_cot, const gbtn_grad_opts* op
  *     (abstractbeliefpropagationcache.jl:397-408) and grad = d/dA of the sum;
  *   gbtn_expect1_grad: value[n] = sum_v <O_v> over network n's vertices
  *     (expect.jl:5-19, one d x d operator O[s', s] for all) and its gradient.
- * Real FP64 quadratic-form plans whose vertices all have a link and fit the
- * shared-memory kernels; others return GBTN_ERR_UNSUPPORTED. */
+ * Complex plans take the real part of the value (log|.| for the log-norm)
+ * and return the gradient as dL/dRe + i dL/dIm (interleaved, the tensors'
+ * layout); op is then complex too.  FP64 quadratic-form plans whose vertices
+ * all have a link and fit the shared-memory kernels; others return
+ * GBTN_ERR_UNSUPPORTED. */
 int gbtn_logscalar_grad(gbtn_plan* plan, const gbtn_grad_opts* opts, double* value, double* grad, int32_t* iters,
                         double* resid);
 int gbtn_expect1_grad(gbtn_plan* plan, const double* op, const gbtn_grad_opts* opts, double* value, double* grad,

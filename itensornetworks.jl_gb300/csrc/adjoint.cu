@@ -27,39 +27,55 @@ namespace gbtn {
 namespace {
 
 // out[v] = O . A_v on the site index (O[s', s], d x d, column-major).
-__global__ void site_op_kernel(int nv, const VDesc* __restrict__ vd, const double* __restrict__ fac,
-                               const double* __restrict__ op, double* __restrict__ out) {
+template <typename T>
+__global__ void site_op_kernel(int nv, const VDesc* __restrict__ vd, const T* __restrict__ fac,
+                               const T* __restrict__ op, T* __restrict__ out) {
   const int v = blockIdx.x;
   if (v >= nv) return;
   const VDesc d = vd[v];
-  const double* a = fac + d.a_off;
-  double* o = out + d.a_off;
+  const T* a = fac + d.a_off;
+  T* o = out + d.a_off;
   for (int i = threadIdx.x; i < d.n; i += blockDim.x) {
     const int s = i % d.d, r = i - s;
-    double acc = 0.0;
-    for (int t = 0; t < d.d; ++t) acc += op[s + d.d * t] * a[r + t];
+    T acc = T(0);
+    for (int t = 0; t < d.d; ++t) acc = mac(op[s + d.d * t], a[r + t], acc);
     o[i] = acc;
   }
 }
 
-// Normalisation VJP per directed edge (one warp each).
+__device__ __forceinline__ double re_of(double x) { return x; }
+__device__ __forceinline__ double re_of(zdouble x) { return x.re; }
+__device__ __forceinline__ double abs2(double x) { return x * x; }
+__device__ __forceinline__ double abs2(zdouble x) { return x.re * x.re + x.im * x.im; }
+__device__ __forceinline__ zdouble operator*(zdouble a, zdouble b) {
+  return zdouble(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+__device__ __forceinline__ zdouble operator*(double a, zdouble b) { return zdouble(a * b.re, a * b.im); }
+__device__ __forceinline__ zdouble operator-(zdouble a, zdouble b) { return zdouble(a.re - b.re, a.im - b.im); }
+__device__ __forceinline__ zdouble zwarp_sum(zdouble x) { return zdouble(warp_sum(x.re), warp_sum(x.im)); }
+__device__ __forceinline__ double zwarp_sum(double x) { return warp_sum(x); }
+
+// Normalisation VJP per directed edge (one warp each).  Complex entries (the
+// cotangent of a real loss being dL/dRe + i dL/dIm): with n = f / |f|,
+// f_bar = (n_bar - n Re<n, n_bar>) / |f|, <x, y> = sum conj(x) y.
+template <typename T>
 __global__ void norm_vjp_kernel(int ndir, const int* __restrict__ dchi, const long long* __restrict__ msg_off,
-                                const double* __restrict__ f, const double* __restrict__ nbar,
-                                double* __restrict__ fbar) {
+                                const T* __restrict__ f, const T* __restrict__ nbar, T* __restrict__ fbar) {
   const int de = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (de >= ndir) return;
   const int c2 = dchi[de] * dchi[de];
   const long long off = msg_off[de];
-  const double f0 = lane < c2 ? f[off + lane] : 0.0, f1 = lane + 32 < c2 ? f[off + lane + 32] : 0.0;
-  const double g0 = lane < c2 ? nbar[off + lane] : 0.0, g1 = lane + 32 < c2 ? nbar[off + lane + 32] : 0.0;
-  const double nrm = sqrt(warp_sum(f0 * f0 + f1 * f1));
-  double r0 = 0.0, r1 = 0.0;
+  const T zero = T(0);
+  const T f0 = lane < c2 ? f[off + lane] : zero, f1 = lane + 32 < c2 ? f[off + lane + 32] : zero;
+  const T g0 = lane < c2 ? nbar[off + lane] : zero, g1 = lane + 32 < c2 ? nbar[off + lane + 32] : zero;
+  const double nrm = sqrt(warp_sum(abs2(f0) + abs2(f1)));
+  T r0 = zero, r1 = zero;
   if (nrm > 0.0) {
     const double inv = 1.0 / nrm;
-    const double dot = warp_sum(f0 * g0 + f1 * g1) * inv;  // <n, n_bar>
-    r0 = (g0 - dot * f0 * inv) * inv;
-    r1 = (g1 - dot * f1 * inv) * inv;
+    const double dot = warp_sum(re_of(conj_of(f0) * g0) + re_of(conj_of(f1) * g1)) * inv;  // Re<n, n_bar>
+    r0 = inv * (g0 - (dot * inv) * f0);
+    r1 = inv * (g1 - (dot * inv) * f1);
   }
   if (lane < c2) fbar[off + lane] = r0;
   if (lane + 32 < c2) fbar[off + lane + 32] = r1;
@@ -68,29 +84,39 @@ __global__ void norm_vjp_kernel(int ndir, const int* __restrict__ dchi, const lo
 // One CTA per vertex (256 threads); see the file comment.  mbar / abar may be
 // NULL to skip that part.  Results are accumulated (+=): mbar by incoming
 // directed edge (each one belongs to exactly one vertex), abar by tensor entry.
+//
+// Complex tensors (T = zdouble; the forward message is
+// F_w = sum conj(A[s,b]) K[s,a] prod m, and a cotangent is dL/dRe + i dL/dIm
+// of a real loss): with the outgoing cotangents conjugated on load (Cc = conj C),
+//   dL/dm_p = conj(CLOSE_p(K absorbed with m_q and Cc_w, bra A)),
+//   dL/dK   = conj(conj(A) absorbed with every m_q^T and Cc_w^T),
+//   dL/dA   = O^H dL/dK + K absorbed with every m_q and Cc_w;
+// every conj is the identity for real tensors, which gives the real rules.
 constexpr int kVjpTeam = 256;
 
+template <typename T>
 __global__ void __launch_bounds__(kVjpTeam)
     vertex_vjp_kernel(const int* __restrict__ work, int nwork, const VDesc* __restrict__ vd,
-                      const double* __restrict__ ket, const double* __restrict__ bra, const double* __restrict__ msgs,
-                      const double* __restrict__ cot, const long long* __restrict__ msg_off, const double* __restrict__ op,
-                      double* mbar, double* abar, int ncap) {
+                      const T* __restrict__ ket, const T* __restrict__ bra, const T* __restrict__ msgs,
+                      const T* __restrict__ cot, const long long* __restrict__ msg_off, const T* __restrict__ op,
+                      T* mbar, T* abar, int ncap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TEAM = kVjpTeam;
   const int tid = threadIdx.x;
   VDesc* D = reinterpret_cast<VDesc*>(smem_raw);
-  double* base = reinterpret_cast<double*>(smem_raw + align_up(sizeof(VDesc), 16));
-  double* K = base;
-  double* B = K + ncap;
-  double* W[2] = {B + ncap, B + 2 * (size_t)ncap};
-  double* GK = B + 3 * (size_t)ncap;
-  double* GB = B + 4 * (size_t)ncap;
-  double* MS = B + 5 * (size_t)ncap;  // incoming messages, kMaxDeg x 64
-  double* CT = MS + kMaxDeg * 64;     // cotangents of outgoing messages, kMaxDeg x 64
-  double* MT = CT + kMaxDeg * 64;     // one transposed message
-  double* MB = MT + 64;               // accumulated incoming-message cotangents, kMaxDeg x 64
-  double* red = MB + kMaxDeg * 64;    // (TEAM/32) x kRedStride
-  double* res = red + (TEAM / 32) * kRedStride;
+  T* base = reinterpret_cast<T*>(smem_raw + align_up(sizeof(VDesc), 16));
+  T* K = base;
+  T* B = K + ncap;
+  T* W[2] = {B + ncap, B + 2 * (size_t)ncap};
+  T* GK = B + 3 * (size_t)ncap;
+  T* GB = B + 4 * (size_t)ncap;
+  T* MS = B + 5 * (size_t)ncap;  // incoming messages, kMaxDeg x 64
+  T* CT = MS + kMaxDeg * 64;     // conjugated cotangents of outgoing messages, kMaxDeg x 64
+  T* MT = CT + kMaxDeg * 64;     // one transposed message
+  T* MB = MT + 64;               // accumulated incoming-message cotangents, kMaxDeg x 64
+  T* red = MB + kMaxDeg * 64;    // (TEAM/32) x kRedStride
+  T* res = red + (TEAM / 32) * kRedStride;
+  const T zero = T(0);
   for (int w_ = blockIdx.x; w_ < nwork; w_ += gridDim.x) {
     const int v = work[w_];
     load_desc<TEAM>(D, vd + v, tid);
@@ -100,15 +126,15 @@ __global__ void __launch_bounds__(kVjpTeam)
     for (int i = tid; i < n; i += TEAM) {
       K[i] = ket[d.a_off + i];
       B[i] = bra[d.a_off + i];
-      GK[i] = 0.0;
-      GB[i] = 0.0;
+      GK[i] = zero;
+      GB[i] = zero;
     }
     for (int p = 0; p < k; ++p) {
       const int c2 = d.chi[p] * d.chi[p];
       for (int i = tid; i < c2; i += TEAM) {
         MS[p * 64 + i] = msgs[msg_off[d.in_de[p]] + i];
-        CT[p * 64 + i] = cot[msg_off[d.out_de[p]] + i];
-        MB[p * 64 + i] = 0.0;
+        CT[p * 64 + i] = conj_of(cot[msg_off[d.out_de[p]] + i]);
+        MB[p * 64 + i] = zero;
       }
     }
     __syncthreads();
@@ -116,17 +142,17 @@ __global__ void __launch_bounds__(kVjpTeam)
       for (int w = 0; w < k; ++w)
         for (int p = 0; p < k; ++p) {
           if (p == w) continue;
-          const double* cur = K;
+          const T* cur = K;
           int nx = 0;
           for (int q = 0; q < k; ++q) {
             if (q == p) continue;
-            absorb_any<double>(d.chi[q], cur, W[nx], n, d.st[q], q == w ? CT + w * 64 : MS + q * 64, tid, TEAM);
+            absorb_any<T>(d.chi[q], cur, W[nx], n, d.st[q], q == w ? CT + w * 64 : MS + q * 64, tid, TEAM);
             __syncthreads();
             cur = W[nx];
             nx ^= 1;
           }
-          close_any<double, TEAM>(d.chi[p], cur, B, n, d.st[p], 1, 0, 0, red, res, tid);
-          for (int i = tid; i < d.chi[p] * d.chi[p]; i += TEAM) MB[p * 64 + i] += res[i];
+          close_any<T, TEAM>(d.chi[p], cur, B, n, d.st[p], 1, 0, 0, red, res, tid);
+          for (int i = tid; i < d.chi[p] * d.chi[p]; i += TEAM) MB[p * 64 + i] += conj_of(res[i]);
           __syncthreads();
         }
       for (int p = 0; p < k; ++p) {
@@ -136,26 +162,32 @@ __global__ void __launch_bounds__(kVjpTeam)
       }
     }
     if (abar) {
+      if constexpr (!std::is_same<T, double>::value) {
+        // the ket-side rule reads conj(A); the incoming-message part above was
+        // the only other reader of B
+        for (int i = tid; i < n; i += TEAM) B[i] = conj_of(B[i]);
+        __syncthreads();
+      }
       for (int w = 0; w < k; ++w) {
-        // dL/dK: the bra absorbed with every transposed message
-        const double* cur = B;
+        // dL/dK: conj(A) absorbed with every transposed message, conjugated at the end
+        const T* cur = B;
         int nx = 0;
         for (int q = 0; q < k; ++q) {
           const int c = d.chi[q];
-          const double* M = q == w ? CT + w * 64 : MS + q * 64;
+          const T* M = q == w ? CT + w * 64 : MS + q * 64;
           for (int i = tid; i < c * c; i += TEAM) MT[(i / c) + c * (i % c)] = M[i];
           __syncthreads();
-          absorb_any<double>(c, cur, W[nx], n, d.st[q], MT, tid, TEAM);
+          absorb_any<T>(c, cur, W[nx], n, d.st[q], MT, tid, TEAM);
           __syncthreads();
           cur = W[nx];
           nx ^= 1;
         }
-        for (int i = tid; i < n; i += TEAM) GK[i] += cur[i];
+        for (int i = tid; i < n; i += TEAM) GK[i] += conj_of(cur[i]);
         __syncthreads();
         // dL/dA (bra side): the ket absorbed with every message
         cur = K;
         for (int q = 0; q < k; ++q) {
-          absorb_any<double>(d.chi[q], cur, W[nx], n, d.st[q], q == w ? CT + w * 64 : MS + q * 64, tid, TEAM);
+          absorb_any<T>(d.chi[q], cur, W[nx], n, d.st[q], q == w ? CT + w * 64 : MS + q * 64, tid, TEAM);
           __syncthreads();
           cur = W[nx];
           nx ^= 1;
@@ -163,16 +195,93 @@ __global__ void __launch_bounds__(kVjpTeam)
         for (int i = tid; i < n; i += TEAM) GB[i] += cur[i];
         __syncthreads();
       }
-      // abar += O^T . GK + GB
+      // abar += O^H . GK + GB
       for (int i = tid; i < n; i += TEAM) {
         const int s = i % d.d, r = i - s;
-        double acc = GB[i];
-        for (int t = 0; t < d.d; ++t) acc += (op ? op[t + d.d * s] : (t == s ? 1.0 : 0.0)) * GK[r + t];
+        T acc = GB[i];
+        for (int t = 0; t < d.d; ++t) {
+          if (op)
+            acc = mac(conj_of(op[t + d.d * s]), GK[r + t], acc);
+          else if (t == s)
+            acc += GK[r + t];
+        }
         abar[d.a_off + i] += acc;
       }
     }
     __syncthreads();
   }
+}
+
+// Complex networks: remove from a message cotangent lam its component along the
+// message's own phase direction i m (real inner product Im<m, lam>), one warp
+// per directed edge.  Every loss built from region scalars is invariant under
+// a phase per message, and the BP Jacobian maps those phase directions into
+// themselves with gain ~3 per sweep (the phase of m_{u->v} reaches every
+// m_{v->w}), so the adjoint solution has no such component while rounding in
+// the adjoint iteration would feed one that grows threefold per iteration.
+__global__ void phase_project_kernel(int ndir, const int* __restrict__ dchi, const long long* __restrict__ msg_off,
+                                     const zdouble* __restrict__ m, zdouble* lam) {
+  const int de = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (de >= ndir) return;
+  const int c2 = dchi[de] * dchi[de];
+  const long long off = msg_off[de];
+  double im = 0.0, n2 = 0.0;
+  for (int i = lane; i < c2; i += 32) {
+    const zdouble a = m[off + i], b = lam[off + i];
+    im += a.re * b.im - a.im * b.re;
+    n2 += a.re * a.re + a.im * a.im;
+  }
+  im = warp_sum(im);
+  n2 = warp_sum(n2);
+  if (n2 <= 0.0) return;
+  const double t = im / n2;
+  for (int i = lane; i < c2; i += 32) {
+    const zdouble a = m[off + i];
+    lam[off + i] = zdouble(lam[off + i].re + t * a.im, lam[off + i].im - t * a.re);
+  }
+}
+
+// Complex networks: the phase by which one sweep moves each message.  BP on a
+// loopy complex network does not settle the phases of its messages (they
+// drift), so one sweep from the converged messages m returns n = R m with R a
+// unit complex factor per message, rho_e = <m_e, f_e> / |<m_e, f_e>|
+// (f the unnormalised update).  The adjoint linearises f^ = R^-1 f, which has
+// m as its exact fixed point; every loss here is invariant under message
+// phases, so its value and gradient are those of the quotient, and
+// (df^/dm)^H = (df/dm)^H R: each message cotangent is multiplied by rho_e
+// before the VJP of the update.  One warp per directed edge.
+__global__ void edge_phase_kernel(int ndir, const int* __restrict__ dchi, const long long* __restrict__ msg_off,
+                                  const zdouble* __restrict__ m, const zdouble* __restrict__ f, zdouble* rho) {
+  const int de = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (de >= ndir) return;
+  const int c2 = dchi[de] * dchi[de];
+  const long long off = msg_off[de];
+  double re = 0.0, im = 0.0;
+  for (int i = lane; i < c2; i += 32) {
+    const zdouble a = m[off + i], b = f[off + i];
+    re += a.re * b.re + a.im * b.im;
+    im += a.re * b.im - a.im * b.re;
+  }
+  re = warp_sum(re);
+  im = warp_sum(im);
+  if (lane == 0) {
+    const double r = sqrt(re * re + im * im);
+    rho[de] = r > 0.0 ? zdouble(re / r, im / r) : zdouble(1.0, 0.0);
+  }
+}
+
+// out_e = rho_e * in_e per directed edge (one warp each).
+__global__ void edge_rotate_kernel(int ndir, const int* __restrict__ dchi, const long long* __restrict__ msg_off,
+                                   const zdouble* __restrict__ rho, const zdouble* __restrict__ in, zdouble* out) {
+  const int de = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (de >= ndir) return;
+  const int c2 = dchi[de] * dchi[de];
+  const long long off = msg_off[de];
+  const zdouble r = rho[de];
+  for (int i = lane; i < c2; i += 32) out[off + i] = r * in[off + i];
 }
 
 // Per edge: t[e] = <F[2e], F[2e+1]> (one warp per edge).
@@ -259,115 +368,165 @@ __global__ void axpy_resid_kernel(long long n, const double* __restrict__ a, con
 
 }  // namespace
 
-size_t vertex_vjp_smem(int ncap) {
+size_t vertex_vjp_smem(int ncap, size_t elt) {
   return align_up(sizeof(VDesc), 16) +
-         sizeof(double) * (6 * (size_t)ncap + 3 * kMaxDeg * 64 + 64 + (kVjpTeam / 32) * kRedStride + 64);
+         elt * (6 * (size_t)ncap + 3 * kMaxDeg * 64 + 64 + (kVjpTeam / 32) * kRedStride + 64);
 }
 
-void launch_site_op(int nv, const VDesc* vd, const double* fac, const double* op, double* out, cudaStream_t s) {
-  site_op_kernel<<<nv, 256, 0, s>>>(nv, vd, fac, op, out);
+template <typename T>
+void launch_site_op(int nv, const VDesc* vd, const T* fac, const T* op, T* out, cudaStream_t s) {
+  site_op_kernel<T><<<nv, 256, 0, s>>>(nv, vd, fac, op, out);
   GBTN_CUDA(cudaGetLastError());
 }
 
 // Vertex terms of the log-norm and of one-site expectation values, as
 // contractions of an unnormalised outgoing message with the incoming one on
 // the same leg (leg 0 of every vertex): the full contraction of a partition is
-// D_v = <F_{v->w}, m_{w->v}> (region_scalar, beliefpropagationcache.jl:107-113),
-// and with O applied to the ket N_v = <F^O_{v->w}, m_{w->v}> = tr(rho_v O).
-// One warp per vertex (degree >= 1).
+// D_v = <F_{v->w}, m_{w->v}> = sum F m (bilinear; region_scalar,
+// beliefpropagationcache.jl:107-113), and with O applied to the ket
+// N_v = sum F^O m = tr(rho_v O).  One warp per vertex (degree >= 1).  The loss
+// is real: log|D_v| = Re log D_v, and Re(N_v / D_v); a cotangent is the
+// conjugate of the holomorphic derivative (dL/dRe + i dL/dIm), which for real
+// tensors is the derivative itself.
 //   mode 0 (log-norm, logscalar abstractbeliefpropagationcache.jl:397-408):
-//     val[v] = log|D_v|; cotangent of F_{v->w}: m_{w->v} / D_v (into ci);
-//     g[w->v] += F_{v->w} / D_v.
-//   mode 1 (expect, expect.jl:5-19): val[v] = N_v / D_v; cotangents
-//     co (of F^O_{v->w}) = m / D_v and ci (of F_{v->w}) = -N_v / D_v^2 m;
-//     g[w->v] += F^O / D_v - N_v / D_v^2 F.
+//     val[v] = log|D_v|; cotangent of F_{v->w}: conj(m_{w->v} / D_v) (into ci);
+//     g[w->v] += conj(F_{v->w} / D_v).
+//   mode 1 (expect, expect.jl:5-19): val[v] = Re(N_v / D_v); cotangents
+//     co (of F^O_{v->w}) = conj(m / D_v) and ci (of F_{v->w}) = conj(-N_v / D_v^2 m);
+//     g[w->v] += conj(F^O / D_v - N_v / D_v^2 F).
+__device__ __forceinline__ double inv_of(double x) { return 1.0 / x; }
+__device__ __forceinline__ zdouble inv_of(zdouble x) {
+  const double r = 1.0 / (x.re * x.re + x.im * x.im);
+  return zdouble(x.re * r, -x.im * r);
+}
+__device__ __forceinline__ double log_abs(double x) { return log(fabs(x)); }
+__device__ __forceinline__ double log_abs(zdouble x) { return 0.5 * log(x.re * x.re + x.im * x.im); }
+
+template <typename T>
 __global__ void vertex_term_cot_kernel(int nv, const VDesc* __restrict__ vd, const long long* __restrict__ msg_off,
-                                       const double* __restrict__ msgs, const double* __restrict__ F,
-                                       const double* __restrict__ FO, int mode, double* ci, double* co, double* g,
-                                       double* val) {
+                                       const T* __restrict__ msgs, const T* __restrict__ F,
+                                       const T* __restrict__ FO, int mode, T* ci, T* co, T* g, double* val) {
   const int v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (v >= nv) return;
   const VDesc& d = vd[v];
   const int c2 = d.chi[0] * d.chi[0];
   const long long oo = msg_off[d.out_de[0]], oi = msg_off[d.in_de[0]];
-  double dd = 0.0, nn = 0.0;
+  T dd = T(0), nn = T(0);
   for (int i = lane; i < c2; i += 32) {
-    dd = fma(F[oo + i], msgs[oi + i], dd);
-    if (mode == 1) nn = fma(FO[oo + i], msgs[oi + i], nn);
+    dd = mac(F[oo + i], msgs[oi + i], dd);
+    if (mode == 1) nn = mac(FO[oo + i], msgs[oi + i], nn);
   }
-  dd = warp_sum(dd);
-  nn = warp_sum(nn);
-  const double inv = 1.0 / dd;
+  dd = zwarp_sum(dd);
+  nn = zwarp_sum(nn);
+  const T inv = inv_of(dd);
   if (mode == 0) {
     for (int i = lane; i < c2; i += 32) {
-      ci[oo + i] = msgs[oi + i] * inv;
-      g[oi + i] += F[oo + i] * inv;
+      ci[oo + i] = conj_of(msgs[oi + i] * inv);
+      g[oi + i] += conj_of(F[oo + i] * inv);
     }
-    if (lane == 0) val[v] = log(fabs(dd));
+    if (lane == 0) val[v] = log_abs(dd);
   } else {
-    const double r = nn * inv * inv;
+    const T r = nn * inv * inv;
     for (int i = lane; i < c2; i += 32) {
-      co[oo + i] = msgs[oi + i] * inv;
-      ci[oo + i] = -r * msgs[oi + i];
-      g[oi + i] += FO[oo + i] * inv - r * F[oo + i];
+      co[oo + i] = conj_of(msgs[oi + i] * inv);
+      ci[oo + i] = conj_of(T(0) - r * msgs[oi + i]);
+      g[oi + i] += conj_of(FO[oo + i] * inv - r * F[oo + i]);
     }
-    if (lane == 0) val[v] = nn * inv;
+    if (lane == 0) val[v] = re_of(nn * inv);
   }
 }
 
-// Edge terms of the log-norm: z_e = <m_e, m_ebar>, val[e] = log|z_e|,
-// g[e] -= m_ebar / z_e and g[ebar] -= m_e / z_e.  One warp per edge.
+// Edge terms of the log-norm: z_e = sum m_e m_ebar, val[e] = log|z_e|,
+// g[e] -= conj(m_ebar / z_e) and g[ebar] -= conj(m_e / z_e).  One warp per edge.
+template <typename T>
 __global__ void edge_term_cot_kernel(int ne, const int* __restrict__ dchi, const long long* __restrict__ msg_off,
-                                     const double* __restrict__ msgs, double* g, double* val) {
+                                     const T* __restrict__ msgs, T* g, double* val) {
   const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (e >= ne) return;
   const int c2 = dchi[2 * e] * dchi[2 * e];
   const long long o1 = msg_off[2 * e], o2 = msg_off[2 * e + 1];
-  double z = 0.0;
-  for (int i = lane; i < c2; i += 32) z = fma(msgs[o1 + i], msgs[o2 + i], z);
-  z = warp_sum(z);
-  const double inv = 1.0 / z;
+  T z = T(0);
+  for (int i = lane; i < c2; i += 32) z = mac(msgs[o1 + i], msgs[o2 + i], z);
+  z = zwarp_sum(z);
+  const T inv = inv_of(z);
   for (int i = lane; i < c2; i += 32) {
-    const double a = msgs[o1 + i], b = msgs[o2 + i];
-    g[o1 + i] -= b * inv;
-    g[o2 + i] -= a * inv;
+    const T a = msgs[o1 + i], b = msgs[o2 + i];
+    g[o1 + i] = g[o1 + i] - conj_of(b * inv);
+    g[o2 + i] = g[o2 + i] - conj_of(a * inv);
   }
-  if (lane == 0) val[e] = log(fabs(z));
+  if (lane == 0) val[e] = log_abs(z);
 }
 
-void launch_vertex_term_cot(int nv, const VDesc* vd, const long long* msg_off, const double* msgs, const double* F,
-                            const double* FO, int mode, double* ci, double* co, double* g, double* val,
-                            cudaStream_t s) {
+template <typename T>
+void launch_vertex_term_cot(int nv, const VDesc* vd, const long long* msg_off, const T* msgs, const T* F,
+                            const T* FO, int mode, T* ci, T* co, T* g, double* val, cudaStream_t s) {
   if (nv == 0) return;
-  vertex_term_cot_kernel<<<(nv + 7) / 8, 256, 0, s>>>(nv, vd, msg_off, msgs, F, FO, mode, ci, co, g, val);
+  vertex_term_cot_kernel<T><<<(nv + 7) / 8, 256, 0, s>>>(nv, vd, msg_off, msgs, F, FO, mode, ci, co, g, val);
   GBTN_CUDA(cudaGetLastError());
 }
 
-void launch_edge_term_cot(int ne, const int* dchi, const long long* msg_off, const double* msgs, double* g,
-                          double* val, cudaStream_t s) {
+template <typename T>
+void launch_edge_term_cot(int ne, const int* dchi, const long long* msg_off, const T* msgs, T* g, double* val,
+                          cudaStream_t s) {
   if (ne == 0) return;
-  edge_term_cot_kernel<<<(ne + 7) / 8, 256, 0, s>>>(ne, dchi, msg_off, msgs, g, val);
+  edge_term_cot_kernel<T><<<(ne + 7) / 8, 256, 0, s>>>(ne, dchi, msg_off, msgs, g, val);
   GBTN_CUDA(cudaGetLastError());
 }
 
-void launch_norm_vjp(int ndir, const int* dchi, const long long* msg_off, const double* f, const double* nbar,
-                     double* fbar, cudaStream_t s) {
+template <typename T>
+void launch_norm_vjp(int ndir, const int* dchi, const long long* msg_off, const T* f, const T* nbar, T* fbar,
+                     cudaStream_t s) {
   if (ndir == 0) return;
-  norm_vjp_kernel<<<(ndir + 7) / 8, 256, 0, s>>>(ndir, dchi, msg_off, f, nbar, fbar);
+  norm_vjp_kernel<T><<<(ndir + 7) / 8, 256, 0, s>>>(ndir, dchi, msg_off, f, nbar, fbar);
   GBTN_CUDA(cudaGetLastError());
 }
 
-void launch_vertex_vjp(const int* work, int nwork, const VDesc* vd, const double* ket, const double* bra,
-                       const double* msgs, const double* cot, const long long* msg_off, const double* op, double* mbar,
-                       double* abar, int ncap, cudaStream_t s) {
+template <typename T>
+void launch_vertex_vjp(const int* work, int nwork, const VDesc* vd, const T* ket, const T* bra, const T* msgs,
+                       const T* cot, const long long* msg_off, const T* op, T* mbar, T* abar, int ncap,
+                       cudaStream_t s) {
   if (nwork == 0) return;
-  const size_t sm = vertex_vjp_smem(ncap);
-  GBTN_CUDA(cudaFuncSetAttribute(vertex_vjp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  vertex_vjp_kernel<<<nwork, kVjpTeam, sm, s>>>(work, nwork, vd, ket, bra, msgs, cot, msg_off, op, mbar, abar, ncap);
+  const size_t sm = vertex_vjp_smem(ncap, sizeof(T));
+  GBTN_CUDA(cudaFuncSetAttribute(vertex_vjp_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  vertex_vjp_kernel<T><<<nwork, kVjpTeam, sm, s>>>(work, nwork, vd, ket, bra, msgs, cot, msg_off, op, mbar, abar,
+                                                   ncap);
   GBTN_CUDA(cudaGetLastError());
 }
+
+void launch_phase_project(int ndir, const int* dchi, const long long* msg_off, const zdouble* m, zdouble* lam,
+                          cudaStream_t s) {
+  if (ndir == 0) return;
+  phase_project_kernel<<<(ndir + 7) / 8, 256, 0, s>>>(ndir, dchi, msg_off, m, lam);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_edge_phase(int ndir, const int* dchi, const long long* msg_off, const zdouble* m, const zdouble* f,
+                       zdouble* rho, cudaStream_t s) {
+  if (ndir == 0) return;
+  edge_phase_kernel<<<(ndir + 7) / 8, 256, 0, s>>>(ndir, dchi, msg_off, m, f, rho);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void launch_edge_rotate(int ndir, const int* dchi, const long long* msg_off, const zdouble* rho, const zdouble* in,
+                        zdouble* out, cudaStream_t s) {
+  if (ndir == 0) return;
+  edge_rotate_kernel<<<(ndir + 7) / 8, 256, 0, s>>>(ndir, dchi, msg_off, rho, in, out);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+#define GBTN_ADJOINT_INSTANTIATE(T)                                                                                \
+  template void launch_site_op<T>(int, const VDesc*, const T*, const T*, T*, cudaStream_t);                        \
+  template void launch_vertex_term_cot<T>(int, const VDesc*, const long long*, const T*, const T*, const T*, int,  \
+                                          T*, T*, T*, double*, cudaStream_t);                                      \
+  template void launch_edge_term_cot<T>(int, const int*, const long long*, const T*, T*, double*, cudaStream_t);   \
+  template void launch_norm_vjp<T>(int, const int*, const long long*, const T*, const T*, T*, cudaStream_t);       \
+  template void launch_vertex_vjp<T>(const int*, int, const VDesc*, const T*, const T*, const T*, const T*,        \
+                                     const long long*, const T*, T*, T*, int, cudaStream_t);
+GBTN_ADJOINT_INSTANTIATE(double)
+GBTN_ADJOINT_INSTANTIATE(zdouble)
+#undef GBTN_ADJOINT_INSTANTIATE
 
 void launch_edge_dot(int ne, const int* dchi, const long long* msg_off, const double* F, double* out, cudaStream_t s) {
   if (ne == 0) return;

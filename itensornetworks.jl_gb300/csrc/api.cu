@@ -194,6 +194,11 @@ namespace {
 // The interleaved (re, im) doubles of a complex plan's arrays as elements.
 inline zdouble* zptr(double* p) { return reinterpret_cast<zdouble*>(p); }
 inline zfloat* zfptr(float* p) { return reinterpret_cast<zfloat*>(p); }
+// An interleaved double buffer as elements of T (double, or zdouble for complex plans).
+template <typename T>
+inline T* as(double* p) { return reinterpret_cast<T*>(p); }
+template <typename T>
+inline const T* as(const double* p) { return reinterpret_cast<const T*>(p); }
 
 // Arithmetic tag of the double-FP32 sweeps (FP64 storage, df32 arithmetic).
 struct DF32 {};
@@ -2462,17 +2467,26 @@ struct Energy2 {
 // Unnormalised (or normalised) messages of every directed edge computed with
 // ket tensor `ket` and bra = the plan's tensors (bra pointer NULL when ket is
 // the plan's own tensors).
-void raw_forward(gbtn_plan* P, const double* ket, const double* bra, const double* msgs, double* out, int normalize) {
+template <typename T>
+void raw_forward_t(gbtn_plan* P, const double* ket, const double* bra, const double* msgs, double* out, int normalize) {
   cudaStream_t s = P->ctx->stream;
-  launch_bp_vertices<double>(P->lists[0].first, P->d_vd.p, ket, bra, msgs, out, P->d_msg_off.p, P->d_diffs.p, nullptr,
-                             normalize, 0, s);
-  launch_bp_vertices<double>(P->lists[0].second, P->d_vd.p, ket, bra, msgs, out, P->d_msg_off.p, P->d_diffs.p,
-                             nullptr, normalize, 0, s);
+  launch_bp_vertices<T>(P->lists[0].first, P->d_vd.p, as<T>(ket), as<T>(bra), as<T>(msgs), as<T>(out),
+                        P->d_msg_off.p, P->d_diffs.p, nullptr, normalize, 0, s);
+  launch_bp_vertices<T>(P->lists[0].second, P->d_vd.p, as<T>(ket), as<T>(bra), as<T>(msgs), as<T>(out),
+                        P->d_msg_off.p, P->d_diffs.p, nullptr, normalize, 0, s);
+}
+
+// (Complex plans: interleaved (re, im) doubles.)
+void raw_forward(gbtn_plan* P, const double* ket, const double* bra, const double* msgs, double* out, int normalize) {
+  if (P->cplx)
+    raw_forward_t<zdouble>(P, ket, bra, msgs, out, normalize);
+  else
+    raw_forward_t<double>(P, ket, bra, msgs, out, normalize);
 }
 
 const double* term_ket(Energy2& E, int k) {
   if (k == 0) return E.P->d_fac.p;
-  launch_site_op(E.P->nv, E.P->d_vd.p, E.P->d_fac.p, E.ops.p + (size_t)(k - 1) * E.d * E.d, E.ket.p,
+  launch_site_op<double>(E.P->nv, E.P->d_vd.p, E.P->d_fac.p, E.ops.p + (size_t)(k - 1) * E.d * E.d, E.ket.p,
                  E.P->ctx->stream);
   return E.ket.p;
 }
@@ -2526,33 +2540,64 @@ void energy_direct_vjp(Energy2& E, const double* msgs, double* cot, double* g, d
   for (int k = 0; k <= E.nterms; ++k) {
     launch_energy_cot(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, E.F[k]->p, E.scale.p + (size_t)k * P->ne, cot, s);
     const double* ket = term_ket(E, k);
-    launch_vertex_vjp(E.allv.p, P->nv, P->d_vd.p, ket, P->d_fac.p, msgs, cot, P->d_msg_off.p,
-                      k == 0 ? nullptr : E.ops.p + (size_t)(k - 1) * E.d * E.d, g, grad, P->ncap, s);
+    launch_vertex_vjp<double>(E.allv.p, P->nv, P->d_vd.p, ket, P->d_fac.p, msgs, cot, P->d_msg_off.p,
+                              k == 0 ? nullptr : E.ops.p + (size_t)(k - 1) * E.d * E.d, g, grad, P->ncap, s);
   }
 }
 
-// lambda = g + (dF/dm)^T lambda at the fixed point `msgs`, then grad += (dF/dA)^T lambda.
-void implicit_adjoint(gbtn_plan* P, const int* allv, const double* msgs, const double* g, double* grad, int maxiter,
-                      double tol, int32_t* iters, double* resid) {
+// lambda = g + (dF/dm)^T lambda at the fixed point `msgs`, then grad += (dF/dA)^T lambda
+// (T = zdouble for complex plans: conjugate-transposed products, cotangents dL/dRe + i dL/dIm).
+template <typename T>
+void implicit_adjoint_t(gbtn_plan* P, const int* allv, const double* msgs_d, const double* g_d, double* grad_d,
+                        int maxiter, double tol, int32_t* iters, double* resid) {
+  constexpr bool cplx = std::is_same<T, zdouble>::value;
   cudaStream_t s = P->ctx->stream;
-  const long long nm = std::max<long long>(P->n_msg, 1);
-  DevBuf<double> fraw, fbar, lam, lam2, mbar, acc;
+  const long long nm = std::max<long long>(P->n_msg, 1) * (long long)(sizeof(T) / sizeof(double));
+  const int ndir = 2 * P->ne;
+  const T* msgs = as<T>(msgs_d);
+  T* grad = as<T>(grad_d);
+  DevBuf<double> fraw, fbar, lam, lam2, mbar, acc, gp, lrot, rho;
   fraw.alloc(nm);
   fbar.alloc(nm);
   lam.alloc(nm);
   lam2.alloc(nm);
   mbar.alloc(nm);
   acc.alloc(2);
-  raw_forward(P, P->d_fac.p, nullptr, msgs, fraw.p, 0);
-  GBTN_CUDA(cudaMemcpyAsync(lam.p, g, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
+  raw_forward(P, P->d_fac.p, nullptr, msgs_d, fraw.p, 0);
+  // complex: the cotangent without its message-phase components, and the phase
+  // each message takes in one sweep (see edge_phase_kernel)
+  const double* g0 = g_d;
+  auto project = [&](double* x) {
+    if constexpr (cplx) launch_phase_project(ndir, P->d_dchi.p, P->d_msg_off.p, msgs, as<zdouble>(x), s);
+  };
+  // the cotangent handed to the VJP of the update: R lam (complex), lam (real)
+  auto rotated = [&](const double* x) -> const double* {
+    if constexpr (cplx) {
+      launch_edge_rotate(ndir, P->d_dchi.p, P->d_msg_off.p, as<zdouble>(rho.p), as<zdouble>(x), as<zdouble>(lrot.p),
+                         s);
+      return lrot.p;
+    }
+    return x;
+  };
+  if constexpr (cplx) {
+    gp.alloc(nm);
+    lrot.alloc(nm);
+    rho.alloc(2 * (size_t)std::max(ndir, 1));
+    launch_edge_phase(ndir, P->d_dchi.p, P->d_msg_off.p, msgs, as<zdouble>(fraw.p), as<zdouble>(rho.p), s);
+    GBTN_CUDA(cudaMemcpyAsync(gp.p, g_d, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
+    project(gp.p);
+    g0 = gp.p;
+  }
+  GBTN_CUDA(cudaMemcpyAsync(lam.p, g0, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
   int it = 0;
   double rel = 0.0;
   for (it = 1; it <= maxiter; ++it) {
-    launch_norm_vjp(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, fraw.p, lam.p, fbar.p, s);
+    launch_norm_vjp<T>(ndir, P->d_dchi.p, P->d_msg_off.p, as<T>(fraw.p), as<T>(rotated(lam.p)), as<T>(fbar.p), s);
     GBTN_CUDA(cudaMemsetAsync(mbar.p, 0, sizeof(double) * nm, s));
-    launch_vertex_vjp(allv, P->nv, P->d_vd.p, P->d_fac.p, P->d_fac.p, msgs, fbar.p, P->d_msg_off.p, nullptr, mbar.p,
-                      nullptr, P->ncap, s);
-    launch_axpy_resid(nm, g, mbar.p, lam.p, lam2.p, acc.p, s);
+    launch_vertex_vjp<T>(allv, P->nv, P->d_vd.p, as<T>(P->d_fac.p), as<T>(P->d_fac.p), msgs, as<T>(fbar.p),
+                         P->d_msg_off.p, nullptr, as<T>(mbar.p), nullptr, P->ncap, s);
+    project(mbar.p);
+    launch_axpy_resid(nm, g0, mbar.p, lam.p, lam2.p, acc.p, s);
     double h[2];
     GBTN_CUDA(cudaMemcpyAsync(h, acc.p, sizeof(h), cudaMemcpyDeviceToHost, s));
     GBTN_CUDA(cudaStreamSynchronize(s));
@@ -2562,11 +2607,19 @@ void implicit_adjoint(gbtn_plan* P, const int* allv, const double* msgs, const d
     if (rel <= tol) break;
   }
   if (it > maxiter) it = maxiter;
-  launch_norm_vjp(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, fraw.p, lam.p, fbar.p, s);
-  launch_vertex_vjp(allv, P->nv, P->d_vd.p, P->d_fac.p, P->d_fac.p, msgs, fbar.p, P->d_msg_off.p, nullptr, nullptr,
-                    grad, P->ncap, s);
+  launch_norm_vjp<T>(ndir, P->d_dchi.p, P->d_msg_off.p, as<T>(fraw.p), as<T>(rotated(lam.p)), as<T>(fbar.p), s);
+  launch_vertex_vjp<T>(allv, P->nv, P->d_vd.p, as<T>(P->d_fac.p), as<T>(P->d_fac.p), msgs, as<T>(fbar.p),
+                       P->d_msg_off.p, nullptr, nullptr, grad, P->ncap, s);
   if (iters) *iters = it;
   if (resid) *resid = rel;
+}
+
+void implicit_adjoint(gbtn_plan* P, const int* allv, const double* msgs, const double* g, double* grad, int maxiter,
+                      double tol, int32_t* iters, double* resid) {
+  if (P->cplx)
+    implicit_adjoint_t<zdouble>(P, allv, msgs, g, grad, maxiter, tol, iters, resid);
+  else
+    implicit_adjoint_t<double>(P, allv, msgs, g, grad, maxiter, tol, iters, resid);
 }
 
 }  // namespace
@@ -2658,10 +2711,10 @@ int gbtn_energy2_grad(gbtn_plan* P, int32_t nterms, const double* coef, const do
       for (int t = t1; t > t0; --t) {
         const double* mprev = seg[t - 1 - t0]->p;
         raw_forward(P, P->d_fac.p, nullptr, mprev, fraw.p, 0);
-        launch_norm_vjp(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, fraw.p, lam.p, fbar.p, s);
+        launch_norm_vjp<double>(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, fraw.p, lam.p, fbar.p, s);
         GBTN_CUDA(cudaMemsetAsync(mbar.p, 0, sizeof(double) * nm, s));
-        launch_vertex_vjp(E.allv.p, P->nv, P->d_vd.p, P->d_fac.p, P->d_fac.p, mprev, fbar.p, P->d_msg_off.p, nullptr,
-                          mbar.p, dgrad.p, P->ncap, s);
+        launch_vertex_vjp<double>(E.allv.p, P->nv, P->d_vd.p, P->d_fac.p, P->d_fac.p, mprev, fbar.p, P->d_msg_off.p,
+                                  nullptr, mbar.p, dgrad.p, P->ncap, s);
         std::swap(lam.p, mbar.p);
       }
     }
@@ -2677,17 +2730,17 @@ int gbtn_energy2_grad(gbtn_plan* P, int32_t nterms, const double* coef, const do
 
 namespace {
 
-// Checks shared by the scalar gradients (real FP64 quadratic form, every
+// Checks shared by the scalar gradients (quadratic-form network, every
 // vertex with a link, shared-memory vertices).
 void scalar_grad_checks(gbtn_plan* P) {
   if (P->has_large)
     throw Unsupported("energies and gradients take vertices of the shared-memory kernels only (bond and site "
                       "dimensions <= 8)");
-  if (P->cplx) throw Unsupported("gradients of complex networks are not implemented");
   require(!P->sep_bra, "gradients need bra = conj(ket) (a quadratic-form network)");
   for (int v = 0; v < P->nv; ++v)
     if (P->vd[v].k < 1) throw Unsupported("gradients take vertices with at least one link");
-  if (vertex_vjp_smem(P->ncap) > 227 * 1024) throw Unsupported("vertex tensor too large for the adjoint kernels");
+  if (vertex_vjp_smem(P->ncap, P->cplx ? sizeof(zdouble) : sizeof(double)) > 227 * 1024)
+    throw Unsupported("vertex tensor too large for the adjoint kernels");
 }
 
 // Per-network sums of per-vertex (and, when ev is given, minus per-edge) values.
@@ -2702,6 +2755,58 @@ void net_sums(gbtn_plan* P, const DevBuf<double>& vv, const DevBuf<double>* ev, 
   std::copy(acc.begin(), acc.end(), out);
 }
 
+// The log-norm (mode 0) or one-site expectation (mode 1, operator `op`, d x d
+// elements of T) and its gradient: direct cotangents of the vertex and edge
+// terms, vertex VJPs, then the implicit adjoint through the fixed point.
+template <typename T>
+void scalar_grad_t(gbtn_plan* P, int mode, const double* op, const gbtn_grad_opts* o, double* value, double* grad,
+                   int32_t* iters, double* resid) {
+  cudaStream_t s = P->ctx->stream;
+  const long long es = sizeof(T) / sizeof(double);
+  const long long nm = std::max<long long>(P->n_msg, 1) * es, nf = std::max<long long>(P->n_fac, 1) * es;
+  DevBuf<double> dop, ketO, F, FO, ci, co, g, dgrad, vval, eval;
+  DevBuf<int> allv;
+  std::vector<int> all(P->nv);
+  std::iota(all.begin(), all.end(), 0);
+  allv.upload(all, s);
+  F.alloc(nm);
+  ci.alloc(nm);
+  g.alloc(nm);
+  dgrad.alloc(nf);
+  vval.alloc(P->nv);
+  for (DevBuf<double>* b : {&ci, &g}) GBTN_CUDA(cudaMemsetAsync(b->p, 0, sizeof(double) * nm, s));
+  GBTN_CUDA(cudaMemsetAsync(dgrad.p, 0, sizeof(double) * nf, s));
+  const double* m = P->d_msg[P->cur].p;
+  raw_forward(P, P->d_fac.p, nullptr, m, F.p, 0);
+  if (mode == 0) {
+    eval.alloc(std::max(P->ne, 1));
+    launch_vertex_term_cot<T>(P->nv, P->d_vd.p, P->d_msg_off.p, as<T>(m), as<T>(F.p), nullptr, 0, as<T>(ci.p),
+                              nullptr, as<T>(g.p), vval.p, s);
+    launch_edge_term_cot<T>(P->ne, P->d_dchi.p, P->d_msg_off.p, as<T>(m), as<T>(g.p), eval.p, s);
+    launch_vertex_vjp<T>(allv.p, P->nv, P->d_vd.p, as<T>(P->d_fac.p), as<T>(P->d_fac.p), as<T>(m), as<T>(ci.p),
+                         P->d_msg_off.p, nullptr, as<T>(g.p), as<T>(dgrad.p), P->ncap, s);
+  } else {
+    const int d = P->dsite[0];
+    dop.upload(std::vector<double>(op, op + (size_t)d * d * es), s);
+    ketO.alloc(nf);
+    FO.alloc(nm);
+    co.alloc(nm);
+    GBTN_CUDA(cudaMemsetAsync(co.p, 0, sizeof(double) * nm, s));
+    launch_site_op<T>(P->nv, P->d_vd.p, as<T>(P->d_fac.p), as<T>(dop.p), as<T>(ketO.p), s);
+    raw_forward(P, ketO.p, P->d_fac.p, m, FO.p, 0);
+    launch_vertex_term_cot<T>(P->nv, P->d_vd.p, P->d_msg_off.p, as<T>(m), as<T>(F.p), as<T>(FO.p), 1, as<T>(ci.p),
+                              as<T>(co.p), as<T>(g.p), vval.p, s);
+    launch_vertex_vjp<T>(allv.p, P->nv, P->d_vd.p, as<T>(P->d_fac.p), as<T>(P->d_fac.p), as<T>(m), as<T>(ci.p),
+                         P->d_msg_off.p, nullptr, as<T>(g.p), as<T>(dgrad.p), P->ncap, s);
+    launch_vertex_vjp<T>(allv.p, P->nv, P->d_vd.p, as<T>(ketO.p), as<T>(P->d_fac.p), as<T>(m), as<T>(co.p),
+                         P->d_msg_off.p, as<T>(dop.p), as<T>(g.p), as<T>(dgrad.p), P->ncap, s);
+  }
+  implicit_adjoint(P, allv.p, m, g.p, dgrad.p, o && o->maxiter > 0 ? o->maxiter : 500,
+                   o && o->tol > 0 ? o->tol : 1e-12, iters, resid);
+  copy_out(P, grad, dgrad.p, sizeof(double) * P->n_fac * es, GBTN_HOST);
+  if (value) net_sums(P, vval, mode == 0 ? &eval : nullptr, value);
+}
+
 }  // namespace
 
 extern "C" {
@@ -2713,32 +2818,10 @@ int gbtn_logscalar_grad(gbtn_plan* P, const gbtn_grad_opts* o, double* value, do
   API_TRY
   require(P && grad, "NULL argument");
   scalar_grad_checks(P);
-  cudaStream_t s = P->ctx->stream;
-  const long long nm = std::max<long long>(P->n_msg, 1), nf = std::max<long long>(P->n_fac, 1);
-  DevBuf<double> F, ci, g, dgrad, vval, eval;
-  DevBuf<int> allv;
-  std::vector<int> all(P->nv);
-  std::iota(all.begin(), all.end(), 0);
-  allv.upload(all, s);
-  F.alloc(nm);
-  ci.alloc(nm);
-  g.alloc(nm);
-  dgrad.alloc(nf);
-  vval.alloc(P->nv);
-  eval.alloc(std::max(P->ne, 1));
-  GBTN_CUDA(cudaMemsetAsync(ci.p, 0, sizeof(double) * nm, s));
-  GBTN_CUDA(cudaMemsetAsync(g.p, 0, sizeof(double) * nm, s));
-  GBTN_CUDA(cudaMemsetAsync(dgrad.p, 0, sizeof(double) * nf, s));
-  const double* m = P->d_msg[P->cur].p;
-  raw_forward(P, P->d_fac.p, nullptr, m, F.p, 0);
-  launch_vertex_term_cot(P->nv, P->d_vd.p, P->d_msg_off.p, m, F.p, nullptr, 0, ci.p, nullptr, g.p, vval.p, s);
-  launch_edge_term_cot(P->ne, P->d_dchi.p, P->d_msg_off.p, m, g.p, eval.p, s);
-  launch_vertex_vjp(allv.p, P->nv, P->d_vd.p, P->d_fac.p, P->d_fac.p, m, ci.p, P->d_msg_off.p, nullptr, g.p,
-                    dgrad.p, P->ncap, s);
-  implicit_adjoint(P, allv.p, m, g.p, dgrad.p, o && o->maxiter > 0 ? o->maxiter : 500,
-                   o && o->tol > 0 ? o->tol : 1e-12, iters, resid);
-  copy_out(P, grad, dgrad.p, sizeof(double) * P->n_fac, GBTN_HOST);
-  if (value) net_sums(P, vval, &eval, value);
+  if (P->cplx)
+    scalar_grad_t<zdouble>(P, 0, nullptr, o, value, grad, iters, resid);
+  else
+    scalar_grad_t<double>(P, 0, nullptr, o, value, grad, iters, resid);
   API_CATCH(C)
 }
 
@@ -2751,37 +2834,10 @@ int gbtn_expect1_grad(gbtn_plan* P, const double* op, const gbtn_grad_opts* o, d
   scalar_grad_checks(P);
   const int d = P->dsite[0];
   for (int v = 0; v < P->nv; ++v) require(P->dsite[v] == d, "all vertices must share the site dimension of the operator");
-  cudaStream_t s = P->ctx->stream;
-  const long long nm = std::max<long long>(P->n_msg, 1), nf = std::max<long long>(P->n_fac, 1);
-  DevBuf<double> dop, ketO, F, FO, ci, co, g, dgrad, vval;
-  DevBuf<int> allv;
-  std::vector<int> all(P->nv);
-  std::iota(all.begin(), all.end(), 0);
-  allv.upload(all, s);
-  dop.upload(std::vector<double>(op, op + (size_t)d * d), s);
-  ketO.alloc(nf);
-  F.alloc(nm);
-  FO.alloc(nm);
-  ci.alloc(nm);
-  co.alloc(nm);
-  g.alloc(nm);
-  dgrad.alloc(nf);
-  vval.alloc(P->nv);
-  for (DevBuf<double>* b : {&ci, &co, &g}) GBTN_CUDA(cudaMemsetAsync(b->p, 0, sizeof(double) * nm, s));
-  GBTN_CUDA(cudaMemsetAsync(dgrad.p, 0, sizeof(double) * nf, s));
-  const double* m = P->d_msg[P->cur].p;
-  launch_site_op(P->nv, P->d_vd.p, P->d_fac.p, dop.p, ketO.p, s);
-  raw_forward(P, P->d_fac.p, nullptr, m, F.p, 0);
-  raw_forward(P, ketO.p, P->d_fac.p, m, FO.p, 0);
-  launch_vertex_term_cot(P->nv, P->d_vd.p, P->d_msg_off.p, m, F.p, FO.p, 1, ci.p, co.p, g.p, vval.p, s);
-  launch_vertex_vjp(allv.p, P->nv, P->d_vd.p, P->d_fac.p, P->d_fac.p, m, ci.p, P->d_msg_off.p, nullptr, g.p,
-                    dgrad.p, P->ncap, s);
-  launch_vertex_vjp(allv.p, P->nv, P->d_vd.p, ketO.p, P->d_fac.p, m, co.p, P->d_msg_off.p, dop.p, g.p, dgrad.p,
-                    P->ncap, s);
-  implicit_adjoint(P, allv.p, m, g.p, dgrad.p, o && o->maxiter > 0 ? o->maxiter : 500,
-                   o && o->tol > 0 ? o->tol : 1e-12, iters, resid);
-  copy_out(P, grad, dgrad.p, sizeof(double) * P->n_fac, GBTN_HOST);
-  if (value) net_sums(P, vval, nullptr, value);
+  if (P->cplx)
+    scalar_grad_t<zdouble>(P, 1, op, o, value, grad, iters, resid);
+  else
+    scalar_grad_t<double>(P, 1, op, o, value, grad, iters, resid);
   API_CATCH(C)
 }
 
@@ -2794,27 +2850,27 @@ int gbtn_bp_vjp(gbtn_plan* P, const double* msg_cot, const gbtn_grad_opts* o, do
   if (P->has_large)
     throw Unsupported("energies and gradients take vertices of the shared-memory kernels only (bond and site "
                       "dimensions <= 8)");
-  if (P && P->cplx) throw Unsupported("the BP vector-Jacobian product of complex networks is not implemented");
   require(P && msg_cot && o && grad, "NULL argument");
   require(o->mode == GBTN_GRAD_IMPLICIT, "gbtn_bp_vjp differentiates through the fixed point (IMPLICIT)");
   require(!P->sep_bra, "gradients need bra = conj(ket) (a quadratic-form network)");
-  if (vertex_vjp_smem(P->ncap) > 227 * 1024) throw Unsupported("vertex tensor too large for the adjoint kernels");
+  if (vertex_vjp_smem(P->ncap, P->cplx ? sizeof(zdouble) : sizeof(double)) > 227 * 1024)
+    throw Unsupported("vertex tensor too large for the adjoint kernels");
   cudaStream_t s = P->ctx->stream;
-  const long long nm = std::max<long long>(P->n_msg, 1);
+  const long long es = P->es();
+  const long long nm = std::max<long long>(P->n_msg, 1) * es, nf = std::max<long long>(P->n_fac, 1) * es;
   DevBuf<double> g, dgrad;
   DevBuf<int> allv;
-  std::vector<double> hg(msg_cot, msg_cot + P->n_msg);
-  if (hg.empty()) hg.push_back(0.0);
+  std::vector<double> hg(msg_cot, msg_cot + P->n_msg * es);
+  hg.resize(nm, 0.0);
   g.upload(hg, s);
-  dgrad.alloc(std::max<long long>(P->n_fac, 1));
-  GBTN_CUDA(cudaMemsetAsync(dgrad.p, 0, sizeof(double) * std::max<long long>(P->n_fac, 1), s));
+  dgrad.alloc(nf);
+  GBTN_CUDA(cudaMemsetAsync(dgrad.p, 0, sizeof(double) * nf, s));
   std::vector<int> all(P->nv);
   std::iota(all.begin(), all.end(), 0);
   allv.upload(all, s);
   implicit_adjoint(P, allv.p, P->d_msg[P->cur].p, g.p, dgrad.p, o->maxiter > 0 ? o->maxiter : 500,
                    o->tol > 0 ? o->tol : 1e-12, iters, resid);
-  copy_out(P, grad, dgrad.p, sizeof(double) * P->n_fac, GBTN_HOST);
-  (void)nm;
+  copy_out(P, grad, dgrad.p, sizeof(double) * P->n_fac * es, GBTN_HOST);
   API_CATCH(C)
 }
 

@@ -320,24 +320,36 @@ void launch_tc_vertices(const TcRec* recs, int nwork, const __nv_bfloat16* zimg,
                         int want_diff, int* err, cudaStream_t s);
 
 // Adjoint kernels (adjoint.cu), FP64.
-size_t vertex_vjp_smem(int ncap);
-void launch_site_op(int nv, const VDesc* vd, const double* fac, const double* op, double* out, cudaStream_t s);
-void launch_norm_vjp(int ndir, const int* dchi, const long long* msg_off, const double* f, const double* nbar,
-                     double* fbar, cudaStream_t s);
-void launch_vertex_vjp(const int* work, int nwork, const VDesc* vd, const double* ket, const double* bra,
-                       const double* msgs, const double* cot, const long long* msg_off, const double* op, double* mbar,
-                       double* abar, int ncap, cudaStream_t s);
+// Adjoint launchers: T = double or zdouble (complex cotangents are
+// dL/dRe + i dL/dIm of a real loss).
+size_t vertex_vjp_smem(int ncap, size_t elt = sizeof(double));
+template <typename T>
+void launch_site_op(int nv, const VDesc* vd, const T* fac, const T* op, T* out, cudaStream_t s);
+template <typename T>
+void launch_norm_vjp(int ndir, const int* dchi, const long long* msg_off, const T* f, const T* nbar, T* fbar,
+                     cudaStream_t s);
+template <typename T>
+void launch_vertex_vjp(const int* work, int nwork, const VDesc* vd, const T* ket, const T* bra, const T* msgs,
+                       const T* cot, const long long* msg_off, const T* op, T* mbar, T* abar, int ncap,
+                       cudaStream_t s);
 void launch_edge_dot(int ne, const int* dchi, const long long* msg_off, const double* F, double* out, cudaStream_t s);
 void launch_energy_cot(int ndir, const int* dchi, const long long* msg_off, const double* F, const double* scale,
                        double* C, cudaStream_t s);
 void launch_energy_terms(int ne, int nterms, const double* coef, const double* t, double* Ee, double* scale,
                          cudaStream_t s);
 void launch_net_sum(int nnet, const int* net_e_ptr, const int* net_e, const double* Ee, double* out, cudaStream_t s);
-void launch_vertex_term_cot(int nv, const VDesc* vd, const long long* msg_off, const double* msgs, const double* F,
-                            const double* FO, int mode, double* ci, double* co, double* g, double* val,
-                            cudaStream_t s);
-void launch_edge_term_cot(int ne, const int* dchi, const long long* msg_off, const double* msgs, double* g,
-                          double* val, cudaStream_t s);
+void launch_phase_project(int ndir, const int* dchi, const long long* msg_off, const zdouble* m, zdouble* lam,
+                          cudaStream_t s);
+void launch_edge_phase(int ndir, const int* dchi, const long long* msg_off, const zdouble* m, const zdouble* f,
+                       zdouble* rho, cudaStream_t s);
+void launch_edge_rotate(int ndir, const int* dchi, const long long* msg_off, const zdouble* rho, const zdouble* in,
+                        zdouble* out, cudaStream_t s);
+template <typename T>
+void launch_vertex_term_cot(int nv, const VDesc* vd, const long long* msg_off, const T* msgs, const T* F, const T* FO,
+                            int mode, T* ci, T* co, T* g, double* val, cudaStream_t s);
+template <typename T>
+void launch_edge_term_cot(int ne, const int* dchi, const long long* msg_off, const T* msgs, T* g, double* val,
+                          cudaStream_t s);
 void launch_axpy_resid(long long n, const double* a, const double* b, const double* old, double* y, double* acc,
                        cudaStream_t s);
 

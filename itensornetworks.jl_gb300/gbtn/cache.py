@@ -353,39 +353,44 @@ class BeliefPropagationCache:
         return (e[0] if self.tn.n_networks == 1 else e), self.tn.unflat(g)
 
     def vjp(self, msg_cot, maxiter=500, tol=1e-12):
-        """dL/dA from dL/dm at the fixed point (implicit differentiation)."""
-        mc = self.tn.flat_messages(msg_cot) if isinstance(msg_cot, (list, tuple)) else np.ascontiguousarray(msg_cot, float)
+        """dL/dA from dL/dm at the fixed point (implicit differentiation).
+        Complex networks: cotangents and gradients are dL/dRe + i dL/dIm of a
+        real loss L."""
+        mc = (self.tn.flat_messages(msg_cot, self.complex) if isinstance(msg_cot, (list, tuple))
+              else np.ascontiguousarray(msg_cot, self.dtype))
         o = _lib.GradOpts()
         o.mode, o.maxiter, o.tol = 0, int(maxiter), float(tol)
-        g = np.empty(self.n_factor)
+        g = np.empty(self.n_factor, dtype=self.dtype)
         it = np.zeros(1, dtype=np.int32)
         res = np.zeros(1)
-        self._c(self.lib.gbtn_bp_vjp(self.handle, dptr(mc), C.byref(o), dptr(g), iptr(it), dptr(res)))
+        self._c(self.lib.gbtn_bp_vjp(self.handle, dptr(mc.view(np.float64)), C.byref(o), dptr(g.view(np.float64)),
+                                     iptr(it), dptr(res)))
         return self.tn.unflat(g)
 
     def _scalar_grad(self, fn, extra, maxiter, tol):
         o = _lib.GradOpts()
         o.mode, o.maxiter, o.tol = 0, int(maxiter), float(tol)
         val = np.empty(self.tn.n_networks)
-        g = np.empty(self.n_factor)
+        g = np.empty(self.n_factor, dtype=self.dtype)
         it = np.zeros(1, dtype=np.int32)
         res = np.zeros(1)
-        self._c(fn(self.handle, *extra, C.byref(o), dptr(val), dptr(g), iptr(it), dptr(res)))
+        self._c(fn(self.handle, *extra, C.byref(o), dptr(val), dptr(g.view(np.float64)), iptr(it), dptr(res)))
         self.grad_iterations, self.grad_residual = int(it[0]), float(res[0])
         return (float(val[0]) if self.tn.n_networks == 1 else val), self.tn.unflat(g)
 
     def logscalar_grad(self, maxiter=500, tol=1e-12):
-        """(logscalar, d logscalar / dA) at the current (converged) messages:
+        """(Re logscalar, its gradient dA) at the current (converged) messages:
         the direct derivative plus the implicit part through the BP fixed point.
-        Real quadratic-form networks; summed over a batch's networks for the
-        gradient, per network for the value."""
+        Quadratic-form networks, real or complex (gradient dL/dRe + i dL/dIm);
+        summed over a batch's networks for the gradient, per network for the
+        value."""
         return self._scalar_grad(self.lib.gbtn_logscalar_grad, (), maxiter, tol)
 
     def expect_sum_grad(self, op, maxiter=500, tol=1e-12):
-        """(sum_v <O_v>, its gradient dA) at the current (converged) messages,
-        one d x d operator O[s', s] for every vertex."""
-        op = np.ascontiguousarray(np.asarray(op, dtype=np.float64).reshape(-1, order="F"))
-        return self._scalar_grad(self.lib.gbtn_expect1_grad, (dptr(op),), maxiter, tol)
+        """(Re sum_v <O_v>, its gradient dA) at the current (converged)
+        messages, one d x d operator O[s', s] for every vertex."""
+        op = np.ascontiguousarray(np.asarray(op, dtype=self.dtype).reshape(-1, order="F"))
+        return self._scalar_grad(self.lib.gbtn_expect1_grad, (dptr(op.view(np.float64)),), maxiter, tol)
 
     # -- rescaling -------------------------------------------------------------
     def rescale_messages(self):
