@@ -342,7 +342,10 @@ typedef struct gbtn_grad_opts {
 int gbtn_energy2(gbtn_plan* plan, int32_t n_terms, const double* coef, const double* ops, double* energy);
 /* Energy and its gradient with respect to every site tensor (n_factor values,
  * same layout as gbtn_set_factors).  iters / resid (may be NULL): adjoint
- * iterations and final relative residual (IMPLICIT), or sweeps (UNROLLED). */
+ * iterations and final relative residual (IMPLICIT), or sweeps (UNROLLED).
+ * Complex plans: ops are complex d x d matrices (interleaved), the energy is
+ * the real part of sum_e sum_t c_t <O_t (x) O_t>_e, and the gradient is
+ * dE/dRe + i dE/dIm (interleaved). */
 int gbtn_energy2_grad(gbtn_plan* plan, int32_t n_terms, const double* coef, const double* ops,
                       const gbtn_grad_opts* opts, double* energy, double* grad, int32_t* iters, double* resid);
 /* Vector-Jacobian product through the BP fixed point: given dL/dm for the

@@ -54,6 +54,13 @@ __device__ __forceinline__ zdouble operator*(double a, zdouble b) { return zdoub
 __device__ __forceinline__ zdouble operator-(zdouble a, zdouble b) { return zdouble(a.re - b.re, a.im - b.im); }
 __device__ __forceinline__ zdouble zwarp_sum(zdouble x) { return zdouble(warp_sum(x.re), warp_sum(x.im)); }
 __device__ __forceinline__ double zwarp_sum(double x) { return warp_sum(x); }
+__device__ __forceinline__ double inv_of(double x) { return 1.0 / x; }
+__device__ __forceinline__ zdouble inv_of(zdouble x) {
+  const double r = 1.0 / (x.re * x.re + x.im * x.im);
+  return zdouble(x.re * r, -x.im * r);
+}
+__device__ __forceinline__ double log_abs(double x) { return log(fabs(x)); }
+__device__ __forceinline__ double log_abs(zdouble x) { return 0.5 * log(x.re * x.re + x.im * x.im); }
 
 // Normalisation VJP per directed edge (one warp each).  Complex entries (the
 // cotangent of a real loss being dL/dRe + i dL/dIm): with n = f / |f|,
@@ -284,30 +291,31 @@ __global__ void edge_rotate_kernel(int ndir, const int* __restrict__ dchi, const
   for (int i = lane; i < c2; i += 32) out[off + i] = r * in[off + i];
 }
 
-// Per edge: t[e] = <F[2e], F[2e+1]> (one warp per edge).
+// Per edge: t[e] = sum F[2e] F[2e+1] (bilinear; one warp per edge).
+template <typename T>
 __global__ void edge_dot_kernel(int ne, const int* __restrict__ dchi, const long long* __restrict__ msg_off,
-                                const double* __restrict__ F, double* __restrict__ out) {
+                                const T* __restrict__ F, T* __restrict__ out) {
   const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (e >= ne) return;
   const int c2 = dchi[2 * e] * dchi[2 * e];
-  double s = 0.0;
-  for (int i = lane; i < c2; i += 32) s += F[msg_off[2 * e] + i] * F[msg_off[2 * e + 1] + i];
-  s = warp_sum(s);
+  T s = T(0);
+  for (int i = lane; i < c2; i += 32) s = mac(F[msg_off[2 * e] + i], F[msg_off[2 * e + 1] + i], s);
+  s = zwarp_sum(s);
   if (lane == 0) out[e] = s;
 }
 
 // Cotangents of the energy on the term messages: for directed edge de of edge e,
-// C[de] = scale[e] * F[de ^ 1] (scale = c_t / t_I for an operator term,
-// -E_e / t_I for the identity term).
+// C[de] = conj(scale[e] * F[de ^ 1]) (scale = c_t / t_I for an operator term,
+// -E_e / t_I for the identity term; the conjugate is the identity for real tensors).
+template <typename T>
 __global__ void energy_cot_kernel(int ndir, const int* __restrict__ dchi, const long long* __restrict__ msg_off,
-                                  const double* __restrict__ F, const double* __restrict__ scale,
-                                  double* __restrict__ C) {
+                                  const T* __restrict__ F, const T* __restrict__ scale, T* __restrict__ C) {
   const int de = blockIdx.x;
   if (de >= ndir) return;
   const int c2 = dchi[de] * dchi[de];
-  const double sc = scale[de >> 1];
-  for (int i = threadIdx.x; i < c2; i += blockDim.x) C[msg_off[de] + i] = sc * F[msg_off[de ^ 1] + i];
+  const T sc = scale[de >> 1];
+  for (int i = threadIdx.x; i < c2; i += blockDim.x) C[msg_off[de] + i] = conj_of(sc * F[msg_off[de ^ 1] + i]);
 }
 
 }  // namespace
@@ -315,19 +323,21 @@ __global__ void energy_cot_kernel(int ndir, const int* __restrict__ dchi, const 
 namespace {
 
 // Per edge: E_e = sum_t c_t t[t][e] / t[I][e] and the cotangent scales
-// scale[t][e] = c_t / t[I][e], scale[I][e] = -E_e / t[I][e] (term 0 = identity).
-__global__ void energy_terms_kernel(int ne, int nterms, const double* __restrict__ coef, const double* __restrict__ t,
-                                    double* __restrict__ Ee, double* __restrict__ scale) {
+// scale[t][e] = c_t / t[I][e], scale[I][e] = -E_e / t[I][e] (term 0 = identity);
+// Ee receives Re E_e (the energy of a complex network is its real part).
+template <typename T>
+__global__ void energy_terms_kernel(int ne, int nterms, const double* __restrict__ coef, const T* __restrict__ t,
+                                    double* __restrict__ Ee, T* __restrict__ scale) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
-  const double tI = t[e];
-  double E = 0.0;
+  const T itI = inv_of(t[e]);
+  T E = T(0);
   for (int k = 1; k <= nterms; ++k) {
-    E += coef[k - 1] * t[(size_t)k * ne + e] / tI;
-    scale[(size_t)k * ne + e] = coef[k - 1] / tI;
+    E = mac(T(coef[k - 1]) * itI, t[(size_t)k * ne + e], E);
+    scale[(size_t)k * ne + e] = T(coef[k - 1]) * itI;
   }
-  Ee[e] = E;
-  scale[e] = -E / tI;
+  Ee[e] = re_of(E);
+  scale[e] = T(0) - E * itI;
 }
 
 // Per network: sum of its edges' energies.
@@ -394,13 +404,6 @@ void launch_site_op(int nv, const VDesc* vd, const T* fac, const T* op, T* out, 
 //   mode 1 (expect, expect.jl:5-19): val[v] = Re(N_v / D_v); cotangents
 //     co (of F^O_{v->w}) = conj(m / D_v) and ci (of F_{v->w}) = conj(-N_v / D_v^2 m);
 //     g[w->v] += conj(F^O / D_v - N_v / D_v^2 F).
-__device__ __forceinline__ double inv_of(double x) { return 1.0 / x; }
-__device__ __forceinline__ zdouble inv_of(zdouble x) {
-  const double r = 1.0 / (x.re * x.re + x.im * x.im);
-  return zdouble(x.re * r, -x.im * r);
-}
-__device__ __forceinline__ double log_abs(double x) { return log(fabs(x)); }
-__device__ __forceinline__ double log_abs(zdouble x) { return 0.5 * log(x.re * x.re + x.im * x.im); }
 
 template <typename T>
 __global__ void vertex_term_cot_kernel(int nv, const VDesc* __restrict__ vd, const long long* __restrict__ msg_off,
@@ -528,25 +531,36 @@ GBTN_ADJOINT_INSTANTIATE(double)
 GBTN_ADJOINT_INSTANTIATE(zdouble)
 #undef GBTN_ADJOINT_INSTANTIATE
 
-void launch_edge_dot(int ne, const int* dchi, const long long* msg_off, const double* F, double* out, cudaStream_t s) {
+template <typename T>
+void launch_edge_dot(int ne, const int* dchi, const long long* msg_off, const T* F, T* out, cudaStream_t s) {
   if (ne == 0) return;
-  edge_dot_kernel<<<(ne + 7) / 8, 256, 0, s>>>(ne, dchi, msg_off, F, out);
+  edge_dot_kernel<T><<<(ne + 7) / 8, 256, 0, s>>>(ne, dchi, msg_off, F, out);
   GBTN_CUDA(cudaGetLastError());
 }
 
-void launch_energy_cot(int ndir, const int* dchi, const long long* msg_off, const double* F, const double* scale,
-                       double* C, cudaStream_t s) {
+template <typename T>
+void launch_energy_cot(int ndir, const int* dchi, const long long* msg_off, const T* F, const T* scale, T* C,
+                       cudaStream_t s) {
   if (ndir == 0) return;
-  energy_cot_kernel<<<ndir, 64, 0, s>>>(ndir, dchi, msg_off, F, scale, C);
+  energy_cot_kernel<T><<<ndir, 64, 0, s>>>(ndir, dchi, msg_off, F, scale, C);
   GBTN_CUDA(cudaGetLastError());
 }
 
-void launch_energy_terms(int ne, int nterms, const double* coef, const double* t, double* Ee, double* scale,
-                         cudaStream_t s) {
+template <typename T>
+void launch_energy_terms(int ne, int nterms, const double* coef, const T* t, double* Ee, T* scale, cudaStream_t s) {
   if (ne == 0) return;
-  energy_terms_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, nterms, coef, t, Ee, scale);
+  energy_terms_kernel<T><<<(ne + 127) / 128, 128, 0, s>>>(ne, nterms, coef, t, Ee, scale);
   GBTN_CUDA(cudaGetLastError());
 }
+
+template void launch_edge_dot<double>(int, const int*, const long long*, const double*, double*, cudaStream_t);
+template void launch_edge_dot<zdouble>(int, const int*, const long long*, const zdouble*, zdouble*, cudaStream_t);
+template void launch_energy_cot<double>(int, const int*, const long long*, const double*, const double*, double*,
+                                        cudaStream_t);
+template void launch_energy_cot<zdouble>(int, const int*, const long long*, const zdouble*, const zdouble*,
+                                         zdouble*, cudaStream_t);
+template void launch_energy_terms<double>(int, int, const double*, const double*, double*, double*, cudaStream_t);
+template void launch_energy_terms<zdouble>(int, int, const double*, const zdouble*, double*, zdouble*, cudaStream_t);
 
 void launch_net_sum(int nnet, const int* net_e_ptr, const int* net_e, const double* Ee, double* out, cudaStream_t s) {
   net_sum_kernel<<<nnet, 256, 0, s>>>(net_e_ptr, net_e, Ee, out);

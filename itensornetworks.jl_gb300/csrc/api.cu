@@ -2484,35 +2484,39 @@ void raw_forward(gbtn_plan* P, const double* ket, const double* bra, const doubl
     raw_forward_t<double>(P, ket, bra, msgs, out, normalize);
 }
 
+// (Complex plans: every buffer holds interleaved (re, im) doubles; the
+// energy is the real part, its cotangents conj of the holomorphic derivatives.)
+template <typename T>
 const double* term_ket(Energy2& E, int k) {
   if (k == 0) return E.P->d_fac.p;
-  launch_site_op<double>(E.P->nv, E.P->d_vd.p, E.P->d_fac.p, E.ops.p + (size_t)(k - 1) * E.d * E.d, E.ket.p,
-                 E.P->ctx->stream);
+  const size_t es = sizeof(T) / sizeof(double);
+  launch_site_op<T>(E.P->nv, E.P->d_vd.p, as<T>(E.P->d_fac.p), as<T>(E.ops.p + (size_t)(k - 1) * E.d * E.d * es),
+                    as<T>(E.ket.p), E.P->ctx->stream);
   return E.ket.p;
 }
 
 void energy_setup(Energy2& E, gbtn_plan* P, int nterms, const double* coef, const double* ops) {
-  if (P->cplx) throw Unsupported("energies and gradients of complex networks are not implemented");
   require(!P->sep_bra, "energies and gradients need bra = conj(ket) (a quadratic-form network)");
   require(nterms >= 1 && coef && ops, "need at least one operator term");
   cudaStream_t s = P->ctx->stream;
+  const size_t es = P->es();
   E.P = P;
   E.nterms = nterms;
   E.d = P->dsite[0];
   for (int v = 0; v < P->nv; ++v) require(P->dsite[v] == E.d, "all vertices must share the site dimension of the operators");
-  const size_t need = vertex_vjp_smem(P->ncap);
+  const size_t need = vertex_vjp_smem(P->ncap, P->cplx ? sizeof(zdouble) : sizeof(double));
   if (need > 227 * 1024) throw Unsupported("vertex tensor too large for the adjoint kernels");
-  std::vector<double> h(ops, ops + (size_t)nterms * E.d * E.d), c(coef, coef + nterms);
+  std::vector<double> h(ops, ops + (size_t)nterms * E.d * E.d * es), c(coef, coef + nterms);
   E.ops.upload(h, s);
   E.coef.upload(c, s);
-  E.ket.alloc(P->n_fac);
-  E.t.alloc((size_t)(nterms + 1) * std::max(P->ne, 1));
-  E.scale.alloc((size_t)(nterms + 1) * std::max(P->ne, 1));
+  E.ket.alloc(std::max<long long>(P->n_fac, 1) * es);
+  E.t.alloc((size_t)(nterms + 1) * std::max(P->ne, 1) * es);
+  E.scale.alloc((size_t)(nterms + 1) * std::max(P->ne, 1) * es);
   E.Ee.alloc(std::max(P->ne, 1));
   E.netE.alloc(P->nnet);
   for (int k = 0; k <= nterms; ++k) {
     E.F.push_back(std::make_unique<DevBuf<double>>());
-    E.F.back()->alloc(std::max<long long>(P->n_msg, 1));
+    E.F.back()->alloc(std::max<long long>(P->n_msg, 1) * es);
   }
   std::vector<int> all(P->nv);
   std::iota(all.begin(), all.end(), 0);
@@ -2521,27 +2525,80 @@ void energy_setup(Energy2& E, gbtn_plan* P, int nterms, const double* coef, cons
 
 // Forward energy at messages `msgs`: term messages, edge dots, per-edge energies
 // and cotangent scales, per-network sums.
-void energy_forward(Energy2& E, const double* msgs) {
+template <typename T>
+void energy_forward_t(Energy2& E, const double* msgs) {
   gbtn_plan* P = E.P;
   cudaStream_t s = P->ctx->stream;
+  const size_t es = sizeof(T) / sizeof(double);
   for (int k = 0; k <= E.nterms; ++k) {
-    const double* ket = term_ket(E, k);
+    const double* ket = term_ket<T>(E, k);
     raw_forward(P, ket, k == 0 ? nullptr : P->d_fac.p, msgs, E.F[k]->p, 0);
-    launch_edge_dot(P->ne, P->d_dchi.p, P->d_msg_off.p, E.F[k]->p, E.t.p + (size_t)k * P->ne, s);
+    launch_edge_dot<T>(P->ne, P->d_dchi.p, P->d_msg_off.p, as<T>(E.F[k]->p),
+                       as<T>(E.t.p + (size_t)k * P->ne * es), s);
   }
-  launch_energy_terms(P->ne, E.nterms, E.coef.p, E.t.p, E.Ee.p, E.scale.p, s);
+  launch_energy_terms<T>(P->ne, E.nterms, E.coef.p, as<T>(E.t.p), E.Ee.p, as<T>(E.scale.p), s);
   launch_net_sum(P->nnet, P->d_net_e_ptr.p, P->d_net_e.p, E.Ee.p, E.netE.p, s);
 }
 
 // Direct part of the energy gradient at messages `msgs`: g += dE/dm, grad += dE/dA.
-void energy_direct_vjp(Energy2& E, const double* msgs, double* cot, double* g, double* grad) {
+template <typename T>
+void energy_direct_vjp_t(Energy2& E, const double* msgs, double* cot, double* g, double* grad) {
   gbtn_plan* P = E.P;
   cudaStream_t s = P->ctx->stream;
+  const size_t es = sizeof(T) / sizeof(double);
   for (int k = 0; k <= E.nterms; ++k) {
-    launch_energy_cot(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, E.F[k]->p, E.scale.p + (size_t)k * P->ne, cot, s);
-    const double* ket = term_ket(E, k);
-    launch_vertex_vjp<double>(E.allv.p, P->nv, P->d_vd.p, ket, P->d_fac.p, msgs, cot, P->d_msg_off.p,
-                              k == 0 ? nullptr : E.ops.p + (size_t)(k - 1) * E.d * E.d, g, grad, P->ncap, s);
+    launch_energy_cot<T>(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, as<T>(E.F[k]->p),
+                         as<T>(E.scale.p + (size_t)k * P->ne * es), as<T>(cot), s);
+    const double* ket = term_ket<T>(E, k);
+    launch_vertex_vjp<T>(E.allv.p, P->nv, P->d_vd.p, as<T>(ket), as<T>(P->d_fac.p), as<T>(msgs), as<T>(cot),
+                         P->d_msg_off.p, k == 0 ? nullptr : as<T>(E.ops.p + (size_t)(k - 1) * E.d * E.d * es),
+                         as<T>(g), as<T>(grad), P->ncap, s);
+  }
+}
+
+void energy_forward(Energy2& E, const double* msgs) {
+  if (E.P->cplx)
+    energy_forward_t<zdouble>(E, msgs);
+  else
+    energy_forward_t<double>(E, msgs);
+}
+
+void energy_direct_vjp(Energy2& E, const double* msgs, double* cot, double* g, double* grad) {
+  if (E.P->cplx)
+    energy_direct_vjp_t<zdouble>(E, msgs, cot, g, grad);
+  else
+    energy_direct_vjp_t<double>(E, msgs, cot, g, grad);
+}
+
+// Backpropagation through T normalised Jacobi sweeps from identity messages,
+// checkpointed every c sweeps; complex cotangents lose their message-phase
+// components at every step (the energy is invariant under them).
+template <typename T>
+void unrolled_backward_t(gbtn_plan* P, Energy2& E, int Tn, int c, std::vector<std::unique_ptr<DevBuf<double>>>& ck,
+                         std::vector<std::unique_ptr<DevBuf<double>>>& seg, double* lam_p, double* dgrad, long long nm) {
+  cudaStream_t s = P->ctx->stream;
+  const int ndir = 2 * P->ne;
+  DevBuf<double> fraw, fbar, mbar;
+  fraw.alloc(nm);
+  fbar.alloc(nm);
+  mbar.alloc(nm);
+  double* lam = lam_p;
+  double* mb = mbar.p;
+  for (int j = (Tn - 1) / c; j >= 0; --j) {
+    const int t0 = j * c, t1 = std::min(Tn, (j + 1) * c);
+    GBTN_CUDA(cudaMemcpyAsync(seg[0]->p, ck[j]->p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
+    for (int i = 1; i < t1 - t0; ++i) raw_forward(P, P->d_fac.p, nullptr, seg[i - 1]->p, seg[i]->p, 1);
+    for (int t = t1; t > t0; --t) {
+      const double* mprev = seg[t - 1 - t0]->p;
+      raw_forward(P, P->d_fac.p, nullptr, mprev, fraw.p, 0);
+      launch_norm_vjp<T>(ndir, P->d_dchi.p, P->d_msg_off.p, as<T>(fraw.p), as<T>(lam), as<T>(fbar.p), s);
+      GBTN_CUDA(cudaMemsetAsync(mb, 0, sizeof(double) * nm, s));
+      launch_vertex_vjp<T>(E.allv.p, P->nv, P->d_vd.p, as<T>(P->d_fac.p), as<T>(P->d_fac.p), as<T>(mprev),
+                           as<T>(fbar.p), P->d_msg_off.p, nullptr, as<T>(mb), as<T>(dgrad), P->ncap, s);
+      if constexpr (std::is_same<T, zdouble>::value)
+        launch_phase_project(ndir, P->d_dchi.p, P->d_msg_off.p, as<zdouble>(mprev), as<zdouble>(mb), s);
+      std::swap(lam, mb);
+    }
   }
 }
 
@@ -2655,13 +2712,14 @@ int gbtn_energy2_grad(gbtn_plan* P, int32_t nterms, const double* coef, const do
   cudaStream_t s = P->ctx->stream;
   Energy2 E;
   energy_setup(E, P, nterms, coef, ops);
-  const long long nm = std::max<long long>(P->n_msg, 1);
+  const long long es = P->es();
+  const long long nm = std::max<long long>(P->n_msg, 1) * es, nf = std::max<long long>(P->n_fac, 1) * es;
   DevBuf<double> g, cot, dgrad;
   g.alloc(nm);
   cot.alloc(nm);
-  dgrad.alloc(std::max<long long>(P->n_fac, 1));
+  dgrad.alloc(nf);
   GBTN_CUDA(cudaMemsetAsync(g.p, 0, sizeof(double) * nm, s));
-  GBTN_CUDA(cudaMemsetAsync(dgrad.p, 0, sizeof(double) * std::max<long long>(P->n_fac, 1), s));
+  GBTN_CUDA(cudaMemsetAsync(dgrad.p, 0, sizeof(double) * nf, s));
   if (o->mode == GBTN_GRAD_IMPLICIT) {
     const double* m = P->d_msg[P->cur].p;
     energy_forward(E, m);
@@ -2682,15 +2740,12 @@ int gbtn_energy2_grad(gbtn_plan* P, int32_t nterms, const double* coef, const do
       seg.push_back(std::make_unique<DevBuf<double>>());
       seg.back()->alloc(nm);
     }
-    DevBuf<double> cur, nxt, fraw, fbar, lam, mbar;
+    DevBuf<double> cur, nxt, lam;
     cur.alloc(nm);
     nxt.alloc(nm);
-    fraw.alloc(nm);
-    fbar.alloc(nm);
     lam.alloc(nm);
-    mbar.alloc(nm);
     // forward: identity messages, T normalised Jacobi sweeps, every c-th kept
-    launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, cur.p, GBTN_INIT_IDENTITY, s);
+    launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, cur.p, GBTN_INIT_IDENTITY, s, P->cplx);
     GBTN_CUDA(cudaMemcpyAsync(ck[0]->p, cur.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
     for (int t = 1; t <= T; ++t) {
       raw_forward(P, P->d_fac.p, nullptr, cur.p, nxt.p, 1);
@@ -2704,25 +2759,17 @@ int gbtn_energy2_grad(gbtn_plan* P, int32_t nterms, const double* coef, const do
     energy_direct_vjp(E, cur.p, cot.p, g.p, dgrad.p);
     GBTN_CUDA(cudaMemcpyAsync(lam.p, g.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
     // backward, one checkpoint segment at a time
-    for (int j = (T - 1) / c; j >= 0; --j) {
-      const int t0 = j * c, t1 = std::min(T, (j + 1) * c);
-      GBTN_CUDA(cudaMemcpyAsync(seg[0]->p, ck[j]->p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
-      for (int i = 1; i < t1 - t0; ++i) raw_forward(P, P->d_fac.p, nullptr, seg[i - 1]->p, seg[i]->p, 1);
-      for (int t = t1; t > t0; --t) {
-        const double* mprev = seg[t - 1 - t0]->p;
-        raw_forward(P, P->d_fac.p, nullptr, mprev, fraw.p, 0);
-        launch_norm_vjp<double>(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, fraw.p, lam.p, fbar.p, s);
-        GBTN_CUDA(cudaMemsetAsync(mbar.p, 0, sizeof(double) * nm, s));
-        launch_vertex_vjp<double>(E.allv.p, P->nv, P->d_vd.p, P->d_fac.p, P->d_fac.p, mprev, fbar.p, P->d_msg_off.p,
-                                  nullptr, mbar.p, dgrad.p, P->ncap, s);
-        std::swap(lam.p, mbar.p);
-      }
+    if (P->cplx) {
+      launch_phase_project(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, as<zdouble>(cur.p), as<zdouble>(lam.p), s);
+      unrolled_backward_t<zdouble>(P, E, T, c, ck, seg, lam.p, dgrad.p, nm);
+    } else {
+      unrolled_backward_t<double>(P, E, T, c, ck, seg, lam.p, dgrad.p, nm);
     }
     if (iters) *iters = T;
     if (resid) *resid = 0.0;
   }
   if (energy) copy_out(P, energy, E.netE.p, sizeof(double) * P->nnet, GBTN_HOST);
-  copy_out(P, grad, dgrad.p, sizeof(double) * P->n_fac, GBTN_HOST);
+  copy_out(P, grad, dgrad.p, sizeof(double) * P->n_fac * es, GBTN_HOST);
   API_CATCH(C)
 }
 

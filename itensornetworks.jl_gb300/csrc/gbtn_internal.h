@@ -332,11 +332,13 @@ template <typename T>
 void launch_vertex_vjp(const int* work, int nwork, const VDesc* vd, const T* ket, const T* bra, const T* msgs,
                        const T* cot, const long long* msg_off, const T* op, T* mbar, T* abar, int ncap,
                        cudaStream_t s);
-void launch_edge_dot(int ne, const int* dchi, const long long* msg_off, const double* F, double* out, cudaStream_t s);
-void launch_energy_cot(int ndir, const int* dchi, const long long* msg_off, const double* F, const double* scale,
-                       double* C, cudaStream_t s);
-void launch_energy_terms(int ne, int nterms, const double* coef, const double* t, double* Ee, double* scale,
-                         cudaStream_t s);
+template <typename T>
+void launch_edge_dot(int ne, const int* dchi, const long long* msg_off, const T* F, T* out, cudaStream_t s);
+template <typename T>
+void launch_energy_cot(int ndir, const int* dchi, const long long* msg_off, const T* F, const T* scale, T* C,
+                       cudaStream_t s);
+template <typename T>
+void launch_energy_terms(int ne, int nterms, const double* coef, const T* t, double* Ee, T* scale, cudaStream_t s);
 void launch_net_sum(int nnet, const int* net_e_ptr, const int* net_e, const double* Ee, double* out, cudaStream_t s);
 void launch_phase_project(int ndir, const int* dchi, const long long* msg_off, const zdouble* m, zdouble* lam,
                           cudaStream_t s);

@@ -323,11 +323,11 @@ class BeliefPropagationCache:
         return out
 
     # -- energies and gradients -----------------------------------------------
-    @staticmethod
-    def _terms(terms):
+    def _terms(self, terms):
+        """(coefficients, operators in the plan's element type as doubles)."""
         coef = np.ascontiguousarray([float(c) for c, _ in terms])
-        ops = np.ascontiguousarray(np.concatenate([np.asarray(o, float).reshape(-1, order="F") for _, o in terms]))
-        return coef, ops
+        ops = np.ascontiguousarray(np.concatenate([np.asarray(o, self.dtype).reshape(-1, order="F") for _, o in terms]))
+        return coef, ops.view(np.float64)
 
     def energy2(self, terms):
         """sum_e sum_t c_t <O_t (x) O_t>_e over every edge (terms = [(c_t, O_t)])."""
@@ -338,17 +338,19 @@ class BeliefPropagationCache:
 
     def energy2_grad(self, terms, mode="implicit", maxiter=500, tol=1e-12, unroll=30, checkpoint=0):
         """(energy, [dE/dA_v]) through the converged messages ("implicit") or
-        through `unroll` Jacobi sweeps from identity messages ("unrolled")."""
+        through `unroll` Jacobi sweeps from identity messages ("unrolled").
+        Complex networks: the real part of the energy, and the gradient as
+        dE/dRe + i dE/dIm."""
         coef, ops = self._terms(terms)
         o = _lib.GradOpts()
         o.mode = 0 if mode == "implicit" else 1
         o.maxiter, o.tol, o.unroll, o.checkpoint = int(maxiter), float(tol), int(unroll), int(checkpoint)
         e = np.empty(self.tn.n_networks)
-        g = np.empty(self.n_factor)
+        g = np.empty(self.n_factor, dtype=self.dtype)
         it = np.zeros(1, dtype=np.int32)
         res = np.zeros(1)
         self._c(self.lib.gbtn_energy2_grad(self.handle, len(terms), dptr(coef), dptr(ops), C.byref(o), dptr(e),
-                                           dptr(g), iptr(it), dptr(res)))
+                                           dptr(g.view(np.float64)), iptr(it), dptr(res)))
         self.adjoint_iterations, self.adjoint_residual = int(it[0]), float(res[0])
         return (e[0] if self.tn.n_networks == 1 else e), self.tn.unflat(g)
 

@@ -129,14 +129,17 @@ def test_complex_mixed_reaches_the_fp64_fixed_point():
     np.testing.assert_allclose(mix.expect(O.SZ), sz_ref, rtol=0, atol=1e-6 * np.max(np.abs(sz_ref)))
 
 
-def test_complex_paths_outside_fp64_are_unsupported():
+def test_complex_bf16_is_unsupported_and_energies_are_real_parts():
     g = O.square_lattice(3, 3, chi=2)
     tn, A = cnet(g, 1)
     bpc = gbtn.BeliefPropagationCache(tn)
     with pytest.raises(gbtn.Unsupported):
         bpc.update(maxiter=2, schedule="parallel", precision="bf16")
-    with pytest.raises(gbtn.Unsupported):
-        bpc.energy2([(1.0, O.SZ)])
+    # the two-site energy of a complex network: the real part of the oracle's
+    bpc.init_messages("identity")
+    bpc.update(maxiter=30, schedule="parallel")
+    want = float(np.real(np.sum(O.expect2(g, A, bpc.messages(), np.kron(O.SZ, O.SZ)))))
+    assert bpc.energy2([(1.0, O.SZ)]) == pytest.approx(want, rel=1e-10, abs=1e-13)
 
 
 def test_complex_rescale_partitions_and_normalize_match_the_oracle():
