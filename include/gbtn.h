@@ -421,6 +421,14 @@ int gbtn_qn_get_messages(gbtn_qn_plan* plan, double* msgs, int mem);
 /* Replaces: update(bpc; maxiter, tol) with the parallel (Jacobi) schedule;
  * message_diff and its mean as the dense plan (abstractbeliefpropagationcache.jl:32-36, 313-329). */
 int gbtn_qn_bp_run(gbtn_qn_plan* plan, int32_t maxiter, double tol, int32_t* iters, double* mean_diff);
+/* Replaces: update(bpc; maxiter, tol, edge_sequence) with the reference's
+ * default sequential schedule (abstractbeliefpropagationcache.jl:272-287):
+ * the messages of edge_sequence (directed edges, repeats allowed) updated in
+ * order, each seeing every earlier update; executed in waves of messages that
+ * do not depend on one another, so the result is the strictly sequential one.
+ * The mean diff is over the sequence positions. */
+int gbtn_qn_bp_run_sequential(gbtn_qn_plan* plan, const int32_t* edge_sequence, int32_t edge_sequence_len,
+                              int32_t maxiter, double tol, int32_t* iters, double* mean_diff);
 /* Replaces: the one-site environments of expect (expect.jl:5-19): dense
  * rho_v[s', s] (d x d, block-diagonal in the site sectors) per vertex. */
 int gbtn_qn_vertex_rdms(gbtn_qn_plan* plan, double* out);

@@ -63,14 +63,21 @@ struct QBuf {
 // the shares of the blocks with that outgoing sector (slot lists in order);
 // the message is normalised over all its sectors in FP64 and compared with
 // the old one (message_diff).
+// de_list / pos_list (may be NULL: job j is directed edge j, diff slot j)
+// select the messages of one wave of the sequential schedule, which finalises
+// them in place (msg_old == msg_out: each entry is read before it is written,
+// by the same lane) and records each diff at its sequence position.
 __global__ void qn_finalize_kernel(int ndir, const int* __restrict__ vm_ptr, const int* __restrict__ vm_dim,
                                    const long long* __restrict__ sec_off, const int* __restrict__ slot_ptr,
                                    const int* __restrict__ slots, const long long* __restrict__ part_off,
-                                   const double* __restrict__ partial, const double* __restrict__ msg_old,
-                                   double* __restrict__ msg_out, double* diffs, int normalize, int want_diff) {
-  const int de = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+                                   const double* __restrict__ partial, const double* msg_old, double* msg_out,
+                                   double* diffs, int normalize, int want_diff, const int* __restrict__ de_list,
+                                   const int* __restrict__ pos_list) {
+  const int job = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (de >= ndir) return;
+  if (job >= ndir) return;
+  const int de = de_list ? de_list[job] : job;
+  const int pos = pos_list ? pos_list[job] : de;
   double nr2 = 0.0, dot = 0.0, nb = 0.0;
   for (int vm = vm_ptr[de]; vm < vm_ptr[de + 1]; ++vm) {
     const int c2 = vm_dim[vm] * vm_dim[vm];
@@ -95,7 +102,7 @@ __global__ void qn_finalize_kernel(int ndir, const int* __restrict__ vm_ptr, con
     const long long off = sec_off[vm];
     for (int i = lane; i < c2; i += 32) msg_out[off + i] *= sc;
   }
-  if (want_diff && lane == 0) diffs[de] = 1.0 - (dot * dot) / (nr2 * nb);
+  if (want_diff && lane == 0) diffs[pos] = 1.0 - (dot * dot) / (nr2 * nb);
 }
 
 // One thread block per vertex: the dense rho_v (d x d) from the shares of its
@@ -162,6 +169,13 @@ struct gbtn_qn_plan {
   QBuf<int> d_vm_ptr, d_vm_dim, d_slot_ptr, d_slots, d_vb_ptr, d_vblocks, d_blk_site_off, d_blk_ds, d_dsite, d_de_len;
   QBuf<int> d_conv, d_iters, d_net_de_ptr, d_net_de, d_net_v_ptr, d_net_v, d_net_e_ptr, d_net_e, d_nconv;
   int cur = 0;
+  // the graph (sequential schedule) and the waves of the last edge sequence
+  std::vector<int> eu, ev, leg_ptr, leg_edge, vblocks_ptr, vblocks_flat;
+  std::vector<VDesc> bd_host;
+  std::vector<int> seq_cached;
+  std::vector<WorkList> wave_small, wave_large;
+  std::vector<int> wave_job_ptr;
+  QBuf<int> d_wave_blocks, d_wave_de, d_wave_pos, d_seq_ptr, d_seq_pos;
 };
 
 namespace {
@@ -230,9 +244,145 @@ void qn_rdms(gbtn_qn_plan* P) {
   GBTN_CUDA(cudaGetLastError());
 }
 
+// Cut an edge sequence into waves (as the dense plan does): message j goes to
+// the first wave after every earlier message it depends on -- the last writer
+// of each message it reads (the incoming messages of its source vertex except
+// the one from its target), the readers of its own message since that
+// message's last write, and its last writer.  A wave runs the block kernel on
+// the blocks of its source vertices and finalises its messages in place.
+void build_qn_waves(gbtn_qn_plan* P, const int32_t* seq, int len) {
+  std::vector<int> key(seq, seq + len);
+  if (key == P->seq_cached && !P->wave_job_ptr.empty()) return;
+  const int ndir = 2 * P->ne;
+  std::vector<int> last_write(ndir, -1), last_read(ndir, -1), level(len, 0);
+  int nlev = 0;
+  auto src_of = [&](int de) { return (de & 1) ? P->ev[de >> 1] : P->eu[de >> 1]; };
+  for (int j = 0; j < len; ++j) {
+    const int de = seq[j];
+    require(de >= 0 && de < ndir, "edge_sequence entry out of range");
+    const int v = src_of(de), e = de >> 1;
+    int lv = 0;
+    std::vector<int> reads;
+    for (int q = P->leg_ptr[v]; q < P->leg_ptr[v + 1]; ++q) {
+      const int f = P->leg_edge[q];
+      if (f == e) continue;
+      const int din = 2 * f + (P->eu[f] == v ? 1 : 0);  // the message into v along f
+      reads.push_back(din);
+      lv = std::max(lv, last_write[din] + 1);
+    }
+    lv = std::max(lv, last_read[de] + 1);
+    lv = std::max(lv, last_write[de] + 1);
+    level[j] = lv;
+    nlev = std::max(nlev, lv + 1);
+    last_write[de] = lv;
+    for (int din : reads) last_read[din] = std::max(last_read[din], lv);
+  }
+  std::vector<std::vector<int>> jobs(nlev);
+  for (int j = 0; j < len; ++j) jobs[level[j]].push_back(j);
+  std::vector<int> blocks_flat, de_flat, pos_flat;
+  std::vector<std::pair<int, int>> ranges_small, ranges_large;  // (offset, count) into blocks_flat
+  P->wave_job_ptr.assign(1, 0);
+  std::vector<int> seen(P->nv, -1);
+  for (int l = 0; l < nlev; ++l) {
+    std::vector<int> sm, lg;
+    for (int j : jobs[l]) {
+      de_flat.push_back(seq[j]);
+      pos_flat.push_back(j);
+      const int v = src_of(seq[j]);
+      if (seen[v] == l) continue;
+      seen[v] = l;
+      for (int q = P->vblocks_ptr[v]; q < P->vblocks_ptr[v + 1]; ++q) {
+        const int b = P->vblocks_flat[q];
+        (P->bd_host[b].n <= kQnSmallN ? sm : lg).push_back(b);
+      }
+    }
+    P->wave_job_ptr.push_back((int)de_flat.size());
+    ranges_small.push_back({(int)blocks_flat.size(), (int)sm.size()});
+    blocks_flat.insert(blocks_flat.end(), sm.begin(), sm.end());
+    ranges_large.push_back({(int)blocks_flat.size(), (int)lg.size()});
+    blocks_flat.insert(blocks_flat.end(), lg.begin(), lg.end());
+  }
+  cudaStream_t s = ctx_stream(P->ctx);
+  if (blocks_flat.empty()) blocks_flat.push_back(0);
+  if (de_flat.empty()) {
+    de_flat.push_back(0);
+    pos_flat.push_back(0);
+  }
+  P->d_wave_blocks.upload(blocks_flat, s);
+  P->d_wave_de.upload(de_flat, s);
+  P->d_wave_pos.upload(pos_flat, s);
+  std::vector<int> pos_all(std::max(len, 1));
+  std::iota(pos_all.begin(), pos_all.end(), 0);
+  P->d_seq_pos.upload(pos_all, s);
+  P->d_seq_ptr.upload(std::vector<int>{0, len}, s);
+  P->d_diffs.alloc(std::max({2 * P->ne, len, 1}));
+  P->wave_small.clear();
+  P->wave_large.clear();
+  for (int l = 0; l < nlev; ++l) {
+    for (int which = 0; which < 2; ++which) {
+      const auto r = which == 0 ? ranges_small[l] : ranges_large[l];
+      WorkList w;
+      w.team = which == 0 ? 32 : 256;
+      w.count = r.second;
+      w.d_vertices = P->d_wave_blocks.p + r.first;
+      for (int i = 0; i < r.second; ++i) {
+        const VDesc& d = P->bd_host[blocks_flat[r.first + i]];
+        w.ncap = std::max(w.ncap, d.n);
+        w.maxdeg = std::max(w.maxdeg, d.k);
+      }
+      (which == 0 ? P->wave_small : P->wave_large).push_back(w);
+    }
+  }
+  P->seq_cached = key;
+}
+
 }  // namespace
 
 extern "C" {
+
+int gbtn_qn_bp_run_sequential(gbtn_qn_plan* P, const int32_t* edge_sequence, int32_t len, int32_t maxiter,
+                              double tol, int32_t* iters, double* mean_diff) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  QN_TRY
+  require(P && (edge_sequence || len == 0), "NULL argument");
+  require(maxiter >= 1, "You need to specify a number of iterations for BP!");
+  require(len >= 0, "edge_sequence_len must be >= 0");
+  cudaStream_t s = ctx_stream(P->ctx);
+  const bool want_diff = tol >= 0.0;
+  int it = 0;
+  double md = NAN;
+  if (len > 0) build_qn_waves(P, edge_sequence, len);
+  GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int), s));
+  GBTN_CUDA(cudaMemsetAsync(P->d_iters.p, 0, sizeof(int), s));
+  double* m = P->d_msg[P->cur].p;
+  for (it = 1; it <= maxiter; ++it) {
+    if (len == 0) break;
+    for (size_t l = 0; l + 1 < P->wave_job_ptr.size(); ++l) {
+      for (const WorkList* wl : {&P->wave_small[l], &P->wave_large[l]})
+        if (wl->count) launch_qn_blocks(*wl, P->d_bd.p, P->d_blocks.p, m, P->d_sec_off.p, P->d_partial.p,
+                                        P->d_part_off.p, 0, s);
+      const int j0 = P->wave_job_ptr[l], nj = P->wave_job_ptr[l + 1] - j0;
+      qn_finalize_kernel<<<(nj + 7) / 8, 256, 0, s>>>(nj, P->d_vm_ptr.p, P->d_vm_dim.p, P->d_sec_off.p,
+                                                      P->d_slot_ptr.p, P->d_slots.p, P->d_part_off.p, P->d_partial.p,
+                                                      m, m, P->d_diffs.p, 1, want_diff ? 1 : 0,
+                                                      P->d_wave_de.p + j0, P->d_wave_pos.p + j0);
+      GBTN_CUDA(cudaGetLastError());
+    }
+    if (want_diff) {
+      launch_reduce_diffs(1, P->d_seq_ptr.p, P->d_seq_pos.p, P->d_diffs.p, tol, P->d_conv.p, P->d_iters.p, P->d_mean.p,
+                          s);
+      int conv = 0;
+      GBTN_CUDA(cudaMemcpyAsync(&conv, P->d_conv.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      GBTN_CUDA(cudaMemcpyAsync(&md, P->d_mean.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+      GBTN_CUDA(cudaStreamSynchronize(s));
+      if (conv) break;
+    }
+  }
+  GBTN_CUDA(cudaStreamSynchronize(s));
+  if (iters) *iters = len == 0 ? maxiter : std::min(it, (int)maxiter);
+  if (mean_diff) *mean_diff = want_diff && len > 0 ? md : NAN;
+  QN_CATCH(C)
+}
 
 int gbtn_qn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, const gbtn_qn_desc* q, gbtn_qn_plan** out) {
   QN_TRY
@@ -417,6 +567,14 @@ int gbtn_qn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, const gbtn_qn_d
     roff += (long long)P->dsite[v] * P->dsite[v];
   }
   P->n_rdm = roff;
+  // the graph and the blocks of every vertex, for the sequential schedule
+  P->eu.assign(g->edge_u, g->edge_u + ne);
+  P->ev.assign(g->edge_v, g->edge_v + ne);
+  P->leg_ptr.assign(g->leg_ptr, g->leg_ptr + nv + 1);
+  P->leg_edge.assign(g->leg_edge, g->leg_edge + g->leg_ptr[nv]);
+  P->vblocks_ptr = vb_ptr;
+  P->vblocks_flat = vbl;
+  P->bd_host = bd;
   // device arrays
   P->d_bd.upload(bd, s);
   P->d_vm_ptr.upload(vm_ptr, s);
@@ -541,7 +699,7 @@ int gbtn_qn_bp_run(gbtn_qn_plan* P, int32_t maxiter, double tol, int32_t* iters,
     qn_finalize_kernel<<<(ndir + 7) / 8, 256, 0, s>>>(ndir, P->d_vm_ptr.p, P->d_vm_dim.p, P->d_sec_off.p,
                                                       P->d_slot_ptr.p, P->d_slots.p, P->d_part_off.p,
                                                       P->d_partial.p, P->d_msg[P->cur].p, P->d_msg[P->cur ^ 1].p,
-                                                      P->d_diffs.p, 1, want_diff ? 1 : 0);
+                                                      P->d_diffs.p, 1, want_diff ? 1 : 0, nullptr, nullptr);
     GBTN_CUDA(cudaGetLastError());
     P->cur ^= 1;
     if (want_diff) {

@@ -21,7 +21,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import check, dptr, iptr
-from .network import TensorNetwork
+from .network import TensorNetwork, default_edge_sequence
 
 
 def _csr(lists):
@@ -171,13 +171,31 @@ class QNBeliefPropagationCache:
         check(self.ctx.handle, self.lib.gbtn_qn_init_messages(self.handle))
         return self
 
-    def update(self, maxiter=None, tol=None):
+    def update(self, maxiter=None, tol=None, schedule="sequential", edge_sequence=None):
+        """update(bpc; maxiter, tol, edge_sequence): the reference's default
+        sequential schedule (forest-cover order unless ``edge_sequence`` is
+        given) or "parallel" (Jacobi) sweeps.  maxiter defaults to 1 on trees
+        and is required otherwise, as in the reference."""
+        if maxiter is None and self.q.tn.is_tree():
+            maxiter = 1
         if maxiter is None:
             raise _lib.InvalidArgument(1, "You need to specify a number of iterations for BP!")
         it = np.zeros(1, dtype=np.int32)
         md = np.zeros(1)
-        check(self.ctx.handle, self.lib.gbtn_qn_bp_run(self.handle, int(maxiter), -1.0 if tol is None else float(tol),
-                                                       iptr(it), dptr(md)))
+        t = -1.0 if tol is None else float(tol)
+        if schedule == "parallel":
+            check(self.ctx.handle, self.lib.gbtn_qn_bp_run(self.handle, int(maxiter), t, iptr(it), dptr(md)))
+        elif schedule == "sequential":
+            if edge_sequence is None:
+                if getattr(self, "_default_seq", None) is None:
+                    self._default_seq = np.ascontiguousarray(default_edge_sequence(self.q.tn), dtype=np.int32)
+                seq = self._default_seq
+            else:
+                seq = np.ascontiguousarray(edge_sequence, dtype=np.int32)
+            check(self.ctx.handle, self.lib.gbtn_qn_bp_run_sequential(self.handle, iptr(seq), len(seq), int(maxiter),
+                                                                      t, iptr(it), dptr(md)))
+        else:
+            raise _lib.InvalidArgument(1, f"unknown schedule {schedule!r}")
         self.iterations, self.mean_diff = int(it[0]), float(md[0])
         return self
 

@@ -53,7 +53,7 @@ def test_qn_bp_matches_dense_oracle(L):
                     assert np.max(np.abs(m[de][a1:b1, a2:b2])) < 1e-14
     bpc = gbtn.QNBeliefPropagationCache(q)
     assert bpc.n_block_elems < sum(tn.size(v) for v in range(tn.nv))  # only the allowed blocks are stored
-    bpc.update(maxiter=25)
+    bpc.update(maxiter=25, schedule="parallel")
     got = bpc.messages()
     assert max(float(np.max(np.abs(got[de] - m[de]))) for de in range(2 * g.ne)) <= 1e-12
     sz = bpc.expect(O.SZ)
@@ -71,7 +71,7 @@ def test_qn_convergence_and_diff():
     q = random_u1_lattice(4, 4, seed=3)
     g = oracle_graph(q.tn)
     m, it, md = O.bp_update(g, q.tn.tensors, O.identity_messages(g), maxiter=200, tol=1e-12, schedule="parallel")
-    bpc = gbtn.QNBeliefPropagationCache(q).update(maxiter=200, tol=1e-12)
+    bpc = gbtn.QNBeliefPropagationCache(q).update(maxiter=200, tol=1e-12, schedule="parallel")
     assert abs(bpc.iterations - it) <= 1
     assert max(float(np.max(np.abs(bpc.messages()[de] - m[de]))) for de in range(2 * g.ne)) <= 1e-6
     bpc.close()
@@ -91,7 +91,7 @@ def test_qn_graded_loopy_product_state_scalar():
         flux.append(1 if odd else -1)
     tn.tensors = ts
     q = gbtn.QNNetwork(tn, [[(0, 1)]] * tn.ne, [UP_DOWN] * tn.nv, flux)
-    bpc = gbtn.QNBeliefPropagationCache(q).update(maxiter=25)
+    bpc = gbtn.QNBeliefPropagationCache(q).update(maxiter=25)  # the reference's default: sequential
     n2 = bpc.scalar()
     assert np.isfinite(n2) and n2 != 0
     assert n2 == pytest.approx(O.exact_scalar(oracle_graph(tn), ts), rel=1e-12)
@@ -108,3 +108,38 @@ def test_qn_refusals():
     q9 = gbtn.random_qn_network(tn9, [[(0, 9)]] * tn9.ne, [UP_DOWN] * tn9.nv, [1, 1, 1, 1], 1)
     with pytest.raises(gbtn.Unsupported, match="sector dimensions"):
         gbtn.QNBeliefPropagationCache(q9)
+
+
+@pytest.mark.parametrize("L", [(3, 3), (4, 3)])
+def test_qn_sequential_schedule_matches_the_strict_sequence(L):
+    """The reference's default update: the forest-cover edge sequence, each
+    message seeing every earlier one.  Three sweeps (far from converged, so
+    the order matters) equal the dense oracle's strictly sequential sweeps to
+    1e-12, with the mean diff over the sequence; a sequence with repeats and
+    a converged run with a tolerance as well."""
+    q = random_u1_lattice(*L, seed=30 + L[0])
+    tn = q.tn
+    g = oracle_graph(tn)
+    A = tn.tensors
+    seq = list(gbtn.default_edge_sequence(tn))
+    m, _, md = O.bp_update(g, A, O.identity_messages(g), maxiter=3, tol=0.0, schedule="sequential", edge_sequence=seq)
+    bpc = gbtn.QNBeliefPropagationCache(q).update(maxiter=3, tol=0.0)
+    got = bpc.messages()
+    assert max(float(np.max(np.abs(got[de] - m[de]))) for de in range(2 * g.ne)) <= 1e-12
+    assert bpc.mean_diff == pytest.approx(md, rel=1e-9, abs=1e-15)
+    # repeats and gaps in the sequence
+    seq2 = seq[: len(seq) // 2] + seq[:3] + seq[len(seq) // 2:][::2]
+    m2, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=2, schedule="sequential", edge_sequence=seq2)
+    bpc.init_messages()
+    bpc.update(maxiter=2, edge_sequence=seq2)
+    got2 = bpc.messages()
+    assert max(float(np.max(np.abs(got2[de] - m2[de]))) for de in range(2 * g.ne)) <= 1e-12
+    # to convergence under the tolerance: the oracle's sequential run (Jacobi
+    # sweeps may oscillate or settle elsewhere on a loopy graph)
+    bpc.init_messages()
+    bpc.update(maxiter=200, tol=1e-14)
+    ref, it, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=200, tol=1e-14, schedule="sequential",
+                             edge_sequence=seq)
+    assert abs(bpc.iterations - it) <= 1
+    np.testing.assert_allclose(bpc.expect(O.SZ), O.expect1(g, A, ref, O.SZ), rtol=1e-9, atol=1e-12)
+    bpc.close()
