@@ -1173,10 +1173,11 @@ void compute_rdms(gbtn_plan* P) {
     large_rdms(P, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p, P->d_rdm.p);
     return;
   }
-  launch_vertex_rdms(P->lists[0].first, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p,
-                     P->d_msg_off.p, P->d_rdm_off.p, P->d_rdm.p, s);
-  launch_vertex_rdms(P->lists[0].second, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p,
-                     P->d_msg_off.p, P->d_rdm_off.p, P->d_rdm.p, s);
+  // real plans: the contractions in double-FP32 (~48-bit, FP64 in and out),
+  // at ~2.7x the FP64 pipe's rate; traces, ratios and logs stay FP64
+  for (const WorkList* wl : {&P->lists[0].first, &P->lists[0].second})
+    launch_vertex_rdms_df32(*wl, P->d_vd.p, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p,
+                            P->d_msg_off.p, P->d_rdm_off.p, P->d_rdm.p, s);
   large_rdms(P, P->d_fac.p, P->sep_bra ? P->d_bra.p : nullptr, P->d_msg[P->cur].p, P->d_rdm.p);
 }
 

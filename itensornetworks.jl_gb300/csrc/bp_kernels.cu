@@ -329,27 +329,35 @@ __global__ void __launch_bounds__(256)
 
 // rho_v[s', s] for every listed vertex: absorb all incoming messages, CLOSE on
 // the site index.
-template <typename T, int TEAM>
+// rho_v of every listed vertex: all incoming messages absorbed, CLOSE on the
+// site index.  T is the arithmetic, S the storage (S = T, or double under
+// df32 arithmetic: FP64 tensors, messages and RDMs, ~48-bit contractions).
+template <typename T, int TEAM, typename S = T>
 __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
     vertex_rdm_kernel(const int* __restrict__ work, int nwork, const VDesc* __restrict__ vd,
-                      const T* __restrict__ fac, const T* __restrict__ bra_g, const T* msgs,
-                      const long long* __restrict__ msg_off, const long long* __restrict__ rdm_off, T* rdm,
+                      const S* __restrict__ fac, const S* __restrict__ bra_g, const S* msgs,
+                      const long long* __restrict__ msg_off, const long long* __restrict__ rdm_off, S* rdm,
                       int ncap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPB = TEAM == 32 ? 4 : 1;
   const int team = threadIdx.x / TEAM, tid = threadIdx.x % TEAM;
   const size_t tb = team_smem_bytes<T>(padded_len(ncap), 3, bra_g != nullptr, TEAM);
-  TeamSmem<T> S = carve<T>(smem_raw + team * tb, padded_len(ncap), 3, bra_g != nullptr, TEAM);
+  TeamSmem<T> Sm = carve<T>(smem_raw + team * tb, padded_len(ncap), 3, bra_g != nullptr, TEAM);
   for (int w = blockIdx.x * TPB + team; w < nwork; w += gridDim.x * TPB) {
     const int v = work[w];
-    load_desc<TEAM>(S.desc, vd + v, tid);
+    load_desc<TEAM>(Sm.desc, vd + v, tid);
     tsync<TEAM>();
-    load_vertex<T, TEAM, T, true>(S, fac, bra_g, msgs, msg_off, -1, tid);
+    load_vertex<T, TEAM, S, true>(Sm, fac, bra_g, msgs, msg_off, -1, tid);
     tsync<TEAM>();
-    const int cur = chain_absorb<T, TEAM>(S, -1, tid);
-    const VDesc& d = *S.desc;
-    close_any<T, TEAM, true>(d.d, S.buf[cur], S.bra, d.n, 1, 1, 0, 0, S.red, S.res, tid);
-    for (int i = tid; i < d.d * d.d; i += TEAM) rdm[rdm_off[v] + i] = S.res[i];
+    const int cur = chain_absorb<T, TEAM>(Sm, -1, tid);
+    const VDesc& d = *Sm.desc;
+    close_any<T, TEAM, true>(d.d, Sm.buf[cur], Sm.bra, d.n, 1, 1, 0, 0, Sm.red, Sm.res, tid);
+    for (int i = tid; i < d.d * d.d; i += TEAM) {
+      if constexpr (std::is_same<T, df32>::value)
+        rdm[rdm_off[v] + i] = df_to_double(Sm.res[i]);
+      else
+        rdm[rdm_off[v] + i] = Sm.res[i];
+    }
     tsync<TEAM>();
   }
 }
@@ -877,6 +885,25 @@ void launch_vertex_rdms(const WorkList& wl, const VDesc* vd, const T* fac, const
 }
 template void launch_vertex_rdms<double>(const WorkList&, const VDesc*, const double*, const double*, const double*,
                                          const long long*, const long long*, double*, cudaStream_t);
+
+void launch_vertex_rdms_df32(const WorkList& wl, const VDesc* vd, const double* fac, const double* bra,
+                             const double* msgs, const long long* msg_off, const long long* rdm_off, double* rdm,
+                             cudaStream_t s) {
+  if (wl.count == 0) return;
+  if (wl.team == 32) {
+    const size_t sm = 4 * team_smem_bytes<df32>(padded_len(wl.ncap), 3, bra != nullptr, 32);
+    auto kern = vertex_rdm_kernel<df32, 32, double>;
+    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    kern<<<(wl.count + 3) / 4, 128, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msgs, msg_off, rdm_off, rdm,
+                                              wl.ncap);
+  } else {
+    const size_t sm = team_smem_bytes<df32>(padded_len(wl.ncap), 3, bra != nullptr, 256);
+    auto kern = vertex_rdm_kernel<df32, 256, double>;
+    GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    kern<<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, vd, fac, bra, msgs, msg_off, rdm_off, rdm, wl.ncap);
+  }
+  GBTN_CUDA(cudaGetLastError());
+}
 template void launch_vertex_rdms<zdouble>(const WorkList&, const VDesc*, const zdouble*, const zdouble*,
                                           const zdouble*, const long long*, const long long*, zdouble*, cudaStream_t);
 

@@ -257,6 +257,9 @@ template <typename T>
 void launch_vertex_rdms(const WorkList& wl, const VDesc* vd, const T* fac, const T* bra,
                         const T* msgs, const long long* msg_off, const long long* rdm_off,
                         T* rdm, cudaStream_t s);
+void launch_vertex_rdms_df32(const WorkList& wl, const VDesc* vd, const double* fac, const double* bra,
+                             const double* msgs, const long long* msg_off, const long long* rdm_off, double* rdm,
+                             cudaStream_t s);
 
 template <typename T>
 void launch_edge_halves(const int* jobs /*pairs (v, leg)*/, int njobs, int ncap, int maxdeg,
