@@ -33,9 +33,10 @@
 # It also adds `apply(Algorithm("gb300"), gates, psi; maxdim, cutoff, normalize,
 # envs)`, the simple update of src/apply.jl:33-160 on the GPU (FP64 truncated
 # SVD), `tebd(Algorithm("gb300"), ℋ, ψ; β, Δβ, maxdim, cutoff)` over it (src/tebd.jl),
-# and a ChainRulesCore rrule for `bp_energy(psi, ops, coefs)`, the BP
-# two-site energy, whose pullback is the library's hand-written adjoint
-# (implicit differentiation at the BP fixed point).
+# and ChainRulesCore rrules for `bp_energy(psi, ops, coefs)` (the BP two-site
+# energy), `bp_logscalar(psi)` and `bp_expect_sum(psi, op)`, whose pullbacks are
+# the library's hand-written adjoints (implicit differentiation at the BP fixed
+# point; complex tensors too).
 #
 # Not executed in the environment this file was written in (no Julia
 # toolchain); it documents the binding a maintainer adds.
@@ -739,6 +740,86 @@ function ChainRulesCore.rrule(::typeof(bp_energy), psi, ops, coefs; maxiter=500)
         return (NoTangent(), Dict(v => dE * t for (v, t) in dpsi), NoTangent(), NoTangent())
     end
     return E, bp_energy_pullback
+end
+
+# ---- BP log-norm and one-site expectation values with their adjoints -----------
+
+"""
+    bp_logscalar(psi; maxiter=500)
+
+Re logscalar of the BP cache of psi (abstractbeliefpropagationcache.jl:397-408)
+at the converged (mixed-precision, refined) messages.
+"""
+bp_logscalar(psi; maxiter=500) = first(scalar_and_grad(psi, nothing; maxiter, want_grad=false))
+
+"""
+    bp_expect_sum(psi, op; maxiter=500)
+
+Re sum_v <op>_v (expect.jl:5-19) with one d x d operator op[s', s] for every site.
+"""
+bp_expect_sum(psi, op::AbstractMatrix; maxiter=500) = first(scalar_and_grad(psi, op; maxiter, want_grad=false))
+
+# value and gradient (dL/dA as one ITensor per vertex; for complex tensors
+# dL/dRe + i dL/dIm, ChainRulesCore's convention) through the fixed point
+function scalar_and_grad(psi, op; maxiter=500, want_grad=true)
+    cplx = any(v -> eltype(psi[v]) <: Complex, ITensorNetworks.vertices(psi)) || eltype(op) <: Complex
+    p = pack_state(psi; cplx)
+    ctx = context()
+    opbuf = op === nothing ? Float64[] : (cplx ? collect(reinterpret(Float64, vec(ComplexF64.(op)))) : vec(Float64.(op)))
+    data = cplx ? reinterpret(Float64, p.data) : p.data
+    GC.@preserve p opbuf data begin
+        desc = GraphDesc(length(p.vs), length(p.es), pointer(p.eu), pointer(p.ev), pointer(p.edim),
+            pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0, cplx ? 1 : 0)
+        plan = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ctx, ccall((:gbtn_plan_create, libgbtn), Cint, (Ptr{Cvoid}, Ref{GraphDesc}, Ref{Ptr{Cvoid}}),
+            ctx, desc, plan))
+        try
+            check(ctx, ccall((:gbtn_set_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Cint),
+                plan[], data, C_NULL, 0))
+            # real tensors: the mixed pipeline; complex ones: FP32 then FP64 sweeps
+            opts = BPOpts(1, 3, maxiter, 1, 1e-14, C_NULL, 0, 0.0, 0.0, 0, 0, 0, 0, 0)
+            check(ctx, ccall((:gbtn_bp_run, libgbtn), Cint, (Ptr{Cvoid}, Ref{BPOpts}, Ptr{Int32}, Ptr{Float64}),
+                plan[], opts, C_NULL, C_NULL))
+            val = Ref{Float64}(0.0)
+            grad = similar(data)
+            gopts = GradOpts(0, 500, 1e-12, 0, 0)
+            if op === nothing
+                check(ctx, ccall((:gbtn_logscalar_grad, libgbtn), Cint,
+                    (Ptr{Cvoid}, Ref{GradOpts}, Ref{Float64}, Ptr{Float64}, Ptr{Int32}, Ptr{Float64}),
+                    plan[], gopts, val, grad, C_NULL, C_NULL))
+            else
+                check(ctx, ccall((:gbtn_expect1_grad, libgbtn), Cint,
+                    (Ptr{Cvoid}, Ptr{Float64}, Ref{GradOpts}, Ref{Float64}, Ptr{Float64}, Ptr{Int32}, Ptr{Float64}),
+                    plan[], opbuf, gopts, val, grad, C_NULL, C_NULL))
+            end
+            want_grad || return (val[], nothing)
+            g = cplx ? reinterpret(ComplexF64, grad) : grad
+            dpsi = Dict{Any, ITensor}()
+            off = 0
+            for (i, v) in enumerate(p.vs)
+                ls = [p.links[p.leg_edge[q] + 1] for q in (p.leg_ptr[i] + 1):p.leg_ptr[i + 1]]
+                shp = (Int(p.sdim[i]), length.(ls)...)
+                len = prod(shp)
+                dpsi[v] = itensor(reshape(g[(off + 1):(off + len)], shp), p.sites[i], ls...)
+                off += len
+            end
+            return (val[], dpsi)
+        finally
+            ccall((:gbtn_plan_destroy, libgbtn), Cint, (Ptr{Cvoid},), plan[])
+        end
+    end
+end
+
+function ChainRulesCore.rrule(::typeof(bp_logscalar), psi; maxiter=500)
+    L, dpsi = scalar_and_grad(psi, nothing; maxiter)
+    bp_logscalar_pullback(dL) = (NoTangent(), Dict(v => dL * t for (v, t) in dpsi))
+    return L, bp_logscalar_pullback
+end
+
+function ChainRulesCore.rrule(::typeof(bp_expect_sum), psi, op; maxiter=500)
+    X, dpsi = scalar_and_grad(psi, op; maxiter)
+    bp_expect_sum_pullback(dX) = (NoTangent(), Dict(v => dX * t for (v, t) in dpsi), NoTangent())
+    return X, bp_expect_sum_pullback
 end
 
 end
