@@ -579,6 +579,27 @@ def run_ours(args):
         return max_ranks(e0.elapsed_time(e1) / n)
 
     seq_ms = {p: per_sweep_seq(p, 3) for p in ("f32", "df32", "f64")}
+
+    # time to solution with the sequential schedule (tol as the headline): the
+    # mixed pipeline's FP32 and double-FP32 waves against plain FP64 waves
+    def solve_seq(precision):
+        bpc.init_messages("identity")
+        barrier()
+        e0.record(stream)
+        bpc.update(maxiter=args.solve_maxiter, tol=args.solve_tol, schedule="sequential", precision=precision)
+        e1.record(stream)
+        barrier()
+        return max_ranks(e0.elapsed_time(e1)), bpc.expect(sz_op), bpc.phase_sweeps()
+
+    solve_seq("mixed")
+    seq64_ms, seq64_sz, seq64_ph = solve_seq("f64")
+    seqmix_ms, seqmix_sz, seqmix_ph = solve_seq("mixed")
+    seq_tts = {"tol": args.solve_tol, "fp64_ms": seq64_ms, "fp64_sweeps": seq64_ph["f64"], "mixed_ms": seqmix_ms,
+               "mixed_phase_sweeps": seqmix_ph, "speedup": seq64_ms / seqmix_ms,
+               "mixed_max_rel_err_sz_vs_oracle": oracle_sz_error(seqmix_sz, "peps32x32_chi8_batch16.npz", sizes)
+               if rank == 0 else None,
+               "fp64_max_rel_err_sz_vs_oracle": oracle_sz_error(seq64_sz, "peps32x32_chi8_batch16.npz", sizes)
+               if rank == 0 else None}
     ctx.set_profiling(True)
     bpc.update(maxiter=args.steps, schedule="parallel", precision="bf16")
     barrier()
@@ -695,7 +716,8 @@ def run_ours(args):
             "paths_ms_per_sweep": {"bf16_tensor_core": ms_bf16, "f32_simt": ms_f32, "df32_simt": ms_df32,
                                    "f64_simt": ms_f64},
             "sequential_schedule": {"ms_per_sweep": seq_ms,
-                                    "msg_updates_per_s": {p: msgs_step / (ms * 1e-3) for p, ms in seq_ms.items()}},
+                                    "msg_updates_per_s": {p: msgs_step / (ms * 1e-3) for p, ms in seq_ms.items()},
+                                    "time_to_solution": seq_tts},
             "tc_split": {"tensor_core_vertices": n_tc, "simt_vertices": tn.nv - n_tc, "tuned_split_ms": tune_ms},
             "gauge_scaling": gauge,
             "batched_uneven": batched,

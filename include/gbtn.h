@@ -61,10 +61,14 @@ enum gbtn_schedule { GBTN_SCHED_SEQUENTIAL = 0, GBTN_SCHED_PARALLEL = 1, GBTN_SC
  * by default, or FP64: gbtn_bp_opts.refine), each phase started from the
  * previous phase's fixed point.  DF32 is double-FP32 arithmetic (a value is
  * the unevaluated sum of two floats, ~48 significant bits, on the FP32 pipe)
- * on FP64 tensors and messages, with message norms and diffs in FP64.  BF16,
- * DF32 and MIXED run the PARALLEL and COLORED schedules (SEQUENTIAL returns
- * GBTN_ERR_UNSUPPORTED); FP32 and FP64 run all three.  Complex plans have no
- * BF16 or DF32 path: their MIXED pipeline is FP32 then FP64. */
+ * on FP64 tensors and messages, with message norms and diffs in FP64.  BF16
+ * runs the PARALLEL and COLORED schedules (SEQUENTIAL returns
+ * GBTN_ERR_UNSUPPORTED: the tensor-core kernel computes every message of a
+ * vertex at once); MIXED with SEQUENTIAL runs its FP32 and refinement phases
+ * in waves, without the BF16 phase.  FP32 and FP64 run all three schedules
+ * on any plan, DF32 and MIXED SEQUENTIAL on plans without vertices of the
+ * global-memory path.  Complex plans have no BF16 or DF32 path: their MIXED
+ * pipeline is FP32 then FP64. */
 enum gbtn_precision { GBTN_F64 = 0, GBTN_F32 = 1, GBTN_BF16 = 2, GBTN_MIXED = 3, GBTN_DF32 = 4 };
 /* Refinement arithmetic of MIXED after its FP32 phase. */
 enum gbtn_refine { GBTN_REFINE_DF32 = 0, GBTN_REFINE_F64 = 1 };

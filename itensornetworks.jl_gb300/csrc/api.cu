@@ -1089,25 +1089,29 @@ void build_waves(gbtn_plan* P, const std::vector<std::vector<int2>>& per) {
 
 // Sweeps of the sequential schedule as waves (see build_waves), in place on
 // msgs, in arithmetic `arith`; per-network convergence as the other schedules.
-void run_waves(gbtn_plan* P, int arith, const void* fac, const void* bra, void* msgs, const gbtn_bp_opts* o) {
+// Sequential sweeps in waves: `maxiter` sweeps in arithmetic `arith`, per-network
+// convergence at `tol` (< 0: none), and a reduced-precision phase's noise-floor
+// stop after `stall` sweeps without progress (0: none).
+void run_waves(gbtn_plan* P, int arith, const void* fac, const void* bra, void* msgs, int maxiter, double tol,
+               int normalize, int stall = 0) {
   cudaStream_t s = P->ctx->stream;
-  const bool want_diff = o->tol >= 0.0;
+  const bool want_diff = tol >= 0.0;
   GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int) * P->nnet, s));
   GBTN_CUDA(cudaMemsetAsync(P->d_iters.p, 0, sizeof(int) * P->nnet, s));
   GBTN_CUDA(cudaMemsetAsync(P->d_nconv.p, 0, sizeof(int), s));
   const int* conv = want_diff ? P->d_conv.p : nullptr;
-  const GraphKey key{20 + arith, GBTN_SCHED_SEQUENTIAL, o->normalize, want_diff ? 1 : 0, 0, P->wave_version,
-                     P->list_version, o->tol};
-  sweep_loop(P, o->maxiter, key, [&] {
+  const GraphKey key{20 + arith, GBTN_SCHED_SEQUENTIAL, normalize, want_diff ? 1 : 0, stall, P->wave_version,
+                     P->list_version, tol};
+  sweep_loop(P, maxiter, key, [&] {
     for (const auto& w : P->waves) {
       launch_bp_wave_any(arith, w.first, P->d_vd.p, fac, bra, msgs, P->d_msg_off.p, P->d_pos_diffs.p, conv,
-                         o->normalize, want_diff, s);
+                         normalize, want_diff, s);
       launch_bp_wave_any(arith, w.second, P->d_vd.p, fac, bra, msgs, P->d_msg_off.p, P->d_pos_diffs.p, conv,
-                         o->normalize, want_diff, s);
+                         normalize, want_diff, s);
     }
     if (want_diff)
-      launch_reduce_diffs(P->nnet, P->d_wave_ptr.p, P->d_wave_iota.p, P->d_pos_diffs.p, o->tol, P->d_conv.p,
-                          P->d_iters.p, P->d_mean.p, s, 0, P->d_best.p, P->d_since.p, P->d_nconv.p);
+      launch_reduce_diffs(P->nnet, P->d_wave_ptr.p, P->d_wave_iota.p, P->d_pos_diffs.p, tol, P->d_conv.p,
+                          P->d_iters.p, P->d_mean.p, s, stall, P->d_best.p, P->d_since.p, P->d_nconv.p);
   }, want_diff);
 }
 
@@ -1916,14 +1920,20 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
   }
   if (o->precision == GBTN_BF16 && o->schedule == GBTN_SCHED_SEQUENTIAL)
     throw Unsupported("BF16 sweeps run the parallel or coloured schedule");
-  if (o->precision == GBTN_MIXED && o->schedule == GBTN_SCHED_SEQUENTIAL)
-    throw Unsupported("the mixed BF16 -> FP32 -> FP64 pipeline runs the parallel or coloured schedule");
-  if (o->precision == GBTN_DF32 && o->schedule == GBTN_SCHED_SEQUENTIAL && P->has_large)
-    throw Unsupported("double-FP32 sequential sweeps take vertices of the shared-memory kernels only");
+  if ((o->precision == GBTN_DF32 || o->precision == GBTN_MIXED) && o->schedule == GBTN_SCHED_SEQUENTIAL &&
+      P->has_large)
+    throw Unsupported("double-FP32 and mixed sequential sweeps take vertices of the shared-memory kernels only");
   if (P->cplx && o->precision == GBTN_BF16)
     throw Unsupported("complex tensors have no tensor-core (BF16) path: use f32, mixed or f64");
   if (P->cplx && o->precision == GBTN_DF32)
     throw Unsupported("complex tensors have no double-FP32 path: use f32, mixed or f64");
+  // phase slots of gbtn_plan_phase_sweeps: 0 BF16, 1 FP32, 2 refinement, 3 FP64
+  auto phase_done = [&](int slot, double phase_tol, int sweeps_run) {
+    if (phase_tol >= 0.0)
+      record_phase(P, slot);  // the reduction kernel counted each network's sweeps
+    else
+      P->phase_fixed[slot] = sweeps_run;  // no convergence test: every sweep ran
+  };
   if (o->schedule == GBTN_SCHED_SEQUENTIAL) {
     require(o->edge_sequence && o->edge_sequence_len > 0, "SEQUENTIAL needs an edge sequence");
     std::vector<std::vector<int2>> per(P->nnet);
@@ -1951,28 +1961,46 @@ int gbtn_bp_run(gbtn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mea
     }
     // waves of independent messages, in sequence order (see build_waves)
     build_waves(P, per);
-    const void* bra = nullptr;
-    if (o->precision == GBTN_F32) {
+    const void* bra64 = P->sep_bra ? P->d_bra.p : nullptr;
+    auto f32_waves = [&](int maxit, double tol, int stall) {
       ensure_f32(P);
       launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->es() * P->n_msg, s);
-      if (P->sep_bra) bra = P->d_bra32.p;
-      run_waves(P, P->cplx ? kArithZ32 : kArithF32, P->d_fac32.p, bra, P->d_msg32[0].p, o);
+      run_waves(P, P->cplx ? kArithZ32 : kArithF32, P->d_fac32.p, P->sep_bra ? P->d_bra32.p : nullptr,
+                P->d_msg32[0].p, maxit, tol, o->normalize, stall);
       launch_convert_f32_to_f64(P->d_msg32[0].p, P->d_msg[P->cur].p, P->es() * P->n_msg, s);
+    };
+    if (o->precision == GBTN_F32) {
+      f32_waves(o->maxiter, o->tol, 0);
+      phase_done(1, o->tol, o->maxiter);
+      finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
+    } else if (o->precision == GBTN_MIXED) {
+      // FP32 waves to their tolerance or noise floor, then double-FP32 (or
+      // FP64) waves to tol from that point; the BF16 tensor-core kernel
+      // computes every message of a vertex at once, which this schedule's
+      // one-message jobs do not use
+      const double tol32 = o->tol_f32 > 0 ? o->tol_f32 : 1e-13;
+      const int it32 = o->maxiter_f32 > 0 ? o->maxiter_f32 : o->maxiter;
+      f32_waves(it32, tol32, kStallSweeps);
+      phase_done(1, tol32, it32);
+      const int nref = o->refine_f64 > 0 ? std::min(o->refine_f64, o->maxiter) : o->maxiter;
+      const int arith = P->cplx ? kArithZ64 : (o->refine == GBTN_REFINE_F64 ? kArithF64 : kArithDF32);
+      run_waves(P, arith, P->d_fac.p, bra64, P->d_msg[P->cur].p, nref, o->tol, o->normalize);
+      phase_done(2, o->tol, nref);
+      int last = nref;
+      if (o->confirm_f64 > 0 && !P->cplx && arith == kArithDF32) {
+        last = std::min(o->confirm_f64, o->maxiter);
+        run_waves(P, kArithF64, P->d_fac.p, bra64, P->d_msg[P->cur].p, last, o->tol, o->normalize);
+        phase_done(3, o->tol, last);
+      }
+      finish_iters(P, want_diff, last, iters, mean_diff);
     } else {
-      if (P->sep_bra) bra = P->d_bra.p;
       const int arith = P->cplx ? kArithZ64 : (o->precision == GBTN_DF32 ? kArithDF32 : kArithF64);
-      run_waves(P, arith, P->d_fac.p, bra, P->d_msg[P->cur].p, o);
+      run_waves(P, arith, P->d_fac.p, bra64, P->d_msg[P->cur].p, o->maxiter, o->tol, o->normalize);
+      phase_done(o->precision == GBTN_DF32 ? 2 : 3, o->tol, o->maxiter);
+      finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
     }
-    finish_iters(P, want_diff, o->maxiter, iters, mean_diff);
     return GBTN_OK;
   }
-  // phase slots of gbtn_plan_phase_sweeps: 0 BF16, 1 FP32, 2 refinement, 3 FP64
-  auto phase_done = [&](int slot, double phase_tol, int sweeps_run) {
-    if (phase_tol >= 0.0)
-      record_phase(P, slot);  // the reduction kernel counted each network's sweeps
-    else
-      P->phase_fixed[slot] = sweeps_run;  // no convergence test: every sweep ran
-  };
   if (P->cplx && o->precision == GBTN_F64) {
     run_sweeps<zdouble>(P, o->schedule, o->maxiter, o->tol, o->normalize, zptr(P->d_msg[0].p), zptr(P->d_msg[1].p),
                         zptr(P->d_fac.p), P->sep_bra ? zptr(P->d_bra.p) : nullptr, P->cur);

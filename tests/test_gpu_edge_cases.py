@@ -111,13 +111,14 @@ def test_site_dimension_one_and_mixed_site_dimensions(precision):
     np.testing.assert_allclose(got, want, rtol=0, atol=(1e-10 if precision == "f64" else 1e-5))
 
 
-def test_reduced_precision_pipelines_refuse_the_sequential_schedule():
-    # BF16 and the mixed pipeline sweep in parallel or in colour classes; a
-    # sequential request is refused rather than run at another precision
+def test_bf16_refuses_the_sequential_schedule():
+    # the tensor-core kernel computes every message of a vertex at once, so
+    # BF16 sweeps run in parallel or in colour classes; a sequential request is
+    # refused rather than run at another precision (the mixed pipeline runs its
+    # FP32 and refinement phases in waves: test_gpu_sequential.py)
     bpc = gbtn.BeliefPropagationCache(gbtn.random_network(gbtn.square_lattice(3, 3, chi=2), 1))
-    for precision in ("bf16", "mixed"):
-        with pytest.raises(gbtn.Unsupported):
-            bpc.update(maxiter=2, schedule="sequential", precision=precision)
+    with pytest.raises(gbtn.Unsupported):
+        bpc.update(maxiter=2, schedule="sequential", precision="bf16")
 
 
 def test_degree_eight_vertex_on_a_star_is_exact():

@@ -73,3 +73,32 @@ def test_sequences_with_repeats_and_gaps():
     assert max_err(bpc.messages(), m) <= 1e-12
     assert float(bpc.mean_diff[0]) == pytest.approx(md, rel=1e-9, abs=1e-15)
     bpc.close()
+
+
+def test_mixed_sequential_pipeline_reaches_the_oracle_fixed_point():
+    """MIXED with the reference's default schedule: FP32 waves to their
+    tolerance or noise floor, then double-FP32 waves to tol.  The result
+    is within 1e-6 relative <Sz> of the oracle's sequential fixed point (the
+    mixed pipeline's bound; tol 1e-14 itself leaves ~1e-7), with the phase
+    sweeps recorded; refine="f64" and confirm_f64 run their FP64 waves."""
+    g = O.square_lattice(6, 6, chi=6)
+    A = O.random_network(g, 19)
+    seq = list(gbtn.default_edge_sequence(net(g, A)))
+    ref_m, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=60, schedule="sequential", edge_sequence=seq)
+    ref = O.expect1(g, A, ref_m, O.SZ)
+    scale = np.max(np.abs(ref))
+    bpc = gbtn.BeliefPropagationCache(net(g, A))
+    bpc.update(maxiter=200, tol=1e-14, precision="mixed")
+    ph = bpc.phase_sweeps()
+    assert ph["bf16"] == 0 and ph["f32"] >= 1 and ph["refine"] >= 1 and ph["f64"] == 0
+    assert np.max(np.abs(bpc.expect(O.SZ) - ref)) / scale <= 1e-6
+    bpc.init_messages("identity")
+    bpc.update(maxiter=200, tol=1e-14, precision="mixed", refine="f64")
+    assert np.max(np.abs(bpc.expect(O.SZ) - ref)) / scale <= 1e-6
+    bpc.init_messages("identity")
+    bpc.update(maxiter=200, tol=1e-14, precision="mixed", confirm_f64=1)
+    assert bpc.phase_sweeps()["f64"] == 1
+    assert np.max(np.abs(bpc.expect(O.SZ) - ref)) / scale <= 1e-6
+    with pytest.raises(gbtn.Unsupported):
+        bpc.update(maxiter=2, tol=1e-14, precision="bf16")
+    bpc.close()
