@@ -33,6 +33,7 @@ namespace gbtn {
 namespace {
 
 constexpr int kLargeThreads = 256;
+constexpr int kCloseRed = 16 * kLargeThreads;  // CLOSE: one 4 x 4 block per thread and slice
 
 __host__ __device__ inline long long lmin(long long a, long long b) { return a < b ? a : b; }
 
@@ -103,13 +104,27 @@ __global__ void __launch_bounds__(kLargeThreads)
     for (int i = threadIdx.x; i < cnt; i += kLargeThreads) tile[i] = in[(long long)(i / nl) * st + i % nl];
   }
   __syncthreads();
+  // four outputs b0 .. b0 + 3 of one fiber (j, l) per work item: each fiber
+  // value is loaded once for the four; adjacent threads take adjacent l with
+  // the same b0, so M is read by broadcast and the tile without conflicts
   T* out = wave_buf(scratch, a.buf_off, w, dst, n) + base;
-  for (int i = threadIdx.x; i < cnt; i += kLargeThreads) {
-    const int l = i % nl, r = i / nl, b = r % chi, j = r / chi;
+  const int nb4 = (chi + 3) / 4;
+  const int items = nj * nb4 * nl;
+  for (int i = threadIdx.x; i < items; i += kLargeThreads) {
+    const int l = i % nl, rest = i / nl, b0 = (rest % nb4) * 4, j = rest / nb4;
     const T* x = tile + (long long)j * chi * nl + l;
-    T y = T(0);
-    for (int q = 0; q < chi; ++q) y = mac(M[b + chi * q], x[q * nl], y);
-    out[(long long)r * st + l] = settle(y);
+    T y[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) y[k] = T(0);
+    for (int q = 0; q < chi; ++q) {
+      const T xq = x[q * nl];
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (b0 + k < chi) y[k] = mac(M[b0 + k + chi * q], xq, y[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (b0 + k < chi) out[((long long)j * chi + b0 + k) * st + l] = settle(y[k]);
   }
 }
 
@@ -149,40 +164,57 @@ __global__ void __launch_bounds__(kLargeThreads)
   for (int i = threadIdx.x; i < cnt; i += kLargeThreads)
     tb[i] = conj_of(to_elem<T>(braw[(long long)(i / nl) * st + i % nl]));
   __syncthreads();
+  // res[b, q] = sum over the tile's fibers f of bra[f, b] ket[f, q]: a small
+  // GEMM.  A thread accumulates a 4 x 4 block (b0.., q0..) over the fibers
+  // f = s, s + NS, ... of its slice s (8 loads per 16 multiply-adds; adjacent
+  // threads take adjacent fibers, so the loads do not conflict); the slices are
+  // then added in slice order (deterministic).  Blocks are taken `groups` at a
+  // time when there are more than the threads' share.
   const int P = chi * chi;
   const int nf = nj * nl;  // fibers of the tile: (j, l)
+  const int nbb = (chi + 3) / 4, nblk = nbb * nbb;
+  const int NS = nblk >= kLargeThreads ? 1 : kLargeThreads / nblk;  // fiber slices
+  const int groups = kLargeThreads / NS;                           // blocks per pass
   T* out = partial + (long long)w * vstride + (long long)t * P;
-  if (P >= kLargeThreads) {
-    for (int o = threadIdx.x; o < P; o += kLargeThreads) {
-      const int b = o % chi, q = o / chi;
-      T acc = T(0);
-      for (int f = 0; f < nf; ++f) {
+  for (int bk0 = 0; bk0 < nblk; bk0 += groups) {
+    const int sl = threadIdx.x % NS, gb = threadIdx.x / NS, bk = bk0 + gb;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc[i][k] = T(0);
+    if (gb < groups && bk < nblk) {
+      const int b0 = (bk % nbb) * 4, q0 = (bk / nbb) * 4;
+      for (int f = sl; f < nf; f += NS) {
         const int j = f / nl, l = f % nl;
         const long long row = (long long)j * chi * nl + l;
-        acc = mac(tb[row + b * nl], tt[row + q * nl], acc);
+        T yb[4], xq[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          yb[i] = b0 + i < chi ? tb[row + (long long)(b0 + i) * nl] : T(0);
+          xq[i] = q0 + i < chi ? tt[row + (long long)(q0 + i) * nl] : T(0);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int k = 0; k < 4; ++k) acc[i][k] = mac(yb[i], xq[k], acc[i][k]);
       }
-      out[o] = settle(acc);
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) red[((long long)sl * groups + gb) * 16 + i * 4 + k] = settle(acc[i][k]);
     }
-  } else {
-    // G groups of P threads, group gi sums the fibers f = gi, gi + G, ...
-    const int G = kLargeThreads / P;
-    const int gi = threadIdx.x / P, o = threadIdx.x % P;
-    T acc = T(0);
-    if (gi < G) {
-      const int b = o % chi, q = o / chi;
-      for (int f = gi; f < nf; f += G) {
-        const int j = f / nl, l = f % nl;
-        const long long row = (long long)j * chi * nl + l;
-        acc = mac(tb[row + b * nl], tt[row + q * nl], acc);
-      }
-    }
-    red[threadIdx.x] = settle(acc);
     __syncthreads();
-    if (threadIdx.x < P) {
-      T s = red[threadIdx.x];
-      for (int k = 1; k < G; ++k) s += red[threadIdx.x + k * P];
-      out[threadIdx.x] = s;
+    for (int o = threadIdx.x; o < groups * 16; o += kLargeThreads) {
+      const int g = o / 16, e = o % 16, bkk = bk0 + g;
+      if (bkk >= nblk) continue;
+      const int b = (bkk % nbb) * 4 + e / 4, q = (bkk / nbb) * 4 + e % 4;
+      if (b >= chi || q >= chi) continue;
+      T sum = T(0);
+      for (int s2 = 0; s2 < NS; ++s2) sum += red[((long long)s2 * groups + g) * 16 + e];
+      out[b + chi * q] = sum;
     }
+    __syncthreads();
   }
 }
 
@@ -269,7 +301,7 @@ void launch_large_op(const LargeArgs<S>& a, int nverts, int max_tiles, int max_c
     GBTN_CUDA(cudaFuncSetAttribute(large_absorb_kernel<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     large_absorb_kernel<T, S><<<grid, kLargeThreads, sm, s>>>(a, scratch, op.src, op.dst, op.leg, converged);
   } else {
-    const size_t sm = sizeof(T) * (2 * (size_t)kTile + kLargeThreads);
+    const size_t sm = sizeof(T) * (2 * (size_t)kTile + kCloseRed);
     GBTN_CUDA(cudaFuncSetAttribute(large_close_kernel<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     large_close_kernel<T, S><<<grid, kLargeThreads, sm, s>>>(a, scratch, op.src, op.leg, partial, vstride, converged);
     GBTN_CUDA(cudaGetLastError());
@@ -285,7 +317,7 @@ void launch_large_rdm(const LargeArgs<S>& a, int nverts, int max_tiles, int src,
   if (nverts == 0) return;
   T* scratch = static_cast<T*>(scratch_v);
   T* partial = static_cast<T*>(partial_v);
-  const size_t sm = sizeof(T) * (2 * (size_t)kTile + kLargeThreads);
+  const size_t sm = sizeof(T) * (2 * (size_t)kTile + kCloseRed);
   GBTN_CUDA(cudaFuncSetAttribute(large_close_kernel<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   large_close_kernel<T, S><<<dim3(max_tiles, nverts), kLargeThreads, sm, s>>>(a, scratch, src, -1, partial, vstride,
                                                                                nullptr);
