@@ -50,6 +50,23 @@ def flops_per_sweep(L=L, chi=CHI, d=D):
     return tot
 
 
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # SMs x FP32 lanes x 2 flops x max SM clock
+
+
+def executed_flops_per_sweep(L=L, chi=CHI, d=D):
+    """Flops the SIMT vertex kernel executes in one sweep: 12 contraction steps
+    of 2 n chi at a degree-4 vertex (the shared-prefix schedule; the reference's
+    per-message count is 16), the reference's count at the lower-degree
+    boundary vertices (an upper bound there, 1 % of the total)."""
+    tot = 0
+    for j in range(L):
+        for i in range(L):
+            k = (i > 0) + (i < L - 1) + (j > 0) + (j < L - 1)
+            n = d * chi ** k
+            tot += (12 if k == 4 else k * k) * 2 * n * chi
+    return tot
+
+
 def bytes_per_sweep(elt, L=L, chi=CHI, d=D):
     """Compulsory traffic of one Jacobi sweep: every site tensor read once,
     every message read once and written once."""
@@ -773,6 +790,15 @@ def run_ours(args):
             "kernel_shares_of_mixed_solve": shares,
             "paths_ms_per_sweep": {"bf16_tensor_core": ms_bf16, "f32_simt": ms_f32, "df32_simt": ms_df32,
                                    "f64_simt": ms_f64},
+            # the SIMT kernels that carry the solve, against the nominal FP32 pipe
+            # rate (no measured FP32 peak exists for these GPUs); df32 runs ~12
+            # FP32 instructions per multiply-add
+            "simt_rates": {"executed_gflop_per_sweep": executed_flops_per_sweep() * BATCH / 1e9,
+                           "fp32_tflops": executed_flops_per_sweep() * BATCH / (ms_f32 * 1e-3) / 1e12,
+                           "fp32_frac_of_nominal": executed_flops_per_sweep() * BATCH / (ms_f32 * 1e-3) / 1e12
+                           / FP32_NOMINAL_TFLOPS,
+                           "df32_tflops": executed_flops_per_sweep() * BATCH / (ms_df32 * 1e-3) / 1e12,
+                           "fp32_nominal_tflops": FP32_NOMINAL_TFLOPS},
             "sequential_schedule": {"ms_per_sweep": seq_ms,
                                     "msg_updates_per_s": {p: msgs_step / (ms * 1e-3) for p, ms in seq_ms.items()},
                                     "time_to_solution": seq_tts},
