@@ -433,6 +433,19 @@ int gbtn_qn_bp_run(gbtn_qn_plan* plan, int32_t maxiter, double tol, int32_t* ite
  * The mean diff is over the sequence positions. */
 int gbtn_qn_bp_run_sequential(gbtn_qn_plan* plan, const int32_t* edge_sequence, int32_t edge_sequence_len,
                               int32_t maxiter, double tol, int32_t* iters, double* mean_diff);
+/* Replaces: update(bpc; maxiter, tol, ...) on a block-sparse network, with
+ * the precision and schedule choices of gbtn_bp_run: PARALLEL or SEQUENTIAL
+ * (edge_sequence as above); F64, F32 (FP32 blocks and messages, FP64 norms
+ * and diffs), DF32 (double-FP32 arithmetic on the FP64 blocks), or MIXED
+ * (FP32 sweeps to tol_f32 or their noise floor, then DF32 -- or FP64 with
+ * refine = GBTN_REFINE_F64 -- sweeps to tol, optional FP64 confirm_f64
+ * sweeps).  BF16 and COLORED are refused (GBTN_ERR_UNSUPPORTED /
+ * GBTN_ERR_INVALID): block-sparse vertices have no tensor-core path.
+ * iters: sweeps of the last phase. */
+int gbtn_qn_bp_run_ex(gbtn_qn_plan* plan, const gbtn_bp_opts* opts, int32_t* iters, double* mean_diff);
+/* Sweeps each phase of the last QN run took: [BF16 (always 0), FP32,
+ * refinement, FP64]. */
+int gbtn_qn_phase_sweeps(const gbtn_qn_plan* plan, int32_t* sweeps);
 /* Replaces: the one-site environments of expect (expect.jl:5-19): dense
  * rho_v[s', s] (d x d, block-diagonal in the site sectors) per vertex. */
 int gbtn_qn_vertex_rdms(gbtn_qn_plan* plan, double* out);

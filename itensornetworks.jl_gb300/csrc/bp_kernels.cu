@@ -194,28 +194,36 @@ __device__ __forceinline__ int chain_absorb(const TeamSmem<T>& S, int skip_leg, 
 // mode 0: every outgoing share (the shared-prefix schedule); mode 1: the
 // block's share of rho_v (all legs absorbed, CLOSE on the site index).
 // ---------------------------------------------------------------------------
-template <int TEAM>
+// T is the arithmetic, S the storage of blocks, messages and shares (S = T,
+// or double under double-FP32 arithmetic).
+template <typename T, int TEAM, typename S = T>
 __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
     qn_block_kernel(const int* __restrict__ work, int nwork, const VDesc* __restrict__ bd,
-                    const double* __restrict__ blocks, const double* __restrict__ msg_in,
-                    const long long* __restrict__ sec_off, double* __restrict__ partial,
+                    const S* __restrict__ blocks, const S* __restrict__ msg_in,
+                    const long long* __restrict__ sec_off, S* __restrict__ partial,
                     const long long* __restrict__ part_off, int mode, int ncap, int nbuf) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPB = TEAM == 32 ? 4 : 1;
   const int team = threadIdx.x / TEAM, tid = threadIdx.x % TEAM;
-  const size_t tb = team_smem_bytes<double>(padded_len(ncap), nbuf, false, TEAM);
-  TeamSmem<double> Sm = carve<double>(smem_raw + team * tb, padded_len(ncap), nbuf, false, TEAM);
+  const size_t tb = team_smem_bytes<T>(padded_len(ncap), nbuf, false, TEAM);
+  TeamSmem<T> Sm = carve<T>(smem_raw + team * tb, padded_len(ncap), nbuf, false, TEAM);
+  auto store = [](T x) -> S {
+    if constexpr (std::is_same<T, df32>::value)
+      return df_to_double(x);
+    else
+      return x;
+  };
   for (int w = blockIdx.x * TPB + team; w < nwork; w += gridDim.x * TPB) {
     load_desc<TEAM>(Sm.desc, bd + work[w], tid);
     tsync<TEAM>();
     const VDesc& d = *Sm.desc;
-    load_vertex<double, TEAM, double, true>(Sm, blocks, nullptr, msg_in, sec_off, -1, tid);
+    load_vertex<T, TEAM, S, true>(Sm, blocks, nullptr, msg_in, sec_off, -1, tid);
     tsync<TEAM>();
     if (mode == 1) {
-      const int cur = chain_absorb<double, TEAM>(Sm, -1, tid);
-      close_any<double, TEAM, true>(d.d, Sm.buf[cur], Sm.bra, d.n, 1, 1, 0, 0, Sm.red, Sm.res, tid);
-      double* out = partial + part_off[d.net];
-      for (int i = tid; i < d.d * d.d; i += TEAM) out[i] = Sm.res[i];
+      const int cur = chain_absorb<T, TEAM>(Sm, -1, tid);
+      close_any<T, TEAM, true>(d.d, Sm.buf[cur], Sm.bra, d.n, 1, 1, 0, 0, Sm.red, Sm.res, tid);
+      S* out = partial + part_off[d.net];
+      for (int i = tid; i < d.d * d.d; i += TEAM) out[i] = store(Sm.res[i]);
       tsync<TEAM>();
       continue;
     }
@@ -226,38 +234,56 @@ __global__ void __launch_bounds__(TEAM == 32 ? 128 : 256)
       const int leg = op.leg;
       const int chi = d.chi[leg], st = d.st[leg];
       if (op.type == 0) {
-        absorb_any<double, true>(chi, Sm.buf[op.src], Sm.buf[op.dst], d.n, st, Sm.msg + leg * 64, tid, TEAM);
+        absorb_any<T, true>(chi, Sm.buf[op.src], Sm.buf[op.dst], d.n, st, Sm.msg + leg * 64, tid, TEAM);
         tsync<TEAM>();
       } else {
-        close_any<double, TEAM, true>(chi, Sm.buf[op.src], Sm.bra, d.n, st, 1, 0, 0, Sm.red, Sm.res, tid);
-        double* out = partial + part_off[d.out_de[leg]];
-        for (int j = tid; j < chi * chi; j += TEAM) out[j] = Sm.res[j];
+        close_any<T, TEAM, true>(chi, Sm.buf[op.src], Sm.bra, d.n, st, 1, 0, 0, Sm.red, Sm.res, tid);
+        S* out = partial + part_off[d.out_de[leg]];
+        for (int j = tid; j < chi * chi; j += TEAM) out[j] = store(Sm.res[j]);
         tsync<TEAM>();
       }
     }
   }
 }
 
-void launch_qn_blocks(const WorkList& wl_all, const VDesc* bd, const double* blocks, const double* msg_in,
-                      const long long* sec_off, double* partial, const long long* part_off, int mode,
-                      cudaStream_t s) {
+template <typename T, typename S>
+void launch_qn_blocks_t(const WorkList& wl_all, const VDesc* bd, const S* blocks, const S* msg_in,
+                        const long long* sec_off, S* partial, const long long* part_off, int mode, cudaStream_t s) {
   for (int c = 0; c < wl_all.nsubs(); ++c) {
     const WorkList wl = wl_all.sub(c);
     if (wl.count == 0) continue;
     const int nbuf = wl.maxdeg <= 4 ? 3 : kNumBufs;
     if (wl.team == 32) {
-      const size_t sm = 4 * team_smem_bytes<double>(padded_len(wl.ncap), nbuf, false, 32);
-      GBTN_CUDA(cudaFuncSetAttribute(qn_block_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      qn_block_kernel<32><<<(wl.count + 3) / 4, 128, sm, s>>>(wl.d_vertices, wl.count, bd, blocks, msg_in, sec_off,
-                                                              partial, part_off, mode, wl.ncap, nbuf);
+      const size_t sm = 4 * team_smem_bytes<T>(padded_len(wl.ncap), nbuf, false, 32);
+      auto kern = qn_block_kernel<T, 32, S>;
+      GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      kern<<<(wl.count + 3) / 4, 128, sm, s>>>(wl.d_vertices, wl.count, bd, blocks, msg_in, sec_off, partial, part_off,
+                                               mode, wl.ncap, nbuf);
     } else {
-      const size_t sm = team_smem_bytes<double>(padded_len(wl.ncap), nbuf, false, 256);
-      GBTN_CUDA(cudaFuncSetAttribute(qn_block_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      qn_block_kernel<256><<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, bd, blocks, msg_in, sec_off, partial,
-                                                     part_off, mode, wl.ncap, nbuf);
+      const size_t sm = team_smem_bytes<T>(padded_len(wl.ncap), nbuf, false, 256);
+      auto kern = qn_block_kernel<T, 256, S>;
+      GBTN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      kern<<<wl.count, 256, sm, s>>>(wl.d_vertices, wl.count, bd, blocks, msg_in, sec_off, partial, part_off, mode,
+                                     wl.ncap, nbuf);
     }
     GBTN_CUDA(cudaGetLastError());
   }
+}
+
+void launch_qn_blocks(const WorkList& wl_all, const VDesc* bd, const double* blocks, const double* msg_in,
+                      const long long* sec_off, double* partial, const long long* part_off, int mode,
+                      cudaStream_t s) {
+  launch_qn_blocks_t<double, double>(wl_all, bd, blocks, msg_in, sec_off, partial, part_off, mode, s);
+}
+
+void launch_qn_blocks_f32(const WorkList& wl_all, const VDesc* bd, const float* blocks, const float* msg_in,
+                          const long long* sec_off, float* partial, const long long* part_off, cudaStream_t s) {
+  launch_qn_blocks_t<float, float>(wl_all, bd, blocks, msg_in, sec_off, partial, part_off, 0, s);
+}
+
+void launch_qn_blocks_df32(const WorkList& wl_all, const VDesc* bd, const double* blocks, const double* msg_in,
+                           const long long* sec_off, double* partial, const long long* part_off, cudaStream_t s) {
+  launch_qn_blocks_t<df32, double>(wl_all, bd, blocks, msg_in, sec_off, partial, part_off, 0, s);
 }
 
 // One wave of the sequential schedule: every job (vertex, leg, sequence

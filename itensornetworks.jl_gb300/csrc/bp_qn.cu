@@ -36,6 +36,7 @@ namespace {
 
 constexpr int kBlockFields = 2 + kMaxDeg;  // vertex, site sector, leg sectors
 constexpr int kQnSmallN = 1024;            // blocks up to this size run one per warp
+constexpr int kQnStallSweeps = 3;          // noise-floor test of the FP32 phase, as for dense plans
 
 template <typename T>
 struct QBuf {
@@ -67,11 +68,14 @@ struct QBuf {
 // select the messages of one wave of the sequential schedule, which finalises
 // them in place (msg_old == msg_out: each entry is read before it is written,
 // by the same lane) and records each diff at its sequence position.
+// S is the storage of shares and messages (FP64, or FP32 for the FP32 sweeps):
+// the sums, norms and diff are formed in FP64 from the stored values.
+template <typename S>
 __global__ void qn_finalize_kernel(int ndir, const int* __restrict__ vm_ptr, const int* __restrict__ vm_dim,
                                    const long long* __restrict__ sec_off, const int* __restrict__ slot_ptr,
                                    const int* __restrict__ slots, const long long* __restrict__ part_off,
-                                   const double* __restrict__ partial, const double* msg_old, double* msg_out,
-                                   double* diffs, int normalize, int want_diff, const int* __restrict__ de_list,
+                                   const S* __restrict__ partial, const S* msg_old, S* msg_out, double* diffs,
+                                   int normalize, int want_diff, const int* __restrict__ de_list,
                                    const int* __restrict__ pos_list) {
   const int job = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -83,13 +87,14 @@ __global__ void qn_finalize_kernel(int ndir, const int* __restrict__ vm_ptr, con
     const int c2 = vm_dim[vm] * vm_dim[vm];
     const long long off = sec_off[vm];
     for (int i = lane; i < c2; i += 32) {
-      double s = 0.0;
-      for (int q = slot_ptr[vm]; q < slot_ptr[vm + 1]; ++q) s += partial[part_off[slots[q]] + i];
-      const double o = msg_old[off + i];
+      double acc = 0.0;
+      for (int q = slot_ptr[vm]; q < slot_ptr[vm + 1]; ++q) acc += (double)partial[part_off[slots[q]] + i];
+      const S sv = (S)acc;
+      const double s = (double)sv, o = (double)msg_old[off + i];
       nr2 = fma(s, s, nr2);
       dot = fma(o, s, dot);
       nb = fma(o, o, nb);
-      msg_out[off + i] = s;
+      msg_out[off + i] = sv;
     }
   }
   nr2 = warp_sum(nr2);
@@ -100,7 +105,7 @@ __global__ void qn_finalize_kernel(int ndir, const int* __restrict__ vm_ptr, con
   for (int vm = vm_ptr[de]; vm < vm_ptr[de + 1]; ++vm) {
     const int c2 = vm_dim[vm] * vm_dim[vm];
     const long long off = sec_off[vm];
-    for (int i = lane; i < c2; i += 32) msg_out[off + i] *= sc;
+    for (int i = lane; i < c2; i += 32) msg_out[off + i] = (S)((double)msg_out[off + i] * sc);
   }
   if (want_diff && lane == 0) diffs[pos] = 1.0 - (dot * dot) / (nr2 * nb);
 }
@@ -176,6 +181,13 @@ struct gbtn_qn_plan {
   std::vector<WorkList> wave_small, wave_large;
   std::vector<int> wave_job_ptr;
   QBuf<int> d_wave_blocks, d_wave_de, d_wave_pos, d_seq_ptr, d_seq_pos;
+  // FP32 copies for the FP32 sweeps (made on first use, blocks refreshed per
+  // run), the noise-floor state of the reduced-precision phases, and the
+  // sweeps each phase of the last run took (0 BF16, 1 FP32, 2 refinement, 3 FP64)
+  QBuf<float> d_blocks32, d_msg32[2], d_partial32;
+  QBuf<double> d_best;
+  QBuf<int> d_since;
+  int phase_sweeps[4] = {0, 0, 0, 0};
 };
 
 namespace {
@@ -336,6 +348,105 @@ void build_qn_waves(gbtn_qn_plan* P, const int32_t* seq, int len) {
   P->seq_cached = key;
 }
 
+// One sweep: the block kernel (blocks(worklist, messages in, shares)) on every
+// block, then the finalize.  Parallel: all messages from msg_in into msg_out.
+// Sequential: wave by wave, each wave finalising its messages in place in
+// msg_in (msg_out unused).
+template <typename S, typename Blocks>
+void qn_sweep(gbtn_qn_plan* P, const Blocks& blocks, S* partial, S* msg_in, S* msg_out, bool seq, int normalize,
+              bool want_diff, cudaStream_t s) {
+  if (!seq) {
+    for (const WorkList* wl : {&P->small, &P->large})
+      if (wl->count) blocks(*wl, msg_in, partial);
+    const int ndir = 2 * P->ne;
+    qn_finalize_kernel<S><<<(ndir + 7) / 8, 256, 0, s>>>(ndir, P->d_vm_ptr.p, P->d_vm_dim.p, P->d_sec_off.p,
+                                                         P->d_slot_ptr.p, P->d_slots.p, P->d_part_off.p, partial,
+                                                         msg_in, msg_out, P->d_diffs.p, normalize, want_diff ? 1 : 0,
+                                                         nullptr, nullptr);
+    GBTN_CUDA(cudaGetLastError());
+    return;
+  }
+  for (size_t l = 0; l + 1 < P->wave_job_ptr.size(); ++l) {
+    for (const WorkList* wl : {&P->wave_small[l], &P->wave_large[l]})
+      if (wl->count) blocks(*wl, msg_in, partial);
+    const int j0 = P->wave_job_ptr[l], nj = P->wave_job_ptr[l + 1] - j0;
+    qn_finalize_kernel<S><<<(nj + 7) / 8, 256, 0, s>>>(nj, P->d_vm_ptr.p, P->d_vm_dim.p, P->d_sec_off.p,
+                                                       P->d_slot_ptr.p, P->d_slots.p, P->d_part_off.p, partial, msg_in,
+                                                       msg_in, P->d_diffs.p, normalize, want_diff ? 1 : 0,
+                                                       P->d_wave_de.p + j0, P->d_wave_pos.p + j0);
+    GBTN_CUDA(cudaGetLastError());
+  }
+}
+
+// Sweeps of one arithmetic until the mean diff is <= tol (tol < 0: no test),
+// the noise floor (stall > 0: the mean diff has not dropped below 0.9x its
+// best for `stall` sweeps) or maxiter sweeps; msg[cur] holds the messages and
+// cur follows the parallel sweeps' double buffer.  Returns the sweeps run; md
+// gets the last mean diff (NAN without a test).
+template <typename S, typename Blocks>
+int qn_phase(gbtn_qn_plan* P, const Blocks& blocks, S* partial, S* const msg[2], int& cur, bool seq, int maxiter,
+             double tol, int normalize, int stall, double* md) {
+  cudaStream_t s = ctx_stream(P->ctx);
+  const bool test = tol >= 0.0 || stall > 0;
+  *md = NAN;
+  GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int), s));
+  GBTN_CUDA(cudaMemsetAsync(P->d_iters.p, 0, sizeof(int), s));
+  for (int it = 1; it <= maxiter; ++it) {
+    qn_sweep<S>(P, blocks, partial, msg[cur], msg[cur ^ 1], seq, normalize, test, s);
+    if (!seq) cur ^= 1;
+    if (test) {
+      launch_reduce_diffs(1, seq ? P->d_seq_ptr.p : P->d_net_de_ptr.p, seq ? P->d_seq_pos.p : P->d_net_de.p,
+                          P->d_diffs.p, tol, P->d_conv.p, P->d_iters.p, P->d_mean.p, s, stall, P->d_best.p,
+                          P->d_since.p);
+      int conv = 0;
+      GBTN_CUDA(cudaMemcpyAsync(&conv, P->d_conv.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      GBTN_CUDA(cudaMemcpyAsync(md, P->d_mean.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+      GBTN_CUDA(cudaStreamSynchronize(s));
+      if (conv) return it;
+    }
+  }
+  return maxiter;
+}
+
+auto f64_blocks(gbtn_qn_plan* P) {
+  return [P](const WorkList& wl, const double* m, double* part) {
+    launch_qn_blocks(wl, P->d_bd.p, P->d_blocks.p, m, P->d_sec_off.p, part, P->d_part_off.p, 0, ctx_stream(P->ctx));
+  };
+}
+
+auto df32_blocks(gbtn_qn_plan* P) {
+  return [P](const WorkList& wl, const double* m, double* part) {
+    launch_qn_blocks_df32(wl, P->d_bd.p, P->d_blocks.p, m, P->d_sec_off.p, part, P->d_part_off.p,
+                          ctx_stream(P->ctx));
+  };
+}
+
+auto f32_blocks(gbtn_qn_plan* P) {
+  return [P](const WorkList& wl, const float* m, float* part) {
+    launch_qn_blocks_f32(wl, P->d_bd.p, P->d_blocks32.p, m, P->d_sec_off.p, part, P->d_part_off.p,
+                         ctx_stream(P->ctx));
+  };
+}
+
+// FP32 sweeps from the FP64 messages and back (the blocks rounded to FP32
+// afresh, so later changes of the FP64 blocks are seen).
+int qn_f32_phase(gbtn_qn_plan* P, bool seq, int maxiter, double tol, int normalize, int stall, double* md) {
+  cudaStream_t s = ctx_stream(P->ctx);
+  if (!P->d_msg32[0].p) {
+    P->d_blocks32.alloc(std::max<long long>(P->n_blk, 1));
+    P->d_msg32[0].alloc(std::max<long long>(P->n_msg, 1));
+    P->d_msg32[1].alloc(std::max<long long>(P->n_msg, 1));
+    P->d_partial32.alloc(std::max<long long>(P->n_part, 1));
+  }
+  launch_convert_f64_to_f32(P->d_blocks.p, P->d_blocks32.p, P->n_blk, s);
+  launch_convert_f64_to_f32(P->d_msg[P->cur].p, P->d_msg32[0].p, P->n_msg, s);
+  float* const m32[2] = {P->d_msg32[0].p, P->d_msg32[1].p};
+  int c32 = 0;
+  const int n = qn_phase<float>(P, f32_blocks(P), P->d_partial32.p, m32, c32, seq, maxiter, tol, normalize, stall, md);
+  launch_convert_f32_to_f64(P->d_msg32[c32].p, P->d_msg[P->cur].p, P->n_msg, s);
+  return n;
+}
+
 }  // namespace
 
 extern "C" {
@@ -347,40 +458,19 @@ int gbtn_qn_bp_run_sequential(gbtn_qn_plan* P, const int32_t* edge_sequence, int
   require(P && (edge_sequence || len == 0), "NULL argument");
   require(maxiter >= 1, "You need to specify a number of iterations for BP!");
   require(len >= 0, "edge_sequence_len must be >= 0");
-  cudaStream_t s = ctx_stream(P->ctx);
-  const bool want_diff = tol >= 0.0;
-  int it = 0;
+  for (int& n : P->phase_sweeps) n = 0;
   double md = NAN;
-  if (len > 0) build_qn_waves(P, edge_sequence, len);
-  GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int), s));
-  GBTN_CUDA(cudaMemsetAsync(P->d_iters.p, 0, sizeof(int), s));
-  double* m = P->d_msg[P->cur].p;
-  for (it = 1; it <= maxiter; ++it) {
-    if (len == 0) break;
-    for (size_t l = 0; l + 1 < P->wave_job_ptr.size(); ++l) {
-      for (const WorkList* wl : {&P->wave_small[l], &P->wave_large[l]})
-        if (wl->count) launch_qn_blocks(*wl, P->d_bd.p, P->d_blocks.p, m, P->d_sec_off.p, P->d_partial.p,
-                                        P->d_part_off.p, 0, s);
-      const int j0 = P->wave_job_ptr[l], nj = P->wave_job_ptr[l + 1] - j0;
-      qn_finalize_kernel<<<(nj + 7) / 8, 256, 0, s>>>(nj, P->d_vm_ptr.p, P->d_vm_dim.p, P->d_sec_off.p,
-                                                      P->d_slot_ptr.p, P->d_slots.p, P->d_part_off.p, P->d_partial.p,
-                                                      m, m, P->d_diffs.p, 1, want_diff ? 1 : 0,
-                                                      P->d_wave_de.p + j0, P->d_wave_pos.p + j0);
-      GBTN_CUDA(cudaGetLastError());
-    }
-    if (want_diff) {
-      launch_reduce_diffs(1, P->d_seq_ptr.p, P->d_seq_pos.p, P->d_diffs.p, tol, P->d_conv.p, P->d_iters.p, P->d_mean.p,
-                          s);
-      int conv = 0;
-      GBTN_CUDA(cudaMemcpyAsync(&conv, P->d_conv.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-      GBTN_CUDA(cudaMemcpyAsync(&md, P->d_mean.p, sizeof(double), cudaMemcpyDeviceToHost, s));
-      GBTN_CUDA(cudaStreamSynchronize(s));
-      if (conv) break;
-    }
+  int it = maxiter;
+  if (len > 0) {
+    build_qn_waves(P, edge_sequence, len);
+    double* const m[2] = {P->d_msg[P->cur].p, P->d_msg[P->cur].p};
+    int cur = 0;
+    it = qn_phase<double>(P, f64_blocks(P), P->d_partial.p, m, cur, true, maxiter, tol, 1, 0, &md);
+    P->phase_sweeps[3] = it;
   }
-  GBTN_CUDA(cudaStreamSynchronize(s));
-  if (iters) *iters = len == 0 ? maxiter : std::min(it, (int)maxiter);
-  if (mean_diff) *mean_diff = want_diff && len > 0 ? md : NAN;
+  GBTN_CUDA(cudaStreamSynchronize(ctx_stream(P->ctx)));
+  if (iters) *iters = it;
+  if (mean_diff) *mean_diff = tol >= 0.0 && len > 0 ? md : NAN;
   QN_CATCH(C)
 }
 
@@ -605,6 +695,8 @@ int gbtn_qn_plan_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, const gbtn_qn_d
   P->d_conv.alloc(1);
   P->d_iters.alloc(1);
   P->d_nconv.alloc(1);
+  P->d_best.alloc(1);
+  P->d_since.alloc(1);
   std::vector<int> all_de(std::max(2 * ne, 1)), all_v(nv), all_e(std::max(ne, 1));
   std::iota(all_de.begin(), all_de.end(), 0);
   std::iota(all_v.begin(), all_v.end(), 0);
@@ -684,38 +776,81 @@ int gbtn_qn_bp_run(gbtn_qn_plan* P, int32_t maxiter, double tol, int32_t* iters,
   QN_TRY
   require(P, "NULL plan");
   require(maxiter >= 1, "You need to specify a number of iterations for BP!");
-  cudaStream_t s = ctx_stream(P->ctx);
-  const bool want_diff = tol >= 0.0;
-  int it = 0;
+  for (int& n : P->phase_sweeps) n = 0;
   double md = NAN;
-  GBTN_CUDA(cudaMemsetAsync(P->d_conv.p, 0, sizeof(int), s));
-  GBTN_CUDA(cudaMemsetAsync(P->d_iters.p, 0, sizeof(int), s));
-  for (it = 1; it <= maxiter; ++it) {
-    if (P->ne == 0) break;
-    for (const WorkList* wl : {&P->small, &P->large})
-      launch_qn_blocks(*wl, P->d_bd.p, P->d_blocks.p, P->d_msg[P->cur].p, P->d_sec_off.p, P->d_partial.p,
-                       P->d_part_off.p, 0, s);
-    const int ndir = 2 * P->ne;
-    qn_finalize_kernel<<<(ndir + 7) / 8, 256, 0, s>>>(ndir, P->d_vm_ptr.p, P->d_vm_dim.p, P->d_sec_off.p,
-                                                      P->d_slot_ptr.p, P->d_slots.p, P->d_part_off.p,
-                                                      P->d_partial.p, P->d_msg[P->cur].p, P->d_msg[P->cur ^ 1].p,
-                                                      P->d_diffs.p, 1, want_diff ? 1 : 0, nullptr, nullptr);
-    GBTN_CUDA(cudaGetLastError());
-    P->cur ^= 1;
-    if (want_diff) {
-      launch_reduce_diffs(1, P->d_net_de_ptr.p, P->d_net_de.p, P->d_diffs.p, tol, P->d_conv.p, P->d_iters.p,
-                          P->d_mean.p, s);
-      int conv = 0;
-      GBTN_CUDA(cudaMemcpyAsync(&conv, P->d_conv.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-      GBTN_CUDA(cudaMemcpyAsync(&md, P->d_mean.p, sizeof(double), cudaMemcpyDeviceToHost, s));
-      GBTN_CUDA(cudaStreamSynchronize(s));
-      if (conv) break;
+  int it = 1;
+  if (P->ne > 0) {
+    double* const m[2] = {P->d_msg[0].p, P->d_msg[1].p};
+    it = qn_phase<double>(P, f64_blocks(P), P->d_partial.p, m, P->cur, false, maxiter, tol, 1, 0, &md);
+    P->phase_sweeps[3] = it;
+  }
+  GBTN_CUDA(cudaStreamSynchronize(ctx_stream(P->ctx)));
+  if (iters) *iters = it;
+  if (mean_diff) *mean_diff = tol >= 0.0 ? md : NAN;
+  QN_CATCH(C)
+}
+
+int gbtn_qn_bp_run_ex(gbtn_qn_plan* P, const gbtn_bp_opts* o, int32_t* iters, double* mean_diff) {
+  gbtn_ctx* C = P ? P->ctx : nullptr;
+  QN_TRY
+  require(P && o, "NULL argument");
+  require(o->maxiter >= 1, "You need to specify a number of iterations for BP!");
+  require(o->schedule == GBTN_SCHED_PARALLEL || o->schedule == GBTN_SCHED_SEQUENTIAL,
+          "block-sparse plans run the parallel or the sequential schedule");
+  require(o->precision >= 0 && o->precision <= 4, "unknown precision");
+  require(o->refine == GBTN_REFINE_DF32 || o->refine == GBTN_REFINE_F64, "unknown refinement arithmetic");
+  require(o->confirm_f64 >= 0, "confirm_f64 must be >= 0");
+  if (o->precision == GBTN_BF16) throw Unsupported("block-sparse plans have no tensor-core (BF16) path");
+  for (int& n : P->phase_sweeps) n = 0;
+  const bool seq = o->schedule == GBTN_SCHED_SEQUENTIAL;
+  if (seq) {
+    require(o->edge_sequence && o->edge_sequence_len > 0, "SEQUENTIAL needs an edge sequence");
+    build_qn_waves(P, o->edge_sequence, o->edge_sequence_len);
+  }
+  double md = NAN;
+  int last = o->maxiter;
+  if (P->ne > 0) {
+    double* const m[2] = {seq ? P->d_msg[P->cur].p : P->d_msg[0].p, seq ? P->d_msg[P->cur].p : P->d_msg[1].p};
+    int seq_cur = 0;
+    int& cur = seq ? seq_cur : P->cur;
+    auto fp64 = [&](int maxit, int slot) {
+      last = qn_phase<double>(P, f64_blocks(P), P->d_partial.p, m, cur, seq, maxit, o->tol, o->normalize, 0, &md);
+      P->phase_sweeps[slot] = last;
+    };
+    auto df32 = [&](int maxit) {
+      last = qn_phase<double>(P, df32_blocks(P), P->d_partial.p, m, cur, seq, maxit, o->tol, o->normalize, 0, &md);
+      P->phase_sweeps[2] = last;
+    };
+    if (o->precision == GBTN_F64) {
+      fp64(o->maxiter, 3);
+    } else if (o->precision == GBTN_DF32) {
+      df32(o->maxiter);
+    } else if (o->precision == GBTN_F32) {
+      last = qn_f32_phase(P, seq, o->maxiter, o->tol, o->normalize, 0, &md);
+      P->phase_sweeps[1] = last;
+    } else {  // MIXED: FP32 to its tolerance or noise floor, then DF32 (or FP64) to tol
+      const double tol32 = o->tol_f32 > 0 ? o->tol_f32 : 1e-13;
+      const int it32 = o->maxiter_f32 > 0 ? o->maxiter_f32 : o->maxiter;
+      P->phase_sweeps[1] = qn_f32_phase(P, seq, it32, tol32, o->normalize, kQnStallSweeps, &md);
+      const int nref = o->refine_f64 > 0 ? std::min(o->refine_f64, o->maxiter) : o->maxiter;
+      if (o->refine == GBTN_REFINE_F64) {
+        fp64(nref, 2);
+      } else {
+        df32(nref);
+        if (o->confirm_f64 > 0) fp64(std::min(o->confirm_f64, o->maxiter), 3);
+      }
     }
   }
-  GBTN_CUDA(cudaStreamSynchronize(s));
-  if (iters) *iters = std::min(it, (int)maxiter);
-  if (mean_diff) *mean_diff = want_diff ? md : NAN;
+  GBTN_CUDA(cudaStreamSynchronize(ctx_stream(P->ctx)));
+  if (iters) *iters = last;
+  if (mean_diff) *mean_diff = o->tol >= 0.0 && P->ne > 0 ? md : NAN;
   QN_CATCH(C)
+}
+
+int gbtn_qn_phase_sweeps(const gbtn_qn_plan* P, int32_t* sweeps) {
+  if (!P || !sweeps) return GBTN_ERR_INVALID;
+  for (int k = 0; k < 4; ++k) sweeps[k] = P->phase_sweeps[k];
+  return GBTN_OK;
 }
 
 int gbtn_qn_vertex_rdms(gbtn_qn_plan* P, double* out) {

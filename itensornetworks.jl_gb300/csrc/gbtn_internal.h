@@ -229,6 +229,12 @@ size_t large_elem_size(int arith);
 void launch_qn_blocks(const WorkList& wl, const VDesc* bd, const double* blocks, const double* msg_in,
                       const long long* sec_off, double* partial, const long long* part_off, int mode,
                       cudaStream_t s);
+// The same shares in FP32 (FP32 blocks, messages and shares) or in
+// double-FP32 arithmetic on FP64 storage (mode 0: message shares).
+void launch_qn_blocks_f32(const WorkList& wl, const VDesc* bd, const float* blocks, const float* msg_in,
+                          const long long* sec_off, float* partial, const long long* part_off, cudaStream_t s);
+void launch_qn_blocks_df32(const WorkList& wl, const VDesc* bd, const double* blocks, const double* msg_in,
+                           const long long* sec_off, double* partial, const long long* part_off, cudaStream_t s);
 
 // One wave of the sequential schedule (bp_kernels.cu): jobs (vertex, leg,
 // sequence position, network), one message each, in place; team 32 (four jobs

@@ -174,6 +174,8 @@ SIGNATURES = {
     "gbtn_qn_get_messages": (_I, [_P, _P, _I]),
     "gbtn_qn_bp_run": (_I, [_P, C.c_int32, C.c_double, _I32, _D]),
     "gbtn_qn_bp_run_sequential": (_I, [_P, _I32, C.c_int32, C.c_int32, C.c_double, _I32, _D]),
+    "gbtn_qn_bp_run_ex": (_I, [_P, C.POINTER(BPOpts), _I32, _D]),
+    "gbtn_qn_phase_sweeps": (_I, [_P, _I32]),
     "gbtn_qn_vertex_rdms": (_I, [_P, _D]),
     "gbtn_qn_logscalar": (_I, [_P, _D, _D]),
 }

@@ -28,6 +28,33 @@ from ._lib import check, dptr, iptr
 from .network import TensorNetwork, default_edge_sequence
 
 
+def bp_opts(maxiter, tol, schedule, seq, precision, normalize, mixed):
+    """gbtn_bp_opts for one update; ``seq`` (int32, kept alive by the caller)
+    is the directed-edge sequence of the sequential schedule, else None;
+    ``mixed`` holds the per-phase limits (tol_bf16, tol_f32, maxiter_bf16,
+    maxiter_f32, refine_f64, refine, confirm_f64)."""
+    o = _lib.BPOpts()
+    o.schedule = _lib.SCHED[schedule]
+    o.precision = _lib.PRECISION[precision]
+    o.maxiter = int(maxiter)
+    o.normalize = 1 if normalize else 0
+    o.tol = -1.0 if tol is None else float(tol)
+    if seq is not None:
+        o.edge_sequence = iptr(seq)
+        o.edge_sequence_len = len(seq)
+    else:
+        o.edge_sequence = C.cast(None, C.POINTER(C.c_int32))
+        o.edge_sequence_len = 0
+    o.tol_bf16 = float(mixed.get("tol_bf16", 0.0))
+    o.tol_f32 = float(mixed.get("tol_f32", 0.0))
+    o.maxiter_bf16 = int(mixed.get("maxiter_bf16", 0))
+    o.maxiter_f32 = int(mixed.get("maxiter_f32", 0))
+    o.refine_f64 = int(mixed.get("refine_f64", 0))
+    o.refine = _lib.REFINE[mixed.get("refine", "df32")]
+    o.confirm_f64 = int(mixed.get("confirm_f64", 0))
+    return o
+
+
 class BeliefPropagationCache:
     def __init__(self, tn: TensorNetwork, messages=None, bra=None, ctx=None):
         if tn.tensors is None:
@@ -152,12 +179,6 @@ class BeliefPropagationCache:
             maxiter = self.default_maxiter()
         if maxiter is None:
             raise _lib.InvalidArgument(1, "You need to specify a number of iterations for BP!")
-        o = _lib.BPOpts()
-        o.schedule = _lib.SCHED[schedule]
-        o.precision = _lib.PRECISION[precision]
-        o.maxiter = int(maxiter)
-        o.normalize = 1 if normalize else 0
-        o.tol = -1.0 if tol is None else float(tol)
         seq = None
         if schedule == "sequential":
             if edge_sequence is None:
@@ -166,18 +187,7 @@ class BeliefPropagationCache:
                 seq = self._default_seq
             else:
                 seq = np.ascontiguousarray(edge_sequence, dtype=np.int32)
-            o.edge_sequence = iptr(seq)
-            o.edge_sequence_len = len(seq)
-        else:
-            o.edge_sequence = C.cast(None, C.POINTER(C.c_int32))
-            o.edge_sequence_len = 0
-        o.tol_bf16 = float(mixed.get("tol_bf16", 0.0))
-        o.tol_f32 = float(mixed.get("tol_f32", 0.0))
-        o.maxiter_bf16 = int(mixed.get("maxiter_bf16", 0))
-        o.maxiter_f32 = int(mixed.get("maxiter_f32", 0))
-        o.refine_f64 = int(mixed.get("refine_f64", 0))
-        o.refine = _lib.REFINE[mixed.get("refine", "df32")]
-        o.confirm_f64 = int(mixed.get("confirm_f64", 0))
+        o = bp_opts(maxiter, tol, schedule, seq, precision, normalize, mixed)
         it = np.zeros(self.tn.n_networks, dtype=np.int32)
         md = np.zeros(self.tn.n_networks)
         self._c(self.lib.gbtn_bp_run(self.handle, C.byref(o), iptr(it), dptr(md)))

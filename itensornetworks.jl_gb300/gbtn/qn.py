@@ -21,6 +21,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import check, dptr, iptr
+from .cache import bp_opts
 from .network import TensorNetwork, default_edge_sequence
 
 
@@ -171,33 +172,48 @@ class QNBeliefPropagationCache:
         check(self.ctx.handle, self.lib.gbtn_qn_init_messages(self.handle))
         return self
 
-    def update(self, maxiter=None, tol=None, schedule="sequential", edge_sequence=None):
+    def update(self, maxiter=None, tol=None, schedule="sequential", edge_sequence=None, precision="f64",
+               normalize=True, **mixed):
         """update(bpc; maxiter, tol, edge_sequence): the reference's default
         sequential schedule (forest-cover order unless ``edge_sequence`` is
         given) or "parallel" (Jacobi) sweeps.  maxiter defaults to 1 on trees
-        and is required otherwise, as in the reference."""
+        and is required otherwise, as in the reference.  ``precision``: "f64",
+        "f32", "df32" or "mixed" (FP32 sweeps, then double-FP32 refinement to
+        tol; ``mixed`` takes the per-phase limits of the dense cache)."""
         if maxiter is None and self.q.tn.is_tree():
             maxiter = 1
         if maxiter is None:
             raise _lib.InvalidArgument(1, "You need to specify a number of iterations for BP!")
-        it = np.zeros(1, dtype=np.int32)
-        md = np.zeros(1)
-        t = -1.0 if tol is None else float(tol)
-        if schedule == "parallel":
-            check(self.ctx.handle, self.lib.gbtn_qn_bp_run(self.handle, int(maxiter), t, iptr(it), dptr(md)))
-        elif schedule == "sequential":
+        if schedule not in ("parallel", "sequential"):
+            raise _lib.InvalidArgument(1, f"unknown schedule {schedule!r}")
+        seq = None
+        if schedule == "sequential":
             if edge_sequence is None:
                 if getattr(self, "_default_seq", None) is None:
                     self._default_seq = np.ascontiguousarray(default_edge_sequence(self.q.tn), dtype=np.int32)
                 seq = self._default_seq
             else:
                 seq = np.ascontiguousarray(edge_sequence, dtype=np.int32)
-            check(self.ctx.handle, self.lib.gbtn_qn_bp_run_sequential(self.handle, iptr(seq), len(seq), int(maxiter),
-                                                                      t, iptr(it), dptr(md)))
+        it = np.zeros(1, dtype=np.int32)
+        md = np.zeros(1)
+        if precision == "f64" and normalize and not mixed:
+            t = -1.0 if tol is None else float(tol)
+            if seq is None:
+                check(self.ctx.handle, self.lib.gbtn_qn_bp_run(self.handle, int(maxiter), t, iptr(it), dptr(md)))
+            else:
+                check(self.ctx.handle, self.lib.gbtn_qn_bp_run_sequential(self.handle, iptr(seq), len(seq),
+                                                                          int(maxiter), t, iptr(it), dptr(md)))
         else:
-            raise _lib.InvalidArgument(1, f"unknown schedule {schedule!r}")
+            o = bp_opts(maxiter, tol, schedule, seq, precision, normalize, mixed)
+            check(self.ctx.handle, self.lib.gbtn_qn_bp_run_ex(self.handle, C.byref(o), iptr(it), dptr(md)))
         self.iterations, self.mean_diff = int(it[0]), float(md[0])
         return self
+
+    def phase_sweeps(self):
+        """Sweeps of each phase of the last update: {"bf16", "f32", "refine", "f64"}."""
+        out = np.zeros(4, dtype=np.int32)
+        check(self.ctx.handle, self.lib.gbtn_qn_phase_sweeps(self.handle, iptr(out)))
+        return dict(zip(("bf16", "f32", "refine", "f64"), (int(x) for x in out)))
 
     def messages(self):
         """Dense chi x chi messages per directed edge (block-diagonal)."""

@@ -143,3 +143,63 @@ def test_qn_sequential_schedule_matches_the_strict_sequence(L):
     assert abs(bpc.iterations - it) <= 1
     np.testing.assert_allclose(bpc.expect(O.SZ), O.expect1(g, A, ref, O.SZ), rtol=1e-9, atol=1e-12)
     bpc.close()
+
+
+def max_msg_err(got, ref):
+    return max(float(np.max(np.abs(g - r))) for g, r in zip(got, ref))
+
+
+def test_qn_reduced_precision_sweeps_against_the_oracle():
+    """FP32 and double-FP32 parallel sweeps on the blocks: 25 sweeps from
+    identity messages against the oracle's FP64 sweeps -- FP32 to 1e-5 on the
+    unit-norm messages (a few FP32 roundings per sweep, contracted by BP),
+    double-FP32 to 1e-12 (unit roundoff 2^-48 in the products and sums, FP64
+    storage)."""
+    q = random_u1_lattice(4, 4, seed=3)
+    g = oracle_graph(q.tn)
+    A = q.tn.tensors
+    m, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=25, schedule="parallel")
+    bpc = gbtn.QNBeliefPropagationCache(q)
+    bpc.update(maxiter=25, schedule="parallel", precision="f32")
+    assert bpc.phase_sweeps()["f32"] == 25
+    assert max_msg_err(bpc.messages(), m) <= 1e-5
+    bpc.init_messages()
+    bpc.update(maxiter=25, schedule="parallel", precision="df32")
+    assert bpc.phase_sweeps()["refine"] == 25
+    assert max_msg_err(bpc.messages(), m) <= 1e-12
+    bpc.close()
+
+
+@pytest.mark.parametrize("schedule", ["parallel", "sequential"])
+def test_qn_mixed_solve_reaches_the_fp64_fixed_point(schedule):
+    """MIXED: FP32 sweeps to their tolerance or noise floor, then double-FP32
+    sweeps from there.  With every refinement sweep run (no tolerance) the
+    result is the FP64 fixed point of the same schedule: <Sz> to 1e-10
+    relative against the oracle run to its rounding floor."""
+    q = random_u1_lattice(4, 4, seed=3)
+    g = oracle_graph(q.tn)
+    A = q.tn.tensors
+    seq = list(gbtn.default_edge_sequence(q.tn)) if schedule == "sequential" else None
+    ref, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=400, schedule=schedule, edge_sequence=seq)
+    bpc = gbtn.QNBeliefPropagationCache(q)
+    bpc.update(maxiter=150, schedule=schedule, precision="mixed")
+    ph = bpc.phase_sweeps()
+    assert 0 < ph["f32"] < 150 and ph["refine"] == 150
+    np.testing.assert_allclose(bpc.expect(O.SZ), O.expect1(g, A, ref, O.SZ), rtol=1e-10, atol=1e-13)
+    assert bpc.logscalar() == pytest.approx(float(np.real(O.logscalar(g, A, A, ref))), rel=1e-10)
+    # with a tolerance the refinement stops when the mean diff reaches it
+    bpc.init_messages()
+    bpc.update(maxiter=150, tol=1e-13, schedule=schedule, precision="mixed", refine="f64")
+    assert bpc.mean_diff <= 1e-13 and bpc.phase_sweeps()["refine"] == bpc.iterations < 150
+    np.testing.assert_allclose(bpc.expect(O.SZ), O.expect1(g, A, ref, O.SZ), rtol=1e-5, atol=1e-8)
+    bpc.close()
+
+
+def test_qn_precision_refusals():
+    q = random_u1_lattice(3, 3, seed=4)
+    bpc = gbtn.QNBeliefPropagationCache(q)
+    with pytest.raises(gbtn.Unsupported, match="tensor-core"):
+        bpc.update(maxiter=3, schedule="parallel", precision="bf16")
+    with pytest.raises(gbtn.InvalidArgument):
+        bpc.update(maxiter=3, schedule="colored", precision="f32")
+    bpc.close()
