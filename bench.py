@@ -382,14 +382,34 @@ def qn_timing(gbtn, ctx, stream, barrier, L=24, sweeps=10):
     ms_qn = ms(lambda n: qc.update(maxiter=n, schedule="parallel"))
     ms_dense = ms(lambda n: dc.update(maxiter=n, schedule="parallel", precision="f64"))
     ms_qn_seq = ms(lambda n: qc.update(maxiter=n))  # the reference's default sequential schedule
+    ms_qn32 = ms(lambda n: qc.update(maxiter=n, schedule="parallel", precision="f32"))
+    ms_qndf = ms(lambda n: qc.update(maxiter=n, schedule="parallel", precision="df32"))
     qc.init_messages()
     qc.update(maxiter=sweeps + 2, schedule="parallel")
     dc.init_messages("identity")
     dc.update(maxiter=sweeps + 2, schedule="parallel", precision="f64")
     err = max(float(np.max(np.abs(a - b))) for a, b in zip(qc.messages(), dc.messages()))
+
+    # time to solution from identity messages to a mean diff of 1e-13: FP64
+    # sweeps against the mixed FP32 -> double-FP32 solve
+    def solve(**kw):
+        qc.init_messages()
+        barrier()
+        t0 = time.perf_counter()
+        qc.update(maxiter=400, tol=1e-13, schedule="parallel", **kw)
+        barrier()
+        return 1e3 * (time.perf_counter() - t0), qc.expect(np.diag([0.5, -0.5])), qc.iterations
+    solve()
+    t64, sz64, it64 = solve()
+    solve(precision="mixed")
+    tmx, szmx, _ = solve(precision="mixed")
     out = {"workload": f"u1_peps{L}x{L}_chi8_sectors2-4-2_d2", "fp64_ms_per_sweep_block_sparse": ms_qn,
            "fp64_ms_per_sweep_dense": ms_dense, "speedup": ms_dense / ms_qn,
            "fp64_ms_per_sweep_block_sparse_sequential": ms_qn_seq,
+           "fp32_ms_per_sweep_block_sparse": ms_qn32, "df32_ms_per_sweep_block_sparse": ms_qndf,
+           "time_to_solution_tol1e-13_ms": {"fp64": t64, "fp64_sweeps": it64, "mixed": tmx,
+                                            "mixed_phase_sweeps": qc.phase_sweeps(), "speedup": t64 / tmx,
+                                            "max_abs_sz_difference": float(np.max(np.abs(szmx - sz64)))},
            "stored_elements_block_sparse": qc.n_block_elems,
            "stored_elements_dense": int(sum(q.tn.size(v) for v in range(tn.nv))),
            "max_message_difference_vs_dense": err}
