@@ -325,6 +325,24 @@ int gbtn_su_get_factors(gbtn_su* su, double* ket, int64_t capacity);
 int gbtn_su_apply(gbtn_su* su, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
                   const double* envs, int32_t maxdim, double cutoff, int32_t normalize, double* truncerr,
                   double* svals);
+/* Set every bond dimension (1..chi_max), e.g. to restore a saved state before
+ * gbtn_su_set_factors. */
+int gbtn_su_set_edge_dims(gbtn_su* su, const int32_t* dims);
+/* Adjoint of gbtn_su_apply (no counterpart in the reference), real tensors:
+ * the current tensors are the gates' inputs (they are not changed).  The
+ * gates of one call act on disjoint vertices (apply the adjoints of a longer
+ * gate sequence batch by batch, in reverse order, from saved states).
+ * post_edge_dims: the bond dimensions gbtn_su_apply left (checked against
+ * the recomputed truncation).  cot_out: dL/d(tensors after the gates),
+ * concatenated in vertex order with post_edge_dims; cot_in receives
+ * dL/d(current tensors) in the current shapes (sites without a gate pass
+ * theirs through); gate_cot (may be NULL): n_gates (du dv)^2 matrices dL/dG
+ * (with per_gate = 0 the shared gate's cotangent is their sum).  The
+ * environments are held constant.  Degenerate singular values (closer than
+ * 1e-14 sigma_max^2) and kept zero singular values contribute no derivative. */
+int gbtn_su_apply_vjp(gbtn_su* su, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
+                      const double* envs, int32_t maxdim, double cutoff, int32_t normalize,
+                      const int32_t* post_edge_dims, const double* cot_out, double* cot_in, double* gate_cot);
 
 /* ---- energies and gradients (FP64) ------------------------------------------ */
 /* Two-site energy sum_e sum_t coef[t] <O_t (x) O_t>_e with BP reduced density

@@ -656,6 +656,10 @@ struct SuArgs {
   double* truncerr;          // [njobs] or NULL
   double* svals;             // [njobs * maxdim] or NULL
   int* status;               // set to 1 when a shape exceeds the kernel limits
+  // adjoint runs only (NULL otherwise): the full SVD of theta per job and the
+  // square-root environments per (job, side), written by the forward stages
+  double* svd_full;
+  double* side_sqrt;
 };
 
 struct SideShape {
@@ -708,6 +712,11 @@ constexpr int kJobV = kSuMaxTheta * kSuMaxTheta;       // right factor, nt x kk 
 constexpr int kJobS = 2 * kSuMaxTheta * kSuMaxTheta;   // sqrt of the kept singular values
 constexpr int kJobMeta = kJobS + kSuMaxTheta;          // [0] = kk, [1] = ok
 constexpr int kJobStride = kJobMeta + 8;
+constexpr int kFullU = 0;                              // all left singular vectors, mt x n (ld mt)
+constexpr int kFullV = kSuMaxTheta * kSuMaxTheta;      // all right singular vectors, nt x n (ld nt)
+constexpr int kFullSig = 2 * kSuMaxTheta * kSuMaxTheta;  // all n singular values, descending
+constexpr int kFullStride = kFullSig + kSuMaxTheta;
+constexpr int kSqrtStride = kMaxDeg * 64;              // sqrt environment of every leg, chi x chi
 
 // The gate's site on `side`: shape with the current bond dimensions, and
 // whether the stages' limits hold (uniform over the CTA).
@@ -716,7 +725,9 @@ __device__ bool site_of(const SuArgs& a, const SuJob& job, int side, int& x, Sid
   side_shape(a, x, side ? job.pv : job.pu, h);
   const int ce = h.chi[h.p];
   const int r = min(h.m, h.d * ce);
-  return h.n <= kSuMaxN && h.d * ce <= 32 && h.k <= kMaxDeg && r * h.d <= a.bmax;
+  // the rebuilt site (bond up to maxdim) must fit the same buffers
+  return h.n <= kSuMaxN && h.n / ce * max(a.maxdim, ce) <= kSuMaxN && h.d * ce <= 32 && h.k <= kMaxDeg &&
+         r * h.d <= a.bmax;
 }
 
 // Stage 1, one CTA per (gate, side): square-root environments absorbed,
@@ -770,6 +781,9 @@ __global__ void __launch_bounds__(kSuThreads, 3) su_qr_kernel(SuArgs a) {
         sb.work = nxt;                   // free here: m n + n^2 <= 128 doubles used
         sb.extra = nxt + kSuMaxN / 2;    // 2 n^2 <= 128 doubles
         cta_env_sqrt(env, h.chi[q], S, out + kSideSI + q * 64, A8, V8, sig, sb);
+        if (a.side_sqrt)
+          for (int i = tid; i < h.chi[q] * h.chi[q]; i += kSuThreads)
+            a.side_sqrt[(size_t)blockIdx.x * kSqrtStride + q * 64 + i] = S[i];
         absorb_any<double>(h.chi[q], cur, nxt, h.n, st, S, tid, kSuThreads);
         __syncthreads();
         double* t = cur;
@@ -906,9 +920,38 @@ __global__ void __launch_bounds__(kSuThreads, 2) su_svd_kernel(SuArgs a) {
   }
   __syncthreads();
   const int kk = s_k;
+  if (a.svd_full) {
+    const int nsv = min(mt, nt);
+    double* full = a.svd_full + (size_t)j * kFullStride;
+    for (int i = tid; i < mt * nsv; i += kSuThreads) full[kFullU + i] = UF[i];
+    for (int i = tid; i < nt * nsv; i += kSuThreads) full[kFullV + i] = VF[i];
+    if (tid < nsv) full[kFullSig + tid] = sig[tid];
+  }
   for (int i = tid; i < mt * kk; i += kSuThreads) out[kJobU + i] = UF[i];
   for (int i = tid; i < nt * kk; i += kSuThreads) out[kJobV + i] = VF[i];
   if (tid < kk) out[kJobS + tid] = sqrt(sig[tid]);  // sqrt(S), split onto both sites
+}
+
+// Y (m x ncol, ld m) <- Q Y = H_0 ... H_{r-1} Y, or Q^T Y = H_{r-1} ... H_0 Y
+// with transpose (each H_j = I - beta_j v_j v_j^T is symmetric), with the
+// reflectors of a side's scratch: v_j in rows j..m of column j (beta_j = 0:
+// skipped).  Ends with a CTA barrier.
+__device__ void apply_reflectors(const double* ss, int m, int r, double* Y, int ncol, bool transpose) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int t = 0; t < r; ++t) {
+    const int jr = transpose ? t : r - 1 - t;
+    const double bj = ss[kSideBeta + jr];
+    if (bj == 0.0) continue;
+    const double* v = ss + kSideRefl + (size_t)jr * m;
+    for (int c = warp; c < ncol; c += kSuWarps) {
+      double* y = Y + (size_t)c * m;
+      double w = 0.0;
+      for (int i = jr + lane; i < m; i += 32) w = fma(v[i], y[i], w);
+      w = warp_sum(w) * bj;
+      for (int i = jr + lane; i < m; i += 32) y[i] = fma(-w, v[i], y[i]);
+    }
+    __syncthreads();
+  }
 }
 
 // Stage 3, one CTA per (gate, side): the new site = Q (U sqrt(S)) (or
@@ -918,7 +961,6 @@ __global__ void __launch_bounds__(kSuThreads, 2) su_svd_kernel(SuArgs a) {
 __global__ void __launch_bounds__(kSuThreads, 3) su_rebuild_kernel(SuArgs a) {
   extern __shared__ __align__(16) double smem[];
   const int j = blockIdx.x >> 1, side = blockIdx.x & 1, tid = threadIdx.x;
-  const int lane = tid & 31, warp = tid >> 5;
   if (j >= a.njobs) return;
   const double* js = a.job_scratch + (size_t)j * kJobStride;
   if (js[kJobMeta + 1] == 0.0) return;  // the gate exceeded the limits (status already set)
@@ -956,20 +998,7 @@ __global__ void __launch_bounds__(kSuThreads, 3) su_rebuild_kernel(SuArgs a) {
     Y[i] = v;
   }
   __syncthreads();
-  // Y <- H_0 ... H_{r-1} Y, reflector j from row j on (beta_j = 0: skipped)
-  for (int jr = r - 1; jr >= 0; --jr) {
-    const double bj = ss[kSideBeta + jr];
-    if (bj == 0.0) continue;
-    const double* v = ss + kSideRefl + (size_t)jr * m;
-    for (int c = warp; c < ncol2; c += kSuWarps) {
-      double* y = Y + (size_t)c * m;
-      double w = 0.0;
-      for (int i = jr + lane; i < m; i += 32) w = fma(v[i], y[i], w);
-      w = warp_sum(w) * bj;
-      for (int i = jr + lane; i < m; i += 32) y[i] = fma(-w, v[i], y[i]);
-    }
-    __syncthreads();
-  }
+  apply_reflectors(ss, m, r, Y, ncol2, false);
   double* dst = a.tens + a.cap_off[x];
   if (a.envs) {
     // tensor layout into T, then the inverse-sqrt environments (T <-> Y)
@@ -1016,6 +1045,437 @@ __global__ void __launch_bounds__(kSuThreads, 3) su_rebuild_kernel(SuArgs a) {
       split_index(h, chi2, i, row, s, b);
       dst[i] = Y[row + (size_t)m * (s + d * b)] * s_scale;
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint of a gate batch (real FP64).  The forward stages have left, per
+// job, the reflectors Q, R, beta and the inverse-sqrt environments of both
+// sides, the full SVD theta = U diag(sigma) V^T (n = min(mt, nt) values,
+// descending), the kept dimension k and the square-root environments.  With
+// W_x = Q_x R_x the matricised site (sqrt environments absorbed) and P_x =
+// Q_x (x) 1_site, the outputs are the two halves L = P_u U_k sqrt(sigma_k),
+// R = P_v V_k sqrt(sigma_k) of the truncated SVD of Theta = P_u theta P_v^T,
+// inverse-sqrt environments absorbed, optionally normalised.  Given their
+// cotangents:
+//   1. normalisation and environment absorption backwards (both linear maps of
+//      symmetric matrices, transposed);
+//   2. the cotangents of L and R split into their parts in range(P_x)
+//      (Z = Q^T Ybar) and orthogonal to it (Ybar_perp);
+//   3. the truncated-SVD adjoint in range(P_u) x range(P_v) (Townsend 2016,
+//      "Differentiating the singular value decomposition", with the
+//      discarded singular values of theta in F_ij = 1/(sigma_j^2 - sigma_i^2)
+//      and zero cotangents on the discarded vectors):
+//        thetabar = U [F o (U^T Ubar - Ubar^T U) S + diag(sigmabar)
+//                      + S F o (V^T Vbar - Vbar^T V)] V^T
+//                   + (1 - U U^T) Ubar S_k^-1 V_k^T + U_k S_k^-1 Vbar^T (1 - V V^T);
+//      the parts orthogonal to range(P_x) add Ubar_perp S_k^-1 (P_v V_k)^T and
+//      (P_u U_k) S_k^-1 Vbar_perp^T, whose contraction with the other site
+//      only sees R of that site (Q^T Q = 1) and nothing of its own R;
+//   4. through the gate (its transpose) and the bond contraction to Rbar_x,
+//      Wbar_x = Q_x Rbar_x + the orthogonal term, then the square-root
+//      environments backwards to the cotangent of the site tensor.
+// The gate's cotangent is <thetabar, theta_pre> over the row and column
+// indices.  Environments are constants.  Pairs of singular values closer
+// than 1e-14 sigma_max^2 (degenerate) get F = 0, and kept singular values at
+// zero give no derivative (S_k^-1 as a pseudo-inverse).
+// ---------------------------------------------------------------------------
+
+constexpr int kVjpSmall = kSuMaxTheta * kSuMaxTheta;  // 4096
+// per side
+constexpr int kVjY = 0;                     // Ybar (m x d k), then its part orthogonal to range(Q)
+constexpr int kVjT0 = kVjY + kSuMaxN;       // tensor ping
+constexpr int kVjT1 = kVjT0 + kSuMaxN;      // tensor pong
+constexpr int kVjW = kVjT1 + kSuMaxN;       // Wbar (m x d chi)
+constexpr int kVjZ = kVjW + kSuMaxN;        // Z = Q^T Ybar (r x d k)
+constexpr int kVjRb = kVjZ + kVjpSmall;     // Rbar (r x d chi)
+constexpr int kVjH = kVjRb + kVjpSmall;     // H (d k x d chi)
+constexpr int kVjM = kVjH + kVjpSmall;      // M (k x d x d chi)
+constexpr int kVjSide = kVjM + kVjpSmall;
+// per job, after both sides
+constexpr int kVjUb = 2 * kVjSide;          // Ubar in range (mt x k)
+constexpr int kVjVb = kVjUb + kVjpSmall;    // Vbar in range (nt x k)
+constexpr int kVjUtUb = kVjVb + kVjpSmall;  // U^T Ubar (n x k)
+constexpr int kVjVtVb = kVjUtUb + kVjpSmall;
+constexpr int kVjJ = kVjVtVb + kVjpSmall;   // n x n
+constexpr int kVjUJ = kVjJ + kVjpSmall;     // U J (mt x n)
+constexpr int kVjP1 = kVjUJ + kVjpSmall;    // (1 - U U^T) Ubar S^-1 (mt x k)
+constexpr int kVjP2 = kVjP1 + kVjpSmall;    // (1 - V V^T) Vbar S^-1 (nt x k)
+constexpr int kVjTb = kVjP2 + kVjpSmall;    // thetabar (mt x nt)
+constexpr int kVjPhi = kVjTb + kVjpSmall;   // gate^T thetabar (mt x nt)
+constexpr int kVjPsi = kVjPhi + kVjpSmall;  // theta before the gate (mt x nt)
+constexpr int kVjSb = kVjPsi + kVjpSmall;   // sigmabar (n)
+constexpr int kVjStride = kVjSb + kSuMaxTheta;
+
+__device__ __forceinline__ double safe_inv(double x) { return x > 0.0 ? 1.0 / x : 0.0; }
+
+// One CTA per gate of the batch.  cot_out / cot_in: capacity layout (the
+// state's slots), the gate's sites after (bond k) / before the gate.
+// post_dims: the bond dimension the caller saw after the gates.
+__global__ void __launch_bounds__(kSuThreads, 1)
+    su_vjp_kernel(SuArgs a, const int* post_dims, const double* cot_out, double* cot_in, double* gate_cot,
+                  double* work) {
+  const int j = blockIdx.x, tid = threadIdx.x;
+  if (j >= a.njobs) return;
+  __shared__ double red[kSuWarps + 1];
+  __shared__ double s_scale, s_dot;
+  const SuJob job = a.jobs[j];
+  const double* ssd[2] = {a.side_scratch + (size_t)(2 * j) * kSideStride,
+                          a.side_scratch + (size_t)(2 * j + 1) * kSideStride};
+  const double* js = a.job_scratch + (size_t)j * kJobStride;
+  if (ssd[0][kSideMeta + 1] != 0.0 || ssd[1][kSideMeta + 1] != 0.0 || js[kJobMeta + 1] == 0.0) return;
+  const int k = (int)js[kJobMeta];
+  if (k != post_dims[job.e]) {
+    if (tid == 0) atomicExch(a.status, 2);
+    return;
+  }
+  const double* full = a.svd_full + (size_t)j * kFullStride;
+  const double* UF = full + kFullU;
+  const double* VF = full + kFullV;
+  const double* sig = full + kFullSig;
+  double* wj = work + (size_t)j * kVjStride;
+  SideShape hs[2];
+  int xs[2];
+  site_of(a, job, 0, xs[0], hs[0]);
+  site_of(a, job, 1, xs[1], hs[1]);
+  const int ce = hs[0].chi[hs[0].p];
+  const int du = hs[0].d, dv = hs[1].d, D = du * dv;
+  const int ru = (int)ssd[0][kSideMeta], rv = (int)ssd[1][kSideMeta];
+  const int mt = ru * du, nt = dv * rv, n = min(mt, nt);
+  const double* G = a.gates + (size_t)a.gate_stride * j;
+  const double* RU = ssd[0] + kSideR;
+  const double* RV = ssd[1] + kSideR;
+  double* Ub = wj + kVjUb;
+  double* Vb = wj + kVjVb;
+  double* sb = wj + kVjSb;
+  for (int i = tid; i < n; i += kSuThreads) sb[i] = 0.0;
+  __syncthreads();
+
+  // ---- 1-2: per side, the cotangent of L (or R) split by range(Q)
+  for (int side = 0; side < 2; ++side) {
+    const SideShape& h = hs[side];
+    const double* ss = ssd[side];
+    double* ws = wj + (size_t)side * kVjSide;
+    double* Y = ws + kVjY;
+    double* Z = ws + kVjZ;
+    const int x = xs[side], m = h.m, d = h.d, r = (int)ss[kSideMeta];
+    int chi2[kMaxDeg];
+    for (int q = 0; q < h.k; ++q) chi2[q] = h.chi[q];
+    chi2[h.p] = k;
+    int n2 = d;
+    for (int q = 0; q < h.k; ++q) n2 *= chi2[q];
+    const int ncol2 = d * k;
+    // the forward output before normalisation: C = Si-absorbed (Q [X; 0])
+    for (int i = tid; i < m * ncol2; i += kSuThreads) {
+      const int row = i % m, col = i / m, s_ = col % d, b = col / d;
+      double v = 0.0;
+      if (row < r)
+        v = side == 0 ? js[kJobU + (row + ru * s_) + (size_t)mt * b] * js[kJobS + b]
+                      : js[kJobV + (s_ + dv * row) + (size_t)nt * b] * js[kJobS + b];
+      Y[i] = v;
+    }
+    __syncthreads();
+    apply_reflectors(ss, m, r, Y, ncol2, false);
+    double* cur = ws + kVjT0;
+    double* nxt = ws + kVjT1;
+    for (int i = tid; i < n2; i += kSuThreads) {
+      int row, s_, b;
+      split_index(h, chi2, i, row, s_, b);
+      cur[i] = Y[row + (size_t)m * (s_ + d * b)];
+    }
+    __syncthreads();
+    double* Mt = ws + kVjM;  // a transposed chi x chi environment
+    if (a.envs) {
+      int st = d;
+      for (int q = 0; q < h.k; ++q) {
+        if (q != h.p) {
+          const int c = chi2[q];
+          const double* si = ss + kSideSI + q * 64;
+          for (int i = tid; i < c * c; i += kSuThreads) Mt[(i / c) + c * (i % c)] = si[i];
+          __syncthreads();
+          absorb_any<double>(c, cur, nxt, n2, st, Mt, tid, kSuThreads);
+          __syncthreads();
+          double* t = cur;
+          cur = nxt;
+          nxt = t;
+        }
+        st *= chi2[q];
+      }
+    }
+    // normalisation backwards: Cbar = (Abar - A <A, Abar>) / |C|
+    const double* Ab = cot_out + a.cap_off[x];
+    double s2 = 0.0, dt = 0.0;
+    for (int i = tid; i < n2; i += kSuThreads) {
+      s2 = fma(cur[i], cur[i], s2);
+      dt = fma(cur[i], Ab[i], dt);
+    }
+    s2 = block_sum(s2, red);
+    dt = block_sum(dt, red);
+    if (tid == 0) {
+      const double nc = sqrt(s2);
+      s_scale = (a.normalize && nc > 0.0) ? 1.0 / nc : 1.0;
+      s_dot = (a.normalize && nc > 0.0) ? dt / s2 : 0.0;  // <A, Abar> / |C| with A = C / |C|
+    }
+    __syncthreads();
+    for (int i = tid; i < n2; i += kSuThreads) nxt[i] = (Ab[i] - cur[i] * s_dot) * s_scale;
+    __syncthreads();
+    {
+      double* t = cur;
+      cur = nxt;
+      nxt = t;
+    }
+    // inverse-sqrt environments backwards: the transposes of the matrices absorbed
+    if (a.envs) {
+      int st = d;
+      for (int q = 0; q < h.k; ++q) {
+        if (q != h.p) {
+          const int c = chi2[q];
+          absorb_any<double>(c, cur, nxt, n2, st, ss + kSideSI + q * 64, tid, kSuThreads);
+          __syncthreads();
+          double* t = cur;
+          cur = nxt;
+          nxt = t;
+        }
+        st *= chi2[q];
+      }
+    }
+    for (int i = tid; i < n2; i += kSuThreads) {
+      int row, s_, b;
+      split_index(h, chi2, i, row, s_, b);
+      Y[row + (size_t)m * (s_ + d * b)] = cur[i];
+    }
+    __syncthreads();
+    // Ybar = Q [Z; 0] + Ybar_perp
+    apply_reflectors(ss, m, r, Y, ncol2, true);
+    for (int i = tid; i < r * ncol2; i += kSuThreads) {
+      const int t = i % r, col = i / r;
+      Z[i] = Y[t + (size_t)m * col];
+    }
+    __syncthreads();
+    for (int i = tid; i < r * ncol2; i += kSuThreads) Y[(i % r) + (size_t)m * (i / r)] = 0.0;
+    __syncthreads();
+    apply_reflectors(ss, m, r, Y, ncol2, false);
+    // in-range cotangents of the singular vectors, and of sigma
+    for (int i = tid; i < (side == 0 ? mt : nt) * k; i += kSuThreads) {
+      const int row = i % (side == 0 ? mt : nt), b = i / (side == 0 ? mt : nt);
+      const int t = side == 0 ? row % ru : row / dv;
+      const int s_ = side == 0 ? row / ru : row % dv;
+      (side == 0 ? Ub : Vb)[i] = Z[t + r * (s_ + d * b)] * js[kJobS + b];
+    }
+    for (int b = threadIdx.x >> 5; b < k; b += kSuWarps) {
+      const int lane = tid & 31;
+      double acc = 0.0;
+      for (int i = lane; i < r * d; i += 32) {
+        const int t = i % r, s_ = i / r;
+        const double f = side == 0 ? UF[(t + ru * s_) + (size_t)mt * b] : VF[(s_ + dv * t) + (size_t)nt * b];
+        acc = fma(f, Z[t + r * (s_ + d * b)], acc);
+      }
+      acc = warp_sum(acc);
+      if (lane == 0) sb[b] += 0.5 * acc * safe_inv(js[kJobS + b]);
+    }
+    __syncthreads();
+  }
+
+  // ---- 3: the SVD adjoint in range
+  double* UtUb = wj + kVjUtUb;
+  double* VtVb = wj + kVjVtVb;
+  double* J = wj + kVjJ;
+  for (int i = tid; i < n * k; i += kSuThreads) {
+    const int a_ = i % n, c = i / n;
+    double su_ = 0.0, sv_ = 0.0;
+    for (int row = 0; row < mt; ++row) su_ = fma(UF[row + (size_t)mt * a_], Ub[row + (size_t)mt * c], su_);
+    for (int col = 0; col < nt; ++col) sv_ = fma(VF[col + (size_t)nt * a_], Vb[col + (size_t)nt * c], sv_);
+    UtUb[i] = su_;
+    VtVb[i] = sv_;
+  }
+  __syncthreads();
+  const double smax2 = sig[0] * sig[0];
+  for (int i = tid; i < n * n; i += kSuThreads) {
+    const int p = i % n, q = i / n;
+    double v = 0.0;
+    if (p == q) {
+      v = p < k ? sb[p] : 0.0;
+    } else if (p < k || q < k) {
+      const double den = sig[q] * sig[q] - sig[p] * sig[p];
+      const double F = fabs(den) > 1e-14 * smax2 ? 1.0 / den : 0.0;
+      const double au = (q < k ? UtUb[p + n * q] : 0.0) - (p < k ? UtUb[q + n * p] : 0.0);
+      const double av = (q < k ? VtVb[p + n * q] : 0.0) - (p < k ? VtVb[q + n * p] : 0.0);
+      v = F * (au * sig[q] + sig[p] * av);
+    }
+    J[i] = v;
+  }
+  __syncthreads();
+  double* UJ = wj + kVjUJ;
+  double* P1 = wj + kVjP1;
+  double* P2 = wj + kVjP2;
+  for (int i = tid; i < mt * n; i += kSuThreads) {
+    const int row = i % mt, q = i / mt;
+    double acc = 0.0;
+    for (int p = 0; p < n; ++p) acc = fma(UF[row + (size_t)mt * p], J[p + n * q], acc);
+    UJ[i] = acc;
+  }
+  for (int i = tid; i < mt * k; i += kSuThreads) {
+    const int row = i % mt, c = i / mt;
+    double acc = Ub[i];
+    for (int p = 0; p < n; ++p) acc = fma(-UF[row + (size_t)mt * p], UtUb[p + n * c], acc);
+    P1[i] = acc * safe_inv(sig[c]);
+  }
+  for (int i = tid; i < nt * k; i += kSuThreads) {
+    const int col = i % nt, c = i / nt;
+    double acc = Vb[i];
+    for (int p = 0; p < n; ++p) acc = fma(-VF[col + (size_t)nt * p], VtVb[p + n * c], acc);
+    P2[i] = acc * safe_inv(sig[c]);
+  }
+  __syncthreads();
+  double* Tb = wj + kVjTb;
+  for (int i = tid; i < mt * nt; i += kSuThreads) {
+    const int row = i % mt, col = i / mt;
+    double acc = 0.0;
+    for (int q = 0; q < n; ++q) acc = fma(UJ[row + (size_t)mt * q], VF[col + (size_t)nt * q], acc);
+    for (int c = 0; c < k; ++c) {
+      acc = fma(P1[row + (size_t)mt * c], VF[col + (size_t)nt * c], acc);
+      acc = fma(UF[row + (size_t)mt * c], P2[col + (size_t)nt * c], acc);
+    }
+    Tb[i] = acc;
+  }
+  // the theta of the forward before the gate (rows iu + ru su, columns sv + dv iv)
+  double* Psi = wj + kVjPsi;
+  for (int i = tid; i < mt * nt; i += kSuThreads) {
+    const int row = i % mt, col = i / mt;
+    const int iu = row % ru, su_ = row / ru, sv_ = col % dv, iv = col / dv;
+    double acc = 0.0;
+    for (int e = 0; e < ce; ++e) acc = fma(RU[iu + ru * (su_ + du * e)], RV[iv + rv * (sv_ + dv * e)], acc);
+    Psi[i] = acc;
+  }
+  __syncthreads();
+
+  // ---- 4: through the gate and the bond contraction
+  double* Phi = wj + kVjPhi;
+  for (int i = tid; i < mt * nt; i += kSuThreads) {
+    const int row = i % mt, col = i / mt;
+    const int iu = row % ru, su_ = row / ru, sv_ = col % dv, iv = col / dv;
+    double acc = 0.0;
+    for (int spv = 0; spv < dv; ++spv)
+      for (int spu = 0; spu < du; ++spu)
+        acc = fma(G[(spu + du * spv) + D * (su_ + du * sv_)], Tb[(iu + ru * spu) + mt * (spv + dv * iv)], acc);
+    Phi[i] = acc;
+  }
+  if (gate_cot)
+    for (int i = tid; i < D * D; i += kSuThreads) {
+      const int o = i % D, in = i / D;
+      const int spu = o % du, spv = o / du, su_ = in % du, sv_ = in / du;
+      double acc = 0.0;
+      for (int iv = 0; iv < rv; ++iv)
+        for (int iu = 0; iu < ru; ++iu)
+          acc = fma(Tb[(iu + ru * spu) + mt * (spv + dv * iv)], Psi[(iu + ru * su_) + mt * (sv_ + dv * iv)], acc);
+      gate_cot[(size_t)j * D * D + i] = acc;
+    }
+  __syncthreads();
+  double* Rbu = wj + kVjRb;
+  double* Rbv = wj + kVjSide + kVjRb;
+  for (int i = tid; i < ru * du * ce; i += kSuThreads) {
+    const int iu = i % ru, su_ = (i / ru) % du, e = i / (ru * du);
+    double acc = 0.0;
+    for (int iv = 0; iv < rv; ++iv)
+      for (int sv_ = 0; sv_ < dv; ++sv_)
+        acc = fma(Phi[(iu + ru * su_) + mt * (sv_ + dv * iv)], RV[iv + rv * (sv_ + dv * e)], acc);
+    Rbu[i] = acc;
+  }
+  for (int i = tid; i < rv * dv * ce; i += kSuThreads) {
+    const int iv = i % rv, sv_ = (i / rv) % dv, e = i / (rv * dv);
+    double acc = 0.0;
+    for (int su_ = 0; su_ < du; ++su_)
+      for (int iu = 0; iu < ru; ++iu)
+        acc = fma(Phi[(iu + ru * su_) + mt * (sv_ + dv * iv)], RU[iu + ru * (su_ + du * e)], acc);
+    Rbv[i] = acc;
+  }
+  // the orthogonal parts: M[c, s', (s, e)] = sum_t (V or U)[(s', t), c] R_other[t, (s, e)],
+  // H[(s'_x, c), (s_x, e)] = sum gate M / sqrt(sigma_c)
+  for (int side = 0; side < 2; ++side) {
+    double* ws = wj + (size_t)side * kVjSide;
+    double* M = ws + kVjM;
+    const int dy = side == 0 ? dv : du;  // the other side's site dimension
+    for (int i = tid; i < k * dy * dy * ce; i += kSuThreads) {
+      const int c = i % k, sp = (i / k) % dy, se = i / (k * dy);  // se = s + dy e
+      const int s_ = se % dy, e = se / dy;
+      double acc = 0.0;
+      if (side == 0)
+        for (int iv = 0; iv < rv; ++iv) acc = fma(VF[(sp + dv * iv) + (size_t)nt * c], RV[iv + rv * (s_ + dv * e)], acc);
+      else
+        for (int iu = 0; iu < ru; ++iu) acc = fma(UF[(iu + ru * sp) + (size_t)mt * c], RU[iu + ru * (s_ + du * e)], acc);
+      M[i] = acc;
+    }
+  }
+  __syncthreads();
+  for (int side = 0; side < 2; ++side) {
+    double* ws = wj + (size_t)side * kVjSide;
+    const double* M = ws + kVjM;
+    double* H = ws + kVjH;
+    const int dx = side == 0 ? du : dv, dy = side == 0 ? dv : du;
+    const int rowsH = dx * k;
+    for (int i = tid; i < rowsH * dx * ce; i += kSuThreads) {
+      const int spx = (i % rowsH) % dx, c = (i % rowsH) / dx, col = i / rowsH, sx = col % dx, e = col / dx;
+      double acc = 0.0;
+      for (int sy = 0; sy < dy; ++sy)
+        for (int spy = 0; spy < dy; ++spy) {
+          const int o = side == 0 ? spx + du * spy : spy + du * spx;
+          const int in = side == 0 ? sx + du * sy : sy + du * sx;
+          acc = fma(G[o + D * in], M[c + k * (spy + dy * (sy + dy * e))], acc);
+        }
+      H[i] = acc * safe_inv(js[kJobS + c]);
+    }
+  }
+  __syncthreads();
+
+  // ---- 5: Wbar = Q [Rbar; 0] + Ybar_perp H, then the sqrt environments backwards
+  for (int side = 0; side < 2; ++side) {
+    const SideShape& h = hs[side];
+    const double* ss = ssd[side];
+    double* ws = wj + (size_t)side * kVjSide;
+    const double* Y = ws + kVjY;
+    const double* Rb = ws + kVjRb;
+    const double* H = ws + kVjH;
+    double* W = ws + kVjW;
+    const int x = xs[side], m = h.m, d = h.d, r = (int)ss[kSideMeta], ncol = d * ce, rowsH = d * k;
+    for (int i = tid; i < m * ncol; i += kSuThreads) W[i] = (i % m) < r ? Rb[(i % m) + r * (i / m)] : 0.0;
+    __syncthreads();
+    apply_reflectors(ss, m, r, W, ncol, false);
+    for (int i = tid; i < m * ncol; i += kSuThreads) {
+      const int row = i % m, col = i / m;
+      double acc = W[i];
+      for (int q = 0; q < rowsH; ++q) acc = fma(Y[row + (size_t)m * q], H[q + rowsH * col], acc);
+      W[i] = acc;
+    }
+    __syncthreads();
+    double* cur = ws + kVjT0;
+    double* nxt = ws + kVjT1;
+    for (int i = tid; i < h.n; i += kSuThreads) {
+      int row, s_, b;
+      split_index(h, h.chi, i, row, s_, b);
+      cur[i] = W[row + (size_t)m * (s_ + d * b)];
+    }
+    __syncthreads();
+    if (a.envs) {
+      double* Mt = ws + kVjM;
+      int st = d;
+      for (int q = 0; q < h.k; ++q) {
+        if (q != h.p) {
+          const int c = h.chi[q];
+          const double* sq = a.side_sqrt + (size_t)(2 * j + side) * kSqrtStride + q * 64;
+          for (int i = tid; i < c * c; i += kSuThreads) Mt[(i / c) + c * (i % c)] = sq[i];
+          __syncthreads();
+          absorb_any<double>(c, cur, nxt, h.n, st, Mt, tid, kSuThreads);
+          __syncthreads();
+          double* t = cur;
+          cur = nxt;
+          nxt = t;
+        }
+        st *= h.chi[q];
+      }
+    }
+    double* dst = cot_in + a.cap_off[x];
+    for (int i = tid; i < h.n; i += kSuThreads) dst[i] = cur[i];
+    __syncthreads();
   }
 }
 
@@ -1483,6 +1943,9 @@ namespace gbtn {
 
 constexpr size_t kSuSideStride = kSideStride;
 constexpr size_t kSuJobStride = kJobStride;
+constexpr size_t kSuFullStride = kFullStride;
+constexpr size_t kSuSqrtStride = kSqrtStride;
+constexpr size_t kSuVjpStride = kVjStride;
 
 // Shared memory of the three stages.
 size_t su_qr_smem(bool envs) {
@@ -1505,6 +1968,28 @@ void su_launch(const SuArgs& a, cudaStream_t s) {
   su_svd_kernel<<<a.njobs, kSuThreads, s2, s>>>(a);
   GBTN_CUDA(cudaGetLastError());
   su_rebuild_kernel<<<2 * a.njobs, kSuThreads, s3, s>>>(a);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+// The forward's QR and SVD stages with their adjoint outputs (the state is
+// not written: edim must be a scratch copy of the bond dimensions), then the
+// adjoint kernel.
+void su_launch_fwd_stages(const SuArgs& a, cudaStream_t s) {
+  if (a.njobs == 0) return;
+  const bool envs = a.envs != nullptr;
+  const size_t s1 = su_qr_smem(envs), s2 = su_svd_smem(a.bmax);
+  GBTN_CUDA(cudaFuncSetAttribute(su_qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1));
+  GBTN_CUDA(cudaFuncSetAttribute(su_svd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+  su_qr_kernel<<<2 * a.njobs, kSuThreads, s1, s>>>(a);
+  GBTN_CUDA(cudaGetLastError());
+  su_svd_kernel<<<a.njobs, kSuThreads, s2, s>>>(a);
+  GBTN_CUDA(cudaGetLastError());
+}
+
+void su_launch_vjp_kernel(const SuArgs& a, const int* post_dims, const double* cot_out, double* cot_in,
+                          double* gate_cot, double* work, cudaStream_t s) {
+  if (a.njobs == 0) return;
+  su_vjp_kernel<<<a.njobs, kSuThreads, 0, s>>>(a, post_dims, cot_out, cot_in, gate_cot, work);
   GBTN_CUDA(cudaGetLastError());
 }
 
@@ -1797,12 +2282,201 @@ int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const doubl
       return su_fail(S, GBTN_ERR_UNSUPPORTED,
                      S->cplx ? "simple update: a gate exceeds the complex kernel's limits (site tensor, also with the "
                                "bond at chi_max, > 4096 elements, or theta > 32 x 32)"
-                             : "simple update: a gate exceeds the kernel limits (site tensor > 8192 elements or theta > 64 x 64)");
+                             : "simple update: a gate exceeds the kernel limits (site tensor, also with the bond at maxdim, "
+                               "> 8192 elements, or theta > 64 x 64)");
     if (truncerr) std::copy(te.begin(), te.end(), truncerr);
     if (svals)
       for (int j = 0; j < n_gates; ++j)
         for (int i = 0; i < maxdim; ++i) svals[(size_t)j * maxdim + i] = i < md ? sv[(size_t)j * md + i] : 0.0;
     su_pull_dims(S);
+  } catch (const std::exception& e) {
+    return su_fail(S, GBTN_ERR_CUDA, e.what());
+  }
+  return GBTN_OK;
+}
+
+int gbtn_su_set_edge_dims(gbtn_su* S, const int32_t* dims) {
+  if (!S || !dims) return GBTN_ERR_INVALID;
+  for (int e = 0; e < S->ne; ++e)
+    if (dims[e] < 1 || dims[e] > S->chimax)
+      return su_fail(S, GBTN_ERR_INVALID, "simple update: bond dimension outside 1..chi_max");
+  try {
+    S->edim.assign(dims, dims + S->ne);
+    if (S->ne)
+      GBTN_CUDA(cudaMemcpyAsync(S->d_edim, S->edim.data(), sizeof(int) * S->ne, cudaMemcpyHostToDevice, S->stream));
+    GBTN_CUDA(cudaStreamSynchronize(S->stream));
+  } catch (const std::exception& e) {
+    return su_fail(S, GBTN_ERR_CUDA, e.what());
+  }
+  return GBTN_OK;
+}
+
+int gbtn_su_apply_vjp(gbtn_su* S, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
+                      const double* envs, int32_t maxdim, double cutoff, int32_t normalize,
+                      const int32_t* post_edge_dims, const double* cot_out, double* cot_in, double* gate_cot) {
+  const gbtn::NvtxRange nvtx_range("gbtn_su_apply_vjp");
+  if (!S || n_gates < 0 || (n_gates > 0 && (!edges || !gates)) || !post_edge_dims || !cot_out || !cot_in)
+    return GBTN_ERR_INVALID;
+  if (S->cplx) return su_fail(S, GBTN_ERR_UNSUPPORTED, "simple update adjoint: real tensors only");
+  try {
+    cudaStream_t s = S->stream;
+    su_pull_dims(S);
+    std::vector<SuJob> jobs(n_gates);
+    std::vector<int> mark(S->nv, 0), gate_edge(S->ne, 0);
+    int D = 0;
+    for (int j = 0; j < n_gates; ++j) {
+      const int e = edges[j];
+      if (e < 0 || e >= S->ne) return su_fail(S, GBTN_ERR_INVALID, "simple update: edge out of range");
+      SuJob jb{e, S->eu[e], S->ev[e], -1, -1};
+      if (mark[jb.u] || mark[jb.v])
+        return su_fail(S, GBTN_ERR_INVALID, "simple update adjoint: the gates of one call must act on disjoint vertices");
+      mark[jb.u] = mark[jb.v] = 1;
+      gate_edge[e] = 1;
+      for (int q = S->leg_ptr[jb.u]; q < S->leg_ptr[jb.u + 1]; ++q)
+        if (S->leg_edge[q] == e) jb.pu = q - S->leg_ptr[jb.u];
+      for (int q = S->leg_ptr[jb.v]; q < S->leg_ptr[jb.v + 1]; ++q)
+        if (S->leg_edge[q] == e) jb.pv = q - S->leg_ptr[jb.v];
+      jobs[j] = jb;
+      const int dd = S->dsite[jb.u] * S->dsite[jb.v];
+      if (j == 0) D = dd;
+      if (dd != D) return su_fail(S, GBTN_ERR_INVALID, "simple update adjoint: gates of one call need equal sizes");
+    }
+    for (int e = 0; e < S->ne; ++e)
+      if (gate_edge[e] ? (post_edge_dims[e] < 1 || post_edge_dims[e] > S->chimax) : post_edge_dims[e] != S->edim[e])
+        return su_fail(S, GBTN_ERR_INVALID, "simple update adjoint: post_edge_dims do not follow the gates");
+    // sizes of every site before (current dims) and after (post dims)
+    std::vector<long long> pre_n(S->nv), post_n(S->nv);
+    long long pre_tot = 0, post_tot = 0;
+    for (int v = 0; v < S->nv; ++v) {
+      long long a = S->dsite[v], b = S->dsite[v];
+      for (int q = S->leg_ptr[v]; q < S->leg_ptr[v + 1]; ++q) {
+        a *= S->edim[S->leg_edge[q]];
+        b *= post_edge_dims[S->leg_edge[q]];
+      }
+      pre_n[v] = a;
+      post_n[v] = b;
+      pre_tot += a;
+      post_tot += b;
+    }
+    (void)pre_tot;
+    // untouched sites: the cotangent passes through
+    {
+      long long oi = 0, oo = 0;
+      for (int v = 0; v < S->nv; ++v) {
+        if (!mark[v]) std::copy(cot_out + oo, cot_out + oo + post_n[v], cot_in + oi);
+        oi += pre_n[v];
+        oo += post_n[v];
+      }
+    }
+    if (n_gates == 0) return GBTN_OK;
+    const long long gsz = (long long)D * D;
+    const int md = maxdim > 0 ? std::min(maxdim, S->chimax) : S->chimax;
+    int dmax = 1;
+    for (int dd : S->dsite) dmax = std::max(dmax, dd);
+    const int bmax = std::min(64, dmax * dmax * S->chimax);
+    const long long cap = std::max<long long>(S->cap_total, 1);
+    const int chunk = std::min(n_gates, 128);
+    // device buffers
+    std::vector<void*> owned;
+    auto dalloc = [&](size_t bytes) {
+      void* p = nullptr;
+      GBTN_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 8)));
+      owned.push_back(p);
+      return p;
+    };
+    struct Guard {
+      std::vector<void*>& v;
+      ~Guard() {
+        for (void* p : v) cudaFree(p);
+      }
+    } guard{owned};
+    double* d_gates = (double*)dalloc(sizeof(double) * gsz * (per_gate ? n_gates : 1));
+    GBTN_CUDA(cudaMemcpyAsync(d_gates, gates, sizeof(double) * gsz * (per_gate ? n_gates : 1), cudaMemcpyHostToDevice, s));
+    double* d_envs = nullptr;
+    if (envs) {
+      const long long ne2 = 2LL * S->ne * S->chimax * S->chimax;
+      d_envs = (double*)dalloc(sizeof(double) * ne2);
+      GBTN_CUDA(cudaMemcpyAsync(d_envs, envs, sizeof(double) * ne2, cudaMemcpyHostToDevice, s));
+    }
+    SuJob* d_jobs = (SuJob*)dalloc(sizeof(SuJob) * n_gates);
+    GBTN_CUDA(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SuJob) * n_gates, cudaMemcpyHostToDevice, s));
+    int* d_post = (int*)dalloc(sizeof(int) * std::max(S->ne, 1));
+    int* d_edim_fwd = (int*)dalloc(sizeof(int) * std::max(S->ne, 1));
+    if (S->ne) {
+      GBTN_CUDA(cudaMemcpyAsync(d_post, post_edge_dims, sizeof(int) * S->ne, cudaMemcpyHostToDevice, s));
+    }
+    double* d_cout = (double*)dalloc(sizeof(double) * cap);
+    double* d_cin = (double*)dalloc(sizeof(double) * cap);
+    {  // cotangents of the gates' sites into their slots (post shapes)
+      long long oo = 0;
+      for (int v = 0; v < S->nv; ++v) {
+        if (mark[v])
+          GBTN_CUDA(cudaMemcpyAsync(d_cout + S->cap_off[v], cot_out + oo, sizeof(double) * post_n[v],
+                                    cudaMemcpyHostToDevice, s));
+        oo += post_n[v];
+      }
+    }
+    double* d_q = (double*)dalloc(sizeof(double) * (size_t)chunk * 2 * gbtn::kSuSideStride);
+    double* d_js = (double*)dalloc(sizeof(double) * (size_t)chunk * gbtn::kSuJobStride);
+    double* d_full = (double*)dalloc(sizeof(double) * (size_t)chunk * gbtn::kSuFullStride);
+    double* d_sqrt = (double*)dalloc(sizeof(double) * (size_t)chunk * 2 * gbtn::kSuSqrtStride);
+    double* d_work = (double*)dalloc(sizeof(double) * (size_t)chunk * gbtn::kSuVjpStride);
+    double* d_gc = gate_cot ? (double*)dalloc(sizeof(double) * gsz * n_gates) : nullptr;
+    GBTN_CUDA(cudaMemsetAsync(S->d_status, 0, sizeof(int), s));
+    for (int j0 = 0; j0 < n_gates; j0 += chunk) {
+      SuArgs a{};
+      a.jobs = d_jobs + j0;
+      a.njobs = std::min(chunk, n_gates - j0);
+      a.leg_ptr = S->d_leg_ptr;
+      a.leg_edge = S->d_leg_edge;
+      a.edge_u = S->d_edge_u;
+      a.site_dim = S->d_dsite;
+      a.cap_off = S->d_cap_off;
+      a.tens = S->d_tens;
+      a.envs = d_envs;
+      a.gates = d_gates + (per_gate ? gsz * j0 : 0);
+      a.gate_stride = per_gate ? gsz : 0;
+      a.maxdim = md;
+      a.cutoff = cutoff;
+      a.normalize = normalize;
+      a.chimax = S->chimax;
+      a.side_scratch = d_q;
+      a.job_scratch = d_js;
+      a.bmax = bmax;
+      a.status = S->d_status;
+      a.svd_full = d_full;
+      a.side_sqrt = d_sqrt;
+      // the forward stages write the new bond dimensions into a scratch copy
+      if (S->ne)
+        GBTN_CUDA(cudaMemcpyAsync(d_edim_fwd, S->d_edim, sizeof(int) * S->ne, cudaMemcpyDeviceToDevice, s));
+      a.edim = d_edim_fwd;
+      gbtn::su_launch_fwd_stages(a, s);
+      a.edim = S->d_edim;
+      gbtn::su_launch_vjp_kernel(a, d_post, d_cout, d_cin, d_gc ? d_gc + gsz * j0 : nullptr, d_work, s);
+    }
+    int status = 0;
+    GBTN_CUDA(cudaMemcpyAsync(&status, S->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GBTN_CUDA(cudaStreamSynchronize(s));
+    if (status == 2)
+      return su_fail(S, GBTN_ERR_INVALID,
+                     "simple update adjoint: a gate's truncation differs from post_edge_dims (not the tensors the "
+                     "gates were applied to?)");
+    if (status)
+      return su_fail(S, GBTN_ERR_UNSUPPORTED,
+                     "simple update: a gate exceeds the kernel limits (site tensor, also with the bond at maxdim, "
+                     "> 8192 elements, or theta > 64 x 64)");
+    {
+      long long oi = 0;
+      for (int v = 0; v < S->nv; ++v) {
+        if (mark[v])
+          GBTN_CUDA(cudaMemcpyAsync(cot_in + oi, d_cin + S->cap_off[v], sizeof(double) * pre_n[v],
+                                    cudaMemcpyDeviceToHost, s));
+        oi += pre_n[v];
+      }
+    }
+    if (gate_cot)
+      GBTN_CUDA(cudaMemcpyAsync(gate_cot, d_gc, sizeof(double) * gsz * n_gates, cudaMemcpyDeviceToHost, s));
+    GBTN_CUDA(cudaStreamSynchronize(s));
   } catch (const std::exception& e) {
     return su_fail(S, GBTN_ERR_CUDA, e.what());
   }

@@ -52,12 +52,7 @@ class SimpleUpdateState:
         net.tensors = net.unflat(out[:n])
         return net
 
-    def apply(self, gates, edges, envs=None, maxdim=None, cutoff=None, normalize=False):
-        """Apply gates[j] on edges[j] in order.  ``gates`` is one matrix (shared)
-        or a list.  ``envs``: None or a list of 2*ne message matrices (the BP
-        environment).  Returns (truncation errors, kept singular values)."""
-        edges = np.ascontiguousarray(edges, dtype=np.int32)
-        n = len(edges)
+    def _pack(self, gates, envs):
         shared = not isinstance(gates, (list, tuple))
         glist = [gates] if shared else list(gates)
         if not self.complex and (any(np.iscomplexobj(x) for x in glist)
@@ -72,6 +67,15 @@ class SimpleUpdateState:
             for de, m in enumerate(envs):
                 c = m.shape[0]
                 env_arr[de * cm * cm:de * cm * cm + c * c] = np.asarray(m, dt).reshape(-1, order="F")
+        return shared, g, env_arr
+
+    def apply(self, gates, edges, envs=None, maxdim=None, cutoff=None, normalize=False):
+        """Apply gates[j] on edges[j] in order.  ``gates`` is one matrix (shared)
+        or a list.  ``envs``: None or a list of 2*ne message matrices (the BP
+        environment).  Returns (truncation errors, kept singular values)."""
+        edges = np.ascontiguousarray(edges, dtype=np.int32)
+        n = len(edges)
+        shared, g, env_arr = self._pack(gates, envs)
         md = int(maxdim) if maxdim else self.chi_max
         te = np.zeros(max(n, 1))
         sv = np.zeros(max(n * md, 1))
@@ -81,6 +85,95 @@ class SimpleUpdateState:
             -1.0 if cutoff is None else float(cutoff),
             1 if normalize else 0, dptr(te), dptr(sv)))
         return te[:n], sv[:n * md].reshape(n, md)
+
+    def set_state(self, net: TensorNetwork):
+        """Replace the bond dimensions and tensors by those of ``net`` (same graph)."""
+        dims = np.ascontiguousarray(net.edge_dims, dtype=np.int32)
+        if len(dims):
+            check(self.ctx.handle, self.lib.gbtn_su_set_edge_dims(self.handle, iptr(dims)))
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(t, self.dtype).reshape(-1, order="F")
+                                                    for t in net.tensors]))
+        check(self.ctx.handle, self.lib.gbtn_su_set_factors(self.handle, dptr(flat.view(np.float64))))
+
+    def apply_vjp(self, gates, edges, post_dims, cot, envs=None, maxdim=None, cutoff=None, normalize=False):
+        """Adjoint of ``apply`` for gates on disjoint vertices, at the current
+        tensors (the gates' inputs).  ``cot``: per vertex dL/d(tensor after the
+        gates) with bond dimensions ``post_dims``.  Returns (dL/d(current
+        tensors) per vertex, dL/dG per gate as an (n, D, D) array)."""
+        if self.complex:
+            raise _lib.Unsupported(2, "simple update adjoint: real tensors only")
+        edges = np.ascontiguousarray(edges, dtype=np.int32)
+        n = len(edges)
+        shared, g, env_arr = self._pack(gates, envs)
+        post = np.ascontiguousarray(post_dims, dtype=np.int32)
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(t, float).reshape(-1, order="F") for t in cot]))
+        pre_dims = self.edge_dims()
+        pre = TensorNetwork(self.tn.nv, self.tn.edges, self.tn.site_dims, pre_dims, None, self.tn.legs,
+                            self.tn.vertex_network, self.tn.n_networks)
+        out = np.zeros(max(sum(pre.size(v) for v in range(pre.nv)), 1))
+        D = self.tn.site_dims[self.tn.edges[int(edges[0])][0]] * self.tn.site_dims[self.tn.edges[int(edges[0])][1]] \
+            if n else 1
+        gc = np.zeros(max(n * D * D, 1))
+        md = int(maxdim) if maxdim else self.chi_max
+        check(self.ctx.handle, self.lib.gbtn_su_apply_vjp(
+            self.handle, n, iptr(edges), dptr(g), 0 if shared else 1,
+            None if env_arr is None else dptr(env_arr), md, -1.0 if cutoff is None else float(cutoff),
+            1 if normalize else 0, iptr(post), dptr(flat), dptr(out), dptr(gc)))
+        n_el = sum(pre.size(v) for v in range(pre.nv))
+        return pre.unflat(out[:n_el]), gc[:n * D * D].reshape(n, D, D).transpose(0, 2, 1)
+
+    def apply_with_pullback(self, gates, edges, envs=None, maxdim=None, cutoff=None, normalize=False):
+        """``apply`` that also returns its pullback: (truncation errors, kept
+        singular values, pullback), pullback(cot) -> (dL/d(tensors before the
+        gates) per vertex, dL/dG per gate (n, D, D)).  The gates run in batches
+        of consecutive vertex-disjoint gates (the order ``apply`` gives them);
+        the state before each batch is kept on the host for the pullback,
+        which leaves the state where ``apply`` left it."""
+        edges = [int(e) for e in edges]
+        shared = not isinstance(gates, (list, tuple))
+        glist = [gates] * len(edges) if shared else list(gates)
+        batches, cur, used = [], [], set()
+        for j, e in enumerate(edges):
+            u, v = self.tn.edges[e]
+            if u in used or v in used:
+                batches.append(cur)
+                cur, used = [], set()
+            cur.append(j)
+            used.update((u, v))
+        if cur:
+            batches.append(cur)
+        saved, tes, svs = [], [], []
+        for b in batches:
+            saved.append(self.network())
+            te, sv = self.apply([glist[j] for j in b], [edges[j] for j in b], envs=envs, maxdim=maxdim,
+                                cutoff=cutoff, normalize=normalize)
+            tes.append(te)
+            svs.append(sv)
+        final = self.network()
+        order = [j for b in batches for j in b]
+
+        def pullback(cot):
+            cot = [np.asarray(c, float) for c in cot]
+            gcs = [None] * len(edges)
+            post = final.edge_dims
+            for b, net in zip(reversed(batches), reversed(saved)):
+                self.set_state(net)
+                cot, gc = self.apply_vjp([glist[j] for j in b], [edges[j] for j in b], post, cot, envs=envs,
+                                         maxdim=maxdim, cutoff=cutoff, normalize=normalize)
+                for i, j in enumerate(b):
+                    gcs[j] = gc[i]
+                post = net.edge_dims
+            self.set_state(final)
+            return cot, np.array(gcs)
+
+        te = np.zeros(len(edges))
+        sv = None
+        te[order] = np.concatenate(tes) if tes else []
+        if svs:
+            allsv = np.concatenate(svs)
+            sv = np.zeros_like(allsv)
+            sv[order] = allsv
+        return te, sv, pullback
 
     def close(self):
         if getattr(self, "handle", None):

@@ -1,0 +1,147 @@
+"""Hand-written adjoint of the simple update (gbtn_su_apply_vjp) against
+central finite differences of the oracle's simple_update_bp restatement
+(src/apply.jl:33-95; the reference itself has no derivative).
+
+The factors a gate leaves are gauge dependent (a sign per kept singular
+vector, paired across the bond), so the loss is gauge invariant: L = <W, psi>
+for a fixed random W and psi the contracted state vector of the network after
+the gates.  The test computes dL/d(tensors after the gates) by contracting W
+with the other tensors, pulls it back through the GPU adjoint, and compares
+the directional derivative <G, D> with (L(A + hD) - L(A - hD)) / 2h of the
+oracle for unit directions D (h = 1e-5: truncation ~h^2 and rounding
+~1e-16 / h, both below 1e-9 relative here); 1e-6 relative, the tolerance of
+the BP gradients' finite-difference tests.  The same for the gate matrices."""
+import numpy as np
+import pytest
+
+import bp_oracle as O
+import gbtn
+from test_gpu_su import gpu_net, oracle_gate, random_gate
+
+pytestmark = pytest.mark.gpu
+
+H = 1e-5
+RTOL = 1e-6
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(lib_built):
+    yield
+
+
+def psi(g, A):
+    ops, lid = [], {e: 20 + e for e in range(g.ne)}
+    for v in range(g.nv):
+        ops += [A[v], [v] + [lid[e] for e in g.legs[v]]]
+    return np.einsum(*ops, list(range(g.nv)), optimize=True)
+
+
+def psi_cotangents(g, A, W):
+    """d<W, psi>/dA_v for every v: W contracted with every other tensor."""
+    lid = {e: 20 + e for e in range(g.ne)}
+    out = []
+    for v in range(g.nv):
+        ops = [W, list(range(g.nv))]
+        for w in range(g.nv):
+            if w != v:
+                ops += [A[w], [w] + [lid[e] for e in g.legs[w]]]
+        out.append(np.einsum(*ops, [v] + [lid[e] for e in g.legs[v]], optimize=True))
+    return out
+
+
+def oracle_layers(g, A, layers, envs, maxdim, cutoff, normalize):
+    """Apply layers[i] = [(edge, gate), ...] in order with the oracle."""
+    for layer in layers:
+        for e, gate in layer:
+            g, A, _, _ = oracle_gate(g, A, gate, e, envs=envs, maxdim=maxdim, cutoff=cutoff, normalize=normalize)
+    return g, A
+
+
+def unit(rng, shapes):
+    d = [rng.standard_normal(s) for s in shapes]
+    nrm = np.sqrt(sum(np.sum(x * x) for x in d))
+    return [x / nrm for x in d]
+
+
+def check_case(g, A, layers, envs=None, maxdim=3, cutoff=None, normalize=False, seed=0):
+    rng = np.random.default_rng(seed)
+    g_out, A_out = oracle_layers(g, A, layers, envs, maxdim, cutoff, normalize)
+    W = rng.standard_normal(psi(g_out, A_out).shape)
+    loss = lambda AA, lay: float(np.sum(W * psi(*oracle_layers(g, AA, lay, envs, maxdim, cutoff, normalize))))
+
+    st = gbtn.SimpleUpdateState(gpu_net(g, A), chi_max=4)
+    edges = [e for layer in layers for e, _ in layer]
+    gates = [gt for layer in layers for _, gt in layer]
+    _, _, pull = st.apply_with_pullback(gates, edges, envs=envs, maxdim=maxdim, cutoff=cutoff, normalize=normalize)
+    out = st.network()
+    assert list(out.edge_dims) == list(g_out.edge_dims)
+    cot = psi_cotangents(g_out, out.tensors, W)
+    G, Gg = pull(cot)
+    assert [x.shape for x in G] == [a.shape for a in A]
+    # the state is where apply left it
+    np.testing.assert_array_equal(np.concatenate([t.ravel() for t in st.network().tensors]),
+                                  np.concatenate([t.ravel() for t in out.tensors]))
+    for s in range(2):
+        D = unit(rng, [a.shape for a in A])
+        fd = (loss([a + H * d for a, d in zip(A, D)], layers) - loss([a - H * d for a, d in zip(A, D)], layers)) / (2 * H)
+        an = sum(float(np.sum(x * d)) for x, d in zip(G, D))
+        assert an == pytest.approx(fd, rel=RTOL, abs=1e-9), ("tensors", s)
+    # gate cotangents: a direction per gate
+    Dg = unit(rng, [gt.shape for gt in gates])
+
+    def shifted(sgn):
+        it = iter(Dg)
+        return [[(e, gt + sgn * H * next(it)) for e, gt in layer] for layer in layers]
+    fd = (loss(A, shifted(1)) - loss(A, shifted(-1))) / (2 * H)
+    an = sum(float(np.sum(x * d)) for x, d in zip(Gg, Dg))
+    assert an == pytest.approx(fd, rel=RTOL, abs=1e-9), "gates"
+    st.close()
+
+
+@pytest.mark.parametrize("normalize", [False, True])
+@pytest.mark.parametrize("e", [0, 5])
+def test_single_gate_adjoint(e, normalize):
+    """One gate, truncated to maxdim = 3 of up to 8 singular values (the
+    discarded ones enter the adjoint), without environments."""
+    g = O.square_lattice(3, 3, chi=2)
+    A = O.random_network(g, 40 + e)
+    check_case(g, A, [[(e, random_gate(e))]], maxdim=3, normalize=normalize, seed=e)
+
+
+def test_gate_layer_with_bp_environments():
+    """A checkerboard layer of vertex-disjoint gates in one batch, with the
+    BP messages of the state as (constant) environments, a cutoff and
+    normalisation (BP-gauged TEBD, tebd.jl with envs)."""
+    g = O.square_lattice(3, 3, chi=2)
+    A = O.random_network(g, 7, unit_norm=True)
+    envs, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=200, schedule="parallel")
+    layer = [(e, random_gate(10 + e)) for e in (0, 5, 10, 4)]
+    assert len({v for e, _ in layer for v in g.edges[e]}) == 8  # disjoint
+    check_case(g, A, [layer], envs=envs, maxdim=3, cutoff=1e-10, normalize=True, seed=3)
+
+
+def test_pullback_through_a_gate_sequence():
+    """Two layers sharing vertices: the pullback restores each batch's saved
+    input state and runs the adjoints in reverse."""
+    g = O.square_lattice(3, 2, chi=2)
+    A = O.random_network(g, 11)
+    layers = [[(0, random_gate(1)), (6, random_gate(2))], [(1, random_gate(3))], [(0, random_gate(4))]]
+    check_case(g, A, layers, maxdim=4, normalize=True, seed=5)
+
+
+def test_adjoint_refusals():
+    g = O.square_lattice(2, 2, chi=2)
+    A = O.random_network(g, 3)
+    st = gbtn.SimpleUpdateState(gpu_net(g, A), chi_max=4)
+    cot = [np.zeros_like(a) for a in A]
+    with pytest.raises(gbtn.InvalidArgument, match="disjoint"):
+        st.apply_vjp([random_gate(1), random_gate(2)], [0, 1], g.edge_dims, cot)
+    with pytest.raises(gbtn.InvalidArgument):  # a truncation that does not match the gate's
+        st.apply_vjp(random_gate(1), [0], [1] + list(g.edge_dims[1:]), cot, maxdim=4)
+    st.close()
+    gc = O.square_lattice(2, 2, chi=2)
+    Ac = O.random_network(gc, 3, dtype=np.complex128)
+    sc = gbtn.SimpleUpdateState(gpu_net(gc, Ac), chi_max=4)
+    with pytest.raises(gbtn.Unsupported):
+        sc.apply_vjp(random_gate(1), [0], gc.edge_dims, [np.zeros_like(a) for a in Ac])
+    sc.close()
