@@ -145,3 +145,52 @@ def test_adjoint_refusals():
     with pytest.raises(gbtn.Unsupported):
         sc.apply_vjp(random_gate(1), [0], gc.edge_dims, [np.zeros_like(a) for a in Ac])
     sc.close()
+
+
+def test_bp_energy_gradient_through_a_tebd_step():
+    """d<H>_BP/dA0 through one Trotter step: A0 -> four checkerboard layers of
+    Heisenberg gates exp(-0.1 h) (simple update, maxdim 4, normalised) -> A1
+    -> BP energy.  The BP adjoint gives dE/dA1 (implicit, at the converged
+    messages), the simple-update pullback carries it to A0; against central
+    differences of the oracle (its simple update, then its BP fixed point and
+    two-site energy)."""
+    torch = pytest.importorskip("torch")  # noqa: F841 (bp_autograd needs it)
+    import bp_autograd as AG
+    from gbtn.operators import HEISENBERG
+    g = O.square_lattice(3, 3, chi=2)
+    A = O.random_network(g, 17, unit_norm=True)
+    hm = AG.heisenberg_matrix()
+    w, U = np.linalg.eigh(hm)
+    gate = (U * np.exp(-0.1 * w)) @ U.T
+    colours = [[0, 5, 10], [2, 7, 11], [1, 3, 4], [6, 8, 9]]  # checkerboard classes of the 3x3 edges
+    for c in colours:
+        assert len({v for e in c for v in g.edges[e]}) == 2 * len(c)
+    layers = [[(e, gate) for e in c] for c in colours]
+    st = gbtn.SimpleUpdateState(gpu_net(g, A), chi_max=4)
+    edges = [e for c in colours for e in c]
+    _, _, pull = st.apply_with_pullback(gate, edges, maxdim=4, normalize=True)
+    net1 = st.network()
+    bpc = gbtn.BeliefPropagationCache(net1).update(maxiter=500, schedule="parallel")
+    E, G1 = bpc.energy2_grad(HEISENBERG, mode="implicit", tol=1e-13)
+    G0, Gg = pull(G1)
+
+    def energy(AA, gt=gate):
+        lay = [[(e, gt) for e in c] for c in colours]
+        g1, A1 = oracle_layers(g, AA, lay, None, 4, None, True)
+        m, _, _ = O.bp_update(g1, A1, O.identity_messages(g1), maxiter=500, schedule="parallel")
+        return float(np.sum(O.expect2(g1, A1, m, hm)))
+
+    assert E == pytest.approx(energy(A), rel=1e-10)
+    rng = np.random.default_rng(8)
+    D = unit(rng, [a.shape for a in A])
+    h = 1e-4
+    fd = (energy([a + h * d for a, d in zip(A, D)]) - energy([a - h * d for a, d in zip(A, D)])) / (2 * h)
+    an = sum(float(np.sum(x * d)) for x, d in zip(G0, D))
+    assert an == pytest.approx(fd, rel=RTOL)
+    # one shared gate: its cotangent is the sum over its applications
+    Dg = rng.standard_normal(gate.shape)
+    Dg /= np.linalg.norm(Dg)
+    fdg = (energy(A, gate + h * Dg) - energy(A, gate - h * Dg)) / (2 * h)
+    assert float(np.sum(Gg.sum(axis=0) * Dg)) == pytest.approx(fdg, rel=RTOL)
+    bpc.close()
+    st.close()
