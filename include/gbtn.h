@@ -343,6 +343,24 @@ int gbtn_su_set_edge_dims(gbtn_su* su, const int32_t* dims);
 int gbtn_su_apply_vjp(gbtn_su* su, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
                       const double* envs, int32_t maxdim, double cutoff, int32_t normalize,
                       const int32_t* post_edge_dims, const double* cot_out, double* cot_in, double* gate_cot);
+/* gbtn_su_apply that also records a tape for the adjoint of the whole gate
+ * sequence (real tensors): the state before every batch of consecutive
+ * vertex-disjoint gates (device copies of the tensors and bond dimensions),
+ * the final state, the gates, environments and options.  Memory: one copy of
+ * the state's tensor storage per batch, plus one. */
+typedef struct gbtn_su_tape gbtn_su_tape;
+int gbtn_su_apply_taped(gbtn_su* su, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
+                        const double* envs, int32_t maxdim, double cutoff, int32_t normalize, double* truncerr,
+                        double* svals, gbtn_su_tape** tape);
+/* The pullback of a taped apply: cot_out = dL/d(tensors it left), in their
+ * shapes; cot_in = dL/d(tensors before it), in those shapes; gate_cot
+ * (may be NULL): n_gates (du dv)^2 matrices dL/dG in the order given.  The
+ * batches run backwards on the device (each batch's saved state restored, the
+ * cotangents kept in device memory); the state is left as the taped apply
+ * left it.  The tape can be pulled back more than once. */
+int gbtn_su_tape_vjp(gbtn_su* su, const gbtn_su_tape* tape, const double* cot_out, double* cot_in,
+                     double* gate_cot);
+int gbtn_su_tape_destroy(gbtn_su_tape* tape);
 
 /* ---- energies and gradients (FP64) ------------------------------------------ */
 /* Two-site energy sum_e sum_t coef[t] <O_t (x) O_t>_e with BP reduced density

@@ -2055,6 +2055,147 @@ int su_fail(gbtn_su* S, int code, const char* msg) {
 using gbtn::SuArgs;
 using gbtn::SuJob;
 
+// The record of a taped gbtn_su_apply: per batch of vertex-disjoint gates
+// the tensors and bond dimensions before it (device snapshots), the final
+// state, and the gates, environments and options, for gbtn_su_tape_vjp.
+struct gbtn_su_tape {
+  gbtn_su* su = nullptr;
+  int n_gates = 0, per_gate = 0, md = 0, normalize = 0, bmax = 0;
+  long long gsz = 0;
+  double cutoff = -1.0;
+  double* d_gates = nullptr;
+  double* d_envs = nullptr;
+  SuJob* d_jobs = nullptr;
+  std::vector<std::pair<int, int>> batches;
+  std::vector<double*> d_tens_snap;  // before batch b; the last one after all
+  std::vector<int*> d_edim_snap;
+  std::vector<int> dims_before;
+  ~gbtn_su_tape() {
+    for (void* p : {(void*)d_gates, (void*)d_envs, (void*)d_jobs})
+      if (p) cudaFree(p);
+    for (double* p : d_tens_snap) cudaFree(p);
+    for (int* p : d_edim_snap) cudaFree(p);
+  }
+};
+
+namespace {
+
+void tape_snapshot(gbtn_su* S, gbtn_su_tape* T, cudaStream_t s) {
+  double* t = nullptr;
+  int* d = nullptr;
+  GBTN_CUDA(cudaMalloc(&t, sizeof(double) * std::max<long long>(S->cap_total, 1)));
+  T->d_tens_snap.push_back(t);
+  GBTN_CUDA(cudaMalloc(&d, sizeof(int) * std::max(S->ne, 1)));
+  T->d_edim_snap.push_back(d);
+  GBTN_CUDA(cudaMemcpyAsync(t, S->d_tens, sizeof(double) * S->cap_total, cudaMemcpyDeviceToDevice, s));
+  if (S->ne) GBTN_CUDA(cudaMemcpyAsync(d, S->d_edim, sizeof(int) * S->ne, cudaMemcpyDeviceToDevice, s));
+}
+
+// Scratch of the adjoint for up to `chunk` gates at a time.
+struct VjpScratch {
+  std::vector<void*> owned;
+  double *q = nullptr, *js = nullptr, *full = nullptr, *sq = nullptr, *work = nullptr;
+  int* edim_fwd = nullptr;
+  int chunk = 0;
+  VjpScratch(const gbtn_su* S, int max_jobs) {
+    chunk = std::max(1, std::min(max_jobs, 128));
+    q = (double*)get(sizeof(double) * (size_t)chunk * 2 * gbtn::kSuSideStride);
+    js = (double*)get(sizeof(double) * (size_t)chunk * gbtn::kSuJobStride);
+    full = (double*)get(sizeof(double) * (size_t)chunk * gbtn::kSuFullStride);
+    sq = (double*)get(sizeof(double) * (size_t)chunk * 2 * gbtn::kSuSqrtStride);
+    work = (double*)get(sizeof(double) * (size_t)chunk * gbtn::kSuVjpStride);
+    edim_fwd = (int*)get(sizeof(int) * std::max(S->ne, 1));
+  }
+  void* get(size_t bytes) {
+    void* p = nullptr;
+    GBTN_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 8)));
+    owned.push_back(p);
+    return p;
+  }
+  ~VjpScratch() {
+    for (void* p : owned) cudaFree(p);
+  }
+};
+
+// Adjoint of one batch of vertex-disjoint gates at the state's current
+// tensors and bond dimensions.  Cotangents: device, capacity layout (cot_out
+// and cot_in may be the same buffer: each gate reads its sites' cotangents
+// before it writes them, and no other gate touches them).
+void su_vjp_batch(gbtn_su* S, const SuJob* d_jobs, int njobs, const double* d_gates, int per_gate, long long gsz,
+                  const double* d_envs, int md, double cutoff, int normalize, int bmax, const int* d_post,
+                  const double* d_cot_out, double* d_cot_in, double* d_gc, VjpScratch& w) {
+  cudaStream_t s = S->stream;
+  for (int j0 = 0; j0 < njobs; j0 += w.chunk) {
+    SuArgs a{};
+    a.jobs = d_jobs + j0;
+    a.njobs = std::min(w.chunk, njobs - j0);
+    a.leg_ptr = S->d_leg_ptr;
+    a.leg_edge = S->d_leg_edge;
+    a.edge_u = S->d_edge_u;
+    a.site_dim = S->d_dsite;
+    a.cap_off = S->d_cap_off;
+    a.tens = S->d_tens;
+    a.envs = d_envs;
+    a.gates = d_gates + (per_gate ? gsz * j0 : 0);
+    a.gate_stride = per_gate ? gsz : 0;
+    a.maxdim = md;
+    a.cutoff = cutoff;
+    a.normalize = normalize;
+    a.chimax = S->chimax;
+    a.side_scratch = w.q;
+    a.job_scratch = w.js;
+    a.bmax = bmax;
+    a.status = S->d_status;
+    a.svd_full = w.full;
+    a.side_sqrt = w.sq;
+    // the forward stages write the new bond dimensions into a scratch copy
+    if (S->ne)
+      GBTN_CUDA(cudaMemcpyAsync(w.edim_fwd, S->d_edim, sizeof(int) * S->ne, cudaMemcpyDeviceToDevice, s));
+    a.edim = w.edim_fwd;
+    gbtn::su_launch_fwd_stages(a, s);
+    a.edim = S->d_edim;
+    gbtn::su_launch_vjp_kernel(a, d_post, d_cot_out, d_cot_in, d_gc ? d_gc + gsz * j0 : nullptr, w.work, s);
+  }
+}
+
+int su_bmax(const gbtn_su* S) {
+  int dmax = 1;
+  for (int dd : S->dsite) dmax = std::max(dmax, dd);
+  return std::min(64, dmax * dmax * S->chimax);
+}
+
+// Host tensors (concatenated in vertex order with bond dimensions dims) into
+// a capacity-layout device buffer (host_in) or out of it (host_out), through
+// one staging copy.
+void su_scatter(gbtn_su* S, const std::vector<int>& dims, const double* host_in, double* host_out, double* dev) {
+  const bool to_device = host_in != nullptr;
+  cudaStream_t s = S->stream;
+  std::vector<long long> n(S->nv);
+  long long tot = 0;
+  for (int v = 0; v < S->nv; ++v) {
+    long long a = S->dsite[v];
+    for (int q = S->leg_ptr[v]; q < S->leg_ptr[v + 1]; ++q) a *= dims[S->leg_edge[q]];
+    n[v] = a;
+    tot += a;
+  }
+  double* stage = nullptr;
+  GBTN_CUDA(cudaMalloc(&stage, sizeof(double) * std::max<long long>(tot, 1)));
+  std::unique_ptr<double, decltype(&cudaFree)> guard(stage, cudaFree);
+  if (to_device) GBTN_CUDA(cudaMemcpyAsync(stage, host_in, sizeof(double) * tot, cudaMemcpyHostToDevice, s));
+  long long off = 0;
+  for (int v = 0; v < S->nv; ++v) {
+    if (to_device)
+      GBTN_CUDA(cudaMemcpyAsync(dev + S->cap_off[v], stage + off, sizeof(double) * n[v], cudaMemcpyDeviceToDevice, s));
+    else
+      GBTN_CUDA(cudaMemcpyAsync(stage + off, dev + S->cap_off[v], sizeof(double) * n[v], cudaMemcpyDeviceToDevice, s));
+    off += n[v];
+  }
+  if (!to_device) GBTN_CUDA(cudaMemcpyAsync(host_out, stage, sizeof(double) * tot, cudaMemcpyDeviceToHost, s));
+  GBTN_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace
+
 extern "C" {
 
 int gbtn_su_create(gbtn_ctx* ctx, const gbtn_graph_desc* g, int32_t chi_max, gbtn_su** out) {
@@ -2170,12 +2311,11 @@ int gbtn_su_get_factors(gbtn_su* S, double* ket, int64_t capacity) {
   return GBTN_OK;
 }
 
-int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
-                  const double* envs, int32_t maxdim, double cutoff, int32_t normalize, double* truncerr,
-                  double* svals) {
-  const gbtn::NvtxRange nvtx_range("gbtn_su_apply");
+static int su_apply_impl(gbtn_su* S, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
+                         const double* envs, int32_t maxdim, double cutoff, int32_t normalize, double* truncerr,
+                         double* svals, gbtn_su_tape* tape) {
   if (!S || n_gates < 0 || (n_gates > 0 && (!edges || !gates))) return GBTN_ERR_INVALID;
-  if (n_gates == 0) return GBTN_OK;
+  if (n_gates == 0) return tape ? GBTN_ERR_INVALID : GBTN_OK;
   try {
     cudaStream_t s = S->stream;
     int D = 0;
@@ -2243,7 +2383,9 @@ int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const doubl
     for (int dd : S->dsite) dmax = std::max(dmax, dd);
     const int bmax = std::min(64, dmax * dmax * S->chimax);
     GBTN_CUDA(cudaMemsetAsync(S->d_status, 0, sizeof(int), s));
+    if (tape) tape->dims_before = S->edim;
     for (auto& b : batches) {
+      if (tape) tape_snapshot(S, tape, s);
       SuArgs a{};
       a.jobs = d_jobs + b.first;
       a.njobs = b.second - b.first;
@@ -2272,6 +2414,21 @@ int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const doubl
       else
         gbtn::su_launch(a, s);
     }
+    if (tape) {
+      tape_snapshot(S, tape, s);
+      tape->su = S;
+      tape->n_gates = n_gates;
+      tape->per_gate = per_gate;
+      tape->md = md;
+      tape->cutoff = cutoff;
+      tape->normalize = normalize;
+      tape->bmax = bmax;
+      tape->gsz = gsz;
+      tape->batches = batches;
+      tape->d_gates = g_guard.release();
+      tape->d_envs = e_guard.release();
+      tape->d_jobs = j_guard.release();
+    }
     int status = 0;
     GBTN_CUDA(cudaMemcpyAsync(&status, S->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
     std::vector<double> te(n_gates), sv((size_t)n_gates * md);
@@ -2289,6 +2446,93 @@ int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const doubl
       for (int j = 0; j < n_gates; ++j)
         for (int i = 0; i < maxdim; ++i) svals[(size_t)j * maxdim + i] = i < md ? sv[(size_t)j * md + i] : 0.0;
     su_pull_dims(S);
+  } catch (const std::exception& e) {
+    return su_fail(S, GBTN_ERR_CUDA, e.what());
+  }
+  return GBTN_OK;
+}
+
+int gbtn_su_apply(gbtn_su* S, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
+                  const double* envs, int32_t maxdim, double cutoff, int32_t normalize, double* truncerr,
+                  double* svals) {
+  const gbtn::NvtxRange nvtx_range("gbtn_su_apply");
+  return su_apply_impl(S, n_gates, edges, gates, per_gate, envs, maxdim, cutoff, normalize, truncerr, svals, nullptr);
+}
+
+int gbtn_su_apply_taped(gbtn_su* S, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
+                        const double* envs, int32_t maxdim, double cutoff, int32_t normalize, double* truncerr,
+                        double* svals, gbtn_su_tape** tape) {
+  const gbtn::NvtxRange nvtx_range("gbtn_su_apply_taped");
+  if (!tape) return GBTN_ERR_INVALID;
+  *tape = nullptr;
+  if (S && S->cplx) return su_fail(S, GBTN_ERR_UNSUPPORTED, "simple update adjoint: real tensors only");
+  gbtn_su_tape* T = nullptr;
+  try {
+    T = new gbtn_su_tape();
+  } catch (const std::bad_alloc&) {
+    return su_fail(S, GBTN_ERR_NOMEM, "host allocation failed");
+  }
+  const int rc = su_apply_impl(S, n_gates, edges, gates, per_gate, envs, maxdim, cutoff, normalize, truncerr, svals, T);
+  if (rc != GBTN_OK) {
+    if (S) cudaStreamSynchronize(S->stream);
+    delete T;
+    return rc;
+  }
+  *tape = T;
+  return GBTN_OK;
+}
+
+// Valid after the state was destroyed (the tape does not use it here;
+// cudaFree waits for the device).
+int gbtn_su_tape_destroy(gbtn_su_tape* T) {
+  delete T;
+  return GBTN_OK;
+}
+
+int gbtn_su_tape_vjp(gbtn_su* S, const gbtn_su_tape* T, const double* cot_out, double* cot_in, double* gate_cot) {
+  const gbtn::NvtxRange nvtx_range("gbtn_su_tape_vjp");
+  if (!S || !T || !cot_out || !cot_in) return GBTN_ERR_INVALID;
+  if (T->su != S) return su_fail(S, GBTN_ERR_INVALID, "simple update adjoint: the tape belongs to another state");
+  try {
+    cudaStream_t s = S->stream;
+    const int nb = (int)T->batches.size();
+    std::vector<int> final_dims(S->ne);
+    if (S->ne)
+      GBTN_CUDA(cudaMemcpyAsync(final_dims.data(), T->d_edim_snap[nb], sizeof(int) * S->ne, cudaMemcpyDeviceToHost, s));
+    GBTN_CUDA(cudaStreamSynchronize(s));
+    const long long cap = std::max<long long>(S->cap_total, 1);
+    double* d_cot = nullptr;
+    GBTN_CUDA(cudaMalloc(&d_cot, sizeof(double) * cap));
+    std::unique_ptr<double, decltype(&cudaFree)> c_guard(d_cot, cudaFree);
+    double* d_gc = nullptr;
+    GBTN_CUDA(cudaMalloc(&d_gc, sizeof(double) * std::max<long long>(T->gsz * T->n_gates, 1)));
+    std::unique_ptr<double, decltype(&cudaFree)> gc_guard(d_gc, cudaFree);
+    su_scatter(S, final_dims, cot_out, nullptr, d_cot);
+    int maxb = 1;
+    for (auto& b : T->batches) maxb = std::max(maxb, b.second - b.first);
+    VjpScratch w(S, maxb);
+    GBTN_CUDA(cudaMemsetAsync(S->d_status, 0, sizeof(int), s));
+    for (int b = nb - 1; b >= 0; --b) {
+      const auto& bt = T->batches[b];
+      GBTN_CUDA(cudaMemcpyAsync(S->d_tens, T->d_tens_snap[b], sizeof(double) * S->cap_total, cudaMemcpyDeviceToDevice, s));
+      if (S->ne)
+        GBTN_CUDA(cudaMemcpyAsync(S->d_edim, T->d_edim_snap[b], sizeof(int) * S->ne, cudaMemcpyDeviceToDevice, s));
+      su_vjp_batch(S, T->d_jobs + bt.first, bt.second - bt.first, T->d_gates + (T->per_gate ? T->gsz * bt.first : 0),
+                   T->per_gate, T->gsz, T->d_envs, T->md, T->cutoff, T->normalize, T->bmax, T->d_edim_snap[b + 1],
+                   d_cot, d_cot, d_gc + T->gsz * bt.first, w);
+    }
+    // back to the state the taped apply left
+    GBTN_CUDA(cudaMemcpyAsync(S->d_tens, T->d_tens_snap[nb], sizeof(double) * S->cap_total, cudaMemcpyDeviceToDevice, s));
+    if (S->ne) GBTN_CUDA(cudaMemcpyAsync(S->d_edim, T->d_edim_snap[nb], sizeof(int) * S->ne, cudaMemcpyDeviceToDevice, s));
+    S->edim = final_dims;
+    int status = 0;
+    GBTN_CUDA(cudaMemcpyAsync(&status, S->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GBTN_CUDA(cudaStreamSynchronize(s));
+    if (status) return su_fail(S, GBTN_ERR_NUMERIC, "simple update adjoint: a recomputed gate differs from the tape");
+    su_scatter(S, T->dims_before, nullptr, cot_in, d_cot);
+    if (gate_cot)
+      GBTN_CUDA(cudaMemcpyAsync(gate_cot, d_gc, sizeof(double) * T->gsz * T->n_gates, cudaMemcpyDeviceToHost, s));
+    GBTN_CUDA(cudaStreamSynchronize(s));
   } catch (const std::exception& e) {
     return su_fail(S, GBTN_ERR_CUDA, e.what());
   }
@@ -2341,142 +2585,64 @@ int gbtn_su_apply_vjp(gbtn_su* S, int32_t n_gates, const int32_t* edges, const d
       if (j == 0) D = dd;
       if (dd != D) return su_fail(S, GBTN_ERR_INVALID, "simple update adjoint: gates of one call need equal sizes");
     }
+    std::vector<int> post(post_edge_dims, post_edge_dims + S->ne);
     for (int e = 0; e < S->ne; ++e)
-      if (gate_edge[e] ? (post_edge_dims[e] < 1 || post_edge_dims[e] > S->chimax) : post_edge_dims[e] != S->edim[e])
+      if (gate_edge[e] ? (post[e] < 1 || post[e] > S->chimax) : post[e] != S->edim[e])
         return su_fail(S, GBTN_ERR_INVALID, "simple update adjoint: post_edge_dims do not follow the gates");
-    // sizes of every site before (current dims) and after (post dims)
-    std::vector<long long> pre_n(S->nv), post_n(S->nv);
-    long long pre_tot = 0, post_tot = 0;
-    for (int v = 0; v < S->nv; ++v) {
-      long long a = S->dsite[v], b = S->dsite[v];
-      for (int q = S->leg_ptr[v]; q < S->leg_ptr[v + 1]; ++q) {
-        a *= S->edim[S->leg_edge[q]];
-        b *= post_edge_dims[S->leg_edge[q]];
-      }
-      pre_n[v] = a;
-      post_n[v] = b;
-      pre_tot += a;
-      post_tot += b;
-    }
-    (void)pre_tot;
-    // untouched sites: the cotangent passes through
-    {
-      long long oi = 0, oo = 0;
-      for (int v = 0; v < S->nv; ++v) {
-        if (!mark[v]) std::copy(cot_out + oo, cot_out + oo + post_n[v], cot_in + oi);
-        oi += pre_n[v];
-        oo += post_n[v];
-      }
-    }
-    if (n_gates == 0) return GBTN_OK;
-    const long long gsz = (long long)D * D;
-    const int md = maxdim > 0 ? std::min(maxdim, S->chimax) : S->chimax;
-    int dmax = 1;
-    for (int dd : S->dsite) dmax = std::max(dmax, dd);
-    const int bmax = std::min(64, dmax * dmax * S->chimax);
     const long long cap = std::max<long long>(S->cap_total, 1);
-    const int chunk = std::min(n_gates, 128);
-    // device buffers
-    std::vector<void*> owned;
-    auto dalloc = [&](size_t bytes) {
-      void* p = nullptr;
-      GBTN_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 8)));
-      owned.push_back(p);
-      return p;
-    };
-    struct Guard {
-      std::vector<void*>& v;
-      ~Guard() {
-        for (void* p : v) cudaFree(p);
+    double* d_cot = nullptr;
+    GBTN_CUDA(cudaMalloc(&d_cot, sizeof(double) * cap));
+    std::unique_ptr<double, decltype(&cudaFree)> c_guard(d_cot, cudaFree);
+    su_scatter(S, post, cot_out, nullptr, d_cot);  // sites without a gate keep theirs (same shapes)
+    if (n_gates > 0) {
+      const long long gsz = (long long)D * D;
+      std::vector<void*> owned;
+      struct Guard {
+        std::vector<void*>& v;
+        ~Guard() {
+          for (void* p : v) cudaFree(p);
+        }
+      } guard{owned};
+      auto dalloc = [&](size_t bytes) {
+        void* p = nullptr;
+        GBTN_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 8)));
+        owned.push_back(p);
+        return p;
+      };
+      double* d_gates = (double*)dalloc(sizeof(double) * gsz * (per_gate ? n_gates : 1));
+      GBTN_CUDA(cudaMemcpyAsync(d_gates, gates, sizeof(double) * gsz * (per_gate ? n_gates : 1),
+                                cudaMemcpyHostToDevice, s));
+      double* d_envs = nullptr;
+      if (envs) {
+        const long long ne2 = 2LL * S->ne * S->chimax * S->chimax;
+        d_envs = (double*)dalloc(sizeof(double) * ne2);
+        GBTN_CUDA(cudaMemcpyAsync(d_envs, envs, sizeof(double) * ne2, cudaMemcpyHostToDevice, s));
       }
-    } guard{owned};
-    double* d_gates = (double*)dalloc(sizeof(double) * gsz * (per_gate ? n_gates : 1));
-    GBTN_CUDA(cudaMemcpyAsync(d_gates, gates, sizeof(double) * gsz * (per_gate ? n_gates : 1), cudaMemcpyHostToDevice, s));
-    double* d_envs = nullptr;
-    if (envs) {
-      const long long ne2 = 2LL * S->ne * S->chimax * S->chimax;
-      d_envs = (double*)dalloc(sizeof(double) * ne2);
-      GBTN_CUDA(cudaMemcpyAsync(d_envs, envs, sizeof(double) * ne2, cudaMemcpyHostToDevice, s));
+      SuJob* d_jobs = (SuJob*)dalloc(sizeof(SuJob) * n_gates);
+      GBTN_CUDA(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SuJob) * n_gates, cudaMemcpyHostToDevice, s));
+      int* d_post = (int*)dalloc(sizeof(int) * std::max(S->ne, 1));
+      if (S->ne) GBTN_CUDA(cudaMemcpyAsync(d_post, post.data(), sizeof(int) * S->ne, cudaMemcpyHostToDevice, s));
+      double* d_gc = (double*)dalloc(sizeof(double) * gsz * n_gates);
+      const int md = maxdim > 0 ? std::min(maxdim, S->chimax) : S->chimax;
+      VjpScratch w(S, n_gates);
+      GBTN_CUDA(cudaMemsetAsync(S->d_status, 0, sizeof(int), s));
+      su_vjp_batch(S, d_jobs, n_gates, d_gates, per_gate, gsz, d_envs, md, cutoff, normalize, su_bmax(S), d_post,
+                   d_cot, d_cot, d_gc, w);
+      int status = 0;
+      GBTN_CUDA(cudaMemcpyAsync(&status, S->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+      GBTN_CUDA(cudaStreamSynchronize(s));
+      if (status == 2)
+        return su_fail(S, GBTN_ERR_INVALID,
+                       "simple update adjoint: a gate's truncation differs from post_edge_dims (not the tensors the "
+                       "gates were applied to?)");
+      if (status)
+        return su_fail(S, GBTN_ERR_UNSUPPORTED,
+                       "simple update: a gate exceeds the kernel limits (site tensor, also with the bond at maxdim, "
+                       "> 8192 elements, or theta > 64 x 64)");
+      if (gate_cot)
+        GBTN_CUDA(cudaMemcpyAsync(gate_cot, d_gc, sizeof(double) * gsz * n_gates, cudaMemcpyDeviceToHost, s));
     }
-    SuJob* d_jobs = (SuJob*)dalloc(sizeof(SuJob) * n_gates);
-    GBTN_CUDA(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SuJob) * n_gates, cudaMemcpyHostToDevice, s));
-    int* d_post = (int*)dalloc(sizeof(int) * std::max(S->ne, 1));
-    int* d_edim_fwd = (int*)dalloc(sizeof(int) * std::max(S->ne, 1));
-    if (S->ne) {
-      GBTN_CUDA(cudaMemcpyAsync(d_post, post_edge_dims, sizeof(int) * S->ne, cudaMemcpyHostToDevice, s));
-    }
-    double* d_cout = (double*)dalloc(sizeof(double) * cap);
-    double* d_cin = (double*)dalloc(sizeof(double) * cap);
-    {  // cotangents of the gates' sites into their slots (post shapes)
-      long long oo = 0;
-      for (int v = 0; v < S->nv; ++v) {
-        if (mark[v])
-          GBTN_CUDA(cudaMemcpyAsync(d_cout + S->cap_off[v], cot_out + oo, sizeof(double) * post_n[v],
-                                    cudaMemcpyHostToDevice, s));
-        oo += post_n[v];
-      }
-    }
-    double* d_q = (double*)dalloc(sizeof(double) * (size_t)chunk * 2 * gbtn::kSuSideStride);
-    double* d_js = (double*)dalloc(sizeof(double) * (size_t)chunk * gbtn::kSuJobStride);
-    double* d_full = (double*)dalloc(sizeof(double) * (size_t)chunk * gbtn::kSuFullStride);
-    double* d_sqrt = (double*)dalloc(sizeof(double) * (size_t)chunk * 2 * gbtn::kSuSqrtStride);
-    double* d_work = (double*)dalloc(sizeof(double) * (size_t)chunk * gbtn::kSuVjpStride);
-    double* d_gc = gate_cot ? (double*)dalloc(sizeof(double) * gsz * n_gates) : nullptr;
-    GBTN_CUDA(cudaMemsetAsync(S->d_status, 0, sizeof(int), s));
-    for (int j0 = 0; j0 < n_gates; j0 += chunk) {
-      SuArgs a{};
-      a.jobs = d_jobs + j0;
-      a.njobs = std::min(chunk, n_gates - j0);
-      a.leg_ptr = S->d_leg_ptr;
-      a.leg_edge = S->d_leg_edge;
-      a.edge_u = S->d_edge_u;
-      a.site_dim = S->d_dsite;
-      a.cap_off = S->d_cap_off;
-      a.tens = S->d_tens;
-      a.envs = d_envs;
-      a.gates = d_gates + (per_gate ? gsz * j0 : 0);
-      a.gate_stride = per_gate ? gsz : 0;
-      a.maxdim = md;
-      a.cutoff = cutoff;
-      a.normalize = normalize;
-      a.chimax = S->chimax;
-      a.side_scratch = d_q;
-      a.job_scratch = d_js;
-      a.bmax = bmax;
-      a.status = S->d_status;
-      a.svd_full = d_full;
-      a.side_sqrt = d_sqrt;
-      // the forward stages write the new bond dimensions into a scratch copy
-      if (S->ne)
-        GBTN_CUDA(cudaMemcpyAsync(d_edim_fwd, S->d_edim, sizeof(int) * S->ne, cudaMemcpyDeviceToDevice, s));
-      a.edim = d_edim_fwd;
-      gbtn::su_launch_fwd_stages(a, s);
-      a.edim = S->d_edim;
-      gbtn::su_launch_vjp_kernel(a, d_post, d_cout, d_cin, d_gc ? d_gc + gsz * j0 : nullptr, d_work, s);
-    }
-    int status = 0;
-    GBTN_CUDA(cudaMemcpyAsync(&status, S->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
-    GBTN_CUDA(cudaStreamSynchronize(s));
-    if (status == 2)
-      return su_fail(S, GBTN_ERR_INVALID,
-                     "simple update adjoint: a gate's truncation differs from post_edge_dims (not the tensors the "
-                     "gates were applied to?)");
-    if (status)
-      return su_fail(S, GBTN_ERR_UNSUPPORTED,
-                     "simple update: a gate exceeds the kernel limits (site tensor, also with the bond at maxdim, "
-                     "> 8192 elements, or theta > 64 x 64)");
-    {
-      long long oi = 0;
-      for (int v = 0; v < S->nv; ++v) {
-        if (mark[v])
-          GBTN_CUDA(cudaMemcpyAsync(cot_in + oi, d_cin + S->cap_off[v], sizeof(double) * pre_n[v],
-                                    cudaMemcpyDeviceToHost, s));
-        oi += pre_n[v];
-      }
-    }
-    if (gate_cot)
-      GBTN_CUDA(cudaMemcpyAsync(gate_cot, d_gc, sizeof(double) * gsz * n_gates, cudaMemcpyDeviceToHost, s));
-    GBTN_CUDA(cudaStreamSynchronize(s));
+    su_scatter(S, S->edim, nullptr, cot_in, d_cot);
   } catch (const std::exception& e) {
     return su_fail(S, GBTN_ERR_CUDA, e.what());
   }

@@ -125,55 +125,44 @@ class SimpleUpdateState:
     def apply_with_pullback(self, gates, edges, envs=None, maxdim=None, cutoff=None, normalize=False):
         """``apply`` that also returns its pullback: (truncation errors, kept
         singular values, pullback), pullback(cot) -> (dL/d(tensors before the
-        gates) per vertex, dL/dG per gate (n, D, D)).  The gates run in batches
-        of consecutive vertex-disjoint gates (the order ``apply`` gives them);
-        the state before each batch is kept on the host for the pullback,
-        which leaves the state where ``apply`` left it."""
-        edges = [int(e) for e in edges]
-        shared = not isinstance(gates, (list, tuple))
-        glist = [gates] * len(edges) if shared else list(gates)
-        batches, cur, used = [], [], set()
-        for j, e in enumerate(edges):
-            u, v = self.tn.edges[e]
-            if u in used or v in used:
-                batches.append(cur)
-                cur, used = [], set()
-            cur.append(j)
-            used.update((u, v))
-        if cur:
-            batches.append(cur)
-        saved, tes, svs = [], [], []
-        for b in batches:
-            saved.append(self.network())
-            te, sv = self.apply([glist[j] for j in b], [edges[j] for j in b], envs=envs, maxdim=maxdim,
-                                cutoff=cutoff, normalize=normalize)
-            tes.append(te)
-            svs.append(sv)
-        final = self.network()
-        order = [j for b in batches for j in b]
+        gates) per vertex, dL/dG per gate (n, D, D)).  The library keeps a tape
+        of the state before every batch of consecutive vertex-disjoint gates
+        in device memory (gbtn_su_apply_taped); the pullback runs the batches'
+        adjoints backwards on the device and leaves the state where ``apply``
+        left it.  Real tensors."""
+        if self.complex:
+            raise _lib.Unsupported(2, "simple update adjoint: real tensors only")
+        edges = np.ascontiguousarray(edges, dtype=np.int32)
+        n = len(edges)
+        shared, g, env_arr = self._pack(gates, envs)
+        md = int(maxdim) if maxdim else self.chi_max
+        te = np.zeros(max(n, 1))
+        sv = np.zeros(max(n * md, 1))
+        before = self.network()
+        tape = _Tape(self)
+        check(self.ctx.handle, self.lib.gbtn_su_apply_taped(
+            self.handle, n, iptr(edges), dptr(g), 0 if shared else 1,
+            None if env_arr is None else dptr(env_arr), md, -1.0 if cutoff is None else float(cutoff),
+            1 if normalize else 0, dptr(te), dptr(sv), C.byref(tape.handle)))
+        after_dims = self.edge_dims()
+        du = [self.tn.site_dims[self.tn.edges[int(e)][0]] * self.tn.site_dims[self.tn.edges[int(e)][1]] for e in edges]
+        D = du[0] if n else 1
 
         def pullback(cot):
-            cot = [np.asarray(c, float) for c in cot]
-            gcs = [None] * len(edges)
-            post = final.edge_dims
-            for b, net in zip(reversed(batches), reversed(saved)):
-                self.set_state(net)
-                cot, gc = self.apply_vjp([glist[j] for j in b], [edges[j] for j in b], post, cot, envs=envs,
-                                         maxdim=maxdim, cutoff=cutoff, normalize=normalize)
-                for i, j in enumerate(b):
-                    gcs[j] = gc[i]
-                post = net.edge_dims
-            self.set_state(final)
-            return cot, np.array(gcs)
+            flat = np.ascontiguousarray(np.concatenate([np.asarray(c, float).reshape(-1, order="F") for c in cot]))
+            n_after = sum(int(np.prod(np.asarray(c).shape)) for c in cot)
+            want = sum(self.tn.site_dims[v] * int(np.prod([after_dims[e] for e in self.tn.legs[v]]))
+                       for v in range(self.tn.nv))
+            if n_after != want:
+                raise _lib.InvalidArgument(1, "cotangents do not have the shapes the gates left")
+            out = np.zeros(max(sum(before.size(v) for v in range(before.nv)), 1))
+            gc = np.zeros(max(n * D * D, 1))
+            check(self.ctx.handle, self.lib.gbtn_su_tape_vjp(self.handle, tape.handle, dptr(flat), dptr(out), dptr(gc)))
+            n_el = sum(before.size(v) for v in range(before.nv))
+            return before.unflat(out[:n_el]), gc[:n * D * D].reshape(n, D, D).transpose(0, 2, 1)
 
-        te = np.zeros(len(edges))
-        sv = None
-        te[order] = np.concatenate(tes) if tes else []
-        if svs:
-            allsv = np.concatenate(svs)
-            sv = np.zeros_like(allsv)
-            sv[order] = allsv
-        return te, sv, pullback
+        pullback.tape = tape  # freed with the pullback
+        return te[:n], sv[:n * md].reshape(n, md), pullback
 
     def close(self):
         if getattr(self, "handle", None):
@@ -183,6 +172,22 @@ class SimpleUpdateState:
     def __del__(self):
         try:
             self.close()
+        except Exception:
+            pass
+
+
+class _Tape:
+    """Owner of a gbtn_su_tape."""
+
+    def __init__(self, st):
+        self.st = st
+        self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            if self.handle:
+                self.st.lib.gbtn_su_tape_destroy(self.handle)
+            self.handle = C.c_void_p()
         except Exception:
             pass
 
