@@ -2012,10 +2012,17 @@ struct gbtn_su {
   int* d_status = nullptr;
   long long* d_cap_off = nullptr;
   double* d_tens = nullptr;
+  // adjoint scratch, kept between calls and grown on demand (device), and a
+  // pinned host staging buffer for cotangents
+  void* d_vjp = nullptr;
+  size_t vjp_bytes = 0;
+  double* h_stage = nullptr;
+  size_t stage_bytes = 0;
   ~gbtn_su() {
     for (void* p : {(void*)d_leg_ptr, (void*)d_leg_edge, (void*)d_edge_u, (void*)d_dsite, (void*)d_edim,
-                    (void*)d_status, (void*)d_cap_off, (void*)d_tens})
+                    (void*)d_status, (void*)d_cap_off, (void*)d_tens, d_vjp})
       if (p) cudaFree(p);
+    if (h_stage) cudaFreeHost(h_stage);
   }
 };
 
@@ -2091,29 +2098,39 @@ void tape_snapshot(gbtn_su* S, gbtn_su_tape* T, cudaStream_t s) {
   if (S->ne) GBTN_CUDA(cudaMemcpyAsync(d, S->d_edim, sizeof(int) * S->ne, cudaMemcpyDeviceToDevice, s));
 }
 
-// Scratch of the adjoint for up to `chunk` gates at a time.
+// Scratch of the adjoint for up to `chunk` gates at a time, plus the
+// cotangent buffer (capacity layout), a staging copy and the gate
+// cotangents, carved from the state's adjoint buffer.
 struct VjpScratch {
-  std::vector<void*> owned;
   double *q = nullptr, *js = nullptr, *full = nullptr, *sq = nullptr, *work = nullptr;
+  double *cot = nullptr, *stage = nullptr, *gc = nullptr;
   int* edim_fwd = nullptr;
   int chunk = 0;
-  VjpScratch(const gbtn_su* S, int max_jobs) {
-    chunk = std::max(1, std::min(max_jobs, 128));
-    q = (double*)get(sizeof(double) * (size_t)chunk * 2 * gbtn::kSuSideStride);
-    js = (double*)get(sizeof(double) * (size_t)chunk * gbtn::kSuJobStride);
-    full = (double*)get(sizeof(double) * (size_t)chunk * gbtn::kSuFullStride);
-    sq = (double*)get(sizeof(double) * (size_t)chunk * 2 * gbtn::kSuSqrtStride);
-    work = (double*)get(sizeof(double) * (size_t)chunk * gbtn::kSuVjpStride);
-    edim_fwd = (int*)get(sizeof(int) * std::max(S->ne, 1));
-  }
-  void* get(size_t bytes) {
-    void* p = nullptr;
-    GBTN_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 8)));
-    owned.push_back(p);
-    return p;
-  }
-  ~VjpScratch() {
-    for (void* p : owned) cudaFree(p);
+  VjpScratch(gbtn_su* S, int max_jobs, long long gc_elems) {
+    chunk = std::max(1, std::min(max_jobs, 2 * 152));
+    const size_t cap = (size_t)std::max<long long>(S->cap_total, 1);
+    const size_t sizes[] = {(size_t)chunk * 2 * gbtn::kSuSideStride, (size_t)chunk * gbtn::kSuJobStride,
+                            (size_t)chunk * gbtn::kSuFullStride,     (size_t)chunk * 2 * gbtn::kSuSqrtStride,
+                            (size_t)chunk * gbtn::kSuVjpStride,      cap,
+                            cap,                                     (size_t)std::max<long long>(gc_elems, 1),
+                            (size_t)std::max(S->ne, 1)};
+    size_t total = 0;
+    for (size_t n : sizes) total += (n + 31) / 32 * 32;
+    const size_t bytes = total * sizeof(double);
+    if (S->vjp_bytes < bytes) {
+      if (S->d_vjp) cudaFree(S->d_vjp);
+      S->d_vjp = nullptr;
+      S->vjp_bytes = 0;
+      GBTN_CUDA(cudaMalloc(&S->d_vjp, bytes));
+      S->vjp_bytes = bytes;
+    }
+    double* p = static_cast<double*>(S->d_vjp);
+    double** dst[] = {&q, &js, &full, &sq, &work, &cot, &stage, &gc};
+    for (int i = 0; i < 8; ++i) {
+      *dst[i] = p;
+      p += (sizes[i] + 31) / 32 * 32;
+    }
+    edim_fwd = reinterpret_cast<int*>(p);
   }
 };
 
@@ -2166,10 +2183,11 @@ int su_bmax(const gbtn_su* S) {
 
 // Host tensors (concatenated in vertex order with bond dimensions dims) into
 // a capacity-layout device buffer (host_in) or out of it (host_out), through
-// one staging copy.
-void su_scatter(gbtn_su* S, const std::vector<int>& dims, const double* host_in, double* host_out, double* dev) {
-  const bool to_device = host_in != nullptr;
+// the state's pinned staging buffer and one device staging copy.
+void su_scatter(gbtn_su* S, const std::vector<int>& dims, const double* host_in, double* host_out, double* dev,
+                double* stage) {
   cudaStream_t s = S->stream;
+  const bool to_device = host_in != nullptr;
   std::vector<long long> n(S->nv);
   long long tot = 0;
   for (int v = 0; v < S->nv; ++v) {
@@ -2178,10 +2196,18 @@ void su_scatter(gbtn_su* S, const std::vector<int>& dims, const double* host_in,
     n[v] = a;
     tot += a;
   }
-  double* stage = nullptr;
-  GBTN_CUDA(cudaMalloc(&stage, sizeof(double) * std::max<long long>(tot, 1)));
-  std::unique_ptr<double, decltype(&cudaFree)> guard(stage, cudaFree);
-  if (to_device) GBTN_CUDA(cudaMemcpyAsync(stage, host_in, sizeof(double) * tot, cudaMemcpyHostToDevice, s));
+  const size_t bytes = sizeof(double) * std::max<long long>(tot, 1);
+  if (S->stage_bytes < bytes) {
+    if (S->h_stage) cudaFreeHost(S->h_stage);
+    S->h_stage = nullptr;
+    S->stage_bytes = 0;
+    GBTN_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&S->h_stage), bytes, cudaHostAllocDefault));
+    S->stage_bytes = bytes;
+  }
+  if (to_device) {
+    std::copy(host_in, host_in + tot, S->h_stage);
+    GBTN_CUDA(cudaMemcpyAsync(stage, S->h_stage, sizeof(double) * tot, cudaMemcpyHostToDevice, s));
+  }
   long long off = 0;
   for (int v = 0; v < S->nv; ++v) {
     if (to_device)
@@ -2190,7 +2216,11 @@ void su_scatter(gbtn_su* S, const std::vector<int>& dims, const double* host_in,
       GBTN_CUDA(cudaMemcpyAsync(stage + off, dev + S->cap_off[v], sizeof(double) * n[v], cudaMemcpyDeviceToDevice, s));
     off += n[v];
   }
-  if (!to_device) GBTN_CUDA(cudaMemcpyAsync(host_out, stage, sizeof(double) * tot, cudaMemcpyDeviceToHost, s));
+  if (!to_device) {
+    GBTN_CUDA(cudaMemcpyAsync(S->h_stage, stage, sizeof(double) * tot, cudaMemcpyDeviceToHost, s));
+    GBTN_CUDA(cudaStreamSynchronize(s));
+    std::copy(S->h_stage, S->h_stage + tot, host_out);
+  }
   GBTN_CUDA(cudaStreamSynchronize(s));
 }
 
@@ -2500,17 +2530,12 @@ int gbtn_su_tape_vjp(gbtn_su* S, const gbtn_su_tape* T, const double* cot_out, d
     if (S->ne)
       GBTN_CUDA(cudaMemcpyAsync(final_dims.data(), T->d_edim_snap[nb], sizeof(int) * S->ne, cudaMemcpyDeviceToHost, s));
     GBTN_CUDA(cudaStreamSynchronize(s));
-    const long long cap = std::max<long long>(S->cap_total, 1);
-    double* d_cot = nullptr;
-    GBTN_CUDA(cudaMalloc(&d_cot, sizeof(double) * cap));
-    std::unique_ptr<double, decltype(&cudaFree)> c_guard(d_cot, cudaFree);
-    double* d_gc = nullptr;
-    GBTN_CUDA(cudaMalloc(&d_gc, sizeof(double) * std::max<long long>(T->gsz * T->n_gates, 1)));
-    std::unique_ptr<double, decltype(&cudaFree)> gc_guard(d_gc, cudaFree);
-    su_scatter(S, final_dims, cot_out, nullptr, d_cot);
     int maxb = 1;
     for (auto& b : T->batches) maxb = std::max(maxb, b.second - b.first);
-    VjpScratch w(S, maxb);
+    VjpScratch w(S, maxb, T->gsz * T->n_gates);
+    double* d_cot = w.cot;
+    double* d_gc = w.gc;
+    su_scatter(S, final_dims, cot_out, nullptr, d_cot, w.stage);
     GBTN_CUDA(cudaMemsetAsync(S->d_status, 0, sizeof(int), s));
     for (int b = nb - 1; b >= 0; --b) {
       const auto& bt = T->batches[b];
@@ -2529,7 +2554,7 @@ int gbtn_su_tape_vjp(gbtn_su* S, const gbtn_su_tape* T, const double* cot_out, d
     GBTN_CUDA(cudaMemcpyAsync(&status, S->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
     GBTN_CUDA(cudaStreamSynchronize(s));
     if (status) return su_fail(S, GBTN_ERR_NUMERIC, "simple update adjoint: a recomputed gate differs from the tape");
-    su_scatter(S, T->dims_before, nullptr, cot_in, d_cot);
+    su_scatter(S, T->dims_before, nullptr, cot_in, d_cot, w.stage);
     if (gate_cot)
       GBTN_CUDA(cudaMemcpyAsync(gate_cot, d_gc, sizeof(double) * T->gsz * T->n_gates, cudaMemcpyDeviceToHost, s));
     GBTN_CUDA(cudaStreamSynchronize(s));
@@ -2589,13 +2614,11 @@ int gbtn_su_apply_vjp(gbtn_su* S, int32_t n_gates, const int32_t* edges, const d
     for (int e = 0; e < S->ne; ++e)
       if (gate_edge[e] ? (post[e] < 1 || post[e] > S->chimax) : post[e] != S->edim[e])
         return su_fail(S, GBTN_ERR_INVALID, "simple update adjoint: post_edge_dims do not follow the gates");
-    const long long cap = std::max<long long>(S->cap_total, 1);
-    double* d_cot = nullptr;
-    GBTN_CUDA(cudaMalloc(&d_cot, sizeof(double) * cap));
-    std::unique_ptr<double, decltype(&cudaFree)> c_guard(d_cot, cudaFree);
-    su_scatter(S, post, cot_out, nullptr, d_cot);  // sites without a gate keep theirs (same shapes)
+    const long long gsz = (long long)D * D;
+    VjpScratch w(S, std::max<int>(n_gates, 1), gsz * n_gates);
+    double* d_cot = w.cot;
+    su_scatter(S, post, cot_out, nullptr, d_cot, w.stage);  // sites without a gate keep theirs (same shapes)
     if (n_gates > 0) {
-      const long long gsz = (long long)D * D;
       std::vector<void*> owned;
       struct Guard {
         std::vector<void*>& v;
@@ -2622,9 +2645,8 @@ int gbtn_su_apply_vjp(gbtn_su* S, int32_t n_gates, const int32_t* edges, const d
       GBTN_CUDA(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SuJob) * n_gates, cudaMemcpyHostToDevice, s));
       int* d_post = (int*)dalloc(sizeof(int) * std::max(S->ne, 1));
       if (S->ne) GBTN_CUDA(cudaMemcpyAsync(d_post, post.data(), sizeof(int) * S->ne, cudaMemcpyHostToDevice, s));
-      double* d_gc = (double*)dalloc(sizeof(double) * gsz * n_gates);
+      double* d_gc = w.gc;
       const int md = maxdim > 0 ? std::min(maxdim, S->chimax) : S->chimax;
-      VjpScratch w(S, n_gates);
       GBTN_CUDA(cudaMemsetAsync(S->d_status, 0, sizeof(int), s));
       su_vjp_batch(S, d_jobs, n_gates, d_gates, per_gate, gsz, d_envs, md, cutoff, normalize, su_bmax(S), d_post,
                    d_cot, d_cot, d_gc, w);
@@ -2642,7 +2664,7 @@ int gbtn_su_apply_vjp(gbtn_su* S, int32_t n_gates, const int32_t* edges, const d
       if (gate_cot)
         GBTN_CUDA(cudaMemcpyAsync(gate_cot, d_gc, sizeof(double) * gsz * n_gates, cudaMemcpyDeviceToHost, s));
     }
-    su_scatter(S, S->edim, nullptr, cot_in, d_cot);
+    su_scatter(S, S->edim, nullptr, cot_in, d_cot, w.stage);
   } catch (const std::exception& e) {
     return su_fail(S, GBTN_ERR_CUDA, e.what());
   }
