@@ -36,7 +36,9 @@
 # and ChainRulesCore rrules for `bp_energy(psi, ops, coefs)` (the BP two-site
 # energy), `bp_logscalar(psi)` and `bp_expect_sum(psi, op)`, whose pullbacks are
 # the library's hand-written adjoints (implicit differentiation at the BP fixed
-# point; complex tensors too).
+# point; complex tensors too), and for `gb300_apply(gates, psi; ...)` (the real
+# simple update through the library's taped adjoint of QR, truncated SVD and
+# environment roots, to the input tensors and the gates).
 #
 # Not executed in the environment this file was written in (no Julia
 # toolchain); it documents the binding a maintainer adds.
@@ -675,6 +677,141 @@ function ITensorNetworks.tebd(::Algorithm"gb300", ℋ, ψ; β, Δβ, maxdim, cut
         ψ = ITensorNetworks.apply(Algorithm("gb300"), u⃗, ψ; maxdim, cutoff, normalize=true)
     end
     return ψ
+end
+
+# ---- the simple update with its adjoint (ChainRulesCore) -----------------------
+
+# Owner of a simple-update state and the tape of one taped apply; both are
+# released when the pullback that holds it is collected.
+mutable struct SUTape
+    state::Ptr{Cvoid}
+    tape::Ptr{Cvoid}
+    function SUTape(state)
+        t = new(state, C_NULL)
+        finalizer(t) do x
+            x.tape != C_NULL && ccall((:gbtn_su_tape_destroy, libgbtn), Cint, (Ptr{Cvoid},), x.tape)
+            x.state != C_NULL && ccall((:gbtn_su_destroy, libgbtn), Cint, (Ptr{Cvoid},), x.state)
+            x.tape = C_NULL
+            x.state = C_NULL
+        end
+        return t
+    end
+end
+
+"""
+    gb300_apply(gates, psi; maxdim, cutoff=nothing, normalize=true, envs=nothing)
+
+The two-site `gates` (real ITensors on the site indices of neighbouring
+vertices) applied in order by the GPU simple update, as
+`apply(Algorithm("gb300"), gates, psi; ...)`, differentiable: its rrule pulls
+a cotangent of the returned network (a Dict vertex => ITensor with the
+returned tensors' indices) back to the input tensors and to the gates, through
+the library's taped adjoint (gbtn_su_apply_taped / gbtn_su_tape_vjp).  The
+environments are constants.
+"""
+gb300_apply(gates::Vector{ITensor}, psi; kwargs...) = first(gb300_apply_with_pullback(gates, psi; kwargs...))
+
+function gb300_apply_with_pullback(gates::Vector{ITensor}, psi; maxdim, cutoff=nothing, normalize=true,
+                                   envs=nothing)
+    all(g -> length(inds(g)) == 4 && eltype(g) <: Real, gates) ||
+        error("gb300_apply: real two-site gates only")
+    p = pack_state(psi)
+    ctx = context()
+    chimax = max(maxdim, maximum(p.edim))
+    eidx = Int32[]
+    gdata = Float64[]
+    gsites = Tuple{Index, Index}[]
+    for g in gates
+        vs = [v for v in p.vs if !isempty(intersect(inds(g), [p.sites[findfirst(==(v), p.vs)]]))]
+        iu, iv = findfirst(==(vs[1]), p.vs) - 1, findfirst(==(vs[2]), p.vs) - 1
+        e = findfirst(k -> Set((p.eu[k], p.ev[k])) == Set((iu, iv)), eachindex(p.eu))
+        a, b = p.eu[e] == iu ? (p.sites[iu + 1], p.sites[iv + 1]) : (p.sites[iv + 1], p.sites[iu + 1])
+        push!(eidx, e - 1)
+        push!(gsites, (a, b))
+        append!(gdata, vec(array(g, prime(a), prime(b), a, b)))
+    end
+    envbuf = Float64[]
+    if envs !== nothing
+        envbuf = zeros(2 * length(p.es) * chimax^2)
+        for (k, e) in enumerate(p.es), (dir, qe) in ((0, e), (1, reverse(e)))
+            M = array(only(envs[qe]))
+            c = size(M, 1)
+            o = (2 * (k - 1) + dir) * chimax^2
+            envbuf[(o + 1):(o + c * c)] = vec(M)
+        end
+    end
+    n = length(gates)
+    desc = GraphDesc(length(p.vs), length(p.es), pointer(p.eu), pointer(p.ev), pointer(p.edim),
+        pointer(p.sdim), pointer(p.leg_ptr), pointer(p.leg_edge), C_NULL, 1, 0, 0)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve p begin
+        check(ctx, ccall((:gbtn_su_create, libgbtn), Cint, (Ptr{Cvoid}, Ref{GraphDesc}, Int32, Ref{Ptr{Cvoid}}),
+            ctx, desc, chimax, h))
+    end
+    holder = SUTape(h[])
+    check(ctx, ccall((:gbtn_su_set_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Float64}), holder.state, p.data))
+    tref = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ctx, ccall((:gbtn_su_apply_taped, libgbtn), Cint,
+        (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Float64}, Int32, Ptr{Float64}, Int32, Float64, Int32,
+         Ptr{Float64}, Ptr{Float64}, Ref{Ptr{Cvoid}}),
+        holder.state, n, eidx, gdata, 1, envs === nothing ? C_NULL : envbuf, maxdim, something(cutoff, -1.0),
+        normalize ? 1 : 0, C_NULL, C_NULL, tref))
+    holder.tape = tref[]
+    dims = zeros(Int32, length(p.es))
+    check(ctx, ccall((:gbtn_su_edge_dims, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Int32}), holder.state, dims))
+    newlinks = [d == length(l) ? l : Index(Int(d), tags(l)) for (d, l) in zip(dims, p.links)]
+    legs(i, ls) = [ls[p.leg_edge[q] + 1] for q in (p.leg_ptr[i] + 1):p.leg_ptr[i + 1]]
+    total = sum(Int(p.sdim[i]) * prod(length.(legs(i, newlinks)); init=1) for i in eachindex(p.vs))
+    flat = Vector{Float64}(undef, total)
+    check(ctx, ccall((:gbtn_su_get_factors, libgbtn), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int64),
+        holder.state, flat, total))
+    out = copy(psi)
+    off = 0
+    for (i, v) in enumerate(p.vs)
+        ls = legs(i, newlinks)
+        len = Int(p.sdim[i]) * prod(length.(ls); init=1)
+        out[v] = itensor(reshape(flat[(off + 1):(off + len)], Int(p.sdim[i]), length.(ls)...), p.sites[i], ls...)
+        off += len
+    end
+    function pullback(dout)
+        cot = Float64[]
+        for (i, v) in enumerate(p.vs)
+            append!(cot, vec(haskey(dout, v) ? array(dout[v], p.sites[i], legs(i, newlinks)...) :
+                             zeros(Int(p.sdim[i]), length.(legs(i, newlinks))...)))
+        end
+        din = zeros(length(p.data))
+        gc = zeros(length(gdata))
+        check(ctx, ccall((:gbtn_su_tape_vjp, libgbtn), Cint,
+            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+            holder.state, holder.tape, cot, din, gc))
+        dpsi = Dict{Any, ITensor}()
+        o = 0
+        for (i, v) in enumerate(p.vs)
+            ls = legs(i, p.links)
+            len = Int(p.sdim[i]) * prod(length.(ls); init=1)
+            dpsi[v] = itensor(reshape(din[(o + 1):(o + len)], Int(p.sdim[i]), length.(ls)...), p.sites[i], ls...)
+            o += len
+        end
+        dgates = ITensor[]
+        og = 0
+        for (a, b) in gsites
+            da, db = length(a), length(b)
+            len = (da * db)^2
+            push!(dgates, itensor(reshape(gc[(og + 1):(og + len)], da, db, da, db), prime(a), prime(b), a, b))
+            og += len
+        end
+        return dgates, dpsi
+    end
+    return out, pullback
+end
+
+function ChainRulesCore.rrule(::typeof(gb300_apply), gates::Vector{ITensor}, psi; kwargs...)
+    out, pb = gb300_apply_with_pullback(gates, psi; kwargs...)
+    function gb300_apply_pullback(dout)
+        dgates, dpsi = pb(ChainRulesCore.unthunk(dout))
+        return (NoTangent(), dgates, dpsi)
+    end
+    return out, gb300_apply_pullback
 end
 
 # ---- BP energy and its adjoint (ChainRulesCore) ------------------------------
