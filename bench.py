@@ -874,6 +874,34 @@ def run_sweeps_only(args):
     ctx.close()
 
 
+def run_su_pullback(args):
+    """Profiling mode (--su-pullback L): the L x L TFIM state of the simple-update
+    configuration after `steps` steps at chi 8, then one taped step and its
+    pullback (the command of the adjoint kernel's ncu captures)."""
+    import torch
+
+    import gbtn
+    L, chi = args.su_pullback, 8
+    tn = gbtn.square_lattice(L, L, chi=1)
+    plus = np.array([1.0, 1.0]) / np.sqrt(2)
+    tn.tensors = [plus.reshape((2,) + (1,) * len(tn.legs[v])) for v in range(tn.nv)]
+    z = [len(l) for l in tn.legs]
+    order = [e for c in gbtn.checkerboard_edges(L, L) for e in c]
+    gates = [gbtn.tfim_gate(0.01, 3.0, z[tn.edges[e][0]], z[tn.edges[e][1]]) for e in order]
+    st = gbtn.SimpleUpdateState(tn, chi)
+    for _ in range(args.steps):
+        st.apply(gates, order, maxdim=chi, cutoff=1e-10, normalize=True)
+    _, _, pull = st.apply_with_pullback(gates, order, maxdim=chi, cutoff=1e-10, normalize=True)
+    cot = [np.random.default_rng(1).standard_normal(t.shape) for t in st.network().tensors]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pull(cot)
+    torch.cuda.synchronize()
+    print(json.dumps({"su_pullback_lattice": L, "steps_before": args.steps, "max_bond_dim": max(st.edge_dims()),
+                      "pullback_s": time.perf_counter() - t0}))
+    st.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -885,10 +913,15 @@ def main():
     ap.add_argument("--solve-maxiter", type=int, default=300)
     ap.add_argument("--sweeps-only", default=None, choices=["f64", "f32", "df32", "bf16"],
                     help="only run warmup + steps parallel sweeps in this arithmetic (for profiler captures)")
+    ap.add_argument("--su-pullback", type=int, default=0, metavar="L",
+                    help="only run one taped simple-update step and its pullback on the L x L TFIM state after "
+                         "--steps steps (for profiler captures)")
     args = ap.parse_args()
     globals()["BATCH"] = args.batch
     if args.sweeps_only:
         run_sweeps_only(args)
+    elif args.su_pullback:
+        run_su_pullback(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
