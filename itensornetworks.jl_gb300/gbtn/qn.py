@@ -167,6 +167,7 @@ class QNBeliefPropagationCache:
     def set_tensors(self, tensors):
         data = np.ascontiguousarray(self.pack(tensors))
         check(self.ctx.handle, self.lib.gbtn_qn_set_blocks(self.handle, C.c_void_p(data.ctypes.data), _lib.HOST))
+        self._dense = [np.asarray(t, dtype=np.float64) * self.q.mask(v) for v, t in enumerate(tensors)]
 
     def init_messages(self):
         check(self.ctx.handle, self.lib.gbtn_qn_init_messages(self.handle))
@@ -255,6 +256,53 @@ class QNBeliefPropagationCache:
     def scalar(self):
         ls = self.logscalar()
         return complex(np.exp(ls)) if isinstance(ls, complex) else float(np.exp(ls))
+
+    # -- gradients ------------------------------------------------------------
+    # The dense tensors are the blocks embedded with zeros (a linear map E), and
+    # dense BP from the block-diagonal messages reproduces this plan's messages,
+    # so dL/d(blocks) = E^T dL/d(dense tensors): the dense plan's hand-written
+    # adjoints at the QN fixed point, gathered at the allowed blocks.  The
+    # gradients come back as dense arrays, zero outside the blocks (pack() gives
+    # the block storage).
+    def _dense_cache(self):
+        from .cache import BeliefPropagationCache
+        tn = self.q.tn
+        net = TensorNetwork(tn.nv, tn.edges, tn.site_dims, tn.edge_dims, [t.copy() for t in self._dense], tn.legs)
+        bpc = BeliefPropagationCache(net, ctx=self.ctx)
+        bpc.set_messages(self.messages())
+        return bpc
+
+    def _masked(self, G):
+        return [np.asarray(g) * self.q.mask(v) for v, g in enumerate(G)]
+
+    def energy2_grad(self, terms, mode="implicit", **kw):
+        """(energy, dE/dA) of sum_e sum_t c_t <O_t (x) O_t>_e at the converged
+        messages (mode "implicit"), or through unrolled sweeps from identity
+        messages (mode "unrolled"), as BeliefPropagationCache.energy2_grad."""
+        bpc = self._dense_cache()
+        try:
+            E, G = bpc.energy2_grad(terms, mode=mode, **kw)
+        finally:
+            bpc.close()
+        return E, self._masked(G)
+
+    def logscalar_grad(self, **kw):
+        """(Re logscalar, its gradient) at the converged messages."""
+        bpc = self._dense_cache()
+        try:
+            val, G = bpc.logscalar_grad(**kw)
+        finally:
+            bpc.close()
+        return val, self._masked(G)
+
+    def expect_sum_grad(self, op, **kw):
+        """(sum_v <op>_v, its gradient) at the converged messages."""
+        bpc = self._dense_cache()
+        try:
+            val, G = bpc.expect_sum_grad(op, **kw)
+        finally:
+            bpc.close()
+        return val, self._masked(G)
 
     def close(self):
         if getattr(self, "handle", None):
