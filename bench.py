@@ -542,7 +542,8 @@ def simple_update_timing(gbtn, ctx, barrier, rank, Ls=20, steps=200, g_field=3.0
         _, _, pull = st.apply_with_pullback(gates, order, maxdim=chi_max, cutoff=1e-10, normalize=True)
         barrier()
         fwd_ckpt_s = time.perf_counter() - t2
-        cot = [rng.standard_normal(t.shape) for t in st.network().tensors]
+        # column-major, as every gradient the library returns (energy2_grad, ...)
+        cot = [rng.standard_normal(t.size).reshape(t.shape, order="F") for t in st.network().tensors]
         barrier()
         t3 = time.perf_counter()
         pull(cot)
@@ -892,7 +893,8 @@ def run_su_pullback(args):
     for _ in range(args.steps):
         st.apply(gates, order, maxdim=chi, cutoff=1e-10, normalize=True)
     _, _, pull = st.apply_with_pullback(gates, order, maxdim=chi, cutoff=1e-10, normalize=True)
-    cot = [np.random.default_rng(1).standard_normal(t.shape) for t in st.network().tensors]
+    rng = np.random.default_rng(1)
+    cot = [rng.standard_normal(t.size).reshape(t.shape, order="F") for t in st.network().tensors]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     pull(cot)

@@ -1104,178 +1104,219 @@ constexpr int kVjP2 = kVjP1 + kVjpSmall;    // (1 - V V^T) Vbar S^-1 (nt x k)
 constexpr int kVjTb = kVjP2 + kVjpSmall;    // thetabar (mt x nt)
 constexpr int kVjPhi = kVjTb + kVjpSmall;   // gate^T thetabar (mt x nt)
 constexpr int kVjPsi = kVjPhi + kVjpSmall;  // theta before the gate (mt x nt)
-constexpr int kVjSb = kVjPsi + kVjpSmall;   // sigmabar (n)
-constexpr int kVjStride = kVjSb + kSuMaxTheta;
+constexpr int kVjSb = kVjPsi + kVjpSmall;   // sigmabar, each side's part (2 x kSuMaxTheta)
+constexpr int kVjStride = kVjSb + 2 * kSuMaxTheta;  // sigmabar: one part per side
 
 __device__ __forceinline__ double safe_inv(double x) { return x > 0.0 ? 1.0 / x : 0.0; }
 
-// One CTA per gate of the batch.  cot_out / cot_in: capacity layout (the
-// state's slots), the gate's sites after (bond k) / before the gate.
-// post_dims: the bond dimension the caller saw after the gates.
-__global__ void __launch_bounds__(kSuThreads, 1)
-    su_vjp_kernel(SuArgs a, const int* post_dims, const double* cot_out, double* cot_in, double* gate_cot,
-                  double* work) {
-  const int j = blockIdx.x, tid = threadIdx.x;
+// The per-gate context of the three adjoint launches.
+struct VjpCtx {
+  SuJob job;
+  const double* ssd[2];  // the sides' scratch of the forward's QR stage
+  const double* js;      // the job's scratch of the forward's SVD stage
+  SideShape hs[2];
+  int xs[2];
+  int k, ce, du, dv, D, ru, rv, mt, nt, n;
+  double* wj;
+};
+
+// False when the gate is skipped: a forward stage exceeded its limits (status
+// already set) or the recomputed truncation differs from post_dims (status 2).
+__device__ bool vjp_ctx(const SuArgs& a, const int* post_dims, double* work, int j, VjpCtx& c) {
+  c.job = a.jobs[j];
+  c.ssd[0] = a.side_scratch + (size_t)(2 * j) * kSideStride;
+  c.ssd[1] = a.side_scratch + (size_t)(2 * j + 1) * kSideStride;
+  c.js = a.job_scratch + (size_t)j * kJobStride;
+  if (c.ssd[0][kSideMeta + 1] != 0.0 || c.ssd[1][kSideMeta + 1] != 0.0 || c.js[kJobMeta + 1] == 0.0) return false;
+  c.k = (int)c.js[kJobMeta];
+  if (c.k != post_dims[c.job.e]) {
+    if (threadIdx.x == 0) atomicExch(a.status, 2);
+    return false;
+  }
+  site_of(a, c.job, 0, c.xs[0], c.hs[0]);
+  site_of(a, c.job, 1, c.xs[1], c.hs[1]);
+  c.ce = c.hs[0].chi[c.hs[0].p];
+  c.du = c.hs[0].d;
+  c.dv = c.hs[1].d;
+  c.D = c.du * c.dv;
+  c.ru = (int)c.ssd[0][kSideMeta];
+  c.rv = (int)c.ssd[1][kSideMeta];
+  c.mt = c.ru * c.du;
+  c.nt = c.dv * c.rv;
+  c.n = min(c.mt, c.nt);
+  c.wj = work + (size_t)j * kVjStride;
+  return true;
+}
+
+// Stage 1, one CTA per (gate, side): the forward's output rebuilt for the
+// normalisation, normalisation and inverse-sqrt environments backwards, the
+// cotangent split into Z = Q^T Ybar and Ybar_perp, the in-range cotangents of
+// the singular vectors and this side's part of sigmabar.
+__global__ void __launch_bounds__(kSuThreads, 2)
+    su_vjp_side_kernel(SuArgs a, const int* post_dims, const double* cot_out, double* work) {
+  const int j = blockIdx.x >> 1, side = blockIdx.x & 1, tid = threadIdx.x;
   if (j >= a.njobs) return;
   __shared__ double red[kSuWarps + 1];
   __shared__ double s_scale, s_dot;
-  const SuJob job = a.jobs[j];
-  const double* ssd[2] = {a.side_scratch + (size_t)(2 * j) * kSideStride,
-                          a.side_scratch + (size_t)(2 * j + 1) * kSideStride};
-  const double* js = a.job_scratch + (size_t)j * kJobStride;
-  if (ssd[0][kSideMeta + 1] != 0.0 || ssd[1][kSideMeta + 1] != 0.0 || js[kJobMeta + 1] == 0.0) return;
-  const int k = (int)js[kJobMeta];
-  if (k != post_dims[job.e]) {
-    if (tid == 0) atomicExch(a.status, 2);
-    return;
+  VjpCtx c;
+  if (!vjp_ctx(a, post_dims, work, j, c)) return;
+  const double* ssd[2] = {c.ssd[0], c.ssd[1]};
+  const SideShape* hs = c.hs;
+  const int* xs = c.xs;
+  const int k = c.k, ru = c.ru, dv = c.dv, mt = c.mt, nt = c.nt;
+  const double* js = c.js;
+  const double* full = a.svd_full + (size_t)j * kFullStride;
+  const double* UF = full + kFullU;
+  const double* VF = full + kFullV;
+  double* wj = c.wj;
+  double* Ub = wj + kVjUb;
+  double* Vb = wj + kVjVb;
+  double* sb = wj + kVjSb;
+  const SideShape& h = hs[side];
+  const double* ss = ssd[side];
+  double* ws = wj + (size_t)side * kVjSide;
+  double* Y = ws + kVjY;
+  double* Z = ws + kVjZ;
+  const int x = xs[side], m = h.m, d = h.d, r = (int)ss[kSideMeta];
+  int chi2[kMaxDeg];
+  for (int q = 0; q < h.k; ++q) chi2[q] = h.chi[q];
+  chi2[h.p] = k;
+  int n2 = d;
+  for (int q = 0; q < h.k; ++q) n2 *= chi2[q];
+  const int ncol2 = d * k;
+  // the forward output before normalisation: C = Si-absorbed (Q [X; 0])
+  for (int i = tid; i < m * ncol2; i += kSuThreads) {
+    const int row = i % m, col = i / m, s_ = col % d, b = col / d;
+    double v = 0.0;
+    if (row < r)
+      v = side == 0 ? js[kJobU + (row + ru * s_) + (size_t)mt * b] * js[kJobS + b]
+                    : js[kJobV + (s_ + dv * row) + (size_t)nt * b] * js[kJobS + b];
+    Y[i] = v;
   }
+  __syncthreads();
+  apply_reflectors(ss, m, r, Y, ncol2, false);
+  double* cur = ws + kVjT0;
+  double* nxt = ws + kVjT1;
+  for (int i = tid; i < n2; i += kSuThreads) {
+    int row, s_, b;
+    split_index(h, chi2, i, row, s_, b);
+    cur[i] = Y[row + (size_t)m * (s_ + d * b)];
+  }
+  __syncthreads();
+  double* Mt = ws + kVjM;  // a transposed chi x chi environment
+  if (a.envs) {
+    int st = d;
+    for (int q = 0; q < h.k; ++q) {
+      if (q != h.p) {
+        const int c = chi2[q];
+        const double* si = ss + kSideSI + q * 64;
+        for (int i = tid; i < c * c; i += kSuThreads) Mt[(i / c) + c * (i % c)] = si[i];
+        __syncthreads();
+        absorb_any<double>(c, cur, nxt, n2, st, Mt, tid, kSuThreads);
+        __syncthreads();
+        double* t = cur;
+        cur = nxt;
+        nxt = t;
+      }
+      st *= chi2[q];
+    }
+  }
+  // normalisation backwards: Cbar = (Abar - A <A, Abar>) / |C|
+  const double* Ab = cot_out + a.cap_off[x];
+  double s2 = 0.0, dt = 0.0;
+  for (int i = tid; i < n2; i += kSuThreads) {
+    s2 = fma(cur[i], cur[i], s2);
+    dt = fma(cur[i], Ab[i], dt);
+  }
+  s2 = block_sum(s2, red);
+  dt = block_sum(dt, red);
+  if (tid == 0) {
+    const double nc = sqrt(s2);
+    s_scale = (a.normalize && nc > 0.0) ? 1.0 / nc : 1.0;
+    s_dot = (a.normalize && nc > 0.0) ? dt / s2 : 0.0;  // <A, Abar> / |C| with A = C / |C|
+  }
+  __syncthreads();
+  for (int i = tid; i < n2; i += kSuThreads) nxt[i] = (Ab[i] - cur[i] * s_dot) * s_scale;
+  __syncthreads();
+  {
+    double* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  // inverse-sqrt environments backwards: the transposes of the matrices absorbed
+  if (a.envs) {
+    int st = d;
+    for (int q = 0; q < h.k; ++q) {
+      if (q != h.p) {
+        const int c = chi2[q];
+        absorb_any<double>(c, cur, nxt, n2, st, ss + kSideSI + q * 64, tid, kSuThreads);
+        __syncthreads();
+        double* t = cur;
+        cur = nxt;
+        nxt = t;
+      }
+      st *= chi2[q];
+    }
+  }
+  for (int i = tid; i < n2; i += kSuThreads) {
+    int row, s_, b;
+    split_index(h, chi2, i, row, s_, b);
+    Y[row + (size_t)m * (s_ + d * b)] = cur[i];
+  }
+  __syncthreads();
+  // Ybar = Q [Z; 0] + Ybar_perp
+  apply_reflectors(ss, m, r, Y, ncol2, true);
+  for (int i = tid; i < r * ncol2; i += kSuThreads) {
+    const int t = i % r, col = i / r;
+    Z[i] = Y[t + (size_t)m * col];
+  }
+  __syncthreads();
+  for (int i = tid; i < r * ncol2; i += kSuThreads) Y[(i % r) + (size_t)m * (i / r)] = 0.0;
+  __syncthreads();
+  apply_reflectors(ss, m, r, Y, ncol2, false);
+  // in-range cotangents of the singular vectors, and of sigma
+  for (int i = tid; i < (side == 0 ? mt : nt) * k; i += kSuThreads) {
+    const int row = i % (side == 0 ? mt : nt), b = i / (side == 0 ? mt : nt);
+    const int t = side == 0 ? row % ru : row / dv;
+    const int s_ = side == 0 ? row / ru : row % dv;
+    (side == 0 ? Ub : Vb)[i] = Z[t + r * (s_ + d * b)] * js[kJobS + b];
+  }
+  for (int b = threadIdx.x >> 5; b < k; b += kSuWarps) {
+    const int lane = tid & 31;
+    double acc = 0.0;
+    for (int i = lane; i < r * d; i += 32) {
+      const int t = i % r, s_ = i / r;
+      const double f = side == 0 ? UF[(t + ru * s_) + (size_t)mt * b] : VF[(s_ + dv * t) + (size_t)nt * b];
+      acc = fma(f, Z[t + r * (s_ + d * b)], acc);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) sb[side * kSuMaxTheta + b] = 0.5 * acc * safe_inv(js[kJobS + b]);
+  }
+  __syncthreads();
+}
+
+// Stage 2, one CTA per gate: the truncated-SVD adjoint in range, the gate
+// transposed and the bond contraction back to Rbar of both sides, the gate's
+// cotangent, and the factors H of the orthogonal terms.
+__global__ void __launch_bounds__(kSuThreads, 1)
+    su_vjp_core_kernel(SuArgs a, const int* post_dims, double* gate_cot, double* work) {
+  const int j = blockIdx.x, tid = threadIdx.x;
+  if (j >= a.njobs) return;
+  VjpCtx c;
+  if (!vjp_ctx(a, post_dims, work, j, c)) return;
+  const int k = c.k, ce = c.ce, du = c.du, dv = c.dv, D = c.D, ru = c.ru, rv = c.rv, mt = c.mt, nt = c.nt, n = c.n;
+  const double* js = c.js;
   const double* full = a.svd_full + (size_t)j * kFullStride;
   const double* UF = full + kFullU;
   const double* VF = full + kFullV;
   const double* sig = full + kFullSig;
-  double* wj = work + (size_t)j * kVjStride;
-  SideShape hs[2];
-  int xs[2];
-  site_of(a, job, 0, xs[0], hs[0]);
-  site_of(a, job, 1, xs[1], hs[1]);
-  const int ce = hs[0].chi[hs[0].p];
-  const int du = hs[0].d, dv = hs[1].d, D = du * dv;
-  const int ru = (int)ssd[0][kSideMeta], rv = (int)ssd[1][kSideMeta];
-  const int mt = ru * du, nt = dv * rv, n = min(mt, nt);
   const double* G = a.gates + (size_t)a.gate_stride * j;
-  const double* RU = ssd[0] + kSideR;
-  const double* RV = ssd[1] + kSideR;
-  double* Ub = wj + kVjUb;
-  double* Vb = wj + kVjVb;
-  double* sb = wj + kVjSb;
-  for (int i = tid; i < n; i += kSuThreads) sb[i] = 0.0;
-  __syncthreads();
-
-  // ---- 1-2: per side, the cotangent of L (or R) split by range(Q)
-  for (int side = 0; side < 2; ++side) {
-    const SideShape& h = hs[side];
-    const double* ss = ssd[side];
-    double* ws = wj + (size_t)side * kVjSide;
-    double* Y = ws + kVjY;
-    double* Z = ws + kVjZ;
-    const int x = xs[side], m = h.m, d = h.d, r = (int)ss[kSideMeta];
-    int chi2[kMaxDeg];
-    for (int q = 0; q < h.k; ++q) chi2[q] = h.chi[q];
-    chi2[h.p] = k;
-    int n2 = d;
-    for (int q = 0; q < h.k; ++q) n2 *= chi2[q];
-    const int ncol2 = d * k;
-    // the forward output before normalisation: C = Si-absorbed (Q [X; 0])
-    for (int i = tid; i < m * ncol2; i += kSuThreads) {
-      const int row = i % m, col = i / m, s_ = col % d, b = col / d;
-      double v = 0.0;
-      if (row < r)
-        v = side == 0 ? js[kJobU + (row + ru * s_) + (size_t)mt * b] * js[kJobS + b]
-                      : js[kJobV + (s_ + dv * row) + (size_t)nt * b] * js[kJobS + b];
-      Y[i] = v;
-    }
-    __syncthreads();
-    apply_reflectors(ss, m, r, Y, ncol2, false);
-    double* cur = ws + kVjT0;
-    double* nxt = ws + kVjT1;
-    for (int i = tid; i < n2; i += kSuThreads) {
-      int row, s_, b;
-      split_index(h, chi2, i, row, s_, b);
-      cur[i] = Y[row + (size_t)m * (s_ + d * b)];
-    }
-    __syncthreads();
-    double* Mt = ws + kVjM;  // a transposed chi x chi environment
-    if (a.envs) {
-      int st = d;
-      for (int q = 0; q < h.k; ++q) {
-        if (q != h.p) {
-          const int c = chi2[q];
-          const double* si = ss + kSideSI + q * 64;
-          for (int i = tid; i < c * c; i += kSuThreads) Mt[(i / c) + c * (i % c)] = si[i];
-          __syncthreads();
-          absorb_any<double>(c, cur, nxt, n2, st, Mt, tid, kSuThreads);
-          __syncthreads();
-          double* t = cur;
-          cur = nxt;
-          nxt = t;
-        }
-        st *= chi2[q];
-      }
-    }
-    // normalisation backwards: Cbar = (Abar - A <A, Abar>) / |C|
-    const double* Ab = cot_out + a.cap_off[x];
-    double s2 = 0.0, dt = 0.0;
-    for (int i = tid; i < n2; i += kSuThreads) {
-      s2 = fma(cur[i], cur[i], s2);
-      dt = fma(cur[i], Ab[i], dt);
-    }
-    s2 = block_sum(s2, red);
-    dt = block_sum(dt, red);
-    if (tid == 0) {
-      const double nc = sqrt(s2);
-      s_scale = (a.normalize && nc > 0.0) ? 1.0 / nc : 1.0;
-      s_dot = (a.normalize && nc > 0.0) ? dt / s2 : 0.0;  // <A, Abar> / |C| with A = C / |C|
-    }
-    __syncthreads();
-    for (int i = tid; i < n2; i += kSuThreads) nxt[i] = (Ab[i] - cur[i] * s_dot) * s_scale;
-    __syncthreads();
-    {
-      double* t = cur;
-      cur = nxt;
-      nxt = t;
-    }
-    // inverse-sqrt environments backwards: the transposes of the matrices absorbed
-    if (a.envs) {
-      int st = d;
-      for (int q = 0; q < h.k; ++q) {
-        if (q != h.p) {
-          const int c = chi2[q];
-          absorb_any<double>(c, cur, nxt, n2, st, ss + kSideSI + q * 64, tid, kSuThreads);
-          __syncthreads();
-          double* t = cur;
-          cur = nxt;
-          nxt = t;
-        }
-        st *= chi2[q];
-      }
-    }
-    for (int i = tid; i < n2; i += kSuThreads) {
-      int row, s_, b;
-      split_index(h, chi2, i, row, s_, b);
-      Y[row + (size_t)m * (s_ + d * b)] = cur[i];
-    }
-    __syncthreads();
-    // Ybar = Q [Z; 0] + Ybar_perp
-    apply_reflectors(ss, m, r, Y, ncol2, true);
-    for (int i = tid; i < r * ncol2; i += kSuThreads) {
-      const int t = i % r, col = i / r;
-      Z[i] = Y[t + (size_t)m * col];
-    }
-    __syncthreads();
-    for (int i = tid; i < r * ncol2; i += kSuThreads) Y[(i % r) + (size_t)m * (i / r)] = 0.0;
-    __syncthreads();
-    apply_reflectors(ss, m, r, Y, ncol2, false);
-    // in-range cotangents of the singular vectors, and of sigma
-    for (int i = tid; i < (side == 0 ? mt : nt) * k; i += kSuThreads) {
-      const int row = i % (side == 0 ? mt : nt), b = i / (side == 0 ? mt : nt);
-      const int t = side == 0 ? row % ru : row / dv;
-      const int s_ = side == 0 ? row / ru : row % dv;
-      (side == 0 ? Ub : Vb)[i] = Z[t + r * (s_ + d * b)] * js[kJobS + b];
-    }
-    for (int b = threadIdx.x >> 5; b < k; b += kSuWarps) {
-      const int lane = tid & 31;
-      double acc = 0.0;
-      for (int i = lane; i < r * d; i += 32) {
-        const int t = i % r, s_ = i / r;
-        const double f = side == 0 ? UF[(t + ru * s_) + (size_t)mt * b] : VF[(s_ + dv * t) + (size_t)nt * b];
-        acc = fma(f, Z[t + r * (s_ + d * b)], acc);
-      }
-      acc = warp_sum(acc);
-      if (lane == 0) sb[b] += 0.5 * acc * safe_inv(js[kJobS + b]);
-    }
-    __syncthreads();
-  }
-
+  const double* RU = c.ssd[0] + kSideR;
+  const double* RV = c.ssd[1] + kSideR;
+  double* wj = c.wj;
+  const double* Ub = wj + kVjUb;
+  const double* Vb = wj + kVjVb;
+  const double* sb = wj + kVjSb;
   // ---- 3: the SVD adjoint in range
   double* UtUb = wj + kVjUtUb;
   double* VtVb = wj + kVjVtVb;
@@ -1294,7 +1335,7 @@ __global__ void __launch_bounds__(kSuThreads, 1)
     const int p = i % n, q = i / n;
     double v = 0.0;
     if (p == q) {
-      v = p < k ? sb[p] : 0.0;
+      v = p < k ? sb[p] + sb[kSuMaxTheta + p] : 0.0;
     } else if (p < k || q < k) {
       const double den = sig[q] * sig[q] - sig[p] * sig[p];
       const double F = fabs(den) > 1e-14 * smax2 ? 1.0 / den : 0.0;
@@ -1427,56 +1468,68 @@ __global__ void __launch_bounds__(kSuThreads, 1)
   }
   __syncthreads();
 
-  // ---- 5: Wbar = Q [Rbar; 0] + Ybar_perp H, then the sqrt environments backwards
-  for (int side = 0; side < 2; ++side) {
-    const SideShape& h = hs[side];
-    const double* ss = ssd[side];
-    double* ws = wj + (size_t)side * kVjSide;
-    const double* Y = ws + kVjY;
-    const double* Rb = ws + kVjRb;
-    const double* H = ws + kVjH;
-    double* W = ws + kVjW;
-    const int x = xs[side], m = h.m, d = h.d, r = (int)ss[kSideMeta], ncol = d * ce, rowsH = d * k;
-    for (int i = tid; i < m * ncol; i += kSuThreads) W[i] = (i % m) < r ? Rb[(i % m) + r * (i / m)] : 0.0;
-    __syncthreads();
-    apply_reflectors(ss, m, r, W, ncol, false);
-    for (int i = tid; i < m * ncol; i += kSuThreads) {
-      const int row = i % m, col = i / m;
-      double acc = W[i];
-      for (int q = 0; q < rowsH; ++q) acc = fma(Y[row + (size_t)m * q], H[q + rowsH * col], acc);
-      W[i] = acc;
-    }
-    __syncthreads();
-    double* cur = ws + kVjT0;
-    double* nxt = ws + kVjT1;
-    for (int i = tid; i < h.n; i += kSuThreads) {
-      int row, s_, b;
-      split_index(h, h.chi, i, row, s_, b);
-      cur[i] = W[row + (size_t)m * (s_ + d * b)];
-    }
-    __syncthreads();
-    if (a.envs) {
-      double* Mt = ws + kVjM;
-      int st = d;
-      for (int q = 0; q < h.k; ++q) {
-        if (q != h.p) {
-          const int c = h.chi[q];
-          const double* sq = a.side_sqrt + (size_t)(2 * j + side) * kSqrtStride + q * 64;
-          for (int i = tid; i < c * c; i += kSuThreads) Mt[(i / c) + c * (i % c)] = sq[i];
-          __syncthreads();
-          absorb_any<double>(c, cur, nxt, h.n, st, Mt, tid, kSuThreads);
-          __syncthreads();
-          double* t = cur;
-          cur = nxt;
-          nxt = t;
-        }
-        st *= h.chi[q];
-      }
-    }
-    double* dst = cot_in + a.cap_off[x];
-    for (int i = tid; i < h.n; i += kSuThreads) dst[i] = cur[i];
-    __syncthreads();
+}
+
+// Stage 3, one CTA per (gate, side): Wbar = Q [Rbar; 0] + Ybar_perp H, then the
+// sqrt environments backwards, into the cotangent of the site tensor.
+__global__ void __launch_bounds__(kSuThreads, 2)
+    su_vjp_rebuild_kernel(SuArgs a, const int* post_dims, double* cot_in, double* work) {
+  const int j = blockIdx.x >> 1, side = blockIdx.x & 1, tid = threadIdx.x;
+  if (j >= a.njobs) return;
+  VjpCtx c;
+  if (!vjp_ctx(a, post_dims, work, j, c)) return;
+  const double* ssd[2] = {c.ssd[0], c.ssd[1]};
+  const SideShape* hs = c.hs;
+  const int* xs = c.xs;
+  const int k = c.k, ce = c.ce;
+  double* wj = c.wj;
+  const SideShape& h = hs[side];
+  const double* ss = ssd[side];
+  double* ws = wj + (size_t)side * kVjSide;
+  const double* Y = ws + kVjY;
+  const double* Rb = ws + kVjRb;
+  const double* H = ws + kVjH;
+  double* W = ws + kVjW;
+  const int x = xs[side], m = h.m, d = h.d, r = (int)ss[kSideMeta], ncol = d * ce, rowsH = d * k;
+  for (int i = tid; i < m * ncol; i += kSuThreads) W[i] = (i % m) < r ? Rb[(i % m) + r * (i / m)] : 0.0;
+  __syncthreads();
+  apply_reflectors(ss, m, r, W, ncol, false);
+  for (int i = tid; i < m * ncol; i += kSuThreads) {
+    const int row = i % m, col = i / m;
+    double acc = W[i];
+    for (int q = 0; q < rowsH; ++q) acc = fma(Y[row + (size_t)m * q], H[q + rowsH * col], acc);
+    W[i] = acc;
   }
+  __syncthreads();
+  double* cur = ws + kVjT0;
+  double* nxt = ws + kVjT1;
+  for (int i = tid; i < h.n; i += kSuThreads) {
+    int row, s_, b;
+    split_index(h, h.chi, i, row, s_, b);
+    cur[i] = W[row + (size_t)m * (s_ + d * b)];
+  }
+  __syncthreads();
+  if (a.envs) {
+    double* Mt = ws + kVjM;
+    int st = d;
+    for (int q = 0; q < h.k; ++q) {
+      if (q != h.p) {
+        const int c = h.chi[q];
+        const double* sq = a.side_sqrt + (size_t)(2 * j + side) * kSqrtStride + q * 64;
+        for (int i = tid; i < c * c; i += kSuThreads) Mt[(i / c) + c * (i % c)] = sq[i];
+        __syncthreads();
+        absorb_any<double>(c, cur, nxt, h.n, st, Mt, tid, kSuThreads);
+        __syncthreads();
+        double* t = cur;
+        cur = nxt;
+        nxt = t;
+      }
+      st *= h.chi[q];
+    }
+  }
+  double* dst = cot_in + a.cap_off[x];
+  for (int i = tid; i < h.n; i += kSuThreads) dst[i] = cur[i];
+  __syncthreads();
 }
 
 }  // namespace
@@ -1986,10 +2039,16 @@ void su_launch_fwd_stages(const SuArgs& a, cudaStream_t s) {
   GBTN_CUDA(cudaGetLastError());
 }
 
+// cot_out and cot_in may be the same buffer: stage 1 reads every gate site's
+// cotangent before stage 3 (a later launch) writes any.
 void su_launch_vjp_kernel(const SuArgs& a, const int* post_dims, const double* cot_out, double* cot_in,
                           double* gate_cot, double* work, cudaStream_t s) {
   if (a.njobs == 0) return;
-  su_vjp_kernel<<<a.njobs, kSuThreads, 0, s>>>(a, post_dims, cot_out, cot_in, gate_cot, work);
+  su_vjp_side_kernel<<<2 * a.njobs, kSuThreads, 0, s>>>(a, post_dims, cot_out, work);
+  GBTN_CUDA(cudaGetLastError());
+  su_vjp_core_kernel<<<a.njobs, kSuThreads, 0, s>>>(a, post_dims, gate_cot, work);
+  GBTN_CUDA(cudaGetLastError());
+  su_vjp_rebuild_kernel<<<2 * a.njobs, kSuThreads, 0, s>>>(a, post_dims, cot_in, work);
   GBTN_CUDA(cudaGetLastError());
 }
 
