@@ -106,9 +106,10 @@ typedef struct gbtn_graph_desc {
                                     expect / expect2 (real part of <O>, O
                                     real), vertex and edge scalars,
                                     logscalar, rescale_messages and
-                                    rescale_partitions.  BF16 sweeps and the
-                                    energy / gradient entry points return
-                                    GBTN_ERR_UNSUPPORTED.
+                                    rescale_partitions, and the energy and
+                                    gradient entry points (the real part of
+                                    the loss; gradients dL/dRe + i dL/dIm).
+                                    BF16 sweeps return GBTN_ERR_UNSUPPORTED.
                                     (test/test_belief_propagation.jl:18-20) */
 } gbtn_graph_desc;
 
@@ -337,12 +338,17 @@ int gbtn_su_set_edge_dims(gbtn_su* su, const int32_t* dims);
  * concatenated in vertex order with post_edge_dims; cot_in receives
  * dL/d(current tensors) in the current shapes (sites without a gate pass
  * theirs through); gate_cot (may be NULL): n_gates (du dv)^2 matrices dL/dG
- * (with per_gate = 0 the shared gate's cotangent is their sum).  The
- * environments are held constant.  Degenerate singular values (closer than
- * 1e-14 sigma_max^2) and kept zero singular values contribute no derivative. */
+ * (with per_gate = 0 the shared gate's cotangent is their sum); env_cot
+ * (may be NULL): dL/d(envs) in the layout of envs (2 ne messages of chi_max^2
+ * values, each chi x chi message's leading entries; zeros without envs),
+ * through the square-root and inverse-square-root environments (positive
+ * semi-definite messages, as BP's are).  Degenerate singular values (closer
+ * than 1e-14 sigma_max^2) and kept zero singular values contribute no
+ * derivative. */
 int gbtn_su_apply_vjp(gbtn_su* su, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
                       const double* envs, int32_t maxdim, double cutoff, int32_t normalize,
-                      const int32_t* post_edge_dims, const double* cot_out, double* cot_in, double* gate_cot);
+                      const int32_t* post_edge_dims, const double* cot_out, double* cot_in, double* gate_cot,
+                      double* env_cot);
 /* gbtn_su_apply that also records a tape for the adjoint of the whole gate
  * sequence (real tensors): the state before every batch of consecutive
  * vertex-disjoint gates (device copies of the tensors and bond dimensions),
@@ -354,12 +360,14 @@ int gbtn_su_apply_taped(gbtn_su* su, int32_t n_gates, const int32_t* edges, cons
                         double* svals, gbtn_su_tape** tape);
 /* The pullback of a taped apply: cot_out = dL/d(tensors it left), in their
  * shapes; cot_in = dL/d(tensors before it), in those shapes; gate_cot
- * (may be NULL): n_gates (du dv)^2 matrices dL/dG in the order given.  The
- * batches run backwards on the device (each batch's saved state restored, the
- * cotangents kept in device memory); the state is left as the taped apply
- * left it.  The tape can be pulled back more than once. */
+ * (may be NULL): n_gates (du dv)^2 matrices dL/dG in the order given;
+ * env_cot (may be NULL): dL/d(envs), summed over the batches, as in
+ * gbtn_su_apply_vjp.  The batches run backwards on the device (each batch's
+ * saved state restored, the cotangents kept in device memory); the state is
+ * left as the taped apply left it.  The tape can be pulled back more than
+ * once. */
 int gbtn_su_tape_vjp(gbtn_su* su, const gbtn_su_tape* tape, const double* cot_out, double* cot_in,
-                     double* gate_cot);
+                     double* gate_cot, double* env_cot);
 int gbtn_su_tape_destroy(gbtn_su_tape* tape);
 
 /* ---- energies and gradients (FP64) ------------------------------------------ */

@@ -1091,7 +1091,11 @@ constexpr int kVjZ = kVjW + kSuMaxN;        // Z = Q^T Ybar (r x d k)
 constexpr int kVjRb = kVjZ + kVjpSmall;     // Rbar (r x d chi)
 constexpr int kVjH = kVjRb + kVjpSmall;     // H (d k x d chi)
 constexpr int kVjM = kVjH + kVjpSmall;      // M (k x d x d chi)
-constexpr int kVjSide = kVjM + kVjpSmall;
+constexpr int kVjChainC = kVjM + kVjpSmall;  // Y and its inverse-sqrt-absorbed stages (kMaxDeg tensors)
+constexpr int kVjChainB = kVjChainC + kMaxDeg * kSuMaxN;  // A and its sqrt-absorbed stages
+constexpr int kVjSiBar = kVjChainB + kMaxDeg * kSuMaxN;   // dL/d(inverse sqrt environment), per leg
+constexpr int kVjSBar = kVjSiBar + kMaxDeg * 64;          // dL/d(sqrt environment), per leg
+constexpr int kVjSide = kVjSBar + kMaxDeg * 64;
 // per job, after both sides
 constexpr int kVjUb = 2 * kVjSide;          // Ubar in range (mt x k)
 constexpr int kVjVb = kVjUb + kVjpSmall;    // Vbar in range (nt x k)
@@ -1108,6 +1112,26 @@ constexpr int kVjSb = kVjPsi + kVjpSmall;   // sigmabar, each side's part (2 x k
 constexpr int kVjStride = kVjSb + 2 * kSuMaxTheta;  // sigmabar: one part per side
 
 __device__ __forceinline__ double safe_inv(double x) { return x > 0.0 ? 1.0 / x : 0.0; }
+
+// R[b + c a] = sum over the fibers of leg (st, c) of X[.. b ..] Y[.. a ..]
+// (n elements): the cotangent of the matrix M of an absorption
+// out[.. b ..] = sum_a M[b + c a] in[.. a ..], with X = dL/d(out), Y = in.
+// One warp per entry; ends with a CTA barrier.
+__device__ void leg_gram(const double* X, const double* Y, int n, int st, int c, double* R) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nfib = n / c;
+  for (int o = warp; o < c * c; o += kSuWarps) {
+    const int b = o % c, a_ = o / c;
+    double acc = 0.0;
+    for (int f = lane; f < nfib; f += 32) {
+      const int lo = f % st, base = lo + (f - lo) * c;
+      acc = fma(X[base + b * st], Y[base + a_ * st], acc);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) R[o] = acc;
+  }
+  __syncthreads();
+}
 
 // The per-gate context of the three adjoint launches.
 struct VjpCtx {
@@ -1153,7 +1177,7 @@ __device__ bool vjp_ctx(const SuArgs& a, const int* post_dims, double* work, int
 // cotangent split into Z = Q^T Ybar and Ybar_perp, the in-range cotangents of
 // the singular vectors and this side's part of sigmabar.
 __global__ void __launch_bounds__(kSuThreads, 2)
-    su_vjp_side_kernel(SuArgs a, const int* post_dims, const double* cot_out, double* work) {
+    su_vjp_side_kernel(SuArgs a, const int* post_dims, const double* cot_out, double* work, int want_env) {
   const int j = blockIdx.x >> 1, side = blockIdx.x & 1, tid = threadIdx.x;
   if (j >= a.njobs) return;
   __shared__ double red[kSuWarps + 1];
@@ -1195,15 +1219,17 @@ __global__ void __launch_bounds__(kSuThreads, 2)
   }
   __syncthreads();
   apply_reflectors(ss, m, r, Y, ncol2, false);
-  double* cur = ws + kVjT0;
-  double* nxt = ws + kVjT1;
+  // C = Y with the inverse-sqrt environments absorbed leg by leg; every stage
+  // is kept (stage 0 = Y in tensor layout) for their cotangents
+  double* chain = ws + kVjChainC;
   for (int i = tid; i < n2; i += kSuThreads) {
     int row, s_, b;
     split_index(h, chi2, i, row, s_, b);
-    cur[i] = Y[row + (size_t)m * (s_ + d * b)];
+    chain[i] = Y[row + (size_t)m * (s_ + d * b)];
   }
   __syncthreads();
   double* Mt = ws + kVjM;  // a transposed chi x chi environment
+  int nst = 0;             // absorbed legs
   if (a.envs) {
     int st = d;
     for (int q = 0; q < h.k; ++q) {
@@ -1212,21 +1238,21 @@ __global__ void __launch_bounds__(kSuThreads, 2)
         const double* si = ss + kSideSI + q * 64;
         for (int i = tid; i < c * c; i += kSuThreads) Mt[(i / c) + c * (i % c)] = si[i];
         __syncthreads();
-        absorb_any<double>(c, cur, nxt, n2, st, Mt, tid, kSuThreads);
+        absorb_any<double>(c, chain + (size_t)nst * kSuMaxN, chain + (size_t)(nst + 1) * kSuMaxN, n2, st, Mt, tid,
+                           kSuThreads);
         __syncthreads();
-        double* t = cur;
-        cur = nxt;
-        nxt = t;
+        ++nst;
       }
       st *= chi2[q];
     }
   }
+  const double* C = chain + (size_t)nst * kSuMaxN;
   // normalisation backwards: Cbar = (Abar - A <A, Abar>) / |C|
   const double* Ab = cot_out + a.cap_off[x];
   double s2 = 0.0, dt = 0.0;
   for (int i = tid; i < n2; i += kSuThreads) {
-    s2 = fma(cur[i], cur[i], s2);
-    dt = fma(cur[i], Ab[i], dt);
+    s2 = fma(C[i], C[i], s2);
+    dt = fma(C[i], Ab[i], dt);
   }
   s2 = block_sum(s2, red);
   dt = block_sum(dt, red);
@@ -1236,26 +1262,36 @@ __global__ void __launch_bounds__(kSuThreads, 2)
     s_dot = (a.normalize && nc > 0.0) ? dt / s2 : 0.0;  // <A, Abar> / |C| with A = C / |C|
   }
   __syncthreads();
-  for (int i = tid; i < n2; i += kSuThreads) nxt[i] = (Ab[i] - cur[i] * s_dot) * s_scale;
+  double* cur = ws + kVjT0;
+  double* nxt = ws + kVjT1;
+  for (int i = tid; i < n2; i += kSuThreads) cur[i] = (Ab[i] - C[i] * s_dot) * s_scale;
   __syncthreads();
-  {
-    double* t = cur;
-    cur = nxt;
-    nxt = t;
-  }
-  // inverse-sqrt environments backwards: the transposes of the matrices absorbed
+  // inverse-sqrt environments backwards, last leg first: the cotangent of each
+  // matrix (M = si^T was absorbed, so dL/dsi = gram^T), then the transposed absorb
   if (a.envs) {
-    int st = d;
-    for (int q = 0; q < h.k; ++q) {
-      if (q != h.p) {
-        const int c = chi2[q];
-        absorb_any<double>(c, cur, nxt, n2, st, ss + kSideSI + q * 64, tid, kSuThreads);
-        __syncthreads();
-        double* t = cur;
-        cur = nxt;
-        nxt = t;
+    double* sib = ws + kVjSiBar;
+    int st_q[kMaxDeg];
+    {
+      int st = d;
+      for (int q = 0; q < h.k; ++q) {
+        st_q[q] = st;
+        st *= chi2[q];
       }
-      st *= chi2[q];
+    }
+    int stage = nst;
+    for (int q = h.k - 1; q >= 0; --q) {
+      if (q == h.p) continue;
+      const int c = chi2[q];
+      --stage;
+      if (want_env) {
+        leg_gram(cur, chain + (size_t)stage * kSuMaxN, n2, st_q[q], c, Mt);
+        for (int i = tid; i < c * c; i += kSuThreads) sib[q * 64 + i] = Mt[(i / c) + c * (i % c)];
+      }
+      absorb_any<double>(c, cur, nxt, n2, st_q[q], ss + kSideSI + q * 64, tid, kSuThreads);
+      __syncthreads();
+      double* t = cur;
+      cur = nxt;
+      nxt = t;
     }
   }
   for (int i = tid; i < n2; i += kSuThreads) {
@@ -1473,7 +1509,7 @@ __global__ void __launch_bounds__(kSuThreads, 1)
 // Stage 3, one CTA per (gate, side): Wbar = Q [Rbar; 0] + Ybar_perp H, then the
 // sqrt environments backwards, into the cotangent of the site tensor.
 __global__ void __launch_bounds__(kSuThreads, 2)
-    su_vjp_rebuild_kernel(SuArgs a, const int* post_dims, double* cot_in, double* work) {
+    su_vjp_rebuild_kernel(SuArgs a, const int* post_dims, double* cot_in, double* work, int want_env) {
   const int j = blockIdx.x >> 1, side = blockIdx.x & 1, tid = threadIdx.x;
   if (j >= a.njobs) return;
   VjpCtx c;
@@ -1511,25 +1547,159 @@ __global__ void __launch_bounds__(kSuThreads, 2)
   __syncthreads();
   if (a.envs) {
     double* Mt = ws + kVjM;
-    int st = d;
-    for (int q = 0; q < h.k; ++q) {
-      if (q != h.p) {
-        const int c = h.chi[q];
-        const double* sq = a.side_sqrt + (size_t)(2 * j + side) * kSqrtStride + q * 64;
-        for (int i = tid; i < c * c; i += kSuThreads) Mt[(i / c) + c * (i % c)] = sq[i];
-        __syncthreads();
-        absorb_any<double>(c, cur, nxt, h.n, st, Mt, tid, kSuThreads);
-        __syncthreads();
-        double* t = cur;
-        cur = nxt;
-        nxt = t;
+    const double* sq0 = a.side_sqrt + (size_t)(2 * j + side) * kSqrtStride;
+    int st_q[kMaxDeg];
+    {
+      int st = d;
+      for (int q = 0; q < h.k; ++q) {
+        st_q[q] = st;
+        st *= h.chi[q];
       }
-      st *= h.chi[q];
+    }
+    // with the environments' cotangents wanted: the forward's stages A, A S_q0,
+    // A S_q0 S_q1, ... (B = the last), recomputed from the site tensor
+    double* chain = ws + kVjChainB;
+    int stage = 0;
+    if (want_env) {
+      const double* A = a.tens + a.cap_off[x];
+      for (int i = tid; i < h.n; i += kSuThreads) chain[i] = A[i];
+      __syncthreads();
+      for (int q = 0; q < h.k; ++q) {
+        if (q == h.p) continue;
+        absorb_any<double>(h.chi[q], chain + (size_t)stage * kSuMaxN, chain + (size_t)(stage + 1) * kSuMaxN, h.n,
+                           st_q[q], sq0 + q * 64, tid, kSuThreads);
+        __syncthreads();
+        ++stage;
+      }
+    }
+    // sqrt environments backwards, last leg first (each S_q was absorbed as is)
+    for (int q = h.k - 1; q >= 0; --q) {
+      if (q == h.p) continue;
+      const int c = h.chi[q];
+      const double* sq = sq0 + q * 64;
+      if (want_env) {
+        --stage;
+        leg_gram(cur, chain + (size_t)stage * kSuMaxN, h.n, st_q[q], c, ws + kVjSBar + q * 64);
+      }
+      for (int i = tid; i < c * c; i += kSuThreads) Mt[(i / c) + c * (i % c)] = sq[i];
+      __syncthreads();
+      absorb_any<double>(c, cur, nxt, h.n, st_q[q], Mt, tid, kSuThreads);
+      __syncthreads();
+      double* t = cur;
+      cur = nxt;
+      nxt = t;
     }
   }
   double* dst = cot_in + a.cap_off[x];
   for (int i = tid; i < h.n; i += kSuThreads) dst[i] = cur[i];
   __syncthreads();
+}
+
+// Stage 4 (environments' cotangents wanted), one CTA per (gate, side): for
+// every other leg q, the environment M of the message into the site along q
+// entered as S = f(M) = V f(L) V^T (f = sqrt) and Si (f = 1/sqrt) on the kept
+// eigenvalues of (M + M^T)/2 (the forward's rule; dropped ones give f = 0), so
+// dL/dM = sym(V [Lf o (V^T Sbar V) + Lg o (V^T Sibar V)] V^T), with the divided
+// differences Lf_ij = (f(l_i) - f(l_j)) / (l_i - l_j) (f'(l_i) on the diagonal):
+// 1 / (sqrt(l_i) + sqrt(l_j)) and -1 / (sqrt(l_i l_j) (sqrt(l_i) + sqrt(l_j))) for
+// two kept eigenvalues (Daleckii-Krein).  Added to env_cot (each directed
+// edge's environment serves one side of one gate of a batch).
+__global__ void __launch_bounds__(kSuThreads, 1)
+    su_vjp_env_kernel(SuArgs a, const int* post_dims, double* work, double* env_cot) {
+  const int j = blockIdx.x >> 1, side = blockIdx.x & 1, tid = threadIdx.x;
+  if (j >= a.njobs || !a.envs) return;
+  VjpCtx c;
+  if (!vjp_ctx(a, post_dims, work, j, c)) return;
+  const SideShape& h = c.hs[side];
+  const int x = c.xs[side];
+  double* ws = c.wj + (size_t)side * kVjSide;
+  // scratch for the eigen-decomposition (the side's M region is free now)
+  double* E = ws + kVjM;
+  double* Sd = E;            // 64: S (recomputed)
+  double* Sid = E + 64;      // 64: Si (recomputed)
+  double* A8 = E + 128;      // 64
+  double* V8 = E + 192;      // 64
+  double* sig = E + 256;     // 64
+  double* T1 = E + 320;      // 64
+  double* T2 = E + 384;      // 64
+  double* red = E + 448;     // 32
+  double* aux = E + 480;     // 192
+  double* wk = E + 672;      // 256: SVD work
+  double* ex = E + 928;      // 256: SVD extra
+  int* iord = reinterpret_cast<int*>(E + 1184);  // 64
+  int* iperm = iord + 64;                         // 64
+  __shared__ int s_flag;
+  SvdBufs sb{wk, aux, aux + 64, aux + 128, iperm, iord, &s_flag, red, ex};
+  for (int q = 0; q < h.k; ++q) {
+    if (q == h.p) continue;
+    const int cq = h.chi[q];
+    const int f = a.leg_edge[a.leg_ptr[x] + q];
+    const int de_in = a.edge_u[f] == x ? 2 * f + 1 : 2 * f;
+    const double* env = a.envs + (size_t)de_in * a.chimax * a.chimax;
+    cta_env_sqrt(env, cq, Sd, Sid, A8, V8, sig, sb);
+    // the kept count, by the forward's rule
+    __shared__ int s_keep;
+    if (tid == 0) {
+      double tot = 0.0;
+      for (int i = 0; i < cq; ++i) tot += sig[i];
+      if (tot == 0.0) tot = 1.0;
+      int kk = cq;
+      double disc = 0.0;
+      while (kk > 1 && disc + sig[kk - 1] <= 10.0 * 2.220446049250313e-16 * tot) {
+        disc += sig[kk - 1];
+        --kk;
+      }
+      s_keep = kk;
+    }
+    __syncthreads();
+    const int kk = s_keep;
+    const double* sbar = ws + kVjSBar + q * 64;
+    const double* sibar = ws + kVjSiBar + q * 64;
+    // T1 = V^T Sbar V, T2 = V^T Sibar V
+    for (int i = tid; i < cq * cq; i += kSuThreads) {
+      const int p_ = i % cq, r_ = i / cq;
+      double a1 = 0.0, a2 = 0.0;
+      for (int u = 0; u < cq; ++u)
+        for (int v = 0; v < cq; ++v) {
+          const double w = V8[u + cq * p_] * V8[v + cq * r_];
+          a1 = fma(w, sbar[u + cq * v], a1);
+          a2 = fma(w, sibar[u + cq * v], a2);
+        }
+      T1[i] = a1;
+      T2[i] = a2;
+    }
+    __syncthreads();
+    // divided differences, in place: T1 <- Lf o T1 + Lg o T2
+    for (int i = tid; i < cq * cq; i += kSuThreads) {
+      const int p_ = i % cq, r_ = i / cq;
+      const bool kp = p_ < kk, kr = r_ < kk;
+      double lf = 0.0, lg = 0.0;
+      if (kp && kr) {
+        const double sp = sqrt(sig[p_]), sr = sqrt(sig[r_]);
+        lf = 1.0 / (sp + sr);
+        lg = -1.0 / (sp * sr * (sp + sr));
+      } else if (kp || kr) {  // one kept, one dropped (f = 0 there)
+        const double lk = kp ? sig[p_] : sig[r_], ld = kp ? sig[r_] : sig[p_];
+        const double den = lk - ld;
+        if (den > 0.0) {
+          lf = sqrt(lk) / den;
+          lg = 1.0 / (sqrt(lk) * den);
+        }
+      }
+      T1[i] = lf * T1[i] + lg * T2[i];
+    }
+    __syncthreads();
+    // V T1 V^T, symmetrised (the forward used (M + M^T) / 2)
+    for (int i = tid; i < cq * cq; i += kSuThreads) {
+      const int b = i % cq, a_ = i / cq;
+      double acc = 0.0;
+      for (int u = 0; u < cq; ++u)
+        for (int v = 0; v < cq; ++v)
+          acc = fma(V8[b + cq * u] * V8[a_ + cq * v] + V8[a_ + cq * u] * V8[b + cq * v], 0.5 * T1[u + cq * v], acc);
+      env_cot[(size_t)de_in * a.chimax * a.chimax + i] += acc;
+    }
+    __syncthreads();
+  }
 }
 
 }  // namespace
@@ -2042,14 +2212,19 @@ void su_launch_fwd_stages(const SuArgs& a, cudaStream_t s) {
 // cot_out and cot_in may be the same buffer: stage 1 reads every gate site's
 // cotangent before stage 3 (a later launch) writes any.
 void su_launch_vjp_kernel(const SuArgs& a, const int* post_dims, const double* cot_out, double* cot_in,
-                          double* gate_cot, double* work, cudaStream_t s) {
+                          double* gate_cot, double* env_cot, double* work, cudaStream_t s) {
   if (a.njobs == 0) return;
-  su_vjp_side_kernel<<<2 * a.njobs, kSuThreads, 0, s>>>(a, post_dims, cot_out, work);
+  const int want_env = env_cot && a.envs ? 1 : 0;
+  su_vjp_side_kernel<<<2 * a.njobs, kSuThreads, 0, s>>>(a, post_dims, cot_out, work, want_env);
   GBTN_CUDA(cudaGetLastError());
   su_vjp_core_kernel<<<a.njobs, kSuThreads, 0, s>>>(a, post_dims, gate_cot, work);
   GBTN_CUDA(cudaGetLastError());
-  su_vjp_rebuild_kernel<<<2 * a.njobs, kSuThreads, 0, s>>>(a, post_dims, cot_in, work);
+  su_vjp_rebuild_kernel<<<2 * a.njobs, kSuThreads, 0, s>>>(a, post_dims, cot_in, work, want_env);
   GBTN_CUDA(cudaGetLastError());
+  if (want_env) {
+    su_vjp_env_kernel<<<2 * a.njobs, kSuThreads, 0, s>>>(a, post_dims, work, env_cot);
+    GBTN_CUDA(cudaGetLastError());
+  }
 }
 
 }  // namespace gbtn
@@ -2162,7 +2337,7 @@ void tape_snapshot(gbtn_su* S, gbtn_su_tape* T, cudaStream_t s) {
 // cotangents, carved from the state's adjoint buffer.
 struct VjpScratch {
   double *q = nullptr, *js = nullptr, *full = nullptr, *sq = nullptr, *work = nullptr;
-  double *cot = nullptr, *stage = nullptr, *gc = nullptr;
+  double *cot = nullptr, *stage = nullptr, *gc = nullptr, *env = nullptr;
   int* edim_fwd = nullptr;
   int chunk = 0;
   VjpScratch(gbtn_su* S, int max_jobs, long long gc_elems) {
@@ -2172,6 +2347,7 @@ struct VjpScratch {
                             (size_t)chunk * gbtn::kSuFullStride,     (size_t)chunk * 2 * gbtn::kSuSqrtStride,
                             (size_t)chunk * gbtn::kSuVjpStride,      cap,
                             cap,                                     (size_t)std::max<long long>(gc_elems, 1),
+                            (size_t)std::max(2 * S->ne, 1) * S->chimax * S->chimax,
                             (size_t)std::max(S->ne, 1)};
     size_t total = 0;
     for (size_t n : sizes) total += (n + 31) / 32 * 32;
@@ -2184,8 +2360,8 @@ struct VjpScratch {
       S->vjp_bytes = bytes;
     }
     double* p = static_cast<double*>(S->d_vjp);
-    double** dst[] = {&q, &js, &full, &sq, &work, &cot, &stage, &gc};
-    for (int i = 0; i < 8; ++i) {
+    double** dst[] = {&q, &js, &full, &sq, &work, &cot, &stage, &gc, &env};
+    for (int i = 0; i < 9; ++i) {
       *dst[i] = p;
       p += (sizes[i] + 31) / 32 * 32;
     }
@@ -2199,7 +2375,7 @@ struct VjpScratch {
 // before it writes them, and no other gate touches them).
 void su_vjp_batch(gbtn_su* S, const SuJob* d_jobs, int njobs, const double* d_gates, int per_gate, long long gsz,
                   const double* d_envs, int md, double cutoff, int normalize, int bmax, const int* d_post,
-                  const double* d_cot_out, double* d_cot_in, double* d_gc, VjpScratch& w) {
+                  const double* d_cot_out, double* d_cot_in, double* d_gc, double* d_env_cot, VjpScratch& w) {
   cudaStream_t s = S->stream;
   for (int j0 = 0; j0 < njobs; j0 += w.chunk) {
     SuArgs a{};
@@ -2230,7 +2406,7 @@ void su_vjp_batch(gbtn_su* S, const SuJob* d_jobs, int njobs, const double* d_ga
     a.edim = w.edim_fwd;
     gbtn::su_launch_fwd_stages(a, s);
     a.edim = S->d_edim;
-    gbtn::su_launch_vjp_kernel(a, d_post, d_cot_out, d_cot_in, d_gc ? d_gc + gsz * j0 : nullptr, w.work, s);
+    gbtn::su_launch_vjp_kernel(a, d_post, d_cot_out, d_cot_in, d_gc ? d_gc + gsz * j0 : nullptr, d_env_cot, w.work, s);
   }
 }
 
@@ -2578,7 +2754,8 @@ int gbtn_su_tape_destroy(gbtn_su_tape* T) {
   return GBTN_OK;
 }
 
-int gbtn_su_tape_vjp(gbtn_su* S, const gbtn_su_tape* T, const double* cot_out, double* cot_in, double* gate_cot) {
+int gbtn_su_tape_vjp(gbtn_su* S, const gbtn_su_tape* T, const double* cot_out, double* cot_in, double* gate_cot,
+                     double* env_cot) {
   const gbtn::NvtxRange nvtx_range("gbtn_su_tape_vjp");
   if (!S || !T || !cot_out || !cot_in) return GBTN_ERR_INVALID;
   if (T->su != S) return su_fail(S, GBTN_ERR_INVALID, "simple update adjoint: the tape belongs to another state");
@@ -2594,6 +2771,9 @@ int gbtn_su_tape_vjp(gbtn_su* S, const gbtn_su_tape* T, const double* cot_out, d
     VjpScratch w(S, maxb, T->gsz * T->n_gates);
     double* d_cot = w.cot;
     double* d_gc = w.gc;
+    const size_t env_elems = (size_t)2 * S->ne * S->chimax * S->chimax;
+    double* d_env = env_cot && T->d_envs ? w.env : nullptr;
+    if (d_env) GBTN_CUDA(cudaMemsetAsync(d_env, 0, sizeof(double) * env_elems, s));
     su_scatter(S, final_dims, cot_out, nullptr, d_cot, w.stage);
     GBTN_CUDA(cudaMemsetAsync(S->d_status, 0, sizeof(int), s));
     for (int b = nb - 1; b >= 0; --b) {
@@ -2603,7 +2783,7 @@ int gbtn_su_tape_vjp(gbtn_su* S, const gbtn_su_tape* T, const double* cot_out, d
         GBTN_CUDA(cudaMemcpyAsync(S->d_edim, T->d_edim_snap[b], sizeof(int) * S->ne, cudaMemcpyDeviceToDevice, s));
       su_vjp_batch(S, T->d_jobs + bt.first, bt.second - bt.first, T->d_gates + (T->per_gate ? T->gsz * bt.first : 0),
                    T->per_gate, T->gsz, T->d_envs, T->md, T->cutoff, T->normalize, T->bmax, T->d_edim_snap[b + 1],
-                   d_cot, d_cot, d_gc + T->gsz * bt.first, w);
+                   d_cot, d_cot, d_gc + T->gsz * bt.first, d_env, w);
     }
     // back to the state the taped apply left
     GBTN_CUDA(cudaMemcpyAsync(S->d_tens, T->d_tens_snap[nb], sizeof(double) * S->cap_total, cudaMemcpyDeviceToDevice, s));
@@ -2616,6 +2796,12 @@ int gbtn_su_tape_vjp(gbtn_su* S, const gbtn_su_tape* T, const double* cot_out, d
     su_scatter(S, T->dims_before, nullptr, cot_in, d_cot, w.stage);
     if (gate_cot)
       GBTN_CUDA(cudaMemcpyAsync(gate_cot, d_gc, sizeof(double) * T->gsz * T->n_gates, cudaMemcpyDeviceToHost, s));
+    if (env_cot) {
+      if (d_env)
+        GBTN_CUDA(cudaMemcpyAsync(env_cot, d_env, sizeof(double) * env_elems, cudaMemcpyDeviceToHost, s));
+      else
+        std::fill(env_cot, env_cot + env_elems, 0.0);
+    }
     GBTN_CUDA(cudaStreamSynchronize(s));
   } catch (const std::exception& e) {
     return su_fail(S, GBTN_ERR_CUDA, e.what());
@@ -2641,7 +2827,8 @@ int gbtn_su_set_edge_dims(gbtn_su* S, const int32_t* dims) {
 
 int gbtn_su_apply_vjp(gbtn_su* S, int32_t n_gates, const int32_t* edges, const double* gates, int32_t per_gate,
                       const double* envs, int32_t maxdim, double cutoff, int32_t normalize,
-                      const int32_t* post_edge_dims, const double* cot_out, double* cot_in, double* gate_cot) {
+                      const int32_t* post_edge_dims, const double* cot_out, double* cot_in, double* gate_cot,
+                      double* env_cot) {
   const gbtn::NvtxRange nvtx_range("gbtn_su_apply_vjp");
   if (!S || n_gates < 0 || (n_gates > 0 && (!edges || !gates)) || !post_edge_dims || !cot_out || !cot_in)
     return GBTN_ERR_INVALID;
@@ -2676,6 +2863,9 @@ int gbtn_su_apply_vjp(gbtn_su* S, int32_t n_gates, const int32_t* edges, const d
     const long long gsz = (long long)D * D;
     VjpScratch w(S, std::max<int>(n_gates, 1), gsz * n_gates);
     double* d_cot = w.cot;
+    const size_t env_elems = (size_t)2 * S->ne * S->chimax * S->chimax;
+    double* d_env = env_cot && envs ? w.env : nullptr;
+    if (d_env) GBTN_CUDA(cudaMemsetAsync(d_env, 0, sizeof(double) * env_elems, s));
     su_scatter(S, post, cot_out, nullptr, d_cot, w.stage);  // sites without a gate keep theirs (same shapes)
     if (n_gates > 0) {
       std::vector<void*> owned;
@@ -2708,7 +2898,7 @@ int gbtn_su_apply_vjp(gbtn_su* S, int32_t n_gates, const int32_t* edges, const d
       const int md = maxdim > 0 ? std::min(maxdim, S->chimax) : S->chimax;
       GBTN_CUDA(cudaMemsetAsync(S->d_status, 0, sizeof(int), s));
       su_vjp_batch(S, d_jobs, n_gates, d_gates, per_gate, gsz, d_envs, md, cutoff, normalize, su_bmax(S), d_post,
-                   d_cot, d_cot, d_gc, w);
+                   d_cot, d_cot, d_gc, d_env, w);
       int status = 0;
       GBTN_CUDA(cudaMemcpyAsync(&status, S->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
       GBTN_CUDA(cudaStreamSynchronize(s));
@@ -2722,6 +2912,12 @@ int gbtn_su_apply_vjp(gbtn_su* S, int32_t n_gates, const int32_t* edges, const d
                        "> 8192 elements, or theta > 64 x 64)");
       if (gate_cot)
         GBTN_CUDA(cudaMemcpyAsync(gate_cot, d_gc, sizeof(double) * gsz * n_gates, cudaMemcpyDeviceToHost, s));
+    }
+    if (env_cot) {
+      if (d_env && n_gates > 0)
+        GBTN_CUDA(cudaMemcpyAsync(env_cot, d_env, sizeof(double) * env_elems, cudaMemcpyDeviceToHost, s));
+      else
+        std::fill(env_cot, env_cot + env_elems, 0.0);
     }
     su_scatter(S, S->edim, nullptr, cot_in, d_cot, w.stage);
   } catch (const std::exception& e) {

@@ -160,10 +160,10 @@ SIGNATURES = {
     "gbtn_su_apply": (_I, [_P, C.c_int32, _I32, _D, C.c_int32, _D, C.c_int32, C.c_double, C.c_int32, _D, _D]),
     "gbtn_su_set_edge_dims": (_I, [_P, _I32]),
     "gbtn_su_apply_vjp": (_I, [_P, C.c_int32, _I32, _D, C.c_int32, _D, C.c_int32, C.c_double, C.c_int32, _I32, _D,
-                               _D, _D]),
+                               _D, _D, _D]),
     "gbtn_su_apply_taped": (_I, [_P, C.c_int32, _I32, _D, C.c_int32, _D, C.c_int32, C.c_double, C.c_int32, _D, _D,
                                  C.POINTER(_P)]),
-    "gbtn_su_tape_vjp": (_I, [_P, _P, _D, _D, _D]),
+    "gbtn_su_tape_vjp": (_I, [_P, _P, _D, _D, _D, _D]),
     "gbtn_su_tape_destroy": (_I, [_P]),
     "gbtn_energy2": (_I, [_P, C.c_int32, _D, _D, _D]),
     "gbtn_energy2_grad": (_I, [_P, C.c_int32, _D, _D, C.POINTER(GradOpts), _D, _D, _I32, _D]),

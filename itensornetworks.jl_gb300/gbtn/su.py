@@ -99,7 +99,8 @@ class SimpleUpdateState:
         """Adjoint of ``apply`` for gates on disjoint vertices, at the current
         tensors (the gates' inputs).  ``cot``: per vertex dL/d(tensor after the
         gates) with bond dimensions ``post_dims``.  Returns (dL/d(current
-        tensors) per vertex, dL/dG per gate as an (n, D, D) array)."""
+        tensors) per vertex, dL/dG per gate as an (n, D, D) array, dL/d(envs)
+        as a list of 2*ne matrices, or None without envs)."""
         if self.complex:
             raise _lib.Unsupported(2, "simple update adjoint: real tensors only")
         edges = np.ascontiguousarray(edges, dtype=np.int32)
@@ -114,18 +115,30 @@ class SimpleUpdateState:
         D = self.tn.site_dims[self.tn.edges[int(edges[0])][0]] * self.tn.site_dims[self.tn.edges[int(edges[0])][1]] \
             if n else 1
         gc = np.zeros(max(n * D * D, 1))
+        ec = None if env_arr is None else np.zeros_like(env_arr)
         md = int(maxdim) if maxdim else self.chi_max
         check(self.ctx.handle, self.lib.gbtn_su_apply_vjp(
             self.handle, n, iptr(edges), dptr(g), 0 if shared else 1,
             None if env_arr is None else dptr(env_arr), md, -1.0 if cutoff is None else float(cutoff),
-            1 if normalize else 0, iptr(post), dptr(flat), dptr(out), dptr(gc)))
+            1 if normalize else 0, iptr(post), dptr(flat), dptr(out), dptr(gc), None if ec is None else dptr(ec)))
         n_el = sum(pre.size(v) for v in range(pre.nv))
-        return pre.unflat(out[:n_el]), gc[:n * D * D].reshape(n, D, D).transpose(0, 2, 1)
+        return (pre.unflat(out[:n_el]), gc[:n * D * D].reshape(n, D, D).transpose(0, 2, 1),
+                None if ec is None else self._unpack_envs(ec, envs))
+
+    def _unpack_envs(self, arr, envs):
+        """The 2*ne environment matrices (their shapes) out of the chi_max^2 slots."""
+        cm = self.chi_max
+        out = []
+        for de, m in enumerate(envs):
+            c = np.asarray(m).shape[0]
+            out.append(arr[de * cm * cm:de * cm * cm + c * c].reshape(c, c, order="F").copy())
+        return out
 
     def apply_with_pullback(self, gates, edges, envs=None, maxdim=None, cutoff=None, normalize=False):
         """``apply`` that also returns its pullback: (truncation errors, kept
         singular values, pullback), pullback(cot) -> (dL/d(tensors before the
-        gates) per vertex, dL/dG per gate (n, D, D)).  The library keeps a tape
+        gates) per vertex, dL/dG per gate (n, D, D), dL/d(envs) as 2*ne
+        matrices or None without envs).  The library keeps a tape
         of the state before every batch of consecutive vertex-disjoint gates
         in device memory (gbtn_su_apply_taped); the pullback runs the batches'
         adjoints backwards on the device and leaves the state where ``apply``
@@ -157,9 +170,12 @@ class SimpleUpdateState:
                 raise _lib.InvalidArgument(1, "cotangents do not have the shapes the gates left")
             out = np.zeros(max(sum(before.size(v) for v in range(before.nv)), 1))
             gc = np.zeros(max(n * D * D, 1))
-            check(self.ctx.handle, self.lib.gbtn_su_tape_vjp(self.handle, tape.handle, dptr(flat), dptr(out), dptr(gc)))
+            ec = None if env_arr is None else np.zeros_like(env_arr)
+            check(self.ctx.handle, self.lib.gbtn_su_tape_vjp(self.handle, tape.handle, dptr(flat), dptr(out), dptr(gc),
+                                                             None if ec is None else dptr(ec)))
             n_el = sum(before.size(v) for v in range(before.nv))
-            return before.unflat(out[:n_el]), gc[:n * D * D].reshape(n, D, D).transpose(0, 2, 1)
+            return (before.unflat(out[:n_el]), gc[:n * D * D].reshape(n, D, D).transpose(0, 2, 1),
+                    None if ec is None else self._unpack_envs(ec, envs))
 
         pullback.tape = tape  # freed with the pullback
         return te[:n], sv[:n * md].reshape(n, md), pullback

@@ -782,8 +782,8 @@ function gb300_apply_with_pullback(gates::Vector{ITensor}, psi; maxdim, cutoff=n
         din = zeros(length(p.data))
         gc = zeros(length(gdata))
         check(ctx, ccall((:gbtn_su_tape_vjp, libgbtn), Cint,
-            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
-            holder.state, holder.tape, cot, din, gc))
+            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+            holder.state, holder.tape, cot, din, gc, C_NULL))
         dpsi = Dict{Any, ITensor}()
         o = 0
         for (i, v) in enumerate(p.vs)

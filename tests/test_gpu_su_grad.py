@@ -76,7 +76,7 @@ def check_case(g, A, layers, envs=None, maxdim=3, cutoff=None, normalize=False, 
     out = st.network()
     assert list(out.edge_dims) == list(g_out.edge_dims)
     cot = psi_cotangents(g_out, out.tensors, W)
-    G, Gg = pull(cot)
+    G, Gg, _ = pull(cot)
     assert [x.shape for x in G] == [a.shape for a in A]
     # the state is where apply left it
     np.testing.assert_array_equal(np.concatenate([t.ravel() for t in st.network().tensors]),
@@ -172,7 +172,7 @@ def test_bp_energy_gradient_through_a_tebd_step():
     net1 = st.network()
     bpc = gbtn.BeliefPropagationCache(net1).update(maxiter=500, schedule="parallel")
     E, G1 = bpc.energy2_grad(HEISENBERG, mode="implicit", tol=1e-13)
-    G0, Gg = pull(G1)
+    G0, Gg, _ = pull(G1)
 
     def energy(AA, gt=gate):
         lay = [[(e, gt) for e in c] for c in colours]
@@ -209,14 +209,86 @@ def test_batch_vjp_equals_the_taped_pullback():
     out = st.network()
     rng = np.random.default_rng(2)
     cot = [rng.standard_normal(t.shape) for t in out.tensors]
-    G1, Gg1 = pull(cot)
+    G1, Gg1, E1 = pull(cot)
     st.set_state(gpu_net(g, A))
-    G2, Gg2 = st.apply_vjp(gates, edges, out.edge_dims, cot, envs=envs, maxdim=3, cutoff=1e-12, normalize=True)
+    G2, Gg2, E2 = st.apply_vjp(gates, edges, out.edge_dims, cot, envs=envs, maxdim=3, cutoff=1e-12, normalize=True)
     for a, b in zip(G1, G2):
         np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-14)
     np.testing.assert_allclose(Gg1, Gg2, rtol=1e-12, atol=1e-14)
-    G3, _ = pull(cot)  # a tape can be pulled back again
+    for a, b in zip(E1, E2):
+        np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-14)
+    G3, _, _ = pull(cot)  # a tape can be pulled back again
     for a, b in zip(G1, G3):
         np.testing.assert_array_equal(a, b)
     st.close()
     del pull  # the tape outlives nothing it needs
+
+
+def test_environment_cotangents():
+    """dL/d(envs) through the square-root and inverse-square-root environments
+    (the eigen-decomposition's divided differences): against central
+    differences of the oracle along symmetric directions of every message."""
+    g = O.square_lattice(3, 3, chi=2)
+    A = O.random_network(g, 9, unit_norm=True)
+    envs, _, _ = O.bp_update(g, A, O.identity_messages(g), maxiter=300, schedule="parallel")
+    layer = [(e, random_gate(20 + e)) for e in (0, 5, 10, 4)]
+    rng = np.random.default_rng(6)
+    g_out, A_out = oracle_layers(g, A, [layer], envs, 3, 1e-12, True)
+    W = rng.standard_normal(psi(g_out, A_out).shape)
+    st = gbtn.SimpleUpdateState(gpu_net(g, A), chi_max=4)
+    _, _, pull = st.apply_with_pullback([gt for _, gt in layer], [e for e, _ in layer], envs=envs, maxdim=3,
+                                        cutoff=1e-12, normalize=True)
+    out = st.network()
+    _, _, Eb = pull(psi_cotangents(g_out, out.tensors, W))
+    assert len(Eb) == 2 * g.ne
+    D = [rng.standard_normal(m.shape) for m in envs]
+    D = [(d + d.T) / 2 for d in D]
+    nrm = np.sqrt(sum(np.sum(d * d) for d in D))
+    D = [d / nrm for d in D]
+
+    def loss(ev):
+        return float(np.sum(W * psi(*oracle_layers(g, A, [layer], ev, 3, 1e-12, True))))
+
+    h = 1e-5
+    fd = (loss([m + h * d for m, d in zip(envs, D)]) - loss([m - h * d for m, d in zip(envs, D)])) / (2 * h)
+    an = sum(float(np.sum(x * d)) for x, d in zip(Eb, D))
+    assert an == pytest.approx(fd, rel=RTOL, abs=1e-9)
+    st.close()
+
+
+def test_gradient_through_bp_gauged_gates():
+    """BP-gauged simple update (tebd.jl with envs = the BP messages of the
+    state): L(A) = <W, psi(apply(gates, A; envs = BP(A)))>.  dL/dA = the
+    pullback's tensor cotangent plus the BP fixed point's VJP of its
+    environment cotangent (gbtn_bp_vjp); against central differences of the
+    oracle's BP and simple update."""
+    g = O.square_lattice(3, 3, chi=2)
+    A = O.random_network(g, 19, unit_norm=True)
+    layer = [(e, random_gate(40 + e)) for e in (1, 3, 4, 10)]
+    assert len({v for e, _ in layer for v in g.edges[e]}) == 8
+    rng = np.random.default_rng(7)
+
+    def fwd_oracle(AA):
+        m, _, _ = O.bp_update(g, AA, O.identity_messages(g), maxiter=400, schedule="parallel")
+        return oracle_layers(g, AA, [layer], m, 3, 1e-12, True)
+
+    g_out, A_out = fwd_oracle(A)
+    W = rng.standard_normal(psi(g_out, A_out).shape)
+    tn = gpu_net(g, A)
+    bpc = gbtn.BeliefPropagationCache(tn).update(maxiter=400, schedule="parallel")
+    envs = bpc.messages()
+    st = gbtn.SimpleUpdateState(tn, chi_max=4)
+    _, _, pull = st.apply_with_pullback([gt for _, gt in layer], [e for e, _ in layer], envs=envs, maxdim=3,
+                                        cutoff=1e-12, normalize=True)
+    out = st.network()
+    G, _, Eb = pull(psi_cotangents(g_out, out.tensors, W))
+    Gbp = bpc.vjp(Eb, tol=1e-14)
+    total = [a + b for a, b in zip(G, Gbp)]
+    D = unit(rng, [a.shape for a in A])
+    h = 1e-5
+    loss = lambda AA: float(np.sum(W * psi(*fwd_oracle(AA))))
+    fd = (loss([a + h * d for a, d in zip(A, D)]) - loss([a - h * d for a, d in zip(A, D)])) / (2 * h)
+    an = sum(float(np.sum(x * d)) for x, d in zip(total, D))
+    assert an == pytest.approx(fd, rel=RTOL, abs=1e-9)
+    st.close()
+    bpc.close()
