@@ -11,7 +11,8 @@ from .cache import (BeliefPropagationCache, default_bp_maxiter, edge_scalars, en
                     updated_message, vertex_scalars)
 from .partition import CoarseGraining, PartitionedBPCache, partitioned_cache
 from .sharded import GpuShard, ShardPlan, block_owner, run_distributed, run_local
-from .su import SimpleUpdateState, apply, bp_environments, checkerboard_edges, tebd, tebd_gates, tfim_gate
+from .su import (SimpleUpdateState, apply, bp_environments, checkerboard_edges, tebd, tebd_gates, tebd_with_pullback,
+                 tfim_gate)
 from .opsum import OpSum, group_terms, trotter2_gates
 from .qn import QNBeliefPropagationCache, QNNetwork, random_qn_network
 from .network import (TensorNetwork, default_edge_sequence, disjoint_union, parallel_edge_sequence,
@@ -24,7 +25,8 @@ __all__ = [
     "parallel_edge_sequence", "random_network", "random_tensors", "rescale", "scalar", "square_lattice", "update",
     "updated_message", "SimpleUpdateState", "apply", "checkerboard_edges", "tebd", "tfim_gate", "bp_environments",
     "CoarseGraining", "PartitionedBPCache", "partitioned_cache", "GpuShard", "ShardPlan", "block_owner",
-    "run_distributed", "run_local", "tebd_gates", "OpSum", "group_terms", "trotter2_gates", "edge_scalars",
+    "run_distributed", "run_local", "tebd_gates", "tebd_with_pullback", "OpSum", "group_terms", "trotter2_gates",
+    "edge_scalars",
     "identity_messages", "message", "messages", "update_factor", "update_factors", "vertex_scalars",
     "region_scalar", "scalar_factors_quotient", "incoming_messages", "factors", "default_bp_maxiter",
     "QNBeliefPropagationCache", "QNNetwork", "random_qn_network",

@@ -320,3 +320,52 @@ def bp_environments(st: SimpleUpdateState, maxiter=30, tol=1e-12, precision="f64
     msgs = bpc.messages()
     bpc.close()
     return msgs
+
+
+def tebd_with_pullback(psi: TensorNetwork, gate_of_edge, edge_classes, nsteps, maxdim, cutoff, normalize=True,
+                       chi_max=None, bp_envs=False, bp_maxiter=300, bp_tol=1e-13):
+    """``tebd_gates`` (real tensors) that also returns its pullback:
+    (state, pullback), pullback(cot) -> (dL/d(psi's tensors), {edge: dL/dG}),
+    cot = dL/d(the final tensors).  Without bp_envs the whole gate sequence is
+    one taped apply.  With bp_envs the environments of every colour class are
+    the converged BP messages of the state before it, and the pullback adds
+    their path: each class's environment cotangent goes through that state's
+    BP fixed point (implicit adjoint, gbtn_bp_vjp) to its tensors.  Memory: one
+    device copy of the state per batch of vertex-disjoint gates, and with
+    bp_envs one BP plan per class, kept until the pullback is dropped."""
+    from .cache import BeliefPropagationCache
+    st = SimpleUpdateState(psi, chi_max or maxdim)
+    gates = {e: np.asarray(gate_of_edge(e), dtype=float) for cls in edge_classes for e in cls}
+    if not bp_envs:
+        order = [e for _ in range(nsteps) for cls in edge_classes for e in cls]
+        _, _, pull = st.apply_with_pullback([gates[e] for e in order], order, maxdim=maxdim, cutoff=cutoff,
+                                            normalize=normalize)
+
+        def pullback(cot):
+            g0, gc, _ = pull(cot)
+            dg = {e: np.zeros_like(gates[e]) for e in gates}
+            for e, m in zip(order, gc):
+                dg[e] += m
+            return g0, dg
+        return st, pullback
+    records = []
+    for _ in range(nsteps):
+        for cls in edge_classes:
+            bpc = BeliefPropagationCache(st.network(), ctx=st.ctx)
+            bpc.update(maxiter=bp_maxiter, tol=bp_tol, schedule="parallel", precision="f64")
+            envs = bpc.messages()
+            _, _, pull = st.apply_with_pullback([gates[e] for e in cls], list(cls), envs=envs, maxdim=maxdim,
+                                                cutoff=cutoff, normalize=normalize)
+            records.append((list(cls), bpc, pull))
+    final = st.network()
+
+    def pullback(cot):
+        dg = {e: np.zeros_like(gates[e]) for e in gates}
+        for cls, bpc, pull in reversed(records):
+            cot, gc, denv = pull(cot)
+            cot = [a + b for a, b in zip(cot, bpc.vjp(denv, tol=1e-14))]
+            for e, m in zip(cls, gc):
+                dg[e] += m
+        st.set_state(final)
+        return cot, dg
+    return st, pullback

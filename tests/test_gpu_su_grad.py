@@ -292,3 +292,49 @@ def test_gradient_through_bp_gauged_gates():
     assert an == pytest.approx(fd, rel=RTOL, abs=1e-9)
     st.close()
     bpc.close()
+
+
+@pytest.mark.parametrize("bp_envs,nsteps", [(False, 2), (True, 1)])
+def test_tebd_pullback(bp_envs, nsteps):
+    """tebd_with_pullback: a checkerboard Trotter evolution (Heisenberg gates
+    exp(-0.1 h), maxdim 3, normalised), with BP-gauged environments or
+    without, against central differences of the oracle doing the same steps
+    (its BP before every class when gauged); the shared per-edge gates'
+    cotangents too."""
+    torch = pytest.importorskip("torch")  # noqa: F841 (bp_autograd needs it)
+    import bp_autograd as AG
+    g = O.square_lattice(3, 3, chi=2)
+    A = O.random_network(g, 29, unit_norm=True)
+    hm = AG.heisenberg_matrix()
+    w, U = np.linalg.eigh(hm)
+    gate = (U * np.exp(-0.1 * w)) @ U.T
+    classes = [[0, 5, 10], [2, 7, 11], [1, 3, 4], [6, 8, 9]]
+
+    def fwd_oracle(AA, gt=gate):
+        gg = g
+        for _ in range(nsteps):
+            for cls in classes:
+                envs = None
+                if bp_envs:
+                    envs, _, _ = O.bp_update(gg, AA, O.identity_messages(gg), maxiter=400, schedule="parallel")
+                gg, AA = oracle_layers(gg, AA, [[(e, gt) for e in cls]], envs, 3, None, True)
+        return gg, AA
+
+    g_out, A_out = fwd_oracle(A)
+    rng = np.random.default_rng(12)
+    W = rng.standard_normal(psi(g_out, A_out).shape)
+    st, pull = gbtn.tebd_with_pullback(gpu_net(g, A), lambda e: gate, classes, nsteps, maxdim=3, cutoff=None,
+                                       chi_max=4, bp_envs=bp_envs, bp_maxiter=400, bp_tol=None)
+    out = st.network()
+    assert list(out.edge_dims) == list(g_out.edge_dims)
+    G, dG = pull(psi_cotangents(g_out, out.tensors, W))
+    D = unit(rng, [a.shape for a in A])
+    h = 1e-5
+    loss = lambda AA, gt=gate: float(np.sum(W * psi(*fwd_oracle(AA, gt))))
+    fd = (loss([a + h * d for a, d in zip(A, D)]) - loss([a - h * d for a, d in zip(A, D)])) / (2 * h)
+    assert sum(float(np.sum(x * d)) for x, d in zip(G, D)) == pytest.approx(fd, rel=RTOL, abs=1e-9)
+    Dg = rng.standard_normal(gate.shape)
+    Dg /= np.linalg.norm(Dg)
+    fdg = (loss(A, gate + h * Dg) - loss(A, gate - h * Dg)) / (2 * h)
+    assert float(np.sum(sum(dG.values()) * Dg)) == pytest.approx(fdg, rel=RTOL, abs=1e-9)
+    st.close()
