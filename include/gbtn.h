@@ -396,10 +396,14 @@ int gbtn_energy2(gbtn_plan* plan, int32_t n_terms, const double* coef, const dou
  * dE/dRe + i dE/dIm (interleaved). */
 int gbtn_energy2_grad(gbtn_plan* plan, int32_t n_terms, const double* coef, const double* ops,
                       const gbtn_grad_opts* opts, double* energy, double* grad, int32_t* iters, double* resid);
-/* Vector-Jacobian product through the BP fixed point: given dL/dm for the
- * converged messages (n_message values), the gradient dL/dA (n_factor values)
- * by implicit differentiation (opts->mode must be IMPLICIT).  Complex plans:
- * both are dL/dRe + i dL/dIm of a real loss L, interleaved (re, im). */
+/* Vector-Jacobian product of the BP messages: given dL/dm (n_message
+ * values), the gradient dL/dA (n_factor values).  IMPLICIT: through the fixed
+ * point, the converged messages in the plan (implicit differentiation, the
+ * adjoint BP solve).  UNROLLED: through opts->unroll normalised Jacobi sweeps
+ * from identity messages (dL/dm of their final messages, checkpointed every
+ * opts->checkpoint sweeps, 0 = ceil(sqrt(unroll))); those final messages are
+ * left in the plan.  Complex plans: both are dL/dRe + i dL/dIm of a real loss
+ * L, interleaved (re, im). */
 int gbtn_bp_vjp(gbtn_plan* plan, const double* msg_cot, const gbtn_grad_opts* opts, double* grad, int32_t* iters,
                 double* resid);
 

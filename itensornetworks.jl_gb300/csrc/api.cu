@@ -2603,7 +2603,7 @@ void energy_direct_vjp(Energy2& E, const double* msgs, double* cot, double* g, d
 // checkpointed every c sweeps; complex cotangents lose their message-phase
 // components at every step (the energy is invariant under them).
 template <typename T>
-void unrolled_backward_t(gbtn_plan* P, Energy2& E, int Tn, int c, std::vector<std::unique_ptr<DevBuf<double>>>& ck,
+void unrolled_backward_t(gbtn_plan* P, const int* allv, int Tn, int c, std::vector<std::unique_ptr<DevBuf<double>>>& ck,
                          std::vector<std::unique_ptr<DevBuf<double>>>& seg, double* lam_p, double* dgrad, long long nm) {
   cudaStream_t s = P->ctx->stream;
   const int ndir = 2 * P->ne;
@@ -2622,12 +2622,60 @@ void unrolled_backward_t(gbtn_plan* P, Energy2& E, int Tn, int c, std::vector<st
       raw_forward(P, P->d_fac.p, nullptr, mprev, fraw.p, 0);
       launch_norm_vjp<T>(ndir, P->d_dchi.p, P->d_msg_off.p, as<T>(fraw.p), as<T>(lam), as<T>(fbar.p), s);
       GBTN_CUDA(cudaMemsetAsync(mb, 0, sizeof(double) * nm, s));
-      launch_vertex_vjp<T>(E.allv.p, P->nv, P->d_vd.p, as<T>(P->d_fac.p), as<T>(P->d_fac.p), as<T>(mprev),
+      launch_vertex_vjp<T>(allv, P->nv, P->d_vd.p, as<T>(P->d_fac.p), as<T>(P->d_fac.p), as<T>(mprev),
                            as<T>(fbar.p), P->d_msg_off.p, nullptr, as<T>(mb), as<T>(dgrad), P->ncap, s);
       if constexpr (std::is_same<T, zdouble>::value)
         launch_phase_project(ndir, P->d_dchi.p, P->d_msg_off.p, as<zdouble>(mprev), as<zdouble>(mb), s);
       std::swap(lam, mb);
     }
+  }
+}
+
+// The unrolled computation: identity messages, T normalised Jacobi sweeps,
+// every c-th kept in ck (ck[0] = identity, T/c + 1 of them), c segment
+// buffers for the backward's recomputation; the final messages end in cur
+// and in the plan.
+struct Unrolled {
+  std::vector<std::unique_ptr<DevBuf<double>>> ck, seg;
+  DevBuf<double> cur, nxt;
+  int T = 0, c = 1;
+};
+
+void unrolled_forward(gbtn_plan* P, int T, int checkpoint, long long nm, Unrolled& U) {
+  cudaStream_t s = P->ctx->stream;
+  U.T = T;
+  U.c = checkpoint > 0 ? checkpoint : (int)std::ceil(std::sqrt((double)T));
+  const int nck = T / U.c + 1;
+  for (int j = 0; j < nck; ++j) {
+    U.ck.push_back(std::make_unique<DevBuf<double>>());
+    U.ck.back()->alloc(nm);
+  }
+  for (int j = 0; j < U.c; ++j) {
+    U.seg.push_back(std::make_unique<DevBuf<double>>());
+    U.seg.back()->alloc(nm);
+  }
+  U.cur.alloc(nm);
+  U.nxt.alloc(nm);
+  launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, U.cur.p, GBTN_INIT_IDENTITY, s, P->cplx);
+  GBTN_CUDA(cudaMemcpyAsync(U.ck[0]->p, U.cur.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
+  for (int t = 1; t <= T; ++t) {
+    raw_forward(P, P->d_fac.p, nullptr, U.cur.p, U.nxt.p, 1);
+    std::swap(U.cur.p, U.nxt.p);
+    if (t % U.c == 0 && t / U.c < nck)
+      GBTN_CUDA(cudaMemcpyAsync(U.ck[t / U.c]->p, U.cur.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
+  }
+  GBTN_CUDA(cudaMemcpyAsync(P->d_msg[P->cur].p, U.cur.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
+}
+
+// lam = dL/d(final messages) -> grad += dL/dA through the unrolled sweeps
+// (complex: lam's message-phase components dropped first, as at every step).
+void unrolled_backward(gbtn_plan* P, const int* allv, Unrolled& U, double* lam, double* dgrad, long long nm) {
+  if (P->cplx) {
+    launch_phase_project(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, as<zdouble>(U.cur.p), as<zdouble>(lam),
+                         P->ctx->stream);
+    unrolled_backward_t<zdouble>(P, allv, U.T, U.c, U.ck, U.seg, lam, dgrad, nm);
+  } else {
+    unrolled_backward_t<double>(P, allv, U.T, U.c, U.ck, U.seg, lam, dgrad, nm);
   }
 }
 
@@ -2758,42 +2806,11 @@ int gbtn_energy2_grad(gbtn_plan* P, int32_t nterms, const double* coef, const do
   } else {
     const int T = o->unroll;
     require(T >= 1, "UNROLLED needs unroll >= 1");
-    const int c = o->checkpoint > 0 ? o->checkpoint : (int)std::ceil(std::sqrt((double)T));
-    const int nck = T / c + 1;
-    std::vector<std::unique_ptr<DevBuf<double>>> ck, seg;
-    for (int j = 0; j < nck; ++j) {
-      ck.push_back(std::make_unique<DevBuf<double>>());
-      ck.back()->alloc(nm);
-    }
-    for (int j = 0; j < c; ++j) {
-      seg.push_back(std::make_unique<DevBuf<double>>());
-      seg.back()->alloc(nm);
-    }
-    DevBuf<double> cur, nxt, lam;
-    cur.alloc(nm);
-    nxt.alloc(nm);
-    lam.alloc(nm);
-    // forward: identity messages, T normalised Jacobi sweeps, every c-th kept
-    launch_fill_messages(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, cur.p, GBTN_INIT_IDENTITY, s, P->cplx);
-    GBTN_CUDA(cudaMemcpyAsync(ck[0]->p, cur.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
-    for (int t = 1; t <= T; ++t) {
-      raw_forward(P, P->d_fac.p, nullptr, cur.p, nxt.p, 1);
-      std::swap(cur.p, nxt.p);
-      if (t % c == 0 && t / c < nck)
-        GBTN_CUDA(cudaMemcpyAsync(ck[t / c]->p, cur.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
-    }
-    // the final messages stay in the plan
-    GBTN_CUDA(cudaMemcpyAsync(P->d_msg[P->cur].p, cur.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
-    energy_forward(E, cur.p);
-    energy_direct_vjp(E, cur.p, cot.p, g.p, dgrad.p);
-    GBTN_CUDA(cudaMemcpyAsync(lam.p, g.p, sizeof(double) * nm, cudaMemcpyDeviceToDevice, s));
-    // backward, one checkpoint segment at a time
-    if (P->cplx) {
-      launch_phase_project(2 * P->ne, P->d_dchi.p, P->d_msg_off.p, as<zdouble>(cur.p), as<zdouble>(lam.p), s);
-      unrolled_backward_t<zdouble>(P, E, T, c, ck, seg, lam.p, dgrad.p, nm);
-    } else {
-      unrolled_backward_t<double>(P, E, T, c, ck, seg, lam.p, dgrad.p, nm);
-    }
+    Unrolled U;
+    unrolled_forward(P, T, o->checkpoint, nm, U);  // the final messages stay in the plan
+    energy_forward(E, U.cur.p);
+    energy_direct_vjp(E, U.cur.p, cot.p, g.p, dgrad.p);
+    unrolled_backward(P, E.allv.p, U, g.p, dgrad.p, nm);
     if (iters) *iters = T;
     if (resid) *resid = 0.0;
   }
@@ -2927,7 +2944,8 @@ int gbtn_bp_vjp(gbtn_plan* P, const double* msg_cot, const gbtn_grad_opts* o, do
     throw Unsupported("energies and gradients take vertices of the shared-memory kernels only (bond and site "
                       "dimensions <= 8)");
   require(P && msg_cot && o && grad, "NULL argument");
-  require(o->mode == GBTN_GRAD_IMPLICIT, "gbtn_bp_vjp differentiates through the fixed point (IMPLICIT)");
+  require(o->mode == GBTN_GRAD_IMPLICIT || o->mode == GBTN_GRAD_UNROLLED, "unknown gradient mode");
+  require(o->mode == GBTN_GRAD_IMPLICIT || o->unroll >= 1, "UNROLLED needs unroll >= 1");
   require(!P->sep_bra, "gradients need bra = conj(ket) (a quadratic-form network)");
   if (vertex_vjp_smem(P->ncap, P->cplx ? sizeof(zdouble) : sizeof(double)) > 227 * 1024)
     throw Unsupported("vertex tensor too large for the adjoint kernels");
@@ -2944,8 +2962,16 @@ int gbtn_bp_vjp(gbtn_plan* P, const double* msg_cot, const gbtn_grad_opts* o, do
   std::vector<int> all(P->nv);
   std::iota(all.begin(), all.end(), 0);
   allv.upload(all, s);
-  implicit_adjoint(P, allv.p, P->d_msg[P->cur].p, g.p, dgrad.p, o->maxiter > 0 ? o->maxiter : 500,
-                   o->tol > 0 ? o->tol : 1e-12, iters, resid);
+  if (o->mode == GBTN_GRAD_IMPLICIT) {
+    implicit_adjoint(P, allv.p, P->d_msg[P->cur].p, g.p, dgrad.p, o->maxiter > 0 ? o->maxiter : 500,
+                     o->tol > 0 ? o->tol : 1e-12, iters, resid);
+  } else {  // through `unroll` sweeps from identity messages, which stay in the plan
+    Unrolled U;
+    unrolled_forward(P, o->unroll, o->checkpoint, nm, U);
+    unrolled_backward(P, allv.p, U, g.p, dgrad.p, nm);
+    if (iters) *iters = o->unroll;
+    if (resid) *resid = 0.0;
+  }
   copy_out(P, grad, dgrad.p, sizeof(double) * P->n_fac * es, GBTN_HOST);
   API_CATCH(C)
 }

@@ -364,14 +364,18 @@ class BeliefPropagationCache:
         self.adjoint_iterations, self.adjoint_residual = int(it[0]), float(res[0])
         return (e[0] if self.tn.n_networks == 1 else e), self.tn.unflat(g)
 
-    def vjp(self, msg_cot, maxiter=500, tol=1e-12):
-        """dL/dA from dL/dm at the fixed point (implicit differentiation).
-        Complex networks: cotangents and gradients are dL/dRe + i dL/dIm of a
-        real loss L."""
+    def vjp(self, msg_cot, maxiter=500, tol=1e-12, mode="implicit", unroll=30, checkpoint=0):
+        """dL/dA from dL/dm: at the fixed point (mode "implicit", implicit
+        differentiation at the messages in the cache) or through `unroll`
+        Jacobi sweeps from identity messages (mode "unrolled", checkpointed
+        every `checkpoint` sweeps, default sqrt(unroll); those sweeps' final
+        messages stay in the cache).  Complex networks: cotangents and
+        gradients are dL/dRe + i dL/dIm of a real loss L."""
         mc = (self.tn.flat_messages(msg_cot, self.complex) if isinstance(msg_cot, (list, tuple))
               else np.ascontiguousarray(msg_cot, self.dtype))
         o = _lib.GradOpts()
-        o.mode, o.maxiter, o.tol = 0, int(maxiter), float(tol)
+        o.mode, o.maxiter, o.tol = (0 if mode == "implicit" else 1), int(maxiter), float(tol)
+        o.unroll, o.checkpoint = int(unroll), int(checkpoint)
         g = np.empty(self.n_factor, dtype=self.dtype)
         it = np.zeros(1, dtype=np.int32)
         res = np.zeros(1)
