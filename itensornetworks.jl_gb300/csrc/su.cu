@@ -2647,6 +2647,25 @@ static int su_apply_impl(gbtn_su* S, int32_t n_gates, const int32_t* edges, cons
     int dmax = 1;
     for (int dd : S->dsite) dmax = std::max(dmax, dd);
     const int bmax = std::min(64, dmax * dmax * S->chimax);
+    if (!S->cplx) {
+      // the kernels' limits on every gate's two sites, checked here before any
+      // launch so that no batch is refused half-way: each bond a gate of this
+      // call may grow is taken at maxdim (the device checks the same limits)
+      std::vector<int> eb(S->edim);
+      for (const SuJob& jb : jobs) eb[jb.e] = std::max(eb[jb.e], md);
+      for (const SuJob& jb : jobs)
+        for (int side = 0; side < 2; ++side) {
+          const int x = side ? jb.v : jb.u, p = side ? jb.pv : jb.pu, d = S->dsite[x], ce = eb[jb.e];
+          long long m = 1;
+          for (int q = S->leg_ptr[x]; q < S->leg_ptr[x + 1]; ++q)
+            if (q - S->leg_ptr[x] != p) m *= eb[S->leg_edge[q]];
+          const long long other = m * d, r = std::min<long long>(m, (long long)d * ce);
+          if (other * std::max(md, ce) > gbtn::kSuMaxN || d * ce > 32 || r * d > bmax)
+            return su_fail(S, GBTN_ERR_UNSUPPORTED,
+                           "simple update: a gate exceeds the kernel limits (site tensor, also with the bond at "
+                           "maxdim, > 8192 elements, or theta > 64 x 64)");
+        }
+    }
     GBTN_CUDA(cudaMemsetAsync(S->d_status, 0, sizeof(int), s));
     if (tape) tape->dims_before = S->edim;
     for (auto& b : batches) {

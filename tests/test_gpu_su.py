@@ -186,3 +186,43 @@ def test_bp_gauged_tebd_matches_oracle():
     np.testing.assert_allclose(te_g, tes, rtol=1e-6, atol=1e-12)
     assert st.edge_dims() == gg.edge_dims
     assert same_up_to_sign(state(gg, st.network().tensors), state(gg, B), 1e-8)
+
+
+def test_spin_one_sites_and_the_size_limit():
+    """d = 3 sites (spin 1): a gate on the centre bond against the oracle, and
+    a gate whose rebuilt site would exceed the kernels' 8192 elements
+    (3 x 8^3 x 8 at maxdim 8) refused before any launch, the state untouched."""
+    base = O.square_lattice(3, 3, chi=8, d=3)
+    dims = list(base.edge_dims)
+    dims[3] = 4  # edge (1, 4): the centre site holds 3 x 8^3 x 4 = 6144 elements
+    g = O.square_lattice(3, 3, chi=8, d=3, edge_dims=dims)
+    A = O.random_network(g, 31, unit_norm=True)
+    rng = np.random.default_rng(8)
+    H = rng.standard_normal((9, 9))
+    H = H + H.T
+    w, U = np.linalg.eigh(H)
+    gate = (U * np.exp(-0.2 * w)) @ U.T
+    st = gbtn.SimpleUpdateState(gpu_net(g, A), chi_max=8)
+    before = st.network()
+    with pytest.raises(gbtn.Unsupported, match="limits"):
+        st.apply(gate, [3], maxdim=8, cutoff=1e-12, normalize=True)
+    after = st.network()
+    assert list(after.edge_dims) == list(before.edge_dims)
+    for a, b in zip(after.tensors, before.tensors):
+        np.testing.assert_array_equal(a, b)
+    g2, B, S, te = oracle_gate(g, A, gate, 3, maxdim=4, cutoff=1e-12)
+    te_g, sv = st.apply(gate, [3], maxdim=4, cutoff=1e-12, normalize=True)
+    assert st.edge_dims()[3] == g2.edge_dims[3]
+    np.testing.assert_allclose(sv[0][:len(S)], S, rtol=1e-10)
+    assert te_g[0] == pytest.approx(te, rel=1e-9, abs=1e-14)
+    # the two updated sites contracted over their bond (gauge invariant; the
+    # whole state of nine spin-1 sites at bond 8 is too large to contract here)
+    out = st.network()
+    u, v = g.edges[3]
+    pu, pv = g.legs[u].index(3), g.legs[v].index(3)
+    two = lambda T: np.tensordot(T[u], T[v], axes=([1 + pu], [1 + pv]))
+    np.testing.assert_allclose(two(out.tensors), two(B), rtol=0, atol=1e-10 * np.max(np.abs(two(B))))
+    for w in range(g.nv):
+        if w not in (u, v):
+            np.testing.assert_array_equal(out.tensors[w], A[w])
+    st.close()
