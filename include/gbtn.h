@@ -306,7 +306,10 @@ int gbtn_rescale_partitions(gbtn_plan* plan);
  * are interleaved (re, im) doubles (ComplexF64; e.g. the RandomUnitary gates
  * of test/test_apply.jl), run by a one-kernel complex path limited to site
  * tensors of <= 4096 elements (also with the bond at chi_max) and theta
- * <= 32 x 32; larger gates report GBTN_ERR_UNSUPPORTED. */
+ * <= 32 x 32; larger gates report GBTN_ERR_UNSUPPORTED.  Real tensors: a site
+ * tensor, also rebuilt with the gate's bond at maxdim, holds <= 8192 elements
+ * and theta <= 64 x 64; a call with a gate beyond that returns
+ * GBTN_ERR_UNSUPPORTED before any of its gates runs. */
 typedef struct gbtn_su gbtn_su;
 int gbtn_su_create(gbtn_ctx* ctx, const gbtn_graph_desc* desc, int32_t chi_max, gbtn_su** out);
 int gbtn_su_destroy(gbtn_su* su);
