@@ -81,6 +81,59 @@ class CoarseGraining:
         t = np.einsum(*ops, out, optimize=True)
         return np.ascontiguousarray(t.reshape(shape, order="F"))
 
+    def _contract_vjp(self, i, cot):
+        """The adjoint of _contract: dL/d(each site tensor of partition i) from
+        dL/d(its coarse tensor), the cotangent contracted with the partition's
+        other tensors."""
+        tn, p = self.tn, self.parts[i]
+        label = {}
+
+        def lab(key):
+            if key not in label:
+                label[key] = len(label)
+            return label[key]
+
+        labs = {v: [lab(("s", v))] + [lab(("e", e)) for e in tn.legs[v]] for v in p}
+        out = [lab(("s", v)) for v in p]
+        dims = [tn.site_dims[v] for v in p]
+        for ce in self.coarse.legs[i]:
+            out += [lab(("e", e)) for e in self.crossing[ce]]
+            dims += [tn.edge_dims[e] for e in self.crossing[ce]]
+        c = np.asarray(cot).reshape(dims, order="F")
+        res = {}
+        for v in p:
+            ops = [c, out]
+            for w in p:
+                if w != v:
+                    ops += [np.asarray(tn.tensors[w]), labs[w]]
+            res[v] = np.einsum(*ops, labs[v], optimize=True)
+        return res
+
+    def tensor_cotangents(self, coarse_cot):
+        """dL/d(original site tensors) from dL/d(coarse tensors)."""
+        out = [None] * self.tn.nv
+        for i in range(len(self.parts)):
+            for v, g in self._contract_vjp(i, coarse_cot[i]).items():
+                out[v] = g
+        return out
+
+    def fused_operator(self, op):
+        """sum_{v in p} 1 (x) .. op_v .. (x) 1 on a partition's fused site index
+        (first site fastest), the same for every partition; partitions must
+        share their sites' dimensions in order."""
+        shapes = {tuple(self.tn.site_dims[v] for v in p) for p in self.parts}
+        if len(shapes) != 1:
+            raise ValueError("partitions of different site dimensions have no common fused operator")
+        ds = next(iter(shapes))
+        op = np.asarray(op)
+        total = 0
+        for j in range(len(ds)):
+            m = np.ones((1, 1), dtype=op.dtype)
+            for q in reversed(range(len(ds))):
+                m = np.kron(m, op if q == j else np.eye(ds[q], dtype=op.dtype))
+            total = total + m
+        return total
+
     def site_rdms(self, coarse_rdms):
         """Single-site reduced density matrices of every original vertex from
         the coarse vertices' (fused-site) ones, by partial trace."""
@@ -137,6 +190,19 @@ class PartitionedBPCache:
 
     def logscalar(self):
         return self.cache.logscalar()
+
+    # -- gradients: the coarse plan's hand-written adjoints at its converged
+    #    messages, pulled back through the partition contraction
+    def logscalar_grad(self, **kw):
+        """(Re logscalar, dL/d(site tensors)) at the converged messages."""
+        val, G = self.cache.logscalar_grad(**kw)
+        return val, self.cg.tensor_cotangents(G)
+
+    def expect_sum_grad(self, op, **kw):
+        """(sum_v <op>_v over every original site, its gradient): the coarse
+        expectation of the fused operator (partitions of equal site dimensions)."""
+        val, G = self.cache.expect_sum_grad(self.cg.fused_operator(op), **kw)
+        return val, self.cg.tensor_cotangents(G)
 
     def scalar(self):
         return self.cache.scalar()

@@ -132,3 +132,61 @@ def test_square_block_partitions_on_a_loopy_grid_gpu(lib_built):
     assert pc.logscalar() == pytest.approx(float(np.real(O.logscalar(gc, cg.coarse.tensors, cg.coarse.tensors, m))),
                                            rel=1e-10)
     pc.close()
+
+
+def test_fused_operator_is_the_sum_over_sites():
+    """Tr(rho_fused O_fused) = sum_v tr(rho_v op) for the partial traces of the
+    fused RDM (CPU: the fusion order, first site fastest)."""
+    tn, g, A = grid(4, 2, 3)
+    cg = CoarseGraining(tn, [[0, 1, 4, 5], [2, 3, 6, 7], [8, 9, 12, 13], [10, 11, 14, 15]])
+    rng = np.random.default_rng(1)
+    X = rng.standard_normal((16, 16))
+    rho = X @ X.T
+    op = np.array([[0.3, 0.2], [0.2, -0.5]])
+    fused = cg.fused_operator(op)
+    parts_rho = cg.site_rdms([rho] * 4)
+    assert np.sum(rho * fused) == pytest.approx(sum(np.sum(parts_rho[v] * op) for v in (0, 1, 4, 5)), rel=1e-12)
+
+
+@pytest.mark.gpu
+def test_partition_gradients_against_finite_differences(lib_built):
+    """Gradients on 1x2 domino partitions of a 4x4 grid: the coarse plan's
+    adjoints pulled back through the partition contraction, against central
+    differences of the oracle's BP on the coarse network (h = 1e-5, 1e-6)."""
+    L = 4
+    tn, g, A = grid(L, 2, 61)
+    A = [a / np.linalg.norm(a) for a in A]
+    tn.tensors = [a.copy() for a in A]
+    parts = [[i + L * j, i + 1 + L * j] for j in range(L) for i in range(0, L, 2)]
+    pc = gbtn.partitioned_cache(tn, parts).update(maxiter=400, schedule="parallel")
+    val, G = pc.logscalar_grad(tol=1e-14)
+    sval, GS = pc.expect_sum_grad(O.SZ, tol=1e-14)
+
+    def coarse_oracle(ts):
+        t = gbtn.TensorNetwork(g.nv, g.edges, g.site_dims, g.edge_dims, ts)
+        cg = CoarseGraining(t, parts)
+        gc = as_graph(cg.coarse)
+        m, _, _ = O.bp_update(gc, cg.coarse.tensors, O.identity_messages(gc), maxiter=400, schedule="parallel")
+        return cg, gc, m
+
+    def f_log(ts):
+        cg, gc, m = coarse_oracle(ts)
+        return float(np.real(O.logscalar(gc, cg.coarse.tensors, cg.coarse.tensors, m)))
+
+    def f_sz(ts):
+        cg, gc, m = coarse_oracle(ts)
+        rdms = cg.site_rdms([O.vertex_rdm(gc, cg.coarse.tensors, cg.coarse.tensors, m, i) for i in range(gc.nv)])
+        return float(sum(np.sum(r * O.SZ) / np.trace(r) for r in rdms))
+
+    assert val == pytest.approx(f_log(A), rel=1e-10)
+    assert sval == pytest.approx(f_sz(A), rel=1e-9, abs=1e-12)
+    rng = np.random.default_rng(5)
+    D = [rng.standard_normal(a.shape) for a in A]
+    nrm = np.sqrt(sum(np.sum(d * d) for d in D))
+    D = [d / nrm for d in D]
+    h = 1e-5
+    for f, grad in ((f_log, G), (f_sz, GS)):
+        fd = (f([a + h * d for a, d in zip(A, D)]) - f([a - h * d for a, d in zip(A, D)])) / (2 * h)
+        an = sum(float(np.sum(x * d)) for x, d in zip(grad, D))
+        assert an == pytest.approx(fd, rel=1e-6, abs=1e-10)
+    pc.close()
