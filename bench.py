@@ -762,11 +762,20 @@ def run_ours(args):
              "frac": g_bytes / (g_launch_ms * 1e-3) / 1e9 / hbm_peak}
 
     # 7. the other configurations: gradient (c5), simple update (c4), uneven batch (c3)
-    grad = gradient_timing(gbtn, ctx, barrier, rank)
-    su = simple_update_timing(gbtn, ctx, barrier, rank)
+    def section(fn, *a):
+        """A secondary section; an error is reported in the line instead of
+        losing the line (every rank runs the same sections on the same code)."""
+        try:
+            return fn(*a)
+        except Exception as exc:  # noqa: BLE001
+            torch.cuda.synchronize()
+            return {"error": f"{type(exc).__name__}: {exc}"}
+
+    grad = section(gradient_timing, gbtn, ctx, barrier, rank)
+    su = section(simple_update_timing, gbtn, ctx, barrier, rank)
     batched = batched_uneven_timing(gbtn, ctx, stream, barrier)
-    qn = qn_timing(gbtn, ctx, stream, barrier)
-    large = large_bond_timing(gbtn, ctx, stream, barrier)
+    qn = section(qn_timing, gbtn, ctx, stream, barrier)
+    large = section(large_bond_timing, gbtn, ctx, stream, barrier)
 
     # roofline of the tensor-core kernel: algorithmic flops and compulsory bytes of
     # the routed vertices at their own (unpadded) shapes / its event-timed launch
