@@ -913,6 +913,23 @@ def run_su_pullback(args):
     st.close()
 
 
+def run_qn_sweeps(args):
+    """Profiling mode (--qn-sweeps PRECISION): warmup + steps parallel sweeps of
+    the 24 x 24 U(1) block-sparse network of the QN section in one arithmetic
+    (the command of the QN block kernel's ncu captures)."""
+    import gbtn
+    L = 24
+    tn = gbtn.square_lattice(L, L, chi=8)
+    links = [[(-1, 2), (0, 4), (1, 2)]] * tn.ne
+    flux = [1 if (v % L + v // L) % 2 else -1 for v in range(tn.nv)]
+    q = gbtn.random_qn_network(tn, links, [[(1, 1), (-1, 1)]] * tn.nv, flux, 11, unit_norm=True)
+    qc = gbtn.QNBeliefPropagationCache(q)
+    qc.update(maxiter=args.warmup + args.steps, schedule="parallel", precision=args.qn_sweeps)
+    print(json.dumps({"qn_sweeps": args.qn_sweeps, "sweeps": args.warmup + args.steps,
+                      "blocks": qc.n_blocks, "block_elements": qc.n_block_elems}))
+    qc.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -927,10 +944,14 @@ def main():
     ap.add_argument("--su-pullback", type=int, default=0, metavar="L",
                     help="only run one taped simple-update step and its pullback on the L x L TFIM state after "
                          "--steps steps (for profiler captures)")
+    ap.add_argument("--qn-sweeps", default=None, choices=["f64", "f32", "df32"],
+                    help="only run warmup + steps parallel sweeps of the U(1) block-sparse network (profiler captures)")
     args = ap.parse_args()
     globals()["BATCH"] = args.batch
     if args.sweeps_only:
         run_sweeps_only(args)
+    elif args.qn_sweeps:
+        run_qn_sweeps(args)
     elif args.su_pullback:
         run_su_pullback(args)
     elif args.impl == "reference":
