@@ -272,30 +272,28 @@ __device__ __forceinline__ void absorb_fibers(const T* __restrict__ in, T* __res
                                               const T* __restrict__ M, int tid, int nth) {
   if constexpr (std::is_same<T, float>::value && CHI > 1) {
     absorb_fibers_f32x2<CHI, PAD>(in, out, n, st, M, tid, nth);
-    return;
-  }
-  if constexpr (std::is_same<T, df32>::value && CHI > 1 && PACK) {
+  } else if constexpr (std::is_same<T, df32>::value && CHI > 1 && PACK) {
     absorb_fibers_df32x2<CHI, PAD>(in, out, n, st, M, tid, nth);
-    return;
-  }
-  T m[CHI][CHI];
+  } else {
+    T m[CHI][CHI];
 #pragma unroll
-  for (int b = 0; b < CHI; ++b)
+    for (int b = 0; b < CHI; ++b)
 #pragma unroll
-    for (int a = 0; a < CHI; ++a) m[b][a] = M[b + CHI * a];
-  const int nfib = n / CHI;
-  for (int f = tid; f < nfib; f += nth) {
-    const int lo = f % st;
-    const int base = lo + (f - lo) * CHI;
-    T x[CHI];
+      for (int a = 0; a < CHI; ++a) m[b][a] = M[b + CHI * a];
+    const int nfib = n / CHI;
+    for (int f = tid; f < nfib; f += nth) {
+      const int lo = f % st;
+      const int base = lo + (f - lo) * CHI;
+      T x[CHI];
 #pragma unroll
-    for (int a = 0; a < CHI; ++a) x[a] = in[spos<PAD>(base + a * st)];
+      for (int a = 0; a < CHI; ++a) x[a] = in[spos<PAD>(base + a * st)];
 #pragma unroll
-    for (int b = 0; b < CHI; ++b) {
-      T y = T(0);
+      for (int b = 0; b < CHI; ++b) {
+        T y = T(0);
 #pragma unroll
-      for (int a = 0; a < CHI; ++a) y = mac(m[b][a], x[a], y);
-      out[spos<PAD>(base + b * st)] = settle(y);
+        for (int a = 0; a < CHI; ++a) y = mac(m[b][a], x[a], y);
+        out[spos<PAD>(base + b * st)] = settle(y);
+      }
     }
   }
 }
